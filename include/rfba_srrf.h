@@ -1,0 +1,175 @@
+/*
+ * rfba_srrf.h — C-ABI of the GB300 SRRF radiality library (librfba_srrf.so).
+ *
+ * Drop-in replacement for RFBA's GradientCalc library. Three groups of entry
+ * points:
+ *
+ *  1. The reference's own exports, same names, same signatures, same meaning:
+ *       SRRFGradientCalc      RFBA Main/GradientCalc/GradientCalc.h:4, GradientCalc.cpp:169-173
+ *       SRRFGetMag            RFBA Main/GradientCalc/GradientCalc.h:5, GradientCalc.cpp:176-178
+ *       SRRFGradientCalcGPU   RFBA Main/GradientCalc/kernel.cuh:26,    kernel.cu:560-657
+ *     They read ./SRRF.ini like the reference (sections [SRRF], [Temproal],
+ *     [Radiality], [Weighting], optional [Split]), run synchronously on the
+ *     current CUDA device with host buffers, and return 0 on success. Unlike the
+ *     reference they return a negative rfba_status on failure (the reference
+ *     always returns 0) and never abort the process.
+ *
+ *  2. An extended, stream-ordered interface on an explicit configuration
+ *     (per-axis magnification, uint16 or float input, host or device pointers,
+ *     explicit block lists, forward/backward pair). It replaces the reference's
+ *     per-call cudaMalloc/cudaMemcpy driver (kernel.cu:560-657) and its serial
+ *     per-block loop (GradientCalc.cpp:144-160).
+ *
+ *  3. Helpers: INI loading, block lists following GradientCalc.cpp:47-90 and
+ *     the MATLAB doSplit.m rule, error text.
+ *
+ * Layouts (all little-endian, x fastest, as in the reference):
+ *   input   [t][z][y][x]  (W*H*D*T elements; kernel.cu:36-40)
+ *   output  [z][y][x] on the magnified grid (W*mx, H*my, D*mz), the layout of
+ *           SRRF.raw (multispot5_place_methods.cc:272-274, 314).
+ */
+#ifndef RFBA_SRRF_H
+#define RFBA_SRRF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- 1. Reference-compatible exports -------------------------------------- */
+
+/* The reference's configuration record, field for field (kernel.cuh:3-24). */
+typedef struct SRRFConf {
+    float RingRadius;   /* ring radius, magnified voxels (default 0.5) */
+    int Magnification;  /* integer magnification, all axes (default 5) */
+    int AxesinRing;     /* ring has (2*AxesinRing)^2 samples (default 6) */
+    int MainRange;
+    int XRange;
+    int YRange;
+    int ZRange;
+    int Method;         /* 0 TRM, 1 TRA, 2 TRPPM, 3 TRAC */
+    int ITC;            /* integrate temporal correlations (TRAC) */
+    int TRACOrder;      /* 2, 3 or 4 */
+    int RemoveCon;      /* 1 clamps radiality at 0 */
+    int Renormalize;
+    int GradientSmooth;
+    int IntensityW;
+    int blockSizeX;
+    int blockSizeY;
+    int blockSizeZ;
+} SRRFConf;
+
+/* GradientCalc.cpp:169. imageDim = {W, H, D, T}. inImage: W*H*D*T floats,
+ * outImage: W*H*D*mag^3 floats, both host memory owned by the caller. Splits
+ * the volume into overlapping blocks (border 2, [Split] block sizes, default
+ * 16) and pastes back each block's interior exactly like GradientCalc.cpp:
+ * 92-116; all blocks run in one persistent kernel. Voxels the reference never
+ * writes (the low border of 2*mag on each axis) are set to 0. */
+int SRRFGradientCalc(float* inImage, int* imageDim, float* outImage);
+
+/* GradientCalc.cpp:176-178: Magnification from ./SRRF.ini, default 5. */
+int SRRFGetMag(void);
+
+/* kernel.cu:560. One block (the whole input) with an explicit configuration;
+ * host buffers; full magnified output. */
+int SRRFGradientCalcGPU(float* inImage, int* imageDim, float* outImage, SRRFConf* conf);
+
+/* ---- 2. Extended interface -------------------------------------------------- */
+
+typedef enum rfba_status {
+    RFBA_OK = 0,
+    RFBA_ERR_INVALID = -1,     /* bad argument: null pointer, dims, config */
+    RFBA_ERR_UNSUPPORTED = -2, /* valid but outside what the kernels handle */
+    RFBA_ERR_NOMEM = -3,       /* device or host allocation failed */
+    RFBA_ERR_CUDA = -4,        /* CUDA runtime error (text in rfba_last_error) */
+    RFBA_ERR_TIMEOUT = -5,     /* a bounded device wait gave up */
+    RFBA_ERR_IO = -6           /* file could not be read or written */
+} rfba_status;
+
+typedef enum rfba_dtype { RFBA_F32 = 0, RFBA_U16 = 1 } rfba_dtype;
+
+/* Configuration. Field order mirrors SRRFConf with the magnification split per
+ * axis (the reference's single Magnification is mag[0]=mag[1]=mag[2]). */
+typedef struct rfba_srrf_config {
+    float ring_radius;
+    int mag[3];
+    int axes_in_ring;
+    int main_range, x_range, y_range, z_range;
+    int method, itc, trac_order;
+    int remove_con, renormalize, gradient_smooth, intensity_w;
+    int block_size[3];
+} rfba_srrf_config;
+
+/* Pointer-location flags. */
+#define RFBA_HOST_PTRS 0   /* in/out are host memory (pinned is fastest) */
+#define RFBA_DEVICE_PTRS 1 /* in/out are device memory of the context's device */
+
+/* One independent block of the input: the SRRF of the sub-volume
+ * origin..origin+size (all time points), computed as if it were a whole image
+ * (gradient clamps and interpolation windows at its own edges; kernel.cu:44-125,
+ * 146). Only the magnified sub-region [lo, hi) (block-local fine coordinates) is
+ * computed and written: element (x, y, z) of that region goes to
+ * out[out_offset + (x-lo[0])*out_stride[0] + (y-lo[1])*out_stride[1]
+ *         + (z-lo[2])*out_stride[2]]. */
+typedef struct rfba_block {
+    int32_t origin[3];
+    int32_t size[3];
+    int32_t lo[3];
+    int32_t hi[3];
+    int64_t out_offset;
+    int64_t out_stride[3];
+} rfba_block;
+
+typedef struct rfba_ctx rfba_ctx; /* device, streams, scratch, plans, autotune cache */
+
+/* Context on a CUDA device; scratch_budget_bytes caps the radiality stack (0 =
+ * a default of a quarter of free device memory). */
+int rfba_ctx_create(int device, size_t scratch_budget_bytes, rfba_ctx** out);
+int rfba_ctx_destroy(rfba_ctx* ctx);
+
+int rfba_srrf_config_default(rfba_srrf_config* cfg);        /* GradientCalc.cpp:19-41 */
+int rfba_srrf_config_load_ini(const char* path, rfba_srrf_config* cfg); /* GradientCalc.cpp:15-42 */
+int rfba_srrf_config_from_legacy(const SRRFConf* conf, rfba_srrf_config* cfg);
+
+/* Whole volume as one block: out is the full magnified grid [D*mz][H*my][W*mx].
+ * dims = {W, H, D, T}. stream is a cudaStream_t (NULL = legacy default stream);
+ * with RFBA_HOST_PTRS the call returns when out is written. */
+int rfba_srrf_forward(rfba_ctx* ctx, const rfba_srrf_config* cfg, const void* in, rfba_dtype dtype,
+                      const int dims[4], float* out, int ptr_flags, void* stream);
+
+/* Explicit block list (any sizes, any count) in one persistent launch. The
+ * output pointer and every block's out_offset/out_stride address one array
+ * of out_elems floats. */
+int rfba_srrf_forward_blocks(rfba_ctx* ctx, const rfba_srrf_config* cfg, const void* in, rfba_dtype dtype,
+                             const int dims[4], const rfba_block* blocks, int nblocks, float* out,
+                             int64_t out_elems, int ptr_flags, void* stream);
+
+/* The same block list, one launch per block with its own host<->device copies,
+ * as the reference's GradientCalc.cpp:144-160 loop does (the "plain" path).
+ * Host pointers only. */
+int rfba_srrf_forward_blocks_plain(rfba_ctx* ctx, const rfba_srrf_config* cfg, const void* in, rfba_dtype dtype,
+                                   const int dims[4], const rfba_block* blocks, int nblocks, float* out,
+                                   int64_t out_elems);
+
+/* Block lists. GradientCalc.cpp:47-116 (border 2, put-back into the full
+ * magnified output, isotropic mag = cfg->mag[0]); returns the block count, or a
+ * negative status. With blocks == NULL only counts. */
+int rfba_blocks_gradientcalc(const rfba_srrf_config* cfg, const int dims[4], rfba_block* blocks, int cap);
+/* doSplit.m (Matlab Scripts/doSplit.m:1-19) per axis with block edge max_size
+ * and border; each block writes its whole magnified output into a packed array
+ * (blocks in x-fastest order, each [z][y][x]). */
+int rfba_blocks_dosplit(const rfba_srrf_config* cfg, const int dims[4], const int max_size[3], int border,
+                        rfba_block* blocks, int cap, int64_t* out_elems);
+
+/* Text of the last error on the calling thread ("" if none). */
+const char* rfba_last_error(void);
+
+/* Library version string. */
+const char* rfba_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RFBA_SRRF_H */

@@ -1,0 +1,500 @@
+// CPU oracle for the 3D SRRF radiality path of RFBA's GradientCalc library.
+//
+// TEST INFRASTRUCTURE ONLY. This file restates the reference algorithm on the
+// host so that the CUDA path can be checked against it. Only tests/, the smoke
+// check and the CPU-baseline leg of bench.py load it; the product library never
+// links or calls it.
+//
+// Two instantiations:
+//   * double: the FP64 oracle. Every value is computed in double from the
+//     reference's float inputs (input voxels and the float ring table).
+//     The one discrete decision that cannot be taken in double without changing
+//     the reference's result is the interpolation window test ("return 0 when
+//     x/mag is outside [1.5, dim-1.5]", kernel.cu:146 and :264): it decides
+//     whether a subvoxel becomes NaN, so it is taken exactly as the reference
+//     takes it, in float ((float)X + 0.5f + ring, then / (float)mag).
+//   * float: a literal FP32 port of the reference device code, operation for
+//     operation (same association order, absolute magnified coordinates, all n^2
+//     ring samples, Catmull-Rom weights recomputed per tap). It reproduces the
+//     reference compiled as host code bit for bit (checked in the tests) and is
+//     the timed CPU baseline.
+//
+// Reference map (paths inside the RFBA project):
+//   buildRing                 RFBA Main/GradientCalc/kernel.cu:23-33
+//   gradKernel                kernel.cu:44-125
+//   cubic                     kernel.cu:128-138
+//   interpolateG              kernel.cu:141-169
+//   _calculateDk              kernel.cu:174-183
+//   calculateRadiality        kernel.cu:186-253
+//   interpolateIntensity      kernel.cu:257-287
+//   calculateAVE  (TRA)       kernel.cu:291-327
+//   calculateMIP  (TRM)       kernel.cu:332-366
+//   calculatePairwiseProductSum (TRPPM) kernel.cu:372-419
+//   calculateACRF (TRAC)      kernel.cu:423-555
+//   SRRFGradientCalcGPU       kernel.cu:560-657
+//   getSplitCount/doSplit/doPutback/doSRRFGradientCalc  GradientCalc.cpp:47-163
+//
+// Generalisation kept from the extended interface: one magnification per axis
+// (the reference has a single integer Magnification; with equal factors the
+// arithmetic is the reference's).
+//
+// Out-of-range reads of the reference are defined here as follows:
+//   * the tap u = dim read at q = dim - 1.5 (weight exactly 0) reads the
+//     clamped edge voxel instead of the next row;
+//   * the TRAC binning read past the end of an odd-length series at level 0
+//     (kernel.cu:535 with tBin + _t == T) reads 0.
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+
+extern "C" {
+typedef struct oconf {
+    float ring_radius;
+    int mag[3];
+    int axes_in_ring;
+    int main_range, x_range, y_range, z_range;
+    int method, itc, trac_order;
+    int remove_con, renormalize, gradient_smooth, intensity_w;
+    int block_size[3];
+} oconf;
+}
+
+namespace {
+
+// kernel.cu:17 and :23-33: float angle step, float sin/cos, (r*sin)*cos order.
+void build_ring(float r, int n, float* x, float* y, float* z) {
+    const float PI_F = 3.141592654f;
+    float step = (PI_F * 2.0f) / (float)n;
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+            int idx = i * n + j;
+            x[idx] = r * std::sin(step * (float)i) * std::cos(step * (float)j);
+            y[idx] = r * std::sin(step * (float)i) * std::sin(step * (float)j);
+            z[idx] = r * std::cos(step * (float)i);
+        }
+}
+
+template <class T>
+inline T cubic(T xx) {  // kernel.cu:128-138
+    const T a = T(0.5);
+    T x = xx;
+    if (x < T(0)) x = -x;
+    T z = T(0);
+    if (x < T(1))
+        z = x * x * (x * (-a + T(2)) + (a - T(3))) + T(1);
+    else if (x < T(2))
+        z = -a * x * x * x + T(5) * a * x * x - T(8) * a * x + T(4) * a;
+    return z;
+}
+
+// The reference's window test, always in float (kernel.cu:143-147, :260-265).
+inline bool window_ok(float x0f, int mag, int dim) {
+    float q = x0f / (float)mag;
+    return !(q < 1.5f || q > (float)dim - 1.5f);
+}
+
+inline int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// A block of the input (all time points) and a coarse sub-box of it on which
+// the gradient is evaluated. Arrays are [t][z][y][x] over the sub-box.
+template <class T>
+struct Field {
+    int dim[3];      // block dims (coarse)
+    int c0[3], c1[3];  // sub-box [c0, c1)
+    int n[3];
+    int nt;
+    std::vector<T> g[3];
+    std::vector<T> img;  // input on the sub-box (for intensity interpolation)
+    size_t idx(int x, int y, int z, int t) const {
+        return (((size_t)t * n[2] + (z - c0[2])) * n[1] + (y - c0[1])) * n[0] + (x - c0[0]);
+    }
+};
+
+// gradKernel (kernel.cu:44-125) on the sub-box, reading the block input with
+// clamp-to-edge of the block.
+template <class T>
+void gradient(const float* in, const int dims[4], const oconf& c, Field<T>& F) {
+    const int w = dims[0], h = dims[1], d = dims[2];
+    auto I = [&](int x, int y, int z, int t) -> T {
+        return (T)in[(((size_t)t * d + z) * h + y) * w + x];
+    };
+    const size_t tot = (size_t)F.n[0] * F.n[1] * F.n[2] * F.nt;
+    for (int k = 0; k < 3; ++k) F.g[k].assign(tot, T(0));
+    F.img.assign(tot, T(0));
+    const int mR = c.main_range, xR = c.x_range, yR = c.y_range, zR = c.z_range;
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int t = 0; t < F.nt; ++t)
+        for (int z = F.c0[2]; z < F.c1[2]; ++z)
+            for (int y = F.c0[1]; y < F.c1[1]; ++y)
+                for (int x = F.c0[0]; x < F.c1[0]; ++x) {
+                    size_t o = F.idx(x, y, z, t);
+                    F.img[o] = I(x, y, z, t);
+                    if (c.gradient_smooth == 0) {
+                        int x0 = std::max(x - 1, 0), x1 = std::min(x + 1, w - 1);
+                        int y0 = std::max(y - 1, 0), y1 = std::min(y + 1, h - 1);
+                        int z0 = std::max(z - 1, 0), z1 = std::min(z + 1, d - 1);
+                        F.g[0][o] = -I(x0, y, z, t) + I(x1, y, z, t);
+                        F.g[1][o] = -I(x, y0, z, t) + I(x, y1, z, t);
+                        F.g[2][o] = -I(x, y, z0, t) + I(x, y, z1, t);
+                        continue;
+                    }
+                    T v = 0;
+                    for (int i = -mR; i <= mR; ++i)
+                        for (int j = -yR; j <= yR; ++j)
+                            for (int k = -zR; k <= zR; ++k) {
+                                T p = I(clampi(x + i, 0, w - 1), clampi(y + j, 0, h - 1), clampi(z + k, 0, d - 1), t);
+                                if (i < 0) v -= p;
+                                else if (i > 0) v += p;
+                            }
+                    F.g[0][o] = v;
+                    v = 0;
+                    for (int j = -mR; j <= mR; ++j)
+                        for (int i = -xR; i <= xR; ++i)
+                            for (int k = -zR; k <= zR; ++k) {
+                                T p = I(clampi(x + i, 0, w - 1), clampi(y + j, 0, h - 1), clampi(z + k, 0, d - 1), t);
+                                if (j < 0) v -= p;
+                                else if (j > 0) v += p;
+                            }
+                    F.g[1][o] = v;
+                    v = 0;
+                    for (int k = -mR; k <= mR; ++k)
+                        for (int i = -xR; i <= xR; ++i)
+                            for (int j = -yR; j <= yR; ++j) {
+                                T p = I(clampi(x + i, 0, w - 1), clampi(y + j, 0, h - 1), clampi(z + k, 0, d - 1), t);
+                                if (k < 0) v -= p;
+                                else if (k > 0) v += p;
+                            }
+                    F.g[2][o] = v;
+                }
+}
+
+// interpolateG / interpolateIntensity body (kernel.cu:149-168, :266-285) for a
+// position already divided by the magnification. Tap indices are clamped to the
+// block (see the header note on the u = dim tap).
+template <class T>
+T interp(const Field<T>& F, const std::vector<T>& A, T x, T y, T z, int t) {
+    int u0 = (int)std::floor(x - T(0.5));
+    int v0 = (int)std::floor(y - T(0.5));
+    int w0 = (int)std::floor(z - T(0.5));
+    T s = T(0);
+    for (int k = 0; k <= 3; ++k) {
+        int w = w0 - 1 + k;
+        T q = T(0);
+        for (int j = 0; j <= 3; ++j) {
+            int v = v0 - 1 + j;
+            T p = T(0);
+            for (int i = 0; i <= 3; ++i) {
+                int u = u0 - 1 + i;
+                int uc = clampi(u, F.c0[0], F.c1[0] - 1);
+                int vc = clampi(v, F.c0[1], F.c1[1] - 1);
+                int wc = clampi(w, F.c0[2], F.c1[2] - 1);
+                p = p + A[F.idx(uc, vc, wc, t)] * cubic<T>(x - (T(u) + T(0.5)));
+            }
+            q = q + p * cubic<T>(y - (T(v) + T(0.5)));
+        }
+        s = s + q * cubic<T>(z - (T(w) + T(0.5)));
+    }
+    return s;
+}
+
+struct Ring {
+    int n = 0;  // points per angle (2 * AxesinRing)
+    std::vector<float> x, y, z;
+};
+
+// calculateRadiality (kernel.cu:186-253) for one subvoxel and one time point.
+template <class T>
+T radiality(const Field<T>& F, const Ring& R, const oconf& c, int X, int Y, int Z, int t) {
+    const int mx = c.mag[0], my = c.mag[1], mz = c.mag[2];
+    const T r = (T)c.ring_radius;
+    const T Xc = T(X) + T(0.5), Yc = T(Y) + T(0.5), Zc = T(Z) + T(0.5);
+    const float Xcf = (float)X + 0.5f, Ycf = (float)Y + 0.5f, Zcf = (float)Z + 0.5f;
+    T S = T(0);
+    const int n = R.n;
+    for (int i1 = 0; i1 < n; ++i1)
+        for (int i2 = 0; i2 < n; ++i2) {
+            const int id = i1 * n + i2;
+            const T rx = (T)R.x[id], ry = (T)R.y[id], rz = (T)R.z[id];
+            const T x0 = Xc + rx, y0 = Yc + ry, z0 = Zc + rz;
+            T Gx = 0, Gy = 0, Gz = 0;
+            const bool ok = window_ok(Xcf + R.x[id], mx, F.dim[0]) && window_ok(Ycf + R.y[id], my, F.dim[1]) &&
+                            window_ok(Zcf + R.z[id], mz, F.dim[2]);
+            if (ok) {
+                const T qx = x0 / T(mx), qy = y0 / T(my), qz = z0 / T(mz);
+                Gx = interp(F, F.g[0], qx, qy, qz, t);
+                Gy = interp(F, F.g[1], qx, qy, qz, t);
+                Gz = interp(F, F.g[2], qx, qy, qz, t);
+            }
+            const T GMag = std::sqrt(Gx * Gx + Gy * Gy + Gz * Gz);
+            const T GdotR = (Gx * rx + Gy * ry + Gz * rz) / (GMag * r);
+            const bool div = (GdotR > 0) || (GdotR != GdotR);
+            // _calculateDk (kernel.cu:174-183)
+            const T tt = (Gx * (x0 - Xc) + Gy * (y0 - Yc) + Gz * (z0 - Zc)) / (GMag * GMag);
+            const T xc = Gx * tt + Xc, yc = Gy * tt + Yc, zc = Gz * tt + Zc;
+            const T dk = std::sqrt((x0 - xc) * (x0 - xc) + (y0 - yc) * (y0 - yc) + (z0 - zc) * (z0 - zc));
+            T D = T(1) - dk / r;
+            D = D * D;
+            if (div) S -= D;
+            else S += D;
+        }
+    S = S / T(n);
+    if (c.renormalize == 1) S = T(0.5) + (S / T(2));
+    if (c.remove_con == 1) S = std::fmax(S, T(0));
+    return S;
+}
+
+// interpolateIntensity (kernel.cu:257-287) at the subvoxel centre.
+template <class T>
+T intensity(const Field<T>& F, const oconf& c, int X, int Y, int Z, int t) {
+    const float xf = (float)X + 0.5f, yf = (float)Y + 0.5f, zf = (float)Z + 0.5f;
+    if (!(window_ok(xf, c.mag[0], F.dim[0]) && window_ok(yf, c.mag[1], F.dim[1]) && window_ok(zf, c.mag[2], F.dim[2])))
+        return T(0);
+    const T qx = (T(X) + T(0.5)) / T(c.mag[0]);
+    const T qy = (T(Y) + T(0.5)) / T(c.mag[1]);
+    const T qz = (T(Z) + T(0.5)) / T(c.mag[2]);
+    T s = interp(F, F.img, qx, qy, qz, t);
+    return std::fmax(s, T(0));
+}
+
+// Temporal reductions for one subvoxel. rad has room for nt + 4 entries; the
+// entries past nt are 0 (TRAC binning may read one of them).
+template <class T>
+T temporal(const oconf& c, T* rad, const T* inten, int nt) {
+    const int IWf = c.intensity_w;
+    if (c.method == 1) {  // calculateAVE, kernel.cu:291-327
+        T mean = 0;
+        if (IWf == 1)
+            for (int t = 0; t < nt; ++t) mean += rad[t] * inten[t];
+        else
+            for (int t = 0; t < nt; ++t) mean += rad[t];
+        return mean / T(nt);
+    }
+    if (c.method == 0) {  // calculateMIP, kernel.cu:332-366
+        T mip = 0;
+        for (int t = 0; t < nt; ++t) mip = std::fmax(IWf == 1 ? rad[t] * inten[t] : rad[t], mip);
+        return mip;
+    }
+    if (c.method == 2) {  // calculatePairwiseProductSum, kernel.cu:372-419
+        T pps = 0;
+        long long counter = 0;
+        for (int t0 = 0; t0 < nt; ++t0) {
+            T r0 = std::fmax(rad[t0], T(0));
+            if (r0 > 0) {
+                for (int t1 = t0; t1 < nt; ++t1) {
+                    T r1 = std::fmax(rad[t1], T(0));
+                    pps += r0 * r1;
+                    counter++;
+                }
+            } else
+                counter += nt - t0;
+        }
+        pps /= std::fmax((T)counter, T(1));
+        if (IWf == 1) {
+            T iw = 0;
+            for (int t = 0; t < nt; ++t) iw += inten[t] / T(nt);
+            pps *= iw;
+        }
+        return pps;
+    }
+    // calculateACRF, kernel.cu:423-555
+    const int order = c.trac_order;
+    T mean = 0, IW = 0;
+    for (int t = 0; t < nt; ++t) {
+        IW += rad[t] * inten[t];
+        mean += rad[t];
+    }
+    mean = mean / T(nt);
+    IW = IW / T(nt);
+    T out = 0;
+    T ABCD = 0, ABC = 0, AB = 0, CD = 0, AC = 0, BD = 0, AD = 0, BC = 0;
+    if (c.itc != 1) {
+        for (int t = 0; t < nt - order; ++t) {
+            AB += (rad[t] - mean) * (rad[t + 1] - mean);
+            if (order == 3) ABC += (rad[t] - mean) * (rad[t + 1] - mean) * (rad[t + 2] - mean);
+            if (order == 4) {
+                T A = rad[t] - mean, B = rad[t + 1] - mean, C = rad[t + 2] - mean, D = rad[t + 3] - mean;
+                ABCD += A * B * C * D;
+                CD += C * D;
+                AC += A * C;
+                BD += B * D;
+                AD += A * D;
+                BC += B * C;
+            }
+        }
+        if (order == 3) out = std::fabs(ABC) / T(nt);
+        else if (order == 4) out = std::fabs(ABCD - AB * CD - AC * BD - AD * BC) / T(nt);
+        else out = std::fabs(AB) / T(nt);
+    } else {
+        int nB = nt;
+        while (nB > order) {
+            AB = 0;
+            for (int t = 0; t < nB - order; ++t) {
+                int tBin = t * order;
+                AB += (rad[t] - mean) * (rad[t + 1] - mean);
+                if (order == 3) ABC += (rad[t] - mean) * (rad[t + 1] - mean) * (rad[t + 2] - mean);
+                if (order == 4) {
+                    T A = rad[t] - mean, B = rad[t + 1] - mean, C = rad[t + 2] - mean, D = rad[t + 3] - mean;
+                    ABCD += A * B * C * D;
+                    CD += C * D;
+                    AC += A * C;
+                    BD += B * D;
+                    AD += A * D;
+                    BC += B * C;
+                }
+                rad[t] = 0;
+                if (tBin < nB)
+                    for (int j = 0; j < order; ++j) rad[t] += rad[tBin + j] / T(order);
+            }
+            if (order == 3) out += std::fabs(ABC) / T(nB);
+            else if (order == 4) out += std::fabs(ABCD - AB * CD - AC * BD - AD * BC) / T(nB);
+            else out += std::fabs(AB) / T(nB);
+            nB = nB / order;
+        }
+    }
+    if (IWf == 1) out = IW * out;
+    return out;
+}
+
+// One independent block: input dims[4] = {w,h,d,T} with layout [t][z][y][x];
+// computes the magnified map on the fine region [lo, hi) (block-local fine
+// coordinates), out is [z][y][x] over that region. Optional stacks receive the
+// per-time radiality and interpolated intensity, [t][z][y][x] over the region.
+template <class T>
+void srrf_region(const float* in, const int dims[4], const oconf& c, const int lo[3], const int hi[3], T* out,
+                 T* rad_stack, T* int_stack) {
+    Ring R;
+    R.n = 2 * c.axes_in_ring;
+    R.x.resize(R.n * R.n);
+    R.y.resize(R.n * R.n);
+    R.z.resize(R.n * R.n);
+    build_ring(c.ring_radius, R.n, R.x.data(), R.y.data(), R.z.data());
+    float rmax[3] = {0, 0, 0};
+    for (int i = 0; i < R.n * R.n; ++i) {
+        rmax[0] = std::max(rmax[0], std::fabs(R.x[i]));
+        rmax[1] = std::max(rmax[1], std::fabs(R.y[i]));
+        rmax[2] = std::max(rmax[2], std::fabs(R.z[i]));
+    }
+    Field<T> F;
+    F.nt = dims[3];
+    for (int a = 0; a < 3; ++a) {
+        F.dim[a] = dims[a];
+        const double m = c.mag[a];
+        int a0 = (int)std::floor((lo[a] + 0.5 - rmax[a]) / m - 0.5) - 2;
+        int a1 = (int)std::floor((hi[a] - 1 + 0.5 + rmax[a]) / m - 0.5) + 3;
+        F.c0[a] = std::max(a0, 0);
+        F.c1[a] = std::min(a1 + 1, dims[a]);
+        if (F.c1[a] <= F.c0[a]) F.c1[a] = F.c0[a] + 1;
+        F.n[a] = F.c1[a] - F.c0[a];
+    }
+    gradient<T>(in, dims, c, F);
+    const int nx = hi[0] - lo[0], ny = hi[1] - lo[1], nz = hi[2] - lo[2];
+    const int nt = dims[3];
+    const size_t nvox = (size_t)nx * ny * nz;
+#pragma omp parallel
+    {
+        std::vector<T> rad(nt + 8), inten(nt + 8);
+#pragma omp for schedule(dynamic, 4)
+        for (long long v = 0; v < (long long)nvox; ++v) {
+            const int X = lo[0] + (int)(v % nx);
+            const int Y = lo[1] + (int)((v / nx) % ny);
+            const int Z = lo[2] + (int)(v / ((size_t)nx * ny));
+            std::fill(rad.begin(), rad.end(), T(0));
+            for (int t = 0; t < nt; ++t) {
+                rad[t] = radiality<T>(F, R, c, X, Y, Z, t);
+                inten[t] = intensity<T>(F, c, X, Y, Z, t);
+                if (rad_stack) rad_stack[(size_t)t * nvox + v] = rad[t];
+                if (int_stack) int_stack[(size_t)t * nvox + v] = inten[t];
+            }
+            out[v] = temporal<T>(c, rad.data(), inten.data(), nt);
+        }
+    }
+}
+
+// GradientCalc.cpp:47-163 with border 2 and the INI block sizes. Regions that
+// the reference never writes (the global low border) are left untouched here;
+// callers pre-fill the output.
+template <class T>
+void legacy(const float* in, const int dims[4], const oconf& c, T* out) {
+    const int border = 2;
+    const int mag = c.mag[0];
+    int maxDim[3] = {c.block_size[0], c.block_size[1], c.block_size[2]};
+    int splitN[3];
+    for (int i = 0; i < 3; ++i) {
+        splitN[i] = (dims[i] - 2 * border) / (maxDim[i] - 2 * border);
+        if ((dims[i] - 2 * border) % (maxDim[i] - 2 * border) != 0) splitN[i] += 1;
+    }
+    const int W = dims[0] * mag, H = dims[1] * mag;
+    for (int k = 0; k < splitN[2]; ++k)
+        for (int j = 0; j < splitN[1]; ++j)
+            for (int i = 0; i < splitN[0]; ++i) {
+                int pos[3] = {i, j, k}, res[4], start[3];
+                for (int a = 0; a < 3; ++a) {
+                    res[a] = (pos[a] == splitN[a] - 1) ? dims[a] - (splitN[a] - 1) * (maxDim[a] - 2 * border) : maxDim[a];
+                    start[a] = pos[a] == 0 ? 0 : pos[a] * (maxDim[a] - 2 * border);
+                }
+                res[3] = dims[3];
+                std::vector<float> blk((size_t)res[0] * res[1] * res[2] * res[3]);
+                for (int t = 0; t < res[3]; ++t)
+                    for (int z = 0; z < res[2]; ++z)
+                        for (int y = 0; y < res[1]; ++y)
+                            for (int x = 0; x < res[0]; ++x)
+                                blk[(((size_t)t * res[2] + z) * res[1] + y) * res[0] + x] =
+                                    in[(((size_t)t * dims[2] + z + start[2]) * dims[1] + y + start[1]) * dims[0] + x + start[0]];
+                const int bm = border * mag;
+                int lo[3] = {bm, bm, bm}, hi[3] = {res[0] * mag, res[1] * mag, res[2] * mag};
+                if (hi[0] <= lo[0] || hi[1] <= lo[1] || hi[2] <= lo[2]) continue;
+                std::vector<T> o((size_t)(hi[0] - lo[0]) * (hi[1] - lo[1]) * (hi[2] - lo[2]));
+                oconf cb = c;
+                cb.mag[1] = cb.mag[2] = mag;
+                srrf_region<T>(blk.data(), res, cb, lo, hi, o.data(), nullptr, nullptr);
+                const int nx = hi[0] - lo[0], ny = hi[1] - lo[1];
+                for (int z = lo[2]; z < hi[2]; ++z)
+                    for (int y = lo[1]; y < hi[1]; ++y)
+                        for (int x = lo[0]; x < hi[0]; ++x)
+                            out[((size_t)(z + start[2] * mag) * H + y + start[1] * mag) * W + x + start[0] * mag] =
+                                o[((size_t)(z - lo[2]) * ny + (y - lo[1])) * nx + (x - lo[0])];
+            }
+}
+
+}  // namespace
+
+extern "C" {
+
+int oracle_ring_f32(float r, int axes, float* x, float* y, float* z) {
+    build_ring(r, 2 * axes, x, y, z);
+    return 0;
+}
+
+int oracle_srrf_region_f64(const float* in, const int* dims, const oconf* c, const int* lo, const int* hi, double* out,
+                           double* rad_stack, double* int_stack) {
+    srrf_region<double>(in, dims, *c, lo, hi, out, rad_stack, int_stack);
+    return 0;
+}
+
+int oracle_srrf_region_f32(const float* in, const int* dims, const oconf* c, const int* lo, const int* hi, float* out,
+                           float* rad_stack, float* int_stack) {
+    srrf_region<float>(in, dims, *c, lo, hi, out, rad_stack, int_stack);
+    return 0;
+}
+
+int oracle_legacy_f64(const float* in, const int* dims, const oconf* c, double* out) {
+    legacy<double>(in, dims, *c, out);
+    return 0;
+}
+
+int oracle_legacy_f32(const float* in, const int* dims, const oconf* c, float* out) {
+    legacy<float>(in, dims, *c, out);
+    return 0;
+}
+
+// Temporal reduction alone on a given series (tests of the reduction quirks).
+int oracle_temporal_f64(const oconf* c, const double* rad, const double* inten, int nt, double* out) {
+    std::vector<double> r(nt + 8, 0.0);
+    std::memcpy(r.data(), rad, sizeof(double) * nt);
+    *out = temporal<double>(*c, r.data(), inten, nt);
+    return 0;
+}
+}

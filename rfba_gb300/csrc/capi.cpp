@@ -1,0 +1,722 @@
+// C-ABI of librfba_srrf.so: the reference's GradientCalc exports
+// (GradientCalc.cpp:169-178, kernel.cu:560) and the extended interface
+// declared in include/rfba_srrf.h.
+//
+// The reference allocates and frees every buffer on every call and runs one
+// block after another (kernel.cu:575-654, GradientCalc.cpp:144-160). Here a
+// context owns the device buffers (grown on demand and kept), the ring plan and
+// weight tables (cached per configuration), and launches every block of a call
+// in one persistent radiality kernel followed by one temporal kernel per pass.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "srrf_internal.h"
+
+namespace rfba {
+
+void config_default(rfba_srrf_config* c);
+bool config_load_ini(const char* path, rfba_srrf_config* c);
+bool config_validate(const rfba_srrf_config& c, std::string* err);
+int ring_zero_pair(const RingPlan& rp);
+int blocks_gradientcalc(const rfba_srrf_config& c, const int dims[4], rfba_block* out, int cap, std::string* err);
+int blocks_dosplit(const rfba_srrf_config& c, const int dims[4], const int max_size[3], int border, rfba_block* out,
+                   int cap, long long* out_elems, std::string* err);
+
+static thread_local std::string g_last_error;
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+static bool verbose() {
+    static int v = -1;
+    if (v < 0) {
+        const char* e = std::getenv("RFBA_VERBOSE");
+        v = (e && *e && *e != '0') ? 1 : 0;
+    }
+    return v == 1;
+}
+
+static int cuda_fail(cudaError_t e, const char* what) {
+    set_error(std::string(what) + ": " + cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? RFBA_ERR_NOMEM : RFBA_ERR_CUDA;
+}
+
+#define RFBA_CUDA(call, what)                          \
+    do {                                               \
+        cudaError_t e__ = (call);                      \
+        if (e__ != cudaSuccess) return cuda_fail(e__, what); \
+    } while (0)
+
+// Device buffer that grows and is kept.
+struct DevBuf {
+    void* p = nullptr;
+    size_t n = 0;
+    int ensure(size_t bytes, const char* what) {
+        if (bytes <= n) return RFBA_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        size_t want = std::max(bytes, (size_t)256);
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return cuda_fail(e, what);
+        }
+        n = want;
+        return RFBA_OK;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+struct PlanCache {
+    bool valid = false;
+    float ring_radius = 0.f;
+    int axes = 0, mag[3] = {0, 0, 0};
+    RingPlan ring;
+    std::vector<float> words;
+    TableLayout tl;
+    int zero_pair = -1;
+};
+
+}  // namespace rfba
+
+struct rfba_ctx {
+    int device = 0;
+    int sm_count = 0;
+    size_t budget = 0;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;
+    rfba::DevBuf in, out, rad, inten, blocks, tiles, tables, counter, prefix;
+    rfba::PlanCache plan;
+    bool timing = false;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    double last_rad_ms = 0.0, last_temporal_ms = 0.0;
+    long long launches = 0;
+    long long last_flop_units = 0;  // subvoxel-time-points computed by the last call
+    int grid_override = 0;          // CTAs for the radiality kernel (0 = occupancy x SMs)
+    int chunk_override = 0;         // time points per work item (0 = automatic)
+};
+
+namespace rfba {
+
+static int ctx_init(rfba_ctx* c, int device, size_t budget) {
+    c->device = device;
+    RFBA_CUDA(cudaSetDevice(device), "cudaSetDevice");
+    RFBA_CUDA(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device), "SM count");
+    RFBA_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
+    for (auto& e : c->ev) RFBA_CUDA(cudaEventCreate(&e), "event");
+    if (budget == 0) {
+        size_t fr = 0, tot = 0;
+        RFBA_CUDA(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+        budget = fr / 4;
+    }
+    c->budget = budget;
+    return RFBA_OK;
+}
+
+static rfba_ctx* g_default = nullptr;
+static std::mutex g_default_mu;
+
+static int default_ctx(rfba_ctx** out) {
+    std::lock_guard<std::mutex> lk(g_default_mu);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (g_default && g_default->device != dev) {
+        // the reference always used the current device; follow it
+        g_default = nullptr;
+    }
+    if (!g_default) {
+        rfba_ctx* c = new rfba_ctx();
+        int st = ctx_init(c, dev, 0);
+        if (st != RFBA_OK) {
+            delete c;
+            return st;
+        }
+        g_default = c;
+    }
+    *out = g_default;
+    return RFBA_OK;
+}
+
+static int ensure_plan(rfba_ctx* ctx, const rfba_srrf_config& cfg) {
+    PlanCache& P = ctx->plan;
+    if (P.valid && P.ring_radius == cfg.ring_radius && P.axes == cfg.axes_in_ring && P.mag[0] == cfg.mag[0] &&
+        P.mag[1] == cfg.mag[1] && P.mag[2] == cfg.mag[2])
+        return RFBA_OK;
+    std::string err;
+    P.valid = false;
+    if (!build_ring_plan(cfg, &P.ring, &err) || !build_tables(cfg, P.ring, &P.words, &P.tl, &err)) {
+        set_error(err);
+        return RFBA_ERR_UNSUPPORTED;
+    }
+    P.zero_pair = ring_zero_pair(P.ring);
+    if (P.zero_pair < 0) {
+        set_error("ring has no (0, 0) pair");
+        return RFBA_ERR_UNSUPPORTED;
+    }
+    int st = ctx->tables.ensure(P.words.size() * 4, "tables");
+    if (st) return st;
+    RFBA_CUDA(cudaMemcpy(ctx->tables.p, P.words.data(), P.words.size() * 4, cudaMemcpyHostToDevice), "tables upload");
+    P.ring_radius = cfg.ring_radius;
+    P.axes = cfg.axes_in_ring;
+    for (int a = 0; a < 3; ++a) P.mag[a] = cfg.mag[a];
+    P.valid = true;
+    return RFBA_OK;
+}
+
+static int fz_for(int mz) { return mz * cz_for_mag(mz); }
+
+// Turn caller blocks into device block descriptors, splitting regions along z
+// so that one pass's radiality + intensity stack fits the scratch budget.
+static int make_blocks(rfba_ctx* ctx, const rfba_srrf_config& cfg, const int dims[4], const rfba_block* blocks,
+                       int nblocks, std::vector<BlockDev>* outb) {
+    const RingPlan& rp = ctx->plan.ring;
+    const int T = dims[3];
+    const int FZ = fz_for(cfg.mag[2]);
+    outb->clear();
+    const size_t per_vox = (size_t)T * 2 * sizeof(float);
+    const long long max_vox = std::max<long long>((long long)(ctx->budget / per_vox), 1);
+    for (int i = 0; i < nblocks; ++i) {
+        const rfba_block& b = blocks[i];
+        BlockDev d;
+        std::memset(&d, 0, sizeof d);
+        for (int a = 0; a < 3; ++a) {
+            if (b.size[a] < 1 || b.origin[a] < 0 || (long long)b.origin[a] + b.size[a] > dims[a]) {
+                set_error("block outside the input volume");
+                return RFBA_ERR_INVALID;
+            }
+            if (b.lo[a] < 0 || b.hi[a] > b.size[a] * cfg.mag[a]) {
+                set_error("block region outside the block's magnified grid");
+                return RFBA_ERR_INVALID;
+            }
+            d.origin[a] = b.origin[a];
+            d.size[a] = b.size[a];
+            d.lo[a] = b.lo[a];
+            d.hi[a] = b.hi[a];
+            const std::vector<float>& rc = a == 0 ? rp.rx : (a == 1 ? rp.ry : rp.rz);
+            window_range(cfg.ring_radius, rc, cfg.mag[a], b.size[a], &d.rad_lo[a], &d.rad_hi[a]);
+            fine_window_int(cfg.mag[a], b.size[a], &d.int_lo[a], &d.int_hi[a]);
+        }
+        if (b.hi[0] <= b.lo[0] || b.hi[1] <= b.lo[1] || b.hi[2] <= b.lo[2]) continue;
+        d.out_offset = b.out_offset;
+        for (int a = 0; a < 3; ++a) d.out_stride[a] = b.out_stride[a];
+        // z slabs under the budget
+        const long long plane = (long long)(b.hi[0] - b.lo[0]) * (b.hi[1] - b.lo[1]);
+        long long slab = std::max<long long>(max_vox / plane, 1);
+        if (slab < b.hi[2] - b.lo[2]) slab = std::max<long long>((slab / FZ) * FZ, FZ);
+        for (int z0 = b.lo[2]; z0 < b.hi[2]; z0 += (int)slab) {
+            BlockDev s = d;
+            s.lo[2] = z0;
+            s.hi[2] = (int)std::min<long long>(b.hi[2], z0 + slab);
+            s.out_offset = d.out_offset + (long long)(z0 - b.lo[2]) * d.out_stride[2];
+            for (int a = 0; a < 3; ++a) s.nreg[a] = s.hi[a] - s.lo[a];
+            s.zbase = (s.lo[2] / cfg.mag[2]) * cfg.mag[2];
+            s.ntile[0] = (s.nreg[0] + kTileX - 1) / kTileX;
+            s.ntile[1] = (s.nreg[1] + kTileY - 1) / kTileY;
+            s.ntile[2] = (s.hi[2] - s.zbase + FZ - 1) / FZ;
+            s.vox = (long long)s.nreg[0] * s.nreg[1] * s.nreg[2];
+            outb->push_back(s);
+        }
+    }
+    return RFBA_OK;
+}
+
+static size_t elem_size(rfba_dtype dt) { return dt == RFBA_U16 ? 2 : 4; }
+
+// Run the device pipeline for all blocks. in_dev / out_dev are device pointers.
+static int run_device(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void* in_dev, rfba_dtype dtype,
+                      const int dims[4], const std::vector<BlockDev>& all, float* out_dev, cudaStream_t st) {
+    const int T = dims[3];
+    const PlanCache& P = ctx->plan;
+    // passes under the stack budget
+    const size_t per_vox = (size_t)T * sizeof(float);
+    size_t i0 = 0;
+    ctx->last_rad_ms = ctx->last_temporal_ms = 0.0;
+    ctx->last_flop_units = 0;
+    while (i0 < all.size()) {
+        size_t i1 = i0;
+        long long vox = 0;
+        while (i1 < all.size()) {
+            const long long nv = vox + all[i1].vox;
+            if (i1 > i0 && (size_t)nv * per_vox * 2 > ctx->budget) break;
+            vox = nv;
+            ++i1;
+        }
+        std::vector<BlockDev> pass(all.begin() + i0, all.begin() + i1);
+        std::vector<long long> prefix(pass.size() + 1, 0);
+        std::vector<TileDesc> tiles;
+        long long off = 0;
+        for (size_t b = 0; b < pass.size(); ++b) {
+            pass[b].stack_off = off;
+            off += pass[b].vox * T;
+            prefix[b + 1] = prefix[b] + pass[b].vox;
+        }
+        // tiles: largest blocks first for balance, raster order inside a block
+        std::vector<int> order(pass.size());
+        for (size_t b = 0; b < pass.size(); ++b) order[b] = (int)b;
+        std::stable_sort(order.begin(), order.end(), [&](int u, int v) {
+            return (long long)pass[u].ntile[0] * pass[u].ntile[1] * pass[u].ntile[2] >
+                   (long long)pass[v].ntile[0] * pass[v].ntile[1] * pass[v].ntile[2];
+        });
+        for (int b : order)
+            for (int tz = 0; tz < pass[b].ntile[2]; ++tz)
+                for (int ty = 0; ty < pass[b].ntile[1]; ++ty)
+                    for (int tx = 0; tx < pass[b].ntile[0]; ++tx) tiles.push_back({b, tx, ty, tz});
+        int stc;
+        if ((stc = ctx->rad.ensure((size_t)off * 4, "radiality stack"))) return stc;
+        if ((stc = ctx->inten.ensure((size_t)off * 4, "intensity stack"))) return stc;
+        if ((stc = ctx->blocks.ensure(pass.size() * sizeof(BlockDev), "blocks"))) return stc;
+        if ((stc = ctx->tiles.ensure(tiles.size() * sizeof(TileDesc), "tiles"))) return stc;
+        if ((stc = ctx->prefix.ensure(prefix.size() * sizeof(long long), "prefix"))) return stc;
+        if ((stc = ctx->counter.ensure(256, "counter"))) return stc;
+        RFBA_CUDA(cudaMemcpyAsync(ctx->blocks.p, pass.data(), pass.size() * sizeof(BlockDev), cudaMemcpyHostToDevice, st),
+                  "blocks upload");
+        RFBA_CUDA(cudaMemcpyAsync(ctx->tiles.p, tiles.data(), tiles.size() * sizeof(TileDesc), cudaMemcpyHostToDevice, st),
+                  "tiles upload");
+        RFBA_CUDA(cudaMemcpyAsync(ctx->prefix.p, prefix.data(), prefix.size() * sizeof(long long),
+                                  cudaMemcpyHostToDevice, st),
+                  "prefix upload");
+        RFBA_CUDA(cudaMemsetAsync(ctx->counter.p, 0, 256, st), "counter reset");
+
+        RadParams rp;
+        std::memset(&rp, 0, sizeof rp);
+        rp.in = in_dev;
+        rp.W = dims[0];
+        rp.H = dims[1];
+        rp.D = dims[2];
+        rp.T = T;
+        for (int a = 0; a < 3; ++a) rp.mag[a] = cfg.mag[a];
+        rp.nxv = (int)P.ring.xv.size();
+        rp.nyv = (int)P.ring.yv.size();
+        rp.nzv = (int)P.ring.zv.size();
+        rp.ngroups = (int)P.ring.grp_xval.size();
+        rp.npairs = (int)P.ring.pair_yval.size();
+        rp.npoints = (int)P.ring.pt_zval.size();
+        rp.zero_pair = P.zero_pair;
+        if (cfg.gradient_smooth == 0) {
+            rp.gr[0] = 1;
+            rp.gr[1] = rp.gr[2] = rp.gr[3] = 0;
+        } else {
+            rp.gr[0] = cfg.main_range;
+            rp.gr[1] = cfg.x_range;
+            rp.gr[2] = cfg.y_range;
+            rp.gr[3] = cfg.z_range;
+        }
+        rp.R = std::max(std::max(rp.gr[0], rp.gr[1]), std::max(rp.gr[2], rp.gr[3]));
+        const int CZ = cz_for_mag(cfg.mag[2]);
+        rp.NU = (kTileX - 1) / cfg.mag[0] + 2 + 4;
+        rp.NV = (kTileY - 1) / cfg.mag[1] + 2 + 4;
+        rp.NW = CZ + 4;
+        rp.NIX = rp.NU + 2 * rp.R;
+        rp.NIY = rp.NV + 2 * rp.R;
+        rp.NIZ = rp.NW + 2 * rp.R;
+        rp.renorm = cfg.renormalize == 1;
+        rp.poscon = cfg.remove_con == 1;
+        rp.tables = static_cast<const float*>(ctx->tables.p);
+        rp.tl = P.tl;
+        rp.smem_table_words = P.tl.words;
+        rp.blocks = static_cast<const BlockDev*>(ctx->blocks.p);
+        rp.tiles = static_cast<const TileDesc*>(ctx->tiles.p);
+        rp.ntiles = (int)tiles.size();
+        rp.rad_stack = static_cast<float*>(ctx->rad.p);
+        rp.int_stack = static_cast<float*>(ctx->inten.p);
+        rp.work_counter = static_cast<unsigned int*>(ctx->counter.p);
+        const size_t smem = radiality_smem_bytes(rp);
+        if (smem > 227 * 1024) {
+            set_error("shared memory tile too large for this configuration");
+            return RFBA_ERR_UNSUPPORTED;
+        }
+        int per_sm = 0;
+        int ce = radiality_max_ctas_per_sm(rp, dtype == RFBA_U16, &per_sm);
+        if (ce != 0) return cuda_fail((cudaError_t)ce, "occupancy");
+        if (per_sm < 1) {
+            set_error("radiality kernel does not fit on an SM");
+            return RFBA_ERR_UNSUPPORTED;
+        }
+        const int slots = per_sm * ctx->sm_count;
+        // time chunk: enough work items for ~8 per CTA slot
+        int chunk = ctx->chunk_override;
+        if (chunk <= 0) {
+            const long long want = 8LL * slots;
+            long long nch = (want + rp.ntiles - 1) / rp.ntiles;
+            nch = std::max<long long>(1, std::min<long long>(nch, T));
+            chunk = (int)((T + nch - 1) / nch);
+        }
+        rp.t_chunk = chunk;
+        rp.nchunks = (T + chunk - 1) / chunk;
+        rp.nitems = (long long)rp.ntiles * rp.nchunks;
+        int grid = ctx->grid_override > 0 ? ctx->grid_override : slots;
+        grid = (int)std::min<long long>(grid, rp.nitems);
+        if (grid < 1) grid = 1;
+
+        TemporalParams tp;
+        std::memset(&tp, 0, sizeof tp);
+        tp.blocks = rp.blocks;
+        tp.vox_prefix = static_cast<const long long*>(ctx->prefix.p);
+        tp.nblocks = (int)pass.size();
+        tp.total_vox = prefix.back();
+        tp.T = T;
+        tp.method = cfg.method;
+        tp.itc = cfg.itc;
+        tp.order = cfg.trac_order;
+        tp.iw = cfg.intensity_w;
+        tp.rad_stack = rp.rad_stack;
+        tp.int_stack = rp.int_stack;
+        tp.out = out_dev;
+
+        if (ctx->timing) RFBA_CUDA(cudaEventRecord(ctx->ev[0], st), "event");
+        int le = launch_radiality(rp, grid, smem, dtype == RFBA_U16, st);
+        if (le != 0) return cuda_fail((cudaError_t)le, "radiality launch");
+        if (ctx->timing) RFBA_CUDA(cudaEventRecord(ctx->ev[1], st), "event");
+        le = launch_temporal(tp, st);
+        if (le != 0) return cuda_fail((cudaError_t)le, "temporal launch");
+        if (ctx->timing) RFBA_CUDA(cudaEventRecord(ctx->ev[2], st), "event");
+        ctx->launches += 2;
+        ctx->last_flop_units += (long long)tp.total_vox * T;
+        if (verbose())
+            std::fprintf(stderr, "rfba: pass blocks=%zu tiles=%d chunk=%d items=%lld grid=%d smem=%zu\n", pass.size(),
+                         rp.ntiles, chunk, rp.nitems, grid, smem);
+        if (ctx->timing) {
+            RFBA_CUDA(cudaEventSynchronize(ctx->ev[2]), "event sync");
+            float a = 0, b = 0;
+            cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]);
+            cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]);
+            ctx->last_rad_ms += a;
+            ctx->last_temporal_ms += b;
+        }
+        i0 = i1;
+    }
+    return RFBA_OK;
+}
+
+static int validate_common(const rfba_srrf_config* cfg, const void* in, const int* dims, const void* out) {
+    if (!cfg || !in || !dims || !out) {
+        set_error("null argument");
+        return RFBA_ERR_INVALID;
+    }
+    std::string err;
+    if (!config_validate(*cfg, &err)) {
+        set_error(err);
+        return RFBA_ERR_INVALID;
+    }
+    for (int a = 0; a < 4; ++a)
+        if (dims[a] < 1) {
+            set_error("dims must be positive");
+            return RFBA_ERR_INVALID;
+        }
+    const long long plane = (long long)dims[0] * dims[1] * dims[2];
+    if (plane * dims[3] > (1LL << 40)) {
+        set_error("input too large");
+        return RFBA_ERR_INVALID;
+    }
+    return RFBA_OK;
+}
+
+static int forward_blocks_impl(rfba_ctx* ctx, const rfba_srrf_config* cfg, const void* in, rfba_dtype dtype,
+                               const int dims[4], const rfba_block* blocks, int nblocks, float* out, long long out_elems,
+                               int flags, cudaStream_t st, bool zero_out) {
+    int s = validate_common(cfg, in, dims, out);
+    if (s) return s;
+    if (nblocks < 0 || (nblocks > 0 && !blocks) || out_elems < 0) {
+        set_error("bad block list");
+        return RFBA_ERR_INVALID;
+    }
+    if (dtype != RFBA_F32 && dtype != RFBA_U16) {
+        set_error("dtype must be RFBA_F32 or RFBA_U16");
+        return RFBA_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if ((s = ensure_plan(ctx, *cfg))) return s;
+    std::vector<BlockDev> all;
+    if ((s = make_blocks(ctx, *cfg, dims, blocks, nblocks, &all))) return s;
+    for (const BlockDev& b : all) {
+        const long long last = b.out_offset + (long long)(b.nreg[0] - 1) * b.out_stride[0] +
+                               (long long)(b.nreg[1] - 1) * b.out_stride[1] + (long long)(b.nreg[2] - 1) * b.out_stride[2];
+        if (b.out_offset < 0 || last >= out_elems || b.out_stride[0] < 0 || b.out_stride[1] < 0 || b.out_stride[2] < 0) {
+            set_error("block output outside the output array");
+            return RFBA_ERR_INVALID;
+        }
+    }
+    const size_t in_bytes = (size_t)dims[0] * dims[1] * dims[2] * dims[3] * elem_size(dtype);
+    const void* in_dev = in;
+    float* out_dev = out;
+    if (flags == RFBA_HOST_PTRS) {
+        if ((s = ctx->in.ensure(in_bytes, "input"))) return s;
+        if ((s = ctx->out.ensure((size_t)out_elems * 4, "output"))) return s;
+        RFBA_CUDA(cudaMemcpyAsync(ctx->in.p, in, in_bytes, cudaMemcpyHostToDevice, st), "input copy");
+        in_dev = ctx->in.p;
+        out_dev = static_cast<float*>(ctx->out.p);
+        RFBA_CUDA(cudaMemsetAsync(out_dev, 0, (size_t)out_elems * 4, st), "output clear");
+    } else if (zero_out) {
+        RFBA_CUDA(cudaMemsetAsync(out_dev, 0, (size_t)out_elems * 4, st), "output clear");
+    }
+    if ((s = run_device(ctx, *cfg, in_dev, dtype, dims, all, out_dev, st))) return s;
+    if (flags == RFBA_HOST_PTRS) {
+        RFBA_CUDA(cudaMemcpyAsync(out, out_dev, (size_t)out_elems * 4, cudaMemcpyDeviceToHost, st), "output copy");
+        RFBA_CUDA(cudaStreamSynchronize(st), "synchronize");
+    }
+    return RFBA_OK;
+}
+
+}  // namespace rfba
+
+using namespace rfba;
+
+extern "C" {
+
+const char* rfba_last_error(void) { return g_last_error.c_str(); }
+const char* rfba_version(void) { return "rfba_srrf 0.1 (sm_103a)"; }
+
+int rfba_ctx_create(int device, size_t budget, rfba_ctx** out) {
+    if (!out) {
+        set_error("null argument");
+        return RFBA_ERR_INVALID;
+    }
+    rfba_ctx* c = new rfba_ctx();
+    int s = ctx_init(c, device, budget);
+    if (s) {
+        delete c;
+        return s;
+    }
+    *out = c;
+    return RFBA_OK;
+}
+
+int rfba_ctx_destroy(rfba_ctx* c) {
+    if (!c) return RFBA_OK;
+    {
+        std::lock_guard<std::mutex> lk(g_default_mu);
+        if (c == g_default) g_default = nullptr;
+    }
+    cudaSetDevice(c->device);
+    for (DevBuf* b : {&c->in, &c->out, &c->rad, &c->inten, &c->blocks, &c->tiles, &c->tables, &c->counter, &c->prefix})
+        b->release();
+    for (auto& e : c->ev)
+        if (e) cudaEventDestroy(e);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return RFBA_OK;
+}
+
+// Measurement hooks used by bench.py: CUDA-event times of the last call's
+// kernels (on the stream they were launched on) and the kernel launch count.
+int rfba_ctx_set_timing(rfba_ctx* c, int enable) {
+    if (!c) return RFBA_ERR_INVALID;
+    c->timing = enable != 0;
+    return RFBA_OK;
+}
+int rfba_ctx_last_timing(rfba_ctx* c, double* rad_ms, double* temporal_ms, long long* launches) {
+    if (!c) return RFBA_ERR_INVALID;
+    if (rad_ms) *rad_ms = c->last_rad_ms;
+    if (temporal_ms) *temporal_ms = c->last_temporal_ms;
+    if (launches) *launches = c->launches;
+    return RFBA_OK;
+}
+int rfba_ctx_set_launch(rfba_ctx* c, int grid, int t_chunk) {
+    if (!c) return RFBA_ERR_INVALID;
+    c->grid_override = grid;
+    c->chunk_override = t_chunk;
+    return RFBA_OK;
+}
+
+int rfba_srrf_config_default(rfba_srrf_config* cfg) {
+    if (!cfg) return RFBA_ERR_INVALID;
+    config_default(cfg);
+    return RFBA_OK;
+}
+
+int rfba_srrf_config_load_ini(const char* path, rfba_srrf_config* cfg) {
+    if (!cfg || !path) return RFBA_ERR_INVALID;
+    config_load_ini(path, cfg);  // a missing file gives the defaults, as GetPrivateProfile* does
+    return RFBA_OK;
+}
+
+int rfba_srrf_config_from_legacy(const SRRFConf* c, rfba_srrf_config* cfg) {
+    if (!c || !cfg) return RFBA_ERR_INVALID;
+    cfg->ring_radius = c->RingRadius;
+    cfg->mag[0] = cfg->mag[1] = cfg->mag[2] = c->Magnification;
+    cfg->axes_in_ring = c->AxesinRing;
+    cfg->main_range = c->MainRange;
+    cfg->x_range = c->XRange;
+    cfg->y_range = c->YRange;
+    cfg->z_range = c->ZRange;
+    cfg->method = c->Method;
+    cfg->itc = c->ITC;
+    cfg->trac_order = c->TRACOrder;
+    cfg->remove_con = c->RemoveCon;
+    cfg->renormalize = c->Renormalize;
+    cfg->gradient_smooth = c->GradientSmooth;
+    cfg->intensity_w = c->IntensityW;
+    cfg->block_size[0] = c->blockSizeX;
+    cfg->block_size[1] = c->blockSizeY;
+    cfg->block_size[2] = c->blockSizeZ;
+    return RFBA_OK;
+}
+
+int rfba_blocks_gradientcalc(const rfba_srrf_config* cfg, const int dims[4], rfba_block* blocks, int cap) {
+    if (!cfg || !dims) return RFBA_ERR_INVALID;
+    std::string err;
+    int n = blocks_gradientcalc(*cfg, dims, blocks, blocks ? cap : 0, &err);
+    if (n < 0) set_error(err);
+    return n;
+}
+
+int rfba_blocks_dosplit(const rfba_srrf_config* cfg, const int dims[4], const int max_size[3], int border,
+                        rfba_block* blocks, int cap, int64_t* out_elems) {
+    if (!cfg || !dims || !max_size) return RFBA_ERR_INVALID;
+    std::string err;
+    long long oe = 0;
+    int n = blocks_dosplit(*cfg, dims, max_size, border, blocks, blocks ? cap : 0, &oe, &err);
+    if (n < 0) set_error(err);
+    if (out_elems) *out_elems = oe;
+    return n;
+}
+
+int rfba_srrf_forward_blocks(rfba_ctx* ctx, const rfba_srrf_config* cfg, const void* in, rfba_dtype dtype,
+                             const int dims[4], const rfba_block* blocks, int nblocks, float* out, int64_t out_elems,
+                             int ptr_flags, void* stream) {
+    if (!ctx) {
+        set_error("null context");
+        return RFBA_ERR_INVALID;
+    }
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    return forward_blocks_impl(ctx, cfg, in, dtype, dims, blocks, nblocks, out, out_elems, ptr_flags, st, false);
+}
+
+int rfba_srrf_forward(rfba_ctx* ctx, const rfba_srrf_config* cfg, const void* in, rfba_dtype dtype, const int dims[4],
+                      float* out, int ptr_flags, void* stream) {
+    if (!ctx || !cfg || !dims) {
+        set_error("null argument");
+        return RFBA_ERR_INVALID;
+    }
+    rfba_block b;
+    std::memset(&b, 0, sizeof b);
+    for (int a = 0; a < 3; ++a) {
+        b.size[a] = dims[a];
+        b.hi[a] = dims[a] * cfg->mag[a];
+    }
+    b.out_stride[0] = 1;
+    b.out_stride[1] = b.hi[0];
+    b.out_stride[2] = (int64_t)b.hi[0] * b.hi[1];
+    const int64_t n = (int64_t)b.hi[0] * b.hi[1] * b.hi[2];
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    return forward_blocks_impl(ctx, cfg, in, dtype, dims, &b, 1, out, n, ptr_flags, st, false);
+}
+
+int rfba_srrf_forward_blocks_plain(rfba_ctx* ctx, const rfba_srrf_config* cfg, const void* in, rfba_dtype dtype,
+                                   const int dims[4], const rfba_block* blocks, int nblocks, float* out,
+                                   int64_t out_elems) {
+    // One block at a time: copy the block's input sub-volume to the device,
+    // launch, copy its output region back (GradientCalc.cpp:144-160 with
+    // kernel.cu:560-657 per block).
+    if (!ctx || !cfg || !in || !dims || !out || (nblocks > 0 && !blocks)) {
+        set_error("null argument");
+        return RFBA_ERR_INVALID;
+    }
+    const size_t es = elem_size(dtype);
+    for (int i = 0; i < nblocks; ++i) {
+        const rfba_block& b = blocks[i];
+        for (int a = 0; a < 3; ++a)
+            if (b.size[a] < 1 || b.origin[a] < 0 || b.origin[a] + b.size[a] > dims[a]) {
+                set_error("block outside the input volume");
+                return RFBA_ERR_INVALID;
+            }
+        const int bd[4] = {b.size[0], b.size[1], b.size[2], dims[3]};
+        std::vector<unsigned char> sub((size_t)bd[0] * bd[1] * bd[2] * bd[3] * es);
+        const unsigned char* src = static_cast<const unsigned char*>(in);
+        for (int t = 0; t < bd[3]; ++t)
+            for (int z = 0; z < bd[2]; ++z)
+                for (int y = 0; y < bd[1]; ++y) {
+                    const size_t so = ((((size_t)t * dims[2] + b.origin[2] + z) * dims[1] + b.origin[1] + y) * dims[0] +
+                                       b.origin[0]) * es;
+                    const size_t dof = ((((size_t)t * bd[2] + z) * bd[1] + y) * bd[0]) * es;
+                    std::memcpy(sub.data() + dof, src + so, (size_t)bd[0] * es);
+                }
+        rfba_block lb = b;
+        lb.origin[0] = lb.origin[1] = lb.origin[2] = 0;
+        const int nx = b.hi[0] - b.lo[0], ny = b.hi[1] - b.lo[1], nz = b.hi[2] - b.lo[2];
+        if (nx <= 0 || ny <= 0 || nz <= 0) continue;
+        lb.out_offset = 0;
+        lb.out_stride[0] = 1;
+        lb.out_stride[1] = nx;
+        lb.out_stride[2] = (int64_t)nx * ny;
+        std::vector<float> o((size_t)nx * ny * nz);
+        int s = forward_blocks_impl(ctx, cfg, sub.data(), dtype, bd, &lb, 1, o.data(), (int64_t)o.size(),
+                                    RFBA_HOST_PTRS, ctx->stream, false);
+        if (s) return s;
+        for (int z = 0; z < nz; ++z)
+            for (int y = 0; y < ny; ++y)
+                for (int x = 0; x < nx; ++x) {
+                    const int64_t oi = b.out_offset + x * b.out_stride[0] + y * b.out_stride[1] + z * b.out_stride[2];
+                    if (oi < 0 || oi >= out_elems) {
+                        set_error("block output outside the output array");
+                        return RFBA_ERR_INVALID;
+                    }
+                    out[oi] = o[((size_t)z * ny + y) * nx + x];
+                }
+    }
+    return RFBA_OK;
+}
+
+// ---- reference-compatible exports ------------------------------------------
+
+int SRRFGetMag(void) {
+    rfba_srrf_config c;
+    config_load_ini("SRRF.ini", &c);
+    return c.mag[0];
+}
+
+int SRRFGradientCalcGPU(float* inImage, int* imageDim, float* outImage, SRRFConf* conf) {
+    if (!inImage || !imageDim || !outImage || !conf) {
+        set_error("null argument");
+        return RFBA_ERR_INVALID;
+    }
+    rfba_ctx* ctx = nullptr;
+    int s = default_ctx(&ctx);
+    if (s) return s;
+    rfba_srrf_config cfg;
+    rfba_srrf_config_from_legacy(conf, &cfg);
+    return rfba_srrf_forward(ctx, &cfg, inImage, RFBA_F32, imageDim, outImage, RFBA_HOST_PTRS, nullptr);
+}
+
+int SRRFGradientCalc(float* inImage, int* imageDim, float* outImage) {
+    if (!inImage || !imageDim || !outImage) {
+        set_error("null argument");
+        return RFBA_ERR_INVALID;
+    }
+    rfba_srrf_config cfg;
+    config_load_ini("SRRF.ini", &cfg);  // GradientCalc.cpp:17, re-read on every call
+    if (verbose()) std::fprintf(stderr, "rfba: SRRF Method: %d\n", cfg.method);
+    rfba_ctx* ctx = nullptr;
+    int s = default_ctx(&ctx);
+    if (s) return s;
+    std::string err;
+    int n = blocks_gradientcalc(cfg, imageDim, nullptr, 0, &err);
+    if (n < 0) {
+        set_error(err);
+        return n;
+    }
+    std::vector<rfba_block> bl(std::max(n, 1));
+    blocks_gradientcalc(cfg, imageDim, bl.data(), n, &err);
+    const int64_t out_elems = (int64_t)imageDim[0] * imageDim[1] * imageDim[2] * cfg.mag[0] * cfg.mag[0] * cfg.mag[0];
+    return forward_blocks_impl(ctx, &cfg, inImage, RFBA_F32, imageDim, bl.data(), n, outImage, out_elems,
+                               RFBA_HOST_PTRS, ctx->stream, true);
+}
+
+// Targets of the C++-linkage aliases in compat_cxx.cpp.
+int rfba_compat_gradientcalc(float* in, int* dims, float* out) { return SRRFGradientCalc(in, dims, out); }
+int rfba_compat_getmag(void) { return SRRFGetMag(); }
+
+}  // extern "C"

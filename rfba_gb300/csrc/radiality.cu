@@ -1,0 +1,365 @@
+// Fused gradient + Catmull-Rom magnification + radiality kernel (sm_103a).
+//
+// Replaces the reference's gradKernel (kernel.cu:44-125) and calculateRadiality
+// (kernel.cu:186-253, with interpolateG kernel.cu:141-169, _calculateDk
+// kernel.cu:174-183 and interpolateIntensity kernel.cu:257-287) by one
+// persistent kernel. Per work item (block, 16x16xFZ subvoxel tile, time chunk)
+// and time point:
+//
+//   1. the input tile plus halo is read (block-edge clamped, as the
+//      reference's fminf/fmaxf clamps do) into shared memory;
+//   2. the smoothed gradient G = (Gx, Gy, Gz) and the intensity I of every
+//      coarse cell the tile's taps reach is formed in shared memory (float4);
+//   3. the ring's n^2 samples are reduced to their distinct points (62 for
+//      n = 12) and factorised per axis. Catmull-Rom interpolation is separable,
+//      and a sample's x taps and weights depend only on the subvoxel's x phase
+//      (X mod mag_x) and the ring point's x coordinate, so for each distinct ring
+//      x value the x-filtered field U is formed once in shared memory;
+//   4. each thread owns one (X, Y) subvoxel column; for each distinct (x, y)
+//      ring pair it y-filters U into a register column T[w] over coarse z, and
+//      for each ring point of that pair it z-filters T (5 taps, static register
+//      indices) for its FZ subvoxels and accumulates the radiality term;
+//   5. radiality and interpolated intensity per subvoxel and time point are
+//      written to the stack that the temporal kernel reduces.
+//
+// The radiality term of a sample with interpolated gradient g and ring offset
+// rho (kernel.cu:224-240) is evaluated in the equivalent, rounding-robust form
+//   s = |g x rho| / (|g| r)   (= Dk / r),   D = (1 - s)^2,
+//   S -= D if g.rho > 0, S += D otherwise,
+// with g = 0 giving NaN exactly as the reference's 0/0 does. Coordinates are
+// local (phase + ring offset), so no precision is lost at large volume
+// coordinates. The sample window test (kernel.cu:146) makes the whole subvoxel
+// NaN; it is evaluated on the host per axis with the reference's float
+// arithmetic and applied here as a per-block valid box.
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "srrf_internal.h"
+
+namespace rfba {
+namespace {
+
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+template <typename Tin>
+__device__ __forceinline__ float load_in(const Tin* p, long long i);
+template <>
+__device__ __forceinline__ float load_in<float>(const float* p, long long i) {
+    return __ldg(p + i);
+}
+template <>
+__device__ __forceinline__ float load_in<uint16_t>(const uint16_t* p, long long i) {
+    return (float)__ldg(p + i);
+}
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+__device__ __forceinline__ int floordiv(int a, int b) {  // b > 0
+    int q = a / b;
+    return (a % b != 0 && a < 0) ? q - 1 : q;
+}
+
+template <int MZ, int CZ, typename Tin>
+__global__ void __launch_bounds__(kThreads, 2) radiality_kernel(const RadParams p) {
+    constexpr int FZ = MZ * CZ;
+    constexpr int NW = CZ + 4;
+    extern __shared__ float4 smem4[];
+
+    // Shared layout: [G tile float4][U tile float4][input tile][tables]
+    const int NU = p.NU, NV = p.NV;
+    float4* gt = smem4;                           // [NW][NV][NU]
+    float4* ut = gt + NU * NV * NW;               // [NW][NV][16]
+    float* inp = reinterpret_cast<float*>(ut + kTileX * NV * NW);  // [NIZ][NIY][NIX]
+    float* tab = inp + ((p.NIX * p.NIY * p.NIZ + 3) & ~3);         // 16-byte aligned (float4 reads)
+    __shared__ unsigned int s_item;
+
+    const int tid = threadIdx.x;
+    const int xf = tid & (kTileX - 1);
+    const int yf = tid / kTileX;
+    const int mx = p.mag[0], my = p.mag[1];
+
+    for (int i = tid; i < p.smem_table_words; i += kThreads) tab[i] = p.tables[i];
+    const float* wx = tab + p.tl.wx;
+    const int* offx = reinterpret_cast<const int*>(tab + p.tl.offx);
+    const float* wy = tab + p.tl.wy;
+    const int* offy = reinterpret_cast<const int*>(tab + p.tl.offy);
+    const float* wz = tab + p.tl.wz;
+    const float* wzi = tab + p.tl.wzi;
+    const int* grp_xval = reinterpret_cast<const int*>(tab + p.tl.grp_xval);
+    const int* grp = reinterpret_cast<const int*>(tab + p.tl.grp);
+    const int* pair_yval = reinterpret_cast<const int*>(tab + p.tl.pair_yval);
+    const int* pair_pt = reinterpret_cast<const int*>(tab + p.tl.pair_pt);
+    const int* pt_zval = reinterpret_cast<const int*>(tab + p.tl.pt_zval);
+    const float4* pt_vec = reinterpret_cast<const float4*>(tab + p.tl.pt_vec);
+
+    const Tin* in = static_cast<const Tin*>(p.in);
+    const int NIX = p.NIX, NIY = p.NIY, NIZ = p.NIZ, R = p.R;
+    const int nin = NIX * NIY * NIZ;
+    const int ncell = NU * NV * NW;
+    const int nut = kTileX * NV * NW;
+
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) s_item = atomicAdd(p.work_counter, 1u);
+        __syncthreads();
+        const long long item = s_item;
+        if (item >= p.nitems) break;
+        const int tile_i = (int)(item % p.ntiles);
+        const int chunk = (int)(item / p.ntiles);
+        const TileDesc td = p.tiles[tile_i];
+        const BlockDev& B = p.blocks[td.block];
+        const int bw = B.size[0], bh = B.size[1], bd = B.size[2];
+
+        // Tile geometry (block-local fine and coarse coordinates).
+        const int X0 = B.lo[0] + td.tx * kTileX;
+        const int Y0 = B.lo[1] + td.ty * kTileY;
+        const int Z0 = B.zbase + td.tz * FZ;
+        const int cx0 = floordiv(X0, mx) - 2;
+        const int cy0 = floordiv(Y0, my) - 2;
+        const int cz0 = Z0 / MZ - 2;
+        const int X = X0 + xf, Y = Y0 + yf;
+        const int xi = floordiv(X, mx), xr = X - xi * mx;
+        const int yi = floordiv(Y, my), yr = Y - yi * my;
+        const bool col_in = (X < B.hi[0]) && (Y < B.hi[1]);
+        const bool colx_ok = X >= B.rad_lo[0] && X <= B.rad_hi[0] && Y >= B.rad_lo[1] && Y <= B.rad_hi[1];
+        const bool coli_ok = X >= B.int_lo[0] && X <= B.int_hi[0] && Y >= B.int_lo[1] && Y <= B.int_hi[1];
+
+        const int t0 = chunk * p.t_chunk;
+        const int t1 = min(p.T, t0 + p.t_chunk);
+        for (int t = t0; t < t1; ++t) {
+            // 1. input tile with block-edge clamp
+            const long long tbase = (long long)t * p.D * p.H * p.W;
+            for (int i = tid; i < nin; i += kThreads) {
+                const int ix = i % NIX;
+                const int iy = (i / NIX) % NIY;
+                const int iz = i / (NIX * NIY);
+                const int bx = clampi(cx0 - R + ix, 0, bw - 1);
+                const int by = clampi(cy0 - R + iy, 0, bh - 1);
+                const int bz = clampi(cz0 - R + iz, 0, bd - 1);
+                const long long g = tbase + ((long long)(B.origin[2] + bz) * p.H + (B.origin[1] + by)) * p.W +
+                                    (B.origin[0] + bx);
+                inp[i] = load_in<Tin>(in, g);
+            }
+            __syncthreads();
+            // 2. gradient + intensity per coarse cell
+            for (int c = tid; c < ncell; c += kThreads) {
+                const int u = c % NU;
+                const int v = (c / NU) % NV;
+                const int w = c / (NU * NV);
+                const int cu = cx0 + u, cv = cy0 + v, cw = cz0 + w;
+                float4 g4 = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (cu >= 0 && cu < bw && cv >= 0 && cv < bh && cw >= 0 && cw < bd) {
+                    const int ux = u + R, vy = v + R, wz_ = w + R;
+                    auto I = [&](int dx, int dy, int dz) {
+                        return inp[((wz_ + dz) * NIY + (vy + dy)) * NIX + (ux + dx)];
+                    };
+                    const int mR = p.gr[0], xR = p.gr[1], yR = p.gr[2], zR = p.gr[3];
+                    float gx = 0.f, gy = 0.f, gz = 0.f;
+                    for (int i = 1; i <= mR; ++i)
+                        for (int j = -yR; j <= yR; ++j)
+                            for (int k = -zR; k <= zR; ++k) gx += I(i, j, k) - I(-i, j, k);
+                    for (int j = 1; j <= mR; ++j)
+                        for (int i = -xR; i <= xR; ++i)
+                            for (int k = -zR; k <= zR; ++k) gy += I(i, j, k) - I(i, -j, k);
+                    for (int k = 1; k <= mR; ++k)
+                        for (int i = -xR; i <= xR; ++i)
+                            for (int j = -yR; j <= yR; ++j) gz += I(i, j, k) - I(i, j, -k);
+                    g4 = make_float4(gx, gy, gz, I(0, 0, 0));
+                }
+                gt[c] = g4;
+            }
+
+            float S[FZ];
+            float Iv[FZ];
+#pragma unroll
+            for (int z = 0; z < FZ; ++z) {
+                S[z] = 0.f;
+                Iv[z] = 0.f;
+            }
+
+            for (int gi = 0; gi < p.ngroups; ++gi) {
+                __syncthreads();  // gt ready / previous U consumed
+                // 3. x-filter for ring x value a
+                const int a = grp_xval[gi];
+                {
+                    const int o = offx[a * mx + xr];
+                    const float4 wv = *reinterpret_cast<const float4*>(wx + (a * mx + xr) * 4);
+                    const int ub = xi - cx0 - 2 + o;
+                    for (int e = tid; e < nut; e += kThreads) {
+                        const int vw = e / kTileX;  // (w * NV + v)
+                        const float4* src = gt + vw * NU + ub;
+                        const float4 g0 = src[0], g1 = src[1], g2 = src[2], g3 = src[3];
+                        float4 r;
+                        r.x = fmaf(wv.w, g3.x, fmaf(wv.z, g2.x, fmaf(wv.y, g1.x, wv.x * g0.x)));
+                        r.y = fmaf(wv.w, g3.y, fmaf(wv.z, g2.y, fmaf(wv.y, g1.y, wv.x * g0.y)));
+                        r.z = fmaf(wv.w, g3.z, fmaf(wv.z, g2.z, fmaf(wv.y, g1.z, wv.x * g0.z)));
+                        r.w = fmaf(wv.w, g3.w, fmaf(wv.z, g2.w, fmaf(wv.y, g1.w, wv.x * g0.w)));
+                        ut[e] = r;
+                    }
+                }
+                __syncthreads();
+                // 4. pairs of this x value
+                for (int pi = grp[gi]; pi < grp[gi + 1]; ++pi) {
+                    const int b = pair_yval[pi];
+                    const int o = offy[b * my + yr];
+                    const float4 wv = *reinterpret_cast<const float4*>(wy + (b * my + yr) * 4);
+                    const int vb = yi - cy0 - 2 + o;
+                    const bool with_int = (pi == p.zero_pair);
+                    float Tx[NW], Ty[NW], Tz[NW], Tw[NW];
+#pragma unroll
+                    for (int w = 0; w < NW; ++w) {
+                        const float4* src = ut + (w * NV + vb) * kTileX + xf;
+                        const float4 u0 = src[0], u1 = src[kTileX], u2 = src[2 * kTileX], u3 = src[3 * kTileX];
+                        Tx[w] = fmaf(wv.w, u3.x, fmaf(wv.z, u2.x, fmaf(wv.y, u1.x, wv.x * u0.x)));
+                        Ty[w] = fmaf(wv.w, u3.y, fmaf(wv.z, u2.y, fmaf(wv.y, u1.y, wv.x * u0.y)));
+                        Tz[w] = fmaf(wv.w, u3.z, fmaf(wv.z, u2.z, fmaf(wv.y, u1.z, wv.x * u0.z)));
+                        Tw[w] = fmaf(wv.w, u3.w, fmaf(wv.z, u2.w, fmaf(wv.y, u1.w, wv.x * u0.w)));
+                    }
+                    if (with_int) {
+#pragma unroll
+                        for (int z = 0; z < FZ; ++z) {
+                            const int zr = z % MZ, zi = z / MZ;
+                            const float* q = wzi + zr * 5;
+                            float acc = q[0] * Tw[zi];
+#pragma unroll
+                            for (int m = 1; m < 5; ++m) acc = fmaf(q[m], Tw[zi + m], acc);
+                            Iv[z] = acc;
+                        }
+                    }
+                    for (int qi = pair_pt[pi]; qi < pair_pt[pi + 1]; ++qi) {
+                        const float4 pv = pt_vec[qi];
+                        const float* wzc = wz + pt_zval[qi] * (MZ * 5);
+                        float wzr[MZ][5];
+#pragma unroll
+                        for (int zr = 0; zr < MZ; ++zr)
+#pragma unroll
+                            for (int m = 0; m < 5; ++m) wzr[zr][m] = wzc[zr * 5 + m];
+#pragma unroll
+                        for (int z = 0; z < FZ; ++z) {
+                            const int zr = z % MZ, zi = z / MZ;
+                            float gx = wzr[zr][0] * Tx[zi];
+                            float gy = wzr[zr][0] * Ty[zi];
+                            float gz = wzr[zr][0] * Tz[zi];
+#pragma unroll
+                            for (int m = 1; m < 5; ++m) {
+                                gx = fmaf(wzr[zr][m], Tx[zi + m], gx);
+                                gy = fmaf(wzr[zr][m], Ty[zi + m], gy);
+                                gz = fmaf(wzr[zr][m], Tz[zi + m], gz);
+                            }
+                            const float dot = fmaf(gz, pv.z, fmaf(gy, pv.y, gx * pv.x));
+                            const float crx = fmaf(gy, pv.z, -gz * pv.y);
+                            const float cry = fmaf(gz, pv.x, -gx * pv.z);
+                            const float crz = fmaf(gx, pv.y, -gy * pv.x);
+                            const float c2 = fmaf(crz, crz, fmaf(cry, cry, crx * crx));
+                            const float g2 = fmaf(gz, gz, fmaf(gy, gy, gx * gx));
+                            const float s = sqrt_approx(c2 * rcp_approx(g2));
+                            const float om = 1.0f - s;
+                            const float D = om * om;
+                            S[z] = fmaf(D, dot > 0.f ? -pv.w : pv.w, S[z]);
+                        }
+                    }
+                }
+            }
+
+            // 5. finalize and store
+            if (col_in) {
+                const long long V = B.vox;
+                const long long sbase = B.stack_off + (long long)t * V;
+#pragma unroll
+                for (int z = 0; z < FZ; ++z) {
+                    const int Z = Z0 + z;
+                    if (Z < B.lo[2] || Z >= B.hi[2]) continue;
+                    float r = S[z];
+                    const bool zok = Z >= B.rad_lo[2] && Z <= B.rad_hi[2];
+                    if (!(colx_ok && zok)) r = __int_as_float(0x7fc00000);
+                    if (p.renorm) r = 0.5f + r * 0.5f;
+                    if (p.poscon) r = fmaxf(r, 0.f);
+                    const bool ziok = Z >= B.int_lo[2] && Z <= B.int_hi[2];
+                    const float iv = (coli_ok && ziok) ? fmaxf(Iv[z], 0.f) : 0.f;
+                    const long long v = ((long long)(Z - B.lo[2]) * B.nreg[1] + (Y - B.lo[1])) * B.nreg[0] + (X - B.lo[0]);
+                    p.rad_stack[sbase + v] = r;
+                    p.int_stack[sbase + v] = iv;
+                }
+            }
+        }
+    }
+}
+
+template <int MZ, typename Tin>
+int launch_mz(const RadParams& p, int grid, size_t smem, cudaStream_t st) {
+    constexpr int CZ = cz_for_mag(MZ);
+    auto k = radiality_kernel<MZ, CZ, Tin>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return (int)e;
+    k<<<grid, kThreads, smem, st>>>(p);
+    return (int)cudaGetLastError();
+}
+
+template <int MZ, typename Tin>
+int occ_mz(size_t smem, int* out) {
+    constexpr int CZ = cz_for_mag(MZ);
+    auto k = radiality_kernel<MZ, CZ, Tin>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return (int)e;
+    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k, kThreads, smem);
+}
+
+template <typename Tin>
+int dispatch(const RadParams& p, int grid, size_t smem, cudaStream_t st) {
+    switch (p.mag[2]) {
+        case 1: return launch_mz<1, Tin>(p, grid, smem, st);
+        case 2: return launch_mz<2, Tin>(p, grid, smem, st);
+        case 3: return launch_mz<3, Tin>(p, grid, smem, st);
+        case 4: return launch_mz<4, Tin>(p, grid, smem, st);
+        case 5: return launch_mz<5, Tin>(p, grid, smem, st);
+        case 6: return launch_mz<6, Tin>(p, grid, smem, st);
+        case 7: return launch_mz<7, Tin>(p, grid, smem, st);
+        case 8: return launch_mz<8, Tin>(p, grid, smem, st);
+    }
+    return (int)cudaErrorInvalidValue;
+}
+
+template <typename Tin>
+int occ_dispatch(int mz, size_t smem, int* out) {
+    switch (mz) {
+        case 1: return occ_mz<1, Tin>(smem, out);
+        case 2: return occ_mz<2, Tin>(smem, out);
+        case 3: return occ_mz<3, Tin>(smem, out);
+        case 4: return occ_mz<4, Tin>(smem, out);
+        case 5: return occ_mz<5, Tin>(smem, out);
+        case 6: return occ_mz<6, Tin>(smem, out);
+        case 7: return occ_mz<7, Tin>(smem, out);
+        case 8: return occ_mz<8, Tin>(smem, out);
+    }
+    return (int)cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+size_t radiality_smem_bytes(const RadParams& p) {
+    const int NW = cz_for_mag(p.mag[2]) + 4;
+    size_t b = sizeof(float4) * ((size_t)p.NU * p.NV * NW + (size_t)kTileX * p.NV * NW);
+    b += sizeof(float) * ((((size_t)p.NIX * p.NIY * p.NIZ + 3) & ~(size_t)3) + p.smem_table_words);
+    return (b + 15) & ~(size_t)15;
+}
+
+int launch_radiality(const RadParams& p, int grid, size_t smem, int in_u16, void* stream) {
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    return in_u16 ? dispatch<uint16_t>(p, grid, smem, st) : dispatch<float>(p, grid, smem, st);
+}
+
+int radiality_max_ctas_per_sm(const RadParams& p, int in_u16, int* out) {
+    const size_t smem = radiality_smem_bytes(p);
+    return in_u16 ? occ_dispatch<uint16_t>(p.mag[2], smem, out) : occ_dispatch<float>(p.mag[2], smem, out);
+}
+
+}  // namespace rfba

@@ -1,0 +1,133 @@
+// Internal definitions shared by the host planner (plan.cpp, capi.cpp) and the
+// CUDA kernels (radiality.cu, temporal.cu). Not part of the public C-ABI.
+#pragma once
+#include <cstdint>
+#include <cstddef>
+#include <string>
+#include <vector>
+
+#include "../../include/rfba_srrf.h"
+
+namespace rfba {
+
+// Output tile of the radiality kernel: 16 x 16 subvoxel columns (one thread
+// each) and FZ = MZ * CZ subvoxels deep along z, held in registers.
+constexpr int kTileX = 16;
+constexpr int kTileY = 16;
+constexpr int kThreads = kTileX * kTileY;
+constexpr int kMaxMag = 8;
+constexpr int kMaxGradRange = 3;
+
+// Coarse z cells per tile for a given z magnification (FZ = MZ * CZ).
+constexpr int cz_for_mag(int mz) {
+    return mz == 1 ? 8 : mz == 2 ? 8 : mz == 3 ? 5 : mz == 4 ? 4 : mz == 5 ? 3 : 2;
+}
+
+// One independent block of the input with the fine region it computes.
+struct BlockDev {
+    int origin[3];   // input voxel origin in the full volume
+    int size[3];     // block dims (input voxels)
+    int lo[3];       // fine region [lo, hi) in block-local magnified coords
+    int hi[3];
+    int rad_lo[3];   // fine indices whose ring samples all pass the window (inclusive)
+    int rad_hi[3];
+    int int_lo[3];   // fine indices whose centre passes the window (inclusive)
+    int int_hi[3];
+    int zbase;       // first fine z of the tile grid (multiple of mz, <= lo[2])
+    int ntile[3];    // tiles along x, y, z
+    int nreg[3];     // region extent hi - lo
+    int pad;
+    long long vox;        // region voxels
+    long long stack_off;  // element offset of this block's [t][v] stack slice
+    long long out_offset;
+    long long out_stride[3];
+};
+
+// Tile work unit: block index and tile coordinates.
+struct TileDesc {
+    int block, tx, ty, tz;
+};
+
+// Deduplicated ring and its factorisation per axis. The n^2 ring samples of
+// kernel.cu:23-33 collapse to distinct points (62 for n = 12) with integer
+// multiplicities; distinct x / y / z coordinate values index the separable
+// Catmull-Rom weight tables.
+struct RingPlan {
+    int n = 0;                     // samples per angle (2 * AxesinRing)
+    std::vector<float> xv, yv, zv; // distinct coordinate values per axis
+    // Point list grouped by x value, then y value: group g covers pairs
+    // [grp[g], grp[g+1]); pair p covers points [pair_pt[p], pair_pt[p+1]).
+    std::vector<int> grp_xval;     // per group: x value index
+    std::vector<int> grp;          // ngroups + 1
+    std::vector<int> pair_yval;    // per pair: y value index
+    std::vector<int> pair_pt;      // npairs + 1
+    std::vector<int> pt_zval;      // per point: z value index
+    std::vector<float> pt_vec;     // per point: (x, y, z)/radius and multiplicity/n (4 floats)
+    int zero_x = -1, zero_y = -1;  // value index of 0 on x and y
+    int npoints_raw = 0;
+    // Raw float ring (n*n points) exactly as the reference builds it.
+    std::vector<float> rx, ry, rz;
+};
+
+// Device-side tables (one contiguous buffer), offsets in 4-byte words.
+struct TableLayout {
+    int wx, offx, wy, offy, wz, wzi, grp_xval, grp, pair_yval, pair_pt, pt_zval, pt_vec;
+    int words;
+};
+
+// Everything the radiality kernel needs; passed by value.
+struct RadParams {
+    const void* in;       // input volume [t][z][y][x]
+    int W, H, D, T;       // full input dims
+    int mag[3];
+    int nxv, nyv, nzv;    // distinct ring values per axis
+    int ngroups, npairs, npoints;
+    int zero_pair;        // pair index of (x=0, y=0), carries the intensity
+    int gr[4];            // gradient ranges: main, x, y, z (smooth=0 => 1,0,0,0)
+    int R;                // gradient halo
+    int NU, NV, NW;       // coarse G tile extents
+    int NIX, NIY, NIZ;    // input tile extents (G tile + halo)
+    int renorm, poscon;
+    int t_chunk, nchunks;
+    int ntiles;
+    long long nitems;
+    const float* tables;  // TableLayout words
+    TableLayout tl;
+    const BlockDev* blocks;
+    const TileDesc* tiles;
+    float* rad_stack;     // [block slice][t][v]
+    float* int_stack;
+    unsigned int* work_counter;
+    int smem_table_words;
+};
+
+// Temporal reduction parameters.
+struct TemporalParams {
+    const BlockDev* blocks;
+    const long long* vox_prefix;  // nblocks + 1 cumulative region voxels
+    int nblocks;
+    long long total_vox;
+    int T;
+    int method, itc, order, iw;
+    float* rad_stack;             // ITC=1 bins in place; rows T..T+order-1 are zero
+    const float* int_stack;
+    float* out;
+    long long stack_rows;         // rows per block slice (T + padding)
+};
+
+// Launchers (radiality.cu / temporal.cu). Return a cudaError_t as int.
+int launch_radiality(const RadParams& p, int grid, size_t smem, int in_u16, void* stream);
+size_t radiality_smem_bytes(const RadParams& p);
+int radiality_max_ctas_per_sm(const RadParams& p, int in_u16, int* out);
+int launch_temporal(const TemporalParams& p, void* stream);
+
+// Host planning (plan.cpp).
+bool build_ring_plan(const rfba_srrf_config& c, RingPlan* rp, std::string* err);
+bool build_tables(const rfba_srrf_config& c, const RingPlan& rp, std::vector<float>* words, TableLayout* tl,
+                  std::string* err);
+bool window_range(float ring_radius_dummy, const std::vector<float>& rcoord, int mag, int dim, int* lo, int* hi);
+int fine_window_int(int mag, int dim, int* lo, int* hi);
+
+void set_error(const std::string& msg);
+
+}  // namespace rfba

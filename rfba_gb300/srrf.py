@@ -1,0 +1,320 @@
+"""Python front end of librfba_srrf.so (ctypes over the C-ABI in
+include/rfba_srrf.h).
+
+Mirrors the reference's GradientCalc interface (RFBA Main/GradientCalc/
+GradientCalc.h:4-5, kernel.cuh:3-26): ``SRRFGradientCalc``, ``SRRFGetMag`` and
+``SRRFGradientCalcGPU`` take and return host float arrays laid out like the
+reference's ([t][z][y][x] in, [z][y][x] magnified out), plus the extended
+interface (explicit configuration, uint16 input, device tensors, block lists,
+plain per-block path). There is no CPU implementation behind this module: if
+the CUDA library is missing or no GPU is present, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+from pathlib import Path
+from typing import Sequence
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_lib" / "librfba_srrf.so"
+
+RFBA_F32 = 0
+RFBA_U16 = 1
+RFBA_HOST_PTRS = 0
+RFBA_DEVICE_PTRS = 1
+
+STATUS = {0: "OK", -1: "INVALID", -2: "UNSUPPORTED", -3: "NOMEM", -4: "CUDA", -5: "TIMEOUT", -6: "IO"}
+
+
+class RfbaError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"rfba status {status} ({STATUS.get(status, '?')}): {msg}")
+        self.status = status
+
+
+class SRRFConf(ctypes.Structure):
+    """The reference's configuration record (kernel.cuh:3-24)."""
+
+    _fields_ = [("RingRadius", ctypes.c_float), ("Magnification", ctypes.c_int), ("AxesinRing", ctypes.c_int),
+                ("MainRange", ctypes.c_int), ("XRange", ctypes.c_int), ("YRange", ctypes.c_int),
+                ("ZRange", ctypes.c_int), ("Method", ctypes.c_int), ("ITC", ctypes.c_int),
+                ("TRACOrder", ctypes.c_int), ("RemoveCon", ctypes.c_int), ("Renormalize", ctypes.c_int),
+                ("GradientSmooth", ctypes.c_int), ("IntensityW", ctypes.c_int), ("blockSizeX", ctypes.c_int),
+                ("blockSizeY", ctypes.c_int), ("blockSizeZ", ctypes.c_int)]
+
+
+class Config(ctypes.Structure):
+    """rfba_srrf_config: SRRFConf with one magnification per axis."""
+
+    _fields_ = [("ring_radius", ctypes.c_float), ("mag", ctypes.c_int * 3), ("axes_in_ring", ctypes.c_int),
+                ("main_range", ctypes.c_int), ("x_range", ctypes.c_int), ("y_range", ctypes.c_int),
+                ("z_range", ctypes.c_int), ("method", ctypes.c_int), ("itc", ctypes.c_int),
+                ("trac_order", ctypes.c_int), ("remove_con", ctypes.c_int), ("renormalize", ctypes.c_int),
+                ("gradient_smooth", ctypes.c_int), ("intensity_w", ctypes.c_int), ("block_size", ctypes.c_int * 3)]
+
+    @classmethod
+    def make(cls, **kw) -> "Config":
+        """Defaults of GradientCalc.cpp:19-41, overridden by keyword; ``mag`` may
+        be an int or a 3-sequence (x, y, z)."""
+        c = cls()
+        _check(lib().rfba_srrf_config_default(ctypes.byref(c)))
+        for k, v in kw.items():
+            if k == "mag":
+                v = (v, v, v) if isinstance(v, int) else tuple(v)
+                for i in range(3):
+                    c.mag[i] = int(v[i])
+            elif k == "block_size":
+                v = (v, v, v) if isinstance(v, int) else tuple(v)
+                for i in range(3):
+                    c.block_size[i] = int(v[i])
+            else:
+                setattr(c, k, v)
+        return c
+
+    @classmethod
+    def from_ini(cls, path: str) -> "Config":
+        c = cls()
+        _check(lib().rfba_srrf_config_load_ini(str(path).encode(), ctypes.byref(c)))
+        return c
+
+    def as_dict(self) -> dict:
+        d = {f: getattr(self, f) for f, _ in self._fields_}
+        d["mag"] = tuple(self.mag)
+        d["block_size"] = tuple(self.block_size)
+        return d
+
+
+class Block(ctypes.Structure):
+    """rfba_block: an independent input sub-volume and the magnified region of
+    it that is computed and written."""
+
+    _fields_ = [("origin", ctypes.c_int32 * 3), ("size", ctypes.c_int32 * 3), ("lo", ctypes.c_int32 * 3),
+                ("hi", ctypes.c_int32 * 3), ("out_offset", ctypes.c_int64), ("out_stride", ctypes.c_int64 * 3)]
+
+
+_lib_handle = None
+
+
+def lib():
+    """The loaded CUDA library; raises if it was not built."""
+    global _lib_handle
+    if _lib_handle is None:
+        if not LIB_PATH.exists():
+            raise ImportError(f"{LIB_PATH} is missing: build it with `python -m rfba_gb300.build` "
+                              "(the SRRF path has no CPU fallback)")
+        L = ctypes.CDLL(str(LIB_PATH))
+        vp, ip = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)
+        fp = ctypes.POINTER(ctypes.c_float)
+        cp = ctypes.POINTER(Config)
+        bp = ctypes.POINTER(Block)
+        L.rfba_last_error.restype = ctypes.c_char_p
+        L.rfba_version.restype = ctypes.c_char_p
+        L.rfba_ctx_create.argtypes = [ctypes.c_int, ctypes.c_size_t, ctypes.POINTER(vp)]
+        L.rfba_ctx_destroy.argtypes = [vp]
+        L.rfba_ctx_set_timing.argtypes = [vp, ctypes.c_int]
+        L.rfba_ctx_last_timing.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                           ctypes.POINTER(ctypes.c_longlong)]
+        L.rfba_ctx_set_launch.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+        L.rfba_srrf_config_default.argtypes = [cp]
+        L.rfba_srrf_config_load_ini.argtypes = [ctypes.c_char_p, cp]
+        L.rfba_srrf_config_from_legacy.argtypes = [ctypes.POINTER(SRRFConf), cp]
+        L.rfba_srrf_forward.argtypes = [vp, cp, vp, ctypes.c_int, ip, vp, ctypes.c_int, vp]
+        L.rfba_srrf_forward_blocks.argtypes = [vp, cp, vp, ctypes.c_int, ip, bp, ctypes.c_int, vp, ctypes.c_int64,
+                                               ctypes.c_int, vp]
+        L.rfba_srrf_forward_blocks_plain.argtypes = [vp, cp, vp, ctypes.c_int, ip, bp, ctypes.c_int, vp,
+                                                     ctypes.c_int64]
+        L.rfba_blocks_gradientcalc.argtypes = [cp, ip, bp, ctypes.c_int]
+        L.rfba_blocks_dosplit.argtypes = [cp, ip, ip, ctypes.c_int, bp, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]
+        L.SRRFGradientCalc.argtypes = [fp, ip, fp]
+        L.SRRFGetMag.argtypes = []
+        L.SRRFGradientCalcGPU.argtypes = [fp, ip, fp, ctypes.POINTER(SRRFConf)]
+        _lib_handle = L
+    return _lib_handle
+
+
+def last_error() -> str:
+    return lib().rfba_last_error().decode()
+
+
+def _check(status: int):
+    if status < 0:
+        raise RfbaError(status, last_error())
+    return status
+
+
+def _dims(shape: Sequence[int]) -> np.ndarray:
+    T, D, H, W = shape
+    return np.array([W, H, D, T], np.int32)
+
+
+def _iptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+def _fptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+# ---- reference-compatible entry points ------------------------------------
+
+def SRRFGradientCalc(in_image: np.ndarray) -> np.ndarray:
+    """GradientCalc.cpp:169 on a float32 [T][D][H][W] array; reads ./SRRF.ini.
+    Returns the magnified map [D*m][H*m][W*m]."""
+    a = np.ascontiguousarray(in_image, np.float32)
+    dims = _dims(a.shape)
+    m = SRRFGetMag()
+    out = np.empty((a.shape[1] * m, a.shape[2] * m, a.shape[3] * m), np.float32)
+    _check(lib().SRRFGradientCalc(_fptr(a), _iptr(dims), _fptr(out)))
+    return out
+
+
+def SRRFGetMag() -> int:
+    return int(lib().SRRFGetMag())
+
+
+def SRRFGradientCalcGPU(in_image: np.ndarray, conf: SRRFConf) -> np.ndarray:
+    """kernel.cu:560: one block, explicit SRRFConf, full magnified output."""
+    a = np.ascontiguousarray(in_image, np.float32)
+    dims = _dims(a.shape)
+    m = conf.Magnification
+    out = np.empty((a.shape[1] * m, a.shape[2] * m, a.shape[3] * m), np.float32)
+    _check(lib().SRRFGradientCalcGPU(_fptr(a), _iptr(dims), _fptr(out), ctypes.byref(conf)))
+    return out
+
+
+# ---- block lists -------------------------------------------------------------
+
+def blocks_gradientcalc(cfg: Config, shape: Sequence[int]):
+    """GradientCalc.cpp:47-116 blocks (border 2) for an input [T][D][H][W]."""
+    dims = _dims(shape)
+    n = _check(lib().rfba_blocks_gradientcalc(ctypes.byref(cfg), _iptr(dims), None, 0))
+    arr = (Block * max(n, 1))()
+    _check(lib().rfba_blocks_gradientcalc(ctypes.byref(cfg), _iptr(dims), arr, n))
+    return arr, n
+
+
+def blocks_dosplit(cfg: Config, shape: Sequence[int], max_size, border: int):
+    """doSplit.m blocks; each block's whole magnified output packed in order.
+    Returns (blocks, count, out_elems)."""
+    dims = _dims(shape)
+    ms = np.array(max_size if not isinstance(max_size, int) else (max_size,) * 3, np.int32)
+    oe = ctypes.c_int64()
+    n = _check(lib().rfba_blocks_dosplit(ctypes.byref(cfg), _iptr(dims), _iptr(ms), border, None, 0, ctypes.byref(oe)))
+    arr = (Block * max(n, 1))()
+    _check(lib().rfba_blocks_dosplit(ctypes.byref(cfg), _iptr(dims), _iptr(ms), border, arr, n, ctypes.byref(oe)))
+    return arr, n, int(oe.value)
+
+
+# ---- extended interface --------------------------------------------------------
+
+@dataclass
+class Timing:
+    radiality_ms: float
+    temporal_ms: float
+    launches: int
+
+
+class Context:
+    """A device context: scratch buffers, ring plan cache, stream."""
+
+    def __init__(self, device: int = 0, scratch_budget_bytes: int = 0):
+        h = ctypes.c_void_p()
+        _check(lib().rfba_ctx_create(device, scratch_budget_bytes, ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().rfba_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_timing(self, on: bool):
+        _check(lib().rfba_ctx_set_timing(self.h, int(on)))
+
+    def set_launch(self, grid: int = 0, t_chunk: int = 0):
+        _check(lib().rfba_ctx_set_launch(self.h, grid, t_chunk))
+
+    def timing(self) -> Timing:
+        a, b, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
+        _check(lib().rfba_ctx_last_timing(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(n)))
+        return Timing(a.value, b.value, n.value)
+
+    @staticmethod
+    def _in(x):
+        """(pointer, dtype code, dims, is_device) of a numpy array or torch tensor."""
+        if isinstance(x, np.ndarray):
+            if x.dtype == np.uint16:
+                dt = RFBA_U16
+            elif x.dtype == np.float32:
+                dt = RFBA_F32
+            else:
+                raise TypeError("input must be uint16 or float32")
+            if not x.flags.c_contiguous:
+                raise ValueError("input must be C-contiguous")
+            return ctypes.c_void_p(x.ctypes.data), dt, _dims(x.shape), False
+        import torch  # device tensors
+        if x.dtype == torch.uint16 if hasattr(torch, "uint16") else False:
+            dt = RFBA_U16
+        elif x.dtype == torch.float32:
+            dt = RFBA_F32
+        elif str(x.dtype) == "torch.int16":  # uint16 bits carried in int16
+            dt = RFBA_U16
+        else:
+            raise TypeError("input must be uint16 or float32")
+        if not x.is_contiguous():
+            raise ValueError("input must be contiguous")
+        return ctypes.c_void_p(x.data_ptr()), dt, _dims(tuple(x.shape)), x.is_cuda
+
+    def forward(self, cfg: Config, x, out=None, stream=None):
+        """Whole volume as one block. x: numpy [T][D][H][W] (host) or a CUDA
+        tensor (device); returns / fills the map [D*mz][H*my][W*mx]."""
+        ptr, dt, dims, dev = self._in(x)
+        shape = (int(dims[2]) * cfg.mag[2], int(dims[1]) * cfg.mag[1], int(dims[0]) * cfg.mag[0])
+        if out is None:
+            if dev:
+                import torch
+                out = torch.empty(shape, dtype=torch.float32, device=x.device)
+            else:
+                out = np.empty(shape, np.float32)
+        optr = ctypes.c_void_p(out.data_ptr() if dev else out.ctypes.data)
+        st = ctypes.c_void_p(stream) if stream else None
+        _check(lib().rfba_srrf_forward(self.h, ctypes.byref(cfg), ptr, dt, _iptr(dims), optr,
+                                       RFBA_DEVICE_PTRS if dev else RFBA_HOST_PTRS, st))
+        return out
+
+    def forward_blocks(self, cfg: Config, x, blocks, nblocks: int, out_elems: int, out=None, stream=None):
+        ptr, dt, dims, dev = self._in(x)
+        if out is None:
+            if dev:
+                import torch
+                out = torch.zeros(out_elems, dtype=torch.float32, device=x.device)
+            else:
+                out = np.zeros(out_elems, np.float32)
+        optr = ctypes.c_void_p(out.data_ptr() if dev else out.ctypes.data)
+        st = ctypes.c_void_p(stream) if stream else None
+        _check(lib().rfba_srrf_forward_blocks(self.h, ctypes.byref(cfg), ptr, dt, _iptr(dims), blocks, nblocks, optr,
+                                              out_elems, RFBA_DEVICE_PTRS if dev else RFBA_HOST_PTRS, st))
+        return out
+
+    def forward_blocks_plain(self, cfg: Config, x: np.ndarray, blocks, nblocks: int, out_elems: int, out=None):
+        ptr, dt, dims, dev = self._in(x)
+        if dev:
+            raise ValueError("the plain per-block path takes host arrays")
+        if out is None:
+            out = np.zeros(out_elems, np.float32)
+        _check(lib().rfba_srrf_forward_blocks_plain(self.h, ctypes.byref(cfg), ptr, dt, _iptr(dims), blocks, nblocks,
+                                                    ctypes.c_void_p(out.ctypes.data), out_elems))
+        return out
+
+
+def version() -> str:
+    return lib().rfba_version().decode()
