@@ -1,0 +1,336 @@
+"""Benchmark of the SRRF radiality path on one GB300 (or N replicas).
+
+Workload (default, "mid"): 100 volumes of 128x128x64 uint16 (filament-like
+synthetic scene, seed 1235), magnification 4x4x2 (512x512x128 output), ring
+radius 0.5, 12 ring axes (AxesinRing 6), smoothed gradient with ranges 1,
+TRAC-2 (ITC 0) with intensity weighting. One step = one full forward over the
+whole series: fused gradient+interpolation+radiality kernel, then the temporal
+reduction.
+
+Printed JSON line (rank 0):
+  value    output voxel-volumes per second, inputs already in HBM, device time
+           (CUDA events on the launching stream) over exactly --steps steps;
+  e2e      the same metric through the C-ABI entry point with pinned host
+           buffers (host->device input copy and device->host map copy inside
+           the timed region);
+  roofline FP32 throughput of the radiality kernel: algorithmic flops of the
+           separable method per launch / average launch time, against the
+           nominal FP32 FMA peak at the measured maximum SM clock;
+  cpu_baseline  the FP32 CPU port of the reference radiality loop (oracle/,
+           OpenMP over all host cores) timed on a bounded sub-slab.
+--impl reference times that CPU implementation alone (the reference has no
+runnable GPU path here: its CUDA sources are not available on the GPU host).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD = dict(name="mid", T=100, shape=(128, 128, 64), mag=(4, 4, 2), method=3, itc=0, trac_order=2)
+CFG_KW = dict(mag=(4, 4, 2), method=3, itc=0, trac_order=2, gradient_smooth=1, main_range=1, x_range=1,
+              y_range=1, z_range=1, intensity_w=1, axes_in_ring=6, ring_radius=0.5)
+# CPU sample: a fine sub-slab of the same workload, all time points
+CPU_REGION_LO = (240, 240, 56)
+CPU_REGION_HI = (272, 272, 72)
+# per-step sample of the reference arm (smaller, so K + W steps stay short)
+REF_REGION_LO = (240, 240, 56)
+REF_REGION_HI = (256, 256, 64)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_input(volumes=None):
+    from rfba_gb300 import synth
+    x, _ = synth.workload("mid", n_vol=volumes)
+    return x
+
+
+def algorithmic_flops_per_voxel_volume(cfg) -> dict:
+    """Flops per output voxel-volume of the separable method as implemented
+    (rfba_gb300.srrf.flops_per_voxel_volume), with the direct forms for
+    reference: the reference executes ~90,700 per voxel-volume (144 samples x 3
+    x 64-tap interpolations with recomputed weights); over the 62 distinct points
+    the direct form is ~39,300."""
+    from rfba_gb300 import srrf
+    info = srrf.plan_info(cfg)
+    return {"separable": srrf.flops_per_voxel_volume(cfg), **info,
+            "direct_distinct": 39300.0, "direct_reference": 90700.0}
+
+
+def fp32_peak_tflops(sm_count: int, sm_mhz: float) -> float:
+    return sm_count * 128 * 2 * sm_mhz * 1e6 / 1e12
+
+
+def cpu_baseline(x: np.ndarray, reps: int = 1):
+    """FP32 CPU port of the reference radiality loop on a sub-slab (all T)."""
+    from oracle import oracle as O
+    oc = O.make_conf(**{k: v for k, v in CFG_KW.items()})
+    xf = x.astype(np.float32)
+    lo, hi = CPU_REGION_LO, CPU_REGION_HI
+    n_vox = int(np.prod(np.array(hi) - np.array(lo)))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        O.srrf_region(xf, oc, lo, hi, dtype=np.float32)
+    dt = time.perf_counter() - t0
+    units = n_vox * x.shape[0] * reps
+    return {"value": units / dt, "unit": "voxel-volumes/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"fine region x{lo[0]}:{hi[0]} y{lo[1]}:{hi[1]} z{lo[2]}:{hi[2]} of the 512x512x128 map, "
+                      f"all {x.shape[0]} volumes ({units} voxel-volumes, {dt:.1f} s); FP32 port of kernel.cu "
+                      f"(all 144 ring samples, OpenMP over subvoxels)"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    x = make_input()
+    oc = O.make_conf(**CFG_KW)
+    xf = x.astype(np.float32)
+    lo, hi = REF_REGION_LO, REF_REGION_HI
+    n_vox = int(np.prod(np.array(hi) - np.array(lo)))
+    for _ in range(args.warmup):
+        O.srrf_region(xf, oc, lo, hi, dtype=np.float32)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.srrf_region(xf, oc, lo, hi, dtype=np.float32)
+    dt = time.perf_counter() - t0
+    units = n_vox * x.shape[0] * args.steps
+    v = units / dt
+    line = {
+        "impl": "reference", "metric": "radiality voxel-volumes/s", "value": v, "unit": "voxel-volumes/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "mid: 100 x 128x128x64 u16, mag 4x4x2, TRAC-2 ITC0, 12 axes, r 0.5",
+                   "sample": f"fine region {lo}-{hi}, all volumes"},
+        "cpu_baseline": {"value": v, "unit": "voxel-volumes/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": f"fine region {lo}-{hi} of the 512x512x128 map, all 100 volumes per step; "
+                                   "FP32 port of the reference kernel.cu radiality loop, OpenMP over all cores"},
+        "e2e": {"value": v, "unit": "voxel-volumes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    from rfba_gb300 import build as B
+    B.build()
+    from rfba_gb300 import srrf
+
+    x = make_input(args.volumes)
+    T, D, H, W = x.shape
+    cfg = srrf.Config.make(**CFG_KW)
+    mx, my, mz = CFG_KW["mag"]
+    out_shape = (D * mz, H * my, W * mx)
+    units_per_step = out_shape[0] * out_shape[1] * out_shape[2] * T
+
+    ctx = srrf.Context(local)
+    stream = torch.cuda.current_stream()
+    xd = torch.from_numpy(x.view(np.int16)).cuda()
+    out = torch.empty(out_shape, dtype=torch.float32, device="cuda")
+
+    def step():
+        ctx.forward(cfg, xd, out=out, stream=stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    # timed region: device time over exactly K steps
+    ctx.set_timing(True)
+    launches0 = ctx.timing().launches
+    sampler = ClockSampler(local)
+    sampler.start()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    rad_ms = []
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+        rad_ms.append(ctx.timing().radiality_ms)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1)
+    launches = ctx.timing().launches - launches0
+    ctx.set_timing(False)
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = units_per_step * args.steps * ws / (ms / 1e3)
+
+    # e2e: C-ABI entry point with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        pinned = torch.empty(x.nbytes, dtype=torch.uint8).pin_memory()
+        pinned_np = pinned.numpy().view(np.uint16).reshape(x.shape)
+        pinned_np[...] = x
+        outh = torch.empty(out_shape, dtype=torch.float32).pin_memory()
+        outh_np = outh.numpy()
+        for _ in range(max(1, args.warmup // 2)):
+            ctx.forward(cfg, pinned_np, out=outh_np)
+        if ws > 1:
+            torch.distributed.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            ctx.forward(cfg, pinned_np, out=outh_np)
+        e2e_s = time.perf_counter() - t0
+        if ws > 1:
+            t = torch.tensor([e2e_s], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        e2e = units_per_step * args.steps * ws / e2e_s
+
+    # roofline of the radiality kernel
+    props = torch.cuda.get_device_properties(local)
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        pass
+    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
+    peak = fp32_peak_tflops(props.multi_processor_count, sm_max)
+    fl = algorithmic_flops_per_voxel_volume(cfg)
+    rad_avg_ms = statistics.mean(rad_ms) if rad_ms else float("nan")
+    achieved = fl["separable"] * units_per_step / (rad_avg_ms / 1e3) / 1e12
+    traffic = None
+    tf = ROOT / "profiles" / "traffic_radiality_mid.json"
+    if tf.exists():
+        try:
+            traffic = json.loads(tf.read_text()).get("bytes_per_launch")
+        except Exception:
+            traffic = None
+
+    line = {
+        "metric": "radiality voxel-volumes/s", "value": value, "unit": "voxel-volumes/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "mid: 100 x 128x128x64 u16 -> 512x512x128 map, mag 4x4x2, ring r 0.5, 12 axes, "
+                               "smoothed gradient (ranges 1), TRAC-2 ITC0, intensity weighting",
+                   "global_batch": T, "parallelism": "replicas" if ws > 1 else "single",
+                   "l2": "inputs larger than L2 (210 MB input, 26.8 GB radiality/intensity stack per step)"},
+        "e2e": {"value": e2e, "unit": "voxel-volumes/s", "h2d_bytes_per_step": int(x.nbytes),
+                "d2h_bytes_per_step": int(np.prod(out_shape) * 4)},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "radiality_kernel<4,4,u16>", "kernel_ms": rad_avg_ms,
+                     "flops_per_voxel_volume": fl["separable"],
+                     "peak_note": f"nominal FP32 FMA peak {props.multi_processor_count} SMs x 128 x 2 at the "
+                                  f"measured max SM clock {sm_max:.0f} MHz"},
+        "direct_equivalent_tflops": fl["direct_distinct"] * units_per_step / (rad_avg_ms / 1e3) / 1e12,
+    }
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(x)
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
+    ap.add_argument("--volumes", type=int, default=None,
+                    help="fewer volumes than the workload's 100 (profiling case only)")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl != "reference":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

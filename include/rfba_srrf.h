@@ -163,6 +163,21 @@ int rfba_blocks_gradientcalc(const rfba_srrf_config* cfg, const int dims[4], rfb
 int rfba_blocks_dosplit(const rfba_srrf_config* cfg, const int dims[4], const int max_size[3], int border,
                         rfba_block* blocks, int cap, int64_t* out_elems);
 
+/* Ring factorisation used by the kernels for this configuration: distinct ring
+ * points (the reference evaluates all (2*AxesinRing)^2 samples, kernel.cu:215-
+ * 216; coincident ones are merged with a multiplicity), distinct (x, y) pairs,
+ * distinct x values, and the raw sample count. Any pointer may be NULL. */
+int rfba_srrf_plan_info(const rfba_srrf_config* cfg, int* npoints, int* npairs, int* nxvalues, int* nraw);
+
+/* Measurement hooks: CUDA-event durations of the last call's kernels, taken on
+ * the stream they were launched on (enable first), and the number of kernels
+ * the context has launched. */
+int rfba_ctx_set_timing(rfba_ctx* ctx, int enable);
+int rfba_ctx_last_timing(rfba_ctx* ctx, double* radiality_ms, double* temporal_ms, long long* launches);
+/* Launch overrides for tuning: CTAs of the radiality kernel and time points per
+ * work item (0 = automatic). */
+int rfba_ctx_set_launch(rfba_ctx* ctx, int grid, int t_chunk);
+
 /* Text of the last error on the calling thread ("" if none). */
 const char* rfba_last_error(void);
 

@@ -222,8 +222,9 @@ static int make_blocks(rfba_ctx* ctx, const rfba_srrf_config& cfg, const int dim
             s.out_offset = d.out_offset + (long long)(z0 - b.lo[2]) * d.out_stride[2];
             for (int a = 0; a < 3; ++a) s.nreg[a] = s.hi[a] - s.lo[a];
             s.zbase = (s.lo[2] / cfg.mag[2]) * cfg.mag[2];
+            const int TY = tile_rows_for_mag(cfg.mag[1]);
             s.ntile[0] = (s.nreg[0] + kTileX - 1) / kTileX;
-            s.ntile[1] = (s.nreg[1] + kTileY - 1) / kTileY;
+            s.ntile[1] = (s.nreg[1] + TY - 1) / TY;
             s.ntile[2] = (s.hi[2] - s.zbase + FZ - 1) / FZ;
             s.vox = (long long)s.nreg[0] * s.nreg[1] * s.nreg[2];
             outb->push_back(s);
@@ -315,8 +316,9 @@ static int run_device(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void* in
         }
         rp.R = std::max(std::max(rp.gr[0], rp.gr[1]), std::max(rp.gr[2], rp.gr[3]));
         const int CZ = cz_for_mag(cfg.mag[2]);
+        rp.TY = tile_rows_for_mag(cfg.mag[1]);
         rp.NU = (kTileX - 1) / cfg.mag[0] + 2 + 4;
-        rp.NV = (kTileY - 1) / cfg.mag[1] + 2 + 4;
+        rp.NV = (rp.TY - 1) / cfg.mag[1] + 2 + 4;
         rp.NW = CZ + 4;
         rp.NIX = rp.NU + 2 * rp.R;
         rp.NIY = rp.NV + 2 * rp.R;
@@ -528,6 +530,25 @@ int rfba_ctx_set_launch(rfba_ctx* c, int grid, int t_chunk) {
     if (!c) return RFBA_ERR_INVALID;
     c->grid_override = grid;
     c->chunk_override = t_chunk;
+    return RFBA_OK;
+}
+
+int rfba_srrf_plan_info(const rfba_srrf_config* cfg, int* npoints, int* npairs, int* nxvalues, int* nraw) {
+    if (!cfg) return RFBA_ERR_INVALID;
+    std::string err;
+    if (!config_validate(*cfg, &err)) {
+        set_error(err);
+        return RFBA_ERR_INVALID;
+    }
+    RingPlan rp;
+    if (!build_ring_plan(*cfg, &rp, &err)) {
+        set_error(err);
+        return RFBA_ERR_UNSUPPORTED;
+    }
+    if (npoints) *npoints = (int)rp.pt_zval.size();
+    if (npairs) *npairs = (int)rp.pair_yval.size();
+    if (nxvalues) *nxvalues = (int)rp.grp_xval.size();
+    if (nraw) *nraw = rp.npoints_raw;
     return RFBA_OK;
 }
 

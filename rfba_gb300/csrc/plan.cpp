@@ -245,6 +245,7 @@ bool build_ring_plan(const rfba_srrf_config& c, RingPlan* rp, std::string* err) 
     rp->pair_pt.clear();
     rp->pt_zval.clear();
     rp->pt_vec.clear();
+    rp->pair_rot.clear();
     rp->zero_x = rp->zero_y = -1;
     for (size_t i = 0; i < xv.size(); ++i)
         if (xv[i] == 0.f) rp->zero_x = (int)i;
@@ -263,16 +264,21 @@ bool build_ring_plan(const rfba_srrf_config& c, RingPlan* rp, std::string* err) 
             last_a = p.a;
             last_b = -1;
         }
+        const double ux = (double)p.x / r, uy = (double)p.y / r, uz = (double)p.z / r;
+        const double hxy = std::sqrt(ux * ux + uy * uy);
+        const double un = std::sqrt(ux * ux + uy * uy + uz * uz);
         if (p.b != last_b) {
             rp->pair_yval.push_back(p.b);
             rp->pair_pt.push_back((int)k);
             last_b = p.b;
+            rp->pair_rot.push_back(hxy > 0 ? (float)(ux / hxy) : 1.f);
+            rp->pair_rot.push_back(hxy > 0 ? (float)(uy / hxy) : 0.f);
         }
         rp->pt_zval.push_back(p.c);
-        rp->pt_vec.push_back(p.x / r);
-        rp->pt_vec.push_back(p.y / r);
-        rp->pt_vec.push_back(p.z / r);
+        rp->pt_vec.push_back((float)(hxy / un));
+        rp->pt_vec.push_back((float)(uz / un));
         rp->pt_vec.push_back((float)p.m / (float)n);  // kernel.cu:244 divides by n, not n^2
+        rp->pt_vec.push_back((float)(-un));
     }
     rp->grp.push_back((int)rp->pair_yval.size());
     rp->pair_pt.push_back((int)pts.size());
@@ -394,6 +400,8 @@ bool build_tables(const rfba_srrf_config& c, const RingPlan& rp, std::vector<flo
     align4();
     tl->pt_vec = (int)W.size();
     for (float v : rp.pt_vec) W.push_back(v);
+    tl->pair_rot = (int)W.size();
+    for (float v : rp.pair_rot) W.push_back(v);
     align4();
     tl->words = (int)W.size();
     return true;

@@ -3,8 +3,8 @@
 // Replaces the reference's gradKernel (kernel.cu:44-125) and calculateRadiality
 // (kernel.cu:186-253, with interpolateG kernel.cu:141-169, _calculateDk
 // kernel.cu:174-183 and interpolateIntensity kernel.cu:257-287) by one
-// persistent kernel. Per work item (block, 16x16xFZ subvoxel tile, time chunk)
-// and time point:
+// persistent kernel. Per work item (block, subvoxel tile, time chunk) and time
+// point:
 //
 //   1. the input tile plus halo is read (block-edge clamped, as the
 //      reference's fminf/fmaxf clamps do) into shared memory;
@@ -15,22 +15,30 @@
 //      and a sample's x taps and weights depend only on the subvoxel's x phase
 //      (X mod mag_x) and the ring point's x coordinate, so for each distinct ring
 //      x value the x-filtered field U is formed once in shared memory;
-//   4. each thread owns one (X, Y) subvoxel column; for each distinct (x, y)
-//      ring pair it y-filters U into a register column T[w] over coarse z, and
-//      for each ring point of that pair it z-filters T (5 taps, static register
-//      indices) for its FZ subvoxels and accumulates the radiality term;
+//   4. each thread owns two subvoxel columns (X, Y) and (X, Y + mag_y): same y
+//      phase, adjacent coarse rows, so the y pass reads 5 rows of U for both.
+//      For each distinct (x, y) ring pair it y-filters U into a register column
+//      T[w] over coarse z (one float2 per w: the two columns), and for each ring
+//      point of that pair it z-filters T (5 taps, static register indices) for
+//      its FZ subvoxels per column and accumulates the radiality term. The
+//      per-point work runs on packed f32x2 FMAs (two columns per instruction);
 //   5. radiality and interpolated intensity per subvoxel and time point are
 //      written to the stack that the temporal kernel reduces.
 //
 // The radiality term of a sample with interpolated gradient g and ring offset
-// rho (kernel.cu:224-240) is evaluated in the equivalent, rounding-robust form
-//   s = |g x rho| / (|g| r)   (= Dk / r),   D = (1 - s)^2,
-//   S -= D if g.rho > 0, S += D otherwise,
-// with g = 0 giving NaN exactly as the reference's 0/0 does. Coordinates are
-// local (phase + ring offset), so no precision is lost at large volume
-// coordinates. The sample window test (kernel.cu:146) makes the whole subvoxel
-// NaN; it is evaluated on the host per axis with the reference's float
-// arithmetic and applied here as a per-block valid box.
+// rho (kernel.cu:224-240), with u = rho / r, is evaluated in a rotated frame:
+// (x, y) is turned about z so that u lies in the x'z plane, u = |u| (h x' + c z).
+// Then g.u / |u| = h g_x' + c g_z, the part of g perpendicular to u has the
+// components g_y' and h g_z - c g_x', and
+//   Dk / r = |u| sin(angle(g, u)) = |u| sqrt(|g_perp|^2 / |g|^2),
+//   D = (1 - Dk/r)^2,   S -= D if g.u > 0, S += D otherwise.
+// The perpendicular part is formed directly, so Dk has full relative accuracy
+// even when g is almost parallel to u; g = 0 gives 0 * inf = NaN exactly as the
+// reference's 0/0 does. Coordinates are local (phase + ring offset), so no
+// precision is lost at large volume coordinates. The sample window test
+// (kernel.cu:146) makes a whole subvoxel NaN; it is evaluated on the host per
+// axis with the reference's float arithmetic and applied here as a per-block
+// valid box.
 #include <cuda_runtime.h>
 #include <cstdint>
 
@@ -49,6 +57,16 @@ __device__ __forceinline__ float sqrt_approx(float x) {
     asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
 }
+// copysign(w, -d) for w >= 0: -w when d > 0 (diverging), +w when d < 0. At
+// d = 0 the sample is perpendicular to g, s = |u| and D vanishes, so the sign
+// taken there does not matter.
+__device__ __forceinline__ float sign_weight(float w, float d) {
+    return __int_as_float(__float_as_int(w) | (~__float_as_int(d) & 0x80000000));
+}
+
+__device__ __forceinline__ float2 dup(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 
 template <typename Tin>
 __device__ __forceinline__ float load_in(const Tin* p, long long i);
@@ -68,8 +86,8 @@ __device__ __forceinline__ int floordiv(int a, int b) {  // b > 0
     return (a % b != 0 && a < 0) ? q - 1 : q;
 }
 
-template <int MZ, int CZ, typename Tin>
-__global__ void __launch_bounds__(kThreads, 2) radiality_kernel(const RadParams p) {
+template <int MZ, int CZ, typename Tin, bool WIDE>
+__global__ void __launch_bounds__(WIDE ? kMaxThreads : 128, WIDE ? 2 : 3) radiality_kernel(const RadParams p) {
     constexpr int FZ = MZ * CZ;
     constexpr int NW = CZ + 4;
     extern __shared__ float4 smem4[];
@@ -82,12 +100,15 @@ __global__ void __launch_bounds__(kThreads, 2) radiality_kernel(const RadParams 
     float* tab = inp + ((p.NIX * p.NIY * p.NIZ + 3) & ~3);         // 16-byte aligned (float4 reads)
     __shared__ unsigned int s_item;
 
+    const int nthr = blockDim.x;
     const int tid = threadIdx.x;
-    const int xf = tid & (kTileX - 1);
-    const int yf = tid / kTileX;
     const int mx = p.mag[0], my = p.mag[1];
+    // column pair of this thread: (X, Ya) and (X, Ya + my)
+    const int xf = tid & (kTileX - 1);
+    const int q = tid / kTileX;                   // 0 .. TY/2 - 1
+    const int yfa = (q / my) * (2 * my) + (q % my);
 
-    for (int i = tid; i < p.smem_table_words; i += kThreads) tab[i] = p.tables[i];
+    for (int i = tid; i < p.smem_table_words; i += nthr) tab[i] = p.tables[i];
     const float* wx = tab + p.tl.wx;
     const int* offx = reinterpret_cast<const int*>(tab + p.tl.offx);
     const float* wy = tab + p.tl.wy;
@@ -100,6 +121,7 @@ __global__ void __launch_bounds__(kThreads, 2) radiality_kernel(const RadParams 
     const int* pair_pt = reinterpret_cast<const int*>(tab + p.tl.pair_pt);
     const int* pt_zval = reinterpret_cast<const int*>(tab + p.tl.pt_zval);
     const float4* pt_vec = reinterpret_cast<const float4*>(tab + p.tl.pt_vec);
+    const float2* pair_rot = reinterpret_cast<const float2*>(tab + p.tl.pair_rot);
 
     const Tin* in = static_cast<const Tin*>(p.in);
     const int NIX = p.NIX, NIY = p.NIY, NIZ = p.NIZ, R = p.R;
@@ -121,24 +143,36 @@ __global__ void __launch_bounds__(kThreads, 2) radiality_kernel(const RadParams 
 
         // Tile geometry (block-local fine and coarse coordinates).
         const int X0 = B.lo[0] + td.tx * kTileX;
-        const int Y0 = B.lo[1] + td.ty * kTileY;
+        const int Y0 = B.lo[1] + td.ty * p.TY;
         const int Z0 = B.zbase + td.tz * FZ;
         const int cx0 = floordiv(X0, mx) - 2;
         const int cy0 = floordiv(Y0, my) - 2;
         const int cz0 = Z0 / MZ - 2;
-        const int X = X0 + xf, Y = Y0 + yf;
+        const int X = X0 + xf;
+        const int Ya = Y0 + yfa, Yb = Ya + my;
         const int xi = floordiv(X, mx), xr = X - xi * mx;
-        const int yi = floordiv(Y, my), yr = Y - yi * my;
-        const bool col_in = (X < B.hi[0]) && (Y < B.hi[1]);
-        const bool colx_ok = X >= B.rad_lo[0] && X <= B.rad_hi[0] && Y >= B.rad_lo[1] && Y <= B.rad_hi[1];
-        const bool coli_ok = X >= B.int_lo[0] && X <= B.int_hi[0] && Y >= B.int_lo[1] && Y <= B.int_hi[1];
+        const int yi = floordiv(Ya, my), yr = Ya - yi * my;  // Yb: yi + 1, same phase
+        const bool xin = X < B.hi[0];
+        const bool ina = xin && Ya < B.hi[1];
+        const bool inb = xin && Yb < B.hi[1];
+        const bool xrad = X >= B.rad_lo[0] && X <= B.rad_hi[0];
+        const bool xint = X >= B.int_lo[0] && X <= B.int_hi[0];
+        const bool rada = xrad && Ya >= B.rad_lo[1] && Ya <= B.rad_hi[1];
+        const bool radb = xrad && Yb >= B.rad_lo[1] && Yb <= B.rad_hi[1];
+        const bool inta = xint && Ya >= B.int_lo[1] && Ya <= B.int_hi[1];
+        const bool intb = xint && Yb >= B.int_lo[1] && Yb <= B.int_hi[1];
+        const long long V = B.vox;
+        const long long va = ((long long)(Ya - B.lo[1])) * B.nreg[0] + (X - B.lo[0]);
+        const long long vb = ((long long)(Yb - B.lo[1])) * B.nreg[0] + (X - B.lo[0]);
+        const long long zstride = (long long)B.nreg[0] * B.nreg[1];
 
         const int t0 = chunk * p.t_chunk;
         const int t1 = min(p.T, t0 + p.t_chunk);
         for (int t = t0; t < t1; ++t) {
+            const long long sbase = B.stack_off + (long long)t * V;
             // 1. input tile with block-edge clamp
             const long long tbase = (long long)t * p.D * p.H * p.W;
-            for (int i = tid; i < nin; i += kThreads) {
+            for (int i = tid; i < nin; i += nthr) {
                 const int ix = i % NIX;
                 const int iy = (i / NIX) % NIY;
                 const int iz = i / (NIX * NIY);
@@ -151,17 +185,15 @@ __global__ void __launch_bounds__(kThreads, 2) radiality_kernel(const RadParams 
             }
             __syncthreads();
             // 2. gradient + intensity per coarse cell
-            for (int c = tid; c < ncell; c += kThreads) {
+            for (int c = tid; c < ncell; c += nthr) {
                 const int u = c % NU;
                 const int v = (c / NU) % NV;
                 const int w = c / (NU * NV);
                 const int cu = cx0 + u, cv = cy0 + v, cw = cz0 + w;
                 float4 g4 = make_float4(0.f, 0.f, 0.f, 0.f);
                 if (cu >= 0 && cu < bw && cv >= 0 && cv < bh && cw >= 0 && cw < bd) {
-                    const int ux = u + R, vy = v + R, wz_ = w + R;
-                    auto I = [&](int dx, int dy, int dz) {
-                        return inp[((wz_ + dz) * NIY + (vy + dy)) * NIX + (ux + dx)];
-                    };
+                    const float* base = inp + ((w + R) * NIY + (v + R)) * NIX + (u + R);
+                    auto I = [&](int dx, int dy, int dz) { return base[(dz * NIY + dy) * NIX + dx]; };
                     const int mR = p.gr[0], xR = p.gr[1], yR = p.gr[2], zR = p.gr[3];
                     float gx = 0.f, gy = 0.f, gz = 0.f;
                     for (int i = 1; i <= mR; ++i)
@@ -178,13 +210,9 @@ __global__ void __launch_bounds__(kThreads, 2) radiality_kernel(const RadParams 
                 gt[c] = g4;
             }
 
-            float S[FZ];
-            float Iv[FZ];
+            float2 S[FZ];
 #pragma unroll
-            for (int z = 0; z < FZ; ++z) {
-                S[z] = 0.f;
-                Iv[z] = 0.f;
-            }
+            for (int z = 0; z < FZ; ++z) S[z] = make_float2(0.f, 0.f);
 
             for (int gi = 0; gi < p.ngroups; ++gi) {
                 __syncthreads();  // gt ready / previous U consumed
@@ -194,7 +222,7 @@ __global__ void __launch_bounds__(kThreads, 2) radiality_kernel(const RadParams 
                     const int o = offx[a * mx + xr];
                     const float4 wv = *reinterpret_cast<const float4*>(wx + (a * mx + xr) * 4);
                     const int ub = xi - cx0 - 2 + o;
-                    for (int e = tid; e < nut; e += kThreads) {
+                    for (int e = tid; e < nut; e += nthr) {
                         const int vw = e / kTileX;  // (w * NV + v)
                         const float4* src = gt + vw * NU + ub;
                         const float4 g0 = src[0], g1 = src[1], g2 = src[2], g3 = src[3];
@@ -212,83 +240,124 @@ __global__ void __launch_bounds__(kThreads, 2) radiality_kernel(const RadParams 
                     const int b = pair_yval[pi];
                     const int o = offy[b * my + yr];
                     const float4 wv = *reinterpret_cast<const float4*>(wy + (b * my + yr) * 4);
-                    const int vb = yi - cy0 - 2 + o;
-                    const bool with_int = (pi == p.zero_pair);
-                    float Tx[NW], Ty[NW], Tz[NW], Tw[NW];
+                    const int vbase = yi - cy0 - 2 + o;  // column a rows vbase..+3, column b rows vbase+1..+4
+                    if (pi == p.zero_pair) {
+                        // intensity at the subvoxel centre (interpolateIntensity): the
+                        // (0, 0) pair's x/y passes are the intensity's; z pass with rho_z = 0
+                        float2 Tw[NW];
 #pragma unroll
-                    for (int w = 0; w < NW; ++w) {
-                        const float4* src = ut + (w * NV + vb) * kTileX + xf;
-                        const float4 u0 = src[0], u1 = src[kTileX], u2 = src[2 * kTileX], u3 = src[3 * kTileX];
-                        Tx[w] = fmaf(wv.w, u3.x, fmaf(wv.z, u2.x, fmaf(wv.y, u1.x, wv.x * u0.x)));
-                        Ty[w] = fmaf(wv.w, u3.y, fmaf(wv.z, u2.y, fmaf(wv.y, u1.y, wv.x * u0.y)));
-                        Tz[w] = fmaf(wv.w, u3.z, fmaf(wv.z, u2.z, fmaf(wv.y, u1.z, wv.x * u0.z)));
-                        Tw[w] = fmaf(wv.w, u3.w, fmaf(wv.z, u2.w, fmaf(wv.y, u1.w, wv.x * u0.w)));
-                    }
-                    if (with_int) {
+                        for (int w = 0; w < NW; ++w) {
+                            const float4* src = ut + (w * NV + vbase) * kTileX + xf;
+                            const float u0 = src[0].w, u1 = src[kTileX].w, u2 = src[2 * kTileX].w,
+                                        u3 = src[3 * kTileX].w, u4 = src[4 * kTileX].w;
+                            Tw[w].x = fmaf(wv.w, u3, fmaf(wv.z, u2, fmaf(wv.y, u1, wv.x * u0)));
+                            Tw[w].y = fmaf(wv.w, u4, fmaf(wv.z, u3, fmaf(wv.y, u2, wv.x * u1)));
+                        }
 #pragma unroll
                         for (int z = 0; z < FZ; ++z) {
                             const int zr = z % MZ, zi = z / MZ;
-                            const float* q = wzi + zr * 5;
-                            float acc = q[0] * Tw[zi];
+                            const float* qz = wzi + zr * 5;
+                            float2 acc = mul2(dup(qz[0]), Tw[zi]);
 #pragma unroll
-                            for (int m = 1; m < 5; ++m) acc = fmaf(q[m], Tw[zi + m], acc);
-                            Iv[z] = acc;
+                            for (int m = 1; m < 5; ++m) acc = fma2(dup(qz[m]), Tw[zi + m], acc);
+                            const int Z = Z0 + z;
+                            if (Z >= B.lo[2] && Z < B.hi[2]) {
+                                const bool zint = Z >= B.int_lo[2] && Z <= B.int_hi[2];
+                                const long long zo = sbase + (long long)(Z - B.lo[2]) * zstride;
+                                if (ina) p.int_stack[zo + va] = (inta && zint) ? fmaxf(acc.x, 0.f) : 0.f;
+                                if (inb) p.int_stack[zo + vb] = (intb && zint) ? fmaxf(acc.y, 0.f) : 0.f;
+                            }
+                        }
+                    }
+                    float2 Tx[NW], Ty[NW], Tz[NW];
+#pragma unroll
+                    for (int w = 0; w < NW; ++w) {
+                        const float4* src = ut + (w * NV + vbase) * kTileX + xf;
+                        const float4 u0 = src[0], u1 = src[kTileX], u2 = src[2 * kTileX], u3 = src[3 * kTileX],
+                                     u4 = src[4 * kTileX];
+                        Tx[w].x = fmaf(wv.w, u3.x, fmaf(wv.z, u2.x, fmaf(wv.y, u1.x, wv.x * u0.x)));
+                        Ty[w].x = fmaf(wv.w, u3.y, fmaf(wv.z, u2.y, fmaf(wv.y, u1.y, wv.x * u0.y)));
+                        Tz[w].x = fmaf(wv.w, u3.z, fmaf(wv.z, u2.z, fmaf(wv.y, u1.z, wv.x * u0.z)));
+                        Tx[w].y = fmaf(wv.w, u4.x, fmaf(wv.z, u3.x, fmaf(wv.y, u2.x, wv.x * u1.x)));
+                        Ty[w].y = fmaf(wv.w, u4.y, fmaf(wv.z, u3.y, fmaf(wv.y, u2.y, wv.x * u1.y)));
+                        Tz[w].y = fmaf(wv.w, u4.z, fmaf(wv.z, u3.z, fmaf(wv.y, u2.z, wv.x * u1.z)));
+                    }
+                    // rotate (x, y) about z so that the pair's ring direction lies in the
+                    // x'z plane: P = g.x', E = g.y' (x' = (ux, uy)/h, y' = z x x')
+                    {
+                        const float2 rot = pair_rot[pi];
+                        const float2 ca = dup(rot.x), sb = dup(rot.y), nsb = dup(-rot.y);
+#pragma unroll
+                        for (int w = 0; w < NW; ++w) {
+                            const float2 gx = Tx[w], gy = Ty[w];
+                            Tx[w] = fma2(gy, sb, mul2(gx, ca));
+                            Ty[w] = fma2(gy, ca, mul2(gx, nsb));
                         }
                     }
                     for (int qi = pair_pt[pi]; qi < pair_pt[pi + 1]; ++qi) {
+                        // point u = |u| (h x' + c z): dot = g.u/|u| = h P + c Z, the
+                        // perpendicular part of g is (E, h Z - c P), and Dk/r = |u| sin(angle)
                         const float4 pv = pt_vec[qi];
+                        const float2 hh = dup(pv.x), cc = dup(pv.y), ncc = dup(-pv.y);
+                        const float wgt = pv.z;
+                        const float2 nun = dup(pv.w);  // -|u|
+                        const float2 one = dup(1.0f);
                         const float* wzc = wz + pt_zval[qi] * (MZ * 5);
-                        float wzr[MZ][5];
 #pragma unroll
-                        for (int zr = 0; zr < MZ; ++zr)
+                        for (int zr = 0; zr < MZ; ++zr) {
+                          // z weights of one phase at a time keep register pressure low
+                          float2 wzr[5];
 #pragma unroll
-                            for (int m = 0; m < 5; ++m) wzr[zr][m] = wzc[zr * 5 + m];
+                          for (int m = 0; m < 5; ++m) wzr[m] = dup(wzc[zr * 5 + m]);
 #pragma unroll
-                        for (int z = 0; z < FZ; ++z) {
-                            const int zr = z % MZ, zi = z / MZ;
-                            float gx = wzr[zr][0] * Tx[zi];
-                            float gy = wzr[zr][0] * Ty[zi];
-                            float gz = wzr[zr][0] * Tz[zi];
+                          for (int zi = 0; zi < CZ; ++zi) {
+                            const int z = zi * MZ + zr;
+                            float2 gx = mul2(wzr[0], Tx[zi]);
+                            float2 gy = mul2(wzr[0], Ty[zi]);
+                            float2 gz = mul2(wzr[0], Tz[zi]);
 #pragma unroll
                             for (int m = 1; m < 5; ++m) {
-                                gx = fmaf(wzr[zr][m], Tx[zi + m], gx);
-                                gy = fmaf(wzr[zr][m], Ty[zi + m], gy);
-                                gz = fmaf(wzr[zr][m], Tz[zi + m], gz);
+                                gx = fma2(wzr[m], Tx[zi + m], gx);
+                                gy = fma2(wzr[m], Ty[zi + m], gy);
+                                gz = fma2(wzr[m], Tz[zi + m], gz);
                             }
-                            const float dot = fmaf(gz, pv.z, fmaf(gy, pv.y, gx * pv.x));
-                            const float crx = fmaf(gy, pv.z, -gz * pv.y);
-                            const float cry = fmaf(gz, pv.x, -gx * pv.z);
-                            const float crz = fmaf(gx, pv.y, -gy * pv.x);
-                            const float c2 = fmaf(crz, crz, fmaf(cry, cry, crx * crx));
-                            const float g2 = fmaf(gz, gz, fmaf(gy, gy, gx * gx));
-                            const float s = sqrt_approx(c2 * rcp_approx(g2));
-                            const float om = 1.0f - s;
-                            const float D = om * om;
-                            S[z] = fmaf(D, dot > 0.f ? -pv.w : pv.w, S[z]);
+                            // gx = P, gy = E, gz = Z after the pair rotation
+                            const float2 dot = fma2(cc, gz, mul2(hh, gx));
+                            const float2 cp = fma2(hh, gz, mul2(ncc, gx));
+                            const float2 c2 = fma2(cp, cp, mul2(gy, gy));     // |g x u|^2 / |u|^2
+                            const float2 g2 = fma2(dot, dot, c2);             // |g|^2
+                            const float2 q2 = make_float2(rcp_approx(g2.x), rcp_approx(g2.y));
+                            const float2 s2 = mul2(c2, q2);                   // sin^2; g = 0 gives 0 * inf = NaN
+                            const float2 s = make_float2(sqrt_approx(s2.x), sqrt_approx(s2.y));
+                            const float2 om = fma2(s, nun, one);              // 1 - Dk/r
+                            const float2 D = mul2(om, om);
+                            const float2 sw = make_float2(sign_weight(wgt, dot.x), sign_weight(wgt, dot.y));
+                            S[z] = fma2(D, sw, S[z]);
+                          }
                         }
                     }
                 }
             }
 
-            // 5. finalize and store
-            if (col_in) {
-                const long long V = B.vox;
-                const long long sbase = B.stack_off + (long long)t * V;
+            // 5. finalize and store radiality
 #pragma unroll
-                for (int z = 0; z < FZ; ++z) {
-                    const int Z = Z0 + z;
-                    if (Z < B.lo[2] || Z >= B.hi[2]) continue;
-                    float r = S[z];
-                    const bool zok = Z >= B.rad_lo[2] && Z <= B.rad_hi[2];
-                    if (!(colx_ok && zok)) r = __int_as_float(0x7fc00000);
-                    if (p.renorm) r = 0.5f + r * 0.5f;
-                    if (p.poscon) r = fmaxf(r, 0.f);
-                    const bool ziok = Z >= B.int_lo[2] && Z <= B.int_hi[2];
-                    const float iv = (coli_ok && ziok) ? fmaxf(Iv[z], 0.f) : 0.f;
-                    const long long v = ((long long)(Z - B.lo[2]) * B.nreg[1] + (Y - B.lo[1])) * B.nreg[0] + (X - B.lo[0]);
-                    p.rad_stack[sbase + v] = r;
-                    p.int_stack[sbase + v] = iv;
+            for (int z = 0; z < FZ; ++z) {
+                const int Z = Z0 + z;
+                if (Z < B.lo[2] || Z >= B.hi[2]) continue;
+                const bool zok = Z >= B.rad_lo[2] && Z <= B.rad_hi[2];
+                const long long zo = sbase + (long long)(Z - B.lo[2]) * zstride;
+                float ra = (rada && zok) ? S[z].x : __int_as_float(0x7fc00000);
+                float rb = (radb && zok) ? S[z].y : __int_as_float(0x7fc00000);
+                if (p.renorm) {
+                    ra = 0.5f + ra * 0.5f;
+                    rb = 0.5f + rb * 0.5f;
                 }
+                if (p.poscon) {
+                    ra = fmaxf(ra, 0.f);
+                    rb = fmaxf(rb, 0.f);
+                }
+                if (ina) p.rad_stack[zo + va] = ra;
+                if (inb) p.rad_stack[zo + vb] = rb;
             }
         }
     }
@@ -297,20 +366,20 @@ __global__ void __launch_bounds__(kThreads, 2) radiality_kernel(const RadParams 
 template <int MZ, typename Tin>
 int launch_mz(const RadParams& p, int grid, size_t smem, cudaStream_t st) {
     constexpr int CZ = cz_for_mag(MZ);
-    auto k = radiality_kernel<MZ, CZ, Tin>;
+    auto k = p.TY > 16 ? radiality_kernel<MZ, CZ, Tin, true> : radiality_kernel<MZ, CZ, Tin, false>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
-    k<<<grid, kThreads, smem, st>>>(p);
+    k<<<grid, p.TY * (kTileX / 2), smem, st>>>(p);
     return (int)cudaGetLastError();
 }
 
 template <int MZ, typename Tin>
-int occ_mz(size_t smem, int* out) {
+int occ_mz(int threads, size_t smem, int* out) {
     constexpr int CZ = cz_for_mag(MZ);
-    auto k = radiality_kernel<MZ, CZ, Tin>;
+    auto k = threads > 128 ? radiality_kernel<MZ, CZ, Tin, true> : radiality_kernel<MZ, CZ, Tin, false>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
-    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k, kThreads, smem);
+    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k, threads, smem);
 }
 
 template <typename Tin>
@@ -329,21 +398,32 @@ int dispatch(const RadParams& p, int grid, size_t smem, cudaStream_t st) {
 }
 
 template <typename Tin>
-int occ_dispatch(int mz, size_t smem, int* out) {
+int occ_dispatch(int mz, int threads, size_t smem, int* out) {
     switch (mz) {
-        case 1: return occ_mz<1, Tin>(smem, out);
-        case 2: return occ_mz<2, Tin>(smem, out);
-        case 3: return occ_mz<3, Tin>(smem, out);
-        case 4: return occ_mz<4, Tin>(smem, out);
-        case 5: return occ_mz<5, Tin>(smem, out);
-        case 6: return occ_mz<6, Tin>(smem, out);
-        case 7: return occ_mz<7, Tin>(smem, out);
-        case 8: return occ_mz<8, Tin>(smem, out);
+        case 1: return occ_mz<1, Tin>(threads, smem, out);
+        case 2: return occ_mz<2, Tin>(threads, smem, out);
+        case 3: return occ_mz<3, Tin>(threads, smem, out);
+        case 4: return occ_mz<4, Tin>(threads, smem, out);
+        case 5: return occ_mz<5, Tin>(threads, smem, out);
+        case 6: return occ_mz<6, Tin>(threads, smem, out);
+        case 7: return occ_mz<7, Tin>(threads, smem, out);
+        case 8: return occ_mz<8, Tin>(threads, smem, out);
     }
     return (int)cudaErrorInvalidValue;
 }
 
 }  // namespace
+
+// Tile height (subvoxel rows) for a y magnification: a multiple of 2*my (each
+// thread pairs row y with y + my) and of 4 (whole warps of 16 x 2 threads).
+int tile_rows_for_mag(int my) {
+    switch (my) {
+        case 1: case 2: case 4: case 8: return 16;
+        case 3: case 6: return 12;
+        case 5: return 20;
+        default: return 28;  // 7
+    }
+}
 
 size_t radiality_smem_bytes(const RadParams& p) {
     const int NW = cz_for_mag(p.mag[2]) + 4;
@@ -359,7 +439,9 @@ int launch_radiality(const RadParams& p, int grid, size_t smem, int in_u16, void
 
 int radiality_max_ctas_per_sm(const RadParams& p, int in_u16, int* out) {
     const size_t smem = radiality_smem_bytes(p);
-    return in_u16 ? occ_dispatch<uint16_t>(p.mag[2], smem, out) : occ_dispatch<float>(p.mag[2], smem, out);
+    const int threads = p.TY * (kTileX / 2);
+    return in_u16 ? occ_dispatch<uint16_t>(p.mag[2], threads, smem, out)
+                  : occ_dispatch<float>(p.mag[2], threads, smem, out);
 }
 
 }  // namespace rfba

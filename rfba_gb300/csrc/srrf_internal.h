@@ -10,11 +10,11 @@
 
 namespace rfba {
 
-// Output tile of the radiality kernel: 16 x 16 subvoxel columns (one thread
-// each) and FZ = MZ * CZ subvoxels deep along z, held in registers.
+// Output tile of the radiality kernel: 16 x TY subvoxel columns (two per
+// thread, TY from tile_rows_for_mag) and FZ = MZ * CZ subvoxels deep along z,
+// held in registers.
 constexpr int kTileX = 16;
-constexpr int kTileY = 16;
-constexpr int kThreads = kTileX * kTileY;
+constexpr int kMaxThreads = 224;  // 16 x 14 threads for the 28-row tile (mag_y 7)
 constexpr int kMaxMag = 8;
 constexpr int kMaxGradRange = 3;
 
@@ -62,7 +62,9 @@ struct RingPlan {
     std::vector<int> pair_yval;    // per pair: y value index
     std::vector<int> pair_pt;      // npairs + 1
     std::vector<int> pt_zval;      // per point: z value index
-    std::vector<float> pt_vec;     // per point: (x, y, z)/radius and multiplicity/n (4 floats)
+    std::vector<float> pt_vec;     // per point: h, c, multiplicity/n, -|u| (u = (x, y, z)/radius
+                                   // = |u| (h x' + c z) in the pair's rotated frame)
+    std::vector<float> pair_rot;   // per pair: x' = (ux, uy)/|(ux, uy)|, (1, 0) on the z axis
     int zero_x = -1, zero_y = -1;  // value index of 0 on x and y
     int npoints_raw = 0;
     // Raw float ring (n*n points) exactly as the reference builds it.
@@ -71,7 +73,7 @@ struct RingPlan {
 
 // Device-side tables (one contiguous buffer), offsets in 4-byte words.
 struct TableLayout {
-    int wx, offx, wy, offy, wz, wzi, grp_xval, grp, pair_yval, pair_pt, pt_zval, pt_vec;
+    int wx, offx, wy, offy, wz, wzi, grp_xval, grp, pair_yval, pair_pt, pt_zval, pt_vec, pair_rot;
     int words;
 };
 
@@ -85,6 +87,7 @@ struct RadParams {
     int zero_pair;        // pair index of (x=0, y=0), carries the intensity
     int gr[4];            // gradient ranges: main, x, y, z (smooth=0 => 1,0,0,0)
     int R;                // gradient halo
+    int TY;               // subvoxel rows per tile (threads = 8 * TY)
     int NU, NV, NW;       // coarse G tile extents
     int NIX, NIY, NIZ;    // input tile extents (G tile + halo)
     int renorm, poscon;
@@ -118,6 +121,7 @@ struct TemporalParams {
 // Launchers (radiality.cu / temporal.cu). Return a cudaError_t as int.
 int launch_radiality(const RadParams& p, int grid, size_t smem, int in_u16, void* stream);
 size_t radiality_smem_bytes(const RadParams& p);
+int tile_rows_for_mag(int my);
 int radiality_max_ctas_per_sm(const RadParams& p, int in_u16, int* out);
 int launch_temporal(const TemporalParams& p, void* stream);
 

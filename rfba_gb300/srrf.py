@@ -129,6 +129,7 @@ def lib():
                                                      ctypes.c_int64]
         L.rfba_blocks_gradientcalc.argtypes = [cp, ip, bp, ctypes.c_int]
         L.rfba_blocks_dosplit.argtypes = [cp, ip, ip, ctypes.c_int, bp, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]
+        L.rfba_srrf_plan_info.argtypes = [cp, ip, ip, ip, ip]
         L.SRRFGradientCalc.argtypes = [fp, ip, fp]
         L.SRRFGetMag.argtypes = []
         L.SRRFGradientCalcGPU.argtypes = [fp, ip, fp, ctypes.POINTER(SRRFConf)]
@@ -184,6 +185,28 @@ def SRRFGradientCalcGPU(in_image: np.ndarray, conf: SRRFConf) -> np.ndarray:
     out = np.empty((a.shape[1] * m, a.shape[2] * m, a.shape[3] * m), np.float32)
     _check(lib().SRRFGradientCalcGPU(_fptr(a), _iptr(dims), _fptr(out), ctypes.byref(conf)))
     return out
+
+
+def plan_info(cfg: "Config") -> dict:
+    """Ring factorisation the kernels use: distinct points, (x, y) pairs, x
+    values, and the reference's raw sample count."""
+    v = [ctypes.c_int() for _ in range(4)]
+    _check(lib().rfba_srrf_plan_info(ctypes.byref(cfg), *[ctypes.byref(x) for x in v]))
+    return {"points": v[0].value, "pairs": v[1].value, "xvalues": v[2].value, "raw": v[3].value}
+
+
+def flops_per_voxel_volume(cfg: "Config") -> float:
+    """Flops per output voxel-volume of the separable method as implemented
+    (FMA = 2): per distinct ring point, the 5-tap z interpolation of three
+    gradient components (27) and the radiality term in the rotated frame (19);
+    per (x, y) pair, the 4-tap y pass and the frame rotation over coarse z
+    ((21 + 6) / mag_z); per x value, the 4-tap x pass (21 / (mag_y mag_z)); the
+    smoothed gradient (162 / (mag_x mag_y mag_z)); the intensity interpolation
+    (9) and the temporal reduction (10)."""
+    info = plan_info(cfg)
+    mx, my, mz = cfg.mag[0], cfg.mag[1], cfg.mag[2]
+    return (info["points"] * 46 + info["pairs"] * 27.0 / mz + info["xvalues"] * 21.0 / (my * mz)
+            + 162.0 / (mx * my * mz) + 9 + 10)
 
 
 # ---- block lists -------------------------------------------------------------

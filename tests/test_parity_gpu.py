@@ -56,7 +56,8 @@ def test_forward_matches_oracle(ctx, oracle_mod, name, T, D, H, W, kw):
     x = _series(100 + len(name), T, D, H, W)
     got = ctx.forward(cfg, x)
     ref = oracle_mod.srrf_region(x.astype(np.float32), oc)
-    assert_parity(got, ref, tol_for(cfg.method), name)
+    err = assert_parity(got, ref, tol_for(cfg.method), name)
+    print(f"[parity] {name}: rel L-inf {err:.2e}")
 
 
 def test_float_input_matches_u16(ctx):
