@@ -315,6 +315,12 @@ static int run_device(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void* in
             rp.gr[3] = cfg.z_range;
         }
         rp.R = std::max(std::max(rp.gr[0], rp.gr[1]), std::max(rp.gr[2], rp.gr[3]));
+        if (rp.gr[0] == 1 && rp.gr[1] == 1 && rp.gr[2] == 1 && rp.gr[3] == 1)
+            rp.grad_mode = 1;
+        else if (rp.gr[0] == 1 && rp.gr[1] == 0 && rp.gr[2] == 0 && rp.gr[3] == 0)
+            rp.grad_mode = 2;
+        else
+            rp.grad_mode = 0;
         const int CZ = cz_for_mag(cfg.mag[2]);
         rp.TY = tile_rows_for_mag(cfg.mag[1]);
         rp.NU = (kTileX - 1) / cfg.mag[0] + 2 + 4;

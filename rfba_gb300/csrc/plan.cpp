@@ -372,15 +372,20 @@ bool build_tables(const rfba_srrf_config& c, const RingPlan& rp, std::vector<flo
     tl->offy = (int)W.size();
     for (int v : oy) push_int(v);
     tl->wz = (int)W.size();
+    std::vector<int> oz(nc, 0);
     for (int cc = 0; cc < nc; ++cc)
         for (int ph = 0; ph < mz; ++ph) {
-            float w[5];
-            if (!tap5(ph, rp.zv[cc], mz, w)) {
+            float w[4];
+            int off;
+            if (!tap4(ph, rp.zv[cc], mz, w, &off)) {
                 *err = "ring radius too large for the z magnification (needs ring_radius < (1 + mag)/2)";
                 return false;
             }
-            for (int m = 0; m < 5; ++m) W.push_back(w[m]);
+            for (int m = 0; m < 4; ++m) W.push_back(w[m]);
+            oz[cc] |= off << ph;  // bit ph: taps start one coarse cell later
         }
+    tl->offz = (int)W.size();
+    for (int v : oz) push_int(v);
     tl->wzi = (int)W.size();
     for (int ph = 0; ph < mz; ++ph) {
         float w[5];

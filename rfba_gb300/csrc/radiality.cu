@@ -19,9 +19,11 @@
 //      phase, adjacent coarse rows, so the y pass reads 5 rows of U for both.
 //      For each distinct (x, y) ring pair it y-filters U into a register column
 //      T[w] over coarse z (one float2 per w: the two columns), and for each ring
-//      point of that pair it z-filters T (5 taps, static register indices) for
-//      its FZ subvoxels per column and accumulates the radiality term. The
-//      per-point work runs on packed f32x2 FMAs (two columns per instruction);
+//      point of that pair it z-filters T (4 taps; the tap offset per z phase is
+//      uniform over the warp, so both offsets are unrolled with static register
+//      indices) for its FZ subvoxels per column and accumulates the radiality
+//      term. The per-point work runs on packed f32x2 FMAs (two columns per
+//      instruction);
 //   5. radiality and interpolated intensity per subvoxel and time point are
 //      written to the stack that the temporal kernel reduces.
 //
@@ -47,16 +49,16 @@
 namespace rfba {
 namespace {
 
-__device__ __forceinline__ float rcp_approx(float x) {
+__device__ __forceinline__ float rsqrt_approx(float x) {
     float r;
-    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
 }
-__device__ __forceinline__ float sqrt_approx(float x) {
-    float r;
-    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
+
+template <int V>
+struct IntC {
+    static constexpr int value = V;
+};
 // copysign(w, -d) for w >= 0: -w when d > 0 (diverging), +w when d < 0. At
 // d = 0 the sample is perpendicular to g, s = |u| and D vanishes, so the sign
 // taken there does not matter.
@@ -84,6 +86,53 @@ __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? l
 __device__ __forceinline__ int floordiv(int a, int b) {  // b > 0
     int q = a / b;
     return (a % b != 0 && a < 0) ? q - 1 : q;
+}
+
+// gradKernel's smoothed gradient (kernel.cu:73-124) at one coarse cell from the
+// clamped input tile: Gx = sum over i in [1, mR], j in [-yR, yR], k in
+// [-zR, zR] of I(+i, j, k) - I(-i, j, k), and likewise for y and z; with
+// smoothing off the reference's central difference is the case mR = 1 and all
+// lateral ranges 0. The .w component carries I at the cell. Fixed ranges are
+// fully unrolled; integer inputs make the sums exact in float whatever the order.
+template <int MR, int XR, int YR, int ZR>
+__device__ __forceinline__ float4 gradient_fixed(const float* base, int NIX, int NIY) {
+    auto I = [&](int dx, int dy, int dz) { return base[(dz * NIY + dy) * NIX + dx]; };
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+#pragma unroll
+    for (int i = 1; i <= MR; ++i)
+#pragma unroll
+        for (int j = -YR; j <= YR; ++j)
+#pragma unroll
+            for (int k = -ZR; k <= ZR; ++k) gx += I(i, j, k) - I(-i, j, k);
+#pragma unroll
+    for (int j = 1; j <= MR; ++j)
+#pragma unroll
+        for (int i = -XR; i <= XR; ++i)
+#pragma unroll
+            for (int k = -ZR; k <= ZR; ++k) gy += I(i, j, k) - I(i, -j, k);
+#pragma unroll
+    for (int k = 1; k <= MR; ++k)
+#pragma unroll
+        for (int i = -XR; i <= XR; ++i)
+#pragma unroll
+            for (int j = -YR; j <= YR; ++j) gz += I(i, j, k) - I(i, j, -k);
+    return make_float4(gx, gy, gz, I(0, 0, 0));
+}
+
+__device__ __forceinline__ float4 gradient_generic(const float* base, int NIX, int NIY, const int gr[4]) {
+    auto I = [&](int dx, int dy, int dz) { return base[(dz * NIY + dy) * NIX + dx]; };
+    const int mR = gr[0], xR = gr[1], yR = gr[2], zR = gr[3];
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+    for (int i = 1; i <= mR; ++i)
+        for (int j = -yR; j <= yR; ++j)
+            for (int k = -zR; k <= zR; ++k) gx += I(i, j, k) - I(-i, j, k);
+    for (int j = 1; j <= mR; ++j)
+        for (int i = -xR; i <= xR; ++i)
+            for (int k = -zR; k <= zR; ++k) gy += I(i, j, k) - I(i, -j, k);
+    for (int k = 1; k <= mR; ++k)
+        for (int i = -xR; i <= xR; ++i)
+            for (int j = -yR; j <= yR; ++j) gz += I(i, j, k) - I(i, j, -k);
+    return make_float4(gx, gy, gz, I(0, 0, 0));
 }
 
 template <int MZ, int CZ, typename Tin, bool WIDE>
@@ -114,6 +163,7 @@ __global__ void __launch_bounds__(WIDE ? kMaxThreads : 128, WIDE ? 2 : 3) radial
     const float* wy = tab + p.tl.wy;
     const int* offy = reinterpret_cast<const int*>(tab + p.tl.offy);
     const float* wz = tab + p.tl.wz;
+    const int* offz = reinterpret_cast<const int*>(tab + p.tl.offz);
     const float* wzi = tab + p.tl.wzi;
     const int* grp_xval = reinterpret_cast<const int*>(tab + p.tl.grp_xval);
     const int* grp = reinterpret_cast<const int*>(tab + p.tl.grp);
@@ -170,18 +220,18 @@ __global__ void __launch_bounds__(WIDE ? kMaxThreads : 128, WIDE ? 2 : 3) radial
         const int t1 = min(p.T, t0 + p.t_chunk);
         for (int t = t0; t < t1; ++t) {
             const long long sbase = B.stack_off + (long long)t * V;
-            // 1. input tile with block-edge clamp
+            // 1. input tile with block-edge clamp; 16 lanes per row, one division
+            //    per row
             const long long tbase = (long long)t * p.D * p.H * p.W;
-            for (int i = tid; i < nin; i += nthr) {
-                const int ix = i % NIX;
-                const int iy = (i / NIX) % NIY;
-                const int iz = i / (NIX * NIY);
-                const int bx = clampi(cx0 - R + ix, 0, bw - 1);
+            for (int r = tid / kTileX; r < NIY * NIZ; r += nthr / kTileX) {
+                const int iy = r % NIY, iz = r / NIY;
                 const int by = clampi(cy0 - R + iy, 0, bh - 1);
                 const int bz = clampi(cz0 - R + iz, 0, bd - 1);
-                const long long g = tbase + ((long long)(B.origin[2] + bz) * p.H + (B.origin[1] + by)) * p.W +
-                                    (B.origin[0] + bx);
-                inp[i] = load_in<Tin>(in, g);
+                const long long rowg = tbase + ((long long)(B.origin[2] + bz) * p.H + (B.origin[1] + by)) * p.W +
+                                       B.origin[0];
+                float* rows = inp + r * NIX;
+                for (int ix = xf; ix < NIX; ix += kTileX)
+                    rows[ix] = load_in<Tin>(in, rowg + clampi(cx0 - R + ix, 0, bw - 1));
             }
             __syncthreads();
             // 2. gradient + intensity per coarse cell
@@ -193,19 +243,12 @@ __global__ void __launch_bounds__(WIDE ? kMaxThreads : 128, WIDE ? 2 : 3) radial
                 float4 g4 = make_float4(0.f, 0.f, 0.f, 0.f);
                 if (cu >= 0 && cu < bw && cv >= 0 && cv < bh && cw >= 0 && cw < bd) {
                     const float* base = inp + ((w + R) * NIY + (v + R)) * NIX + (u + R);
-                    auto I = [&](int dx, int dy, int dz) { return base[(dz * NIY + dy) * NIX + dx]; };
-                    const int mR = p.gr[0], xR = p.gr[1], yR = p.gr[2], zR = p.gr[3];
-                    float gx = 0.f, gy = 0.f, gz = 0.f;
-                    for (int i = 1; i <= mR; ++i)
-                        for (int j = -yR; j <= yR; ++j)
-                            for (int k = -zR; k <= zR; ++k) gx += I(i, j, k) - I(-i, j, k);
-                    for (int j = 1; j <= mR; ++j)
-                        for (int i = -xR; i <= xR; ++i)
-                            for (int k = -zR; k <= zR; ++k) gy += I(i, j, k) - I(i, -j, k);
-                    for (int k = 1; k <= mR; ++k)
-                        for (int i = -xR; i <= xR; ++i)
-                            for (int j = -yR; j <= yR; ++j) gz += I(i, j, k) - I(i, j, -k);
-                    g4 = make_float4(gx, gy, gz, I(0, 0, 0));
+                    if (p.grad_mode == 1)
+                        g4 = gradient_fixed<1, 1, 1, 1>(base, NIX, NIY);
+                    else if (p.grad_mode == 2)
+                        g4 = gradient_fixed<1, 0, 0, 0>(base, NIX, NIY);
+                    else
+                        g4 = gradient_generic(base, NIX, NIY, p.gr);
                 }
                 gt[c] = g4;
             }
@@ -301,39 +344,51 @@ __global__ void __launch_bounds__(WIDE ? kMaxThreads : 128, WIDE ? 2 : 3) radial
                         const float2 hh = dup(pv.x), cc = dup(pv.y), ncc = dup(-pv.y);
                         const float wgt = pv.z;
                         const float2 nun = dup(pv.w);  // -|u|
-                        const float2 one = dup(1.0f);
-                        const float* wzc = wz + pt_zval[qi] * (MZ * 5);
+                        const int zc = pt_zval[qi];
+                        const float* wzc = wz + zc * (MZ * 4);
+                        const int offmask = offz[zc];
+                        auto zpass = [&](auto OFF, int zr, const float2 (&w4)[4]) {
+                            constexpr int o = decltype(OFF)::value;
+#pragma unroll
+                            for (int zi = 0; zi < CZ; ++zi) {
+                                const int z = zi * MZ + zr;
+                                float2 gx = mul2(w4[0], Tx[zi + o]);
+                                float2 gy = mul2(w4[0], Ty[zi + o]);
+                                float2 gz = mul2(w4[0], Tz[zi + o]);
+#pragma unroll
+                                for (int m = 1; m < 4; ++m) {
+                                    gx = fma2(w4[m], Tx[zi + o + m], gx);
+                                    gy = fma2(w4[m], Ty[zi + o + m], gy);
+                                    gz = fma2(w4[m], Tz[zi + o + m], gz);
+                                }
+                                // gx = P, gy = E, gz = Z after the pair rotation
+                                const float2 dot = fma2(cc, gz, mul2(hh, gx));
+                                const float2 cp = fma2(hh, gz, mul2(ncc, gx));
+                                const float2 c2 = fma2(cp, cp, mul2(gy, gy));  // |g_perp|^2
+                                const float2 g2 = fma2(dot, dot, c2);          // |g|^2
+                                // sin = c2 / sqrt((c2 + 1e-12 g2) g2): one rsqrt per lane. The
+                                // guard term makes g parallel to u give 0 and leaves g = 0 at
+                                // 0 * inf = NaN (the reference's 0/0).
+                                const float2 xx = mul2(fma2(g2, dup(1e-12f), c2), g2);
+                                const float2 r = make_float2(rsqrt_approx(xx.x), rsqrt_approx(xx.y));
+                                const float2 sn = mul2(c2, r);
+                                const float2 om = fma2(sn, nun, dup(1.0f));     // 1 - Dk/r
+                                const float2 D = mul2(om, om);
+                                const float2 sw = make_float2(sign_weight(wgt, dot.x), sign_weight(wgt, dot.y));
+                                S[z] = fma2(D, sw, S[z]);
+                            }
+                        };
 #pragma unroll
                         for (int zr = 0; zr < MZ; ++zr) {
-                          // z weights of one phase at a time keep register pressure low
-                          float2 wzr[5];
+                            // weights of one phase at a time keep register pressure low;
+                            // the tap offset is uniform over the warp
+                            float2 w4[4];
 #pragma unroll
-                          for (int m = 0; m < 5; ++m) wzr[m] = dup(wzc[zr * 5 + m]);
-#pragma unroll
-                          for (int zi = 0; zi < CZ; ++zi) {
-                            const int z = zi * MZ + zr;
-                            float2 gx = mul2(wzr[0], Tx[zi]);
-                            float2 gy = mul2(wzr[0], Ty[zi]);
-                            float2 gz = mul2(wzr[0], Tz[zi]);
-#pragma unroll
-                            for (int m = 1; m < 5; ++m) {
-                                gx = fma2(wzr[m], Tx[zi + m], gx);
-                                gy = fma2(wzr[m], Ty[zi + m], gy);
-                                gz = fma2(wzr[m], Tz[zi + m], gz);
-                            }
-                            // gx = P, gy = E, gz = Z after the pair rotation
-                            const float2 dot = fma2(cc, gz, mul2(hh, gx));
-                            const float2 cp = fma2(hh, gz, mul2(ncc, gx));
-                            const float2 c2 = fma2(cp, cp, mul2(gy, gy));     // |g x u|^2 / |u|^2
-                            const float2 g2 = fma2(dot, dot, c2);             // |g|^2
-                            const float2 q2 = make_float2(rcp_approx(g2.x), rcp_approx(g2.y));
-                            const float2 s2 = mul2(c2, q2);                   // sin^2; g = 0 gives 0 * inf = NaN
-                            const float2 s = make_float2(sqrt_approx(s2.x), sqrt_approx(s2.y));
-                            const float2 om = fma2(s, nun, one);              // 1 - Dk/r
-                            const float2 D = mul2(om, om);
-                            const float2 sw = make_float2(sign_weight(wgt, dot.x), sign_weight(wgt, dot.y));
-                            S[z] = fma2(D, sw, S[z]);
-                          }
+                            for (int m = 0; m < 4; ++m) w4[m] = dup(wzc[zr * 4 + m]);
+                            if ((offmask >> zr) & 1)
+                                zpass(IntC<1>{}, zr, w4);
+                            else
+                                zpass(IntC<0>{}, zr, w4);
                         }
                     }
                 }

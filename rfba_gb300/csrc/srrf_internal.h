@@ -73,7 +73,7 @@ struct RingPlan {
 
 // Device-side tables (one contiguous buffer), offsets in 4-byte words.
 struct TableLayout {
-    int wx, offx, wy, offy, wz, wzi, grp_xval, grp, pair_yval, pair_pt, pt_zval, pt_vec, pair_rot;
+    int wx, offx, wy, offy, wz, offz, wzi, grp_xval, grp, pair_yval, pair_pt, pt_zval, pt_vec, pair_rot;
     int words;
 };
 
@@ -86,6 +86,7 @@ struct RadParams {
     int ngroups, npairs, npoints;
     int zero_pair;        // pair index of (x=0, y=0), carries the intensity
     int gr[4];            // gradient ranges: main, x, y, z (smooth=0 => 1,0,0,0)
+    int grad_mode;        // 1: ranges (1,1,1,1), 2: (1,0,0,0), 0: generic loops
     int R;                // gradient halo
     int TY;               // subvoxel rows per tile (threads = 8 * TY)
     int NU, NV, NW;       // coarse G tile extents
@@ -112,10 +113,9 @@ struct TemporalParams {
     long long total_vox;
     int T;
     int method, itc, order, iw;
-    float* rad_stack;             // ITC=1 bins in place; rows T..T+order-1 are zero
+    float* rad_stack;             // ITC=1 bins the series in place
     const float* int_stack;
     float* out;
-    long long stack_rows;         // rows per block slice (T + padding)
 };
 
 // Launchers (radiality.cu / temporal.cu). Return a cudaError_t as int.

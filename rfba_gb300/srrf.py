@@ -197,15 +197,15 @@ def plan_info(cfg: "Config") -> dict:
 
 def flops_per_voxel_volume(cfg: "Config") -> float:
     """Flops per output voxel-volume of the separable method as implemented
-    (FMA = 2): per distinct ring point, the 5-tap z interpolation of three
-    gradient components (27) and the radiality term in the rotated frame (19);
+    (FMA = 2): per distinct ring point, the 4-tap z interpolation of three
+    gradient components (21) and the radiality term in the rotated frame (21);
     per (x, y) pair, the 4-tap y pass and the frame rotation over coarse z
     ((21 + 6) / mag_z); per x value, the 4-tap x pass (21 / (mag_y mag_z)); the
     smoothed gradient (162 / (mag_x mag_y mag_z)); the intensity interpolation
     (9) and the temporal reduction (10)."""
     info = plan_info(cfg)
     mx, my, mz = cfg.mag[0], cfg.mag[1], cfg.mag[2]
-    return (info["points"] * 46 + info["pairs"] * 27.0 / mz + info["xvalues"] * 21.0 / (my * mz)
+    return (info["points"] * 42 + info["pairs"] * 27.0 / mz + info["xvalues"] * 21.0 / (my * mz)
             + 162.0 / (mx * my * mz) + 9 + 10)
 
 
