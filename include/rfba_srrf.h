@@ -153,6 +153,22 @@ int rfba_srrf_forward_blocks_plain(rfba_ctx* ctx, const rfba_srrf_config* cfg, c
                                    const int dims[4], const rfba_block* blocks, int nblocks, float* out,
                                    int64_t out_elems);
 
+/* Whole-volume forward that allocates no device memory. No counterpart in the
+ * reference. For callers that cannot call cudaMalloc where they need a map: an
+ * acquisition loop that must not stall on cudaMalloc's device-wide
+ * synchronisation, a host whose device memory belongs to its own pool, a plugin
+ * environment that forbids device allocation. in and out are device pointers
+ * (layouts as rfba_srrf_forward); all temporaries live in one fixed 128 MiB
+ * device array inside the library, which every GPU that loads the library holds
+ * until the process exits. Volumes whose scratch (about 8 bytes per output
+ * subvoxel per time point plus small tables) exceeds it are rejected with
+ * RFBA_ERR_UNSUPPORTED and a message. The first call on a device looks the
+ * array up (cudaGetSymbolAddress) and should come before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race, so serialise
+ * them. Stream-ordered on `stream` (a cudaStream_t, NULL = legacy default). */
+int rfba_srrf_forward_static_scratch(const rfba_srrf_config* cfg, const void* in, rfba_dtype dtype,
+                                     const int dims[4], float* out, void* stream);
+
 /* Block lists. GradientCalc.cpp:47-116 (border 2, put-back into the full
  * magnified output, isotropic mag = cfg->mag[0]); returns the block count, or a
  * negative status. With blocks == NULL only counts. */
