@@ -169,6 +169,26 @@ int rfba_srrf_forward_blocks_plain(rfba_ctx* ctx, const rfba_srrf_config* cfg, c
 int rfba_srrf_forward_static_scratch(const rfba_srrf_config* cfg, const void* in, rfba_dtype dtype,
                                      const int dims[4], float* out, void* stream);
 
+/* Differentiable pair (no counterpart in the reference, which has no
+ * derivatives). Whole volume as one block, float32 device input [t][z][y][x].
+ * shifts: device T x 3 floats (x, y, z per volume) or NULL. The forward first
+ * resamples each volume at x + shifts[t] (Catmull-Rom, the reference's cubic of
+ * kernel.cu:128-138, edge clamped, one axis at a time x, y, z) and then runs the
+ * SRRF forward; out is the map as rfba_srrf_forward writes it.
+ * The backward takes dL/dmap (device, map layout; NaN map voxels get no
+ * gradient) and writes dL/din (T x D x H x W) and, if dL_dshift is not NULL,
+ * dL/dshifts (T x 3). It covers TRA (Method 1) and TRAC with
+ * Integrate_Temporal_Correlations 0, and reuses the radiality stacks of the
+ * last rfba_srrf_forward_shifted on the same context with the same
+ * configuration, input and shifts (otherwise it runs that forward itself); the
+ * interpolated gradient field is recomputed, not stored. Stream-ordered. */
+int rfba_srrf_forward_shifted(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* in, const float* shifts,
+                              const int dims[4], float* out, void* stream);
+int rfba_srrf_backward(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* in, const float* shifts,
+                       const int dims[4], const float* dL_dmap, float* dL_din, float* dL_dshift, void* stream);
+/* CUDA-event duration of the last backward (with timing enabled). */
+int rfba_ctx_last_backward_ms(rfba_ctx* ctx, double* ms);
+
 /* Block lists. GradientCalc.cpp:47-116 (border 2, put-back into the full
  * magnified output, isotropic mag = cfg->mag[0]); returns the block count, or a
  * negative status. With blocks == NULL only counts. */

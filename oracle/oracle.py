@@ -132,6 +132,9 @@ def lib():
         L.oracle_legacy_f64.argtypes = [f32p, i32p, cp, f64p]
         L.oracle_legacy_f32.argtypes = [f32p, i32p, cp, f32p]
         L.oracle_temporal_f64.argtypes = [cp, f64p, f64p, ctypes.c_int, f64p]
+        L.oracle_adjoint_f64.argtypes = [f32p, i32p, cp, f64p, f64p, f64p, f64p, f64p]
+        L.oracle_forward_shifted_f64.argtypes = [f32p, i32p, cp, f64p, f64p]
+        L.oracle_shift_f64.argtypes = [f32p, i32p, f64p, f64p]
         _lib = L
     return _lib
 
@@ -193,6 +196,58 @@ def temporal(conf: OConf, rad: np.ndarray, inten: np.ndarray) -> float:
     lib().oracle_temporal_f64(ctypes.byref(conf), _p(rad, ctypes.c_double), _p(inten, ctypes.c_double),
                               len(rad), ctypes.byref(out))
     return out.value
+
+
+def _shifts_ptr(shifts, T):
+    if shifts is None:
+        return None, None
+    s = np.ascontiguousarray(shifts, np.float64).reshape(T, 3)
+    return s, _p(s, ctypes.c_double)
+
+
+def forward_shifted(img: np.ndarray, conf: OConf, shifts=None) -> np.ndarray:
+    """FP64 map of the drift-corrected series: each volume t resampled at
+    x + shifts[t] (Catmull-Rom, edge clamp; x, y, z order) then the SRRF forward
+    over the whole block."""
+    img = np.ascontiguousarray(img, dtype=np.float32)
+    T, D, H, W = img.shape
+    dims = np.array([W, H, D, T], np.int32)
+    m = [conf.mag[i] for i in range(3)]
+    out = np.zeros((D * m[2], H * m[1], W * m[0]), np.float64)
+    s, sp = _shifts_ptr(shifts, T)
+    lib().oracle_forward_shifted_f64(_p(img, ctypes.c_float), _p(dims, ctypes.c_int), ctypes.byref(conf), sp,
+                                     _p(out, ctypes.c_double))
+    return out
+
+
+def adjoint(img: np.ndarray, conf: OConf, gmap: np.ndarray, shifts=None):
+    """FP64 forward map and the adjoint of L given dL/dmap = gmap: returns
+    (map, dL/dinput [T][D][H][W], dL/dshifts [T][3] or None)."""
+    img = np.ascontiguousarray(img, dtype=np.float32)
+    T, D, H, W = img.shape
+    dims = np.array([W, H, D, T], np.int32)
+    m = [conf.mag[i] for i in range(3)]
+    out = np.zeros((D * m[2], H * m[1], W * m[0]), np.float64)
+    g = np.ascontiguousarray(gmap, np.float64).reshape(out.shape)
+    din = np.zeros(img.shape, np.float64)
+    s, sp = _shifts_ptr(shifts, T)
+    dsh = np.zeros((T, 3), np.float64) if shifts is not None else None
+    rc = lib().oracle_adjoint_f64(_p(img, ctypes.c_float), _p(dims, ctypes.c_int), ctypes.byref(conf), sp,
+                                  _p(g, ctypes.c_double), _p(out, ctypes.c_double), _p(din, ctypes.c_double),
+                                  _p(dsh, ctypes.c_double) if dsh is not None else None)
+    if rc != 0:
+        raise ValueError("no adjoint for this temporal reduction (TRA and TRAC with ITC 0 only)")
+    return out, din, dsh
+
+
+def shift(img: np.ndarray, shifts) -> np.ndarray:
+    img = np.ascontiguousarray(img, dtype=np.float32)
+    T, D, H, W = img.shape
+    dims = np.array([W, H, D, T], np.int32)
+    out = np.zeros(img.shape, np.float64)
+    s, sp = _shifts_ptr(shifts, T)
+    lib().oracle_shift_f64(_p(img, ctypes.c_float), _p(dims, ctypes.c_int), sp, _p(out, ctypes.c_double))
+    return out
 
 
 # ---------------------------------------------------------------------------

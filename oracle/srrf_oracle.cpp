@@ -115,8 +115,8 @@ struct Field {
 
 // gradKernel (kernel.cu:44-125) on the sub-box, reading the block input with
 // clamp-to-edge of the block.
-template <class T>
-void gradient(const float* in, const int dims[4], const oconf& c, Field<T>& F) {
+template <class T, class Tin>
+void gradient(const Tin* in, const int dims[4], const oconf& c, Field<T>& F) {
     const int w = dims[0], h = dims[1], d = dims[2];
     auto I = [&](int x, int y, int z, int t) -> T {
         return (T)in[(((size_t)t * d + z) * h + y) * w + x];
@@ -459,9 +459,381 @@ void legacy(const float* in, const int dims[4], const oconf& c, T* out) {
             }
 }
 
+// ---------------------------------------------------------------------------
+// Differentiable path (FP64): drift shift, forward, and the adjoint of a scalar
+// objective L(map) with respect to the input voxels and the per-volume shifts.
+// The reference has no derivatives; this is the literal reverse of the forward
+// above, sample by sample over all n^2 ring samples and all 64 interpolation
+// taps, so it shares no factorisation with the CUDA adjoint.
+
+// d/dx of the Catmull-Rom kernel (a = 0.5).
+inline double dcubic(double xx) {
+    const double a = 0.5;
+    const double x = std::fabs(xx), s = xx < 0 ? -1.0 : 1.0;
+    if (x < 1.0) return s * (3.0 * (2.0 - a) * x * x + 2.0 * (a - 3.0) * x);
+    if (x < 2.0) return s * (-3.0 * a * x * x + 10.0 * a * x - 8.0 * a);
+    return 0.0;
+}
+
+// One axis of the drift operator: out[x] = sum_k w(x + d - i_k) in[clamp(i_k)],
+// i_k = floor(x + d) - 1 + k, w = cubic (or its derivative). With transpose,
+// accumulates the adjoint into in from out.
+void shift_axis(const double* src, double* dst, int W, int H, int D, int axis, double d, bool deriv, bool transpose) {
+    const int n = axis == 0 ? W : (axis == 1 ? H : D);
+    const size_t stride = axis == 0 ? 1 : (axis == 1 ? (size_t)W : (size_t)W * H);
+    if (transpose) std::fill(dst, dst + (size_t)W * H * D, 0.0);
+    for (int z = 0; z < D; ++z)
+        for (int y = 0; y < H; ++y)
+            for (int x = 0; x < W; ++x) {
+                const int c = axis == 0 ? x : (axis == 1 ? y : z);
+                const size_t line = (size_t)(z * H + y) * W + x - (size_t)c * stride;
+                const double pos = c + d;
+                const int base = (int)std::floor(pos);
+                double acc = 0.0;
+                for (int k = -1; k <= 2; ++k) {
+                    const int i = std::min(std::max(base + k, 0), n - 1);
+                    const double w = deriv ? dcubic(pos - (base + k)) : cubic<double>(pos - (base + k));
+                    if (transpose)
+                        dst[line + (size_t)i * stride] += w * src[line + (size_t)c * stride];
+                    else
+                        acc += w * src[line + (size_t)i * stride];
+                }
+                if (!transpose) dst[line + (size_t)c * stride] = acc;
+            }
+}
+
+// I'_t = shift along x, then y, then z (axes with deriv_axis use derivative weights).
+void shift_volume(const double* in, double* out, int W, int H, int D, const double d[3], int deriv_axis) {
+    const size_t n = (size_t)W * H * D;
+    std::vector<double> a(in, in + n), b(n);
+    for (int ax = 0; ax < 3; ++ax) {
+        shift_axis(a.data(), b.data(), W, H, D, ax, d[ax], ax == deriv_axis, false);
+        a.swap(b);
+    }
+    std::copy(a.begin(), a.end(), out);
+}
+
+void shift_volume_adjoint(const double* g, double* out, int W, int H, int D, const double d[3]) {
+    const size_t n = (size_t)W * H * D;
+    std::vector<double> a(g, g + n), b(n);
+    for (int ax = 2; ax >= 0; --ax) {
+        shift_axis(a.data(), b.data(), W, H, D, ax, d[ax], false, true);
+        a.swap(b);
+    }
+    std::copy(a.begin(), a.end(), out);
+}
+
+// Adjoint of the temporal reduction for one subvoxel: dL/drad_t and dL/dI_t
+// from dL/dmap. TRA (kernel.cu:291-327) and TRAC with ITC 0 (kernel.cu:469-507).
+bool temporal_adjoint(const oconf& c, const double* r, const double* I, int T, double g, double* gr, double* gi) {
+    for (int t = 0; t < T; ++t) gr[t] = gi[t] = 0.0;
+    const bool iw = c.intensity_w == 1;
+    if (c.method == 1) {
+        for (int t = 0; t < T; ++t) {
+            gr[t] = g * (iw ? I[t] : 1.0) / T;
+            gi[t] = iw ? g * r[t] / T : 0.0;
+        }
+        return true;
+    }
+    if (c.method != 3 || c.itc == 1) return false;
+    const int k = c.trac_order;
+    double m = 0, IW = 0;
+    for (int t = 0; t < T; ++t) {
+        m += r[t];
+        IW += r[t] * I[t];
+    }
+    m /= T;
+    IW /= T;
+    std::vector<double> a(T + 4, 0.0), dC(T + 4, 0.0);
+    for (int t = 0; t < T; ++t) a[t] = r[t] - m;
+    const int N = T - k;
+    double C = 0;
+    if (k == 2) {
+        for (int t = 0; t < N; ++t) {
+            C += a[t] * a[t + 1];
+            dC[t] += a[t + 1];
+            dC[t + 1] += a[t];
+        }
+    } else if (k == 3) {
+        for (int t = 0; t < N; ++t) {
+            C += a[t] * a[t + 1] * a[t + 2];
+            dC[t] += a[t + 1] * a[t + 2];
+            dC[t + 1] += a[t] * a[t + 2];
+            dC[t + 2] += a[t] * a[t + 1];
+        }
+    } else {
+        double S4 = 0, AB = 0, CD = 0, AC = 0, BD = 0, AD = 0, BC = 0;
+        for (int t = 0; t < N; ++t) {
+            const double A = a[t], B = a[t + 1], Cc = a[t + 2], Dd = a[t + 3];
+            S4 += A * B * Cc * Dd;
+            AB += A * B;
+            CD += Cc * Dd;
+            AC += A * Cc;
+            BD += B * Dd;
+            AD += A * Dd;
+            BC += B * Cc;
+        }
+        C = S4 - AB * CD - AC * BD - AD * BC;
+        for (int t = 0; t < N; ++t) {
+            const double A = a[t], B = a[t + 1], Cc = a[t + 2], Dd = a[t + 3];
+            // d/dA, d/dB, d/dC, d/dD of the per-t terms
+            dC[t] += B * Cc * Dd - B * CD - Cc * BD - Dd * BC;
+            dC[t + 1] += A * Cc * Dd - A * CD - Dd * AC - Cc * AD;
+            dC[t + 2] += A * B * Dd - Dd * AB - A * BD - B * AD;
+            dC[t + 3] += A * B * Cc - Cc * AB - B * AC - A * BC;
+        }
+    }
+    double mean_dC = 0;
+    for (int t = 0; t < T; ++t) mean_dC += dC[t];
+    mean_dC /= T;
+    const double sgn = C > 0 ? 1.0 : (C < 0 ? -1.0 : 0.0);
+    const double scale = iw ? IW : 1.0;
+    for (int t = 0; t < T; ++t) {
+        gr[t] = g * (sgn / T * scale * (dC[t] - mean_dC) + (iw ? std::fabs(C) / T * I[t] / T : 0.0));
+        gi[t] = iw ? g * std::fabs(C) / T * r[t] / T : 0.0;
+    }
+    return true;
+}
+
+// Forward + adjoint on one whole block. Returns false for configurations
+// without a derivative here (TRM, TRPPM, TRAC with ITC 1).
+bool objective_adjoint(const float* in, const int dims[4], const oconf& c, const double* shifts, const double* gmap,
+                       double* map_out, double* dL_din, double* dL_dshift) {
+    const int W = dims[0], H = dims[1], D = dims[2], T = dims[3];
+    const size_t nv = (size_t)W * H * D;
+    std::vector<double> Ip(nv * T);
+#pragma omp parallel for
+    for (int t = 0; t < T; ++t) {
+        std::vector<double> v(in + (size_t)t * nv, in + (size_t)t * nv + nv);
+        if (shifts)
+            shift_volume(v.data(), Ip.data() + (size_t)t * nv, W, H, D, shifts + 3 * t, -1);
+        else
+            std::copy(v.begin(), v.end(), Ip.begin() + (size_t)t * nv);
+    }
+    Ring R;
+    R.n = 2 * c.axes_in_ring;
+    R.x.resize(R.n * R.n);
+    R.y.resize(R.n * R.n);
+    R.z.resize(R.n * R.n);
+    build_ring(c.ring_radius, R.n, R.x.data(), R.y.data(), R.z.data());
+    Field<double> F;
+    F.nt = T;
+    for (int a = 0; a < 3; ++a) {
+        F.dim[a] = dims[a];
+        F.c0[a] = 0;
+        F.c1[a] = dims[a];
+        F.n[a] = dims[a];
+    }
+    gradient<double>(Ip.data(), dims, c, F);
+    const int mx = c.mag[0], my = c.mag[1], mz = c.mag[2];
+    const int FX = W * mx, FY = H * my, FZ = D * mz;
+    const size_t nfine = (size_t)FX * FY * FZ;
+    std::vector<double> rad(nfine * T), inten(nfine * T), gS(nfine * T), gI(nfine * T);
+    std::vector<char> valid(nfine, 1);
+#pragma omp parallel
+    {
+        std::vector<double> rr(T + 8), ii(T + 8), gr(T), gi(T);
+#pragma omp for schedule(dynamic, 8)
+        for (long long v = 0; v < (long long)nfine; ++v) {
+            const int X = (int)(v % FX), Y = (int)((v / FX) % FY), Z = (int)(v / ((size_t)FX * FY));
+            std::fill(rr.begin(), rr.end(), 0.0);
+            for (int t = 0; t < T; ++t) {
+                rr[t] = radiality<double>(F, R, c, X, Y, Z, t);
+                ii[t] = intensity<double>(F, c, X, Y, Z, t);
+                rad[(size_t)t * nfine + v] = rr[t];
+                inten[(size_t)t * nfine + v] = ii[t];
+            }
+            std::vector<double> rcopy(rr);
+            const double mv = temporal<double>(c, rcopy.data(), ii.data(), T);
+            map_out[v] = mv;
+            const bool ok = std::isfinite(mv) && std::isfinite(gmap[v]);
+            valid[v] = ok;
+            if (ok) temporal_adjoint(c, rr.data(), ii.data(), T, gmap[v], gr.data(), gi.data());
+            for (int t = 0; t < T; ++t) {
+                double gs = ok ? gr[t] : 0.0;
+                if (c.renormalize == 1) gs *= 0.5;
+                if (c.remove_con == 1 && !(rr[t] > 0)) gs = 0.0;
+                gS[(size_t)t * nfine + v] = gs;
+                gI[(size_t)t * nfine + v] = (ok && ii[t] > 0) ? gi[t] : 0.0;
+            }
+        }
+    }
+    // radiality and intensity adjoint per time point
+    const double r = c.ring_radius;
+    const int n = R.n;
+    std::vector<double> dIp(nv * T, 0.0);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int t = 0; t < T; ++t) {
+        std::vector<double> dG[3] = {std::vector<double>(nv, 0.0), std::vector<double>(nv, 0.0),
+                                     std::vector<double>(nv, 0.0)};
+        double* dI = dIp.data() + (size_t)t * nv;
+        auto taps = [&](double qx, double qy, double qz, auto&& fn) {
+            const int u0 = (int)std::floor(qx - 0.5), v0 = (int)std::floor(qy - 0.5), w0 = (int)std::floor(qz - 0.5);
+            for (int k = 0; k <= 3; ++k)
+                for (int j = 0; j <= 3; ++j)
+                    for (int i = 0; i <= 3; ++i) {
+                        const int u = u0 - 1 + i, vv = v0 - 1 + j, w = w0 - 1 + k;
+                        const double wt = cubic<double>(qx - (u + 0.5)) * cubic<double>(qy - (vv + 0.5)) *
+                                          cubic<double>(qz - (w + 0.5));
+                        fn((size_t)(clampi(w, 0, D - 1) * H + clampi(vv, 0, H - 1)) * W + clampi(u, 0, W - 1), wt);
+                    }
+        };
+        for (long long v = 0; v < (long long)nfine; ++v) {
+            const double gs = gS[(size_t)t * nfine + v];
+            const double gi = gI[(size_t)t * nfine + v];
+            if (!valid[v] || (gs == 0.0 && gi == 0.0)) continue;
+            const int X = (int)(v % FX), Y = (int)((v / FX) % FY), Z = (int)(v / ((size_t)FX * FY));
+            const double Xc = X + 0.5, Yc = Y + 0.5, Zc = Z + 0.5;
+            if (gi != 0.0) taps(Xc / mx, Yc / my, Zc / mz, [&](size_t o, double wt) { dI[o] += gi * wt; });
+            if (gs == 0.0) continue;
+            for (int id = 0; id < n * n; ++id) {
+                const double rx = R.x[id], ry = R.y[id], rz = R.z[id];
+                const double qx = (Xc + rx) / mx, qy = (Yc + ry) / my, qz = (Zc + rz) / mz;
+                double G[3] = {0, 0, 0};
+                const size_t tofs = (size_t)t * nv;
+                taps(qx, qy, qz, [&](size_t o, double wt) {
+                    G[0] += wt * F.g[0][tofs + o];
+                    G[1] += wt * F.g[1][tofs + o];
+                    G[2] += wt * F.g[2][tofs + o];
+                });
+                const double G2 = G[0] * G[0] + G[1] * G[1] + G[2] * G[2];
+                const double GdotR = (G[0] * rx + G[1] * ry + G[2] * rz) / (std::sqrt(G2) * r);
+                const double sigma = (GdotR > 0 || GdotR != GdotR) ? -1.0 : 1.0;
+                const double tt = (G[0] * rx + G[1] * ry + G[2] * rz) / G2;
+                const double vv[3] = {rx - G[0] * tt, ry - G[1] * tt, rz - G[2] * tt};
+                const double Dk = std::sqrt(vv[0] * vv[0] + vv[1] * vv[1] + vv[2] * vv[2]);
+                if (!(Dk > 0)) continue;
+                // S = sum sigma (1 - Dk/r)^2 / n; dDk/dG = -(tt/Dk) v since v is perpendicular to G
+                const double coef = gs * sigma / n * 2.0 * (1.0 - Dk / r) * (-1.0 / r) * (-tt / Dk);
+                const double dg[3] = {coef * vv[0], coef * vv[1], coef * vv[2]};
+                taps(qx, qy, qz, [&](size_t o, double wt) {
+                    dG[0][o] += wt * dg[0];
+                    dG[1][o] += wt * dg[1];
+                    dG[2][o] += wt * dg[2];
+                });
+            }
+        }
+        // transpose of the gradient stencil with block-edge clamping
+        int mR = c.main_range, xR = c.x_range, yR = c.y_range, zR = c.z_range;
+        if (c.gradient_smooth == 0) {
+            mR = 1;
+            xR = yR = zR = 0;
+        }
+        for (int z = 0; z < D; ++z)
+            for (int y = 0; y < H; ++y)
+                for (int x = 0; x < W; ++x) {
+                    const size_t o = (size_t)(z * H + y) * W + x;
+                    auto P = [&](int dx, int dy, int dz) {
+                        return (size_t)(clampi(z + dz, 0, D - 1) * H + clampi(y + dy, 0, H - 1)) * W +
+                               clampi(x + dx, 0, W - 1);
+                    };
+                    for (int i = -mR; i <= mR; ++i)
+                        for (int j = -yR; j <= yR; ++j)
+                            for (int k = -zR; k <= zR; ++k)
+                                if (i) dI[P(i, j, k)] += (i > 0 ? 1.0 : -1.0) * dG[0][o];
+                    for (int j = -mR; j <= mR; ++j)
+                        for (int i = -xR; i <= xR; ++i)
+                            for (int k = -zR; k <= zR; ++k)
+                                if (j) dI[P(i, j, k)] += (j > 0 ? 1.0 : -1.0) * dG[1][o];
+                    for (int k = -mR; k <= mR; ++k)
+                        for (int i = -xR; i <= xR; ++i)
+                            for (int j = -yR; j <= yR; ++j)
+                                if (k) dI[P(i, j, k)] += (k > 0 ? 1.0 : -1.0) * dG[2][o];
+                }
+    }
+    // through the drift operator
+#pragma omp parallel for
+    for (int t = 0; t < T; ++t) {
+        const double* g = dIp.data() + (size_t)t * nv;
+        if (!shifts) {
+            std::copy(g, g + nv, dL_din + (size_t)t * nv);
+            continue;
+        }
+        shift_volume_adjoint(g, dL_din + (size_t)t * nv, W, H, D, shifts + 3 * t);
+        if (dL_dshift) {
+            std::vector<double> v(in + (size_t)t * nv, in + (size_t)t * nv + nv), dv(nv);
+            for (int ax = 0; ax < 3; ++ax) {
+                shift_volume(v.data(), dv.data(), W, H, D, shifts + 3 * t, ax);
+                double s = 0;
+                for (size_t i = 0; i < nv; ++i) s += g[i] * dv[i];
+                dL_dshift[3 * t + ax] = s;
+            }
+        }
+    }
+    return true;
+}
+
 }  // namespace
 
 extern "C" {
+
+// Forward map and adjoint of L with dL/dmap = gmap (whole block). shifts (T x 3,
+// x y z) may be NULL (no drift operator). Returns -2 for reductions without a
+// derivative here.
+int oracle_adjoint_f64(const float* in, const int* dims, const oconf* c, const double* shifts, const double* gmap,
+                       double* map_out, double* dL_din, double* dL_dshift) {
+    return objective_adjoint(in, dims, *c, shifts, gmap, map_out, dL_din, dL_dshift) ? 0 : -2;
+}
+
+// Forward map of the shifted input (FP64), for finite differences.
+int oracle_forward_shifted_f64(const float* in, const int* dims, const oconf* c, const double* shifts,
+                               double* map_out) {
+    const int W = dims[0], H = dims[1], D = dims[2], T = dims[3];
+    const size_t nv = (size_t)W * H * D;
+    std::vector<double> Ip(nv * T);
+#pragma omp parallel for
+    for (int t = 0; t < T; ++t) {
+        std::vector<double> v(in + (size_t)t * nv, in + (size_t)t * nv + nv);
+        if (shifts)
+            shift_volume(v.data(), Ip.data() + (size_t)t * nv, W, H, D, shifts + 3 * t, -1);
+        else
+            std::copy(v.begin(), v.end(), Ip.begin() + (size_t)t * nv);
+    }
+    Ring R;
+    R.n = 2 * c->axes_in_ring;
+    R.x.resize(R.n * R.n);
+    R.y.resize(R.n * R.n);
+    R.z.resize(R.n * R.n);
+    build_ring(c->ring_radius, R.n, R.x.data(), R.y.data(), R.z.data());
+    Field<double> F;
+    F.nt = T;
+    for (int a = 0; a < 3; ++a) {
+        F.dim[a] = dims[a];
+        F.c0[a] = 0;
+        F.c1[a] = dims[a];
+        F.n[a] = dims[a];
+    }
+    gradient<double>(Ip.data(), dims, *c, F);
+    const int FX = W * c->mag[0], FY = H * c->mag[1], FZ = D * c->mag[2];
+    const size_t nfine = (size_t)FX * FY * FZ;
+#pragma omp parallel
+    {
+        std::vector<double> rr(T + 8), ii(T + 8);
+#pragma omp for schedule(dynamic, 8)
+        for (long long v = 0; v < (long long)nfine; ++v) {
+            const int X = (int)(v % FX), Y = (int)((v / FX) % FY), Z = (int)(v / ((size_t)FX * FY));
+            std::fill(rr.begin(), rr.end(), 0.0);
+            for (int t = 0; t < T; ++t) {
+                rr[t] = radiality<double>(F, R, *c, X, Y, Z, t);
+                ii[t] = intensity<double>(F, *c, X, Y, Z, t);
+            }
+            map_out[v] = temporal<double>(*c, rr.data(), ii.data(), T);
+        }
+    }
+    return 0;
+}
+
+// The drift operator alone (FP64), for tests of the CUDA resampling.
+int oracle_shift_f64(const float* in, const int* dims, const double* shifts, double* out) {
+    const int W = dims[0], H = dims[1], D = dims[2], T = dims[3];
+    const size_t nv = (size_t)W * H * D;
+#pragma omp parallel for
+    for (int t = 0; t < T; ++t) {
+        std::vector<double> v(in + (size_t)t * nv, in + (size_t)t * nv + nv);
+        shift_volume(v.data(), out + (size_t)t * nv, W, H, D, shifts + 3 * t, -1);
+    }
+    return 0;
+}
 
 int oracle_ring_f32(float r, int axes, float* x, float* y, float* z) {
     build_ring(r, 2 * axes, x, y, z);

@@ -1,0 +1,728 @@
+// Differentiable SRRF path (sm_103a): drift resampling, and the adjoint of a
+// scalar objective on the map with respect to the input voxels and the
+// per-volume drift shifts. The reference has no derivatives; the forward it
+// differentiates is the reference's radiality (kernel.cu:44-287) and temporal
+// reduction (TRA kernel.cu:291-327, TRAC with ITC 0 kernel.cu:469-507) on
+// volumes resampled by the drift operator
+//     I'_t(x) = sum_{i,j,k} c(x + d_x - i) c(y + d_y - j) c(z + d_z - k) I_t[clamp(i, j, k)],
+// c = the reference's Catmull-Rom kernel (kernel.cu:128-138), applied one axis
+// at a time (x, then y, then z).
+//
+// Backward, per call:
+//   1. temporal adjoint, one thread per subvoxel: dL/drad_t and dL/dI_t from
+//      dL/dmap and the stored radiality/intensity stacks;
+//   2. radiality adjoint, persistent over (tile, time) like the forward: the
+//      interpolated gradient at every ring sample is recomputed (not stored),
+//      the derivative of the radiality term is pushed back through the z pass
+//      (registers), the frame rotation, the y pass (shared-memory atomics), the
+//      x pass (shared-memory atomics) and the gradient stencil (gather), and the
+//      tile's contribution to dL/dI' is added to global memory;
+//   3. the drift operator's transpose gives dL/dI, and dL/dd_t is the sum over
+//      the volume of dL/dI'_t times the resampling with derivative weights on
+//      one axis.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cstdint>
+
+#include "srrf_internal.h"
+
+namespace rfba {
+namespace {
+
+__device__ __forceinline__ float rsqrt_approx(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float sign_weight(float w, float d) {
+    return __int_as_float(__float_as_int(w) | (~__float_as_int(d) & 0x80000000));
+}
+__device__ __forceinline__ float2 dup(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+__device__ __forceinline__ int floordiv(int a, int b) {
+    int q = a / b;
+    return (a % b != 0 && a < 0) ? q - 1 : q;
+}
+template <int V>
+struct IntC {
+    static constexpr int value = V;
+};
+
+// Catmull-Rom kernel and its derivative (a = 0.5), kernel.cu:128-138.
+__device__ __forceinline__ float cr(float xx) {
+    const float a = 0.5f;
+    const float x = fabsf(xx);
+    if (x < 1.f) return x * x * (x * (2.f - a) + (a - 3.f)) + 1.f;
+    if (x < 2.f) return ((-a * x + 5.f * a) * x - 8.f * a) * x + 4.f * a;
+    return 0.f;
+}
+__device__ __forceinline__ float dcr(float xx) {
+    const float a = 0.5f;
+    const float x = fabsf(xx), s = xx < 0.f ? -1.f : 1.f;
+    if (x < 1.f) return s * (3.f * (2.f - a) * x * x + 2.f * (a - 3.f) * x);
+    if (x < 2.f) return s * ((-3.f * a * x + 10.f * a) * x - 8.f * a);
+    return 0.f;
+}
+
+// ---------------------------------------------------------------------------
+// Drift operator, one axis: mode 0 resamples, mode 1 resamples with derivative
+// weights, mode 2 applies the transpose (gather over the outputs whose clamped
+// taps hit each input position).
+__global__ void shift_axis_kernel(const float* __restrict__ src, float* __restrict__ dst, int W, int H, int D, int T,
+                                  int axis, const float* __restrict__ shifts, int mode) {
+    const long long n = (long long)W * H * D * T;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % W);
+        const int y = (int)((i / W) % H);
+        const int z = (int)((i / ((long long)W * H)) % D);
+        const int t = (int)(i / ((long long)W * H * D));
+        const int len = axis == 0 ? W : (axis == 1 ? H : D);
+        const long long stride = axis == 0 ? 1 : (axis == 1 ? W : (long long)W * H);
+        const int c = axis == 0 ? x : (axis == 1 ? y : z);
+        const long long line = i - (long long)c * stride;
+        const float d = shifts[3 * t + axis];
+        float acc = 0.f;
+        if (mode != 2) {
+            const float pos = (float)c + d;
+            const int base = (int)floorf(pos);
+#pragma unroll
+            for (int k = -1; k <= 2; ++k) {
+                const int ii = clampi(base + k, 0, len - 1);
+                const float u = pos - (float)(base + k);
+                acc = fmaf(mode == 1 ? dcr(u) : cr(u), src[line + ii * stride], acc);
+            }
+        } else {
+            // outputs x whose taps floor(x + d) - 1 .. + 2, clamped, include c
+            int lo = (int)floorf((float)c - d) - 3, hi = (int)ceilf((float)c - d) + 3;
+            if (c == 0) lo = -1000000;
+            if (c == len - 1) hi = 1000000;
+            lo = max(lo, 0);
+            hi = min(hi, len - 1);
+            for (int xo = lo; xo <= hi; ++xo) {
+                const float pos = (float)xo + d;
+                const int base = (int)floorf(pos);
+                float w = 0.f;
+#pragma unroll
+                for (int k = -1; k <= 2; ++k)
+                    if (clampi(base + k, 0, len - 1) == c) w += cr(pos - (float)(base + k));
+                if (w != 0.f) acc = fmaf(w, src[line + xo * stride], acc);
+            }
+        }
+        dst[i] = acc;
+    }
+}
+
+// dL/dd[t][axis] = sum over volume t of g[t] * dv[t] (double accumulation).
+__global__ void drift_dot_kernel(const float* __restrict__ g, const float* __restrict__ dv, long long nv, int axis,
+                                 double* __restrict__ out) {
+    const int t = blockIdx.y;
+    const float* gt = g + (long long)t * nv;
+    const float* dt = dv + (long long)t * nv;
+    double acc = 0.0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += (long long)gridDim.x * blockDim.x)
+        acc += (double)gt[i] * (double)dt[i];
+    __shared__ double red[256];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) atomicAdd(out + 3 * t + axis, red[0]);
+}
+
+// ---------------------------------------------------------------------------
+// Temporal adjoint, one thread per subvoxel of the single block.
+__global__ void temporal_adjoint_kernel(const BlockDev* __restrict__ blocks, const float* __restrict__ rad,
+                                        const float* __restrict__ inten, const float* __restrict__ gmap, int T,
+                                        int method, int order, int iw, int renorm, int poscon,
+                                        float* __restrict__ gS, float* __restrict__ gI) {
+    const BlockDev& B = blocks[0];
+    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= B.vox) return;
+    const long long V = B.vox;
+    const long long nx = B.nreg[0], ny = B.nreg[1];
+    const long long x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
+    const float g = gmap[B.out_offset + x * B.out_stride[0] + y * B.out_stride[1] + z * B.out_stride[2]];
+    const float* r = rad + v;
+    const float* I = inten + v;
+    // first pass: sums
+    double m = 0.0, IW = 0.0;
+    bool finite = isfinite(g);
+    for (int t = 0; t < T; ++t) {
+        const float rv = r[t * V];
+        finite = finite && isfinite(rv);
+        m += rv;
+        IW += (double)rv * I[t * V];
+    }
+    if (!finite) {
+        for (int t = 0; t < T; ++t) {
+            gS[t * V + v] = 0.f;
+            gI[t * V + v] = 0.f;
+        }
+        return;
+    }
+    m /= T;
+    IW /= T;
+    const double scale_iw = iw ? IW : 1.0;
+    double C = 0.0, AB = 0, CD = 0, AC = 0, BD = 0, AD = 0, BC = 0, S4 = 0;
+    const int N = T - order;
+    if (method == 3) {
+        for (int t = 0; t < N; ++t) {
+            const double A = r[t * V] - m, Bv = r[(t + 1) * V] - m;
+            if (order == 2) C += A * Bv;
+            if (order >= 3) {
+                const double Cv = r[(t + 2) * V] - m;
+                if (order == 3) C += A * Bv * Cv;
+                if (order == 4) {
+                    const double Dv = r[(t + 3) * V] - m;
+                    S4 += A * Bv * Cv * Dv;
+                    AB += A * Bv;
+                    CD += Cv * Dv;
+                    AC += A * Cv;
+                    BD += Bv * Dv;
+                    AD += A * Dv;
+                    BC += Bv * Cv;
+                }
+            }
+        }
+        if (order == 4) C = S4 - AB * CD - AC * BD - AD * BC;
+    }
+    // dC/da_s for every s, then centring (dC/dr_t = dC/da_t - mean_s dC/da_s)
+    auto dCda = [&](int s) -> double {
+        double d = 0.0;
+        auto a = [&](int t) -> double { return (t >= 0 && t < T) ? (double)r[t * V] - m : 0.0; };
+        for (int l = 0; l < order; ++l) {
+            const int t0 = s - l;  // the product starting at t0 contains a_s at lag l
+            if (t0 < 0 || t0 >= N) continue;
+            if (order == 2) d += a(t0 + 1 - l);
+            else if (order == 3) {
+                double p = 1.0;
+                for (int q = 0; q < 3; ++q)
+                    if (q != l) p *= a(t0 + q);
+                d += p;
+            } else {
+                const double A = a(t0), Bv = a(t0 + 1), Cv = a(t0 + 2), Dv = a(t0 + 3);
+                if (l == 0) d += Bv * Cv * Dv - Bv * CD - Cv * BD - Dv * BC;
+                if (l == 1) d += A * Cv * Dv - A * CD - Dv * AC - Cv * AD;
+                if (l == 2) d += A * Bv * Dv - Dv * AB - A * BD - Bv * AD;
+                if (l == 3) d += A * Bv * Cv - Cv * AB - Bv * AC - A * BC;
+            }
+        }
+        return d;
+    };
+    double mean_d = 0.0;
+    if (method == 3)
+        for (int s = 0; s < T; ++s) mean_d += dCda(s);
+    mean_d /= T;
+    const double sgn = C > 0 ? 1.0 : (C < 0 ? -1.0 : 0.0);
+    for (int t = 0; t < T; ++t) {
+        const float rv = r[t * V], Iv = I[t * V];
+        double gr, gi;
+        if (method == 1) {
+            gr = g * (iw ? Iv : 1.f) / T;
+            gi = iw ? g * rv / T : 0.0;
+        } else {
+            gr = g * (sgn / T * scale_iw * (dCda(t) - mean_d) + (iw ? fabs(C) / T * Iv / T : 0.0));
+            gi = iw ? g * fabs(C) / T * rv / T : 0.0;
+        }
+        if (renorm) gr *= 0.5;
+        if (poscon && !(rv > 0.f)) gr = 0.0;
+        gS[t * V + v] = (float)gr;
+        gI[t * V + v] = Iv > 0.f ? (float)gi : 0.f;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Radiality adjoint.
+template <int MR, int XR, int YR, int ZR>
+__device__ __forceinline__ float4 gradient_fixed(const float* base, int NIX, int NIY) {
+    auto I = [&](int dx, int dy, int dz) { return base[(dz * NIY + dy) * NIX + dx]; };
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+#pragma unroll
+    for (int i = 1; i <= MR; ++i)
+#pragma unroll
+        for (int j = -YR; j <= YR; ++j)
+#pragma unroll
+            for (int k = -ZR; k <= ZR; ++k) gx += I(i, j, k) - I(-i, j, k);
+#pragma unroll
+    for (int j = 1; j <= MR; ++j)
+#pragma unroll
+        for (int i = -XR; i <= XR; ++i)
+#pragma unroll
+            for (int k = -ZR; k <= ZR; ++k) gy += I(i, j, k) - I(i, -j, k);
+#pragma unroll
+    for (int k = 1; k <= MR; ++k)
+#pragma unroll
+        for (int i = -XR; i <= XR; ++i)
+#pragma unroll
+            for (int j = -YR; j <= YR; ++j) gz += I(i, j, k) - I(i, j, -k);
+    return make_float4(gx, gy, gz, I(0, 0, 0));
+}
+
+__device__ __forceinline__ float4 gradient_generic(const float* base, int NIX, int NIY, const int gr[4]) {
+    auto I = [&](int dx, int dy, int dz) { return base[(dz * NIY + dy) * NIX + dx]; };
+    const int mR = gr[0], xR = gr[1], yR = gr[2], zR = gr[3];
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+    for (int i = 1; i <= mR; ++i)
+        for (int j = -yR; j <= yR; ++j)
+            for (int k = -zR; k <= zR; ++k) gx += I(i, j, k) - I(-i, j, k);
+    for (int j = 1; j <= mR; ++j)
+        for (int i = -xR; i <= xR; ++i)
+            for (int k = -zR; k <= zR; ++k) gy += I(i, j, k) - I(i, -j, k);
+    for (int k = 1; k <= mR; ++k)
+        for (int i = -xR; i <= xR; ++i)
+            for (int j = -yR; j <= yR; ++j) gz += I(i, j, k) - I(i, j, -k);
+    return make_float4(gx, gy, gz, I(0, 0, 0));
+}
+
+template <int MZ, int CZ>
+__global__ void __launch_bounds__(128, 2) radiality_adjoint_kernel(const RadParams p, const AdjParams a) {
+    constexpr int FZ = MZ * CZ;
+    constexpr int NW = CZ + 4;
+    extern __shared__ float4 smem4[];
+    const int NU = p.NU, NV = p.NV;
+    float4* gt = smem4;                       // forward G + I   [NW][NV][NU]
+    float4* ggt = gt + NU * NV * NW;          // dL/d(G, I)      [NW][NV][NU]
+    float4* ut = ggt + NU * NV * NW;          // forward U       [NW][NV][16]
+    float4* gut = ut + kTileX * NV * NW;      // dL/dU           [NW][NV][16]
+    float* inp = reinterpret_cast<float*>(gut + kTileX * NV * NW);
+    float* tab = inp + ((p.NIX * p.NIY * p.NIZ + 3) & ~3);
+    __shared__ unsigned int s_item;
+
+    const int nthr = blockDim.x;
+    const int tid = threadIdx.x;
+    const int mx = p.mag[0], my = p.mag[1];
+    const int xf = tid & (kTileX - 1);
+    const int q = tid / kTileX;
+    const int yfa = (q / my) * (2 * my) + (q % my);
+
+    for (int i = tid; i < p.smem_table_words; i += nthr) tab[i] = p.tables[i];
+    const float* wx = tab + p.tl.wx;
+    const int* offx = reinterpret_cast<const int*>(tab + p.tl.offx);
+    const float* wy = tab + p.tl.wy;
+    const int* offy = reinterpret_cast<const int*>(tab + p.tl.offy);
+    const float* wz = tab + p.tl.wz;
+    const int* offz = reinterpret_cast<const int*>(tab + p.tl.offz);
+    const float* wzi = tab + p.tl.wzi;
+    const int* grp_xval = reinterpret_cast<const int*>(tab + p.tl.grp_xval);
+    const int* grp = reinterpret_cast<const int*>(tab + p.tl.grp);
+    const int* pair_yval = reinterpret_cast<const int*>(tab + p.tl.pair_yval);
+    const int* pair_pt = reinterpret_cast<const int*>(tab + p.tl.pair_pt);
+    const int* pt_zval = reinterpret_cast<const int*>(tab + p.tl.pt_zval);
+    const float4* pt_vec = reinterpret_cast<const float4*>(tab + p.tl.pt_vec);
+    const float2* pair_rot = reinterpret_cast<const float2*>(tab + p.tl.pair_rot);
+
+    const float* in = static_cast<const float*>(p.in);
+    const int NIX = p.NIX, NIY = p.NIY, NIZ = p.NIZ, R = p.R;
+    const int nin = NIX * NIY * NIZ;
+    const int ncell = NU * NV * NW;
+    const int nut = kTileX * NV * NW;
+
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) s_item = atomicAdd(p.work_counter, 1u);
+        __syncthreads();
+        const long long item = s_item;
+        if (item >= p.nitems) break;
+        const int tile_i = (int)(item % p.ntiles);
+        const int chunk = (int)(item / p.ntiles);
+        const TileDesc td = p.tiles[tile_i];
+        const BlockDev& B = p.blocks[td.block];
+        const int bw = B.size[0], bh = B.size[1], bd = B.size[2];
+        const int X0 = B.lo[0] + td.tx * kTileX;
+        const int Y0 = B.lo[1] + td.ty * p.TY;
+        const int Z0 = B.zbase + td.tz * FZ;
+        const int cx0 = floordiv(X0, mx) - 2;
+        const int cy0 = floordiv(Y0, my) - 2;
+        const int cz0 = Z0 / MZ - 2;
+        const int X = X0 + xf;
+        const int Ya = Y0 + yfa, Yb = Ya + my;
+        const int xi = floordiv(X, mx), xr = X - xi * mx;
+        const int yi = floordiv(Ya, my), yr = Ya - yi * my;
+        const bool xin = X < B.hi[0];
+        const bool ina = xin && Ya < B.hi[1];
+        const bool inb = xin && Yb < B.hi[1];
+        const long long V = B.vox;
+        const long long va = ((long long)(Ya - B.lo[1])) * B.nreg[0] + (X - B.lo[0]);
+        const long long vb = ((long long)(Yb - B.lo[1])) * B.nreg[0] + (X - B.lo[0]);
+        const long long zstride = (long long)B.nreg[0] * B.nreg[1];
+        const int t0 = chunk * p.t_chunk;
+        const int t1 = min(p.T, t0 + p.t_chunk);
+        for (int t = t0; t < t1; ++t) {
+            const long long sbase = B.stack_off + (long long)t * V;
+            const long long tbase = (long long)t * p.D * p.H * p.W;
+            // forward: input tile, gradient cells; clear the adjoint cells
+            for (int r = tid / kTileX; r < NIY * NIZ; r += nthr / kTileX) {
+                const int iy = r % NIY, iz = r / NIY;
+                const int by = clampi(cy0 - R + iy, 0, bh - 1);
+                const int bz = clampi(cz0 - R + iz, 0, bd - 1);
+                const long long rowg = tbase + ((long long)(B.origin[2] + bz) * p.H + (B.origin[1] + by)) * p.W +
+                                       B.origin[0];
+                for (int ix = xf; ix < NIX; ix += kTileX)
+                    inp[r * NIX + ix] = __ldg(in + rowg + clampi(cx0 - R + ix, 0, bw - 1));
+            }
+            __syncthreads();
+            for (int c = tid; c < ncell; c += nthr) {
+                const int u = c % NU;
+                const int v = (c / NU) % NV;
+                const int w = c / (NU * NV);
+                const int cu = cx0 + u, cv = cy0 + v, cw = cz0 + w;
+                float4 g4 = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (cu >= 0 && cu < bw && cv >= 0 && cv < bh && cw >= 0 && cw < bd) {
+                    const float* base = inp + ((w + R) * NIY + (v + R)) * NIX + (u + R);
+                    if (p.grad_mode == 1)
+                        g4 = gradient_fixed<1, 1, 1, 1>(base, NIX, NIY);
+                    else if (p.grad_mode == 2)
+                        g4 = gradient_fixed<1, 0, 0, 0>(base, NIX, NIY);
+                    else
+                        g4 = gradient_generic(base, NIX, NIY, p.gr);
+                }
+                gt[c] = g4;
+                ggt[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            // dL/dS and dL/dI of this thread's subvoxels
+            float2 gS[FZ], gI[FZ];
+#pragma unroll
+            for (int z = 0; z < FZ; ++z) {
+                const int Z = Z0 + z;
+                const bool zin = Z >= B.lo[2] && Z < B.hi[2];
+                const long long zo = sbase + (long long)(Z - B.lo[2]) * zstride;
+                gS[z].x = (zin && ina) ? a.gS[zo + va] : 0.f;
+                gS[z].y = (zin && inb) ? a.gS[zo + vb] : 0.f;
+                gI[z].x = (zin && ina) ? a.gI[zo + va] : 0.f;
+                gI[z].y = (zin && inb) ? a.gI[zo + vb] : 0.f;
+            }
+
+            for (int gi_ = 0; gi_ < p.ngroups; ++gi_) {
+                __syncthreads();
+                const int av = grp_xval[gi_];
+                const int ox = offx[av * mx + xr];
+                const float4 wxv = *reinterpret_cast<const float4*>(wx + (av * mx + xr) * 4);
+                const int ub = xi - cx0 - 2 + ox;
+                for (int e = tid; e < nut; e += nthr) {
+                    const int vw = e / kTileX;
+                    const float4* src = gt + vw * NU + ub;
+                    const float4 g0 = src[0], g1 = src[1], g2 = src[2], g3 = src[3];
+                    float4 r;
+                    r.x = fmaf(wxv.w, g3.x, fmaf(wxv.z, g2.x, fmaf(wxv.y, g1.x, wxv.x * g0.x)));
+                    r.y = fmaf(wxv.w, g3.y, fmaf(wxv.z, g2.y, fmaf(wxv.y, g1.y, wxv.x * g0.y)));
+                    r.z = fmaf(wxv.w, g3.z, fmaf(wxv.z, g2.z, fmaf(wxv.y, g1.z, wxv.x * g0.z)));
+                    r.w = 0.f;
+                    ut[e] = r;
+                    gut[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+                __syncthreads();
+                for (int pi = grp[gi_]; pi < grp[gi_ + 1]; ++pi) {
+                    const int b = pair_yval[pi];
+                    const int oy = offy[b * my + yr];
+                    const float4 wyv = *reinterpret_cast<const float4*>(wy + (b * my + yr) * 4);
+                    const int vbase = yi - cy0 - 2 + oy;
+                    float2 Tx[NW], Ty[NW], Tz[NW];
+#pragma unroll
+                    for (int w = 0; w < NW; ++w) {
+                        const float4* src = ut + (w * NV + vbase) * kTileX + xf;
+                        const float4 u0 = src[0], u1 = src[kTileX], u2 = src[2 * kTileX], u3 = src[3 * kTileX],
+                                     u4 = src[4 * kTileX];
+                        Tx[w].x = fmaf(wyv.w, u3.x, fmaf(wyv.z, u2.x, fmaf(wyv.y, u1.x, wyv.x * u0.x)));
+                        Ty[w].x = fmaf(wyv.w, u3.y, fmaf(wyv.z, u2.y, fmaf(wyv.y, u1.y, wyv.x * u0.y)));
+                        Tz[w].x = fmaf(wyv.w, u3.z, fmaf(wyv.z, u2.z, fmaf(wyv.y, u1.z, wyv.x * u0.z)));
+                        Tx[w].y = fmaf(wyv.w, u4.x, fmaf(wyv.z, u3.x, fmaf(wyv.y, u2.x, wyv.x * u1.x)));
+                        Ty[w].y = fmaf(wyv.w, u4.y, fmaf(wyv.z, u3.y, fmaf(wyv.y, u2.y, wyv.x * u1.y)));
+                        Tz[w].y = fmaf(wyv.w, u4.z, fmaf(wyv.z, u3.z, fmaf(wyv.y, u2.z, wyv.x * u1.z)));
+                    }
+                    const float2 rot = pair_rot[pi];
+                    const float2 ca = dup(rot.x), sb = dup(rot.y), nsb = dup(-rot.y);
+#pragma unroll
+                    for (int w = 0; w < NW; ++w) {
+                        const float2 gx = Tx[w], gy = Ty[w];
+                        Tx[w] = fma2(gy, sb, mul2(gx, ca));   // P
+                        Ty[w] = fma2(gy, ca, mul2(gx, nsb));  // E
+                    }
+                    float2 gP[NW], gE[NW], gZ[NW];
+#pragma unroll
+                    for (int w = 0; w < NW; ++w) gP[w] = gE[w] = gZ[w] = make_float2(0.f, 0.f);
+                    for (int qi = pair_pt[pi]; qi < pair_pt[pi + 1]; ++qi) {
+                        const float4 pv = pt_vec[qi];
+                        const float2 hh = dup(pv.x), cc = dup(pv.y), ncc = dup(-pv.y);
+                        const float wgt = pv.z;
+                        const float2 nun = dup(pv.w);  // -|u|
+                        const int zc = pt_zval[qi];
+                        const float* wzc = wz + zc * (MZ * 4);
+                        const int offmask = offz[zc];
+                        auto zpass = [&](auto OFF, int zr, const float2 (&w4)[4]) {
+                            constexpr int o = decltype(OFF)::value;
+#pragma unroll
+                            for (int zi = 0; zi < CZ; ++zi) {
+                                const int z = zi * MZ + zr;
+                                float2 gx = mul2(w4[0], Tx[zi + o]);
+                                float2 gy = mul2(w4[0], Ty[zi + o]);
+                                float2 gz = mul2(w4[0], Tz[zi + o]);
+#pragma unroll
+                                for (int m = 1; m < 4; ++m) {
+                                    gx = fma2(w4[m], Tx[zi + o + m], gx);
+                                    gy = fma2(w4[m], Ty[zi + o + m], gy);
+                                    gz = fma2(w4[m], Tz[zi + o + m], gz);
+                                }
+                                // forward quantities (P = gx, E = gy, Z = gz)
+                                const float2 dot = fma2(cc, gz, mul2(hh, gx));
+                                const float2 cp = fma2(hh, gz, mul2(ncc, gx));
+                                const float2 c2 = fma2(cp, cp, mul2(gy, gy));
+                                const float2 g2 = fma2(dot, dot, c2);
+                                const float2 xx = mul2(c2, g2);
+                                // inv = 1/(|g| |g_perp|), 0 where g is parallel to u (subgradient)
+                                float2 inv = make_float2(xx.x > 0.f ? rsqrt_approx(xx.x) : 0.f,
+                                                         xx.y > 0.f ? rsqrt_approx(xx.y) : 0.f);
+                                const float2 sn = mul2(c2, inv);                  // sin
+                                const float2 qg = mul2(mul2(inv, inv), c2);       // 1/|g|^2
+                                const float2 om = fma2(sn, nun, dup(1.0f));       // 1 - Dk/r
+                                const float2 sw = make_float2(sign_weight(wgt, dot.x), sign_weight(wgt, dot.y));
+                                // dS/dsin = sw * 2 om * (-|u|), times dL/dS
+                                const float2 coef = mul2(mul2(mul2(sw, om), mul2(nun, dup(2.0f))), gS[z]);
+                                const float2 sq = mul2(sn, qg);
+                                const float2 ci = mul2(cp, inv);
+                                // d sin / d(P, E, Z) = g_perp/(|g||g_perp|) - sin g/|g|^2,
+                                // g_perp = (-c cp, E, h cp)
+                                const float2 dP = mul2(coef, fma2(ncc, ci, mul2(sq, make_float2(-gx.x, -gx.y))));
+                                const float2 dE = mul2(coef, fma2(gy, inv, mul2(sq, make_float2(-gy.x, -gy.y))));
+                                const float2 dZ = mul2(coef, fma2(hh, ci, mul2(sq, make_float2(-gz.x, -gz.y))));
+#pragma unroll
+                                for (int m = 0; m < 4; ++m) {
+                                    gP[zi + o + m] = fma2(w4[m], dP, gP[zi + o + m]);
+                                    gE[zi + o + m] = fma2(w4[m], dE, gE[zi + o + m]);
+                                    gZ[zi + o + m] = fma2(w4[m], dZ, gZ[zi + o + m]);
+                                }
+                            }
+                        };
+#pragma unroll
+                        for (int zr = 0; zr < MZ; ++zr) {
+                            float2 w4[4];
+#pragma unroll
+                            for (int m = 0; m < 4; ++m) w4[m] = dup(wzc[zr * 4 + m]);
+                            if ((offmask >> zr) & 1)
+                                zpass(IntC<1>{}, zr, w4);
+                            else
+                                zpass(IntC<0>{}, zr, w4);
+                        }
+                    }
+                    // back to (x, y): X = ca P - sb E, Y = sb P + ca E
+#pragma unroll
+                    for (int w = 0; w < NW; ++w) {
+                        const float2 P = gP[w], E = gE[w];
+                        gP[w] = fma2(E, nsb, mul2(P, ca));
+                        gE[w] = fma2(E, ca, mul2(P, sb));
+                    }
+                    // intensity at the subvoxel centre rides on the (0, 0) pair: z pass
+                    // transpose with rho_z = 0 (5 taps)
+                    float2 gW[NW];
+#pragma unroll
+                    for (int w = 0; w < NW; ++w) gW[w] = make_float2(0.f, 0.f);
+                    const bool with_int = (pi == p.zero_pair);
+                    if (with_int) {
+#pragma unroll
+                        for (int z = 0; z < FZ; ++z) {
+                            const int zr = z % MZ, zi = z / MZ;
+                            const float* qz = wzi + zr * 5;
+#pragma unroll
+                            for (int m = 0; m < 5; ++m)
+                                if (zi + m < NW) gW[zi + m] = fma2(dup(qz[m]), gI[z], gW[zi + m]);
+                        }
+                    }
+                    // y pass transpose: column a feeds rows vbase..+3, column b rows vbase+1..+4
+#pragma unroll
+                    for (int w = 0; w < NW; ++w) {
+                        float4* dst = gut + (w * NV + vbase) * kTileX + xf;
+                        const float wk[4] = {wyv.x, wyv.y, wyv.z, wyv.w};
+#pragma unroll
+                        for (int j = 0; j < 5; ++j) {
+                            float sx = 0.f, sy = 0.f, sz = 0.f, sw_ = 0.f;
+                            if (j < 4) {
+                                sx = wk[j] * gP[w].x;
+                                sy = wk[j] * gE[w].x;
+                                sz = wk[j] * gZ[w].x;
+                                sw_ = wk[j] * gW[w].x;
+                            }
+                            if (j > 0) {
+                                sx = fmaf(wk[j - 1], gP[w].y, sx);
+                                sy = fmaf(wk[j - 1], gE[w].y, sy);
+                                sz = fmaf(wk[j - 1], gZ[w].y, sz);
+                                sw_ = fmaf(wk[j - 1], gW[w].y, sw_);
+                            }
+                            float4* d4 = dst + j * kTileX;
+                            atomicAdd(&d4->x, sx);
+                            atomicAdd(&d4->y, sy);
+                            atomicAdd(&d4->z, sz);
+                            if (with_int) atomicAdd(&d4->w, sw_);
+                        }
+                    }
+                }
+                __syncthreads();
+                // x pass transpose: entry (xf, v, w) feeds cells ub..ub+3 of row (v, w)
+                for (int e = tid; e < nut; e += nthr) {
+                    const int vw = e / kTileX;
+                    const int xfe = e % kTileX;
+                    const int Xe = X0 + xfe;
+                    const int xie = floordiv(Xe, mx), xre = Xe - xie * mx;
+                    const int oxe = offx[av * mx + xre];
+                    const float4 we = *reinterpret_cast<const float4*>(wx + (av * mx + xre) * 4);
+                    const int ube = xie - cx0 - 2 + oxe;
+                    const float4 gu = gut[e];
+                    float4* dst = ggt + vw * NU + ube;
+                    const float wk[4] = {we.x, we.y, we.z, we.w};
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        atomicAdd(&dst[k].x, wk[k] * gu.x);
+                        atomicAdd(&dst[k].y, wk[k] * gu.y);
+                        atomicAdd(&dst[k].z, wk[k] * gu.z);
+                        if (gu.w != 0.f) atomicAdd(&dst[k].w, wk[k] * gu.w);
+                    }
+                }
+            }
+            __syncthreads();
+            // cells outside the block do not depend on the input
+            for (int c = tid; c < ncell; c += nthr) {
+                const int u = c % NU;
+                const int v = (c / NU) % NV;
+                const int w = c / (NU * NV);
+                const int cu = cx0 + u, cv = cy0 + v, cw = cz0 + w;
+                if (!(cu >= 0 && cu < bw && cv >= 0 && cv < bh && cw >= 0 && cw < bd))
+                    ggt[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            __syncthreads();
+            // stencil transpose onto the input tile positions, then into dL/dI'
+            const int mR = p.gr[0], xR = p.gr[1], yR = p.gr[2], zR = p.gr[3];
+            for (int i = tid; i < nin; i += nthr) {
+                const int ix = i % NIX;
+                const int iy = (i / NIX) % NIY;
+                const int iz = i / (NIX * NIY);
+                const int u = ix - R, v = iy - R, w = iz - R;  // cell with the same position
+                auto G = [&](int du, int dv, int dw) -> float4 {
+                    const int uu = u + du, vv = v + dv, ww = w + dw;
+                    if (uu < 0 || uu >= NU || vv < 0 || vv >= NV || ww < 0 || ww >= NW)
+                        return make_float4(0.f, 0.f, 0.f, 0.f);
+                    return ggt[(ww * NV + vv) * NU + uu];
+                };
+                float acc = G(0, 0, 0).w;
+                // Gx(c) = sum_{i>0, j, k} I(c + (i, j, k)) - I(c + (-i, j, k))
+                for (int ii = 1; ii <= mR; ++ii)
+                    for (int j = -yR; j <= yR; ++j)
+                        for (int k = -zR; k <= zR; ++k) acc += G(-ii, -j, -k).x - G(ii, -j, -k).x;
+                for (int jj = 1; jj <= mR; ++jj)
+                    for (int ii = -xR; ii <= xR; ++ii)
+                        for (int k = -zR; k <= zR; ++k) acc += G(-ii, -jj, -k).y - G(-ii, jj, -k).y;
+                for (int kk = 1; kk <= mR; ++kk)
+                    for (int ii = -xR; ii <= xR; ++ii)
+                        for (int j = -yR; j <= yR; ++j) acc += G(-ii, -j, -kk).z - G(-ii, -j, kk).z;
+                if (acc != 0.f) {
+                    const int bx = clampi(cx0 - R + ix, 0, bw - 1);
+                    const int by = clampi(cy0 - R + iy, 0, bh - 1);
+                    const int bz = clampi(cz0 - R + iz, 0, bd - 1);
+                    const long long gidx = tbase + ((long long)(B.origin[2] + bz) * p.H + (B.origin[1] + by)) * p.W +
+                                           (B.origin[0] + bx);
+                    atomicAdd(a.gin + gidx, acc);
+                }
+            }
+        }
+    }
+}
+
+template <int MZ>
+int launch_adj_mz(const RadParams& p, const AdjParams& a, int grid, size_t smem, cudaStream_t st) {
+    constexpr int CZ = cza_for_mag(MZ);
+    auto k = radiality_adjoint_kernel<MZ, CZ>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return (int)e;
+    k<<<grid, p.TY * (kTileX / 2), smem, st>>>(p, a);
+    return (int)cudaGetLastError();
+}
+
+template <int MZ>
+int occ_adj_mz(int threads, size_t smem, int* out) {
+    constexpr int CZ = cza_for_mag(MZ);
+    auto k = radiality_adjoint_kernel<MZ, CZ>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return (int)e;
+    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k, threads, smem);
+}
+
+}  // namespace
+
+size_t radiality_adjoint_smem_bytes(const RadParams& p) {
+    const int NW = cza_for_mag(p.mag[2]) + 4;
+    size_t b = sizeof(float4) * (2 * (size_t)p.NU * p.NV * NW + 2 * (size_t)kTileX * p.NV * NW);
+    b += sizeof(float) * ((((size_t)p.NIX * p.NIY * p.NIZ + 3) & ~(size_t)3) + p.smem_table_words);
+    return (b + 15) & ~(size_t)15;
+}
+
+int launch_radiality_adjoint(const RadParams& p, const AdjParams& a, int grid, size_t smem, void* stream) {
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    switch (p.mag[2]) {
+        case 1: return launch_adj_mz<1>(p, a, grid, smem, st);
+        case 2: return launch_adj_mz<2>(p, a, grid, smem, st);
+        case 3: return launch_adj_mz<3>(p, a, grid, smem, st);
+        case 4: return launch_adj_mz<4>(p, a, grid, smem, st);
+        case 5: return launch_adj_mz<5>(p, a, grid, smem, st);
+        case 6: return launch_adj_mz<6>(p, a, grid, smem, st);
+        case 7: return launch_adj_mz<7>(p, a, grid, smem, st);
+        case 8: return launch_adj_mz<8>(p, a, grid, smem, st);
+    }
+    return (int)cudaErrorInvalidValue;
+}
+
+int radiality_adjoint_max_ctas_per_sm(const RadParams& p, int* out) {
+    const size_t smem = radiality_adjoint_smem_bytes(p);
+    const int threads = p.TY * (kTileX / 2);
+    switch (p.mag[2]) {
+        case 1: return occ_adj_mz<1>(threads, smem, out);
+        case 2: return occ_adj_mz<2>(threads, smem, out);
+        case 3: return occ_adj_mz<3>(threads, smem, out);
+        case 4: return occ_adj_mz<4>(threads, smem, out);
+        case 5: return occ_adj_mz<5>(threads, smem, out);
+        case 6: return occ_adj_mz<6>(threads, smem, out);
+        case 7: return occ_adj_mz<7>(threads, smem, out);
+        case 8: return occ_adj_mz<8>(threads, smem, out);
+    }
+    return (int)cudaErrorInvalidValue;
+}
+
+int launch_temporal_adjoint(const BlockDev* blocks, long long vox, const float* rad, const float* inten,
+                            const float* gmap, int T, int method, int order, int iw, int renorm, int poscon, float* gS,
+                            float* gI, void* stream) {
+    if (vox == 0) return 0;
+    const long long grid = (vox + 127) / 128;
+    temporal_adjoint_kernel<<<(unsigned)grid, 128, 0, static_cast<cudaStream_t>(stream)>>>(
+        blocks, rad, inten, gmap, T, method, order, iw, renorm, poscon, gS, gI);
+    return (int)cudaGetLastError();
+}
+
+int launch_shift_axis(const float* src, float* dst, int W, int H, int D, int T, int axis, const float* shifts, int mode,
+                      void* stream) {
+    const long long n = (long long)W * H * D * T;
+    const long long grid = std::min<long long>((n + 255) / 256, 152LL * 16);
+    shift_axis_kernel<<<(unsigned)grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(src, dst, W, H, D, T, axis,
+                                                                                     shifts, mode);
+    return (int)cudaGetLastError();
+}
+
+namespace {
+__global__ void d2f_kernel(const double* s, float* d, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) d[i] = (float)s[i];
+}
+}  // namespace
+
+int launch_double_to_float(const double* src, float* dst, int n, void* stream) {
+    if (n <= 0) return 0;
+    d2f_kernel<<<(n + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(src, dst, n);
+    return (int)cudaGetLastError();
+}
+
+int launch_drift_dot(const float* g, const float* dv, long long nv, int T, int axis, double* out, void* stream) {
+    dim3 grid((unsigned)std::min<long long>((nv + 255) / 256, 64), (unsigned)T);
+    drift_dot_kernel<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(g, dv, nv, axis, out);
+    return (int)cudaGetLastError();
+}
+
+}  // namespace rfba

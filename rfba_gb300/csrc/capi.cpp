@@ -105,6 +105,19 @@ struct rfba_ctx {
     long long last_flop_units = 0;  // subvoxel-time-points computed by the last call
     int grid_override = 0;          // CTAs for the radiality kernel (0 = occupancy x SMs)
     int chunk_override = 0;         // time points per work item (0 = automatic)
+    int last_passes = 0;            // passes of the last forward (1 = its stacks are all resident)
+    // differentiable path: buffers and the forward the backward can reuse
+    rfba::DevBuf shifted, tmp1, tmp2, gS, gI, gin, dshift, ablocks, atiles, acounter;
+    struct Train {
+        bool valid = false;
+        rfba_srrf_config cfg;
+        int dims[4] = {0, 0, 0, 0};
+        const void* in = nullptr;
+        const void* shifts = nullptr;
+        const float* iprime = nullptr;
+        rfba::BlockDev blk;
+    } train;
+    double last_backward_ms = 0.0;
 };
 
 namespace rfba {
@@ -235,6 +248,58 @@ static int make_blocks(rfba_ctx* ctx, const rfba_srrf_config& cfg, const int dim
 
 static size_t elem_size(rfba_dtype dt) { return dt == RFBA_U16 ? 2 : 4; }
 
+// Kernel parameters common to the forward and adjoint radiality kernels
+// (everything but the block / tile lists and the schedule).
+static RadParams fill_rad_params(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void* in_dev, const int dims[4],
+                                 int CZ) {
+    const PlanCache& P = ctx->plan;
+    const int T = dims[3];
+    RadParams rp;
+    std::memset(&rp, 0, sizeof rp);
+    rp.in = in_dev;
+    rp.W = dims[0];
+    rp.H = dims[1];
+    rp.D = dims[2];
+    rp.T = T;
+    for (int a = 0; a < 3; ++a) rp.mag[a] = cfg.mag[a];
+    rp.nxv = (int)P.ring.xv.size();
+    rp.nyv = (int)P.ring.yv.size();
+    rp.nzv = (int)P.ring.zv.size();
+    rp.ngroups = (int)P.ring.grp_xval.size();
+    rp.npairs = (int)P.ring.pair_yval.size();
+    rp.npoints = (int)P.ring.pt_zval.size();
+    rp.zero_pair = P.zero_pair;
+    if (cfg.gradient_smooth == 0) {
+        rp.gr[0] = 1;
+        rp.gr[1] = rp.gr[2] = rp.gr[3] = 0;
+    } else {
+        rp.gr[0] = cfg.main_range;
+        rp.gr[1] = cfg.x_range;
+        rp.gr[2] = cfg.y_range;
+        rp.gr[3] = cfg.z_range;
+    }
+    rp.R = std::max(std::max(rp.gr[0], rp.gr[1]), std::max(rp.gr[2], rp.gr[3]));
+    if (rp.gr[0] == 1 && rp.gr[1] == 1 && rp.gr[2] == 1 && rp.gr[3] == 1)
+        rp.grad_mode = 1;
+    else if (rp.gr[0] == 1 && rp.gr[1] == 0 && rp.gr[2] == 0 && rp.gr[3] == 0)
+        rp.grad_mode = 2;
+    else
+        rp.grad_mode = 0;
+    rp.TY = tile_rows_for_mag(cfg.mag[1]);
+    rp.NU = (kTileX - 1) / cfg.mag[0] + 2 + 4;
+    rp.NV = (rp.TY - 1) / cfg.mag[1] + 2 + 4;
+    rp.NW = CZ + 4;
+    rp.NIX = rp.NU + 2 * rp.R;
+    rp.NIY = rp.NV + 2 * rp.R;
+    rp.NIZ = rp.NW + 2 * rp.R;
+    rp.renorm = cfg.renormalize == 1;
+    rp.poscon = cfg.remove_con == 1;
+    rp.tables = static_cast<const float*>(ctx->tables.p);
+    rp.tl = P.tl;
+    rp.smem_table_words = P.tl.words;
+    return rp;
+}
+
 // Run the device pipeline for all blocks. in_dev / out_dev are device pointers.
 static int run_device(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void* in_dev, rfba_dtype dtype,
                       const int dims[4], const std::vector<BlockDev>& all, float* out_dev, cudaStream_t st) {
@@ -245,7 +310,10 @@ static int run_device(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void* in
     size_t i0 = 0;
     ctx->last_rad_ms = ctx->last_temporal_ms = 0.0;
     ctx->last_flop_units = 0;
+    ctx->last_passes = 0;
+    ctx->train.valid = false;
     while (i0 < all.size()) {
+        ctx->last_passes++;
         size_t i1 = i0;
         long long vox = 0;
         while (i1 < all.size()) {
@@ -290,50 +358,7 @@ static int run_device(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void* in
                   "prefix upload");
         RFBA_CUDA(cudaMemsetAsync(ctx->counter.p, 0, 256, st), "counter reset");
 
-        RadParams rp;
-        std::memset(&rp, 0, sizeof rp);
-        rp.in = in_dev;
-        rp.W = dims[0];
-        rp.H = dims[1];
-        rp.D = dims[2];
-        rp.T = T;
-        for (int a = 0; a < 3; ++a) rp.mag[a] = cfg.mag[a];
-        rp.nxv = (int)P.ring.xv.size();
-        rp.nyv = (int)P.ring.yv.size();
-        rp.nzv = (int)P.ring.zv.size();
-        rp.ngroups = (int)P.ring.grp_xval.size();
-        rp.npairs = (int)P.ring.pair_yval.size();
-        rp.npoints = (int)P.ring.pt_zval.size();
-        rp.zero_pair = P.zero_pair;
-        if (cfg.gradient_smooth == 0) {
-            rp.gr[0] = 1;
-            rp.gr[1] = rp.gr[2] = rp.gr[3] = 0;
-        } else {
-            rp.gr[0] = cfg.main_range;
-            rp.gr[1] = cfg.x_range;
-            rp.gr[2] = cfg.y_range;
-            rp.gr[3] = cfg.z_range;
-        }
-        rp.R = std::max(std::max(rp.gr[0], rp.gr[1]), std::max(rp.gr[2], rp.gr[3]));
-        if (rp.gr[0] == 1 && rp.gr[1] == 1 && rp.gr[2] == 1 && rp.gr[3] == 1)
-            rp.grad_mode = 1;
-        else if (rp.gr[0] == 1 && rp.gr[1] == 0 && rp.gr[2] == 0 && rp.gr[3] == 0)
-            rp.grad_mode = 2;
-        else
-            rp.grad_mode = 0;
-        const int CZ = cz_for_mag(cfg.mag[2]);
-        rp.TY = tile_rows_for_mag(cfg.mag[1]);
-        rp.NU = (kTileX - 1) / cfg.mag[0] + 2 + 4;
-        rp.NV = (rp.TY - 1) / cfg.mag[1] + 2 + 4;
-        rp.NW = CZ + 4;
-        rp.NIX = rp.NU + 2 * rp.R;
-        rp.NIY = rp.NV + 2 * rp.R;
-        rp.NIZ = rp.NW + 2 * rp.R;
-        rp.renorm = cfg.renormalize == 1;
-        rp.poscon = cfg.remove_con == 1;
-        rp.tables = static_cast<const float*>(ctx->tables.p);
-        rp.tl = P.tl;
-        rp.smem_table_words = P.tl.words;
+        RadParams rp = fill_rad_params(ctx, cfg, in_dev, dims, cz_for_mag(cfg.mag[2]));
         rp.blocks = static_cast<const BlockDev*>(ctx->blocks.p);
         rp.tiles = static_cast<const TileDesc*>(ctx->tiles.p);
         rp.ntiles = (int)tiles.size();
@@ -431,9 +456,20 @@ static int validate_common(const rfba_srrf_config* cfg, const void* in, const in
     return RFBA_OK;
 }
 
+static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const void* in, rfba_dtype dtype,
+                                 const int dims[4], const rfba_block* blocks, int nblocks, float* out,
+                                 long long out_elems, int flags, cudaStream_t st, bool zero_out);
+
 static int forward_blocks_impl(rfba_ctx* ctx, const rfba_srrf_config* cfg, const void* in, rfba_dtype dtype,
                                const int dims[4], const rfba_block* blocks, int nblocks, float* out, long long out_elems,
                                int flags, cudaStream_t st, bool zero_out) {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    return forward_blocks_locked(ctx, cfg, in, dtype, dims, blocks, nblocks, out, out_elems, flags, st, zero_out);
+}
+
+static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const void* in, rfba_dtype dtype,
+                                 const int dims[4], const rfba_block* blocks, int nblocks, float* out,
+                                 long long out_elems, int flags, cudaStream_t st, bool zero_out) {
     int s = validate_common(cfg, in, dims, out);
     if (s) return s;
     if (nblocks < 0 || (nblocks > 0 && !blocks) || out_elems < 0) {
@@ -444,7 +480,6 @@ static int forward_blocks_impl(rfba_ctx* ctx, const rfba_srrf_config* cfg, const
         set_error("dtype must be RFBA_F32 or RFBA_U16");
         return RFBA_ERR_INVALID;
     }
-    std::lock_guard<std::mutex> lk(ctx->mu);
     RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
     if ((s = ensure_plan(ctx, *cfg))) return s;
     std::vector<BlockDev> all;
@@ -478,11 +513,228 @@ static int forward_blocks_impl(rfba_ctx* ctx, const rfba_srrf_config* cfg, const
     return RFBA_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Differentiable path
+
+static bool same_cfg(const rfba_srrf_config& a, const rfba_srrf_config& b) {
+    return std::memcmp(&a, &b, sizeof a) == 0;
+}
+
+// I' = drift(in) into ctx->shifted (x, then y, then z), or in itself.
+static int apply_drift(rfba_ctx* ctx, const float* in, const float* shifts, const int dims[4], cudaStream_t st,
+                       const float** iprime) {
+    if (!shifts) {
+        *iprime = in;
+        return RFBA_OK;
+    }
+    const size_t n = (size_t)dims[0] * dims[1] * dims[2] * dims[3];
+    int s;
+    if ((s = ctx->shifted.ensure(n * 4, "shifted input")) || (s = ctx->tmp1.ensure(n * 4, "scratch")) ||
+        (s = ctx->tmp2.ensure(n * 4, "scratch")))
+        return s;
+    float* t1 = static_cast<float*>(ctx->tmp1.p);
+    float* t2 = static_cast<float*>(ctx->tmp2.p);
+    float* out = static_cast<float*>(ctx->shifted.p);
+    int e = launch_shift_axis(in, t1, dims[0], dims[1], dims[2], dims[3], 0, shifts, 0, st);
+    if (!e) e = launch_shift_axis(t1, t2, dims[0], dims[1], dims[2], dims[3], 1, shifts, 0, st);
+    if (!e) e = launch_shift_axis(t2, out, dims[0], dims[1], dims[2], dims[3], 2, shifts, 0, st);
+    if (e) return cuda_fail((cudaError_t)e, "drift resampling");
+    ctx->launches += 3;
+    *iprime = out;
+    return RFBA_OK;
+}
+
+static int forward_shifted_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* in, const float* shifts,
+                                  const int dims[4], float* out, cudaStream_t st) {
+    int s = validate_common(cfg, in, dims, out);
+    if (s) return s;
+    RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const float* ip = nullptr;
+    if ((s = apply_drift(ctx, in, shifts, dims, st, &ip))) return s;
+    rfba_block b;
+    std::memset(&b, 0, sizeof b);
+    for (int a = 0; a < 3; ++a) {
+        b.size[a] = dims[a];
+        b.hi[a] = dims[a] * cfg->mag[a];
+    }
+    b.out_stride[0] = 1;
+    b.out_stride[1] = b.hi[0];
+    b.out_stride[2] = (int64_t)b.hi[0] * b.hi[1];
+    const int64_t n = (int64_t)b.hi[0] * b.hi[1] * b.hi[2];
+    if ((s = forward_blocks_locked(ctx, cfg, ip, RFBA_F32, dims, &b, 1, out, n, RFBA_DEVICE_PTRS, st, false)))
+        return s;
+    // the backward can reuse this forward's stacks when they are all resident and
+    // the temporal reduction left them intact (ITC 1 bins the series in place)
+    if (ctx->last_passes == 1 && !(cfg->method == 3 && cfg->itc == 1)) {
+        std::vector<BlockDev> all;
+        if ((s = make_blocks(ctx, *cfg, dims, &b, 1, &all))) return s;
+        if (all.size() == 1) {
+            ctx->train.valid = true;
+            ctx->train.cfg = *cfg;
+            for (int a = 0; a < 4; ++a) ctx->train.dims[a] = dims[a];
+            ctx->train.in = in;
+            ctx->train.shifts = shifts;
+            ctx->train.iprime = ip;
+            ctx->train.blk = all[0];
+            ctx->train.blk.stack_off = 0;
+        }
+    }
+    return RFBA_OK;
+}
+
+static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* in, const float* shifts,
+                           const int dims[4], const float* gmap, float* din, float* dshift, cudaStream_t st) {
+    int s = validate_common(cfg, in, dims, gmap);
+    if (s) return s;
+    if (!din) {
+        set_error("null argument");
+        return RFBA_ERR_INVALID;
+    }
+    if (!(cfg->method == 1 || (cfg->method == 3 && cfg->itc != 1))) {
+        set_error("the adjoint covers TRA (Method 1) and TRAC with Integrate_Temporal_Correlations 0");
+        return RFBA_ERR_UNSUPPORTED;
+    }
+    RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const bool reuse = ctx->train.valid && same_cfg(ctx->train.cfg, *cfg) && ctx->train.in == in &&
+                       ctx->train.shifts == shifts && ctx->train.dims[0] == dims[0] && ctx->train.dims[1] == dims[1] &&
+                       ctx->train.dims[2] == dims[2] && ctx->train.dims[3] == dims[3];
+    if (ctx->timing) RFBA_CUDA(cudaEventRecord(ctx->ev[0], st), "event");
+    if (!reuse) {
+        const size_t nmap = (size_t)dims[0] * cfg->mag[0] * dims[1] * cfg->mag[1] * dims[2] * cfg->mag[2];
+        if ((s = ctx->out.ensure(nmap * 4, "map"))) return s;
+        if ((s = forward_shifted_locked(ctx, cfg, in, shifts, dims, static_cast<float*>(ctx->out.p), st))) return s;
+        if (!ctx->train.valid) {
+            set_error("the adjoint needs the whole radiality stack resident in one pass; raise the scratch budget");
+            return RFBA_ERR_UNSUPPORTED;
+        }
+    }
+    if ((s = ensure_plan(ctx, *cfg))) return s;
+    const int T = dims[3];
+    const size_t nin = (size_t)dims[0] * dims[1] * dims[2] * T;
+    BlockDev blk = ctx->train.blk;
+    const long long V = blk.vox;
+    const int FZ = cfg->mag[2] * cza_for_mag(cfg->mag[2]);
+    blk.ntile[2] = (blk.hi[2] - blk.zbase + FZ - 1) / FZ;
+    std::vector<TileDesc> tiles;
+    for (int tz = 0; tz < blk.ntile[2]; ++tz)
+        for (int ty = 0; ty < blk.ntile[1]; ++ty)
+            for (int tx = 0; tx < blk.ntile[0]; ++tx) tiles.push_back({0, tx, ty, tz});
+    if ((s = ctx->gS.ensure((size_t)V * T * 4, "adjoint stack")) || (s = ctx->gI.ensure((size_t)V * T * 4, "adjoint stack")) ||
+        (s = ctx->gin.ensure(nin * 4, "input adjoint")) || (s = ctx->ablocks.ensure(sizeof(BlockDev), "blocks")) ||
+        (s = ctx->atiles.ensure(tiles.size() * sizeof(TileDesc), "tiles")) || (s = ctx->acounter.ensure(256, "counter")))
+        return s;
+    RFBA_CUDA(cudaMemcpyAsync(ctx->ablocks.p, &blk, sizeof blk, cudaMemcpyHostToDevice, st), "blocks upload");
+    RFBA_CUDA(cudaMemcpyAsync(ctx->atiles.p, tiles.data(), tiles.size() * sizeof(TileDesc), cudaMemcpyHostToDevice, st),
+              "tiles upload");
+    RFBA_CUDA(cudaMemsetAsync(ctx->acounter.p, 0, 256, st), "counter reset");
+    RFBA_CUDA(cudaMemsetAsync(ctx->gin.p, 0, nin * 4, st), "adjoint clear");
+    const BlockDev* dblk = static_cast<const BlockDev*>(ctx->ablocks.p);
+    float* gS = static_cast<float*>(ctx->gS.p);
+    float* gI = static_cast<float*>(ctx->gI.p);
+    float* gin = static_cast<float*>(ctx->gin.p);
+    int e = launch_temporal_adjoint(dblk, V, static_cast<const float*>(ctx->rad.p),
+                                    static_cast<const float*>(ctx->inten.p), gmap, T, cfg->method, cfg->trac_order,
+                                    cfg->intensity_w, cfg->renormalize == 1, cfg->remove_con == 1, gS, gI, st);
+    if (e) return cuda_fail((cudaError_t)e, "temporal adjoint launch");
+    RadParams rp = fill_rad_params(ctx, *cfg, ctx->train.iprime, dims, cza_for_mag(cfg->mag[2]));
+    rp.blocks = dblk;
+    rp.tiles = static_cast<const TileDesc*>(ctx->atiles.p);
+    rp.ntiles = (int)tiles.size();
+    rp.work_counter = static_cast<unsigned int*>(ctx->acounter.p);
+    const size_t smem = radiality_adjoint_smem_bytes(rp);
+    if (smem > 227 * 1024) {
+        set_error("shared memory tile too large for the adjoint of this configuration");
+        return RFBA_ERR_UNSUPPORTED;
+    }
+    int per_sm = 0;
+    e = radiality_adjoint_max_ctas_per_sm(rp, &per_sm);
+    if (e) return cuda_fail((cudaError_t)e, "occupancy");
+    if (per_sm < 1) {
+        set_error("adjoint kernel does not fit on an SM");
+        return RFBA_ERR_UNSUPPORTED;
+    }
+    const int slots = per_sm * ctx->sm_count;
+    long long nch = (8LL * slots + rp.ntiles - 1) / rp.ntiles;
+    nch = std::max<long long>(1, std::min<long long>(nch, T));
+    rp.t_chunk = (int)((T + nch - 1) / nch);
+    rp.nchunks = (T + rp.t_chunk - 1) / rp.t_chunk;
+    rp.nitems = (long long)rp.ntiles * rp.nchunks;
+    const int grid = (int)std::max<long long>(1, std::min<long long>(slots, rp.nitems));
+    AdjParams ap{gS, gI, gin};
+    e = launch_radiality_adjoint(rp, ap, grid, smem, st);
+    if (e) return cuda_fail((cudaError_t)e, "radiality adjoint launch");
+    ctx->launches += 2;
+    // through the drift operator
+    if (shifts) {
+        float* t1 = static_cast<float*>(ctx->tmp1.p);
+        float* t2 = static_cast<float*>(ctx->tmp2.p);
+        e = launch_shift_axis(gin, t1, dims[0], dims[1], dims[2], T, 2, shifts, 2, st);
+        if (!e) e = launch_shift_axis(t1, t2, dims[0], dims[1], dims[2], T, 1, shifts, 2, st);
+        if (!e) e = launch_shift_axis(t2, din, dims[0], dims[1], dims[2], T, 0, shifts, 2, st);
+        ctx->launches += 3;
+        if (!e && dshift) {
+            if ((s = ctx->dshift.ensure((size_t)T * 3 * sizeof(double), "drift adjoint"))) return s;
+            double* ds = static_cast<double*>(ctx->dshift.p);
+            RFBA_CUDA(cudaMemsetAsync(ds, 0, (size_t)T * 3 * sizeof(double), st), "drift adjoint clear");
+            const long long nv = (long long)dims[0] * dims[1] * dims[2];
+            for (int ax = 0; ax < 3 && !e; ++ax) {
+                e = launch_shift_axis(in, t1, dims[0], dims[1], dims[2], T, 0, shifts, ax == 0 ? 1 : 0, st);
+                if (!e) e = launch_shift_axis(t1, t2, dims[0], dims[1], dims[2], T, 1, shifts, ax == 1 ? 1 : 0, st);
+                if (!e) e = launch_shift_axis(t2, t1, dims[0], dims[1], dims[2], T, 2, shifts, ax == 2 ? 1 : 0, st);
+                if (!e) e = launch_drift_dot(gin, t1, nv, T, ax, ds, st);
+                ctx->launches += 4;
+            }
+            if (!e) e = launch_double_to_float(ds, dshift, 3 * T, st);
+            ctx->launches += 1;
+        }
+        if (e) return cuda_fail((cudaError_t)e, "drift adjoint");
+    } else {
+        RFBA_CUDA(cudaMemcpyAsync(din, gin, nin * 4, cudaMemcpyDeviceToDevice, st), "adjoint copy");
+        if (dshift) RFBA_CUDA(cudaMemsetAsync(dshift, 0, (size_t)T * 3 * 4, st), "drift adjoint clear");
+    }
+    if (ctx->timing) {
+        RFBA_CUDA(cudaEventRecord(ctx->ev[3], st), "event");
+        RFBA_CUDA(cudaEventSynchronize(ctx->ev[3]), "event sync");
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[3]);
+        ctx->last_backward_ms = ms;
+    }
+    return RFBA_OK;
+}
+
 }  // namespace rfba
 
 using namespace rfba;
 
 extern "C" {
+
+int rfba_srrf_forward_shifted(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* in, const float* shifts,
+                              const int dims[4], float* out, void* stream) {
+    if (!ctx) {
+        set_error("null context");
+        return RFBA_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    return forward_shifted_locked(ctx, cfg, in, shifts, dims, out, st);
+}
+
+int rfba_srrf_backward(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* in, const float* shifts,
+                       const int dims[4], const float* dL_dmap, float* dL_din, float* dL_dshift, void* stream) {
+    if (!ctx) {
+        set_error("null context");
+        return RFBA_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    return backward_locked(ctx, cfg, in, shifts, dims, dL_dmap, dL_din, dL_dshift, st);
+}
+
+int rfba_ctx_last_backward_ms(rfba_ctx* c, double* ms) {
+    if (!c || !ms) return RFBA_ERR_INVALID;
+    *ms = c->last_backward_ms;
+    return RFBA_OK;
+}
 
 const char* rfba_last_error(void) { return g_last_error.c_str(); }
 const char* rfba_version(void) { return "rfba_srrf 0.1 (sm_103a)"; }

@@ -23,6 +23,10 @@ constexpr int cz_for_mag(int mz) {
     return mz == 1 ? 8 : mz == 2 ? 8 : mz == 3 ? 5 : mz == 4 ? 4 : mz == 5 ? 3 : 2;
 }
 
+// Coarse z cells per tile of the adjoint kernel (it holds twice the register
+// columns of the forward).
+constexpr int cza_for_mag(int mz) { return mz <= 2 ? 4 : (mz <= 4 ? 2 : 1); }
+
 // One independent block of the input with the fine region it computes.
 struct BlockDev {
     int origin[3];   // input voxel origin in the full volume
@@ -118,7 +122,24 @@ struct TemporalParams {
     float* out;
 };
 
-// Launchers (radiality.cu / temporal.cu). Return a cudaError_t as int.
+// Adjoint inputs and output of the radiality adjoint kernel.
+struct AdjParams {
+    const float* gS;  // dL/d(radiality before transforms) per subvoxel and time, [t][v]
+    const float* gI;  // dL/d(interpolated intensity), [t][v]
+    float* gin;       // dL/dI' accumulated, [t][z][y][x] of the full input
+};
+
+// Launchers (radiality.cu / temporal.cu / adjoint.cu). Return a cudaError_t as int.
+int launch_radiality_adjoint(const RadParams& p, const AdjParams& a, int grid, size_t smem, void* stream);
+size_t radiality_adjoint_smem_bytes(const RadParams& p);
+int radiality_adjoint_max_ctas_per_sm(const RadParams& p, int* out);
+int launch_temporal_adjoint(const BlockDev* blocks, long long vox, const float* rad, const float* inten,
+                            const float* gmap, int T, int method, int order, int iw, int renorm, int poscon, float* gS,
+                            float* gI, void* stream);
+int launch_shift_axis(const float* src, float* dst, int W, int H, int D, int T, int axis, const float* shifts, int mode,
+                      void* stream);
+int launch_drift_dot(const float* g, const float* dv, long long nv, int T, int axis, double* out, void* stream);
+int launch_double_to_float(const double* src, float* dst, int n, void* stream);
 int launch_radiality(const RadParams& p, int grid, size_t smem, int in_u16, void* stream);
 size_t radiality_smem_bytes(const RadParams& p);
 int tile_rows_for_mag(int my);

@@ -130,6 +130,9 @@ def lib():
         L.rfba_blocks_gradientcalc.argtypes = [cp, ip, bp, ctypes.c_int]
         L.rfba_blocks_dosplit.argtypes = [cp, ip, ip, ctypes.c_int, bp, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]
         L.rfba_srrf_plan_info.argtypes = [cp, ip, ip, ip, ip]
+        L.rfba_srrf_forward_shifted.argtypes = [vp, cp, vp, vp, ip, vp, vp]
+        L.rfba_srrf_backward.argtypes = [vp, cp, vp, vp, ip, vp, vp, vp, vp]
+        L.rfba_ctx_last_backward_ms.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
         L.SRRFGradientCalc.argtypes = [fp, ip, fp]
         L.SRRFGetMag.argtypes = []
         L.SRRFGradientCalcGPU.argtypes = [fp, ip, fp, ctypes.POINTER(SRRFConf)]
@@ -327,6 +330,41 @@ class Context:
         _check(lib().rfba_srrf_forward_blocks(self.h, ctypes.byref(cfg), ptr, dt, _iptr(dims), blocks, nblocks, optr,
                                               out_elems, RFBA_DEVICE_PTRS if dev else RFBA_HOST_PTRS, st))
         return out
+
+    def forward_shifted(self, cfg: Config, x, shifts=None, out=None, stream=None):
+        """Drift-corrected forward on device tensors: x float32 [T][D][H][W],
+        shifts float32 [T][3] (x, y, z) or None. Keeps the stacks for backward."""
+        import torch
+        T, D, H, W = x.shape
+        dims = _dims(x.shape)
+        if out is None:
+            out = torch.empty((D * cfg.mag[2], H * cfg.mag[1], W * cfg.mag[0]), dtype=torch.float32, device=x.device)
+        sp = ctypes.c_void_p(shifts.data_ptr()) if shifts is not None else None
+        st = ctypes.c_void_p(stream) if stream else None
+        _check(lib().rfba_srrf_forward_shifted(self.h, ctypes.byref(cfg), ctypes.c_void_p(x.data_ptr()), sp,
+                                               _iptr(dims), ctypes.c_void_p(out.data_ptr()), st))
+        return out
+
+    def backward(self, cfg: Config, x, shifts, dL_dmap, din=None, dshift=None, stream=None):
+        """Adjoint of forward_shifted: returns (dL/dx, dL/dshifts or None)."""
+        import torch
+        dims = _dims(x.shape)
+        if din is None:
+            din = torch.empty_like(x)
+        if dshift is None and shifts is not None:
+            dshift = torch.empty_like(shifts)
+        sp = ctypes.c_void_p(shifts.data_ptr()) if shifts is not None else None
+        dsp = ctypes.c_void_p(dshift.data_ptr()) if dshift is not None else None
+        st = ctypes.c_void_p(stream) if stream else None
+        _check(lib().rfba_srrf_backward(self.h, ctypes.byref(cfg), ctypes.c_void_p(x.data_ptr()), sp, _iptr(dims),
+                                        ctypes.c_void_p(dL_dmap.data_ptr()), ctypes.c_void_p(din.data_ptr()), dsp,
+                                        st))
+        return din, dshift
+
+    def last_backward_ms(self) -> float:
+        v = ctypes.c_double()
+        _check(lib().rfba_ctx_last_backward_ms(self.h, ctypes.byref(v)))
+        return v.value
 
     def forward_blocks_plain(self, cfg: Config, x: np.ndarray, blocks, nblocks: int, out_elems: int, out=None):
         ptr, dt, dims, dev = self._in(x)

@@ -1,0 +1,118 @@
+"""The CUDA adjoint (rfba_srrf_forward_shifted / rfba_srrf_backward) against
+the FP64 CPU adjoint of the oracle and against FP64 central differences.
+
+Objective L = -||map||_2 over the finite map voxels, so dL/dmap = -map/||map||.
+"""
+import numpy as np
+import pytest
+
+from tests.parity import assert_parity, rel_linf
+
+pytestmark = pytest.mark.gpu
+
+SHIPPED = dict(gradient_smooth=1, main_range=1, x_range=1, y_range=1, z_range=1)
+
+
+def _objective(m):
+    f = np.where(np.isfinite(m), m, 0.0).astype(np.float64)
+    return -np.sqrt(np.sum(f * f))
+
+
+def _gmap(m):
+    f = np.where(np.isfinite(m), m, 0.0).astype(np.float64)
+    return np.where(np.isfinite(m), -f / np.sqrt(np.sum(f * f)), 0.0)
+
+
+def _case(seed, T, D, H, W, drift=0.3):
+    from rfba_gb300 import synth
+    scene = synth.make_scene(seed, T, (W, H, D), 10)
+    x = synth.render(scene, (W, H, D), seed, np.float32)
+    sh = np.random.default_rng(seed).normal(0, drift, size=(T, 3)).astype(np.float32)
+    return x, sh
+
+
+def _gpu(ctx, cfg, x, sh):
+    import torch
+    xd = torch.from_numpy(x).cuda()
+    sd = torch.from_numpy(sh).cuda() if sh is not None else None
+    m = ctx.forward_shifted(cfg, xd, sd)
+    torch.cuda.synchronize()
+    mh = m.cpu().numpy()
+    g = torch.from_numpy(_gmap(mh).astype(np.float32)).cuda()
+    din, dsh = ctx.backward(cfg, xd, sd, g)
+    torch.cuda.synchronize()
+    return mh, din.cpu().numpy(), (dsh.cpu().numpy() if dsh is not None else None)
+
+
+CASES = [
+    ("trac2_iw_drift", dict(mag=2, method=3, itc=0, trac_order=2, **SHIPPED), (7, 9, 10, 11), True),
+    ("tra_iw_drift", dict(mag=2, method=1, **SHIPPED), (6, 9, 9, 10), True),
+    ("trac4_renorm", dict(mag=2, method=3, itc=0, trac_order=4, renormalize=1, **SHIPPED), (9, 8, 9, 9), True),
+    ("trac3_mag3_nodrift_poscon", dict(mag=3, method=3, itc=0, trac_order=3, remove_con=1, **SHIPPED), (7, 7, 8, 8),
+     False),
+    ("trac2_aniso_nosmooth", dict(mag=(2, 2, 1), method=3, itc=0, trac_order=2), (8, 9, 9, 10), True),
+]
+
+
+@pytest.mark.parametrize("name,kw,shape,drift", CASES, ids=[c[0] for c in CASES])
+def test_adjoint_matches_fp64_adjoint(ctx, oracle_mod, name, kw, shape, drift):
+    from rfba_gb300 import srrf
+    O = oracle_mod
+    cfg = srrf.Config.make(**kw)
+    oc = O.make_conf(**kw)
+    x, sh = _case(11 + len(name), *shape)
+    if not drift:
+        sh = None
+    m, din, dsh = _gpu(ctx, cfg, x, sh)
+    mo = O.forward_shifted(x, oc, sh)
+    assert_parity(m, mo, 1e-4, name + " forward")
+    _, din_o, dsh_o = O.adjoint(x, oc, _gmap(mo), sh)
+    e_in = rel_linf(din, din_o)
+    msg = f"[adjoint] {name}: dL/dI rel L-inf {e_in:.2e}"
+    assert e_in < 2e-4, msg
+    if drift:
+        e_sh = rel_linf(dsh, dsh_o)
+        msg += f", dL/dshift rel L-inf {e_sh:.2e}"
+        assert e_sh < 2e-4, msg
+    print(msg)
+
+
+def test_adjoint_against_central_differences(ctx, oracle_mod):
+    """h = 1e-3 central differences of the FP64 forward at 200 random input
+    voxels and every shift."""
+    from rfba_gb300 import srrf
+    O = oracle_mod
+    kw = dict(mag=2, method=3, itc=0, trac_order=2, **SHIPPED)
+    cfg = srrf.Config.make(**kw)
+    oc = O.make_conf(**kw)
+    x, sh = _case(5, 6, 8, 9, 10, drift=0.15)
+    _, din, dsh = _gpu(ctx, cfg, x, sh)
+    rng = np.random.default_rng(0)
+    T, D, H, W = x.shape
+    # voxels inside the volume whose gradient is not negligible
+    idx = np.argwhere(np.abs(din) > 1e-3 * np.abs(din).max())
+    pick = idx[rng.choice(len(idx), size=min(200, len(idx)), replace=False)]
+    h = 1e-3
+    fd, an = [], []
+    for (t, z, y, xx) in pick:
+        xp = x.copy()
+        xm = x.copy()
+        xp[t, z, y, xx] += h
+        xm[t, z, y, xx] -= h
+        step = float(xp[t, z, y, xx]) - float(xm[t, z, y, xx])
+        fd.append((_objective(O.forward_shifted(xp, oc, sh)) - _objective(O.forward_shifted(xm, oc, sh))) / step)
+        an.append(din[t, z, y, xx])
+    for t in range(T):
+        for a in range(3):
+            sp = sh.astype(np.float64).copy()
+            sm = sh.astype(np.float64).copy()
+            sp[t, a] += h
+            sm[t, a] -= h
+            fd.append((_objective(O.forward_shifted(x, oc, sp)) - _objective(O.forward_shifted(x, oc, sm))) / (2 * h))
+            an.append(dsh[t, a])
+    fd, an = np.array(fd), np.array(an)
+    scale = np.abs(fd).max()
+    err = np.abs(fd - an) / scale
+    print(f"[adjoint] central differences: {len(fd)} points, max |fd - adjoint| / max|fd| = {err.max():.2e}")
+    assert err.max() < 5e-3
+    assert np.median(np.abs(fd - an) / np.maximum(np.abs(fd), 1e-12 * scale)) < 1e-2
