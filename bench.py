@@ -185,6 +185,142 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def measure_batching(ctx, steps: int) -> dict:
+    """Batching workload: 50 volumes of 160^3 u16 (3000 filament emitters) cut by
+    doSplit.m's rule into 29^3 blocks with a 1-voxel overlap (216 blocks, edge
+    blocks 25 voxels), magnification 3, temporal mean. One persistent launch over
+    all blocks and volumes (device buffers, and through the C-ABI with pinned
+    host buffers) against the plain path: one launch per block with that block's
+    host->device and device->host copies."""
+    import torch
+    from rfba_gb300 import srrf, synth
+    x, _ = synth.workload("batching", shape=(160, 160, 160))
+    cfg = srrf.Config.make(mag=3, method=1, gradient_smooth=1, main_range=1, x_range=1, y_range=1, z_range=1)
+    blocks, n, oe = srrf.blocks_dosplit(cfg, x.shape, 29, 1)
+    units = oe * x.shape[0]
+    xd = torch.from_numpy(x.view(np.int16)).cuda()
+    outd = torch.empty(oe, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(2):
+        ctx.forward_blocks(cfg, xd, blocks, n, oe, out=outd, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        ctx.forward_blocks(cfg, xd, blocks, n, oe, out=outd, stream=stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    dev_ms = e0.elapsed_time(e1) / steps
+    pin_in = torch.empty(x.nbytes, dtype=torch.uint8).pin_memory().numpy().view(np.uint16).reshape(x.shape)
+    pin_in[...] = x
+    pin_out = torch.empty(oe, dtype=torch.float32).pin_memory().numpy()
+    ctx.forward_blocks(cfg, pin_in, blocks, n, oe, out=pin_out)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        ctx.forward_blocks(cfg, pin_in, blocks, n, oe, out=pin_out)
+    e2e_ms = (time.perf_counter() - t0) / steps * 1e3
+    plain_out = np.zeros(oe, np.float32)
+    ctx.forward_blocks_plain(cfg, x, blocks, n, oe, out=plain_out)  # warm
+    t0 = time.perf_counter()
+    ctx.forward_blocks_plain(cfg, x, blocks, n, oe, out=plain_out)
+    plain_ms = (time.perf_counter() - t0) * 1e3
+    same = bool(np.array_equal(np.nan_to_num(plain_out), np.nan_to_num(pin_out)) and
+                np.array_equal(np.isnan(plain_out), np.isnan(pin_out)))
+    sizes = sorted({tuple(blocks[i].size) for i in range(n)})
+    return {"workload": "batching: 50 x 160^3 u16, doSplit 29/1 -> %d blocks (edges %s), mag 3, temporal mean" % (
+        n, sorted({s[0] for s in sizes})),
+        "voxel_volumes": units, "batched_device_ms": dev_ms, "batched_e2e_ms": e2e_ms, "plain_per_block_ms": plain_ms,
+        "batched_device_value": units / (dev_ms / 1e3), "batched_e2e_value": units / (e2e_ms / 1e3),
+        "plain_value": units / (plain_ms / 1e3), "speedup_e2e_vs_plain": plain_ms / e2e_ms,
+        "speedup_device_vs_plain": plain_ms / dev_ms, "batched_equals_plain": same}
+
+
+def measure_diff(ctx, steps: int, iters: int = 20, volumes=None) -> dict:
+    """Differentiation workload: 60 volumes of 64^3 float32 (300 emitters) with a
+    random-walk drift (sigma 0.15 voxel per step) applied by Catmull-Rom
+    resampling; forward = drift correction + SRRF at magnification 2, TRAC-2
+    (ITC 0); objective L = -||map||_2. Times forward and forward+adjoint with CUDA
+    events, then runs gradient descent on L over the 60 x 3 shifts."""
+    import torch
+    from rfba_gb300 import srrf, synth
+    x, scene = synth.workload("diff", n_vol=volumes)
+    cfg = srrf.Config.make(mag=2, method=3, itc=0, trac_order=2, gradient_smooth=1, main_range=1, x_range=1,
+                           y_range=1, z_range=1)
+    T = x.shape[0]
+    xd = torch.from_numpy(x).cuda()
+    sh = torch.zeros((T, 3), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    units = x.shape[1] * x.shape[2] * x.shape[3] * 8 * T
+
+    def objective(m):
+        f = torch.nan_to_num(m, nan=0.0).double()
+        return -torch.sqrt((f * f).sum())
+
+    def grad_map(m):
+        f = torch.nan_to_num(m, nan=0.0)
+        return torch.where(torch.isnan(m), torch.zeros_like(m), -f / torch.sqrt((f.double() ** 2).sum()).float())
+
+    m = ctx.forward_shifted(cfg, xd, sh, stream=stream.cuda_stream)
+    g = grad_map(m)
+    ctx.backward(cfg, xd, sh, g, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    e0.record(stream)
+    for _ in range(steps):
+        m = ctx.forward_shifted(cfg, xd, sh, out=m, stream=stream.cuda_stream)
+    e1.record(stream)
+    for _ in range(steps):
+        m = ctx.forward_shifted(cfg, xd, sh, out=m, stream=stream.cuda_stream)
+        g = grad_map(m)
+        ctx.backward(cfg, xd, sh, g, stream=stream.cuda_stream)
+    e2.record(stream)
+    torch.cuda.synchronize()
+    fwd_ms = e0.elapsed_time(e1) / steps
+    fwdadj_ms = e1.elapsed_time(e2) / steps
+    # drift refinement by gradient descent on L (normalised steps, decaying)
+    truth = -torch.from_numpy(scene.drift.astype(np.float32)).cuda()
+
+    def rms(d):
+        e = d - truth
+        e = e - e.mean(0, keepdim=True)  # a common shift of all volumes leaves L unchanged
+        return float(torch.sqrt((e * e).mean()))
+
+    rms0 = rms(sh)
+    L0 = float(objective(ctx.forward_shifted(cfg, xd, sh)))
+    lr = 0.08
+    t0 = time.perf_counter()
+    for it in range(iters):
+        m = ctx.forward_shifted(cfg, xd, sh, out=m, stream=stream.cuda_stream)
+        _, gs = ctx.backward(cfg, xd, sh, grad_map(m), stream=stream.cuda_stream)
+        step = gs / (gs.abs().max() + 1e-30)
+        sh = sh - lr * step
+        lr *= 0.9
+    torch.cuda.synchronize()
+    it_ms = (time.perf_counter() - t0) / iters * 1e3
+    L1 = float(objective(ctx.forward_shifted(cfg, xd, sh)))
+    return {"workload": "diff: 60 x 64^3 f32 with random-walk drift, mag 2, TRAC-2 ITC0, L = -||map||",
+            "voxel_volumes": units, "forward_ms": fwd_ms, "forward_adjoint_ms": fwdadj_ms,
+            "fwd_adj_over_fwd": fwdadj_ms / fwd_ms, "refine_iterations": iters, "refine_ms_per_iteration": it_ms,
+            "objective_before": L0, "objective_after": L1, "drift_rms_error_before": rms0,
+            "drift_rms_error_after": rms(sh)}
+
+
+def run_single_workload(args):
+    """One of the secondary measurements alone, printed as its own JSON line."""
+    import torch
+    from rfba_gb300 import build as B
+    B.build()
+    from rfba_gb300 import srrf
+    torch.cuda.set_device(0)
+    ctx = srrf.Context(0)
+    if args.workload == "batching":
+        r = measure_batching(ctx, max(2, args.steps))
+    else:
+        r = measure_diff(ctx, max(3, args.steps), iters=args.iters, volumes=args.volumes)
+    ctx.close()
+    print(json.dumps({"workload": args.workload, **r}), flush=True)
+
+
 def run_gpu(args):
     import torch
     ws, rank, local = dist_env()
@@ -304,6 +440,9 @@ def run_gpu(args):
                                   f"measured max SM clock {sm_max:.0f} MHz"},
         "direct_equivalent_tflops": fl["direct_distinct"] * units_per_step / (rad_avg_ms / 1e3) / 1e12,
     }
+    if rank == 0 and not args.no_extras:
+        line["batching"] = measure_batching(ctx, max(2, args.steps // 2))
+        line["differentiation"] = measure_diff(ctx, max(3, args.steps))
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(x)
     ctx.close()
@@ -321,13 +460,20 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the batching (blocks vs plain) and differentiation (fwd+adj) measurements")
     ap.add_argument("--volumes", type=int, default=None,
-                    help="fewer volumes than the workload's 100 (profiling case only)")
+                    help="fewer volumes than the workload's (profiling case only)")
+    ap.add_argument("--iters", type=int, default=20, help="drift refinement iterations (diff workload)")
+    ap.add_argument("--workload", default="mid", choices=["mid", "batching", "diff"],
+                    help="mid: the headline line; batching / diff: that measurement alone (one JSON line)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload != "mid":
+        run_single_workload(args)
     else:
         run_gpu(args)
 

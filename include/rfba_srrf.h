@@ -134,8 +134,10 @@ int rfba_srrf_config_load_ini(const char* path, rfba_srrf_config* cfg); /* Gradi
 int rfba_srrf_config_from_legacy(const SRRFConf* conf, rfba_srrf_config* cfg);
 
 /* Whole volume as one block: out is the full magnified grid [D*mz][H*my][W*mx].
- * dims = {W, H, D, T}. stream is a cudaStream_t (NULL = legacy default stream);
- * with RFBA_HOST_PTRS the call returns when out is written. */
+ * dims = {W, H, D, T}. stream is a cudaStream_t (NULL = the legacy default
+ * stream, as everywhere in CUDA); with RFBA_HOST_PTRS the call returns when out
+ * is written. Calls on one context share its scratch: a call on another stream
+ * than the previous call is ordered after that call's work. */
 int rfba_srrf_forward(rfba_ctx* ctx, const rfba_srrf_config* cfg, const void* in, rfba_dtype dtype,
                       const int dims[4], float* out, int ptr_flags, void* stream);
 
@@ -165,7 +167,7 @@ int rfba_srrf_forward_blocks_plain(rfba_ctx* ctx, const rfba_srrf_config* cfg, c
  * RFBA_ERR_UNSUPPORTED and a message. The first call on a device looks the
  * array up (cudaGetSymbolAddress) and should come before any stream capture.
  * All calls share the array: calls that overlap on the GPU race, so serialise
- * them. Stream-ordered on `stream` (a cudaStream_t, NULL = legacy default). */
+ * them. Stream-ordered on `stream` (a cudaStream_t, NULL = the legacy default stream). */
 int rfba_srrf_forward_static_scratch(const rfba_srrf_config* cfg, const void* in, rfba_dtype dtype,
                                      const int dims[4], float* out, void* stream);
 

@@ -50,6 +50,14 @@ struct IntC {
     static constexpr int value = V;
 };
 
+// Bounds check of a computed global index: out of range records the first
+// offence (site in the top byte, index below) and the access is skipped.
+__device__ __forceinline__ bool in_range(long long i, long long n, unsigned long long* err, int site) {
+    if (i >= 0 && i < n) return true;
+    if (err) atomicCAS(err, 0ull, ((unsigned long long)site << 56) | ((unsigned long long)i & 0x00ffffffffffffffull));
+    return false;
+}
+
 // Catmull-Rom kernel and its derivative (a = 0.5), kernel.cu:128-138.
 __device__ __forceinline__ float cr(float xx) {
     const float a = 0.5f;
@@ -71,7 +79,7 @@ __device__ __forceinline__ float dcr(float xx) {
 // weights, mode 2 applies the transpose (gather over the outputs whose clamped
 // taps hit each input position).
 __global__ void shift_axis_kernel(const float* __restrict__ src, float* __restrict__ dst, int W, int H, int D, int T,
-                                  int axis, const float* __restrict__ shifts, int mode) {
+                                  int axis, const float* __restrict__ shifts, int mode, unsigned long long* err) {
     const long long n = (long long)W * H * D * T;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const int x = (int)(i % W);
@@ -91,7 +99,8 @@ __global__ void shift_axis_kernel(const float* __restrict__ src, float* __restri
             for (int k = -1; k <= 2; ++k) {
                 const int ii = clampi(base + k, 0, len - 1);
                 const float u = pos - (float)(base + k);
-                acc = fmaf(mode == 1 ? dcr(u) : cr(u), src[line + ii * stride], acc);
+                const long long si = line + ii * stride;
+                if (in_range(si, n, err, 1)) acc = fmaf(mode == 1 ? dcr(u) : cr(u), src[si], acc);
             }
         } else {
             // outputs x whose taps floor(x + d) - 1 .. + 2, clamped, include c
@@ -107,7 +116,8 @@ __global__ void shift_axis_kernel(const float* __restrict__ src, float* __restri
 #pragma unroll
                 for (int k = -1; k <= 2; ++k)
                     if (clampi(base + k, 0, len - 1) == c) w += cr(pos - (float)(base + k));
-                if (w != 0.f) acc = fmaf(w, src[line + xo * stride], acc);
+                const long long si = line + xo * stride;
+                if (w != 0.f && in_range(si, n, err, 2)) acc = fmaf(w, src[si], acc);
             }
         }
         dst[i] = acc;
@@ -116,7 +126,7 @@ __global__ void shift_axis_kernel(const float* __restrict__ src, float* __restri
 
 // dL/dd[t][axis] = sum over volume t of g[t] * dv[t] (double accumulation).
 __global__ void drift_dot_kernel(const float* __restrict__ g, const float* __restrict__ dv, long long nv, int axis,
-                                 double* __restrict__ out) {
+                                 double* __restrict__ out, unsigned long long* err) {
     const int t = blockIdx.y;
     const float* gt = g + (long long)t * nv;
     const float* dt = dv + (long long)t * nv;
@@ -138,14 +148,17 @@ __global__ void drift_dot_kernel(const float* __restrict__ g, const float* __res
 __global__ void temporal_adjoint_kernel(const BlockDev* __restrict__ blocks, const float* __restrict__ rad,
                                         const float* __restrict__ inten, const float* __restrict__ gmap, int T,
                                         int method, int order, int iw, int renorm, int poscon,
-                                        float* __restrict__ gS, float* __restrict__ gI) {
+                                        float* __restrict__ gS, float* __restrict__ gI, long long nmap,
+                                        unsigned long long* err) {
     const BlockDev& B = blocks[0];
     const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= B.vox) return;
     const long long V = B.vox;
     const long long nx = B.nreg[0], ny = B.nreg[1];
     const long long x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
-    const float g = gmap[B.out_offset + x * B.out_stride[0] + y * B.out_stride[1] + z * B.out_stride[2]];
+    const long long gidx = B.out_offset + x * B.out_stride[0] + y * B.out_stride[1] + z * B.out_stride[2];
+    if (!in_range(gidx, nmap, err, 5)) return;
+    const float g = gmap[gidx];
     const float* r = rad + v;
     const float* I = inten + v;
     // first pass: sums
@@ -361,8 +374,10 @@ __global__ void __launch_bounds__(128, 2) radiality_adjoint_kernel(const RadPara
                 const int bz = clampi(cz0 - R + iz, 0, bd - 1);
                 const long long rowg = tbase + ((long long)(B.origin[2] + bz) * p.H + (B.origin[1] + by)) * p.W +
                                        B.origin[0];
-                for (int ix = xf; ix < NIX; ix += kTileX)
-                    inp[r * NIX + ix] = __ldg(in + rowg + clampi(cx0 - R + ix, 0, bw - 1));
+                for (int ix = xf; ix < NIX; ix += kTileX) {
+                    const long long gi = rowg + clampi(cx0 - R + ix, 0, bw - 1);
+                    inp[r * NIX + ix] = in_range(gi, a.n_in, a.err, 8) ? __ldg(in + gi) : 0.f;
+                }
             }
             __syncthreads();
             for (int c = tid; c < ncell; c += nthr) {
@@ -390,10 +405,12 @@ __global__ void __launch_bounds__(128, 2) radiality_adjoint_kernel(const RadPara
                 const int Z = Z0 + z;
                 const bool zin = Z >= B.lo[2] && Z < B.hi[2];
                 const long long zo = sbase + (long long)(Z - B.lo[2]) * zstride;
-                gS[z].x = (zin && ina) ? a.gS[zo + va] : 0.f;
-                gS[z].y = (zin && inb) ? a.gS[zo + vb] : 0.f;
-                gI[z].x = (zin && ina) ? a.gI[zo + va] : 0.f;
-                gI[z].y = (zin && inb) ? a.gI[zo + vb] : 0.f;
+                const bool oka = zin && ina && in_range(zo + va, a.n_stack, a.err, 9);
+                const bool okb = zin && inb && in_range(zo + vb, a.n_stack, a.err, 9);
+                gS[z].x = oka ? a.gS[zo + va] : 0.f;
+                gS[z].y = okb ? a.gS[zo + vb] : 0.f;
+                gI[z].x = oka ? a.gI[zo + va] : 0.f;
+                gI[z].y = okb ? a.gI[zo + vb] : 0.f;
             }
 
             for (int gi_ = 0; gi_ < p.ngroups; ++gi_) {
@@ -621,7 +638,7 @@ __global__ void __launch_bounds__(128, 2) radiality_adjoint_kernel(const RadPara
                     const int bz = clampi(cz0 - R + iz, 0, bd - 1);
                     const long long gidx = tbase + ((long long)(B.origin[2] + bz) * p.H + (B.origin[1] + by)) * p.W +
                                            (B.origin[0] + bx);
-                    atomicAdd(a.gin + gidx, acc);
+                    if (in_range(gidx, a.n_in, a.err, 10)) atomicAdd(a.gin + gidx, acc);
                 }
             }
         }
@@ -689,20 +706,20 @@ int radiality_adjoint_max_ctas_per_sm(const RadParams& p, int* out) {
 
 int launch_temporal_adjoint(const BlockDev* blocks, long long vox, const float* rad, const float* inten,
                             const float* gmap, int T, int method, int order, int iw, int renorm, int poscon, float* gS,
-                            float* gI, void* stream) {
+                            float* gI, long long nmap, unsigned long long* err, void* stream) {
     if (vox == 0) return 0;
     const long long grid = (vox + 127) / 128;
     temporal_adjoint_kernel<<<(unsigned)grid, 128, 0, static_cast<cudaStream_t>(stream)>>>(
-        blocks, rad, inten, gmap, T, method, order, iw, renorm, poscon, gS, gI);
+        blocks, rad, inten, gmap, T, method, order, iw, renorm, poscon, gS, gI, nmap, err);
     return (int)cudaGetLastError();
 }
 
 int launch_shift_axis(const float* src, float* dst, int W, int H, int D, int T, int axis, const float* shifts, int mode,
-                      void* stream) {
+                      unsigned long long* err, void* stream) {
     const long long n = (long long)W * H * D * T;
     const long long grid = std::min<long long>((n + 255) / 256, 152LL * 16);
     shift_axis_kernel<<<(unsigned)grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(src, dst, W, H, D, T, axis,
-                                                                                     shifts, mode);
+                                                                                     shifts, mode, err);
     return (int)cudaGetLastError();
 }
 
@@ -719,9 +736,10 @@ int launch_double_to_float(const double* src, float* dst, int n, void* stream) {
     return (int)cudaGetLastError();
 }
 
-int launch_drift_dot(const float* g, const float* dv, long long nv, int T, int axis, double* out, void* stream) {
+int launch_drift_dot(const float* g, const float* dv, long long nv, int T, int axis, double* out,
+                     unsigned long long* err, void* stream) {
     dim3 grid((unsigned)std::min<long long>((nv + 255) / 256, 64), (unsigned)T);
-    drift_dot_kernel<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(g, dv, nv, axis, out);
+    drift_dot_kernel<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(g, dv, nv, axis, out, err);
     return (int)cudaGetLastError();
 }
 

@@ -33,6 +33,17 @@ int blocks_dosplit(const rfba_srrf_config& c, const int dims[4], const int max_s
 static thread_local std::string g_last_error;
 void set_error(const std::string& msg) { g_last_error = msg; }
 
+// RFBA_CHECKS=1: the differentiable path reads back its kernels' bounds checks
+// after each call (synchronising) and fails on an out-of-range index.
+static bool checks_enabled() {
+    static int v = -1;
+    if (v < 0) {
+        const char* e = std::getenv("RFBA_CHECKS");
+        v = (e && *e && *e != '0') ? 1 : 0;
+    }
+    return v == 1;
+}
+
 static bool verbose() {
     static int v = -1;
     if (v < 0) {
@@ -53,13 +64,17 @@ static int cuda_fail(cudaError_t e, const char* what) {
         if (e__ != cudaSuccess) return cuda_fail(e__, what); \
     } while (0)
 
-// Device buffer that grows and is kept.
+// Device buffer that grows and is kept. Growing waits for all queued work
+// first, since kernels of earlier calls may still read the old allocation.
 struct DevBuf {
     void* p = nullptr;
     size_t n = 0;
     int ensure(size_t bytes, const char* what) {
         if (bytes <= n) return RFBA_OK;
-        if (p) cudaFree(p);
+        if (p) {
+            cudaDeviceSynchronize();
+            cudaFree(p);
+        }
         p = nullptr;
         n = 0;
         size_t want = std::max(bytes, (size_t)256);
@@ -100,6 +115,11 @@ struct rfba_ctx {
     rfba::PlanCache plan;
     bool timing = false;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // calls share the scratch: a call on another stream than the previous call
+    // first waits for that call's work
+    cudaEvent_t xev = nullptr;
+    cudaStream_t last_stream = nullptr;
+    bool have_last = false;
     double last_rad_ms = 0.0, last_temporal_ms = 0.0;
     long long launches = 0;
     long long last_flop_units = 0;  // subvoxel-time-points computed by the last call
@@ -107,7 +127,7 @@ struct rfba_ctx {
     int chunk_override = 0;         // time points per work item (0 = automatic)
     int last_passes = 0;            // passes of the last forward (1 = its stacks are all resident)
     // differentiable path: buffers and the forward the backward can reuse
-    rfba::DevBuf shifted, tmp1, tmp2, gS, gI, gin, dshift, ablocks, atiles, acounter;
+    rfba::DevBuf shifted, tmp1, tmp2, gS, gI, gin, dshift, ablocks, atiles, acounter, errw;
     struct Train {
         bool valid = false;
         rfba_srrf_config cfg;
@@ -128,6 +148,7 @@ static int ctx_init(rfba_ctx* c, int device, size_t budget) {
     RFBA_CUDA(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device), "SM count");
     RFBA_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
     for (auto& e : c->ev) RFBA_CUDA(cudaEventCreate(&e), "event");
+    RFBA_CUDA(cudaEventCreateWithFlags(&c->xev, cudaEventDisableTiming), "event");
     if (budget == 0) {
         size_t fr = 0, tot = 0;
         RFBA_CUDA(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
@@ -162,7 +183,7 @@ static int default_ctx(rfba_ctx** out) {
     return RFBA_OK;
 }
 
-static int ensure_plan(rfba_ctx* ctx, const rfba_srrf_config& cfg) {
+static int ensure_plan(rfba_ctx* ctx, const rfba_srrf_config& cfg, cudaStream_t st) {
     PlanCache& P = ctx->plan;
     if (P.valid && P.ring_radius == cfg.ring_radius && P.axes == cfg.axes_in_ring && P.mag[0] == cfg.mag[0] &&
         P.mag[1] == cfg.mag[1] && P.mag[2] == cfg.mag[2])
@@ -178,9 +199,10 @@ static int ensure_plan(rfba_ctx* ctx, const rfba_srrf_config& cfg) {
         set_error("ring has no (0, 0) pair");
         return RFBA_ERR_UNSUPPORTED;
     }
-    int st = ctx->tables.ensure(P.words.size() * 4, "tables");
-    if (st) return st;
-    RFBA_CUDA(cudaMemcpy(ctx->tables.p, P.words.data(), P.words.size() * 4, cudaMemcpyHostToDevice), "tables upload");
+    const int rc = ctx->tables.ensure(P.words.size() * 4, "tables");
+    if (rc) return rc;
+    RFBA_CUDA(cudaMemcpyAsync(ctx->tables.p, P.words.data(), P.words.size() * 4, cudaMemcpyHostToDevice, st),
+              "tables upload");
     P.ring_radius = cfg.ring_radius;
     P.axes = cfg.axes_in_ring;
     for (int a = 0; a < 3; ++a) P.mag[a] = cfg.mag[a];
@@ -189,6 +211,17 @@ static int ensure_plan(rfba_ctx* ctx, const rfba_srrf_config& cfg) {
 }
 
 static int fz_for(int mz) { return mz * cz_for_mag(mz); }
+
+// Order this call's work after the previous call's when the streams differ.
+static int order_streams(rfba_ctx* ctx, cudaStream_t st) {
+    if (ctx->have_last && ctx->last_stream != st) {
+        RFBA_CUDA(cudaEventRecord(ctx->xev, ctx->last_stream), "stream order event");
+        RFBA_CUDA(cudaStreamWaitEvent(st, ctx->xev, 0), "stream order wait");
+    }
+    ctx->last_stream = st;
+    ctx->have_last = true;
+    return RFBA_OK;
+}
 
 // Turn caller blocks into device block descriptors, splitting regions along z
 // so that one pass's radiality + intensity stack fits the scratch budget.
@@ -481,7 +514,8 @@ static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, con
         return RFBA_ERR_INVALID;
     }
     RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
-    if ((s = ensure_plan(ctx, *cfg))) return s;
+    if ((s = order_streams(ctx, st))) return s;
+    if ((s = ensure_plan(ctx, *cfg, st))) return s;
     std::vector<BlockDev> all;
     if ((s = make_blocks(ctx, *cfg, dims, blocks, nblocks, &all))) return s;
     for (const BlockDev& b : all) {
@@ -535,12 +569,28 @@ static int apply_drift(rfba_ctx* ctx, const float* in, const float* shifts, cons
     float* t1 = static_cast<float*>(ctx->tmp1.p);
     float* t2 = static_cast<float*>(ctx->tmp2.p);
     float* out = static_cast<float*>(ctx->shifted.p);
-    int e = launch_shift_axis(in, t1, dims[0], dims[1], dims[2], dims[3], 0, shifts, 0, st);
-    if (!e) e = launch_shift_axis(t1, t2, dims[0], dims[1], dims[2], dims[3], 1, shifts, 0, st);
-    if (!e) e = launch_shift_axis(t2, out, dims[0], dims[1], dims[2], dims[3], 2, shifts, 0, st);
+    unsigned long long* err = static_cast<unsigned long long*>(ctx->errw.p);
+    int e = launch_shift_axis(in, t1, dims[0], dims[1], dims[2], dims[3], 0, shifts, 0, err, st);
+    if (!e) e = launch_shift_axis(t1, t2, dims[0], dims[1], dims[2], dims[3], 1, shifts, 0, err, st);
+    if (!e) e = launch_shift_axis(t2, out, dims[0], dims[1], dims[2], dims[3], 2, shifts, 0, err, st);
     if (e) return cuda_fail((cudaError_t)e, "drift resampling");
     ctx->launches += 3;
     *iprime = out;
+    return RFBA_OK;
+}
+
+static int read_checks(rfba_ctx* ctx, cudaStream_t st, const char* what) {
+    if (!checks_enabled() || !ctx->errw.p) return RFBA_OK;
+    unsigned long long w = 0;
+    RFBA_CUDA(cudaMemcpyAsync(&w, ctx->errw.p, 8, cudaMemcpyDeviceToHost, st), "check word read");
+    RFBA_CUDA(cudaStreamSynchronize(st), "check word sync");
+    if (w) {
+        char buf[160];
+        std::snprintf(buf, sizeof buf, "%s: out-of-range global index %llu at check site %llu", what,
+                      w & 0x00ffffffffffffffull, w >> 56);
+        set_error(buf);
+        return RFBA_ERR_CUDA;
+    }
     return RFBA_OK;
 }
 
@@ -549,6 +599,9 @@ static int forward_shifted_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, co
     int s = validate_common(cfg, in, dims, out);
     if (s) return s;
     RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if ((s = order_streams(ctx, st))) return s;
+    if ((s = ctx->errw.ensure(256, "check word"))) return s;
+    RFBA_CUDA(cudaMemsetAsync(ctx->errw.p, 0, 8, st), "check word clear");
     const float* ip = nullptr;
     if ((s = apply_drift(ctx, in, shifts, dims, st, &ip))) return s;
     rfba_block b;
@@ -579,7 +632,7 @@ static int forward_shifted_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, co
             ctx->train.blk.stack_off = 0;
         }
     }
-    return RFBA_OK;
+    return read_checks(ctx, st, "forward_shifted");
 }
 
 static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* in, const float* shifts,
@@ -595,6 +648,7 @@ static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const flo
         return RFBA_ERR_UNSUPPORTED;
     }
     RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if ((s = order_streams(ctx, st))) return s;
     const bool reuse = ctx->train.valid && same_cfg(ctx->train.cfg, *cfg) && ctx->train.in == in &&
                        ctx->train.shifts == shifts && ctx->train.dims[0] == dims[0] && ctx->train.dims[1] == dims[1] &&
                        ctx->train.dims[2] == dims[2] && ctx->train.dims[3] == dims[3];
@@ -608,7 +662,7 @@ static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const flo
             return RFBA_ERR_UNSUPPORTED;
         }
     }
-    if ((s = ensure_plan(ctx, *cfg))) return s;
+    if ((s = ensure_plan(ctx, *cfg, st))) return s;
     const int T = dims[3];
     const size_t nin = (size_t)dims[0] * dims[1] * dims[2] * T;
     BlockDev blk = ctx->train.blk;
@@ -632,9 +686,13 @@ static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const flo
     float* gS = static_cast<float*>(ctx->gS.p);
     float* gI = static_cast<float*>(ctx->gI.p);
     float* gin = static_cast<float*>(ctx->gin.p);
+    if ((s = ctx->errw.ensure(256, "check word"))) return s;
+    unsigned long long* err = static_cast<unsigned long long*>(ctx->errw.p);
+    const long long nmap = (long long)dims[0] * cfg->mag[0] * dims[1] * cfg->mag[1] * dims[2] * cfg->mag[2];
     int e = launch_temporal_adjoint(dblk, V, static_cast<const float*>(ctx->rad.p),
                                     static_cast<const float*>(ctx->inten.p), gmap, T, cfg->method, cfg->trac_order,
-                                    cfg->intensity_w, cfg->renormalize == 1, cfg->remove_con == 1, gS, gI, st);
+                                    cfg->intensity_w, cfg->renormalize == 1, cfg->remove_con == 1, gS, gI, nmap, err,
+                                    st);
     if (e) return cuda_fail((cudaError_t)e, "temporal adjoint launch");
     RadParams rp = fill_rad_params(ctx, *cfg, ctx->train.iprime, dims, cza_for_mag(cfg->mag[2]));
     rp.blocks = dblk;
@@ -660,7 +718,7 @@ static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const flo
     rp.nchunks = (T + rp.t_chunk - 1) / rp.t_chunk;
     rp.nitems = (long long)rp.ntiles * rp.nchunks;
     const int grid = (int)std::max<long long>(1, std::min<long long>(slots, rp.nitems));
-    AdjParams ap{gS, gI, gin};
+    AdjParams ap{gS, gI, gin, (long long)nin, (long long)V * T, err};
     e = launch_radiality_adjoint(rp, ap, grid, smem, st);
     if (e) return cuda_fail((cudaError_t)e, "radiality adjoint launch");
     ctx->launches += 2;
@@ -668,9 +726,9 @@ static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const flo
     if (shifts) {
         float* t1 = static_cast<float*>(ctx->tmp1.p);
         float* t2 = static_cast<float*>(ctx->tmp2.p);
-        e = launch_shift_axis(gin, t1, dims[0], dims[1], dims[2], T, 2, shifts, 2, st);
-        if (!e) e = launch_shift_axis(t1, t2, dims[0], dims[1], dims[2], T, 1, shifts, 2, st);
-        if (!e) e = launch_shift_axis(t2, din, dims[0], dims[1], dims[2], T, 0, shifts, 2, st);
+        e = launch_shift_axis(gin, t1, dims[0], dims[1], dims[2], T, 2, shifts, 2, err, st);
+        if (!e) e = launch_shift_axis(t1, t2, dims[0], dims[1], dims[2], T, 1, shifts, 2, err, st);
+        if (!e) e = launch_shift_axis(t2, din, dims[0], dims[1], dims[2], T, 0, shifts, 2, err, st);
         ctx->launches += 3;
         if (!e && dshift) {
             if ((s = ctx->dshift.ensure((size_t)T * 3 * sizeof(double), "drift adjoint"))) return s;
@@ -678,10 +736,10 @@ static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const flo
             RFBA_CUDA(cudaMemsetAsync(ds, 0, (size_t)T * 3 * sizeof(double), st), "drift adjoint clear");
             const long long nv = (long long)dims[0] * dims[1] * dims[2];
             for (int ax = 0; ax < 3 && !e; ++ax) {
-                e = launch_shift_axis(in, t1, dims[0], dims[1], dims[2], T, 0, shifts, ax == 0 ? 1 : 0, st);
-                if (!e) e = launch_shift_axis(t1, t2, dims[0], dims[1], dims[2], T, 1, shifts, ax == 1 ? 1 : 0, st);
-                if (!e) e = launch_shift_axis(t2, t1, dims[0], dims[1], dims[2], T, 2, shifts, ax == 2 ? 1 : 0, st);
-                if (!e) e = launch_drift_dot(gin, t1, nv, T, ax, ds, st);
+                e = launch_shift_axis(in, t1, dims[0], dims[1], dims[2], T, 0, shifts, ax == 0 ? 1 : 0, err, st);
+                if (!e) e = launch_shift_axis(t1, t2, dims[0], dims[1], dims[2], T, 1, shifts, ax == 1 ? 1 : 0, err, st);
+                if (!e) e = launch_shift_axis(t2, t1, dims[0], dims[1], dims[2], T, 2, shifts, ax == 2 ? 1 : 0, err, st);
+                if (!e) e = launch_drift_dot(gin, t1, nv, T, ax, ds, err, st);
                 ctx->launches += 4;
             }
             if (!e) e = launch_double_to_float(ds, dshift, 3 * T, st);
@@ -699,7 +757,7 @@ static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const flo
         cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[3]);
         ctx->last_backward_ms = ms;
     }
-    return RFBA_OK;
+    return read_checks(ctx, st, "backward");
 }
 
 }  // namespace rfba
@@ -715,7 +773,7 @@ int rfba_srrf_forward_shifted(rfba_ctx* ctx, const rfba_srrf_config* cfg, const 
         return RFBA_ERR_INVALID;
     }
     std::lock_guard<std::mutex> lk(ctx->mu);
-    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL = legacy default stream
     return forward_shifted_locked(ctx, cfg, in, shifts, dims, out, st);
 }
 
@@ -726,7 +784,7 @@ int rfba_srrf_backward(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* 
         return RFBA_ERR_INVALID;
     }
     std::lock_guard<std::mutex> lk(ctx->mu);
-    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL = legacy default stream
     return backward_locked(ctx, cfg, in, shifts, dims, dL_dmap, dL_din, dL_dshift, st);
 }
 
@@ -765,6 +823,7 @@ int rfba_ctx_destroy(rfba_ctx* c) {
         b->release();
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
+    if (c->xev) cudaEventDestroy(c->xev);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return RFBA_OK;
@@ -870,7 +929,7 @@ int rfba_srrf_forward_blocks(rfba_ctx* ctx, const rfba_srrf_config* cfg, const v
         set_error("null context");
         return RFBA_ERR_INVALID;
     }
-    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL = legacy default stream
     return forward_blocks_impl(ctx, cfg, in, dtype, dims, blocks, nblocks, out, out_elems, ptr_flags, st, false);
 }
 
@@ -890,7 +949,7 @@ int rfba_srrf_forward(rfba_ctx* ctx, const rfba_srrf_config* cfg, const void* in
     b.out_stride[1] = b.hi[0];
     b.out_stride[2] = (int64_t)b.hi[0] * b.hi[1];
     const int64_t n = (int64_t)b.hi[0] * b.hi[1] * b.hi[2];
-    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL = legacy default stream
     return forward_blocks_impl(ctx, cfg, in, dtype, dims, &b, 1, out, n, ptr_flags, st, false);
 }
 

@@ -127,6 +127,9 @@ struct AdjParams {
     const float* gS;  // dL/d(radiality before transforms) per subvoxel and time, [t][v]
     const float* gI;  // dL/d(interpolated intensity), [t][v]
     float* gin;       // dL/dI' accumulated, [t][z][y][x] of the full input
+    long long n_in;   // elements of the input / gin
+    long long n_stack;  // elements of gS / gI
+    unsigned long long* err;  // first out-of-range global index (site << 56 | index), 0 if none
 };
 
 // Launchers (radiality.cu / temporal.cu / adjoint.cu). Return a cudaError_t as int.
@@ -135,10 +138,11 @@ size_t radiality_adjoint_smem_bytes(const RadParams& p);
 int radiality_adjoint_max_ctas_per_sm(const RadParams& p, int* out);
 int launch_temporal_adjoint(const BlockDev* blocks, long long vox, const float* rad, const float* inten,
                             const float* gmap, int T, int method, int order, int iw, int renorm, int poscon, float* gS,
-                            float* gI, void* stream);
+                            float* gI, long long nmap, unsigned long long* err, void* stream);
 int launch_shift_axis(const float* src, float* dst, int W, int H, int D, int T, int axis, const float* shifts, int mode,
-                      void* stream);
-int launch_drift_dot(const float* g, const float* dv, long long nv, int T, int axis, double* out, void* stream);
+                      unsigned long long* err, void* stream);
+int launch_drift_dot(const float* g, const float* dv, long long nv, int T, int axis, double* out,
+                     unsigned long long* err, void* stream);
 int launch_double_to_float(const double* src, float* dst, int n, void* stream);
 int launch_radiality(const RadParams& p, int grid, size_t smem, int in_u16, void* stream);
 size_t radiality_smem_bytes(const RadParams& p);

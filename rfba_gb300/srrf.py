@@ -312,7 +312,7 @@ class Context:
             else:
                 out = np.empty(shape, np.float32)
         optr = ctypes.c_void_p(out.data_ptr() if dev else out.ctypes.data)
-        st = ctypes.c_void_p(stream) if stream else None
+        st = _stream_arg(stream, dev)
         _check(lib().rfba_srrf_forward(self.h, ctypes.byref(cfg), ptr, dt, _iptr(dims), optr,
                                        RFBA_DEVICE_PTRS if dev else RFBA_HOST_PTRS, st))
         return out
@@ -326,7 +326,7 @@ class Context:
             else:
                 out = np.zeros(out_elems, np.float32)
         optr = ctypes.c_void_p(out.data_ptr() if dev else out.ctypes.data)
-        st = ctypes.c_void_p(stream) if stream else None
+        st = _stream_arg(stream, dev)
         _check(lib().rfba_srrf_forward_blocks(self.h, ctypes.byref(cfg), ptr, dt, _iptr(dims), blocks, nblocks, optr,
                                               out_elems, RFBA_DEVICE_PTRS if dev else RFBA_HOST_PTRS, st))
         return out
@@ -340,7 +340,7 @@ class Context:
         if out is None:
             out = torch.empty((D * cfg.mag[2], H * cfg.mag[1], W * cfg.mag[0]), dtype=torch.float32, device=x.device)
         sp = ctypes.c_void_p(shifts.data_ptr()) if shifts is not None else None
-        st = ctypes.c_void_p(stream) if stream else None
+        st = _stream_arg(stream, True)
         _check(lib().rfba_srrf_forward_shifted(self.h, ctypes.byref(cfg), ctypes.c_void_p(x.data_ptr()), sp,
                                                _iptr(dims), ctypes.c_void_p(out.data_ptr()), st))
         return out
@@ -355,7 +355,7 @@ class Context:
             dshift = torch.empty_like(shifts)
         sp = ctypes.c_void_p(shifts.data_ptr()) if shifts is not None else None
         dsp = ctypes.c_void_p(dshift.data_ptr()) if dshift is not None else None
-        st = ctypes.c_void_p(stream) if stream else None
+        st = _stream_arg(stream, True)
         _check(lib().rfba_srrf_backward(self.h, ctypes.byref(cfg), ctypes.c_void_p(x.data_ptr()), sp, _iptr(dims),
                                         ctypes.c_void_p(dL_dmap.data_ptr()), ctypes.c_void_p(din.data_ptr()), dsp,
                                         st))
@@ -375,6 +375,19 @@ class Context:
         _check(lib().rfba_srrf_forward_blocks_plain(self.h, ctypes.byref(cfg), ptr, dt, _iptr(dims), blocks, nblocks,
                                                     ctypes.c_void_p(out.ctypes.data), out_elems))
         return out
+
+
+def _stream_arg(stream, device_tensors: bool):
+    """cudaStream_t for a call: the given handle, else torch's current stream
+    when the call works on CUDA tensors (so torch work on them stays ordered),
+    else the legacy default stream. Handle 0 is the legacy default stream."""
+    if stream is not None:
+        return ctypes.c_void_p(stream) if stream else None
+    if device_tensors:
+        import torch
+        h = torch.cuda.current_stream().cuda_stream
+        return ctypes.c_void_p(h) if h else None
+    return None
 
 
 def version() -> str:
