@@ -291,26 +291,71 @@ __device__ __forceinline__ float4 gradient_generic(const float* base, int NIX, i
     return make_float4(gx, gy, gz, I(0, 0, 0));
 }
 
+// Adjoint tile: 16 fine x columns x kAdjRows fine y rows x FZ fine z rows,
+// kAdjThreads threads. Warp k owns x columns 4k..4k+3; lane l of a warp takes
+// column 4k + (l & 3) and the fine rows 2 (l >> 2), 2 (l >> 2) + 1. All
+// threads that touch an x column's U-stage entries sit in one warp, so the
+// y-pass transpose needs no shared-memory atomics: the lanes of one column
+// whose 5-row windows start on the same row (possible when my > 2) add in
+// separate phases, and __syncwarp orders the row updates of lanes whose
+// windows overlap. The x pass and its transpose run one (z, y) row of cells
+// per thread with a sliding 4-cell window, so every cell has one writer.
+//
+// Shared-memory row strides are odd in float4 units (17 for the U stage, NU
+// rounded up to odd for the cell grid): threads walking different rows at the
+// same column, and the 4 columns x 8 row windows of a warp, hit all banks.
+constexpr int kURow = kTileX + 1;
+
+__host__ __device__ __forceinline__ int adj_nup(int NU) { return NU | 1; }
+__host__ __device__ __forceinline__ int adj_u_region_f4(int NV, int NW, int NIX, int NIY, int NIZ) {
+    const int ustage = 2 * kURow * (NV + 1) * NW;
+    const int inp = (NIX * NIY * NIZ + 3) / 4;
+    return ustage > inp ? ustage : inp;
+}
+
+// Division of 0 <= c < 65536 by d >= 2 with one multiply-high.
+struct FastDiv {
+    unsigned m;
+    __device__ explicit FastDiv(int d) : m(0xffffffffu / (unsigned)d + 1u) {}
+    __device__ int operator()(int c) const { return (int)__umulhi((unsigned)c, m); }
+};
+
+__device__ __forceinline__ float4 f4fma(float s, float4 a, float4 c) {
+    return make_float4(fmaf(s, a.x, c.x), fmaf(s, a.y, c.y), fmaf(s, a.z, c.z), fmaf(s, a.w, c.w));
+}
+__device__ __forceinline__ float4 f4add(float4 a, float4 b) {
+    return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+}
+
 template <int MZ, int CZ>
-__global__ void __launch_bounds__(128, 2) radiality_adjoint_kernel(const RadParams p, const AdjParams a) {
+__global__ void __launch_bounds__(kAdjThreads, 2) radiality_adjoint_kernel(const RadParams p, const AdjParams a) {
     constexpr int FZ = MZ * CZ;
     constexpr int NW = CZ + 4;
     extern __shared__ float4 smem4[];
-    const int NU = p.NU, NV = p.NV;
-    float4* gt = smem4;                       // forward G + I   [NW][NV][NU]
-    float4* ggt = gt + NU * NV * NW;          // dL/d(G, I)      [NW][NV][NU]
-    float4* ut = ggt + NU * NV * NW;          // forward U       [NW][NV][16]
-    float4* gut = ut + kTileX * NV * NW;      // dL/dU           [NW][NV][16]
-    float* inp = reinterpret_cast<float*>(gut + kTileX * NV * NW);
-    float* tab = inp + ((p.NIX * p.NIY * p.NIZ + 3) & ~3);
+    const int NU = p.NU, NV = p.NV, NVA = p.NV + 1, NUP = adj_nup(p.NU);
+    const int ncell = NUP * NV * NW;
+    const int nut = kURow * NVA * NW;
+    float4* gt = smem4;                    // forward G + I   [NW][NV][NUP]
+    float4* ggt = gt + ncell;              // dL/d(G, I)      [NW][NV][NUP]
+    float4* ut = ggt + ncell;              // forward U       [NW][NVA][kURow]; row NV is zero
+    float4* gut = ut + nut;                // dL/dU           [NW][NVA][kURow]
+    float* inp = reinterpret_cast<float*>(ut);  // input tile, dead once gt is built
+    float4* xw4 = ut + adj_u_region_f4(NV, NW, p.NIX, p.NIY, p.NIZ);  // x weights of the group [16]
+    int* xub = reinterpret_cast<int*>(xw4 + kTileX);                 // first tap cell of each x column [16]
+    float* tab = reinterpret_cast<float*>(xub + kTileX);
     __shared__ unsigned int s_item;
 
     const int nthr = blockDim.x;
     const int tid = threadIdx.x;
     const int mx = p.mag[0], my = p.mag[1];
-    const int xf = tid & (kTileX - 1);
-    const int q = tid / kTileX;
-    const int yfa = (q / my) * (2 * my) + (q % my);
+    const int lane = tid & 31;
+    const int xf = (tid >> 5) * 4 + (lane & 3);
+    const int tr = lane >> 2;
+    // lanes tr, tr' of one column with tr = tr' mod nph have rows >= my apart,
+    // hence different window starts
+    const int nph = (my + 1) >> 1;
+    const int myph = tr % nph;
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
 
     for (int i = tid; i < p.smem_table_words; i += nthr) tab[i] = p.tables[i];
     const float* wx = tab + p.tl.wx;
@@ -331,8 +376,7 @@ __global__ void __launch_bounds__(128, 2) radiality_adjoint_kernel(const RadPara
     const float* in = static_cast<const float*>(p.in);
     const int NIX = p.NIX, NIY = p.NIY, NIZ = p.NIZ, R = p.R;
     const int nin = NIX * NIY * NIZ;
-    const int ncell = NU * NV * NW;
-    const int nut = kTileX * NV * NW;
+    const FastDiv div_nup(NUP), div_nv(NV), div_nva(NVA), div_nix(NIX), div_niy(NIY), div_nixy(NIX * NIY);
 
     for (;;) {
         __syncthreads();
@@ -346,21 +390,21 @@ __global__ void __launch_bounds__(128, 2) radiality_adjoint_kernel(const RadPara
         const BlockDev& B = p.blocks[td.block];
         const int bw = B.size[0], bh = B.size[1], bd = B.size[2];
         const int X0 = B.lo[0] + td.tx * kTileX;
-        const int Y0 = B.lo[1] + td.ty * p.TY;
+        const int Y0 = B.lo[1] + td.ty * kAdjRows;
         const int Z0 = B.zbase + td.tz * FZ;
         const int cx0 = floordiv(X0, mx) - 2;
         const int cy0 = floordiv(Y0, my) - 2;
         const int cz0 = Z0 / MZ - 2;
         const int X = X0 + xf;
-        const int Ya = Y0 + yfa, Yb = Ya + my;
-        const int xi = floordiv(X, mx), xr = X - xi * mx;
-        const int yi = floordiv(Ya, my), yr = Ya - yi * my;
+        const int Ya = Y0 + 2 * tr, Yb = Ya + 1;
+        const int yia = floordiv(Ya, my), yra = Ya - yia * my;
+        const int yib = floordiv(Yb, my), yrb = Yb - yib * my;
         const bool xin = X < B.hi[0];
         const bool ina = xin && Ya < B.hi[1];
         const bool inb = xin && Yb < B.hi[1];
         const long long V = B.vox;
         const long long va = ((long long)(Ya - B.lo[1])) * B.nreg[0] + (X - B.lo[0]);
-        const long long vb = ((long long)(Yb - B.lo[1])) * B.nreg[0] + (X - B.lo[0]);
+        const long long vb = va + B.nreg[0];
         const long long zstride = (long long)B.nreg[0] * B.nreg[1];
         const int t0 = chunk * p.t_chunk;
         const int t1 = min(p.T, t0 + p.t_chunk);
@@ -369,24 +413,24 @@ __global__ void __launch_bounds__(128, 2) radiality_adjoint_kernel(const RadPara
             const long long tbase = (long long)t * p.D * p.H * p.W;
             // forward: input tile, gradient cells; clear the adjoint cells
             for (int r = tid / kTileX; r < NIY * NIZ; r += nthr / kTileX) {
-                const int iy = r % NIY, iz = r / NIY;
+                const int iz = div_niy(r), iy = r - iz * NIY;
                 const int by = clampi(cy0 - R + iy, 0, bh - 1);
                 const int bz = clampi(cz0 - R + iz, 0, bd - 1);
                 const long long rowg = tbase + ((long long)(B.origin[2] + bz) * p.H + (B.origin[1] + by)) * p.W +
                                        B.origin[0];
-                for (int ix = xf; ix < NIX; ix += kTileX) {
+                for (int ix = tid % kTileX; ix < NIX; ix += kTileX) {
                     const long long gi = rowg + clampi(cx0 - R + ix, 0, bw - 1);
                     inp[r * NIX + ix] = in_range(gi, a.n_in, a.err, 8) ? __ldg(in + gi) : 0.f;
                 }
             }
             __syncthreads();
             for (int c = tid; c < ncell; c += nthr) {
-                const int u = c % NU;
-                const int v = (c / NU) % NV;
-                const int w = c / (NU * NV);
+                const int row = div_nup(c);
+                const int u = c - row * NUP;
+                const int w = div_nv(row), v = row - w * NV;
                 const int cu = cx0 + u, cv = cy0 + v, cw = cz0 + w;
-                float4 g4 = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (cu >= 0 && cu < bw && cv >= 0 && cv < bh && cw >= 0 && cw < bd) {
+                float4 g4 = zero4;
+                if (u < NU && cu >= 0 && cu < bw && cv >= 0 && cv < bh && cw >= 0 && cw < bd) {
                     const float* base = inp + ((w + R) * NIY + (v + R)) * NIX + (u + R);
                     if (p.grad_mode == 1)
                         g4 = gradient_fixed<1, 1, 1, 1>(base, NIX, NIY);
@@ -396,10 +440,10 @@ __global__ void __launch_bounds__(128, 2) radiality_adjoint_kernel(const RadPara
                         g4 = gradient_generic(base, NIX, NIY, p.gr);
                 }
                 gt[c] = g4;
-                ggt[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+                ggt[c] = zero4;
             }
-            // dL/dS and dL/dI of this thread's subvoxels
-            float2 gS[FZ], gI[FZ];
+            // dL/dS of this thread's subvoxels (dL/dI is read in the (0, 0) pair)
+            float2 gS[FZ];
 #pragma unroll
             for (int z = 0; z < FZ; ++z) {
                 const int Z = Z0 + z;
@@ -409,54 +453,89 @@ __global__ void __launch_bounds__(128, 2) radiality_adjoint_kernel(const RadPara
                 const bool okb = zin && inb && in_range(zo + vb, a.n_stack, a.err, 9);
                 gS[z].x = oka ? a.gS[zo + va] : 0.f;
                 gS[z].y = okb ? a.gS[zo + vb] : 0.f;
-                gI[z].x = oka ? a.gI[zo + va] : 0.f;
-                gI[z].y = okb ? a.gI[zo + vb] : 0.f;
             }
 
             for (int gi_ = 0; gi_ < p.ngroups; ++gi_) {
-                __syncthreads();
+                __syncthreads();  // gt built / previous group's x transpose done with gut and the x tables
                 const int av = grp_xval[gi_];
-                const int ox = offx[av * mx + xr];
-                const float4 wxv = *reinterpret_cast<const float4*>(wx + (av * mx + xr) * 4);
-                const int ub = xi - cx0 - 2 + ox;
-                for (int e = tid; e < nut; e += nthr) {
-                    const int vw = e / kTileX;
-                    const float4* src = gt + vw * NU + ub;
-                    const float4 g0 = src[0], g1 = src[1], g2 = src[2], g3 = src[3];
-                    float4 r;
-                    r.x = fmaf(wxv.w, g3.x, fmaf(wxv.z, g2.x, fmaf(wxv.y, g1.x, wxv.x * g0.x)));
-                    r.y = fmaf(wxv.w, g3.y, fmaf(wxv.z, g2.y, fmaf(wxv.y, g1.y, wxv.x * g0.y)));
-                    r.z = fmaf(wxv.w, g3.z, fmaf(wxv.z, g2.z, fmaf(wxv.y, g1.z, wxv.x * g0.z)));
-                    r.w = 0.f;
-                    ut[e] = r;
-                    gut[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (tid < kTileX) {
+                    const int Xc = X0 + tid;
+                    const int xic = floordiv(Xc, mx), xrc = Xc - xic * mx;
+                    xub[tid] = xic - cx0 - 2 + offx[av * mx + xrc];
+                    xw4[tid] = *reinterpret_cast<const float4*>(wx + (av * mx + xrc) * 4);
+                }
+                for (int e = tid; e < nut; e += nthr) gut[e] = zero4;
+                __syncthreads();
+                // x pass, one (w, v) row per thread: U[xf] = sum_k wx_xf[k] G[ub(xf) + k];
+                // ub steps by 0 or 1 from one column to the next
+                for (int row = tid; row < NVA * NW; row += nthr) {
+                    const int w = div_nva(row), v = row - w * NVA;
+                    float4* dst = ut + row * kURow;
+                    if (v >= NV) {
+#pragma unroll
+                        for (int x = 0; x < kTileX; ++x) dst[x] = zero4;
+                        continue;
+                    }
+                    const float4* src = gt + (w * NV + v) * NUP;
+                    int ub = xub[0];
+                    float4 c0 = src[ub], c1 = src[ub + 1], c2 = src[ub + 2], c3 = src[ub + 3];
+#pragma unroll
+                    for (int x = 0; x < kTileX; ++x) {
+                        if (x > 0) {
+                            const int nb = xub[x];
+                            if (nb != ub) {
+                                ub = nb;
+                                c0 = c1;
+                                c1 = c2;
+                                c2 = c3;
+                                c3 = src[ub + 3];
+                            }
+                        }
+                        const float4 wk = xw4[x];
+                        float4 r;
+                        r.x = fmaf(wk.w, c3.x, fmaf(wk.z, c2.x, fmaf(wk.y, c1.x, wk.x * c0.x)));
+                        r.y = fmaf(wk.w, c3.y, fmaf(wk.z, c2.y, fmaf(wk.y, c1.y, wk.x * c0.y)));
+                        r.z = fmaf(wk.w, c3.z, fmaf(wk.z, c2.z, fmaf(wk.y, c1.z, wk.x * c0.z)));
+                        r.w = 0.f;
+                        dst[x] = r;
+                    }
                 }
                 __syncthreads();
                 for (int pi = grp[gi_]; pi < grp[gi_ + 1]; ++pi) {
                     const int b = pair_yval[pi];
-                    const int oy = offy[b * my + yr];
-                    const float4 wyv = *reinterpret_cast<const float4*>(wy + (b * my + yr) * 4);
-                    const int vbase = yi - cy0 - 2 + oy;
+                    const int sa = yia - cy0 - 2 + offy[b * my + yra];
+                    const int sb = yib - cy0 - 2 + offy[b * my + yrb];
+                    const bool sh = sb != sa;  // column b's taps start one row later
+                    const float4 wa = *reinterpret_cast<const float4*>(wy + (b * my + yra) * 4);
+                    const float4 wb = *reinterpret_cast<const float4*>(wy + (b * my + yrb) * 4);
+                    // (column a, column b) weights of rows sa .. sa + 4
+                    float2 w2[5];
+                    w2[0] = make_float2(wa.x, sh ? 0.f : wb.x);
+                    w2[1] = make_float2(wa.y, sh ? wb.x : wb.y);
+                    w2[2] = make_float2(wa.z, sh ? wb.y : wb.z);
+                    w2[3] = make_float2(wa.w, sh ? wb.z : wb.w);
+                    w2[4] = make_float2(0.f, sh ? wb.w : 0.f);
+                    const int r0 = sa * kURow + xf;
                     float2 Tx[NW], Ty[NW], Tz[NW];
 #pragma unroll
                     for (int w = 0; w < NW; ++w) {
-                        const float4* src = ut + (w * NV + vbase) * kTileX + xf;
-                        const float4 u0 = src[0], u1 = src[kTileX], u2 = src[2 * kTileX], u3 = src[3 * kTileX],
-                                     u4 = src[4 * kTileX];
-                        Tx[w].x = fmaf(wyv.w, u3.x, fmaf(wyv.z, u2.x, fmaf(wyv.y, u1.x, wyv.x * u0.x)));
-                        Ty[w].x = fmaf(wyv.w, u3.y, fmaf(wyv.z, u2.y, fmaf(wyv.y, u1.y, wyv.x * u0.y)));
-                        Tz[w].x = fmaf(wyv.w, u3.z, fmaf(wyv.z, u2.z, fmaf(wyv.y, u1.z, wyv.x * u0.z)));
-                        Tx[w].y = fmaf(wyv.w, u4.x, fmaf(wyv.z, u3.x, fmaf(wyv.y, u2.x, wyv.x * u1.x)));
-                        Ty[w].y = fmaf(wyv.w, u4.y, fmaf(wyv.z, u3.y, fmaf(wyv.y, u2.y, wyv.x * u1.y)));
-                        Tz[w].y = fmaf(wyv.w, u4.z, fmaf(wyv.z, u3.z, fmaf(wyv.y, u2.z, wyv.x * u1.z)));
+                        const float4* src = ut + w * NVA * kURow + r0;
+                        const float4 u0 = src[0], u1 = src[kURow], u2 = src[2 * kURow], u3 = src[3 * kURow],
+                                     u4 = src[4 * kURow];
+                        Tx[w].x = fmaf(wa.w, u3.x, fmaf(wa.z, u2.x, fmaf(wa.y, u1.x, wa.x * u0.x)));
+                        Ty[w].x = fmaf(wa.w, u3.y, fmaf(wa.z, u2.y, fmaf(wa.y, u1.y, wa.x * u0.y)));
+                        Tz[w].x = fmaf(wa.w, u3.z, fmaf(wa.z, u2.z, fmaf(wa.y, u1.z, wa.x * u0.z)));
+                        Tx[w].y = fmaf(w2[4].y, u4.x, fmaf(w2[3].y, u3.x, fmaf(w2[2].y, u2.x, fmaf(w2[1].y, u1.x, w2[0].y * u0.x))));
+                        Ty[w].y = fmaf(w2[4].y, u4.y, fmaf(w2[3].y, u3.y, fmaf(w2[2].y, u2.y, fmaf(w2[1].y, u1.y, w2[0].y * u0.y))));
+                        Tz[w].y = fmaf(w2[4].y, u4.z, fmaf(w2[3].y, u3.z, fmaf(w2[2].y, u2.z, fmaf(w2[1].y, u1.z, w2[0].y * u0.z))));
                     }
                     const float2 rot = pair_rot[pi];
-                    const float2 ca = dup(rot.x), sb = dup(rot.y), nsb = dup(-rot.y);
+                    const float2 ca = dup(rot.x), sb2 = dup(rot.y), nsb = dup(-rot.y);
 #pragma unroll
                     for (int w = 0; w < NW; ++w) {
                         const float2 gx = Tx[w], gy = Ty[w];
-                        Tx[w] = fma2(gy, sb, mul2(gx, ca));   // P
-                        Ty[w] = fma2(gy, ca, mul2(gx, nsb));  // E
+                        Tx[w] = fma2(gy, sb2, mul2(gx, ca));   // P
+                        Ty[w] = fma2(gy, ca, mul2(gx, nsb));   // E
                     }
                     float2 gP[NW], gE[NW], gZ[NW];
 #pragma unroll
@@ -465,7 +544,8 @@ __global__ void __launch_bounds__(128, 2) radiality_adjoint_kernel(const RadPara
                         const float4 pv = pt_vec[qi];
                         const float2 hh = dup(pv.x), cc = dup(pv.y), ncc = dup(-pv.y);
                         const float wgt = pv.z;
-                        const float2 nun = dup(pv.w);  // -|u|
+                        const float2 nun2 = dup(2.0f * pv.w);  // -2|u|
+                        const float2 nun = dup(pv.w);          // -|u|
                         const int zc = pt_zval[qi];
                         const float* wzc = wz + zc * (MZ * 4);
                         const int offmask = offz[zc];
@@ -489,22 +569,22 @@ __global__ void __launch_bounds__(128, 2) radiality_adjoint_kernel(const RadPara
                                 const float2 c2 = fma2(cp, cp, mul2(gy, gy));
                                 const float2 g2 = fma2(dot, dot, c2);
                                 const float2 xx = mul2(c2, g2);
-                                // inv = 1/(|g| |g_perp|), 0 where g is parallel to u (subgradient)
-                                float2 inv = make_float2(xx.x > 0.f ? rsqrt_approx(xx.x) : 0.f,
-                                                         xx.y > 0.f ? rsqrt_approx(xx.y) : 0.f);
-                                const float2 sn = mul2(c2, inv);                  // sin
-                                const float2 qg = mul2(mul2(inv, inv), c2);       // 1/|g|^2
-                                const float2 om = fma2(sn, nun, dup(1.0f));       // 1 - Dk/r
+                                // inv = 1/(|g| |g_perp|); where g is parallel to u (c2 = 0) every
+                                // product below carries a factor c2, cp or E and vanishes
+                                const float2 inv = make_float2(rsqrt_approx(fmaxf(xx.x, 1e-30f)),
+                                                               rsqrt_approx(fmaxf(xx.y, 1e-30f)));
+                                const float2 sn = mul2(c2, inv);                          // sin
+                                const float2 nsq = mul2(mul2(sn, inv), mul2(inv, mul2(c2, dup(-1.0f))));  // -sin/|g|^2
+                                const float2 om = fma2(sn, nun, dup(1.0f));               // 1 - Dk/r
                                 const float2 sw = make_float2(sign_weight(wgt, dot.x), sign_weight(wgt, dot.y));
                                 // dS/dsin = sw * 2 om * (-|u|), times dL/dS
-                                const float2 coef = mul2(mul2(mul2(sw, om), mul2(nun, dup(2.0f))), gS[z]);
-                                const float2 sq = mul2(sn, qg);
+                                const float2 coef = mul2(mul2(sw, om), mul2(nun2, gS[z]));
                                 const float2 ci = mul2(cp, inv);
                                 // d sin / d(P, E, Z) = g_perp/(|g||g_perp|) - sin g/|g|^2,
                                 // g_perp = (-c cp, E, h cp)
-                                const float2 dP = mul2(coef, fma2(ncc, ci, mul2(sq, make_float2(-gx.x, -gx.y))));
-                                const float2 dE = mul2(coef, fma2(gy, inv, mul2(sq, make_float2(-gy.x, -gy.y))));
-                                const float2 dZ = mul2(coef, fma2(hh, ci, mul2(sq, make_float2(-gz.x, -gz.y))));
+                                const float2 dP = mul2(coef, fma2(nsq, gx, mul2(ncc, ci)));
+                                const float2 dE = mul2(coef, mul2(gy, __fadd2_rn(inv, nsq)));
+                                const float2 dZ = mul2(coef, fma2(nsq, gz, mul2(hh, ci)));
 #pragma unroll
                                 for (int m = 0; m < 4; ++m) {
                                     gP[zi + o + m] = fma2(w4[m], dP, gP[zi + o + m]);
@@ -529,109 +609,164 @@ __global__ void __launch_bounds__(128, 2) radiality_adjoint_kernel(const RadPara
                     for (int w = 0; w < NW; ++w) {
                         const float2 P = gP[w], E = gE[w];
                         gP[w] = fma2(E, nsb, mul2(P, ca));
-                        gE[w] = fma2(E, ca, mul2(P, sb));
+                        gE[w] = fma2(E, ca, mul2(P, sb2));
                     }
                     // intensity at the subvoxel centre rides on the (0, 0) pair: z pass
-                    // transpose with rho_z = 0 (5 taps)
+                    // transpose with rho_z = 0 (5 taps) of dL/dI
                     float2 gW[NW];
 #pragma unroll
                     for (int w = 0; w < NW; ++w) gW[w] = make_float2(0.f, 0.f);
-                    const bool with_int = (pi == p.zero_pair);
-                    if (with_int) {
+                    if (pi == p.zero_pair) {
 #pragma unroll
                         for (int z = 0; z < FZ; ++z) {
+                            const int Z = Z0 + z;
+                            const bool zin = Z >= B.lo[2] && Z < B.hi[2];
+                            const long long zo = sbase + (long long)(Z - B.lo[2]) * zstride;
+                            const bool oka = zin && ina && in_range(zo + va, a.n_stack, a.err, 9);
+                            const bool okb = zin && inb && in_range(zo + vb, a.n_stack, a.err, 9);
+                            const float2 gi = make_float2(oka ? a.gI[zo + va] : 0.f, okb ? a.gI[zo + vb] : 0.f);
                             const int zr = z % MZ, zi = z / MZ;
                             const float* qz = wzi + zr * 5;
 #pragma unroll
                             for (int m = 0; m < 5; ++m)
-                                if (zi + m < NW) gW[zi + m] = fma2(dup(qz[m]), gI[z], gW[zi + m]);
+                                if (zi + m < NW) gW[zi + m] = fma2(dup(qz[m]), gi, gW[zi + m]);
                         }
                     }
-                    // y pass transpose: column a feeds rows vbase..+3, column b rows vbase+1..+4
+                    // y pass transpose: row sa + m of every z cell gets w2[m] . (column a, column b)
+                    for (int ph = 0; ph < nph; ++ph) {
+                        const bool act = myph == ph;
 #pragma unroll
-                    for (int w = 0; w < NW; ++w) {
-                        float4* dst = gut + (w * NV + vbase) * kTileX + xf;
-                        const float wk[4] = {wyv.x, wyv.y, wyv.z, wyv.w};
+                        for (int w = 0; w < NW; ++w) {
+                            float4* dst = gut + w * NVA * kURow + r0;
+                            const float2 xya = make_float2(gP[w].x, gE[w].x), xyb = make_float2(gP[w].y, gE[w].y);
+                            const float2 zwa = make_float2(gZ[w].x, gW[w].x), zwb = make_float2(gZ[w].y, gW[w].y);
 #pragma unroll
-                        for (int j = 0; j < 5; ++j) {
-                            float sx = 0.f, sy = 0.f, sz = 0.f, sw_ = 0.f;
-                            if (j < 4) {
-                                sx = wk[j] * gP[w].x;
-                                sy = wk[j] * gE[w].x;
-                                sz = wk[j] * gZ[w].x;
-                                sw_ = wk[j] * gW[w].x;
+                            for (int m = 0; m < 5; ++m) {
+                                if (act) {
+                                    float4* d = dst + m * kURow;
+                                    const float4 o4 = *d;
+                                    float2 xy = make_float2(o4.x, o4.y), zw = make_float2(o4.z, o4.w);
+                                    xy = fma2(dup(w2[m].x), xya, xy);
+                                    xy = fma2(dup(w2[m].y), xyb, xy);
+                                    zw = fma2(dup(w2[m].x), zwa, zw);
+                                    zw = fma2(dup(w2[m].y), zwb, zw);
+                                    *d = make_float4(xy.x, xy.y, zw.x, zw.y);
+                                }
+                                if (m < 4) __syncwarp();
                             }
-                            if (j > 0) {
-                                sx = fmaf(wk[j - 1], gP[w].y, sx);
-                                sy = fmaf(wk[j - 1], gE[w].y, sy);
-                                sz = fmaf(wk[j - 1], gZ[w].y, sz);
-                                sw_ = fmaf(wk[j - 1], gW[w].y, sw_);
-                            }
-                            float4* d4 = dst + j * kTileX;
-                            atomicAdd(&d4->x, sx);
-                            atomicAdd(&d4->y, sy);
-                            atomicAdd(&d4->z, sz);
-                            if (with_int) atomicAdd(&d4->w, sw_);
                         }
+                        if (nph > 1) __syncwarp();
                     }
                 }
                 __syncthreads();
-                // x pass transpose: entry (xf, v, w) feeds cells ub..ub+3 of row (v, w)
-                for (int e = tid; e < nut; e += nthr) {
-                    const int vw = e / kTileX;
-                    const int xfe = e % kTileX;
-                    const int Xe = X0 + xfe;
-                    const int xie = floordiv(Xe, mx), xre = Xe - xie * mx;
-                    const int oxe = offx[av * mx + xre];
-                    const float4 we = *reinterpret_cast<const float4*>(wx + (av * mx + xre) * 4);
-                    const int ube = xie - cx0 - 2 + oxe;
-                    const float4 gu = gut[e];
-                    float4* dst = ggt + vw * NU + ube;
-                    const float wk[4] = {we.x, we.y, we.z, we.w};
+                // x pass transpose, one (w, v) row of cells per thread: a 4-cell window
+                // slides with ub; a cell leaving the window is final for this group
+                for (int row = tid; row < NV * NW; row += nthr) {
+                    const int w = div_nv(row), v = row - w * NV;
+                    const float4* src = gut + (w * NVA + v) * kURow;
+                    float4* dst = ggt + row * NUP;
+                    int ub = xub[0];
+                    float4 a0 = zero4, a1 = zero4, a2 = zero4, a3 = zero4;
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        atomicAdd(&dst[k].x, wk[k] * gu.x);
-                        atomicAdd(&dst[k].y, wk[k] * gu.y);
-                        atomicAdd(&dst[k].z, wk[k] * gu.z);
-                        if (gu.w != 0.f) atomicAdd(&dst[k].w, wk[k] * gu.w);
+                    for (int x = 0; x < kTileX; ++x) {
+                        if (x > 0) {
+                            const int nb = xub[x];
+                            if (nb != ub) {
+                                dst[ub] = f4add(dst[ub], a0);
+                                a0 = a1;
+                                a1 = a2;
+                                a2 = a3;
+                                a3 = zero4;
+                                ub = nb;
+                            }
+                        }
+                        const float4 g = src[x];
+                        const float4 wk = xw4[x];
+                        a0 = f4fma(wk.x, g, a0);
+                        a1 = f4fma(wk.y, g, a1);
+                        a2 = f4fma(wk.z, g, a2);
+                        a3 = f4fma(wk.w, g, a3);
                     }
+                    dst[ub] = f4add(dst[ub], a0);
+                    dst[ub + 1] = f4add(dst[ub + 1], a1);
+                    dst[ub + 2] = f4add(dst[ub + 2], a2);
+                    dst[ub + 3] = f4add(dst[ub + 3], a3);
                 }
             }
             __syncthreads();
-            // cells outside the block do not depend on the input
-            for (int c = tid; c < ncell; c += nthr) {
-                const int u = c % NU;
-                const int v = (c / NU) % NV;
-                const int w = c / (NU * NV);
-                const int cu = cx0 + u, cv = cy0 + v, cw = cz0 + w;
-                if (!(cu >= 0 && cu < bw && cv >= 0 && cv < bh && cw >= 0 && cw < bd))
-                    ggt[c] = make_float4(0.f, 0.f, 0.f, 0.f);
-            }
-            __syncthreads();
-            // stencil transpose onto the input tile positions, then into dL/dI'
-            const int mR = p.gr[0], xR = p.gr[1], yR = p.gr[2], zR = p.gr[3];
+            // stencil transpose onto the input tile positions, then into dL/dI'. Cells
+            // outside the tile grid or the block do not depend on the input.
             for (int i = tid; i < nin; i += nthr) {
-                const int ix = i % NIX;
-                const int iy = (i / NIX) % NIY;
-                const int iz = i / (NIX * NIY);
+                const int iz = div_nixy(i);
+                const int rem = i - iz * (NIX * NIY);
+                const int iy = div_nix(rem), ix = rem - iy * NIX;
                 const int u = ix - R, v = iy - R, w = iz - R;  // cell with the same position
-                auto G = [&](int du, int dv, int dw) -> float4 {
-                    const int uu = u + du, vv = v + dv, ww = w + dw;
-                    if (uu < 0 || uu >= NU || vv < 0 || vv >= NV || ww < 0 || ww >= NW)
-                        return make_float4(0.f, 0.f, 0.f, 0.f);
-                    return ggt[(ww * NV + vv) * NU + uu];
-                };
-                float acc = G(0, 0, 0).w;
-                // Gx(c) = sum_{i>0, j, k} I(c + (i, j, k)) - I(c + (-i, j, k))
-                for (int ii = 1; ii <= mR; ++ii)
-                    for (int j = -yR; j <= yR; ++j)
-                        for (int k = -zR; k <= zR; ++k) acc += G(-ii, -j, -k).x - G(ii, -j, -k).x;
-                for (int jj = 1; jj <= mR; ++jj)
-                    for (int ii = -xR; ii <= xR; ++ii)
-                        for (int k = -zR; k <= zR; ++k) acc += G(-ii, -jj, -k).y - G(-ii, jj, -k).y;
-                for (int kk = 1; kk <= mR; ++kk)
-                    for (int ii = -xR; ii <= xR; ++ii)
-                        for (int j = -yR; j <= yR; ++j) acc += G(-ii, -j, -kk).z - G(-ii, -j, kk).z;
+                float acc = 0.f;
+                if (p.grad_mode == 1 || p.grad_mode == 2) {
+                    // 3 x 3 x 3 neighbourhood with clamped indices and 0/1 masks
+                    int cu[3], cv[3], cw[3];
+                    float mu[3], mv[3], mw[3];
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        const int uu = u + d - 1, vv = v + d - 1, ww = w + d - 1;
+                        mu[d] = (uu >= 0 && uu < NU && cx0 + uu >= 0 && cx0 + uu < bw) ? 1.f : 0.f;
+                        mv[d] = (vv >= 0 && vv < NV && cy0 + vv >= 0 && cy0 + vv < bh) ? 1.f : 0.f;
+                        mw[d] = (ww >= 0 && ww < NW && cz0 + ww >= 0 && cz0 + ww < bd) ? 1.f : 0.f;
+                        cu[d] = clampi(uu, 0, NU - 1);
+                        cv[d] = clampi(vv, 0, NV - 1) * NUP;
+                        cw[d] = clampi(ww, 0, NW - 1) * (NV * NUP);
+                    }
+                    auto G = [&](int dx, int dy, int dz) -> float4 { return ggt[cw[dz + 1] + cv[dy + 1] + cu[dx + 1]]; };
+                    if (p.grad_mode == 1) {
+                        // neighbour d adds -(dx Gx + dy Gy + dz Gz) (ranges 1, 1, 1, 1)
+#pragma unroll
+                        for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+                            for (int dy = -1; dy <= 1; ++dy) {
+                                const float myz = mv[dy + 1] * mw[dz + 1];
+#pragma unroll
+                                for (int dx = -1; dx <= 1; ++dx) {
+                                    const float4 g = G(dx, dy, dz);
+                                    float s = 0.f;
+                                    if (dx) s = dx < 0 ? s + g.x : s - g.x;
+                                    if (dy) s = dy < 0 ? s + g.y : s - g.y;
+                                    if (dz) s = dz < 0 ? s + g.z : s - g.z;
+                                    if (!dx && !dy && !dz) s = g.w;
+                                    acc = fmaf(myz * mu[dx + 1], s, acc);
+                                }
+                            }
+                    } else {
+                        // ranges 1, 0, 0, 0: axis neighbours only
+                        acc = mu[1] * mv[1] * mw[1] * G(0, 0, 0).w;
+                        acc = fmaf(mu[0] * mv[1] * mw[1], G(-1, 0, 0).x, acc);
+                        acc = fmaf(-mu[2] * mv[1] * mw[1], G(1, 0, 0).x, acc);
+                        acc = fmaf(mu[1] * mv[0] * mw[1], G(0, -1, 0).y, acc);
+                        acc = fmaf(-mu[1] * mv[2] * mw[1], G(0, 1, 0).y, acc);
+                        acc = fmaf(mu[1] * mv[1] * mw[0], G(0, 0, -1).z, acc);
+                        acc = fmaf(-mu[1] * mv[1] * mw[2], G(0, 0, 1).z, acc);
+                    }
+                } else {
+                    const int mR = p.gr[0], xR = p.gr[1], yR = p.gr[2], zR = p.gr[3];
+                    auto G = [&](int du, int dv, int dw) -> float4 {
+                        const int uu = u + du, vv = v + dv, ww = w + dw;
+                        if (uu < 0 || uu >= NU || vv < 0 || vv >= NV || ww < 0 || ww >= NW) return zero4;
+                        if (cx0 + uu < 0 || cx0 + uu >= bw || cy0 + vv < 0 || cy0 + vv >= bh || cz0 + ww < 0 ||
+                            cz0 + ww >= bd)
+                            return zero4;
+                        return ggt[(ww * NV + vv) * NUP + uu];
+                    };
+                    acc = G(0, 0, 0).w;
+                    // Gx(c) = sum_{i>0, j, k} I(c + (i, j, k)) - I(c + (-i, j, k))
+                    for (int ii = 1; ii <= mR; ++ii)
+                        for (int j = -yR; j <= yR; ++j)
+                            for (int k = -zR; k <= zR; ++k) acc += G(-ii, -j, -k).x - G(ii, -j, -k).x;
+                    for (int jj = 1; jj <= mR; ++jj)
+                        for (int ii = -xR; ii <= xR; ++ii)
+                            for (int k = -zR; k <= zR; ++k) acc += G(-ii, -jj, -k).y - G(-ii, jj, -k).y;
+                    for (int kk = 1; kk <= mR; ++kk)
+                        for (int ii = -xR; ii <= xR; ++ii)
+                            for (int j = -yR; j <= yR; ++j) acc += G(-ii, -j, -kk).z - G(-ii, -j, kk).z;
+                }
                 if (acc != 0.f) {
                     const int bx = clampi(cx0 - R + ix, 0, bw - 1);
                     const int by = clampi(cy0 - R + iy, 0, bh - 1);
@@ -644,14 +779,13 @@ __global__ void __launch_bounds__(128, 2) radiality_adjoint_kernel(const RadPara
         }
     }
 }
-
 template <int MZ>
 int launch_adj_mz(const RadParams& p, const AdjParams& a, int grid, size_t smem, cudaStream_t st) {
     constexpr int CZ = cza_for_mag(MZ);
     auto k = radiality_adjoint_kernel<MZ, CZ>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
-    k<<<grid, p.TY * (kTileX / 2), smem, st>>>(p, a);
+    k<<<grid, kAdjThreads, smem, st>>>(p, a);
     return (int)cudaGetLastError();
 }
 
@@ -668,8 +802,10 @@ int occ_adj_mz(int threads, size_t smem, int* out) {
 
 size_t radiality_adjoint_smem_bytes(const RadParams& p) {
     const int NW = cza_for_mag(p.mag[2]) + 4;
-    size_t b = sizeof(float4) * (2 * (size_t)p.NU * p.NV * NW + 2 * (size_t)kTileX * p.NV * NW);
-    b += sizeof(float) * ((((size_t)p.NIX * p.NIY * p.NIZ + 3) & ~(size_t)3) + p.smem_table_words);
+    size_t b = sizeof(float4) * (2 * (size_t)adj_nup(p.NU) * p.NV * NW +
+                                 (size_t)adj_u_region_f4(p.NV, NW, p.NIX, p.NIY, p.NIZ));
+    b += sizeof(float4) * kTileX + sizeof(int) * kTileX;  // x weights and first tap cell of each column
+    b += sizeof(float) * p.smem_table_words;
     return (b + 15) & ~(size_t)15;
 }
 
@@ -690,7 +826,7 @@ int launch_radiality_adjoint(const RadParams& p, const AdjParams& a, int grid, s
 
 int radiality_adjoint_max_ctas_per_sm(const RadParams& p, int* out) {
     const size_t smem = radiality_adjoint_smem_bytes(p);
-    const int threads = p.TY * (kTileX / 2);
+    const int threads = kAdjThreads;
     switch (p.mag[2]) {
         case 1: return occ_adj_mz<1>(threads, smem, out);
         case 2: return occ_adj_mz<2>(threads, smem, out);

@@ -668,6 +668,7 @@ static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const flo
     BlockDev blk = ctx->train.blk;
     const long long V = blk.vox;
     const int FZ = cfg->mag[2] * cza_for_mag(cfg->mag[2]);
+    blk.ntile[1] = (blk.hi[1] - blk.lo[1] + kAdjRows - 1) / kAdjRows;
     blk.ntile[2] = (blk.hi[2] - blk.zbase + FZ - 1) / FZ;
     std::vector<TileDesc> tiles;
     for (int tz = 0; tz < blk.ntile[2]; ++tz)
@@ -695,6 +696,9 @@ static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const flo
                                     st);
     if (e) return cuda_fail((cudaError_t)e, "temporal adjoint launch");
     RadParams rp = fill_rad_params(ctx, *cfg, ctx->train.iprime, dims, cza_for_mag(cfg->mag[2]));
+    rp.TY = kAdjRows;
+    rp.NV = (kAdjRows - 1) / cfg->mag[1] + 2 + 4;
+    rp.NIY = rp.NV + 2 * rp.R;
     rp.blocks = dblk;
     rp.tiles = static_cast<const TileDesc*>(ctx->atiles.p);
     rp.ntiles = (int)tiles.size();

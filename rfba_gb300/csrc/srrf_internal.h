@@ -17,6 +17,9 @@ constexpr int kTileX = 16;
 constexpr int kMaxThreads = 224;  // 16 x 14 threads for the 28-row tile (mag_y 7)
 constexpr int kMaxMag = 8;
 constexpr int kMaxGradRange = 3;
+// Adjoint tile: 16 x 16 subvoxel columns (two consecutive rows per thread).
+constexpr int kAdjRows = 16;
+constexpr int kAdjThreads = kTileX * kAdjRows / 2;
 
 // Coarse z cells per tile for a given z magnification (FZ = MZ * CZ).
 constexpr int cz_for_mag(int mz) {
