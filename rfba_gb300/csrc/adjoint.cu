@@ -293,7 +293,7 @@ __device__ __forceinline__ float4 gradient_generic(const float* base, int NIX, i
 
 // Adjoint tile: 16 fine x columns x kAdjRows fine y rows x FZ fine z rows,
 // kAdjThreads threads. Warp k owns x columns 4k..4k+3; lane l of a warp takes
-// column 4k + (l & 3) and the fine rows 2 (l >> 2), 2 (l >> 2) + 1. All
+// column 4k + (l >> 3) and the fine rows 2 (l & 7), 2 (l & 7) + 1. All
 // threads that touch an x column's U-stage entries sit in one warp, so the
 // y-pass transpose needs no shared-memory atomics: the lanes of one column
 // whose 5-row windows start on the same row (possible when my > 2) add in
@@ -302,8 +302,10 @@ __device__ __forceinline__ float4 gradient_generic(const float* base, int NIX, i
 // per thread with a sliding 4-cell window, so every cell has one writer.
 //
 // Shared-memory row strides are odd in float4 units (17 for the U stage, NU
-// rounded up to odd for the cell grid): threads walking different rows at the
-// same column, and the 4 columns x 8 row windows of a warp, hit all banks.
+// rounded up to odd for the cell grid). A 16-byte access is served a quarter
+// warp (8 lanes) at a time; 8 lanes walking 8 consecutive rows at one column
+// (the row windows of one x column, or one cell row per thread) then hit 8
+// different bank groups.
 constexpr int kURow = kTileX + 1;
 
 __host__ __device__ __forceinline__ int adj_nup(int NU) { return NU | 1; }
@@ -349,8 +351,8 @@ __global__ void __launch_bounds__(kAdjThreads, 2) radiality_adjoint_kernel(const
     const int tid = threadIdx.x;
     const int mx = p.mag[0], my = p.mag[1];
     const int lane = tid & 31;
-    const int xf = (tid >> 5) * 4 + (lane & 3);
-    const int tr = lane >> 2;
+    const int xf = (tid >> 5) * 4 + (lane >> 3);
+    const int tr = lane & 7;
     // lanes tr, tr' of one column with tr = tr' mod nph have rows >= my apart,
     // hence different window starts
     const int nph = (my + 1) >> 1;
