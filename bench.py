@@ -185,24 +185,25 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def measure_batching(ctx, steps: int) -> dict:
-    """Batching workload: 50 volumes of 160^3 u16 (3000 filament emitters) cut by
-    doSplit.m's rule into 29^3 blocks with a 1-voxel overlap (216 blocks, edge
-    blocks 25 voxels), magnification 3, temporal mean. One persistent launch over
-    all blocks and volumes (device buffers, and through the C-ABI with pinned
-    host buffers) against the plain path: one launch per block with that block's
-    host->device and device->host copies."""
+def _batching_case(ctx, x, cfg, steps: int, label: str) -> dict:
+    """One batching measurement: doSplit's 29-voxel blocks with a 1-voxel
+    overlap over the whole series; the batched path (one persistent launch per
+    pass, autotuned schedule, replayed as a CUDA graph) on device buffers and
+    through the C-ABI with pinned host buffers, against the plain path (one
+    launch sequence per block with that block's host<->device copies)."""
     import torch
-    from rfba_gb300 import srrf, synth
-    x, _ = synth.workload("batching", shape=(160, 160, 160))
-    cfg = srrf.Config.make(mag=3, method=1, gradient_smooth=1, main_range=1, x_range=1, y_range=1, z_range=1)
+    from rfba_gb300 import srrf
     blocks, n, oe = srrf.blocks_dosplit(cfg, x.shape, 29, 1)
     units = oe * x.shape[0]
     xd = torch.from_numpy(x.view(np.int16)).cuda()
     outd = torch.empty(oe, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
-    for _ in range(2):
-        ctx.forward_blocks(cfg, xd, blocks, n, oe, out=outd, stream=stream.cuda_stream)
+    t0 = time.perf_counter()
+    ctx.forward_blocks(cfg, xd, blocks, n, oe, out=outd, stream=stream.cuda_stream)  # autotune + capture
+    torch.cuda.synchronize()
+    first_s = time.perf_counter() - t0
+    sched = ctx.schedule()
+    ctx.forward_blocks(cfg, xd, blocks, n, oe, out=outd, stream=stream.cuda_stream)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -210,6 +211,7 @@ def measure_batching(ctx, steps: int) -> dict:
         ctx.forward_blocks(cfg, xd, blocks, n, oe, out=outd, stream=stream.cuda_stream)
     e1.record(stream)
     torch.cuda.synchronize()
+    replay = ctx.schedule()
     dev_ms = e0.elapsed_time(e1) / steps
     pin_in = torch.empty(x.nbytes, dtype=torch.uint8).pin_memory().numpy().view(np.uint16).reshape(x.shape)
     pin_in[...] = x
@@ -226,13 +228,31 @@ def measure_batching(ctx, steps: int) -> dict:
     plain_ms = (time.perf_counter() - t0) * 1e3
     same = bool(np.array_equal(np.nan_to_num(plain_out), np.nan_to_num(pin_out)) and
                 np.array_equal(np.isnan(plain_out), np.isnan(pin_out)))
-    sizes = sorted({tuple(blocks[i].size) for i in range(n)})
-    return {"workload": "batching: 50 x 160^3 u16, doSplit 29/1 -> %d blocks (edges %s), mag 3, temporal mean" % (
-        n, sorted({s[0] for s in sizes})),
-        "voxel_volumes": units, "batched_device_ms": dev_ms, "batched_e2e_ms": e2e_ms, "plain_per_block_ms": plain_ms,
-        "batched_device_value": units / (dev_ms / 1e3), "batched_e2e_value": units / (e2e_ms / 1e3),
-        "plain_value": units / (plain_ms / 1e3), "speedup_e2e_vs_plain": plain_ms / e2e_ms,
-        "speedup_device_vs_plain": plain_ms / dev_ms, "batched_equals_plain": same}
+    edges = sorted({int(blocks[i].size[a]) for i in range(n) for a in range(3)})
+    return {"case": label, "blocks": n, "block_edges": edges, "voxel_volumes": units,
+            "schedule": {"tile_rows": sched["tile_rows"], "tile_order": sched["tile_order"],
+                         "graph_replay": replay["graph"], "first_call_s": first_s},
+            "batched_device_ms": dev_ms, "batched_e2e_ms": e2e_ms, "plain_per_block_ms": plain_ms,
+            "batched_device_value": units / (dev_ms / 1e3), "batched_e2e_value": units / (e2e_ms / 1e3),
+            "plain_value": units / (plain_ms / 1e3), "speedup_device_vs_plain": plain_ms / dev_ms,
+            "speedup_e2e_vs_plain": plain_ms / e2e_ms, "batched_equals_plain": same}
+
+
+def measure_batching(ctx, steps: int) -> dict:
+    """Batching workload: 50 volumes (3000 filament emitters) at magnification
+    3, cut by doSplit's rule (29, 1-voxel overlap). 160x160x160 gives the 216
+    blocks (edges 25 and 29) of the batching config, measured with the temporal
+    mean and with TRAC-2; the literal 160x160x120 series gives 180 blocks."""
+    from rfba_gb300 import srrf, synth
+    kw = dict(mag=3, gradient_smooth=1, main_range=1, x_range=1, y_range=1, z_range=1)
+    x, _ = synth.workload("batching", shape=(160, 160, 160))
+    cases = [_batching_case(ctx, x, srrf.Config.make(method=1, **kw), steps, "160^3 TRA"),
+             _batching_case(ctx, x, srrf.Config.make(method=3, itc=0, trac_order=2, **kw), steps, "160^3 TRAC-2")]
+    x, _ = synth.workload("batching")
+    cases.append(_batching_case(ctx, x, srrf.Config.make(method=1, **kw), steps, "160x160x120 TRA"))
+    head = cases[0]
+    return {"workload": "batching: 50 volumes, 3000 filament emitters, doSplit 29/1 blocks, mag 3", **head,
+            "cases": cases}
 
 
 def measure_diff(ctx, steps: int, iters: int = 20, volumes=None) -> dict:

@@ -215,6 +215,15 @@ int rfba_ctx_last_timing(rfba_ctx* ctx, double* radiality_ms, double* temporal_m
 /* Launch overrides for tuning: CTAs of the radiality kernel and time points per
  * work item (0 = automatic). */
 int rfba_ctx_set_launch(rfba_ctx* ctx, int grid, int t_chunk);
+/* Schedule of the last rfba_srrf_forward / rfba_srrf_forward_blocks call: tile
+ * rows (tile shape), tile order (0 largest block first, 1 interleaved across
+ * blocks), whether it was replayed as a CUDA graph, and whether this call ran
+ * the autotuner. The extended forward autotunes the schedule once per
+ * (configuration, dims, block shapes) on the first volumes of the input and
+ * captures each (arguments, scratch) combination as a CUDA graph (pinned or
+ * device buffers; RFBA_TUNE=0 / RFBA_GRAPH=0 turn either off). No counterpart
+ * in the reference. */
+int rfba_ctx_last_schedule(rfba_ctx* ctx, int* tile_rows, int* tile_order, int* graph, int* tuned);
 
 /* Text of the last error on the calling thread ("" if none). */
 const char* rfba_last_error(void);

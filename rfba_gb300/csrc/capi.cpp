@@ -14,6 +14,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -103,6 +105,53 @@ struct PlanCache {
     int zero_pair = -1;
 };
 
+// Schedule choices of the forward: tile rows (tile shape) and tile order
+// (block-to-CTA schedule). 0 = defaults.
+struct Tuning {
+    int ty = 0;
+    int order = 0;  // 0: largest blocks first, raster inside a block; 1: tiles interleaved across blocks
+};
+
+// One pass = the blocks whose radiality + intensity stacks fit the budget
+// together; lists of all passes are concatenated (tile block indices are
+// relative to the pass's first block).
+struct PassPlan {
+    size_t b0 = 0, b1 = 0, t0 = 0, t1 = 0, p0 = 0;
+    long long stack_elems = 0;
+    int chunk = 1, nchunks = 1, grid = 1;
+    size_t smem = 0;
+    long long nitems = 0, units = 0;
+};
+struct PassSet {
+    std::vector<BlockDev> blocks;
+    std::vector<TileDesc> tiles;
+    std::vector<long long> prefix;
+    std::vector<PassPlan> passes;
+    long long max_stack = 0;
+    int ty = 0;
+};
+
+
+// A captured forward: the whole launch sequence of one call (copies, clears,
+// all passes) replayed with one cudaGraphLaunch while the call's arguments and
+// the scratch it was captured on are unchanged.
+struct GraphPlan {
+    std::string key;
+    std::vector<const void*> deps;  // scratch pointers baked into the graph
+    cudaGraphExec_t exec = nullptr;
+    PassSet ps;
+    DevBuf blocks, tiles, prefix, counters;
+    std::vector<cudaEvent_t> evs;
+    ~GraphPlan() {
+        if (exec) cudaGraphExecDestroy(exec);
+        for (cudaEvent_t e : evs) cudaEventDestroy(e);
+        blocks.release();
+        tiles.release();
+        prefix.release();
+        counters.release();
+    }
+};
+
 }  // namespace rfba
 
 struct rfba_ctx {
@@ -138,6 +187,12 @@ struct rfba_ctx {
         rfba::BlockDev blk;
     } train;
     double last_backward_ms = 0.0;
+    // forward schedule: per-pass timing events, autotuned schedules, captured graphs
+    std::vector<cudaEvent_t> pev;
+    cudaStream_t cap = nullptr;  // stream the graphs are captured on
+    std::map<std::string, std::pair<int, int>> tunes;  // schedule key -> (tile rows, tile order)
+    std::vector<std::unique_ptr<rfba::GraphPlan>> graphs;  // most recent first
+    int last_ty = 0, last_order = 0, last_graph = 0, last_tuned = 0;
 };
 
 namespace rfba {
@@ -226,7 +281,7 @@ static int order_streams(rfba_ctx* ctx, cudaStream_t st) {
 // Turn caller blocks into device block descriptors, splitting regions along z
 // so that one pass's radiality + intensity stack fits the scratch budget.
 static int make_blocks(rfba_ctx* ctx, const rfba_srrf_config& cfg, const int dims[4], const rfba_block* blocks,
-                       int nblocks, std::vector<BlockDev>* outb) {
+                       int nblocks, std::vector<BlockDev>* outb, int ty = 0) {
     const RingPlan& rp = ctx->plan.ring;
     const int T = dims[3];
     const int FZ = fz_for(cfg.mag[2]);
@@ -268,7 +323,7 @@ static int make_blocks(rfba_ctx* ctx, const rfba_srrf_config& cfg, const int dim
             s.out_offset = d.out_offset + (long long)(z0 - b.lo[2]) * d.out_stride[2];
             for (int a = 0; a < 3; ++a) s.nreg[a] = s.hi[a] - s.lo[a];
             s.zbase = (s.lo[2] / cfg.mag[2]) * cfg.mag[2];
-            const int TY = tile_rows_for_mag(cfg.mag[1]);
+            const int TY = ty > 0 ? ty : tile_rows_for_mag(cfg.mag[1]);
             s.ntile[0] = (s.nreg[0] + kTileX - 1) / kTileX;
             s.ntile[1] = (s.nreg[1] + TY - 1) / TY;
             s.ntile[2] = (s.hi[2] - s.zbase + FZ - 1) / FZ;
@@ -284,7 +339,7 @@ static size_t elem_size(rfba_dtype dt) { return dt == RFBA_U16 ? 2 : 4; }
 // Kernel parameters common to the forward and adjoint radiality kernels
 // (everything but the block / tile lists and the schedule).
 static RadParams fill_rad_params(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void* in_dev, const int dims[4],
-                                 int CZ) {
+                                 int CZ, int ty = 0) {
     const PlanCache& P = ctx->plan;
     const int T = dims[3];
     RadParams rp;
@@ -318,7 +373,7 @@ static RadParams fill_rad_params(rfba_ctx* ctx, const rfba_srrf_config& cfg, con
         rp.grad_mode = 2;
     else
         rp.grad_mode = 0;
-    rp.TY = tile_rows_for_mag(cfg.mag[1]);
+    rp.TY = ty > 0 ? ty : tile_rows_for_mag(cfg.mag[1]);
     rp.NU = (kTileX - 1) / cfg.mag[0] + 2 + 4;
     rp.NV = (rp.TY - 1) / cfg.mag[1] + 2 + 4;
     rp.NW = CZ + 4;
@@ -333,20 +388,32 @@ static RadParams fill_rad_params(rfba_ctx* ctx, const rfba_srrf_config& cfg, con
     return rp;
 }
 
-// Run the device pipeline for all blocks. in_dev / out_dev are device pointers.
-static int run_device(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void* in_dev, rfba_dtype dtype,
-                      const int dims[4], const std::vector<BlockDev>& all, float* out_dev, cudaStream_t st) {
+static int plan_passes(rfba_ctx* ctx, const rfba_srrf_config& cfg, rfba_dtype dtype, const int dims[4],
+                       const std::vector<BlockDev>& all, const Tuning& tune, PassSet* ps) {
     const int T = dims[3];
-    const PlanCache& P = ctx->plan;
-    // passes under the stack budget
     const size_t per_vox = (size_t)T * sizeof(float);
+    ps->blocks.clear();
+    ps->tiles.clear();
+    ps->prefix.clear();
+    ps->passes.clear();
+    ps->max_stack = 0;
+    ps->ty = tune.ty > 0 ? tune.ty : tile_rows_for_mag(cfg.mag[1]);
+    RadParams rp = fill_rad_params(ctx, cfg, nullptr, dims, cz_for_mag(cfg.mag[2]), ps->ty);
+    const size_t smem = radiality_smem_bytes(rp);
+    if (smem > 227 * 1024) {
+        set_error("shared memory tile too large for this configuration");
+        return RFBA_ERR_UNSUPPORTED;
+    }
+    int per_sm = 0;
+    int ce = radiality_max_ctas_per_sm(rp, dtype == RFBA_U16, &per_sm);
+    if (ce != 0) return cuda_fail((cudaError_t)ce, "occupancy");
+    if (per_sm < 1) {
+        set_error("radiality kernel does not fit on an SM");
+        return RFBA_ERR_UNSUPPORTED;
+    }
+    const int slots = per_sm * ctx->sm_count;
     size_t i0 = 0;
-    ctx->last_rad_ms = ctx->last_temporal_ms = 0.0;
-    ctx->last_flop_units = 0;
-    ctx->last_passes = 0;
-    ctx->train.valid = false;
     while (i0 < all.size()) {
-        ctx->last_passes++;
         size_t i1 = i0;
         long long vox = 0;
         while (i1 < all.size()) {
@@ -355,84 +422,100 @@ static int run_device(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void* in
             vox = nv;
             ++i1;
         }
-        std::vector<BlockDev> pass(all.begin() + i0, all.begin() + i1);
-        std::vector<long long> prefix(pass.size() + 1, 0);
-        std::vector<TileDesc> tiles;
-        long long off = 0;
-        for (size_t b = 0; b < pass.size(); ++b) {
-            pass[b].stack_off = off;
-            off += pass[b].vox * T;
-            prefix[b + 1] = prefix[b] + pass[b].vox;
+        PassPlan pp;
+        pp.b0 = ps->blocks.size();
+        pp.t0 = ps->tiles.size();
+        pp.p0 = ps->prefix.size();
+        long long off = 0, pre = 0;
+        ps->prefix.push_back(0);
+        for (size_t b = i0; b < i1; ++b) {
+            BlockDev d = all[b];
+            d.stack_off = off;
+            off += d.vox * T;
+            pre += d.vox;
+            ps->prefix.push_back(pre);
+            ps->blocks.push_back(d);
         }
-        // tiles: largest blocks first for balance, raster order inside a block
-        std::vector<int> order(pass.size());
-        for (size_t b = 0; b < pass.size(); ++b) order[b] = (int)b;
-        std::stable_sort(order.begin(), order.end(), [&](int u, int v) {
-            return (long long)pass[u].ntile[0] * pass[u].ntile[1] * pass[u].ntile[2] >
-                   (long long)pass[v].ntile[0] * pass[v].ntile[1] * pass[v].ntile[2];
-        });
-        for (int b : order)
-            for (int tz = 0; tz < pass[b].ntile[2]; ++tz)
-                for (int ty = 0; ty < pass[b].ntile[1]; ++ty)
-                    for (int tx = 0; tx < pass[b].ntile[0]; ++tx) tiles.push_back({b, tx, ty, tz});
-        int stc;
-        if ((stc = ctx->rad.ensure((size_t)off * 4, "radiality stack"))) return stc;
-        if ((stc = ctx->inten.ensure((size_t)off * 4, "intensity stack"))) return stc;
-        if ((stc = ctx->blocks.ensure(pass.size() * sizeof(BlockDev), "blocks"))) return stc;
-        if ((stc = ctx->tiles.ensure(tiles.size() * sizeof(TileDesc), "tiles"))) return stc;
-        if ((stc = ctx->prefix.ensure(prefix.size() * sizeof(long long), "prefix"))) return stc;
-        if ((stc = ctx->counter.ensure(256, "counter"))) return stc;
-        RFBA_CUDA(cudaMemcpyAsync(ctx->blocks.p, pass.data(), pass.size() * sizeof(BlockDev), cudaMemcpyHostToDevice, st),
-                  "blocks upload");
-        RFBA_CUDA(cudaMemcpyAsync(ctx->tiles.p, tiles.data(), tiles.size() * sizeof(TileDesc), cudaMemcpyHostToDevice, st),
-                  "tiles upload");
-        RFBA_CUDA(cudaMemcpyAsync(ctx->prefix.p, prefix.data(), prefix.size() * sizeof(long long),
-                                  cudaMemcpyHostToDevice, st),
-                  "prefix upload");
-        RFBA_CUDA(cudaMemsetAsync(ctx->counter.p, 0, 256, st), "counter reset");
-
-        RadParams rp = fill_rad_params(ctx, cfg, in_dev, dims, cz_for_mag(cfg.mag[2]));
-        rp.blocks = static_cast<const BlockDev*>(ctx->blocks.p);
-        rp.tiles = static_cast<const TileDesc*>(ctx->tiles.p);
-        rp.ntiles = (int)tiles.size();
-        rp.rad_stack = static_cast<float*>(ctx->rad.p);
-        rp.int_stack = static_cast<float*>(ctx->inten.p);
-        rp.work_counter = static_cast<unsigned int*>(ctx->counter.p);
-        const size_t smem = radiality_smem_bytes(rp);
-        if (smem > 227 * 1024) {
-            set_error("shared memory tile too large for this configuration");
-            return RFBA_ERR_UNSUPPORTED;
+        const int nb = (int)(i1 - i0);
+        const BlockDev* pb = ps->blocks.data() + pp.b0;
+        auto ntiles = [&](int b) { return (long long)pb[b].ntile[0] * pb[b].ntile[1] * pb[b].ntile[2]; };
+        if (tune.order == 1) {
+            // round robin over blocks, one tile at a time
+            long long most = 0;
+            for (int b = 0; b < nb; ++b) most = std::max(most, ntiles(b));
+            for (long long k = 0; k < most; ++k)
+                for (int b = 0; b < nb; ++b) {
+                    if (k >= ntiles(b)) continue;
+                    const int tx = (int)(k % pb[b].ntile[0]);
+                    const int ty = (int)((k / pb[b].ntile[0]) % pb[b].ntile[1]);
+                    const int tz = (int)(k / ((long long)pb[b].ntile[0] * pb[b].ntile[1]));
+                    ps->tiles.push_back({b, tx, ty, tz});
+                }
+        } else {
+            // largest blocks first for balance, raster order inside a block
+            std::vector<int> order(nb);
+            for (int b = 0; b < nb; ++b) order[b] = b;
+            std::stable_sort(order.begin(), order.end(), [&](int u, int v) { return ntiles(u) > ntiles(v); });
+            for (int b : order)
+                for (int tz = 0; tz < pb[b].ntile[2]; ++tz)
+                    for (int ty = 0; ty < pb[b].ntile[1]; ++ty)
+                        for (int tx = 0; tx < pb[b].ntile[0]; ++tx) ps->tiles.push_back({b, tx, ty, tz});
         }
-        int per_sm = 0;
-        int ce = radiality_max_ctas_per_sm(rp, dtype == RFBA_U16, &per_sm);
-        if (ce != 0) return cuda_fail((cudaError_t)ce, "occupancy");
-        if (per_sm < 1) {
-            set_error("radiality kernel does not fit on an SM");
-            return RFBA_ERR_UNSUPPORTED;
-        }
-        const int slots = per_sm * ctx->sm_count;
+        pp.b1 = ps->blocks.size();
+        pp.t1 = ps->tiles.size();
+        pp.stack_elems = off;
+        pp.units = vox * T;
+        const long long nt = (long long)(pp.t1 - pp.t0);
         // time chunk: enough work items for ~8 per CTA slot
         int chunk = ctx->chunk_override;
         if (chunk <= 0) {
             const long long want = 8LL * slots;
-            long long nch = (want + rp.ntiles - 1) / rp.ntiles;
+            long long nch = (want + nt - 1) / nt;
             nch = std::max<long long>(1, std::min<long long>(nch, T));
             chunk = (int)((T + nch - 1) / nch);
         }
-        rp.t_chunk = chunk;
-        rp.nchunks = (T + chunk - 1) / chunk;
-        rp.nitems = (long long)rp.ntiles * rp.nchunks;
+        pp.chunk = chunk;
+        pp.nchunks = (T + chunk - 1) / chunk;
+        pp.nitems = nt * pp.nchunks;
         int grid = ctx->grid_override > 0 ? ctx->grid_override : slots;
-        grid = (int)std::min<long long>(grid, rp.nitems);
-        if (grid < 1) grid = 1;
+        grid = (int)std::min<long long>(grid, pp.nitems);
+        pp.grid = std::max(grid, 1);
+        pp.smem = smem;
+        ps->max_stack = std::max(ps->max_stack, off);
+        ps->passes.push_back(pp);
+        i0 = i1;
+    }
+    return RFBA_OK;
+}
 
+// Queue the passes on st: counter reset, radiality, temporal per pass. The
+// device lists hold ps's concatenated blocks / tiles / prefixes; evs (3 per
+// pass) are recorded around the kernels when given.
+static int enqueue_passes(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void* in_dev, rfba_dtype dtype,
+                          const int dims[4], const PassSet& ps, const BlockDev* dblocks, const TileDesc* dtiles,
+                          const long long* dprefix, unsigned int* dcounters, float* out_dev, cudaStream_t st,
+                          const cudaEvent_t* evs) {
+    for (size_t i = 0; i < ps.passes.size(); ++i) {
+        const PassPlan& pp = ps.passes[i];
+        unsigned int* counter = dcounters + 64 * i;
+        RFBA_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned int), st), "counter reset");
+        RadParams rp = fill_rad_params(ctx, cfg, in_dev, dims, cz_for_mag(cfg.mag[2]), ps.ty);
+        rp.blocks = dblocks + pp.b0;
+        rp.tiles = dtiles + pp.t0;
+        rp.ntiles = (int)(pp.t1 - pp.t0);
+        rp.rad_stack = static_cast<float*>(ctx->rad.p);
+        rp.int_stack = static_cast<float*>(ctx->inten.p);
+        rp.work_counter = counter;
+        rp.t_chunk = pp.chunk;
+        rp.nchunks = pp.nchunks;
+        rp.nitems = pp.nitems;
         TemporalParams tp;
         std::memset(&tp, 0, sizeof tp);
         tp.blocks = rp.blocks;
-        tp.vox_prefix = static_cast<const long long*>(ctx->prefix.p);
-        tp.nblocks = (int)pass.size();
-        tp.total_vox = prefix.back();
-        tp.T = T;
+        tp.vox_prefix = dprefix + pp.p0;
+        tp.nblocks = (int)(pp.b1 - pp.b0);
+        tp.total_vox = ps.prefix[pp.p0 + (pp.b1 - pp.b0)];
+        tp.T = dims[3];
         tp.method = cfg.method;
         tp.itc = cfg.itc;
         tp.order = cfg.trac_order;
@@ -440,29 +523,80 @@ static int run_device(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void* in
         tp.rad_stack = rp.rad_stack;
         tp.int_stack = rp.int_stack;
         tp.out = out_dev;
-
-        if (ctx->timing) RFBA_CUDA(cudaEventRecord(ctx->ev[0], st), "event");
-        int le = launch_radiality(rp, grid, smem, dtype == RFBA_U16, st);
+        if (evs) RFBA_CUDA(cudaEventRecord(evs[3 * i], st), "event");
+        int le = launch_radiality(rp, pp.grid, pp.smem, dtype == RFBA_U16, st);
         if (le != 0) return cuda_fail((cudaError_t)le, "radiality launch");
-        if (ctx->timing) RFBA_CUDA(cudaEventRecord(ctx->ev[1], st), "event");
+        if (evs) RFBA_CUDA(cudaEventRecord(evs[3 * i + 1], st), "event");
         le = launch_temporal(tp, st);
         if (le != 0) return cuda_fail((cudaError_t)le, "temporal launch");
-        if (ctx->timing) RFBA_CUDA(cudaEventRecord(ctx->ev[2], st), "event");
-        ctx->launches += 2;
-        ctx->last_flop_units += (long long)tp.total_vox * T;
+        if (evs) RFBA_CUDA(cudaEventRecord(evs[3 * i + 2], st), "event");
         if (verbose())
-            std::fprintf(stderr, "rfba: pass blocks=%zu tiles=%d chunk=%d items=%lld grid=%d smem=%zu\n", pass.size(),
-                         rp.ntiles, chunk, rp.nitems, grid, smem);
-        if (ctx->timing) {
-            RFBA_CUDA(cudaEventSynchronize(ctx->ev[2]), "event sync");
-            float a = 0, b = 0;
-            cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]);
-            cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]);
-            ctx->last_rad_ms += a;
-            ctx->last_temporal_ms += b;
-        }
-        i0 = i1;
+            std::fprintf(stderr, "rfba: pass blocks=%zu tiles=%d ty=%d chunk=%d items=%lld grid=%d smem=%zu\n",
+                         pp.b1 - pp.b0, rp.ntiles, ps.ty, pp.chunk, pp.nitems, pp.grid, pp.smem);
     }
+    return RFBA_OK;
+}
+
+static int ensure_events(rfba_ctx* ctx, std::vector<cudaEvent_t>* evs, size_t n) {
+    while (evs->size() < n) {
+        cudaEvent_t e;
+        RFBA_CUDA(cudaEventCreate(&e), "event");
+        evs->push_back(e);
+    }
+    return RFBA_OK;
+}
+
+// Per-pass kernel times from the events of the last run.
+static int collect_timing(rfba_ctx* ctx, const PassSet& ps, const std::vector<cudaEvent_t>& evs) {
+    ctx->last_rad_ms = ctx->last_temporal_ms = 0.0;
+    for (size_t i = 0; i < ps.passes.size(); ++i) {
+        RFBA_CUDA(cudaEventSynchronize(evs[3 * i + 2]), "event sync");
+        float a = 0.f, b = 0.f;
+        RFBA_CUDA(cudaEventElapsedTime(&a, evs[3 * i], evs[3 * i + 1]), "event time");
+        RFBA_CUDA(cudaEventElapsedTime(&b, evs[3 * i + 1], evs[3 * i + 2]), "event time");
+        ctx->last_rad_ms += a;
+        ctx->last_temporal_ms += b;
+    }
+    return RFBA_OK;
+}
+
+static void account(rfba_ctx* ctx, const PassSet& ps) {
+    ctx->last_passes = (int)ps.passes.size();
+    ctx->launches += 2 * (long long)ps.passes.size();
+    ctx->last_flop_units = 0;
+    for (const PassPlan& pp : ps.passes) ctx->last_flop_units += pp.units;
+}
+
+// Run the device pipeline for all blocks now (no graph). in_dev / out_dev are
+// device pointers.
+static int run_device(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void* in_dev, rfba_dtype dtype,
+                      const int dims[4], const std::vector<BlockDev>& all, float* out_dev, cudaStream_t st,
+                      const Tuning& tune = Tuning()) {
+    ctx->train.valid = false;
+    PassSet ps;
+    int s;
+    if ((s = plan_passes(ctx, cfg, dtype, dims, all, tune, &ps))) return s;
+    const size_t np = ps.passes.size();
+    if ((s = ctx->rad.ensure((size_t)ps.max_stack * 4, "radiality stack"))) return s;
+    if ((s = ctx->inten.ensure((size_t)ps.max_stack * 4, "intensity stack"))) return s;
+    if ((s = ctx->blocks.ensure(ps.blocks.size() * sizeof(BlockDev), "blocks"))) return s;
+    if ((s = ctx->tiles.ensure(ps.tiles.size() * sizeof(TileDesc), "tiles"))) return s;
+    if ((s = ctx->prefix.ensure(ps.prefix.size() * sizeof(long long), "prefix"))) return s;
+    if ((s = ctx->counter.ensure(np * 256, "counter"))) return s;
+    RFBA_CUDA(cudaMemcpyAsync(ctx->blocks.p, ps.blocks.data(), ps.blocks.size() * sizeof(BlockDev),
+                              cudaMemcpyHostToDevice, st), "blocks upload");
+    RFBA_CUDA(cudaMemcpyAsync(ctx->tiles.p, ps.tiles.data(), ps.tiles.size() * sizeof(TileDesc),
+                              cudaMemcpyHostToDevice, st), "tiles upload");
+    RFBA_CUDA(cudaMemcpyAsync(ctx->prefix.p, ps.prefix.data(), ps.prefix.size() * sizeof(long long),
+                              cudaMemcpyHostToDevice, st), "prefix upload");
+    if (ctx->timing && (s = ensure_events(ctx, &ctx->pev, 3 * np))) return s;
+    if ((s = enqueue_passes(ctx, cfg, in_dev, dtype, dims, ps, static_cast<const BlockDev*>(ctx->blocks.p),
+                            static_cast<const TileDesc*>(ctx->tiles.p), static_cast<const long long*>(ctx->prefix.p),
+                            static_cast<unsigned int*>(ctx->counter.p), out_dev, st,
+                            ctx->timing ? ctx->pev.data() : nullptr)))
+        return s;
+    account(ctx, ps);
+    if (ctx->timing && (s = collect_timing(ctx, ps, ctx->pev))) return s;
     return RFBA_OK;
 }
 
@@ -491,18 +625,116 @@ static int validate_common(const rfba_srrf_config* cfg, const void* in, const in
 
 static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const void* in, rfba_dtype dtype,
                                  const int dims[4], const rfba_block* blocks, int nblocks, float* out,
-                                 long long out_elems, int flags, cudaStream_t st, bool zero_out);
+                                 long long out_elems, int flags, cudaStream_t st, bool zero_out, bool fast = false);
 
 static int forward_blocks_impl(rfba_ctx* ctx, const rfba_srrf_config* cfg, const void* in, rfba_dtype dtype,
                                const int dims[4], const rfba_block* blocks, int nblocks, float* out, long long out_elems,
-                               int flags, cudaStream_t st, bool zero_out) {
+                               int flags, cudaStream_t st, bool zero_out, bool fast = false) {
     std::lock_guard<std::mutex> lk(ctx->mu);
-    return forward_blocks_locked(ctx, cfg, in, dtype, dims, blocks, nblocks, out, out_elems, flags, st, zero_out);
+    return forward_blocks_locked(ctx, cfg, in, dtype, dims, blocks, nblocks, out, out_elems, flags, st, zero_out,
+                                 fast);
+}
+
+static bool env_on(const char* name, bool dflt) {
+    const char* e = std::getenv(name);
+    if (!e || !*e) return dflt;
+    return !(e[0] == '0' && e[1] == 0);
+}
+
+// Calls below this many voxel-volumes keep the default schedule (RFBA_TUNE_MIN overrides).
+static long long tune_min_work() {
+    const char* e = std::getenv("RFBA_TUNE_MIN");
+    return (e && *e) ? std::atoll(e) : 200000000LL;
+}
+
+static bool host_pinned(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+template <typename T>
+static void key_put(std::string* k, const T* p, size_t n) {
+    k->append(reinterpret_cast<const char*>(p), n * sizeof(T));
+}
+
+// Schedule key: what the best tile shape / order depends on.
+static std::string sched_key(const rfba_srrf_config& cfg, rfba_dtype dtype, const int dims[4],
+                             const rfba_block* blocks, int nblocks) {
+    std::string k;
+    key_put(&k, &cfg, 1);
+    key_put(&k, &dtype, 1);
+    key_put(&k, dims, 4);
+    for (int i = 0; i < nblocks; ++i) {
+        key_put(&k, blocks[i].size, 3);
+        key_put(&k, blocks[i].lo, 3);
+        key_put(&k, blocks[i].hi, 3);
+    }
+    return k;
+}
+
+// Autotuner: time every candidate schedule (tile rows valid for mag_y, and for
+// block lists the two tile orders) on the first few volumes of this call's
+// own input, keep the fastest.
+static int autotune(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void* in_dev, rfba_dtype dtype,
+                    const int dims[4], const rfba_block* blocks, int nblocks, float* out_dev, cudaStream_t st,
+                    Tuning* best) {
+    const int my = cfg.mag[1];
+    std::vector<int> tys;
+    for (int ty : {8, 12, 16, 24})
+        if (ty % (2 * my) == 0 && ty * (kTileX / 2) <= kMaxThreads) tys.push_back(ty);
+    const int dty = tile_rows_for_mag(my);
+    if (std::find(tys.begin(), tys.end(), dty) == tys.end()) tys.push_back(dty);
+    std::vector<int> orders = {0};
+    if (nblocks > 1) orders.push_back(1);
+    const int sd[4] = {dims[0], dims[1], dims[2], std::min(dims[3], 3)};
+    cudaEvent_t e0, e1;
+    RFBA_CUDA(cudaEventCreate(&e0), "event");
+    RFBA_CUDA(cudaEventCreate(&e1), "event");
+    float best_ms = 0.f;
+    int rc = RFBA_OK;
+    bool have = false;
+    const bool timing = ctx->timing;
+    ctx->timing = false;
+    for (int ty : tys) {
+        for (int order : orders) {
+            Tuning t;
+            t.ty = ty;
+            t.order = order;
+            std::vector<BlockDev> all;
+            if ((rc = make_blocks(ctx, cfg, sd, blocks, nblocks, &all, ty))) break;
+            float ms = 0.f;
+            for (int rep = 0; rep < 2 && !rc; ++rep) {
+                if (rep == 1) cudaEventRecord(e0, st);
+                rc = run_device(ctx, cfg, in_dev, dtype, sd, all, out_dev, st, t);
+                if (rep == 1) cudaEventRecord(e1, st);
+            }
+            if (rc) break;
+            if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+                rc = cuda_fail(cudaGetLastError(), "autotune timing");
+                break;
+            }
+            if (verbose()) std::fprintf(stderr, "rfba: autotune ty=%d order=%d %.3f ms\n", ty, order, ms);
+            if (!have || ms < best_ms) {
+                best_ms = ms;
+                *best = t;
+                have = true;
+            }
+        }
+        if (rc) break;
+    }
+    ctx->timing = timing;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
 }
 
 static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const void* in, rfba_dtype dtype,
                                  const int dims[4], const rfba_block* blocks, int nblocks, float* out,
-                                 long long out_elems, int flags, cudaStream_t st, bool zero_out) {
+                                 long long out_elems, int flags, cudaStream_t st, bool zero_out, bool fast) {
     int s = validate_common(cfg, in, dims, out);
     if (s) return s;
     if (nblocks < 0 || (nblocks > 0 && !blocks) || out_elems < 0) {
@@ -518,6 +750,7 @@ static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, con
     if ((s = ensure_plan(ctx, *cfg, st))) return s;
     std::vector<BlockDev> all;
     if ((s = make_blocks(ctx, *cfg, dims, blocks, nblocks, &all))) return s;
+    long long work = 0;
     for (const BlockDev& b : all) {
         const long long last = b.out_offset + (long long)(b.nreg[0] - 1) * b.out_stride[0] +
                                (long long)(b.nreg[1] - 1) * b.out_stride[1] + (long long)(b.nreg[2] - 1) * b.out_stride[2];
@@ -525,8 +758,151 @@ static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, con
             set_error("block output outside the output array");
             return RFBA_ERR_INVALID;
         }
+        work += b.vox * dims[3];
     }
     const size_t in_bytes = (size_t)dims[0] * dims[1] * dims[2] * dims[3] * elem_size(dtype);
+    ctx->last_ty = tile_rows_for_mag(cfg->mag[1]);
+    ctx->last_order = 0;
+    ctx->last_graph = 0;
+    ctx->last_tuned = 0;
+    if (fast) {
+        // schedule: autotuned once per (configuration, dims, block shapes)
+        Tuning tune;
+        const std::string tkey = sched_key(*cfg, dtype, dims, blocks, nblocks);
+        auto it = ctx->tunes.find(tkey);
+        if (it != ctx->tunes.end()) {
+            tune.ty = it->second.first;
+            tune.order = it->second.second;
+        } else if (env_on("RFBA_TUNE", true) && work >= tune_min_work()) {
+            const void* tin = in;
+            float* tout = out;
+            if (flags == RFBA_HOST_PTRS) {
+                // the first volumes of the input are enough for the timing runs
+                const size_t sample = (size_t)dims[0] * dims[1] * dims[2] * std::min(dims[3], 3) * elem_size(dtype);
+                if ((s = ctx->in.ensure(in_bytes, "input"))) return s;
+                if ((s = ctx->out.ensure((size_t)out_elems * 4, "output"))) return s;
+                RFBA_CUDA(cudaMemcpyAsync(ctx->in.p, in, sample, cudaMemcpyHostToDevice, st), "input copy");
+                tin = ctx->in.p;
+                tout = static_cast<float*>(ctx->out.p);
+            }
+            if ((s = autotune(ctx, *cfg, tin, dtype, dims, blocks, nblocks, tout, st, &tune))) return s;
+            ctx->tunes[tkey] = std::make_pair(tune.ty, tune.order);
+            ctx->last_tuned = 1;
+        }
+        if (tune.ty > 0 && tune.ty != tile_rows_for_mag(cfg->mag[1]) &&
+            (s = make_blocks(ctx, *cfg, dims, blocks, nblocks, &all, tune.ty)))
+            return s;
+        ctx->last_ty = tune.ty > 0 ? tune.ty : tile_rows_for_mag(cfg->mag[1]);
+        ctx->last_order = tune.order;
+        // replay: the whole call as one CUDA graph (device pointers, or pinned host buffers)
+        const bool graphable = flags == RFBA_DEVICE_PTRS || (host_pinned(in) && host_pinned(out));
+        if (graphable && env_on("RFBA_GRAPH", true)) {
+            std::string gkey = tkey;
+            key_put(&gkey, &in, 1);
+            key_put(&gkey, &out, 1);
+            key_put(&gkey, &out_elems, 1);
+            key_put(&gkey, &flags, 1);
+            key_put(&gkey, &zero_out, 1);
+            key_put(&gkey, blocks, (size_t)nblocks);
+            const bool host = flags == RFBA_HOST_PTRS;
+            auto deps_now = [&]() {
+                return std::vector<const void*>{ctx->rad.p, ctx->inten.p, ctx->tables.p, host ? ctx->in.p : nullptr,
+                                                host ? ctx->out.p : nullptr};
+            };
+            GraphPlan* gp = nullptr;
+            for (size_t i = 0; i < ctx->graphs.size(); ++i)
+                if (ctx->graphs[i]->key == gkey && ctx->graphs[i]->deps == deps_now()) {
+                    std::unique_ptr<GraphPlan> g = std::move(ctx->graphs[i]);
+                    ctx->graphs.erase(ctx->graphs.begin() + i);
+                    ctx->graphs.insert(ctx->graphs.begin(), std::move(g));
+                    gp = ctx->graphs.front().get();
+                    break;
+                }
+            if (!gp) {
+                std::unique_ptr<GraphPlan> g(new GraphPlan());
+                g->key = gkey;
+                Tuning t2 = tune;
+                if ((s = plan_passes(ctx, *cfg, dtype, dims, all, t2, &g->ps))) return s;
+                const PassSet& ps = g->ps;
+                const size_t np = ps.passes.size();
+                if ((s = ctx->rad.ensure((size_t)ps.max_stack * 4, "radiality stack"))) return s;
+                if ((s = ctx->inten.ensure((size_t)ps.max_stack * 4, "intensity stack"))) return s;
+                if (host) {
+                    if ((s = ctx->in.ensure(in_bytes, "input"))) return s;
+                    if ((s = ctx->out.ensure((size_t)out_elems * 4, "output"))) return s;
+                }
+                if ((s = g->blocks.ensure(ps.blocks.size() * sizeof(BlockDev), "blocks")) ||
+                    (s = g->tiles.ensure(ps.tiles.size() * sizeof(TileDesc), "tiles")) ||
+                    (s = g->prefix.ensure(ps.prefix.size() * sizeof(long long), "prefix")) ||
+                    (s = g->counters.ensure(np * 256, "counters")) || (s = ensure_events(ctx, &g->evs, 3 * np)))
+                    return s;
+                RFBA_CUDA(cudaMemcpy(g->blocks.p, ps.blocks.data(), ps.blocks.size() * sizeof(BlockDev),
+                                     cudaMemcpyHostToDevice), "blocks upload");
+                RFBA_CUDA(cudaMemcpy(g->tiles.p, ps.tiles.data(), ps.tiles.size() * sizeof(TileDesc),
+                                     cudaMemcpyHostToDevice), "tiles upload");
+                RFBA_CUDA(cudaMemcpy(g->prefix.p, ps.prefix.data(), ps.prefix.size() * sizeof(long long),
+                                     cudaMemcpyHostToDevice), "prefix upload");
+                if (!ctx->cap) RFBA_CUDA(cudaStreamCreateWithFlags(&ctx->cap, cudaStreamNonBlocking), "stream");
+                const void* gin = host ? ctx->in.p : in;
+                float* gout = host ? static_cast<float*>(ctx->out.p) : out;
+                RFBA_CUDA(cudaStreamBeginCapture(ctx->cap, cudaStreamCaptureModeThreadLocal), "graph capture");
+                int cs = RFBA_OK;
+                cudaError_t ce = cudaSuccess;
+                if (host) {
+                    ce = cudaMemcpyAsync(ctx->in.p, in, in_bytes, cudaMemcpyHostToDevice, ctx->cap);
+                    if (ce == cudaSuccess) ce = cudaMemsetAsync(gout, 0, (size_t)out_elems * 4, ctx->cap);
+                } else if (zero_out) {
+                    ce = cudaMemsetAsync(gout, 0, (size_t)out_elems * 4, ctx->cap);
+                }
+                if (ce == cudaSuccess)
+                    cs = enqueue_passes(ctx, *cfg, gin, dtype, dims, ps, static_cast<const BlockDev*>(g->blocks.p),
+                                        static_cast<const TileDesc*>(g->tiles.p),
+                                        static_cast<const long long*>(g->prefix.p),
+                                        static_cast<unsigned int*>(g->counters.p), gout, ctx->cap, g->evs.data());
+                if (ce == cudaSuccess && cs == RFBA_OK && host)
+                    ce = cudaMemcpyAsync(out, gout, (size_t)out_elems * 4, cudaMemcpyDeviceToHost, ctx->cap);
+                cudaGraph_t graph = nullptr;
+                const cudaError_t ee = cudaStreamEndCapture(ctx->cap, &graph);
+                if (ce != cudaSuccess || cs != RFBA_OK || ee != cudaSuccess) {
+                    if (graph) cudaGraphDestroy(graph);
+                    if (cs != RFBA_OK) return cs;
+                    return cuda_fail(ce != cudaSuccess ? ce : ee, "graph capture");
+                }
+                ce = cudaGraphInstantiate(&g->exec, graph, 0);
+                cudaGraphDestroy(graph);
+                if (ce != cudaSuccess) return cuda_fail(ce, "graph instantiate");
+                g->deps = deps_now();
+                ctx->graphs.insert(ctx->graphs.begin(), std::move(g));
+                while (ctx->graphs.size() > 4) ctx->graphs.pop_back();
+                gp = ctx->graphs.front().get();
+            }
+            ctx->train.valid = false;
+            RFBA_CUDA(cudaGraphLaunch(gp->exec, st), "graph launch");
+            account(ctx, gp->ps);
+            ctx->last_graph = 1;
+            if (ctx->timing && (s = collect_timing(ctx, gp->ps, gp->evs))) return s;
+            if (host) RFBA_CUDA(cudaStreamSynchronize(st), "synchronize");
+            return RFBA_OK;
+        }
+        const void* in_dev = in;
+        float* out_dev = out;
+        if (flags == RFBA_HOST_PTRS) {
+            if ((s = ctx->in.ensure(in_bytes, "input"))) return s;
+            if ((s = ctx->out.ensure((size_t)out_elems * 4, "output"))) return s;
+            RFBA_CUDA(cudaMemcpyAsync(ctx->in.p, in, in_bytes, cudaMemcpyHostToDevice, st), "input copy");
+            in_dev = ctx->in.p;
+            out_dev = static_cast<float*>(ctx->out.p);
+            RFBA_CUDA(cudaMemsetAsync(out_dev, 0, (size_t)out_elems * 4, st), "output clear");
+        } else if (zero_out) {
+            RFBA_CUDA(cudaMemsetAsync(out_dev, 0, (size_t)out_elems * 4, st), "output clear");
+        }
+        if ((s = run_device(ctx, *cfg, in_dev, dtype, dims, all, out_dev, st, tune))) return s;
+        if (flags == RFBA_HOST_PTRS) {
+            RFBA_CUDA(cudaMemcpyAsync(out, out_dev, (size_t)out_elems * 4, cudaMemcpyDeviceToHost, st), "output copy");
+            RFBA_CUDA(cudaStreamSynchronize(st), "synchronize");
+        }
+        return RFBA_OK;
+    }
     const void* in_dev = in;
     float* out_dev = out;
     if (flags == RFBA_HOST_PTRS) {
@@ -827,6 +1203,9 @@ int rfba_ctx_destroy(rfba_ctx* c) {
         b->release();
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
+    c->graphs.clear();
+    for (cudaEvent_t e : c->pev) cudaEventDestroy(e);
+    if (c->cap) cudaStreamDestroy(c->cap);
     if (c->xev) cudaEventDestroy(c->xev);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -845,6 +1224,14 @@ int rfba_ctx_last_timing(rfba_ctx* c, double* rad_ms, double* temporal_ms, long 
     if (rad_ms) *rad_ms = c->last_rad_ms;
     if (temporal_ms) *temporal_ms = c->last_temporal_ms;
     if (launches) *launches = c->launches;
+    return RFBA_OK;
+}
+int rfba_ctx_last_schedule(rfba_ctx* c, int* tile_rows, int* tile_order, int* graph, int* tuned) {
+    if (!c) return RFBA_ERR_INVALID;
+    if (tile_rows) *tile_rows = c->last_ty;
+    if (tile_order) *tile_order = c->last_order;
+    if (graph) *graph = c->last_graph;
+    if (tuned) *tuned = c->last_tuned;
     return RFBA_OK;
 }
 int rfba_ctx_set_launch(rfba_ctx* c, int grid, int t_chunk) {
@@ -934,7 +1321,8 @@ int rfba_srrf_forward_blocks(rfba_ctx* ctx, const rfba_srrf_config* cfg, const v
         return RFBA_ERR_INVALID;
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL = legacy default stream
-    return forward_blocks_impl(ctx, cfg, in, dtype, dims, blocks, nblocks, out, out_elems, ptr_flags, st, false);
+    return forward_blocks_impl(ctx, cfg, in, dtype, dims, blocks, nblocks, out, out_elems, ptr_flags, st, false,
+                               true);
 }
 
 int rfba_srrf_forward(rfba_ctx* ctx, const rfba_srrf_config* cfg, const void* in, rfba_dtype dtype, const int dims[4],
@@ -954,7 +1342,7 @@ int rfba_srrf_forward(rfba_ctx* ctx, const rfba_srrf_config* cfg, const void* in
     b.out_stride[2] = (int64_t)b.hi[0] * b.hi[1];
     const int64_t n = (int64_t)b.hi[0] * b.hi[1] * b.hi[2];
     cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL = legacy default stream
-    return forward_blocks_impl(ctx, cfg, in, dtype, dims, &b, 1, out, n, ptr_flags, st, false);
+    return forward_blocks_impl(ctx, cfg, in, dtype, dims, &b, 1, out, n, ptr_flags, st, false, true);
 }
 
 int rfba_srrf_forward_blocks_plain(rfba_ctx* ctx, const rfba_srrf_config* cfg, const void* in, rfba_dtype dtype,

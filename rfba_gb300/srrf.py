@@ -119,6 +119,7 @@ def lib():
         L.rfba_ctx_last_timing.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                                            ctypes.POINTER(ctypes.c_longlong)]
         L.rfba_ctx_set_launch.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+        L.rfba_ctx_last_schedule.argtypes = [vp, ip, ip, ip, ip]
         L.rfba_srrf_config_default.argtypes = [cp]
         L.rfba_srrf_config_load_ini.argtypes = [ctypes.c_char_p, cp]
         L.rfba_srrf_config_from_legacy.argtypes = [ctypes.POINTER(SRRFConf), cp]
@@ -268,6 +269,13 @@ class Context:
 
     def set_launch(self, grid: int = 0, t_chunk: int = 0):
         _check(lib().rfba_ctx_set_launch(self.h, grid, t_chunk))
+
+    def schedule(self) -> dict:
+        """Schedule of the last forward: tile rows, tile order, graph replay, autotuned now."""
+        v = [ctypes.c_int() for _ in range(4)]
+        _check(lib().rfba_ctx_last_schedule(self.h, *[ctypes.byref(x) for x in v]))
+        return {"tile_rows": v[0].value, "tile_order": v[1].value, "graph": bool(v[2].value),
+                "tuned": bool(v[3].value)}
 
     def timing(self) -> Timing:
         a, b, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
