@@ -399,6 +399,7 @@ static int plan_passes(rfba_ctx* ctx, const rfba_srrf_config& cfg, rfba_dtype dt
     ps->max_stack = 0;
     ps->ty = tune.ty > 0 ? tune.ty : tile_rows_for_mag(cfg.mag[1]);
     RadParams rp = fill_rad_params(ctx, cfg, nullptr, dims, cz_for_mag(cfg.mag[2]), ps->ty);
+    rp.tma_bx = radiality_tma_box_x(rp, dtype == RFBA_U16);
     const size_t smem = radiality_smem_bytes(rp);
     if (smem > 227 * 1024) {
         set_error("shared memory tile too large for this configuration");
@@ -494,12 +495,18 @@ static int plan_passes(rfba_ctx* ctx, const rfba_srrf_config& cfg, rfba_dtype dt
 static int enqueue_passes(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void* in_dev, rfba_dtype dtype,
                           const int dims[4], const PassSet& ps, const BlockDev* dblocks, const TileDesc* dtiles,
                           const long long* dprefix, unsigned int* dcounters, float* out_dev, cudaStream_t st,
-                          const cudaEvent_t* evs) {
+                          const cudaEvent_t* evs, bool capturing = false) {
+    // inside a stream capture the events become event-record nodes of the graph
+    auto rec = [&](cudaEvent_t e) {
+        return capturing ? cudaEventRecordWithFlags(e, st, cudaEventRecordExternal) : cudaEventRecord(e, st);
+    };
     for (size_t i = 0; i < ps.passes.size(); ++i) {
         const PassPlan& pp = ps.passes[i];
         unsigned int* counter = dcounters + 64 * i;
         RFBA_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned int), st), "counter reset");
         RadParams rp = fill_rad_params(ctx, cfg, in_dev, dims, cz_for_mag(cfg.mag[2]), ps.ty);
+        rp.tma_bx = radiality_tma_box_x(rp, dtype == RFBA_U16);
+        rp.err = static_cast<unsigned long long*>(ctx->errw.p);
         rp.blocks = dblocks + pp.b0;
         rp.tiles = dtiles + pp.t0;
         rp.ntiles = (int)(pp.t1 - pp.t0);
@@ -523,13 +530,13 @@ static int enqueue_passes(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void
         tp.rad_stack = rp.rad_stack;
         tp.int_stack = rp.int_stack;
         tp.out = out_dev;
-        if (evs) RFBA_CUDA(cudaEventRecord(evs[3 * i], st), "event");
+        if (evs) RFBA_CUDA(rec(evs[3 * i]), "event");
         int le = launch_radiality(rp, pp.grid, pp.smem, dtype == RFBA_U16, st);
         if (le != 0) return cuda_fail((cudaError_t)le, "radiality launch");
-        if (evs) RFBA_CUDA(cudaEventRecord(evs[3 * i + 1], st), "event");
+        if (evs) RFBA_CUDA(rec(evs[3 * i + 1]), "event");
         le = launch_temporal(tp, st);
         if (le != 0) return cuda_fail((cudaError_t)le, "temporal launch");
-        if (evs) RFBA_CUDA(cudaEventRecord(evs[3 * i + 2], st), "event");
+        if (evs) RFBA_CUDA(rec(evs[3 * i + 2]), "event");
         if (verbose())
             std::fprintf(stderr, "rfba: pass blocks=%zu tiles=%d ty=%d chunk=%d items=%lld grid=%d smem=%zu\n",
                          pp.b1 - pp.b0, rp.ntiles, ps.ty, pp.chunk, pp.nitems, pp.grid, pp.smem);
@@ -575,6 +582,7 @@ static int run_device(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void* in
     ctx->train.valid = false;
     PassSet ps;
     int s;
+    if ((s = ctx->errw.ensure(256, "check word"))) return s;
     if ((s = plan_passes(ctx, cfg, dtype, dims, all, tune, &ps))) return s;
     const size_t np = ps.passes.size();
     if ((s = ctx->rad.ensure((size_t)ps.max_stack * 4, "radiality stack"))) return s;
@@ -806,8 +814,8 @@ static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, con
             key_put(&gkey, blocks, (size_t)nblocks);
             const bool host = flags == RFBA_HOST_PTRS;
             auto deps_now = [&]() {
-                return std::vector<const void*>{ctx->rad.p, ctx->inten.p, ctx->tables.p, host ? ctx->in.p : nullptr,
-                                                host ? ctx->out.p : nullptr};
+                return std::vector<const void*>{ctx->rad.p, ctx->inten.p, ctx->tables.p, ctx->errw.p,
+                                                host ? ctx->in.p : nullptr, host ? ctx->out.p : nullptr};
             };
             GraphPlan* gp = nullptr;
             for (size_t i = 0; i < ctx->graphs.size(); ++i)
@@ -822,6 +830,7 @@ static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, con
                 std::unique_ptr<GraphPlan> g(new GraphPlan());
                 g->key = gkey;
                 Tuning t2 = tune;
+                if ((s = ctx->errw.ensure(256, "check word"))) return s;
                 if ((s = plan_passes(ctx, *cfg, dtype, dims, all, t2, &g->ps))) return s;
                 const PassSet& ps = g->ps;
                 const size_t np = ps.passes.size();
@@ -858,7 +867,8 @@ static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, con
                     cs = enqueue_passes(ctx, *cfg, gin, dtype, dims, ps, static_cast<const BlockDev*>(g->blocks.p),
                                         static_cast<const TileDesc*>(g->tiles.p),
                                         static_cast<const long long*>(g->prefix.p),
-                                        static_cast<unsigned int*>(g->counters.p), gout, ctx->cap, g->evs.data());
+                                        static_cast<unsigned int*>(g->counters.p), gout, ctx->cap, g->evs.data(),
+                                        true);
                 if (ce == cudaSuccess && cs == RFBA_OK && host)
                     ce = cudaMemcpyAsync(out, gout, (size_t)out_elems * 4, cudaMemcpyDeviceToHost, ctx->cap);
                 cudaGraph_t graph = nullptr;

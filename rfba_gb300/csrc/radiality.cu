@@ -6,8 +6,10 @@
 // persistent kernel. Per work item (block, subvoxel tile, time chunk) and time
 // point:
 //
-//   1. the input tile plus halo is read (block-edge clamped, as the
-//      reference's fminf/fmaxf clamps do) into shared memory;
+//   1. the input tile plus halo is staged into shared memory by a TMA tensor
+//      copy (requested one time point ahead) and converted to float with the
+//      reference's block-edge clamp (its fminf/fmaxf clamps); inputs whose rows
+//      a tensor map cannot address are read with plain loads instead;
 //   2. the smoothed gradient G = (Gx, Gy, Gz) and the intensity I of every
 //      coarse cell the tile's taps reach is formed in shared memory (float4);
 //   3. the ring's n^2 samples are reduced to their distinct points (62 for
@@ -41,13 +43,61 @@
 // (kernel.cu:146) makes a whole subvoxel NaN; it is evaluated on the host per
 // axis with the reference's float arithmetic and applied here as a per-block
 // valid box.
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+
+#include <cudaTypedefs.h>
 
 #include "srrf_internal.h"
 
 namespace rfba {
 namespace {
+
+// ---- TMA staging of the input tile ----------------------------------------
+// The tile's input box (x rounded down to a 16-byte boundary, so the box is
+// wider by up to 15 bytes) is copied by one cp.async.bulk.tensor per time point
+// into a staging area, completion signalled on an mbarrier. The next time
+// point's box is requested as soon as the current one has been converted, so
+// the copy overlaps the radiality work. Coordinates outside the volume read
+// zeros; the reference's block-edge clamp is applied when the staging area is
+// converted to float (clamped positions always lie inside the box).
+__device__ __forceinline__ unsigned smem_u32(const void* ptr) {
+    return (unsigned)__cvta_generic_to_shared(ptr);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tma_load_box(void* dst, const CUtensorMap* map, uint64_t* bar, unsigned bytes, int x,
+                                             int y, int z, int t) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(t), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait for the staging phase; false after the iteration limit.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
+    for (int i = 0; i < (1 << 22); ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
 
 __device__ __forceinline__ float rsqrt_approx(float x) {
     float r;
@@ -136,18 +186,28 @@ __device__ __forceinline__ float4 gradient_generic(const float* base, int NIX, i
 }
 
 template <int MZ, int CZ, typename Tin, bool WIDE>
-__global__ void __launch_bounds__(WIDE ? kMaxThreads : 128, WIDE ? 2 : 3) radiality_kernel(const RadParams p) {
+__global__ void __launch_bounds__(WIDE ? kMaxThreads : 128, WIDE ? 2 : 3)
+    radiality_kernel(const RadParams p, const __grid_constant__ CUtensorMap tmap) {
     constexpr int FZ = MZ * CZ;
     constexpr int NW = CZ + 4;
     extern __shared__ float4 smem4[];
 
-    // Shared layout: [G tile float4][U tile float4][input tile][tables]
+    // Shared layout: [G tile float4][U tile float4][input tile][tables][TMA staging, 128-byte aligned]
     const int NU = p.NU, NV = p.NV;
     float4* gt = smem4;                           // [NW][NV][NU]
     float4* ut = gt + NU * NV * NW;               // [NW][NV][16]
     float* inp = reinterpret_cast<float*>(ut + kTileX * NV * NW);  // [NIZ][NIY][NIX]
     float* tab = inp + ((p.NIX * p.NIY * p.NIZ + 3) & ~3);         // 16-byte aligned (float4 reads)
+    Tin* stage = reinterpret_cast<Tin*>((reinterpret_cast<uintptr_t>(tab + p.smem_table_words) + 127) &
+                                        ~(uintptr_t)127);           // [NIZ][NIY][tma_bx]
     __shared__ unsigned int s_item;
+    __shared__ alignas(8) uint64_t s_bar;
+    const bool use_tma = p.use_tma != 0;
+    unsigned phase = 0;
+    if (use_tma && threadIdx.x == 0) {
+        mbar_init(&s_bar, 1);
+        fence_mbar_init();
+    }
 
     const int nthr = blockDim.x;
     const int tid = threadIdx.x;
@@ -175,7 +235,6 @@ __global__ void __launch_bounds__(WIDE ? kMaxThreads : 128, WIDE ? 2 : 3) radial
 
     const Tin* in = static_cast<const Tin*>(p.in);
     const int NIX = p.NIX, NIY = p.NIY, NIZ = p.NIZ, R = p.R;
-    const int nin = NIX * NIY * NIZ;
     const int ncell = NU * NV * NW;
     const int nut = kTileX * NV * NW;
 
@@ -218,22 +277,66 @@ __global__ void __launch_bounds__(WIDE ? kMaxThreads : 128, WIDE ? 2 : 3) radial
 
         const int t0 = chunk * p.t_chunk;
         const int t1 = min(p.T, t0 + p.t_chunk);
+        // TMA box origin: x rounded down to a 16-byte boundary; the offset back
+        // (0 .. 16 bytes / element size - 1) is where the tile starts in a staged row
+        constexpr int kAl = 16 / (int)sizeof(Tin);
+        auto box_ox = [&]() {
+            const int gx0 = B.origin[0] + cx0 - R;
+            return ((gx0 % kAl) + kAl) % kAl;
+        };
+        auto issue = [&](int tt) {
+            const int gx0 = B.origin[0] + cx0 - R;
+            tma_load_box(stage, &tmap, &s_bar, (unsigned)(p.tma_bx * NIY * NIZ * (int)sizeof(Tin)), gx0 - box_ox(),
+                         B.origin[1] + cy0 - R, B.origin[2] + cz0 - R, tt);
+        };
+        if (use_tma && tid == 0) {
+            fence_proxy_async();  // the previous item's generic reads of the staging area come first
+            issue(t0);
+        }
         for (int t = t0; t < t1; ++t) {
             const long long sbase = B.stack_off + (long long)t * V;
             // 1. input tile with block-edge clamp; 16 lanes per row, one division
             //    per row
             const long long tbase = (long long)t * p.D * p.H * p.W;
-            for (int r = tid / kTileX; r < NIY * NIZ; r += nthr / kTileX) {
-                const int iy = r % NIY, iz = r / NIY;
-                const int by = clampi(cy0 - R + iy, 0, bh - 1);
-                const int bz = clampi(cz0 - R + iz, 0, bd - 1);
-                const long long rowg = tbase + ((long long)(B.origin[2] + bz) * p.H + (B.origin[1] + by)) * p.W +
-                                       B.origin[0];
-                float* rows = inp + r * NIX;
-                for (int ix = xf; ix < NIX; ix += kTileX)
-                    rows[ix] = load_in<Tin>(in, rowg + clampi(cx0 - R + ix, 0, bw - 1));
+            if (use_tma) {
+                const bool ok = mbar_wait_bounded(&s_bar, phase);
+                if (__syncthreads_or(!ok)) {
+                    // the copy did not land: record it, give it a bounded time to
+                    // finish so no write is pending into this CTA's shared memory
+                    if (tid == 0) {
+                        if (p.err) atomicCAS(p.err, 0ull, (0x54ull << 56) | (unsigned long long)item);
+                        mbar_wait_bounded(&s_bar, phase);
+                    }
+                    return;
+                }
+                phase ^= 1u;
+                for (int r = tid / kTileX; r < NIY * NIZ; r += nthr / kTileX) {
+                    const int iy = r % NIY, iz = r / NIY;
+                    const int sy = clampi(cy0 - R + iy, 0, bh - 1) - (cy0 - R);
+                    const int sz = clampi(cz0 - R + iz, 0, bd - 1) - (cz0 - R);
+                    const Tin* srow = stage + (sz * NIY + sy) * p.tma_bx + box_ox();
+                    float* rows = inp + r * NIX;
+                    for (int ix = xf; ix < NIX; ix += kTileX)
+                        rows[ix] = (float)srow[clampi(cx0 - R + ix, 0, bw - 1) - (cx0 - R)];
+                }
+                __syncthreads();
+                if (tid == 0 && t + 1 < t1) {
+                    fence_proxy_async();  // the staging area's generic reads before the next async write
+                    issue(t + 1);
+                }
+            } else {
+                for (int r = tid / kTileX; r < NIY * NIZ; r += nthr / kTileX) {
+                    const int iy = r % NIY, iz = r / NIY;
+                    const int by = clampi(cy0 - R + iy, 0, bh - 1);
+                    const int bz = clampi(cz0 - R + iz, 0, bd - 1);
+                    const long long rowg = tbase + ((long long)(B.origin[2] + bz) * p.H + (B.origin[1] + by)) * p.W +
+                                           B.origin[0];
+                    float* rows = inp + r * NIX;
+                    for (int ix = xf; ix < NIX; ix += kTileX)
+                        rows[ix] = load_in<Tin>(in, rowg + clampi(cx0 - R + ix, 0, bw - 1));
+                }
+                __syncthreads();
             }
-            __syncthreads();
             // 2. gradient + intensity per coarse cell
             for (int c = tid; c < ncell; c += nthr) {
                 const int u = c % NU;
@@ -418,13 +521,55 @@ __global__ void __launch_bounds__(WIDE ? kMaxThreads : 128, WIDE ? 2 : 3) radial
     }
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda
+// link dependency).
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
+// 4D tensor map (x, y, z, t) of the input with the tile's staging box; false
+// (plain loads) when TMA staging is off for this launch or the input cannot be
+// described (base or row pitch not 16-byte aligned).
+bool encode_input_map(const RadParams& p, int es, CUtensorMap* map) {
+    std::memset(map, 0, sizeof *map);
+    if (p.tma_bx <= 0) return false;
+    if ((reinterpret_cast<uintptr_t>(p.in) & 15) != 0 || ((long long)p.W * es) % 16 != 0) return false;
+    if (p.tma_bx > 256 || p.NIY > 256 || p.NIZ > 256 || (p.tma_bx * es) % 16 != 0) return false;
+    PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
+    if (!fn) return false;
+    const cuuint64_t dim[4] = {(cuuint64_t)p.W, (cuuint64_t)p.H, (cuuint64_t)p.D, (cuuint64_t)p.T};
+    const cuuint64_t stride[3] = {(cuuint64_t)p.W * es, (cuuint64_t)p.W * p.H * es, (cuuint64_t)p.W * p.H * p.D * es};
+    const cuuint32_t box[4] = {(cuuint32_t)p.tma_bx, (cuuint32_t)p.NIY, (cuuint32_t)p.NIZ, 1u};
+    const cuuint32_t estr[4] = {1u, 1u, 1u, 1u};
+    const CUresult r = fn(map, es == 2 ? CU_TENSOR_MAP_DATA_TYPE_UINT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
+                          const_cast<void*>(p.in), dim, stride, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
 template <int MZ, typename Tin>
 int launch_mz(const RadParams& p, int grid, size_t smem, cudaStream_t st) {
     constexpr int CZ = cz_for_mag(MZ);
     auto k = p.TY > 16 ? radiality_kernel<MZ, CZ, Tin, true> : radiality_kernel<MZ, CZ, Tin, false>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
-    k<<<grid, p.TY * (kTileX / 2), smem, st>>>(p);
+    RadParams q = p;
+    CUtensorMap map;
+    q.use_tma = encode_input_map(p, (int)sizeof(Tin), &map) ? 1 : 0;
+    k<<<grid, p.TY * (kTileX / 2), smem, st>>>(q, map);
     return (int)cudaGetLastError();
 }
 
@@ -484,7 +629,21 @@ size_t radiality_smem_bytes(const RadParams& p) {
     const int NW = cz_for_mag(p.mag[2]) + 4;
     size_t b = sizeof(float4) * ((size_t)p.NU * p.NV * NW + (size_t)kTileX * p.NV * NW);
     b += sizeof(float) * ((((size_t)p.NIX * p.NIY * p.NIZ + 3) & ~(size_t)3) + p.smem_table_words);
+    if (p.tma_bx > 0) {
+        // staging box (element size 4 covers both input types), 128-byte aligned start
+        b += 128 + (size_t)p.tma_bx * p.NIY * p.NIZ * 4;
+    }
     return (b + 15) & ~(size_t)15;
+}
+
+int radiality_tma_box_x(const RadParams& p, int in_u16) {
+    const int es = in_u16 ? 2 : 4;
+    const int al = 16 / es;
+    if (((long long)p.W * es) % 16 != 0) return 0;
+    const char* e = std::getenv("RFBA_TMA");
+    if (e && e[0] == '0' && e[1] == 0) return 0;
+    const int bx = ((p.NIX + al - 1 + al - 1) / al) * al;  // NIX + up to al - 1 of alignment slack
+    return bx <= 256 ? bx : 0;
 }
 
 int launch_radiality(const RadParams& p, int grid, size_t smem, int in_u16, void* stream) {

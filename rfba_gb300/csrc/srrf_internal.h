@@ -110,6 +110,11 @@ struct RadParams {
     float* int_stack;
     unsigned int* work_counter;
     int smem_table_words;
+    // TMA staging of the input tile (forward only): box width in elements
+    // (0 = no staging area) and whether this launch uses it
+    int tma_bx;
+    int use_tma;
+    unsigned long long* err;  // bounded-wait failures (may be null)
 };
 
 // Temporal reduction parameters.
@@ -148,6 +153,9 @@ int launch_drift_dot(const float* g, const float* dv, long long nv, int T, int a
                      unsigned long long* err, void* stream);
 int launch_double_to_float(const double* src, float* dst, int n, void* stream);
 int launch_radiality(const RadParams& p, int grid, size_t smem, int in_u16, void* stream);
+// Box width (elements) of the TMA input staging for this tile, 0 when the input
+// rows cannot be addressed by a tensor map (row pitch not a multiple of 16 B).
+int radiality_tma_box_x(const RadParams& p, int in_u16);
 size_t radiality_smem_bytes(const RadParams& p);
 int tile_rows_for_mag(int my);
 int radiality_max_ctas_per_sm(const RadParams& p, int in_u16, int* out);

@@ -104,3 +104,21 @@ def test_graph_rebuilt_after_scratch_grows(ctx, env):
     o1.fill_(0)
     ctx.forward(cfg, sd, out=o1)
     assert _same(o1.cpu().numpy(), ref_small)
+
+
+def test_graph_replay_reports_kernel_times(ctx, env):
+    """Kernel times of a replayed graph come from event nodes inside it."""
+    import torch
+    from rfba_gb300 import srrf
+    cfg = srrf.Config.make(mag=2, method=1, **SHIPPED)
+    x = _volume(4, (24, 24, 16))
+    xd = torch.from_numpy(x.view(np.int16)).cuda()
+    ctx.set_timing(True)
+    try:
+        for _ in range(3):
+            ctx.forward(cfg, xd)
+            t = ctx.timing()
+            assert ctx.schedule()["graph"]
+            assert t.radiality_ms > 0 and t.temporal_ms > 0
+    finally:
+        ctx.set_timing(False)
