@@ -337,6 +337,79 @@ def measure_diff(ctx, steps: int, iters: int = 20, volumes=None) -> dict:
             "drift_rms_error_after": rms(sh)}
 
 
+def measure_large(ctx, iters: int = 20, volumes=None) -> dict:
+    """Large batched forward + drift refinement: 200 volumes of 256x256x128
+    uint16 (8000 filament emitters, random-walk drift 0.1 voxel per volume),
+    magnification 4x4x2 (1024x1024x256 map), TRAC-4 (ITC 0), intensity
+    weighting; L = -||map||_2; Adam on the 200 x 3 shifts from a common
+    half-voxel start. The radiality stacks of the whole series (430 GB) do not
+    fit in HBM: forward and backward run in z slices of the map under the
+    context's scratch budget, every slice with all volumes (the input, 3.4 GB,
+    stays resident)."""
+    import torch
+    from rfba_gb300 import srrf, synth
+    w = dict(synth.WORKLOADS["large"])
+    T = volumes or w["n_vol"]
+    seed = 1234 + w["index"]
+    scene = synth.make_scene(seed, T, w["shape"], w["n_emitters"], w["curves"], w["drift"])
+    t0 = time.perf_counter()
+    x = synth.render_parallel(scene, w["shape"], seed, np.uint16)
+    render_s = time.perf_counter() - t0
+    cfg = srrf.Config.make(mag=(4, 4, 2), method=3, itc=0, trac_order=4, gradient_smooth=1, main_range=1,
+                           x_range=1, y_range=1, z_range=1)
+    xd = (torch.from_numpy(x.view(np.int16)).cuda().to(torch.int32) & 0xFFFF).to(torch.float32)
+    del x
+    units = xd.shape[1] * xd.shape[2] * xd.shape[3] * 32 * T
+    stream = torch.cuda.current_stream()
+
+    def objective(m):
+        f = torch.nan_to_num(m, nan=0.0).double()
+        return -torch.sqrt((f * f).sum())
+
+    def grad_map(m):
+        f = torch.nan_to_num(m, nan=0.0)
+        return torch.where(torch.isnan(m), torch.zeros_like(m), -f / torch.sqrt((f.double() ** 2).sum()).float())
+
+    truth = -torch.from_numpy(scene.drift.astype(np.float32)).cuda()
+
+    def rms(d):
+        e = d - truth
+        e = e - e.mean(0, keepdim=True)
+        return float(torch.sqrt((e * e).mean()))
+
+    sh = torch.full((T, 3), 0.5, dtype=torch.float32, device="cuda")
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    e0.record(stream)
+    m = ctx.forward_shifted(cfg, xd, sh, stream=stream.cuda_stream)
+    e1.record(stream)
+    _, gs = ctx.backward(cfg, xd, sh, grad_map(m), stream=stream.cuda_stream)
+    e2.record(stream)
+    torch.cuda.synchronize()
+    fwd_ms, bwd_ms = e0.elapsed_time(e1), e1.elapsed_time(e2)
+    rms0 = rms(sh)
+    L0 = float(objective(m))
+    lr, b1, b2 = 0.03, 0.9, 0.999
+    mom = torch.zeros_like(sh)
+    var = torch.zeros_like(sh)
+    t0 = time.perf_counter()
+    for it in range(iters):
+        m = ctx.forward_shifted(cfg, xd, sh, out=m, stream=stream.cuda_stream)
+        _, gs = ctx.backward(cfg, xd, sh, grad_map(m), stream=stream.cuda_stream)
+        mom = b1 * mom + (1 - b1) * gs
+        var = b2 * var + (1 - b2) * gs * gs
+        sh = sh - lr * (mom / (1 - b1 ** (it + 1))) / (torch.sqrt(var / (1 - b2 ** (it + 1))) + 1e-12)
+    m = ctx.forward_shifted(cfg, xd, sh, out=m, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    wall_s = time.perf_counter() - t0
+    return {"workload": f"large: {T} x 256x256x128 u16, 8000 filament emitters, drift 0.1/volume, mag 4x4x2, "
+                        "TRAC-4 ITC0, L = -||map||, Adam on shifts from +0.5",
+            "voxel_volumes": units, "render_s": render_s, "forward_ms": fwd_ms, "backward_ms": bwd_ms,
+            "forward_value": units / (fwd_ms / 1e3), "fwd_adj_over_fwd": (fwd_ms + bwd_ms) / fwd_ms,
+            "refine_iterations": iters, "refine_wall_s": wall_s, "refine_s_per_iteration": wall_s / max(iters, 1),
+            "objective_before": L0, "objective_after": float(objective(m)),
+            "drift_rms_error_before": rms0, "drift_rms_error_after": rms(sh)}
+
+
 def run_single_workload(args):
     """One of the secondary measurements alone, printed as its own JSON line."""
     import torch
@@ -347,6 +420,8 @@ def run_single_workload(args):
     ctx = srrf.Context(0)
     if args.workload == "batching":
         r = measure_batching(ctx, max(2, args.steps))
+    elif args.workload == "large":
+        r = measure_large(ctx, iters=args.iters, volumes=args.volumes)
     else:
         r = measure_diff(ctx, max(3, args.steps), iters=args.iters, volumes=args.volumes)
     ctx.close()
@@ -497,7 +572,7 @@ def main():
     ap.add_argument("--volumes", type=int, default=None,
                     help="fewer volumes than the workload's (profiling case only)")
     ap.add_argument("--iters", type=int, default=20, help="drift refinement iterations (diff workload)")
-    ap.add_argument("--workload", default="mid", choices=["mid", "batching", "diff"],
+    ap.add_argument("--workload", default="mid", choices=["mid", "batching", "diff", "large"],
                     help="mid: the headline line; batching / diff: that measurement alone (one JSON line)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":

@@ -1021,38 +1021,16 @@ static int forward_shifted_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, co
     return read_checks(ctx, st, "forward_shifted");
 }
 
-static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* in, const float* shifts,
-                           const int dims[4], const float* gmap, float* din, float* dshift, cudaStream_t st) {
-    int s = validate_common(cfg, in, dims, gmap);
-    if (s) return s;
-    if (!din) {
-        set_error("null argument");
-        return RFBA_ERR_INVALID;
-    }
-    if (!(cfg->method == 1 || (cfg->method == 3 && cfg->itc != 1))) {
-        set_error("the adjoint covers TRA (Method 1) and TRAC with Integrate_Temporal_Correlations 0");
-        return RFBA_ERR_UNSUPPORTED;
-    }
-    RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
-    if ((s = order_streams(ctx, st))) return s;
-    const bool reuse = ctx->train.valid && same_cfg(ctx->train.cfg, *cfg) && ctx->train.in == in &&
-                       ctx->train.shifts == shifts && ctx->train.dims[0] == dims[0] && ctx->train.dims[1] == dims[1] &&
-                       ctx->train.dims[2] == dims[2] && ctx->train.dims[3] == dims[3];
-    if (ctx->timing) RFBA_CUDA(cudaEventRecord(ctx->ev[0], st), "event");
-    if (!reuse) {
-        const size_t nmap = (size_t)dims[0] * cfg->mag[0] * dims[1] * cfg->mag[1] * dims[2] * cfg->mag[2];
-        if ((s = ctx->out.ensure(nmap * 4, "map"))) return s;
-        if ((s = forward_shifted_locked(ctx, cfg, in, shifts, dims, static_cast<float*>(ctx->out.p), st))) return s;
-        if (!ctx->train.valid) {
-            set_error("the adjoint needs the whole radiality stack resident in one pass; raise the scratch budget");
-            return RFBA_ERR_UNSUPPORTED;
-        }
-    }
-    if ((s = ensure_plan(ctx, *cfg, st))) return s;
+// Adjoint of one block slice whose radiality and intensity stacks sit at
+// offset 0 of the context's stacks: temporal adjoint, then the radiality
+// adjoint adding into dL/dI' (ctx->gin, cleared by the caller).
+static int adjoint_slab(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* iprime, const int dims[4],
+                        BlockDev blk, const float* gmap, cudaStream_t st) {
+    int s;
     const int T = dims[3];
     const size_t nin = (size_t)dims[0] * dims[1] * dims[2] * T;
-    BlockDev blk = ctx->train.blk;
     const long long V = blk.vox;
+    blk.stack_off = 0;
     const int FZ = cfg->mag[2] * cza_for_mag(cfg->mag[2]);
     blk.ntile[1] = (blk.hi[1] - blk.lo[1] + kAdjRows - 1) / kAdjRows;
     blk.ntile[2] = (blk.hi[2] - blk.zbase + FZ - 1) / FZ;
@@ -1061,19 +1039,17 @@ static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const flo
         for (int ty = 0; ty < blk.ntile[1]; ++ty)
             for (int tx = 0; tx < blk.ntile[0]; ++tx) tiles.push_back({0, tx, ty, tz});
     if ((s = ctx->gS.ensure((size_t)V * T * 4, "adjoint stack")) || (s = ctx->gI.ensure((size_t)V * T * 4, "adjoint stack")) ||
-        (s = ctx->gin.ensure(nin * 4, "input adjoint")) || (s = ctx->ablocks.ensure(sizeof(BlockDev), "blocks")) ||
-        (s = ctx->atiles.ensure(tiles.size() * sizeof(TileDesc), "tiles")) || (s = ctx->acounter.ensure(256, "counter")))
+        (s = ctx->ablocks.ensure(sizeof(BlockDev), "blocks")) ||
+        (s = ctx->atiles.ensure(tiles.size() * sizeof(TileDesc), "tiles")) || (s = ctx->acounter.ensure(256, "counter")) ||
+        (s = ctx->errw.ensure(256, "check word")))
         return s;
     RFBA_CUDA(cudaMemcpyAsync(ctx->ablocks.p, &blk, sizeof blk, cudaMemcpyHostToDevice, st), "blocks upload");
     RFBA_CUDA(cudaMemcpyAsync(ctx->atiles.p, tiles.data(), tiles.size() * sizeof(TileDesc), cudaMemcpyHostToDevice, st),
               "tiles upload");
     RFBA_CUDA(cudaMemsetAsync(ctx->acounter.p, 0, 256, st), "counter reset");
-    RFBA_CUDA(cudaMemsetAsync(ctx->gin.p, 0, nin * 4, st), "adjoint clear");
     const BlockDev* dblk = static_cast<const BlockDev*>(ctx->ablocks.p);
     float* gS = static_cast<float*>(ctx->gS.p);
     float* gI = static_cast<float*>(ctx->gI.p);
-    float* gin = static_cast<float*>(ctx->gin.p);
-    if ((s = ctx->errw.ensure(256, "check word"))) return s;
     unsigned long long* err = static_cast<unsigned long long*>(ctx->errw.p);
     const long long nmap = (long long)dims[0] * cfg->mag[0] * dims[1] * cfg->mag[1] * dims[2] * cfg->mag[2];
     int e = launch_temporal_adjoint(dblk, V, static_cast<const float*>(ctx->rad.p),
@@ -1081,7 +1057,7 @@ static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const flo
                                     cfg->intensity_w, cfg->renormalize == 1, cfg->remove_con == 1, gS, gI, nmap, err,
                                     st);
     if (e) return cuda_fail((cudaError_t)e, "temporal adjoint launch");
-    RadParams rp = fill_rad_params(ctx, *cfg, ctx->train.iprime, dims, cza_for_mag(cfg->mag[2]));
+    RadParams rp = fill_rad_params(ctx, *cfg, iprime, dims, cza_for_mag(cfg->mag[2]));
     rp.TY = kAdjRows;
     rp.NV = (kAdjRows - 1) / cfg->mag[1] + 2 + 4;
     rp.NIY = rp.NV + 2 * rp.R;
@@ -1108,11 +1084,72 @@ static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const flo
     rp.nchunks = (T + rp.t_chunk - 1) / rp.t_chunk;
     rp.nitems = (long long)rp.ntiles * rp.nchunks;
     const int grid = (int)std::max<long long>(1, std::min<long long>(slots, rp.nitems));
-    AdjParams ap{gS, gI, gin, (long long)nin, (long long)V * T, err};
+    AdjParams ap{gS, gI, static_cast<float*>(ctx->gin.p), (long long)nin, (long long)V * T, err};
     e = launch_radiality_adjoint(rp, ap, grid, smem, st);
     if (e) return cuda_fail((cudaError_t)e, "radiality adjoint launch");
     ctx->launches += 2;
+    return RFBA_OK;
+}
+
+static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* in, const float* shifts,
+                           const int dims[4], const float* gmap, float* din, float* dshift, cudaStream_t st) {
+    int s = validate_common(cfg, in, dims, gmap);
+    if (s) return s;
+    if (!din) {
+        set_error("null argument");
+        return RFBA_ERR_INVALID;
+    }
+    if (!(cfg->method == 1 || (cfg->method == 3 && cfg->itc != 1))) {
+        set_error("the adjoint covers TRA (Method 1) and TRAC with Integrate_Temporal_Correlations 0");
+        return RFBA_ERR_UNSUPPORTED;
+    }
+    RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if ((s = order_streams(ctx, st))) return s;
+    const bool reuse = ctx->train.valid && same_cfg(ctx->train.cfg, *cfg) && ctx->train.in == in &&
+                       ctx->train.shifts == shifts && ctx->train.dims[0] == dims[0] && ctx->train.dims[1] == dims[1] &&
+                       ctx->train.dims[2] == dims[2] && ctx->train.dims[3] == dims[3];
+    if (ctx->timing) RFBA_CUDA(cudaEventRecord(ctx->ev[0], st), "event");
+    const int T = dims[3];
+    const size_t nin = (size_t)dims[0] * dims[1] * dims[2] * T;
+    const size_t nmap = (size_t)dims[0] * cfg->mag[0] * dims[1] * cfg->mag[1] * dims[2] * cfg->mag[2];
+    if ((s = ensure_plan(ctx, *cfg, st))) return s;
+    if ((s = ctx->gin.ensure(nin * 4, "input adjoint"))) return s;
+    if ((s = ctx->errw.ensure(256, "check word"))) return s;
+    if (reuse) {
+        RFBA_CUDA(cudaMemsetAsync(ctx->gin.p, 0, nin * 4, st), "adjoint clear");
+        if ((s = adjoint_slab(ctx, cfg, ctx->train.iprime, dims, ctx->train.blk, gmap, st))) return s;
+    } else {
+        // The whole volume's slices under the stack budget: each slice's stacks are
+        // recomputed by the forward kernels, then its adjoint runs (one slice when
+        // everything fits).
+        if ((s = ctx->out.ensure(nmap * 4, "map"))) return s;
+        RFBA_CUDA(cudaMemsetAsync(ctx->errw.p, 0, 8, st), "check word clear");
+        const float* ip = nullptr;
+        if ((s = apply_drift(ctx, in, shifts, dims, st, &ip))) return s;
+        rfba_block b;
+        std::memset(&b, 0, sizeof b);
+        for (int a = 0; a < 3; ++a) {
+            b.size[a] = dims[a];
+            b.hi[a] = dims[a] * cfg->mag[a];
+        }
+        b.out_stride[0] = 1;
+        b.out_stride[1] = b.hi[0];
+        b.out_stride[2] = (int64_t)b.hi[0] * b.hi[1];
+        std::vector<BlockDev> all;
+        if ((s = make_blocks(ctx, *cfg, dims, &b, 1, &all))) return s;
+        RFBA_CUDA(cudaMemsetAsync(ctx->gin.p, 0, nin * 4, st), "adjoint clear");
+        for (const BlockDev& slab : all) {
+            std::vector<BlockDev> one(1, slab);
+            if ((s = run_device(ctx, *cfg, ip, RFBA_F32, dims, one, static_cast<float*>(ctx->out.p), st))) return s;
+            BlockDev blk = slab;
+            blk.stack_off = 0;
+            if ((s = adjoint_slab(ctx, cfg, ip, dims, blk, gmap, st))) return s;
+        }
+    }
     // through the drift operator
+    float* gin = static_cast<float*>(ctx->gin.p);
+    unsigned long long* err = static_cast<unsigned long long*>(ctx->errw.p);
+    int e = 0;
     if (shifts) {
         float* t1 = static_cast<float*>(ctx->tmp1.p);
         float* t2 = static_cast<float*>(ctx->tmp2.p);

@@ -22,6 +22,8 @@ from __future__ import annotations
 import math
 from dataclasses import dataclass
 
+import os
+
 import numpy as np
 
 SIGMA_XY = 1.2
@@ -190,6 +192,38 @@ WORKLOADS = {
     "large": dict(index=4, n_vol=200, shape=(256, 256, 128), n_emitters=8000, curves=200, drift=0.1,
                   dtype=np.uint16),
 }
+
+
+def render_volume(scene: Scene, shape_xyz, seed: int, t: int, dtype=np.uint16) -> np.ndarray:
+    """Volume t of a series with its own noise stream (seed, t), so volumes can
+    be rendered in parallel."""
+    W, H, D = shape_xyz
+    rng = np.random.default_rng([seed + 7919, t])
+    lam = render_expected(scene.positions, scene.states[t], (D, H, W))
+    if np.any(scene.drift[t] != 0):
+        lam = np.maximum(shift_volume(lam, scene.drift[t]), 0.0)
+    noisy = rng.poisson(lam).astype(np.float64) + rng.normal(0.0, READ_SIGMA, size=lam.shape)
+    if dtype == np.uint16:
+        return np.clip(np.rint(noisy), 0, 65535).astype(np.uint16)
+    return noisy.astype(np.float32)
+
+
+def _render_one(args):
+    return render_volume(*args)
+
+
+def render_parallel(scene: Scene, shape_xyz, seed: int, dtype=np.uint16, workers: int | None = None) -> np.ndarray:
+    """render_volume for every volume on a spawn-started process pool."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+    W, H, D = shape_xyz
+    T = scene.states.shape[0]
+    out = np.empty((T, D, H, W), dtype)
+    workers = workers or max(1, min(16, (os.cpu_count() or 1)))
+    with ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+        for t, vol in enumerate(ex.map(_render_one, [(scene, shape_xyz, seed, t, dtype) for t in range(T)])):
+            out[t] = vol
+    return out
 
 
 def workload(name: str, n_vol: int | None = None, shape=None):

@@ -116,3 +116,25 @@ def test_adjoint_against_central_differences(ctx, oracle_mod):
     print(f"[adjoint] central differences: {len(fd)} points, max |fd - adjoint| / max|fd| = {err.max():.2e}")
     assert err.max() < 5e-3
     assert np.median(np.abs(fd - an) / np.maximum(np.abs(fd), 1e-12 * scale)) < 1e-2
+
+
+def test_backward_in_slices_matches_resident(ctx, oracle_mod):
+    """With a scratch budget too small for the whole radiality stack, the
+    forward runs in z slices and the backward recomputes each slice's stacks
+    before its adjoint; the gradients equal the single-slice ones (up to the
+    order of the float atomics that add the tiles' contributions)."""
+    import torch
+    from rfba_gb300 import srrf
+    kw = dict(mag=2, method=3, itc=0, trac_order=2, **SHIPPED)
+    cfg = srrf.Config.make(**kw)
+    x, sh = _case(23, 6, 12, 10, 9, drift=0.2)
+    m, din, dsh = _gpu(ctx, cfg, x, sh)
+    small = srrf.Context(0, 6 * 20 * 18 * 8 * 4 * 2)   # about one 4-row z slab of the 24-deep map
+    try:
+        m2, din2, dsh2 = _gpu(small, cfg, x, sh)
+    finally:
+        small.close()
+    assert np.array_equal(np.isnan(m), np.isnan(m2)) and np.allclose(np.nan_to_num(m), np.nan_to_num(m2), rtol=0,
+                                                                      atol=0)
+    assert rel_linf(din2, din) < 1e-5
+    assert rel_linf(dsh2, dsh) < 1e-5
