@@ -33,8 +33,27 @@ def _cuda_include() -> str:
     return str(Path(_nvcc()).resolve().parent.parent / "include")
 
 
+CLI_SRC = CSRC / "cli_srrf.cpp"
+CLI = OUT_DIR / "rfba-srrf"
+
+
 def sources():
-    return sorted(CSRC.glob("*.cu")), sorted(CSRC.glob("*.cpp"))
+    """Library translation units (the command-line front end is linked separately)."""
+    return sorted(CSRC.glob("*.cu")), sorted(p for p in CSRC.glob("*.cpp") if p != CLI_SRC)
+
+
+def build_cli(force: bool = False) -> Path:
+    """rfba-srrf: the RFBA.bat `--srrf_only 1` step on the library (rpath $ORIGIN)."""
+    if CLI.exists() and not force and CLI.stat().st_mtime >= max(CLI_SRC.stat().st_mtime, LIB.stat().st_mtime):
+        return CLI
+    tmp = CLI.with_suffix(".tmp")
+    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", str(PKG.parent / "include"), str(CLI_SRC),
+           "-o", str(tmp), "-L", str(OUT_DIR), "-lrfba_srrf", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"cli build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, CLI)
+    return CLI
 
 
 def _compile(src: Path, verbose_ptxas: bool) -> Path:
@@ -61,6 +80,7 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
     headers = list(CSRC.glob("*.h")) + list((PKG.parent / "include").glob("*.h"))
     newest = max(p.stat().st_mtime for p in srcs + headers)
     if LIB.exists() and not force and not verbose_ptxas and LIB.stat().st_mtime >= newest:
+        build_cli()
         return LIB
     OBJ_DIR.mkdir(parents=True, exist_ok=True)
     OUT_DIR.mkdir(parents=True, exist_ok=True)
@@ -72,6 +92,7 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_cli(force=True)
     return LIB
 
 
