@@ -215,6 +215,20 @@ int rfba_ctx_last_timing(rfba_ctx* ctx, double* radiality_ms, double* temporal_m
 /* Launch overrides for tuning: CTAs of the radiality kernel and time points per
  * work item (0 = automatic). */
 int rfba_ctx_set_launch(rfba_ctx* ctx, int grid, int t_chunk);
+/* SRRF-guided spot seeding: replaces the rejection loops of
+ * multispot5_place_methods.cc:291-341 (place_spots_intensity_sampled) and
+ * multispot5.cc:2164-2231 (InitGuide / GetPoint). Candidates are the mag^3
+ * subvoxels of each input voxel in `voxels` ([n][3] ints x, y, z, the 3B block
+ * mask's pixels), weighted by the map value ([z][y][x] floats, map_dims = its
+ * x, y, z extents, the SRRF.raw layout; NaN and negative values weigh 0, an
+ * all-zero map weighs every candidate 1). Writes num_spots positions [n][3] in
+ * input-voxel units, (subvoxel + U(-0.5, 0.5)) / mag per axis like the
+ * reference. Drawn on the GPU by inverse CDF with a counter-based generator
+ * keyed by `seed`: the reference's distribution, not its random stream.
+ * Synchronous (returns when xyz is written). */
+int rfba_srrf_seed_spots(rfba_ctx* ctx, const float* map, const int map_dims[3], int mag, const int* voxels,
+                         int nvoxels, int num_spots, unsigned long long seed, float* xyz, int ptr_flags, void* stream);
+
 /* Schedule of the last rfba_srrf_forward / rfba_srrf_forward_blocks call: tile
  * rows (tile shape), tile order (0 largest block first, 1 interleaved across
  * blocks), whether it was replayed as a CUDA graph, and whether this call ran

@@ -299,3 +299,36 @@ def ref_block(img: np.ndarray, conf: OConf) -> np.ndarray:
     rc = to_ref_conf(conf)
     L.SRRFGradientCalcGPU(_p(img, ctypes.c_float), _p(dims, ctypes.c_int), _p(out, ctypes.c_float), ctypes.byref(rc))
     return out
+
+
+def seed_spots_rejection(srrf_map: np.ndarray, voxels: np.ndarray, mag: int, num_spots: int,
+                         rng: np.random.Generator) -> np.ndarray:
+    """The reference's SRRF-guided seeding (multispot5_place_methods.cc:291-341):
+    candidates = the mag^3 subvoxels of each voxel in order (x offset slowest),
+    element = floor(U * n), kept when U * max <= value, position
+    (subvoxel + U - 0.5) / mag per axis in float. numpy's generator stands in
+    for MT19937 (same algorithm, another random stream); draws are taken in
+    batches, each kept in order. The map is used as the caller leaves it
+    (NaN and negative values set to 0 first, multispot5_place_methods.cc:260-269)."""
+    m = np.where(np.isnan(srrf_map) | (srrf_map < 0), 0.0, srrf_map).astype(np.float32)
+    D, H, W = m.shape
+    sub = np.array([(j1, j2, j3) for j1 in range(mag) for j2 in range(mag) for j3 in range(mag)], np.int64)
+    pix = (np.asarray(voxels, np.int64)[:, None, :] * mag + sub[None, :, :]).reshape(-1, 3)
+    inten = m[pix[:, 2], pix[:, 1], pix[:, 0]].astype(np.float64)
+    mx = inten.max()
+    out = []
+    n = len(pix)
+    while len(out) < num_spots:
+        k = max(1024, 2 * (num_spots - len(out)))
+        el = np.floor(rng.random(k) * n).astype(np.int64)
+        y = rng.random(k) * mx
+        keep = el[y <= inten[el]]
+        for e in keep:
+            if len(out) == num_spots:
+                break
+            jx, jy, jz = rng.random(3)
+            x = np.float32(pix[e, 0] + jx - 0.5)
+            yy = np.float32(pix[e, 1] + jy - 0.5)
+            z = np.float32(pix[e, 2] + jz - 0.5)
+            out.append((x / np.float32(mag), yy / np.float32(mag), z / np.float32(mag)))
+    return np.array(out, np.float32)

@@ -192,6 +192,8 @@ struct rfba_ctx {
     cudaStream_t cap = nullptr;  // stream the graphs are captured on
     std::map<std::string, std::pair<int, int>> tunes;  // schedule key -> (tile rows, tile order)
     std::vector<std::unique_ptr<rfba::GraphPlan>> graphs;  // most recent first
+    // spot seeding scratch
+    rfba::DevBuf seed_w, seed_sums, seed_carry, seed_map, seed_vox, seed_xyz;
     int last_ty = 0, last_order = 0, last_graph = 0, last_tuned = 0;
 };
 
@@ -1246,7 +1248,10 @@ int rfba_ctx_destroy(rfba_ctx* c) {
         if (c == g_default) g_default = nullptr;
     }
     cudaSetDevice(c->device);
-    for (DevBuf* b : {&c->in, &c->out, &c->rad, &c->inten, &c->blocks, &c->tiles, &c->tables, &c->counter, &c->prefix})
+    for (DevBuf* b : {&c->in, &c->out, &c->rad, &c->inten, &c->blocks, &c->tiles, &c->tables, &c->counter, &c->prefix,
+                      &c->shifted, &c->tmp1, &c->tmp2, &c->gS, &c->gI, &c->gin, &c->dshift, &c->ablocks, &c->atiles,
+                      &c->acounter, &c->errw, &c->seed_w, &c->seed_sums, &c->seed_carry, &c->seed_map, &c->seed_vox,
+                      &c->seed_xyz})
         b->release();
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
@@ -1273,6 +1278,68 @@ int rfba_ctx_last_timing(rfba_ctx* c, double* rad_ms, double* temporal_ms, long 
     if (launches) *launches = c->launches;
     return RFBA_OK;
 }
+int rfba_srrf_seed_spots(rfba_ctx* ctx, const float* map, const int map_dims[3], int mag, const int* voxels,
+                         int nvoxels, int num_spots, unsigned long long seed, float* xyz, int ptr_flags, void* stream) {
+    if (!ctx || !map || !map_dims || !voxels || !xyz || mag < 1 || nvoxels < 1 || num_spots < 0) {
+        set_error("null argument or bad size");
+        return RFBA_ERR_INVALID;
+    }
+    if (map_dims[0] < 1 || map_dims[1] < 1 || map_dims[2] < 1) {
+        set_error("bad map dims");
+        return RFBA_ERR_INVALID;
+    }
+    const long long ncand = (long long)nvoxels * mag * mag * mag;
+    const long long n1 = (ncand + 511) / 512, n2 = (n1 + 511) / 512;
+    if (n2 > 512) {
+        set_error("too many candidate subvoxels (at most 512^3)");
+        return RFBA_ERR_UNSUPPORTED;
+    }
+    if (num_spots == 0) return RFBA_OK;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL = legacy default stream
+    int s;
+    if ((s = order_streams(ctx, st))) return s;
+    if ((s = ctx->seed_w.ensure((size_t)ncand * 8, "seeding weights")) ||
+        (s = ctx->seed_sums.ensure((size_t)n1 * 8, "seeding scan")) ||
+        (s = ctx->seed_carry.ensure((size_t)(n2 + 1) * 8, "seeding scan")) || (s = ctx->errw.ensure(256, "check word")))
+        return s;
+    const float* dmap = map;
+    const int* dvox = voxels;
+    float* dxyz = xyz;
+    const size_t map_bytes = (size_t)map_dims[0] * map_dims[1] * map_dims[2] * 4;
+    if (ptr_flags == RFBA_HOST_PTRS) {
+        if ((s = ctx->seed_map.ensure(map_bytes, "seeding map")) ||
+            (s = ctx->seed_vox.ensure((size_t)nvoxels * 12, "seeding voxels")) ||
+            (s = ctx->seed_xyz.ensure((size_t)num_spots * 12, "seeding spots")))
+            return s;
+        RFBA_CUDA(cudaMemcpyAsync(ctx->seed_map.p, map, map_bytes, cudaMemcpyHostToDevice, st), "map copy");
+        RFBA_CUDA(cudaMemcpyAsync(ctx->seed_vox.p, voxels, (size_t)nvoxels * 12, cudaMemcpyHostToDevice, st),
+                  "voxel copy");
+        dmap = static_cast<const float*>(ctx->seed_map.p);
+        dvox = static_cast<const int*>(ctx->seed_vox.p);
+        dxyz = static_cast<float*>(ctx->seed_xyz.p);
+    }
+    RFBA_CUDA(cudaMemsetAsync(ctx->errw.p, 0, 8, st), "check word clear");
+    int e = launch_seed_spots(dmap, map_dims, mag, dvox, nvoxels, num_spots, seed, dxyz,
+                              static_cast<double*>(ctx->seed_w.p), static_cast<double*>(ctx->seed_sums.p),
+                              static_cast<double*>(ctx->seed_carry.p),
+                              static_cast<unsigned long long*>(ctx->errw.p), st);
+    if (e) return cuda_fail((cudaError_t)e, "seeding launch");
+    ctx->launches += 3;
+    unsigned long long ew = 0;
+    RFBA_CUDA(cudaMemcpyAsync(&ew, ctx->errw.p, 8, cudaMemcpyDeviceToHost, st), "check word read");
+    if (ptr_flags == RFBA_HOST_PTRS)
+        RFBA_CUDA(cudaMemcpyAsync(xyz, dxyz, (size_t)num_spots * 12, cudaMemcpyDeviceToHost, st), "spots copy");
+    RFBA_CUDA(cudaStreamSynchronize(st), "synchronize");
+    if (ew) {
+        set_error("a candidate voxel lies outside the map (magnified voxel index " +
+                  std::to_string((long long)(ew & 0x00ffffffffffffffull)) + ")");
+        return RFBA_ERR_INVALID;
+    }
+    return RFBA_OK;
+}
+
 int rfba_ctx_last_schedule(rfba_ctx* c, int* tile_rows, int* tile_order, int* graph, int* tuned) {
     if (!c) return RFBA_ERR_INVALID;
     if (tile_rows) *tile_rows = c->last_ty;

@@ -160,6 +160,9 @@ size_t radiality_smem_bytes(const RadParams& p);
 int tile_rows_for_mag(int my);
 int radiality_max_ctas_per_sm(const RadParams& p, int in_u16, int* out);
 int launch_temporal(const TemporalParams& p, void* stream);
+int launch_seed_spots(const float* map, const int map_dims[3], int mag, const int* vox, long long nvox, int nspots,
+                      unsigned long long seed, float* xyz, double* w, double* sums, double* carry,
+                      unsigned long long* err, void* stream);
 
 // Host planning (plan.cpp).
 bool build_ring_plan(const rfba_srrf_config& c, RingPlan* rp, std::string* err);

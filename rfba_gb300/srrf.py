@@ -120,6 +120,8 @@ def lib():
                                            ctypes.POINTER(ctypes.c_longlong)]
         L.rfba_ctx_set_launch.argtypes = [vp, ctypes.c_int, ctypes.c_int]
         L.rfba_ctx_last_schedule.argtypes = [vp, ip, ip, ip, ip]
+        L.rfba_srrf_seed_spots.argtypes = [vp, vp, ip, ctypes.c_int, vp, ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong,
+                                           vp, ctypes.c_int, vp]
         L.rfba_srrf_config_default.argtypes = [cp]
         L.rfba_srrf_config_load_ini.argtypes = [ctypes.c_char_p, cp]
         L.rfba_srrf_config_from_legacy.argtypes = [ctypes.POINTER(SRRFConf), cp]
@@ -269,6 +271,32 @@ class Context:
 
     def set_launch(self, grid: int = 0, t_chunk: int = 0):
         _check(lib().rfba_ctx_set_launch(self.h, grid, t_chunk))
+
+    def seed_spots(self, srrf_map, voxels, mag: int, num_spots: int, seed: int = 0, stream=None):
+        """SRRF-guided spot seeding (multispot5_place_methods.cc:291-341): num_spots
+        positions [n][3] (x, y, z, input voxels) drawn with density proportional to
+        the map over the mag^3 subvoxels of each input voxel in ``voxels`` ([n][3]
+        x, y, z). ``srrf_map`` is [z][y][x] float32, numpy (host) or a CUDA tensor."""
+        dev = not isinstance(srrf_map, np.ndarray)
+        vox = np.ascontiguousarray(voxels, np.int32).reshape(-1, 3)
+        if dev:
+            import torch
+            m = srrf_map.contiguous()
+            vd = torch.from_numpy(vox).to(m.device)
+            out = torch.empty((num_spots, 3), dtype=torch.float32, device=m.device)
+            mp, vp_, op = ctypes.c_void_p(m.data_ptr()), ctypes.c_void_p(vd.data_ptr()), ctypes.c_void_p(out.data_ptr())
+            shape = m.shape
+        else:
+            m = np.ascontiguousarray(srrf_map, np.float32)
+            out = np.empty((num_spots, 3), np.float32)
+            mp, vp_, op = (ctypes.c_void_p(m.ctypes.data), ctypes.c_void_p(vox.ctypes.data),
+                           ctypes.c_void_p(out.ctypes.data))
+            shape = m.shape
+        dims = np.array([shape[2], shape[1], shape[0]], np.int32)
+        st = _stream_arg(stream, dev)
+        _check(lib().rfba_srrf_seed_spots(self.h, mp, _iptr(dims), mag, vp_, len(vox), num_spots, seed, op,
+                                          RFBA_DEVICE_PTRS if dev else RFBA_HOST_PTRS, st))
+        return out
 
     def schedule(self) -> dict:
         """Schedule of the last forward: tile rows, tile order, graph replay, autotuned now."""
