@@ -51,6 +51,7 @@ CASES = [
     ("trac3_mag3_nodrift_poscon", dict(mag=3, method=3, itc=0, trac_order=3, remove_con=1, **SHIPPED), (7, 7, 8, 8),
      False),
     ("trac2_aniso_nosmooth", dict(mag=(2, 2, 1), method=3, itc=0, trac_order=2), (8, 9, 9, 10), True),
+    ("trac2_mag442_deep_tiles", dict(mag=(4, 4, 2), method=3, itc=0, trac_order=2, **SHIPPED), (5, 9, 7, 8), True),
 ]
 
 
