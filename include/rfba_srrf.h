@@ -229,6 +229,29 @@ int rfba_ctx_set_launch(rfba_ctx* ctx, int grid, int t_chunk);
 int rfba_srrf_seed_spots(rfba_ctx* ctx, const float* map, const int map_dims[3], int mag, const int* voxels,
                          int nvoxels, int num_spots, unsigned long long seed, float* xyz, int ptr_flags, void* stream);
 
+/* CombineBlock (Matlab Scripts/CombineBlock.m, genpsf.m, loadResult.m): the
+ * reconstruction from 3B's localisations. No counterpart in the reference's
+ * compiled code (the reference does this in MATLAB).
+ *
+ * rfba_combine_psf: genpsf(sigma, crop_threshold) — uint16 PSF, [z][y][x],
+ * psf_dims = x, y, z extents; returns the element count (PSF copied when cap
+ * suffices, pass NULL/0 to query).
+ * rfba_combine_load_result: loadResult.m on one res_i_j_k.txt — the spots
+ * (intensity, blur, x, y, z as doubles) of every "PASS" line that lie strictly
+ * inside the block minus its border (block_start 1-based, as doSplit.m).
+ * rfba_combine_render: CombineBlock.m:24-173 on the spots of all blocks:
+ * histogram on the zoom-times grid (round half away from zero), noise mask
+ * (box sums of occupied voxels over (2r+1)^2 x (2rz+1) above noise_threshold in
+ * the interior, kept at the borders), convn(..., psf, 'same') in 64-bit
+ * integers, scaled to uint16 by the maximum. out: [Z*zoom][Y*zoom][X*zoom]
+ * uint16 (host); dropped = spots that fell outside the grid. Synchronous. */
+int rfba_combine_psf(double sigma, double crop_threshold, uint16_t* psf, long long cap, int psf_dims[3]);
+int rfba_combine_load_result(const char* path, int border, const int block_start[3], const int block_size[3],
+                             double* spots, long long cap, long long* nspots);
+int rfba_combine_render(rfba_ctx* ctx, const double* spots, long long nspots, const int img_dims[3], int zoom,
+                        const uint16_t* psf, const int psf_dims[3], int noise_r, int noise_rz, int noise_threshold,
+                        uint16_t* out, long long* dropped);
+
 /* Schedule of the last rfba_srrf_forward / rfba_srrf_forward_blocks call: tile
  * rows (tile shape), tile order (0 largest block first, 1 interleaved across
  * blocks), whether it was replayed as a CUDA graph, and whether this call ran

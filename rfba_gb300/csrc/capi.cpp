@@ -546,7 +546,7 @@ static int enqueue_passes(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void
     return RFBA_OK;
 }
 
-static int ensure_events(rfba_ctx* ctx, std::vector<cudaEvent_t>* evs, size_t n) {
+static int ensure_events(std::vector<cudaEvent_t>* evs, size_t n) {
     while (evs->size() < n) {
         cudaEvent_t e;
         RFBA_CUDA(cudaEventCreate(&e), "event");
@@ -599,7 +599,7 @@ static int run_device(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void* in
                               cudaMemcpyHostToDevice, st), "tiles upload");
     RFBA_CUDA(cudaMemcpyAsync(ctx->prefix.p, ps.prefix.data(), ps.prefix.size() * sizeof(long long),
                               cudaMemcpyHostToDevice, st), "prefix upload");
-    if (ctx->timing && (s = ensure_events(ctx, &ctx->pev, 3 * np))) return s;
+    if (ctx->timing && (s = ensure_events(&ctx->pev, 3 * np))) return s;
     if ((s = enqueue_passes(ctx, cfg, in_dev, dtype, dims, ps, static_cast<const BlockDev*>(ctx->blocks.p),
                             static_cast<const TileDesc*>(ctx->tiles.p), static_cast<const long long*>(ctx->prefix.p),
                             static_cast<unsigned int*>(ctx->counter.p), out_dev, st,
@@ -845,7 +845,7 @@ static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, con
                 if ((s = g->blocks.ensure(ps.blocks.size() * sizeof(BlockDev), "blocks")) ||
                     (s = g->tiles.ensure(ps.tiles.size() * sizeof(TileDesc), "tiles")) ||
                     (s = g->prefix.ensure(ps.prefix.size() * sizeof(long long), "prefix")) ||
-                    (s = g->counters.ensure(np * 256, "counters")) || (s = ensure_events(ctx, &g->evs, 3 * np)))
+                    (s = g->counters.ensure(np * 256, "counters")) || (s = ensure_events(&g->evs, 3 * np)))
                     return s;
                 RFBA_CUDA(cudaMemcpy(g->blocks.p, ps.blocks.data(), ps.blocks.size() * sizeof(BlockDev),
                                      cudaMemcpyHostToDevice), "blocks upload");
@@ -1337,6 +1337,66 @@ int rfba_srrf_seed_spots(rfba_ctx* ctx, const float* map, const int map_dims[3],
                   std::to_string((long long)(ew & 0x00ffffffffffffffull)) + ")");
         return RFBA_ERR_INVALID;
     }
+    return RFBA_OK;
+}
+
+int rfba_combine_render(rfba_ctx* ctx, const double* spots, long long nspots, const int img_dims[3], int zoom,
+                        const uint16_t* psf, const int psf_dims[3], int noise_r, int noise_rz, int noise_threshold,
+                        uint16_t* out, long long* dropped) {
+    if (!ctx || (nspots > 0 && !spots) || !img_dims || !psf || !psf_dims || !out || zoom < 1 || noise_r < 0 ||
+        noise_rz < 0 || nspots < 0) {
+        set_error("null argument or bad size");
+        return RFBA_ERR_INVALID;
+    }
+    const long long Xp = (long long)img_dims[0] * zoom, Yp = (long long)img_dims[1] * zoom,
+                    Zp = (long long)img_dims[2] * zoom;
+    const long long nk = (long long)psf_dims[0] * psf_dims[1] * psf_dims[2];
+    if (Xp < 1 || Yp < 1 || Zp < 1 || Xp > (1 << 30) || Yp > (1 << 30) || nk < 1 || nk * 2 > 200 * 1024 ||
+        2 * noise_r + 1 > 255) {
+        set_error("bad image, PSF or noise-window size");
+        return RFBA_ERR_INVALID;
+    }
+    const long long nvox = Xp * Yp * Zp;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = ctx->stream;
+    int s;
+    if ((s = order_streams(ctx, st))) return s;
+    DevBuf hist, L, S, o64, o16, idx, val, sp, ps, cnt;
+    auto release = [&]() {
+        for (DevBuf* b : {&hist, &L, &S, &o64, &o16, &idx, &val, &sp, &ps, &cnt}) b->release();
+    };
+    const unsigned long long cap = (unsigned long long)std::max<long long>(nspots, 1);
+    if ((s = hist.ensure((size_t)nvox * 4, "histogram")) || (s = L.ensure((size_t)nvox, "box sums")) ||
+        (s = S.ensure((size_t)nvox * 2, "box sums")) || (s = o64.ensure((size_t)nvox * 8, "convolution")) ||
+        (s = o16.ensure((size_t)nvox * 2, "output")) || (s = idx.ensure(cap * 8, "nonzeros")) ||
+        (s = val.ensure(cap * 4, "nonzeros")) || (s = sp.ensure((size_t)cap * 40, "spots")) ||
+        (s = ps.ensure((size_t)nk * 2, "psf")) || (s = cnt.ensure(64, "counters"))) {
+        release();
+        return s;
+    }
+    cudaError_t ce = cudaSuccess;
+    if (nspots > 0) ce = cudaMemcpyAsync(sp.p, spots, (size_t)nspots * 40, cudaMemcpyHostToDevice, st);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(ps.p, psf, (size_t)nk * 2, cudaMemcpyHostToDevice, st);
+    int e = ce == cudaSuccess ? launch_combine(static_cast<const double*>(sp.p), nspots, zoom, (int)Xp, (int)Yp,
+                                               (int)Zp, noise_r, noise_rz, noise_threshold,
+                                               static_cast<const uint16_t*>(ps.p), psf_dims[0], psf_dims[1],
+                                               psf_dims[2], static_cast<unsigned int*>(hist.p),
+                                               static_cast<unsigned char*>(L.p), static_cast<unsigned short*>(S.p),
+                                               static_cast<unsigned long long*>(idx.p),
+                                               static_cast<unsigned int*>(val.p), cap,
+                                               static_cast<unsigned long long*>(cnt.p),
+                                               static_cast<unsigned long long*>(o64.p),
+                                               static_cast<uint16_t*>(o16.p), st)
+                              : (int)ce;
+    unsigned long long counters[3] = {0, 0, 0};
+    if (!e) e = (int)cudaMemcpyAsync(out, o16.p, (size_t)nvox * 2, cudaMemcpyDeviceToHost, st);
+    if (!e) e = (int)cudaMemcpyAsync(counters, cnt.p, sizeof counters, cudaMemcpyDeviceToHost, st);
+    if (!e) e = (int)cudaStreamSynchronize(st);
+    release();
+    if (e) return cuda_fail((cudaError_t)e, "combine");
+    ctx->launches += 7;
+    if (dropped) *dropped = (long long)counters[0];
     return RFBA_OK;
 }
 

@@ -98,22 +98,20 @@ bool load_tiff(const char* path, Volume* vol, std::string* err) {
             *err = "bad directory";
             return false;
         }
-        uint32_t w = 0, h = 0, bits = 1, comp = 1, spp = 1, rps = 0;
+        uint32_t w = 0, h = 0, bits = 1, comp = 1, spp = 1;
         size_t e_off = 0, e_cnt = 0;
         for (uint32_t k = 0; k < ne; ++k) {
             const size_t e = ifd + 2 + (size_t)k * 12;
             const uint32_t tag = r.u16(e);
-            uint32_t v = 0;
             switch (tag) {
                 case 256: r.value(e, 0, &w); break;
                 case 257: r.value(e, 0, &h); break;
                 case 258: r.value(e, 0, &bits); break;
                 case 259: r.value(e, 0, &comp); break;
                 case 277: r.value(e, 0, &spp); break;
-                case 278: r.value(e, 0, &rps); break;
                 case 273: e_off = e; break;
                 case 279: e_cnt = e; break;
-                default: (void)v; break;
+                default: break;
             }
         }
         if (comp != 1 || spp != 1 || (bits != 8 && bits != 16) || !w || !h || !e_off || !e_cnt) {

@@ -160,6 +160,10 @@ size_t radiality_smem_bytes(const RadParams& p);
 int tile_rows_for_mag(int my);
 int radiality_max_ctas_per_sm(const RadParams& p, int in_u16, int* out);
 int launch_temporal(const TemporalParams& p, void* stream);
+int launch_combine(const double* spots, long long n, int zoom, int Xp, int Yp, int Zp, int r, int rz, int thr,
+                   const uint16_t* psf, int Kx, int Ky, int Kz, unsigned int* hist, unsigned char* L,
+                   unsigned short* S, unsigned long long* idx, unsigned int* val, unsigned long long cap,
+                   unsigned long long* counters, unsigned long long* out, uint16_t* out16, void* stream);
 int launch_seed_spots(const float* map, const int map_dims[3], int mag, const int* vox, long long nvox, int nspots,
                       unsigned long long seed, float* xyz, double* w, double* sums, double* carry,
                       unsigned long long* err, void* stream);

@@ -120,6 +120,11 @@ def lib():
                                            ctypes.POINTER(ctypes.c_longlong)]
         L.rfba_ctx_set_launch.argtypes = [vp, ctypes.c_int, ctypes.c_int]
         L.rfba_ctx_last_schedule.argtypes = [vp, ip, ip, ip, ip]
+        L.rfba_combine_psf.argtypes = [ctypes.c_double, ctypes.c_double, vp, ctypes.c_longlong, ip]
+        L.rfba_combine_load_result.argtypes = [ctypes.c_char_p, ctypes.c_int, ip, ip, vp, ctypes.c_longlong,
+                                               ctypes.POINTER(ctypes.c_longlong)]
+        L.rfba_combine_render.argtypes = [vp, vp, ctypes.c_longlong, ip, ctypes.c_int, vp, ip, ctypes.c_int,
+                                          ctypes.c_int, ctypes.c_int, vp, ctypes.POINTER(ctypes.c_longlong)]
         L.rfba_srrf_seed_spots.argtypes = [vp, vp, ip, ctypes.c_int, vp, ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong,
                                            vp, ctypes.c_int, vp]
         L.rfba_srrf_config_default.argtypes = [cp]
@@ -238,6 +243,39 @@ def blocks_dosplit(cfg: Config, shape: Sequence[int], max_size, border: int):
     return arr, n, int(oe.value)
 
 
+def combine_psf(sigma: float = 3.5, crop_threshold: float = 1000.0) -> np.ndarray:
+    """genpsf.m: the uint16 PSF of the CombineBlock reconstruction, [z][y][x]."""
+    dims = np.zeros(3, np.int32)
+    n = _check(lib().rfba_combine_psf(sigma, crop_threshold, None, 0, _iptr(dims)))
+    out = np.empty(n, np.uint16)
+    _check(lib().rfba_combine_psf(sigma, crop_threshold, ctypes.c_void_p(out.ctypes.data), n, _iptr(dims)))
+    return out.reshape(int(dims[2]), int(dims[1]), int(dims[0]))
+
+
+def combine_load_result(path, border: int, block_start, block_size) -> np.ndarray:
+    """loadResult.m on one res_i_j_k.txt: spots (intensity, blur, x, y, z) inside the block."""
+    st = np.array(block_start, np.int32)
+    sz = np.array(block_size, np.int32)
+    n = ctypes.c_longlong()
+    _check(lib().rfba_combine_load_result(str(path).encode(), border, _iptr(st), _iptr(sz), None, 0,
+                                          ctypes.byref(n)))
+    out = np.empty((n.value, 5), np.float64)
+    _check(lib().rfba_combine_load_result(str(path).encode(), border, _iptr(st), _iptr(sz),
+                                          ctypes.c_void_p(out.ctypes.data), n.value, ctypes.byref(n)))
+    return out
+
+
+def dosplit(xall: int, max_size: int, border: int):
+    """doSplit.m: (start (1-based), size) of the blocks along one axis."""
+    if max_size >= xall:
+        return [(1, xall)]
+    pos = [[1, max_size]]
+    while pos[-1][0] + max_size <= xall:
+        pos.append([pos[-1][0] + pos[-1][1] - 2 * border, max_size])
+    pos[-1][1] = xall - pos[-1][0] + 1
+    return [tuple(p) for p in pos]
+
+
 # ---- extended interface --------------------------------------------------------
 
 @dataclass
@@ -271,6 +309,42 @@ class Context:
 
     def set_launch(self, grid: int = 0, t_chunk: int = 0):
         _check(lib().rfba_ctx_set_launch(self.h, grid, t_chunk))
+
+    def combine_render(self, spots, img_dims, zoom: int = 10, psf=None, noise_r: int = 30, noise_rz: int = 3,
+                       noise_threshold: int = 70):
+        """CombineBlock.m:24-173 on the GPU: uint16 volume [Z*zoom][Y*zoom][X*zoom] and the number of
+        spots that fell outside the grid."""
+        if psf is None:
+            psf = combine_psf()
+        psf = np.ascontiguousarray(psf, np.uint16)
+        sp = np.ascontiguousarray(spots, np.float64).reshape(-1, 5)
+        X, Y, Z = (int(d) for d in img_dims)
+        out = np.empty((Z * zoom, Y * zoom, X * zoom), np.uint16)
+        dims = np.array([X, Y, Z], np.int32)
+        pd = np.array([psf.shape[2], psf.shape[1], psf.shape[0]], np.int32)
+        dropped = ctypes.c_longlong()
+        _check(lib().rfba_combine_render(self.h, ctypes.c_void_p(sp.ctypes.data) if len(sp) else None, len(sp),
+                                         _iptr(dims), zoom, ctypes.c_void_p(psf.ctypes.data), _iptr(pd), noise_r,
+                                         noise_rz, noise_threshold, ctypes.c_void_p(out.ctypes.data),
+                                         ctypes.byref(dropped)))
+        return out, dropped.value
+
+    def combine_blocks(self, res_dir, img_dims, block_dims, border: int, zoom: int = 10, sigma: float = 3.5,
+                       psf_threshold: float = 1000.0, noise_r: int = 30, noise_rz: int = 3,
+                       noise_threshold: int = 70):
+        """CombineBlock.m end to end: res_i_j_k.txt of every doSplit block (i, j, k 1-based, x outer),
+        loadResult filter, then the GPU reconstruction."""
+        xs, ys, zs = (dosplit(int(img_dims[a]), int(block_dims[a]), border) for a in range(3))
+        parts = []
+        for i, (sx, nx) in enumerate(xs, 1):
+            for j, (sy, ny) in enumerate(ys, 1):
+                for k, (sz, nz) in enumerate(zs, 1):
+                    p = Path(res_dir) / f"res_{i}_{j}_{k}.txt"
+                    if p.exists():
+                        parts.append(combine_load_result(p, border, (sx, sy, sz), (nx, ny, nz)))
+        spots = np.concatenate(parts) if parts else np.zeros((0, 5))
+        return self.combine_render(spots, img_dims, zoom, combine_psf(sigma, psf_threshold), noise_r, noise_rz,
+                                   noise_threshold)
 
     def seed_spots(self, srrf_map, voxels, mag: int, num_spots: int, seed: int = 0, stream=None):
         """SRRF-guided spot seeding (multispot5_place_methods.cc:291-341): num_spots
