@@ -541,7 +541,7 @@ def run_gpu(args):
         "clocks": clocks,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "kernel": "radiality_kernel<4,4,u16>", "kernel_ms": rad_avg_ms,
+                     "kernel": "radiality_kernel<MZ=2, CZ=8, uint16, 128 threads>", "kernel_ms": rad_avg_ms,
                      "flops_per_voxel_volume": fl["separable"],
                      "peak_note": f"nominal FP32 FMA peak {props.multi_processor_count} SMs x 128 x 2 at the "
                                   f"measured max SM clock {sm_max:.0f} MHz"},
