@@ -50,6 +50,25 @@ REF_REGION_LO = (240, 240, 56)
 REF_REGION_HI = (256, 256, 64)
 
 
+def max_over_ranks(x: float) -> float:
+    """Maximum of a per-rank time over all ranks (identity without a process
+    group); the tensor lives where the backend wants it (CUDA for NCCL)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, world_size: int, seconds_max: float) -> float:
+    """Replicas (weak scaling): every rank runs the whole workload; the job rate is
+    all ranks' units over the slowest rank's time."""
+    return units_per_rank * world_size / seconds_max
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -479,11 +498,8 @@ def run_gpu(args):
     ms = e0.elapsed_time(e1)
     launches = ctx.timing().launches - launches0
     ctx.set_timing(False)
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = units_per_step * args.steps * ws / (ms / 1e3)
+    ms = max_over_ranks(ms)
+    value = whole_job_rate(units_per_step * args.steps, ws, ms / 1e3)
 
     # e2e: C-ABI entry point with pinned host buffers
     e2e = None
@@ -501,11 +517,8 @@ def run_gpu(args):
         for _ in range(args.steps):
             ctx.forward(cfg, pinned_np, out=outh_np)
         e2e_s = time.perf_counter() - t0
-        if ws > 1:
-            t = torch.tensor([e2e_s], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            e2e_s = float(t.item())
-        e2e = units_per_step * args.steps * ws / e2e_s
+        e2e_s = max_over_ranks(e2e_s)
+        e2e = whole_job_rate(units_per_step * args.steps, ws, e2e_s)
 
     # roofline of the radiality kernel
     props = torch.cuda.get_device_properties(local)
