@@ -143,8 +143,107 @@ __global__ void drift_dot_kernel(const float* __restrict__ g, const float* __res
     if (threadIdx.x == 0) atomicAdd(out + 3 * t + axis, red[0]);
 }
 
+// Drift operator on all three axes at once: the x-, y- and z-passes with
+// per-axis index clamping compose to one 4 x 4 x 4 tensor-product stencil with
+// clamped indices. mode 0 writes I'_t; mode 1 adds, per volume, the sums over
+// voxels of g * dI'/dd_a (a = x, y, z: derivative weights on axis a) into
+// out[3 t + a] (FP64, one atomic per block and axis).
+template <int MODE>
+__global__ void drift3d_kernel(const float* __restrict__ src, float* __restrict__ dst, const float* __restrict__ g,
+                               int W, int H, int D, const float* __restrict__ shifts, double* __restrict__ out,
+                               unsigned long long* err) {
+    const int t = blockIdx.y;
+    const long long nv = (long long)W * H * D;
+    const float* st = src + (long long)t * nv;
+    const float dx = shifts[3 * t], dy = shifts[3 * t + 1], dz = shifts[3 * t + 2];
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % W), y = (int)((i / W) % H), z = (int)(i / ((long long)W * H));
+        float wx[4], wy[4], wz[4], ex[4], ey[4], ez[4];
+        int ix[4], iy[4], iz[4];
+        const float px = (float)x + dx, py = (float)y + dy, pz = (float)z + dz;
+        const int bx = (int)floorf(px), by = (int)floorf(py), bz = (int)floorf(pz);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            ix[k] = clampi(bx + k - 1, 0, W - 1);
+            iy[k] = clampi(by + k - 1, 0, H - 1);
+            iz[k] = clampi(bz + k - 1, 0, D - 1);
+            wx[k] = cr(px - (float)(bx + k - 1));
+            wy[k] = cr(py - (float)(by + k - 1));
+            wz[k] = cr(pz - (float)(bz + k - 1));
+            if (MODE == 1) {
+                ex[k] = dcr(px - (float)(bx + k - 1));
+                ey[k] = dcr(py - (float)(by + k - 1));
+                ez[k] = dcr(pz - (float)(bz + k - 1));
+            }
+        }
+        // x pass per (z, y) row, then y, then z, as the per-axis passes compose
+        float v = 0.f, gx_ = 0.f, gy_ = 0.f, gz_ = 0.f;
+#pragma unroll
+        for (int kz = 0; kz < 4; ++kz) {
+            float sy = 0.f, sy_dx = 0.f, sy_dy = 0.f;
+#pragma unroll
+            for (int ky = 0; ky < 4; ++ky) {
+                const long long row = ((long long)iz[kz] * H + iy[ky]) * W;
+                float sx = 0.f, sx_d = 0.f;
+#pragma unroll
+                for (int kx = 0; kx < 4; ++kx) {
+                    const long long si = row + ix[kx];
+                    const float val = in_range(si, nv, err, 3) ? __ldg(st + si) : 0.f;
+                    sx = fmaf(wx[kx], val, sx);
+                    if (MODE == 1) sx_d = fmaf(ex[kx], val, sx_d);
+                }
+                sy = fmaf(wy[ky], sx, sy);
+                if (MODE == 1) {
+                    sy_dx = fmaf(wy[ky], sx_d, sy_dx);
+                    sy_dy = fmaf(ey[ky], sx, sy_dy);
+                }
+            }
+            v = fmaf(wz[kz], sy, v);
+            if (MODE == 1) {
+                gx_ = fmaf(wz[kz], sy_dx, gx_);
+                gy_ = fmaf(wz[kz], sy_dy, gy_);
+                gz_ = fmaf(ez[kz], sy, gz_);
+            }
+        }
+        if (MODE == 0) {
+            dst[(long long)t * nv + i] = v;
+        } else {
+            const double gg = g[(long long)t * nv + i];
+            acc[0] += gg * gx_;
+            acc[1] += gg * gy_;
+            acc[2] += gg * gz_;
+        }
+    }
+    if (MODE == 1) {
+        __shared__ double red[3][256];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) red[a][threadIdx.x] = acc[a];
+        __syncthreads();
+        for (int s2 = blockDim.x / 2; s2 > 0; s2 >>= 1) {
+            if (threadIdx.x < s2)
+#pragma unroll
+                for (int a = 0; a < 3; ++a) red[a][threadIdx.x] += red[a][threadIdx.x + s2];
+            __syncthreads();
+        }
+        if (threadIdx.x < 3) atomicAdd(out + 3 * t + threadIdx.x, red[threadIdx.x][0]);
+    }
+}
+
 // ---------------------------------------------------------------------------
-// Temporal adjoint, one thread per subvoxel of the single block.
+// Temporal adjoint, one thread per subvoxel of the single block. FP32 with
+// compensated (Kahan) sums over t: FP64 arithmetic runs at a small fraction of
+// the FP32 rate on this GPU and would make this HBM-sized pass compute-bound.
+struct KSum {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float y = x - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+};
+
 __global__ void temporal_adjoint_kernel(const BlockDev* __restrict__ blocks, const float* __restrict__ rad,
                                         const float* __restrict__ inten, const float* __restrict__ gmap, int T,
                                         int method, int order, int iw, int renorm, int poscon,
@@ -162,13 +261,13 @@ __global__ void temporal_adjoint_kernel(const BlockDev* __restrict__ blocks, con
     const float* r = rad + v;
     const float* I = inten + v;
     // first pass: sums
-    double m = 0.0, IW = 0.0;
+    KSum ms, iws;
     bool finite = isfinite(g);
     for (int t = 0; t < T; ++t) {
         const float rv = r[t * V];
         finite = finite && isfinite(rv);
-        m += rv;
-        IW += (double)rv * I[t * V];
+        ms.add(rv);
+        iws.add(rv * I[t * V]);
     }
     if (!finite) {
         for (int t = 0; t < T; ++t) {
@@ -177,47 +276,51 @@ __global__ void temporal_adjoint_kernel(const BlockDev* __restrict__ blocks, con
         }
         return;
     }
-    m /= T;
-    IW /= T;
-    const double scale_iw = iw ? IW : 1.0;
-    double C = 0.0, AB = 0, CD = 0, AC = 0, BD = 0, AD = 0, BC = 0, S4 = 0;
+    const float invT = 1.f / (float)T;
+    const float m = ms.s * invT;
+    const float IW = iws.s * invT;
+    const float scale_iw = iw ? IW : 1.f;
+    float C = 0.f, AB = 0.f, CD = 0.f, AC = 0.f, BD = 0.f, AD = 0.f, BC = 0.f;
     const int N = T - order;
     if (method == 3) {
+        KSum c1, s4, ab, cd, ac, bd, ad, bc;
         for (int t = 0; t < N; ++t) {
-            const double A = r[t * V] - m, Bv = r[(t + 1) * V] - m;
-            if (order == 2) C += A * Bv;
+            const float A = r[t * V] - m, Bv = r[(t + 1) * V] - m;
+            if (order == 2) c1.add(A * Bv);
             if (order >= 3) {
-                const double Cv = r[(t + 2) * V] - m;
-                if (order == 3) C += A * Bv * Cv;
+                const float Cv = r[(t + 2) * V] - m;
+                if (order == 3) c1.add(A * Bv * Cv);
                 if (order == 4) {
-                    const double Dv = r[(t + 3) * V] - m;
-                    S4 += A * Bv * Cv * Dv;
-                    AB += A * Bv;
-                    CD += Cv * Dv;
-                    AC += A * Cv;
-                    BD += Bv * Dv;
-                    AD += A * Dv;
-                    BC += Bv * Cv;
+                    const float Dv = r[(t + 3) * V] - m;
+                    s4.add(A * Bv * Cv * Dv);
+                    ab.add(A * Bv);
+                    cd.add(Cv * Dv);
+                    ac.add(A * Cv);
+                    bd.add(Bv * Dv);
+                    ad.add(A * Dv);
+                    bc.add(Bv * Cv);
                 }
             }
         }
-        if (order == 4) C = S4 - AB * CD - AC * BD - AD * BC;
+        C = c1.s;
+        AB = ab.s, CD = cd.s, AC = ac.s, BD = bd.s, AD = ad.s, BC = bc.s;
+        if (order == 4) C = s4.s - AB * CD - AC * BD - AD * BC;
     }
     // dC/da_s for every s, then centring (dC/dr_t = dC/da_t - mean_s dC/da_s)
-    auto dCda = [&](int s) -> double {
-        double d = 0.0;
-        auto a = [&](int t) -> double { return (t >= 0 && t < T) ? (double)r[t * V] - m : 0.0; };
+    auto dCda = [&](int s) -> float {
+        float d = 0.f;
+        auto a = [&](int t) -> float { return (t >= 0 && t < T) ? r[t * V] - m : 0.f; };
         for (int l = 0; l < order; ++l) {
             const int t0 = s - l;  // the product starting at t0 contains a_s at lag l
             if (t0 < 0 || t0 >= N) continue;
             if (order == 2) d += a(t0 + 1 - l);
             else if (order == 3) {
-                double p = 1.0;
+                float p = 1.f;
                 for (int q = 0; q < 3; ++q)
                     if (q != l) p *= a(t0 + q);
                 d += p;
             } else {
-                const double A = a(t0), Bv = a(t0 + 1), Cv = a(t0 + 2), Dv = a(t0 + 3);
+                const float A = a(t0), Bv = a(t0 + 1), Cv = a(t0 + 2), Dv = a(t0 + 3);
                 if (l == 0) d += Bv * Cv * Dv - Bv * CD - Cv * BD - Dv * BC;
                 if (l == 1) d += A * Cv * Dv - A * CD - Dv * AC - Cv * AD;
                 if (l == 2) d += A * Bv * Dv - Dv * AB - A * BD - Bv * AD;
@@ -226,25 +329,26 @@ __global__ void temporal_adjoint_kernel(const BlockDev* __restrict__ blocks, con
         }
         return d;
     };
-    double mean_d = 0.0;
+    KSum md;
     if (method == 3)
-        for (int s = 0; s < T; ++s) mean_d += dCda(s);
-    mean_d /= T;
-    const double sgn = C > 0 ? 1.0 : (C < 0 ? -1.0 : 0.0);
+        for (int s = 0; s < T; ++s) md.add(dCda(s));
+    const float mean_d = md.s * invT;
+    const float sgn = C > 0.f ? 1.f : (C < 0.f ? -1.f : 0.f);
+    const float aC = fabsf(C);
     for (int t = 0; t < T; ++t) {
         const float rv = r[t * V], Iv = I[t * V];
-        double gr, gi;
+        float gr, gi;
         if (method == 1) {
-            gr = g * (iw ? Iv : 1.f) / T;
-            gi = iw ? g * rv / T : 0.0;
+            gr = g * (iw ? Iv : 1.f) * invT;
+            gi = iw ? g * rv * invT : 0.f;
         } else {
-            gr = g * (sgn / T * scale_iw * (dCda(t) - mean_d) + (iw ? fabs(C) / T * Iv / T : 0.0));
-            gi = iw ? g * fabs(C) / T * rv / T : 0.0;
+            gr = g * (sgn * invT * scale_iw * (dCda(t) - mean_d) + (iw ? aC * invT * Iv * invT : 0.f));
+            gi = iw ? g * aC * invT * rv * invT : 0.f;
         }
-        if (renorm) gr *= 0.5;
-        if (poscon && !(rv > 0.f)) gr = 0.0;
-        gS[t * V + v] = (float)gr;
-        gI[t * V + v] = Iv > 0.f ? (float)gi : 0.f;
+        if (renorm) gr *= 0.5f;
+        if (poscon && !(rv > 0.f)) gr = 0.f;
+        gS[t * V + v] = gr;
+        gI[t * V + v] = Iv > 0.f ? gi : 0.f;
     }
 }
 
@@ -871,6 +975,17 @@ __global__ void d2f_kernel(const double* s, float* d, int n) {
 int launch_double_to_float(const double* src, float* dst, int n, void* stream) {
     if (n <= 0) return 0;
     d2f_kernel<<<(n + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(src, dst, n);
+    return (int)cudaGetLastError();
+}
+
+int launch_drift3d(const float* src, float* dst, const float* g, int W, int H, int D, int T, const float* shifts,
+                   int mode, double* out, unsigned long long* err, void* stream) {
+    const long long nv = (long long)W * H * D;
+    dim3 grid((unsigned)std::min<long long>((nv + 255) / 256, 152LL * 8 / std::max(T, 1) + 1), (unsigned)T);
+    if (mode == 0)
+        drift3d_kernel<0><<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(src, dst, g, W, H, D, shifts, out, err);
+    else
+        drift3d_kernel<1><<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(src, dst, g, W, H, D, shifts, out, err);
     return (int)cudaGetLastError();
 }
 

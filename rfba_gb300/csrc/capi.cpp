@@ -954,15 +954,11 @@ static int apply_drift(rfba_ctx* ctx, const float* in, const float* shifts, cons
     if ((s = ctx->shifted.ensure(n * 4, "shifted input")) || (s = ctx->tmp1.ensure(n * 4, "scratch")) ||
         (s = ctx->tmp2.ensure(n * 4, "scratch")))
         return s;
-    float* t1 = static_cast<float*>(ctx->tmp1.p);
-    float* t2 = static_cast<float*>(ctx->tmp2.p);
     float* out = static_cast<float*>(ctx->shifted.p);
     unsigned long long* err = static_cast<unsigned long long*>(ctx->errw.p);
-    int e = launch_shift_axis(in, t1, dims[0], dims[1], dims[2], dims[3], 0, shifts, 0, err, st);
-    if (!e) e = launch_shift_axis(t1, t2, dims[0], dims[1], dims[2], dims[3], 1, shifts, 0, err, st);
-    if (!e) e = launch_shift_axis(t2, out, dims[0], dims[1], dims[2], dims[3], 2, shifts, 0, err, st);
+    const int e = launch_drift3d(in, out, nullptr, dims[0], dims[1], dims[2], dims[3], shifts, 0, nullptr, err, st);
     if (e) return cuda_fail((cudaError_t)e, "drift resampling");
-    ctx->launches += 3;
+    ctx->launches += 1;
     *iprime = out;
     return RFBA_OK;
 }
@@ -1163,14 +1159,8 @@ static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const flo
             if ((s = ctx->dshift.ensure((size_t)T * 3 * sizeof(double), "drift adjoint"))) return s;
             double* ds = static_cast<double*>(ctx->dshift.p);
             RFBA_CUDA(cudaMemsetAsync(ds, 0, (size_t)T * 3 * sizeof(double), st), "drift adjoint clear");
-            const long long nv = (long long)dims[0] * dims[1] * dims[2];
-            for (int ax = 0; ax < 3 && !e; ++ax) {
-                e = launch_shift_axis(in, t1, dims[0], dims[1], dims[2], T, 0, shifts, ax == 0 ? 1 : 0, err, st);
-                if (!e) e = launch_shift_axis(t1, t2, dims[0], dims[1], dims[2], T, 1, shifts, ax == 1 ? 1 : 0, err, st);
-                if (!e) e = launch_shift_axis(t2, t1, dims[0], dims[1], dims[2], T, 2, shifts, ax == 2 ? 1 : 0, err, st);
-                if (!e) e = launch_drift_dot(gin, t1, nv, T, ax, ds, err, st);
-                ctx->launches += 4;
-            }
+            e = launch_drift3d(in, nullptr, gin, dims[0], dims[1], dims[2], T, shifts, 1, ds, err, st);
+            ctx->launches += 1;
             if (!e) e = launch_double_to_float(ds, dshift, 3 * T, st);
             ctx->launches += 1;
         }

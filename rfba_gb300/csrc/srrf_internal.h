@@ -149,6 +149,10 @@ int launch_temporal_adjoint(const BlockDev* blocks, long long vox, const float* 
                             float* gI, long long nmap, unsigned long long* err, void* stream);
 int launch_shift_axis(const float* src, float* dst, int W, int H, int D, int T, int axis, const float* shifts, int mode,
                       unsigned long long* err, void* stream);
+// Drift operator, all axes fused: mode 0 resamples src into dst; mode 1 adds
+// sum_voxels g * dI'/dd_a into out[3 t + a] (FP64).
+int launch_drift3d(const float* src, float* dst, const float* g, int W, int H, int D, int T, const float* shifts,
+                   int mode, double* out, unsigned long long* err, void* stream);
 int launch_drift_dot(const float* g, const float* dv, long long nv, int T, int axis, double* out,
                      unsigned long long* err, void* stream);
 int launch_double_to_float(const double* src, float* dst, int n, void* stream);
