@@ -150,69 +150,82 @@ __global__ void drift_dot_kernel(const float* __restrict__ g, const float* __res
 // out[3 t + a] (FP64, one atomic per block and axis).
 template <int MODE>
 __global__ void drift3d_kernel(const float* __restrict__ src, float* __restrict__ dst, const float* __restrict__ g,
-                               int W, int H, int D, const float* __restrict__ shifts, double* __restrict__ out,
-                               unsigned long long* err) {
+                               int W, int H, int D, const float* __restrict__ shifts, double* __restrict__ out) {
     const int t = blockIdx.y;
     const long long nv = (long long)W * H * D;
     const float* st = src + (long long)t * nv;
     const float dx = shifts[3 * t], dy = shifts[3 * t + 1], dz = shifts[3 * t + 2];
     double acc[3] = {0.0, 0.0, 0.0};
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += (long long)gridDim.x * blockDim.x) {
-        const int x = (int)(i % W), y = (int)((i / W) % H), z = (int)(i / ((long long)W * H));
-        float wx[4], wy[4], wz[4], ex[4], ey[4], ez[4];
-        int ix[4], iy[4], iz[4];
-        const float px = (float)x + dx, py = (float)y + dy, pz = (float)z + dz;
-        const int bx = (int)floorf(px), by = (int)floorf(py), bz = (int)floorf(pz);
+    // one (z, y) output row per block iteration, x across the threads; every
+    // index is clamped into the volume, so no tap can leave it
+    for (int row = blockIdx.x; row < D * H; row += gridDim.x) {
+        const int z = row / H, y = row - z * H;
+        const float py = (float)y + dy, pz = (float)z + dz;
+        const int by = (int)floorf(py), bz = (int)floorf(pz);
+        float wy[4], wz[4], ey[4], ez[4];
+        const float* rows[4][4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            ix[k] = clampi(bx + k - 1, 0, W - 1);
-            iy[k] = clampi(by + k - 1, 0, H - 1);
-            iz[k] = clampi(bz + k - 1, 0, D - 1);
-            wx[k] = cr(px - (float)(bx + k - 1));
             wy[k] = cr(py - (float)(by + k - 1));
             wz[k] = cr(pz - (float)(bz + k - 1));
             if (MODE == 1) {
-                ex[k] = dcr(px - (float)(bx + k - 1));
                 ey[k] = dcr(py - (float)(by + k - 1));
                 ez[k] = dcr(pz - (float)(bz + k - 1));
             }
         }
-        // x pass per (z, y) row, then y, then z, as the per-axis passes compose
-        float v = 0.f, gx_ = 0.f, gy_ = 0.f, gz_ = 0.f;
 #pragma unroll
-        for (int kz = 0; kz < 4; ++kz) {
-            float sy = 0.f, sy_dx = 0.f, sy_dy = 0.f;
+        for (int kz = 0; kz < 4; ++kz)
 #pragma unroll
-            for (int ky = 0; ky < 4; ++ky) {
-                const long long row = ((long long)iz[kz] * H + iy[ky]) * W;
-                float sx = 0.f, sx_d = 0.f;
+            for (int ky = 0; ky < 4; ++ky)
+                rows[kz][ky] = st + ((long long)clampi(bz + kz - 1, 0, D - 1) * H + clampi(by + ky - 1, 0, H - 1)) * W;
+        for (int x = threadIdx.x; x < W; x += blockDim.x) {
+            const float px = (float)x + dx;
+            const int bx = (int)floorf(px);
+            float wx[4], ex[4];
+            int ix[4];
 #pragma unroll
-                for (int kx = 0; kx < 4; ++kx) {
-                    const long long si = row + ix[kx];
-                    const float val = in_range(si, nv, err, 3) ? __ldg(st + si) : 0.f;
-                    sx = fmaf(wx[kx], val, sx);
-                    if (MODE == 1) sx_d = fmaf(ex[kx], val, sx_d);
+            for (int k = 0; k < 4; ++k) {
+                ix[k] = clampi(bx + k - 1, 0, W - 1);
+                wx[k] = cr(px - (float)(bx + k - 1));
+                if (MODE == 1) ex[k] = dcr(px - (float)(bx + k - 1));
+            }
+            // x pass per (z, y) row, then y, then z, as the per-axis passes compose
+            float v = 0.f, gx_ = 0.f, gy_ = 0.f, gz_ = 0.f;
+#pragma unroll
+            for (int kz = 0; kz < 4; ++kz) {
+                float sy = 0.f, sy_dx = 0.f, sy_dy = 0.f;
+#pragma unroll
+                for (int ky = 0; ky < 4; ++ky) {
+                    const float* rp = rows[kz][ky];
+                    float sx = 0.f, sx_d = 0.f;
+#pragma unroll
+                    for (int kx = 0; kx < 4; ++kx) {
+                        const float val = __ldg(rp + ix[kx]);
+                        sx = fmaf(wx[kx], val, sx);
+                        if (MODE == 1) sx_d = fmaf(ex[kx], val, sx_d);
+                    }
+                    sy = fmaf(wy[ky], sx, sy);
+                    if (MODE == 1) {
+                        sy_dx = fmaf(wy[ky], sx_d, sy_dx);
+                        sy_dy = fmaf(ey[ky], sx, sy_dy);
+                    }
                 }
-                sy = fmaf(wy[ky], sx, sy);
+                v = fmaf(wz[kz], sy, v);
                 if (MODE == 1) {
-                    sy_dx = fmaf(wy[ky], sx_d, sy_dx);
-                    sy_dy = fmaf(ey[ky], sx, sy_dy);
+                    gx_ = fmaf(wz[kz], sy_dx, gx_);
+                    gy_ = fmaf(wz[kz], sy_dy, gy_);
+                    gz_ = fmaf(ez[kz], sy, gz_);
                 }
             }
-            v = fmaf(wz[kz], sy, v);
-            if (MODE == 1) {
-                gx_ = fmaf(wz[kz], sy_dx, gx_);
-                gy_ = fmaf(wz[kz], sy_dy, gy_);
-                gz_ = fmaf(ez[kz], sy, gz_);
+            const long long o = (long long)t * nv + (long long)row * W + x;
+            if (MODE == 0) {
+                dst[o] = v;
+            } else {
+                const double gg = g[o];
+                acc[0] += gg * gx_;
+                acc[1] += gg * gy_;
+                acc[2] += gg * gz_;
             }
-        }
-        if (MODE == 0) {
-            dst[(long long)t * nv + i] = v;
-        } else {
-            const double gg = g[(long long)t * nv + i];
-            acc[0] += gg * gx_;
-            acc[1] += gg * gy_;
-            acc[2] += gg * gz_;
         }
     }
     if (MODE == 1) {
@@ -980,12 +993,14 @@ int launch_double_to_float(const double* src, float* dst, int n, void* stream) {
 
 int launch_drift3d(const float* src, float* dst, const float* g, int W, int H, int D, int T, const float* shifts,
                    int mode, double* out, unsigned long long* err, void* stream) {
-    const long long nv = (long long)W * H * D;
-    dim3 grid((unsigned)std::min<long long>((nv + 255) / 256, 152LL * 8 / std::max(T, 1) + 1), (unsigned)T);
+    (void)err;  // every tap index is clamped into the volume
+    const int threads = W >= 256 ? 256 : (W >= 128 ? 128 : (W >= 64 ? 64 : 32));
+    dim3 grid((unsigned)std::min<long long>((long long)D * H, std::max(152LL * 16 / std::max(T, 1), 8LL)),
+              (unsigned)T);
     if (mode == 0)
-        drift3d_kernel<0><<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(src, dst, g, W, H, D, shifts, out, err);
+        drift3d_kernel<0><<<grid, threads, 0, static_cast<cudaStream_t>(stream)>>>(src, dst, g, W, H, D, shifts, out);
     else
-        drift3d_kernel<1><<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(src, dst, g, W, H, D, shifts, out, err);
+        drift3d_kernel<1><<<grid, threads, 0, static_cast<cudaStream_t>(stream)>>>(src, dst, g, W, H, D, shifts, out);
     return (int)cudaGetLastError();
 }
 
