@@ -429,6 +429,68 @@ def measure_large(ctx, iters: int = 20, volumes=None) -> dict:
             "drift_rms_error_before": rms0, "drift_rms_error_after": rms(sh)}
 
 
+def measure_seeding(ctx, steps: int = 5) -> dict:
+    """SRRF-guided spot seeding: a 29^3-voxel 3B block mask at magnification 3
+    (658,503 candidate subvoxels) over a synthetic SRRF map, 100,000 spots per
+    call; GPU inverse-CDF sampler (device map and voxel list) against the
+    reference's rejection loop restated on the host (numpy, one core, 10,000
+    spots)."""
+    import torch
+    from oracle import oracle as O
+    rng = np.random.default_rng(12)
+    mag, B = 3, 29
+    m = rng.gamma(0.6, 1.0, size=(B * mag, B * mag, B * mag)).astype(np.float32)
+    vox = np.array([(x, y, z) for z in range(B) for y in range(B) for x in range(B)], np.int32)
+    md = torch.from_numpy(m).cuda()
+    n = 100000
+    ctx.seed_spots(md, vox, mag, n, seed=1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in range(steps):
+        ctx.seed_spots(md, vox, mag, n, seed=2 + s)
+    torch.cuda.synchronize()
+    gpu_s = (time.perf_counter() - t0) / steps
+    nc = 10000
+    t0 = time.perf_counter()
+    O.seed_spots_rejection(m, vox, mag, nc, np.random.default_rng(0))
+    cpu_s = time.perf_counter() - t0
+    return {"workload": "seeding: 29^3 mask voxels x mag 3 (658,503 candidates), 100,000 spots per call",
+            "gpu_ms_per_call": gpu_s * 1e3, "gpu_spots_per_s": n / gpu_s,
+            "cpu_reference_loop_spots_per_s": nc / cpu_s, "cpu_sample": f"{nc} spots, numpy, 1 core"}
+
+
+def measure_combine(ctx, steps: int = 3) -> dict:
+    """CombineBlock reconstruction: 50,000 localisations in a 40x40x30 image,
+    zoom 10 (400x400x300 grid, 48 M voxels), the script's noise mask (r 30, rz 3,
+    threshold 70) and PSF (sigma 3.5, threshold 1000); GPU against the numpy
+    restatement on a 10,000-spot, zoom 5 sample."""
+    from oracle import combine_oracle as C
+    from rfba_gb300 import srrf
+    rng = np.random.default_rng(13)
+    img = (40, 40, 30)
+    sp = np.empty((50000, 5))
+    centres = rng.uniform(5, 25, size=(200, 3))
+    k = rng.integers(0, 200, 50000)
+    for a in range(3):
+        sp[:, 2 + a] = np.clip(centres[k, a] + rng.normal(0, 0.4, 50000), 0, img[a] - 1)
+    sp[:, 0] = 500.0
+    sp[:, 1] = 1.5
+    psf = srrf.combine_psf(3.5, 1000.0)
+    ctx.combine_render(sp, img, 10, psf)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        out, _ = ctx.combine_render(sp, img, 10, psf)
+    gpu_s = (time.perf_counter() - t0) / steps
+    small = sp[:10000]
+    t0 = time.perf_counter()
+    C.render(small, img, 5, psf, 30, 3, 70)
+    cpu_s = time.perf_counter() - t0
+    return {"workload": "combine: 50,000 spots, 40x40x30 image, zoom 10 (48 M grid voxels), PSF 3.5/1000, "
+                        "mask 30/3/70", "gpu_ms_per_call": gpu_s * 1e3, "gpu_grid_voxels_per_s": out.size / gpu_s,
+            "cpu_reference_s": cpu_s, "cpu_sample": "10,000 spots, zoom 5 (6 M grid voxels), numpy, 1 core",
+            "cpu_grid_voxels_per_s": (40 * 5) * (40 * 5) * (30 * 5) / cpu_s}
+
+
 def run_single_workload(args):
     """One of the secondary measurements alone, printed as its own JSON line."""
     import torch
@@ -441,6 +503,10 @@ def run_single_workload(args):
         r = measure_batching(ctx, max(2, args.steps))
     elif args.workload == "large":
         r = measure_large(ctx, iters=args.iters, volumes=args.volumes)
+    elif args.workload == "seeding":
+        r = measure_seeding(ctx)
+    elif args.workload == "combine":
+        r = measure_combine(ctx)
     else:
         r = measure_diff(ctx, max(3, args.steps), iters=args.iters, volumes=args.volumes)
     ctx.close()
@@ -585,7 +651,7 @@ def main():
     ap.add_argument("--volumes", type=int, default=None,
                     help="fewer volumes than the workload's (profiling case only)")
     ap.add_argument("--iters", type=int, default=20, help="drift refinement iterations (diff workload)")
-    ap.add_argument("--workload", default="mid", choices=["mid", "batching", "diff", "large"],
+    ap.add_argument("--workload", default="mid", choices=["mid", "batching", "diff", "large", "seeding", "combine"],
                     help="mid: the headline line; batching / diff: that measurement alone (one JSON line)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
