@@ -47,6 +47,17 @@ CASES = [
     ("axes4", 5, 9, 9, 9, dict(mag=2, method=1, axes_in_ring=4, gradient_smooth=1, x_range=1, y_range=1, z_range=1)),
     ("radius_03", 5, 9, 9, 9, dict(mag=2, method=1, ring_radius=0.3, gradient_smooth=1, x_range=1, y_range=1,
                                    z_range=1)),
+    # 12-row tiles (mag_y 6), the 224-thread 28-row tile (mag_y 7), mag 8
+    ("mag6", 3, 6, 6, 7, dict(mag=6, method=1, gradient_smooth=1, x_range=1, y_range=1, z_range=1)),
+    ("mag7", 3, 5, 6, 5, dict(mag=7, method=3, itc=0, trac_order=2, gradient_smooth=1, x_range=1, y_range=1,
+                              z_range=1)),
+    ("mag8", 2, 5, 5, 6, dict(mag=8, method=1, gradient_smooth=1, x_range=1, y_range=1, z_range=1)),
+    # short series: one volume; TRAC with no full lag window; ITC 1 binning of 3 volumes
+    ("t1_tra", 1, 8, 8, 9, dict(mag=2, method=1, gradient_smooth=1, x_range=1, y_range=1, z_range=1)),
+    ("t2_trac2", 2, 8, 9, 8, dict(mag=2, method=3, itc=0, trac_order=2, gradient_smooth=1, x_range=1, y_range=1,
+                                  z_range=1)),
+    ("t3_trac2_itc1", 3, 8, 8, 8, dict(mag=2, method=3, itc=1, trac_order=2, gradient_smooth=1, x_range=1,
+                                       y_range=1, z_range=1)),
 ]
 
 
