@@ -81,3 +81,42 @@ def test_combine_blocks_pipeline(ctx, tmp_path):
                                 noise_threshold=3)
     exp = C.render(np.concatenate(allsp), img, 3, C.genpsf(1.5, 1000.0), 2, 1, 3)
     assert np.array_equal(got, exp)
+
+
+@pytest.mark.gpu
+def test_combine_cli_writes_tiff(tmp_path):
+    import subprocess
+    import sys
+    from pathlib import Path
+    from rfba_gb300 import srrf
+    rng = np.random.default_rng(9)
+    img, block, border = (12, 10, 8), (7, 6, 6), 1
+    xs, ys, zs = (srrf.dosplit(img[a], block[a], border) for a in range(3))
+    allsp = []
+    for i, (sx, nx) in enumerate(xs, 1):
+        for j, (sy, ny) in enumerate(ys, 1):
+            for k, (sz, nz) in enumerate(zs, 1):
+                sp = _spots(rng, 40, img)
+                _write_res(tmp_path / f"res_{i}_{j}_{k}.txt", sp)
+                allsp.append(C.load_result(tmp_path / f"res_{i}_{j}_{k}.txt", border, (sx, sy, sz), (nx, ny, nz)))
+    out = tmp_path / "reconstruction.tif"
+    root = Path(__file__).resolve().parents[1]
+    subprocess.run([sys.executable, "-m", "rfba_gb300.combine_cli", "--dims", *map(str, img), "--block",
+                    *map(str, block), "--border", str(border), "--zoom", "3", "--sigma", "1.5", "--noise-r", "2",
+                    "--noise-rz", "1", "--noise-threshold", "3", str(tmp_path), str(out)], check=True, cwd=root)
+    exp = C.render(np.concatenate(allsp), img, 3, C.genpsf(1.5, 1000.0), 2, 1, 3)
+    # read back the pages (little-endian, one strip per page as written)
+    import struct
+    b = out.read_bytes()
+    pages = []
+    off = struct.unpack("<I", b[4:8])[0]
+    while off:
+        n = struct.unpack("<H", b[off:off + 2])[0]
+        tags = {}
+        for e in range(n):
+            tag, typ, cnt, val = struct.unpack("<HHII", b[off + 2 + 12 * e: off + 14 + 12 * e])
+            tags[tag] = val & 0xFFFF if typ == 3 else val
+        W, H, so = tags[256], tags[257], tags[273]
+        pages.append(np.frombuffer(b[so:so + W * H * 2], "<u2").reshape(H, W))
+        off = struct.unpack("<I", b[off + 2 + 12 * n: off + 6 + 12 * n])[0]
+    assert np.array_equal(np.stack(pages), exp)
