@@ -75,6 +75,19 @@ def _compile(src: Path, verbose_ptxas: bool) -> Path:
 
 
 def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
+    """Compile when a source is newer than the library. Concurrent callers (one
+    per rank) serialise on a lock file, and the later ones find it up to date."""
+    import fcntl
+    OUT_DIR.mkdir(parents=True, exist_ok=True)
+    with open(OUT_DIR / ".build.lock", "w") as lk:
+        fcntl.flock(lk, fcntl.LOCK_EX)
+        try:
+            return _build_locked(force, verbose_ptxas)
+        finally:
+            fcntl.flock(lk, fcntl.LOCK_UN)
+
+
+def _build_locked(force: bool, verbose_ptxas: bool) -> Path:
     cu, cpp = sources()
     srcs = cu + cpp
     headers = list(CSRC.glob("*.h")) + list((PKG.parent / "include").glob("*.h"))
