@@ -18,8 +18,12 @@ Printed JSON line (rank 0):
            nominal FP32 FMA peak at the measured maximum SM clock;
   cpu_baseline  the FP32 CPU port of the reference radiality loop (oracle/,
            OpenMP over all host cores) timed on a bounded sub-slab.
---impl reference times that CPU implementation alone (the reference has no
-runnable GPU path here: its CUDA sources are not available on the GPU host).
+  reference_gpu  the reference's own CUDA kernels (kernel.cu built for sm_103a
+           into baseline/_ref, driven as its host code drives them) on this
+           GPU, on the small and the 216-block batching series, next to this
+           library (the reference has one magnification for all axes and int
+           index arithmetic, so it cannot run the mid workload itself).
+--impl reference times the CPU port alone, on the mid workload.
 """
 from __future__ import annotations
 
@@ -274,6 +278,80 @@ def measure_batching(ctx, steps: int) -> dict:
             "cases": cases}
 
 
+def measure_reference_gpu(ctx, sample_blocks: int = 8) -> dict:
+    """The reference's own CUDA kernels (kernel.cu, compiled for sm_103a) on this
+    GPU, driven as SRRFGradientCalcGPU and the GradientCalc.cpp block loop drive
+    them (baseline/refgpu.py), next to this library on the same inputs:
+    (1) the small series (30 x 32^3 u16, mag 2, temporal mean with intensity
+    weighting) as one call; (2) the 216-block batching series (50 x 160^3, mag 3,
+    doSplit 29/1 blocks, temporal mean), the reference's per-block loop timed on
+    the first `sample_blocks` blocks (all 50 volumes) and scaled to all blocks by
+    voxel-volumes. Each part reports the relative L-inf difference of the maps."""
+    import torch
+    from baseline import refgpu
+    from rfba_gb300 import srrf, synth
+    from tests.parity import rel_linf
+    if not refgpu.available():
+        return {"unavailable": "baseline/_ref cubin not built (needs the reference sources where build() runs)"}
+    ref = refgpu.RefGPU(0)
+    res = {}
+    try:
+        kw = dict(gradient_smooth=1, main_range=1, x_range=1, y_range=1, z_range=1, method=1, intensity_w=1)
+        cfg = srrf.Config.make(mag=2, **kw)
+        x, _ = synth.workload("small")
+        xf = x.astype(np.float32)
+        ref.gradient_calc_gpu(xf, cfg)
+        rmap, st = ref.gradient_calc_gpu(xf, cfg)
+        xd = torch.from_numpy(x.view(np.int16)).cuda()
+        out = ctx.forward(cfg, xd)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(5):
+            ctx.forward(cfg, xd, out=out)
+        e1.record()
+        torch.cuda.synchronize()
+        ours_ms = e0.elapsed_time(e1) / 5
+        units = int(np.prod(rmap.shape)) * x.shape[0]
+        res["small"] = {"workload": "30 x 32^3 u16 -> 64^3 map, mag 2, TRA (IW), one call",
+                        "reference_kernel_ms": st["kernel_ms"], "reference_call_ms": st["call_ms"],
+                        "ours_device_ms": ours_ms,
+                        "reference_kernel_value": units / (st["kernel_ms"] / 1e3),
+                        "ours_device_value": units / (ours_ms / 1e3),
+                        "speedup_kernels": st["kernel_ms"] / ours_ms,
+                        "nan_masks_equal": bool(np.array_equal(np.isnan(rmap), np.isnan(out.cpu().numpy()))),
+                        "rel_linf_vs_reference": rel_linf(out.cpu().numpy(), rmap)}
+
+        cfg = srrf.Config.make(mag=3, **kw)
+        x, _ = synth.workload("batching", shape=(160, 160, 160))
+        blocks, n, oe = srrf.blocks_dosplit(cfg, x.shape, 29, 1)
+        ours = ctx.forward_blocks(cfg, x, blocks, n, oe)
+        k = min(sample_blocks, n)
+        rout = np.full(oe, np.nan, np.float32)
+        ref.gc_block_loop(x, cfg, blocks, 1, rout)  # warm
+        st = ref.gc_block_loop(x, cfg, blocks, k, rout)
+        mask = np.zeros(oe, bool)
+        for i in range(k):
+            b = blocks[i]
+            mask[b.out_offset:b.out_offset + int(np.prod([b.hi[a] - b.lo[a] for a in range(3)]))] = True
+        units_sample = int(mask.sum()) * x.shape[0]
+        units_all = oe * x.shape[0]
+        scale = units_all / units_sample
+        res["batching_216"] = {
+            "workload": "50 x 160^3 u16, doSplit 29/1 blocks (216), mag 3, TRA (IW)",
+            "sample": f"reference per-block loop on blocks 0-{k - 1} of {n}, all 50 volumes, "
+                      f"scaled by voxel-volumes x{scale:.1f}",
+            "reference_plain_wall_ms_est": st["wall_ms"] * scale,
+            "reference_plain_kernel_ms_est": st["kernel_ms"] * scale,
+            "reference_plain_value": units_sample / (st["wall_ms"] / 1e3),
+            "reference_kernel_value": units_sample / (st["kernel_ms"] / 1e3),
+            "nan_masks_equal": bool(np.array_equal(np.isnan(rout[mask]), np.isnan(ours[mask]))),
+            "rel_linf_vs_reference": rel_linf(ours[mask], rout[mask])}
+    finally:
+        ref.close()
+    return res
+
+
 def measure_diff(ctx, steps: int, iters: int = 20, volumes=None) -> dict:
     """Differentiation workload: 60 volumes of 64^3 float32 (300 emitters) with a
     random-walk drift (sigma 0.15 voxel per step) applied by Catmull-Rom
@@ -507,6 +585,8 @@ def run_single_workload(args):
         r = measure_seeding(ctx)
     elif args.workload == "combine":
         r = measure_combine(ctx)
+    elif args.workload == "refgpu":
+        r = measure_reference_gpu(ctx)
     else:
         r = measure_diff(ctx, max(3, args.steps), iters=args.iters, volumes=args.volumes)
     ctx.close()
@@ -629,6 +709,7 @@ def run_gpu(args):
     if rank == 0 and not args.no_extras:
         line["batching"] = measure_batching(ctx, max(2, args.steps // 2))
         line["differentiation"] = measure_diff(ctx, max(3, args.steps))
+        line["reference_gpu"] = measure_reference_gpu(ctx)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(x)
     ctx.close()
@@ -651,7 +732,7 @@ def main():
     ap.add_argument("--volumes", type=int, default=None,
                     help="fewer volumes than the workload's (profiling case only)")
     ap.add_argument("--iters", type=int, default=20, help="drift refinement iterations (diff workload)")
-    ap.add_argument("--workload", default="mid", choices=["mid", "batching", "diff", "large", "seeding", "combine"],
+    ap.add_argument("--workload", default="mid", choices=["mid", "batching", "diff", "large", "seeding", "combine", "refgpu"],
                     help="mid: the headline line; batching / diff: that measurement alone (one JSON line)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":

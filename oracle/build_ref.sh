@@ -4,10 +4,11 @@
 # headers in oracle/refshim, so the reference's exact FP32 arithmetic and its
 # block split / put-back loop run on CPU cores. It pins the oracle.
 #
-# The only change made to the reference text is mechanical and happens in the
-# build output folder: each CUDA launch `k << <g, b >> > (args)` becomes
-# `REF_LAUNCH(g, b, k, args)` (a host grid loop). GradientCalc.cpp compiles from
-# where it lies. Nothing here is committed; oracle/_ref/ is git-ignored.
+# The only change made to the reference text is mechanical and happens in a
+# temporary folder outside the repository (removed on exit): each CUDA launch
+# `k << <g, b >> > (args)` becomes `REF_LAUNCH(g, b, k, args)` (a host grid
+# loop). GradientCalc.cpp compiles from where it lies. Only the built library
+# lands in oracle/_ref/, which is git-ignored.
 #
 # Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
 set -euo pipefail
@@ -20,14 +21,17 @@ if [ ! -f "$src/kernel.cu" ]; then
 fi
 out="$here/_ref"
 mkdir -p "$out"
+rm -f "$out/kernel_host.cpp"
+tmp="$(mktemp -d)"
+trap 'rm -rf "$tmp"' EXIT
 sed -E 's/([A-Za-z_][A-Za-z0-9_]*) << <([A-Za-z_][A-Za-z0-9_]*), ([A-Za-z_][A-Za-z0-9_]*) >> > \(/REF_LAUNCH(\2, \3, \1, /' \
-  "$src/kernel.cu" > "$out/kernel_host.cpp"
-if grep -q '<<<\|<< <' "$out/kernel_host.cpp"; then
+  "$src/kernel.cu" > "$tmp/kernel_host.cpp"
+if grep -q '<<<\|<< <' "$tmp/kernel_host.cpp"; then
   echo "build_ref: a launch was not rewritten" >&2
   exit 1
 fi
 g++ -O2 -std=c++17 -ffp-contract=off -fno-fast-math -fopenmp -fPIC -shared -w "-D__declspec(x)=" \
   -I "$here/refshim" -I "$src" \
-  "$out/kernel_host.cpp" "$src/GradientCalc.cpp" "$here/refshim/ref_launch.cpp" \
+  "$tmp/kernel_host.cpp" "$src/GradientCalc.cpp" "$here/refshim/ref_launch.cpp" \
   -o "$out/libsrrf_ref_host.so"
 echo "build_ref: built $out/libsrrf_ref_host.so"
