@@ -403,9 +403,14 @@ __global__ void __launch_bounds__(WIDE ? kMaxThreads : 128, WIDE ? 2 : 3)
                         for (int z = 0; z < FZ; ++z) {
                             const int zr = z % MZ, zi = z / MZ;
                             const float* qz = wzi + zr * 5;
-                            float2 acc = mul2(dup(qz[0]), Tw[zi]);
+                            // exactly the reference's 4 taps (kernel.cu:268-283), so a
+                            // non-finite voxel reaches the same subvoxels: they start one
+                            // coarse cell later when floor((zr + 0.5) / mz - 0.5) = 0,
+                            // i.e. when 2 zr + 1 >= mz (the fifth weight is 0)
+                            const int m0 = (2 * zr + 1 >= MZ) ? 1 : 0;
+                            float2 acc = mul2(dup(qz[m0]), Tw[zi + m0]);
 #pragma unroll
-                            for (int m = 1; m < 5; ++m) acc = fma2(dup(qz[m]), Tw[zi + m], acc);
+                            for (int m = m0 + 1; m < m0 + 4; ++m) acc = fma2(dup(qz[m]), Tw[zi + m], acc);
                             const int Z = Z0 + z;
                             if (Z >= B.lo[2] && Z < B.hi[2]) {
                                 const bool zint = Z >= B.int_lo[2] && Z <= B.int_hi[2];

@@ -151,3 +151,56 @@ def test_temporal_reductions_known_answers(oracle_mod):
             for itc in (0, 1):
                 got = O.temporal(O.make_conf(method=3, itc=itc, trac_order=order), rr, ii)
                 assert got == pytest.approx(_trac_known(rr, ii, order, itc), rel=1e-12, abs=1e-12)
+
+
+def special_inputs():
+    """Inputs at the edges of the domain, shared with the GPU tests: flat and
+    all-zero series (every gradient 0, so every sample is the reference's
+    0/0 = NaN), structure along one axis only (gradients exactly parallel to
+    ring axes), and float series with NaN (and one with +Inf) voxels at least 3 voxels from
+    every face (the reference's one-past-row read at the window edge can then
+    never reach them). Returns [(name, x [T][D][H][W] float32, config)]."""
+    rng = np.random.default_rng(17)
+    smooth = dict(gradient_smooth=1, x_range=1, y_range=1, z_range=1)
+    out = []
+    out.append(("flat", np.full((4, 8, 9, 10), 100.0, np.float32), dict(mag=2, method=1, **smooth)))
+    out.append(("zeros", np.zeros((3, 8, 8, 8), np.float32), dict(mag=3, method=3, itc=0, trac_order=2, **smooth)))
+    xs = 100.0 + 30.0 * np.sin(0.7 * np.arange(12))
+    ramp_x = np.broadcast_to(xs, (5, 8, 9, 12)).astype(np.float32).copy()
+    ramp_x *= (1.0 + 0.1 * np.arange(5))[:, None, None, None].astype(np.float32)
+    out.append(("along_x_tra", ramp_x, dict(mag=2, method=1, **smooth)))
+    out.append(("along_x_trm_central", ramp_x, dict(mag=2, method=0, gradient_smooth=0)))
+    zs = 80.0 + 25.0 * np.cos(0.9 * np.arange(9))
+    ramp_z = np.broadcast_to(zs[None, :, None, None], (6, 9, 8, 10)).astype(np.float32).copy()
+    ramp_z *= (1.0 + 0.05 * np.arange(6))[:, None, None, None].astype(np.float32)
+    out.append(("along_z_trac2_m442", ramp_z, dict(mag=(4, 4, 2), method=3, itc=0, trac_order=2, **smooth)))
+    x = (rng.poisson(100, size=(5, 10, 10, 11)) + 20 * rng.random((5, 10, 10, 11))).astype(np.float32)
+    x[1, 4, 5, 6] = np.nan
+    out.append(("nan_tra", x, dict(mag=2, method=1, **smooth)))
+    out.append(("nan_trac2", x, dict(mag=2, method=3, itc=0, trac_order=2, **smooth)))
+    out.append(("nan_trm_mag3", x, dict(mag=3, method=0, **smooth)))
+    x = x.copy()
+    x[3, 6, 3, 4] = np.inf
+    out.append(("inf_tra", x, dict(mag=2, method=1, **smooth)))
+    return out
+
+
+@pytest.mark.parametrize("case", [c[0] for c in special_inputs()])
+def test_oracle_special_inputs_against_reference_build(oracle_mod, case):
+    """The FP32 port reproduces the reference build bit for bit, NaN masks
+    included, on the special inputs."""
+    if oracle_mod.ref_lib() is None:
+        pytest.skip("oracle/_ref not built (reference sources absent)")
+    name, x, kw = next(c for c in special_inputs() if c[0] == case)
+    c = oracle_mod.make_conf(**kw)
+    if len(set(np.atleast_1d(kw["mag"]).tolist())) != 1:
+        pytest.skip("the reference has one magnification for all axes")
+    ref = oracle_mod.ref_block(x, c)
+    got = oracle_mod.srrf_region(x, c, dtype=np.float32)
+    assert np.array_equal(np.isnan(got), np.isnan(ref)), name
+    fin = ~np.isnan(ref)
+    assert np.array_equal(got[fin].view(np.uint32), ref[fin].view(np.uint32)), name
+    if name in ("flat", "zeros"):
+        assert np.isnan(ref).all()
+    if name.startswith(("nan", "inf")) and kw["method"] != 0:  # TRM's fmaxf drops NaN
+        assert 0 < np.isnan(ref).mean() < 1
