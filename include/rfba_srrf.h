@@ -207,6 +207,16 @@ int rfba_blocks_dosplit(const rfba_srrf_config* cfg, const int dims[4], const in
  * distinct x values, and the raw sample count. Any pointer may be NULL. */
 int rfba_srrf_plan_info(const rfba_srrf_config* cfg, int* npoints, int* npairs, int* nxvalues, int* nraw);
 
+/* Device-side failure check. No counterpart in the reference (GradientCalc.cpp
+ * and kernel.cu check no CUDA status; every call returns 0). Waits for the
+ * work the context last enqueued and reports failures its kernels recorded
+ * since the last report: RFBA_ERR_TIMEOUT when a bounded device wait gave up
+ * (an input staging copy that did not land within about a second), and, with
+ * RFBA_CHECKS=1 in the environment, RFBA_ERR_CUDA for an out-of-range index.
+ * Calls with host pointers report these themselves before they return;
+ * device-pointer calls are asynchronous and report through this function. */
+int rfba_ctx_check(rfba_ctx* ctx);
+
 /* Measurement hooks: CUDA-event durations of the last call's kernels, taken on
  * the stream they were launched on (enable first), and the number of kernels
  * the context has launched. */

@@ -46,6 +46,9 @@ static bool checks_enabled() {
     return v == 1;
 }
 
+static int test_tma_stall();
+static int device_status(rfba_ctx* ctx, cudaStream_t st, const char* what);
+
 static bool verbose() {
     static int v = -1;
     if (v < 0) {
@@ -212,6 +215,9 @@ static int ctx_init(rfba_ctx* c, int device, size_t budget) {
         budget = fr / 4;
     }
     c->budget = budget;
+    // device-side status word, zero until a kernel records a failure
+    if (int s = c->errw.ensure(256, "status word")) return s;
+    RFBA_CUDA(cudaMemset(c->errw.p, 0, 256), "status word clear");
     return RFBA_OK;
 }
 
@@ -509,6 +515,7 @@ static int enqueue_passes(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void
         RadParams rp = fill_rad_params(ctx, cfg, in_dev, dims, cz_for_mag(cfg.mag[2]), ps.ty);
         rp.tma_bx = radiality_tma_box_x(rp, dtype == RFBA_U16);
         rp.err = static_cast<unsigned long long*>(ctx->errw.p);
+        rp.test_skip_copy = test_tma_stall();
         rp.blocks = dblocks + pp.b0;
         rp.tiles = dtiles + pp.t0;
         rp.ntiles = (int)(pp.t1 - pp.t0);
@@ -650,6 +657,11 @@ static bool env_on(const char* name, bool dflt) {
     if (!e || !*e) return dflt;
     return !(e[0] == '0' && e[1] == 0);
 }
+
+// Failure-detection test hook (RFBA_TEST_TMA_STALL=1): the radiality kernel
+// leaves out the first input copy request of every work item, so its bounded
+// staging wait gives up and the call reports RFBA_ERR_TIMEOUT. Read per call.
+static int test_tma_stall() { return env_on("RFBA_TEST_TMA_STALL", false) ? 1 : 0; }
 
 // Calls below this many voxel-volumes keep the default schedule (RFBA_TUNE_MIN overrides).
 static long long tune_min_work() {
@@ -813,6 +825,8 @@ static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, con
             key_put(&gkey, &out_elems, 1);
             key_put(&gkey, &flags, 1);
             key_put(&gkey, &zero_out, 1);
+            const int stall = test_tma_stall();
+            key_put(&gkey, &stall, 1);
             key_put(&gkey, blocks, (size_t)nblocks);
             const bool host = flags == RFBA_HOST_PTRS;
             auto deps_now = [&]() {
@@ -893,7 +907,7 @@ static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, con
             account(ctx, gp->ps);
             ctx->last_graph = 1;
             if (ctx->timing && (s = collect_timing(ctx, gp->ps, gp->evs))) return s;
-            if (host) RFBA_CUDA(cudaStreamSynchronize(st), "synchronize");
+            if (host) return device_status(ctx, st, "forward");
             return RFBA_OK;
         }
         const void* in_dev = in;
@@ -911,7 +925,7 @@ static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, con
         if ((s = run_device(ctx, *cfg, in_dev, dtype, dims, all, out_dev, st, tune))) return s;
         if (flags == RFBA_HOST_PTRS) {
             RFBA_CUDA(cudaMemcpyAsync(out, out_dev, (size_t)out_elems * 4, cudaMemcpyDeviceToHost, st), "output copy");
-            RFBA_CUDA(cudaStreamSynchronize(st), "synchronize");
+            return device_status(ctx, st, "forward");
         }
         return RFBA_OK;
     }
@@ -930,7 +944,7 @@ static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, con
     if ((s = run_device(ctx, *cfg, in_dev, dtype, dims, all, out_dev, st))) return s;
     if (flags == RFBA_HOST_PTRS) {
         RFBA_CUDA(cudaMemcpyAsync(out, out_dev, (size_t)out_elems * 4, cudaMemcpyDeviceToHost, st), "output copy");
-        RFBA_CUDA(cudaStreamSynchronize(st), "synchronize");
+        return device_status(ctx, st, "forward");
     }
     return RFBA_OK;
 }
@@ -963,19 +977,39 @@ static int apply_drift(rfba_ctx* ctx, const float* in, const float* shifts, cons
     return RFBA_OK;
 }
 
+// The device status word: 0, or the first failure a kernel recorded, with the
+// site in the top byte and the work item or global index below. Site 0x54 is
+// the radiality kernel's bounded input-staging wait (a copy that did not land
+// within about a second); the other sites are the RFBA_CHECKS index checks.
+static int decode_status(unsigned long long w, const char* what) {
+    if (!w) return RFBA_OK;
+    char buf[200];
+    if ((w >> 56) == 0x54) {
+        std::snprintf(buf, sizeof buf,
+                      "%s: a bounded device wait gave up (the input staging copy of work item %llu did not land)",
+                      what, w & 0x00ffffffffffffffull);
+        set_error(buf);
+        return RFBA_ERR_TIMEOUT;
+    }
+    std::snprintf(buf, sizeof buf, "%s: out-of-range global index %llu at check site %llu", what,
+                  w & 0x00ffffffffffffffull, w >> 56);
+    set_error(buf);
+    return RFBA_ERR_CUDA;
+}
+
+// Wait for stream st, read the status word, clear it when set.
+static int device_status(rfba_ctx* ctx, cudaStream_t st, const char* what) {
+    if (!ctx->errw.p) return RFBA_OK;
+    unsigned long long w = 0;
+    RFBA_CUDA(cudaMemcpyAsync(&w, ctx->errw.p, 8, cudaMemcpyDeviceToHost, st), "status word read");
+    RFBA_CUDA(cudaStreamSynchronize(st), "synchronize");
+    if (w) RFBA_CUDA(cudaMemsetAsync(ctx->errw.p, 0, 8, st), "status word clear");
+    return decode_status(w, what);
+}
+
 static int read_checks(rfba_ctx* ctx, cudaStream_t st, const char* what) {
     if (!checks_enabled() || !ctx->errw.p) return RFBA_OK;
-    unsigned long long w = 0;
-    RFBA_CUDA(cudaMemcpyAsync(&w, ctx->errw.p, 8, cudaMemcpyDeviceToHost, st), "check word read");
-    RFBA_CUDA(cudaStreamSynchronize(st), "check word sync");
-    if (w) {
-        char buf[160];
-        std::snprintf(buf, sizeof buf, "%s: out-of-range global index %llu at check site %llu", what,
-                      w & 0x00ffffffffffffffull, w >> 56);
-        set_error(buf);
-        return RFBA_ERR_CUDA;
-    }
-    return RFBA_OK;
+    return device_status(ctx, st, what);
 }
 
 static int forward_shifted_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* in, const float* shifts,
@@ -1207,6 +1241,16 @@ int rfba_srrf_backward(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* 
     return backward_locked(ctx, cfg, in, shifts, dims, dL_dmap, dL_din, dL_dshift, st);
 }
 
+int rfba_ctx_check(rfba_ctx* c) {
+    if (!c) {
+        set_error("null context");
+        return RFBA_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(c->mu);
+    RFBA_CUDA(cudaSetDevice(c->device), "cudaSetDevice");
+    return device_status(c, c->have_last ? c->last_stream : c->stream, "device work");
+}
+
 int rfba_ctx_last_backward_ms(rfba_ctx* c, double* ms) {
     if (!c || !ms) return RFBA_ERR_INVALID;
     *ms = c->last_backward_ms;
@@ -1323,6 +1367,8 @@ int rfba_srrf_seed_spots(rfba_ctx* ctx, const float* map, const int map_dims[3],
         RFBA_CUDA(cudaMemcpyAsync(xyz, dxyz, (size_t)num_spots * 12, cudaMemcpyDeviceToHost, st), "spots copy");
     RFBA_CUDA(cudaStreamSynchronize(st), "synchronize");
     if (ew) {
+        // reported here, so cleared: the status word carries unreported failures only
+        RFBA_CUDA(cudaMemsetAsync(ctx->errw.p, 0, 8, st), "check word clear");
         set_error("a candidate voxel lies outside the map (magnified voxel index " +
                   std::to_string((long long)(ew & 0x00ffffffffffffffull)) + ")");
         return RFBA_ERR_INVALID;

@@ -92,10 +92,22 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait for the staging phase; false after the iteration limit.
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Bounded wait for the staging phase: false once about a second of wall time
+// (%globaltimer) has passed without the phase completing, whatever the time a
+// single try_wait suspends for; an iteration cap backs the clock up.
+constexpr unsigned long long kWaitLimitNs = 1000000000ull;
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
-    for (int i = 0; i < (1 << 22); ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = global_ns();
+    for (int i = 1; i < (1 << 26); ++i) {
         if (mbar_try_wait(bar, parity)) return true;
+        if ((i & 15) == 0 && global_ns() - t0 > kWaitLimitNs) return false;
+    }
     return false;
 }
 
@@ -291,7 +303,9 @@ __global__ void __launch_bounds__(WIDE ? kMaxThreads : 128, WIDE ? 2 : 3)
         };
         if (use_tma && tid == 0) {
             fence_proxy_async();  // the previous item's generic reads of the staging area come first
-            issue(t0);
+            // failure-detection test hook: without the request the wait below
+            // runs out, the CTA records the timeout and leaves
+            if (!p.test_skip_copy) issue(t0);
         }
         for (int t = t0; t < t1; ++t) {
             const long long sbase = B.stack_off + (long long)t * V;

@@ -115,6 +115,9 @@ struct RadParams {
     int tma_bx;
     int use_tma;
     unsigned long long* err;  // bounded-wait failures (may be null)
+    // failure-detection test (RFBA_TEST_TMA_STALL): the first copy request of
+    // every work item is left out, so the bounded staging wait gives up
+    int test_skip_copy;
 };
 
 // Temporal reduction parameters.

@@ -141,6 +141,7 @@ def lib():
         L.rfba_srrf_forward_shifted.argtypes = [vp, cp, vp, vp, ip, vp, vp]
         L.rfba_srrf_backward.argtypes = [vp, cp, vp, vp, ip, vp, vp, vp, vp]
         L.rfba_ctx_last_backward_ms.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
+        L.rfba_ctx_check.argtypes = [vp]
         L.SRRFGradientCalc.argtypes = [fp, ip, fp]
         L.SRRFGetMag.argtypes = []
         L.SRRFGradientCalcGPU.argtypes = [fp, ip, fp, ctypes.POINTER(SRRFConf)]
@@ -470,6 +471,12 @@ class Context:
                                         ctypes.c_void_p(dL_dmap.data_ptr()), ctypes.c_void_p(din.data_ptr()), dsp,
                                         st))
         return din, dshift
+
+    def check(self):
+        """Wait for this context's queued work and raise RfbaError for a failure its
+        kernels recorded (a bounded device wait that gave up: RFBA_ERR_TIMEOUT).
+        Device-tensor calls are asynchronous and report only through this."""
+        _check(lib().rfba_ctx_check(self.h))
 
     def last_backward_ms(self) -> float:
         v = ctypes.c_double()
