@@ -359,7 +359,7 @@ def measure_diff(ctx, steps: int, iters: int = 20, volumes=None) -> dict:
     (ITC 0); objective L = -||map||_2. Times forward and forward+adjoint with CUDA
     events, then runs gradient descent on L over the 60 x 3 shifts."""
     import torch
-    from rfba_gb300 import srrf, synth
+    from rfba_gb300 import drift, srrf, synth
     x, scene = synth.workload("diff", n_vol=volumes)
     cfg = srrf.Config.make(mag=2, method=3, itc=0, trac_order=2, gradient_smooth=1, main_range=1, x_range=1,
                            y_range=1, z_range=1)
@@ -369,13 +369,7 @@ def measure_diff(ctx, steps: int, iters: int = 20, volumes=None) -> dict:
     stream = torch.cuda.current_stream()
     units = x.shape[1] * x.shape[2] * x.shape[3] * 8 * T
 
-    def objective(m):
-        f = torch.nan_to_num(m, nan=0.0).double()
-        return -torch.sqrt((f * f).sum())
-
-    def grad_map(m):
-        f = torch.nan_to_num(m, nan=0.0)
-        return torch.where(torch.isnan(m), torch.zeros_like(m), -f / torch.sqrt((f.double() ** 2).sum()).float())
+    objective, grad_map = drift.objective, drift.grad_map
 
     m = ctx.forward_shifted(cfg, xd, sh, stream=stream.cuda_stream)
     g = grad_map(m)
@@ -411,21 +405,13 @@ def measure_diff(ctx, steps: int, iters: int = 20, volumes=None) -> dict:
     rms0 = rms(sh)
     L0 = float(objective(ctx.forward_shifted(cfg, xd, sh)))
     Lt = float(objective(ctx.forward_shifted(cfg, xd, truth - truth.mean(0, keepdim=True) + 0.5)))
-    lr, b1, b2 = 0.03, 0.9, 0.999
-    mom = torch.zeros_like(sh)
-    var = torch.zeros_like(sh)
     t0 = time.perf_counter()
-    for it in range(iters):
-        m = ctx.forward_shifted(cfg, xd, sh, out=m, stream=stream.cuda_stream)
-        _, gs = ctx.backward(cfg, xd, sh, grad_map(m), stream=stream.cuda_stream)
-        mom = b1 * mom + (1 - b1) * gs
-        var = b2 * var + (1 - b2) * gs * gs
-        mh = mom / (1 - b1 ** (it + 1))
-        vh = var / (1 - b2 ** (it + 1))
-        sh = sh - lr * mh / (torch.sqrt(vh) + 1e-12)
+    state, m = drift.refine_drift(ctx, cfg, xd, iters, start=np.full((T, 3), 0.5, np.float32), lr=0.03,
+                                  stream=stream.cuda_stream)
     torch.cuda.synchronize()
-    it_ms = (time.perf_counter() - t0) / iters * 1e3
-    L1 = float(objective(ctx.forward_shifted(cfg, xd, sh)))
+    it_ms = (time.perf_counter() - t0) / max(iters, 1) * 1e3  # includes the final forward
+    sh = torch.from_numpy(state.shifts).cuda()
+    L1 = float(objective(m))
     return {"workload": "diff: 60 x 64^3 f32 with random-walk drift, mag 2, TRAC-2 ITC0, L = -||map||",
             "voxel_volumes": units, "forward_ms": fwd_ms, "forward_adjoint_ms": fwdadj_ms,
             "fwd_adj_over_fwd": fwdadj_ms / fwd_ms, "refine_iterations": iters, "refine_ms_per_iteration": it_ms,
@@ -444,7 +430,7 @@ def measure_large(ctx, iters: int = 20, volumes=None) -> dict:
     context's scratch budget, every slice with all volumes (the input, 3.4 GB,
     stays resident)."""
     import torch
-    from rfba_gb300 import srrf, synth
+    from rfba_gb300 import drift, srrf, synth
     w = dict(synth.WORKLOADS["large"])
     T = volumes or w["n_vol"]
     seed = 1234 + w["index"]
@@ -459,13 +445,7 @@ def measure_large(ctx, iters: int = 20, volumes=None) -> dict:
     units = xd.shape[1] * xd.shape[2] * xd.shape[3] * 32 * T
     stream = torch.cuda.current_stream()
 
-    def objective(m):
-        f = torch.nan_to_num(m, nan=0.0).double()
-        return -torch.sqrt((f * f).sum())
-
-    def grad_map(m):
-        f = torch.nan_to_num(m, nan=0.0)
-        return torch.where(torch.isnan(m), torch.zeros_like(m), -f / torch.sqrt((f.double() ** 2).sum()).float())
+    objective, grad_map = drift.objective, drift.grad_map
 
     truth = -torch.from_numpy(scene.drift.astype(np.float32)).cuda()
 
@@ -485,19 +465,13 @@ def measure_large(ctx, iters: int = 20, volumes=None) -> dict:
     fwd_ms, bwd_ms = e0.elapsed_time(e1), e1.elapsed_time(e2)
     rms0 = rms(sh)
     L0 = float(objective(m))
-    lr, b1, b2 = 0.03, 0.9, 0.999
-    mom = torch.zeros_like(sh)
-    var = torch.zeros_like(sh)
+    del m
     t0 = time.perf_counter()
-    for it in range(iters):
-        m = ctx.forward_shifted(cfg, xd, sh, out=m, stream=stream.cuda_stream)
-        _, gs = ctx.backward(cfg, xd, sh, grad_map(m), stream=stream.cuda_stream)
-        mom = b1 * mom + (1 - b1) * gs
-        var = b2 * var + (1 - b2) * gs * gs
-        sh = sh - lr * (mom / (1 - b1 ** (it + 1))) / (torch.sqrt(var / (1 - b2 ** (it + 1))) + 1e-12)
-    m = ctx.forward_shifted(cfg, xd, sh, out=m, stream=stream.cuda_stream)
+    state, m = drift.refine_drift(ctx, cfg, xd, iters, start=np.full((T, 3), 0.5, np.float32), lr=0.03,
+                                  stream=stream.cuda_stream)
     torch.cuda.synchronize()
     wall_s = time.perf_counter() - t0
+    sh = torch.from_numpy(state.shifts).cuda()
     return {"workload": f"large: {T} x 256x256x128 u16, 8000 filament emitters, drift 0.1/volume, mag 4x4x2, "
                         "TRAC-4 ITC0, L = -||map||, Adam on shifts from +0.5",
             "voxel_volumes": units, "render_s": render_s, "forward_ms": fwd_ms, "backward_ms": bwd_ms,
