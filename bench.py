@@ -649,6 +649,7 @@ def run_gpu(args):
         pass
     sm_max = float(peaks.get("sm_max_mhz", 2070.0))
     peak = fp32_peak_tflops(props.multi_processor_count, sm_max)
+    peak_fma = srrf.probe_fp32_fma_peak(local)
     fl = algorithmic_flops_per_voxel_volume(cfg)
     rad_avg_ms = statistics.mean(rad_ms) if rad_ms else float("nan")
     achieved = fl["separable"] * units_per_step / (rad_avg_ms / 1e3) / 1e12
@@ -677,7 +678,10 @@ def run_gpu(args):
                      "kernel": "radiality_kernel<MZ=2, CZ=8, uint16, 128 threads>", "kernel_ms": rad_avg_ms,
                      "flops_per_voxel_volume": fl["separable"],
                      "peak_note": f"nominal FP32 FMA peak {props.multi_processor_count} SMs x 128 x 2 at the "
-                                  f"measured max SM clock {sm_max:.0f} MHz"},
+                                  f"measured max SM clock {sm_max:.0f} MHz",
+                     "peak_measured_fma": peak_fma, "frac_of_measured_fma": achieved / peak_fma if peak_fma else None,
+                     "peak_measured_note": "FP32 FMA chains on every SM (rfba_probe_fp32_fma_peak), measured in "
+                                           "this run"},
         "direct_equivalent_tflops": fl["direct_distinct"] * units_per_step / (rad_avg_ms / 1e3) / 1e12,
     }
     if rank == 0 and not args.no_extras:

@@ -217,6 +217,11 @@ int rfba_srrf_plan_info(const rfba_srrf_config* cfg, int* npoints, int* npairs, 
  * device-pointer calls are asynchronous and report through this function. */
 int rfba_ctx_check(rfba_ctx* ctx);
 
+/* Measured FP32 FMA throughput of a device in TFLOP/s (a short probe kernel of
+ * independent FMA chains on every SM, about 20 ms): the measured ceiling for the
+ * radiality kernel's roofline. No counterpart in the reference (measurement). */
+int rfba_probe_fp32_fma_peak(int device, double* tflops);
+
 /* Measurement hooks: CUDA-event durations of the last call's kernels, taken on
  * the stream they were launched on (enable first), and the number of kernels
  * the context has launched. */

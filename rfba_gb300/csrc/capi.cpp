@@ -1241,6 +1241,17 @@ int rfba_srrf_backward(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* 
     return backward_locked(ctx, cfg, in, shifts, dims, dL_dmap, dL_din, dL_dshift, st);
 }
 
+int rfba_probe_fp32_fma_peak(int device, double* tflops) {
+    if (!tflops) {
+        set_error("null argument");
+        return RFBA_ERR_INVALID;
+    }
+    *tflops = 0.0;
+    const int e = probe_fp32_fma(device, tflops);
+    if (e) return cuda_fail((cudaError_t)e, "FP32 probe");
+    return RFBA_OK;
+}
+
 int rfba_ctx_check(rfba_ctx* c) {
     if (!c) {
         set_error("null context");

@@ -184,4 +184,7 @@ int fine_window_int(int mag, int dim, int* lo, int* hi);
 
 void set_error(const std::string& msg);
 
+// FP32 FMA throughput probe (probe.cu): best of three timed launches, TFLOP/s.
+int probe_fp32_fma(int device, double* tflops);
+
 }  // namespace rfba

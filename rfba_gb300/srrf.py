@@ -142,6 +142,7 @@ def lib():
         L.rfba_srrf_backward.argtypes = [vp, cp, vp, vp, ip, vp, vp, vp, vp]
         L.rfba_ctx_last_backward_ms.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
         L.rfba_ctx_check.argtypes = [vp]
+        L.rfba_probe_fp32_fma_peak.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
         L.SRRFGradientCalc.argtypes = [fp, ip, fp]
         L.SRRFGetMag.argtypes = []
         L.SRRFGradientCalcGPU.argtypes = [fp, ip, fp, ctypes.POINTER(SRRFConf)]
@@ -205,6 +206,13 @@ def plan_info(cfg: "Config") -> dict:
     v = [ctypes.c_int() for _ in range(4)]
     _check(lib().rfba_srrf_plan_info(ctypes.byref(cfg), *[ctypes.byref(x) for x in v]))
     return {"points": v[0].value, "pairs": v[1].value, "xvalues": v[2].value, "raw": v[3].value}
+
+
+def probe_fp32_fma_peak(device: int = 0) -> float:
+    """Measured FP32 FMA throughput of the device, TFLOP/s."""
+    v = ctypes.c_double()
+    _check(lib().rfba_probe_fp32_fma_peak(device, ctypes.byref(v)))
+    return v.value
 
 
 def flops_per_voxel_volume(cfg: "Config") -> float:
