@@ -108,3 +108,15 @@ def test_large_trac4_20_volumes(ctx, oracle_mod):
     _check_regions(got, x.astype(np.float32), oracle_mod, kw,
                    [((16, 16, 8), (24, 24, 14)), ((510, 510, 126), (518, 518, 132)),
                     ((1000, 1004, 240), (1008, 1012, 246))], 1e-4, "large 20 x 256x256x128, mag 4x4x2, TRAC-4")
+
+
+def test_mid_trac2_itc1_reduced_t(ctx, oracle_mod):
+    """The shipped INI's temporal setting (TRAC-2 with integrated lag times) at
+    the mid configuration's spatial size, 24 volumes."""
+    from rfba_gb300.srrf import Config
+    x, _ = _workload("mid", n_vol=24)
+    kw = dict(mag=(4, 4, 2), method=3, itc=1, trac_order=2, **SMOOTH)
+    got = ctx.forward(Config.make(**kw), x)
+    _check_regions(got, x.astype(np.float32), oracle_mod, kw,
+                   [((8, 8, 4), (20, 20, 10)), ((250, 250, 60), (262, 262, 66)), ((490, 495, 118), (502, 507, 124))],
+                   1e-4, "mid 24 x 128x128x64, mag 4x4x2, TRAC-2 ITC 1")
