@@ -139,3 +139,41 @@ def test_backward_in_slices_matches_resident(ctx, oracle_mod):
                                                                       atol=0)
     assert rel_linf(din2, din) < 1e-5
     assert rel_linf(dsh2, dsh) < 1e-5
+
+
+def _random_adjoint_case(i):
+    rng = np.random.default_rng(3000 + i)
+    mag = tuple(int(v) for v in rng.integers(1, 5, size=3))
+    method = int(rng.choice([1, 3]))
+    kw = dict(mag=mag, method=method, itc=0, trac_order=int(rng.integers(2, 5)),
+              gradient_smooth=int(rng.integers(0, 2)), main_range=1, x_range=int(rng.integers(0, 2)),
+              y_range=int(rng.integers(0, 2)), z_range=int(rng.integers(0, 2)),
+              axes_in_ring=int(rng.integers(3, 7)), ring_radius=float(rng.choice([0.4, 0.5, 0.7])),
+              renormalize=int(rng.integers(0, 2)), remove_con=int(rng.integers(0, 2)),
+              intensity_w=int(rng.integers(0, 2)))
+    kw["ring_radius"] = min(kw["ring_radius"], 0.45 * (1 + min(mag)))
+    shape = (int(rng.integers(5, 9)),) + tuple(int(v) for v in rng.integers(7, 11, size=3))
+    return kw, shape
+
+
+@pytest.mark.parametrize("i", range(8))
+def test_random_adjoint_matches_fp64_adjoint(ctx, oracle_mod, i):
+    """Seeded random configurations (per-axis magnification 1-4, TRA or TRAC-2/3/4,
+    ranges, smoothing, ring, renormalisation, positivity, intensity weighting),
+    with drift, against the oracle's FP64 adjoint."""
+    from rfba_gb300 import srrf
+    O = oracle_mod
+    kw, shape = _random_adjoint_case(i)
+    cfg = srrf.Config.make(**kw)
+    oc = O.make_conf(**kw)
+    x, sh = _case(500 + i, *shape, drift=0.25)
+    m, din, dsh = _gpu(ctx, cfg, x, sh)
+    mo = O.forward_shifted(x, oc, sh)
+    assert_parity(m, mo, 1e-4, f"random {i} forward")
+    if not np.isfinite(mo).any():
+        pytest.skip("volume smaller than the interpolation window at this magnification")
+    _, din_o, dsh_o = O.adjoint(x, oc, _gmap(mo), sh)
+    e_in, e_sh = rel_linf(din, din_o), rel_linf(dsh, dsh_o)
+    msg = f"[adjoint] random {i} {kw} {shape}: dL/dI {e_in:.2e}, dL/dshift {e_sh:.2e}"
+    assert e_in < 2e-4 and e_sh < 2e-4, msg
+    print(msg)
