@@ -207,6 +207,37 @@ int rfba_blocks_dosplit(const rfba_srrf_config* cfg, const int dims[4], const in
  * distinct x values, and the raw sample count. Any pointer may be NULL. */
 int rfba_srrf_plan_info(const rfba_srrf_config* cfg, int* npoints, int* npairs, int* nxvalues, int* nraw);
 
+/* ---- 3B spot likelihood (the localisation step downstream of the SRRF map) --- */
+
+/* The model of RFBA's 3B step for one spot: a three-state chain (0 spot on,
+ * 1 off, 2 bleached) with transition matrix A (row-major, [from][to]) and
+ * initial probabilities pi (RFBA Main/multispot5.cfg:15-16), Gaussian pixel
+ * noise of the given variance on the normalised intensities, the spot's z
+ * scale (multispot5_headless.cc:180-181), and log-normal priors on brightness
+ * and blur (storm.h:417-434). */
+typedef struct rfba_3b_model {
+    double A[9];
+    double pi[3];
+    double variance;
+    double z_factor;
+    double mu_brightness, sigma_brightness;
+    double mu_blur, sigma_blur;
+} rfba_3b_model;
+
+/* SpotNegProbabilityDiffWithSampledBackground::operator() (RFBA Main/
+ * multispot5.cc:616-664): the derivative of the negative log probability of
+ * one spot (brightness, blur, x, y, z) with respect to its parameters, averaged
+ * over S samples of the other spots' intensities, the function 3B's
+ * conjugate-gradient spot optimiser evaluates. sample_bg [S][F][P] and
+ * pixel_intensities [F][P] are doubles, pixels [P][3] the mask voxels (x, y, z);
+ * host or device memory (ptr_flags). spot, out[5] and log_prob[S] (each
+ * sample's log probability; may be NULL) are host memory; the call returns
+ * when out is written. spot[0] <= 0 or spot[1] <= 0 gives NaN, as the
+ * reference does. FP64 throughout. */
+int rfba_3b_spot_gradient(rfba_ctx* ctx, const rfba_3b_model* model, const double* sample_bg,
+                          const double* pixel_intensities, const int* pixels, int S, int F, int P,
+                          const double spot[5], double out[5], double* log_prob, int ptr_flags, void* stream);
+
 /* Device-side failure check. No counterpart in the reference (GradientCalc.cpp
  * and kernel.cu check no CUDA status; every call returns 0). Waits for the
  * work the context last enqueued and reports failures its kernels recorded

@@ -35,3 +35,9 @@ g++ -O2 -std=c++17 -ffp-contract=off -fno-fast-math -fopenmp -fPIC -shared -w "-
   "$tmp/kernel_host.cpp" "$src/GradientCalc.cpp" "$here/refshim/ref_launch.cpp" \
   -o "$out/libsrrf_ref_host.so"
 echo "build_ref: built $out/libsrrf_ref_host.so"
+# The 3B spot-gradient pieces (forward_algorithm.h, spot_with_background.hh,
+# storm.h with the vendored TooN and CVD headers) through oracle/refshim/ref3b_harness.cpp.
+main="$ref/RFBA Main"
+g++ -O2 -std=c++11 -ffp-contract=off -fno-fast-math -fPIC -shared -w \
+  -I "$main/include" -I "$main" "$here/refshim/ref3b_harness.cpp" -o "$out/libref3b_host.so"
+echo "build_ref: built $out/libref3b_host.so"

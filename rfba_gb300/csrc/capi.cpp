@@ -16,6 +16,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <limits>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -197,6 +198,8 @@ struct rfba_ctx {
     std::vector<std::unique_ptr<rfba::GraphPlan>> graphs;  // most recent first
     // spot seeding scratch
     rfba::DevBuf seed_w, seed_sums, seed_carry, seed_map, seed_vox, seed_xyz;
+    // 3B spot-gradient scratch
+    rfba::DevBuf tb_val, tb_der, tb_em, tb_res, tb_par, tb_bg, tb_pix, tb_pixels;
     int last_ty = 0, last_order = 0, last_graph = 0, last_tuned = 0;
 };
 
@@ -1241,6 +1244,81 @@ int rfba_srrf_backward(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* 
     return backward_locked(ctx, cfg, in, shifts, dims, dL_dmap, dL_din, dL_dshift, st);
 }
 
+// SpotNegProbabilityDiffWithSampledBackground::operator() (multispot5.cc:616-664)
+int rfba_3b_spot_gradient(rfba_ctx* ctx, const rfba_3b_model* m, const double* sample_bg,
+                          const double* pixel_intensities, const int* pixels, int S, int F, int P, const double spot[5],
+                          double out[5], double* log_prob, int ptr_flags, void* stream) {
+    if (!ctx || !m || !sample_bg || !pixel_intensities || !pixels || !spot || !out) {
+        set_error("null argument");
+        return RFBA_ERR_INVALID;
+    }
+    if (S < 1 || F < 1 || P < 1 || (long long)S * F >= (1LL << 31) || !(m->variance > 0) || m->z_factor == 0) {
+        set_error("bad sizes or model (S, F, P >= 1, S*F < 2^31, variance > 0, z_factor != 0)");
+        return RFBA_ERR_INVALID;
+    }
+    if (ptr_flags != RFBA_HOST_PTRS && ptr_flags != RFBA_DEVICE_PTRS) {
+        set_error("ptr_flags must be RFBA_HOST_PTRS or RFBA_DEVICE_PTRS");
+        return RFBA_ERR_INVALID;
+    }
+    if (spot[0] <= 0 || spot[1] <= 0) {  // multispot5.cc:618-619
+        for (int n = 0; n < 5; ++n) out[n] = std::numeric_limits<double>::quiet_NaN();
+        return RFBA_OK;
+    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int s;
+    if ((s = order_streams(ctx, st))) return s;
+    const size_t nbg = (size_t)S * F * P, npix = (size_t)F * P;
+    if ((s = ctx->tb_val.ensure((size_t)P * 8, "3B spot table")) || (s = ctx->tb_der.ensure((size_t)P * 40, "3B spot table")) ||
+        (s = ctx->tb_em.ensure((size_t)S * F * 64, "3B emissions")) || (s = ctx->tb_res.ensure((size_t)S * 48, "3B results")) ||
+        (s = ctx->tb_par.ensure(17 * 8, "3B parameters")))
+        return s;
+    const double* dbg = sample_bg;
+    const double* dpix = pixel_intensities;
+    const int* dpixels = pixels;
+    if (ptr_flags == RFBA_HOST_PTRS) {
+        if ((s = ctx->tb_bg.ensure(nbg * 8, "3B samples")) || (s = ctx->tb_pix.ensure(npix * 8, "3B data")) ||
+            (s = ctx->tb_pixels.ensure((size_t)P * 12, "3B mask")))
+            return s;
+        RFBA_CUDA(cudaMemcpyAsync(ctx->tb_bg.p, sample_bg, nbg * 8, cudaMemcpyHostToDevice, st), "samples copy");
+        RFBA_CUDA(cudaMemcpyAsync(ctx->tb_pix.p, pixel_intensities, npix * 8, cudaMemcpyHostToDevice, st), "data copy");
+        RFBA_CUDA(cudaMemcpyAsync(ctx->tb_pixels.p, pixels, (size_t)P * 12, cudaMemcpyHostToDevice, st), "mask copy");
+        dbg = static_cast<const double*>(ctx->tb_bg.p);
+        dpix = static_cast<const double*>(ctx->tb_pix.p);
+        dpixels = static_cast<const int*>(ctx->tb_pixels.p);
+    }
+    // parameters: spot, ln A, ln pi with the reference's ln(0) = -1e100 (forward_algorithm.h:34-40)
+    auto ln0 = [](double x) { return x == 0 ? -1e100 : std::log(x); };
+    double par[17];
+    for (int n = 0; n < 5; ++n) par[n] = spot[n];
+    for (int n = 0; n < 9; ++n) par[5 + n] = ln0(m->A[n]);
+    for (int n = 0; n < 3; ++n) par[14 + n] = ln0(m->pi[n]);
+    RFBA_CUDA(cudaMemcpyAsync(ctx->tb_par.p, par, sizeof par, cudaMemcpyHostToDevice, st), "parameter upload");
+    const unsigned int n_pix = (unsigned int)P;
+    const double c0 = n_pix * ::log(2 * M_PI * m->variance) / 2;  // spot_with_background.hh:126-127
+    const double* dpar = static_cast<const double*>(ctx->tb_par.p);
+    int e = launch_threeb(dbg, dpix, dpixels, S, F, P, dpar, m->z_factor, m->variance, c0, dpar + 5, dpar + 14,
+                          static_cast<double*>(ctx->tb_val.p), static_cast<double*>(ctx->tb_der.p),
+                          static_cast<double*>(ctx->tb_em.p), static_cast<double*>(ctx->tb_res.p), st);
+    if (e) return cuda_fail((cudaError_t)e, "3B spot gradient launch");
+    ctx->launches += 3;
+    std::vector<double> res((size_t)S * 6);
+    RFBA_CUDA(cudaMemcpyAsync(res.data(), ctx->tb_res.p, res.size() * 8, cudaMemcpyDeviceToHost, st), "result copy");
+    RFBA_CUDA(cudaStreamSynchronize(st), "synchronize");
+    double sum[5] = {0, 0, 0, 0, 0};
+    for (int i = 0; i < S; ++i)
+        for (int n = 0; n < 5; ++n) sum[n] += res[(size_t)i * 6 + n];
+    // storm.h:431-434: derivatives of the log-normal priors on brightness and blur
+    auto dlln = [&](double x, double mu, double sg) { return -(1 + (ln0(x) - mu) / (sg * sg)) / x; };
+    const double prior[5] = {dlln(spot[0], m->mu_brightness, m->sigma_brightness),
+                             dlln(spot[1], m->mu_blur, m->sigma_blur), 0, 0, 0};
+    for (int n = 0; n < 5; ++n) out[n] = -(sum[n] / (double)S + prior[n]);
+    if (log_prob)
+        for (int i = 0; i < S; ++i) log_prob[i] = res[(size_t)i * 6 + 5];
+    return RFBA_OK;
+}
+
 int rfba_probe_fp32_fma_peak(int device, double* tflops) {
     if (!tflops) {
         set_error("null argument");
@@ -1295,7 +1373,8 @@ int rfba_ctx_destroy(rfba_ctx* c) {
     cudaSetDevice(c->device);
     for (DevBuf* b : {&c->in, &c->out, &c->rad, &c->inten, &c->blocks, &c->tiles, &c->tables, &c->counter, &c->prefix,
                       &c->shifted, &c->tmp1, &c->tmp2, &c->gS, &c->gI, &c->gin, &c->dshift, &c->ablocks, &c->atiles,
-                      &c->acounter, &c->errw, &c->seed_w, &c->seed_sums, &c->seed_carry, &c->seed_map, &c->seed_vox,
+                      &c->acounter, &c->errw, &c->tb_val, &c->tb_der, &c->tb_em, &c->tb_res, &c->tb_par, &c->tb_bg,
+                      &c->tb_pix, &c->tb_pixels, &c->seed_w, &c->seed_sums, &c->seed_carry, &c->seed_map, &c->seed_vox,
                       &c->seed_xyz})
         b->release();
     for (auto& e : c->ev)

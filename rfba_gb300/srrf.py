@@ -88,6 +88,24 @@ class Config(ctypes.Structure):
         return d
 
 
+class ThreeBModel(ctypes.Structure):
+    """rfba_3b_model: the 3B spot model (states on / off / bleached)."""
+
+    _fields_ = [("A", ctypes.c_double * 9), ("pi", ctypes.c_double * 3), ("variance", ctypes.c_double),
+                ("z_factor", ctypes.c_double), ("mu_brightness", ctypes.c_double),
+                ("sigma_brightness", ctypes.c_double), ("mu_blur", ctypes.c_double), ("sigma_blur", ctypes.c_double)]
+
+    @classmethod
+    def make(cls, A, pi, variance=1.0, z_factor=1.0, mu_brightness=3.5, sigma_brightness=1.0, mu_blur=0.252148,
+             sigma_blur=0.1) -> "ThreeBModel":
+        m = cls()
+        m.A[:] = [float(v) for v in np.asarray(A, np.float64).reshape(9)]
+        m.pi[:] = [float(v) for v in np.asarray(pi, np.float64).reshape(3)]
+        m.variance, m.z_factor = variance, z_factor
+        m.mu_brightness, m.sigma_brightness, m.mu_blur, m.sigma_blur = mu_brightness, sigma_brightness, mu_blur, sigma_blur
+        return m
+
+
 class Block(ctypes.Structure):
     """rfba_block: an independent input sub-volume and the magnified region of
     it that is computed and written."""
@@ -142,6 +160,9 @@ def lib():
         L.rfba_srrf_backward.argtypes = [vp, cp, vp, vp, ip, vp, vp, vp, vp]
         L.rfba_ctx_last_backward_ms.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
         L.rfba_ctx_check.argtypes = [vp]
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.rfba_3b_spot_gradient.argtypes = [vp, ctypes.POINTER(ThreeBModel), vp, vp, vp, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_int, dp, dp, dp, ctypes.c_int, vp]
         L.rfba_probe_fp32_fma_peak.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
         L.SRRFGradientCalc.argtypes = [fp, ip, fp]
         L.SRRFGetMag.argtypes = []
@@ -479,6 +500,30 @@ class Context:
                                         ctypes.c_void_p(dL_dmap.data_ptr()), ctypes.c_void_p(din.data_ptr()), dsp,
                                         st))
         return din, dshift
+
+    def spot_gradient_3b(self, model: ThreeBModel, sample_bg, pix, pixels, spot, stream=None):
+        """SpotNegProbabilityDiffWithSampledBackground (multispot5.cc:616-664) on the
+        GPU: returns (gradient [5], log probability per sample [S]). sample_bg
+        [S][F][P], pix [F][P] (float64) and pixels [P][3] (int32) are numpy arrays
+        (copied in) or CUDA tensors."""
+        dev = not isinstance(sample_bg, np.ndarray)
+        if dev:
+            S, F, P = (int(v) for v in sample_bg.shape)
+            ptrs = [ctypes.c_void_p(t.data_ptr()) for t in (sample_bg, pix, pixels)]
+        else:
+            sample_bg = np.ascontiguousarray(sample_bg, np.float64)
+            pix = np.ascontiguousarray(pix, np.float64)
+            pixels = np.ascontiguousarray(pixels, np.int32)
+            S, F, P = sample_bg.shape
+            ptrs = [ctypes.c_void_p(a.ctypes.data) for a in (sample_bg, pix, pixels)]
+        sp = np.ascontiguousarray(spot, np.float64)
+        out = np.zeros(5)
+        logp = np.zeros(S)
+        dp = ctypes.POINTER(ctypes.c_double)
+        _check(lib().rfba_3b_spot_gradient(self.h, ctypes.byref(model), *ptrs, S, F, P, sp.ctypes.data_as(dp),
+                                           out.ctypes.data_as(dp), logp.ctypes.data_as(dp),
+                                           RFBA_DEVICE_PTRS if dev else RFBA_HOST_PTRS, _stream_arg(stream, dev)))
+        return out, logp
 
     def check(self):
         """Wait for this context's queued work and raise RfbaError for a failure its
