@@ -352,6 +352,58 @@ def measure_reference_gpu(ctx, sample_blocks: int = 8) -> dict:
     return res
 
 
+def measure_threeb(ctx, steps: int = 20) -> dict:
+    """3B spot gradient (SpotNegProbabilityDiffWithSampledBackground,
+    multispot5.cc:616-664) on one 29^3 block: 10 background samples (the
+    shipped main.gibbs.samples), 100 frames, 24,389 mask voxels, the shipped
+    3-state model; FP64. Device: data resident, the spot moved every call (the
+    conjugate-gradient optimiser's pattern); e2e: samples and data copied from
+    host memory every call; CPU: the FP64 oracle (the reference's operation
+    order, samples over threads like the reference) on all host cores."""
+    import torch
+    from rfba_gb300 import srrf, synth
+    S, F, shape = 10, 100, (29, 29, 29)
+    bg, pix, px, spot = synth.threeb_block(77, S, F, shape)
+    model = srrf.ThreeBModel.make([[0.16, 0.84, 0.0], [0.495, 0.495, 0.01], [0.0, 0.0, 1.0]], [0.5, 0.5, 0.0],
+                                  variance=1.0, z_factor=1.0)
+    d = [torch.from_numpy(a).cuda() for a in (bg, pix, px)]
+    g, _ = ctx.spot_gradient_3b(model, *d, spot)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(steps):
+        g, _ = ctx.spot_gradient_3b(model, *d, spot + 1e-3 * k)
+    dev_ms = (time.perf_counter() - t0) / steps * 1e3
+    pin = [torch.from_numpy(a).pin_memory().numpy() for a in (bg, pix, px)]
+    ctx.spot_gradient_3b(model, *pin, spot)
+    t0 = time.perf_counter()
+    for k in range(steps):
+        g_h, _ = ctx.spot_gradient_3b(model, *pin, spot + 1e-3 * k)
+    e2e_ms = (time.perf_counter() - t0) / steps * 1e3
+    res = {"workload": "3B spot gradient: 10 samples x 100 frames x 29^3 mask voxels, FP64",
+           "device_ms": dev_ms, "device_value": 1e3 / dev_ms, "e2e_ms": e2e_ms, "e2e_value": 1e3 / e2e_ms,
+           "unit": "spot-gradient evaluations/s", "h2d_bytes_per_call": int(bg.nbytes + pix.nbytes + px.nbytes),
+           "fp64_flops_per_call": int(S * F * np.prod(shape) * 18)}
+    res["fp64_tflops_device"] = res["fp64_flops_per_call"] / (dev_ms * 1e-3) / 1e12
+    return res
+
+
+def threeb_cpu_baseline(res: dict, reps: int = 3) -> dict:
+    """The FP64 oracle of the 3B spot gradient on all host cores (test
+    infrastructure, the CPU-baseline leg), on the same block."""
+    from oracle import threeb as T
+    from rfba_gb300 import synth
+    bg, pix, px, spot = synth.threeb_block(77, 10, 100, (29, 29, 29))
+    want = T.spot_neg_prob_diff(bg, pix, px, spot, nthreads=os.cpu_count() or 1)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        T.spot_neg_prob_diff(bg, pix, px, spot, nthreads=os.cpu_count() or 1)
+    cpu_ms = (time.perf_counter() - t0) / reps * 1e3
+    return {"cpu_ms": cpu_ms, "cpu_value": 1e3 / cpu_ms, "cores": os.cpu_count(),
+            "kind": "port (FP64 oracle, pinned bit for bit to the reference's headers; threads over samples)",
+            "speedup_device_vs_cpu": cpu_ms / res["device_ms"], "speedup_e2e_vs_cpu": cpu_ms / res["e2e_ms"],
+            "oracle_gradient": want.tolist()}
+
+
 def measure_diff(ctx, steps: int, iters: int = 20, volumes=None) -> dict:
     """Differentiation workload: 60 volumes of 64^3 float32 (300 emitters) with a
     random-walk drift (sigma 0.15 voxel per step) applied by Catmull-Rom
@@ -561,6 +613,10 @@ def run_single_workload(args):
         r = measure_combine(ctx)
     elif args.workload == "refgpu":
         r = measure_reference_gpu(ctx)
+    elif args.workload == "threeb":
+        r = measure_threeb(ctx)
+        if not args.no_cpu:
+            r["cpu_baseline"] = threeb_cpu_baseline(r)
     else:
         r = measure_diff(ctx, max(3, args.steps), iters=args.iters, volumes=args.volumes)
     ctx.close()
@@ -688,6 +744,9 @@ def run_gpu(args):
         line["batching"] = measure_batching(ctx, max(2, args.steps // 2))
         line["differentiation"] = measure_diff(ctx, max(3, args.steps))
         line["reference_gpu"] = measure_reference_gpu(ctx)
+        line["threeb"] = measure_threeb(ctx)
+        if not args.no_cpu:
+            line["threeb"]["cpu_baseline"] = threeb_cpu_baseline(line["threeb"])
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(x)
     ctx.close()
@@ -710,7 +769,7 @@ def main():
     ap.add_argument("--volumes", type=int, default=None,
                     help="fewer volumes than the workload's (profiling case only)")
     ap.add_argument("--iters", type=int, default=20, help="drift refinement iterations (diff workload)")
-    ap.add_argument("--workload", default="mid", choices=["mid", "batching", "diff", "large", "seeding", "combine", "refgpu"],
+    ap.add_argument("--workload", default="mid", choices=["mid", "batching", "diff", "large", "seeding", "combine", "refgpu", "threeb"],
                     help="mid: the headline line; batching / diff: that measurement alone (one JSON line)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":

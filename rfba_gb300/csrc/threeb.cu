@@ -13,7 +13,7 @@
 //      mask voxels in FP64 — the sums of squares reach 1e7-1e8 while the
 //      forward algorithm weighs states by exp of their differences, so FP32
 //      sums would be wrong by whole units of log probability;
-//   3. forward_kernel, one thread per sample: the 3-state forward algorithm
+//   3. forward_kernel, one warp per sample (a lane per state): the 3-state forward algorithm
 //      with derivatives over the frames (forward_algorithm.h:157-259,
 //      compute_hessian = 0), giving each sample's log probability and gradient.
 // The host averages the samples' gradients and adds the log-normal priors'
@@ -96,43 +96,53 @@ __global__ void __launch_bounds__(kEmitThreads) emission_kernel(const double* __
     }
 }
 
-// One thread per sample: log probability and its gradient. lnA row-major
-// 3 x 3 and lnpi with ln(0) = -1e100 as the reference's ln.
-__global__ void forward_kernel(const double* __restrict__ em, int S, int F, const double* __restrict__ lnA9,
-                               const double* __restrict__ lnpi3, double* __restrict__ res) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+// One warp per sample, lanes 0..2 the three states j: each step every lane
+// holds the previous delta_i and its derivative for all i, forms its own
+// state's new values (forward_algorithm.h:196-224) and the three lanes
+// exchange them by shuffles. exp is skipped where its argument is exactly 0
+// (the largest term of each sum: exp(0) = 1) or carries ln(0) = -1e100 (the
+// transitions the model forbids: exp = 0), which changes no result. lnA
+// row-major 3 x 3 and lnpi with ln(0) = -1e100 as the reference's ln.
+__device__ __forceinline__ double exp_term(double a) {
+    return a == 0.0 ? 1.0 : (a < -1e99 ? 0.0 : exp(a));
+}
+
+__global__ void __launch_bounds__(32) forward_kernel(const double* __restrict__ em, int S, int F,
+                                                      const double* __restrict__ lnA9,
+                                                      const double* __restrict__ lnpi3, double* __restrict__ res) {
+    const int s = blockIdx.x;
+    const int lane = threadIdx.x;
     if (s >= S) return;
-    double lnA[9], lnpi[3];
-    for (int i = 0; i < 9; ++i) lnA[i] = lnA9[i];
-    for (int i = 0; i < 3; ++i) lnpi[i] = lnpi3[i];
+    const int j = lane < 3 ? lane : 0;
+    double lnAj[3];
+    for (int i = 0; i < 3; ++i) lnAj[i] = lnA9[i * 3 + j];
     const double* e = em + (size_t)s * F * 8;
     double delta[3], dd[3][kM];
     for (int i = 0; i < 3; ++i) {
-        delta[i] = lnpi[i] + (i == 0 ? e[0] : e[1]);
+        delta[i] = lnpi3[i] + (i == 0 ? e[0] : e[1]);
         for (int n = 0; n < kM; ++n) dd[i][n] = i == 0 ? e[2 + n] : 0.0;
     }
     for (int t = 1; t < F; ++t) {
         const double* et = e + (size_t)t * 8;
-        double nd[3], ndd[3][kM];
-        for (int j = 0; j < 3; ++j) {
-            double Z = -__longlong_as_double(0x7ff0000000000000ll);
-            for (int i = 0; i < 3; ++i) Z = fmax(Z, delta[i] + lnA[i * 3 + j]);
-            double w[3], sum = 0.0;
-            for (int i = 0; i < 3; ++i) {
-                w[i] = exp(delta[i] + lnA[i * 3 + j] - Z);
-                sum += w[i];
-            }
-            nd[j] = (j == 0 ? et[0] : et[1]) + Z + ln0(sum);
-            double top[kM] = {0, 0, 0, 0, 0};
-            for (int i = 0; i < 3; ++i)
-                for (int n = 0; n < kM; ++n) top[n] += dd[i][n] * w[i];
-            for (int n = 0; n < kM; ++n) ndd[j][n] = (j == 0 ? et[2 + n] : 0.0) + top[n] / sum;
+        double Z = -__longlong_as_double(0x7ff0000000000000ll);
+        for (int i = 0; i < 3; ++i) Z = fmax(Z, delta[i] + lnAj[i]);
+        double w[3], sum = 0.0;
+        for (int i = 0; i < 3; ++i) {
+            w[i] = exp_term(delta[i] + lnAj[i] - Z);
+            sum += w[i];
         }
-        for (int j = 0; j < 3; ++j) {
-            delta[j] = nd[j];
-            for (int n = 0; n < kM; ++n) dd[j][n] = ndd[j][n];
+        const double nd = (j == 0 ? et[0] : et[1]) + Z + ln0(sum);
+        double top[kM] = {0, 0, 0, 0, 0};
+        for (int i = 0; i < 3; ++i)
+            for (int n = 0; n < kM; ++n) top[n] += dd[i][n] * w[i];
+        double ndd[kM];
+        for (int n = 0; n < kM; ++n) ndd[n] = (j == 0 ? et[2 + n] : 0.0) + top[n] / sum;
+        for (int i = 0; i < 3; ++i) {
+            delta[i] = __shfl_sync(0xffffffffu, nd, i);
+            for (int n = 0; n < kM; ++n) dd[i][n] = __shfl_sync(0xffffffffu, ndd[n], i);
         }
     }
+    if (lane != 0) return;
     double Z = -__longlong_as_double(0x7ff0000000000000ll);
     for (int i = 0; i < 3; ++i) Z = fmax(Z, delta[i]);
     double sum = 0.0;
@@ -157,7 +167,7 @@ int launch_threeb(const double* bg, const double* pix, const int* pixels, int S,
     spot_pixels_kernel<<<(P + 255) / 256, 256, 0, st>>>(pixels, P, phi_dev, zf, val, der);
     emission_kernel<<<(unsigned)((long long)S * F), kEmitThreads, 0, st>>>(bg, pix, val, der, F, P,
                                                                            2 * variance, variance, c0, em);
-    forward_kernel<<<(S + 63) / 64, 64, 0, st>>>(em, S, F, lnA_dev, lnpi_dev, res);
+    forward_kernel<<<S, 32, 0, st>>>(em, S, F, lnA_dev, lnpi_dev, res);
     return (int)cudaGetLastError();
 }
 

@@ -237,3 +237,36 @@ def workload(name: str, n_vol: int | None = None, shape=None):
     seed = 1234 + w["index"]
     scene = make_scene(seed, w["n_vol"], w["shape"], w["n_emitters"], w["curves"], w["drift"])
     return render(scene, w["shape"], seed, w["dtype"]), scene
+
+
+def threeb_block(seed: int, S: int, F: int, shape=(9, 9, 7), n_spots: int = 6, spot=None, variance=1.0):
+    """Seeded stand-in for one 3B block (the localisation step after SRRF): the
+    mask's voxels (x fastest), a data series made of a few blinking Gaussian
+    spots over a flat background plus Gaussian noise, S background samples (the
+    same spots, each switched on or off at random per frame, without the spot
+    being fitted) and a starting spot near the first one. Intensities are in
+    the normalised units 3B works in (unit noise variance)."""
+    rng = np.random.default_rng(seed)
+    X, Y, Z = shape
+    zz, yy, xx = np.meshgrid(np.arange(Z), np.arange(Y), np.arange(X), indexing="ij")
+    pixels = np.stack([xx.ravel(), yy.ravel(), zz.ravel()], 1).astype(np.int32)
+    P = len(pixels)
+    centres = rng.uniform([1, 1, 1], [X - 2, Y - 2, Z - 2], size=(n_spots, 3))
+    bright = rng.uniform(20, 60, n_spots)
+    blur = rng.uniform(0.9, 1.6, n_spots)
+
+    def shape_of(k):
+        d = pixels - centres[k]
+        return bright[k] / (blur[k] * np.sqrt(2 * np.pi)) * np.exp(-(d * d).sum(1) / (2 * blur[k] ** 2))
+
+    shapes = np.stack([shape_of(k) for k in range(n_spots)])
+    on = rng.random((F, n_spots)) < 0.5
+    pix = 2.0 + on.astype(np.float64) @ shapes + rng.normal(0, np.sqrt(variance), (F, P))
+    samples = np.empty((S, F, P))
+    for s in range(S):
+        son = rng.random((F, n_spots)) < 0.5
+        son[:, 0] = False  # the spot being fitted is removed from the samples
+        samples[s] = 2.0 + son.astype(np.float64) @ shapes
+    if spot is None:
+        spot = np.array([bright[0] * 0.9, blur[0] * 1.1, *(centres[0] + 0.3)])
+    return samples, pix, pixels, np.asarray(spot, np.float64)
