@@ -1271,7 +1271,7 @@ int rfba_3b_spot_gradient(rfba_ctx* ctx, const rfba_3b_model* m, const double* s
     if ((s = order_streams(ctx, st))) return s;
     const size_t nbg = (size_t)S * F * P, npix = (size_t)F * P;
     if ((s = ctx->tb_val.ensure((size_t)P * 8, "3B spot table")) || (s = ctx->tb_der.ensure((size_t)P * 40, "3B spot table")) ||
-        (s = ctx->tb_em.ensure((size_t)S * F * 64, "3B emissions")) || (s = ctx->tb_res.ensure((size_t)S * 48, "3B results")) ||
+        (s = ctx->tb_em.ensure((size_t)S * F * 64, "3B emissions")) || (s = ctx->tb_res.ensure((size_t)S * 48 + 48, "3B results")) ||
         (s = ctx->tb_par.ensure(17 * 8, "3B parameters")))
         return s;
     const double* dbg = sample_bg;
@@ -1302,7 +1302,7 @@ int rfba_3b_spot_gradient(rfba_ctx* ctx, const rfba_3b_model* m, const double* s
                           static_cast<double*>(ctx->tb_val.p), static_cast<double*>(ctx->tb_der.p),
                           static_cast<double*>(ctx->tb_em.p), static_cast<double*>(ctx->tb_res.p), st);
     if (e) return cuda_fail((cudaError_t)e, "3B spot gradient launch");
-    ctx->launches += 3;
+    ctx->launches += 4;
     std::vector<double> res((size_t)S * 6);
     RFBA_CUDA(cudaMemcpyAsync(res.data(), ctx->tb_res.p, res.size() * 8, cudaMemcpyDeviceToHost, st), "result copy");
     RFBA_CUDA(cudaStreamSynchronize(st), "synchronize");

@@ -4,16 +4,17 @@
 // its parameters (brightness, blur, x, y, z), given S samples of the other
 // spots' intensities, which 3B's conjugate-gradient spot optimiser evaluates
 // over and over: SpotNegProbabilityDiffWithSampledBackground::operator()
-// (RFBA Main/multispot5.cc:616-664). Three kernels:
+// (RFBA Main/multispot5.cc:616-664). Four kernels:
 //   1. spot_pixels_kernel: the spot's intensity and its parameter derivative
 //      at every mask voxel (spot_shape_diff_position, storm.h:51-84);
-//   2. emission_kernel, one CTA per (sample, frame): the frame's log
+//   2. spot_sums_kernel: the spot's sums over the mask (sum v^2, sum der v);
+//   3. emission_kernel, one CTA per (sample, frame): the frame's log
 //      probability with the spot on and off and the derivative of the "on" one
 //      (SpotWithBackground, spot_with_background.hh:98-133), reduced over the
 //      mask voxels in FP64 — the sums of squares reach 1e7-1e8 while the
 //      forward algorithm weighs states by exp of their differences, so FP32
 //      sums would be wrong by whole units of log probability;
-//   3. forward_kernel, one warp per sample (a lane per state): the 3-state forward algorithm
+//   4. forward_kernel, one warp per state of each sample: the 3-state forward algorithm
 //      with derivatives over the frames (forward_algorithm.h:157-259,
 //      compute_hessian = 0), giving each sample's log probability and gradient.
 // The host averages the samples' gradients and adds the log-normal priors'
@@ -52,26 +53,59 @@ __global__ void spot_pixels_kernel(const int* __restrict__ pixels, int P, const 
     d[4] = k * ((x2 - phi4) * q);
 }
 
+// The spot's own sums over the mask, sum v^2 and sum der_n v (one CTA, fixed
+// order): with d = I - G, sum (d - v)^2 = sum d^2 - 2 sum d v + sum v^2 and
+// sum der_n (d - v) = sum der_n d - sum der_n v, so the per-(sample, frame)
+// pass needs 8 FP64 operations per voxel instead of 10.
+constexpr int kSumThreads = 512;
+__global__ void __launch_bounds__(kSumThreads) spot_sums_kernel(const double* __restrict__ val,
+                                                                 const double* __restrict__ der, int P,
+                                                                 double* __restrict__ sums) {
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    for (int p = threadIdx.x; p < P; p += kSumThreads) {
+        const double v = val[p];
+        acc[0] += v * v;
+#pragma unroll
+        for (int n = 0; n < kM; ++n) acc[1 + n] += der[(size_t)p * kM + n] * v;
+    }
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+        for (int o = 16; o > 0; o >>= 1) acc[i] += __shfl_down_sync(0xffffffffu, acc[i], o);
+    __shared__ double part[kSumThreads / 32][6];
+    if ((threadIdx.x & 31) == 0)
+#pragma unroll
+        for (int i = 0; i < 6; ++i) part[threadIdx.x >> 5][i] = acc[i];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t[6] = {0, 0, 0, 0, 0, 0};
+        for (int w = 0; w < kSumThreads / 32; ++w)
+#pragma unroll
+            for (int i = 0; i < 6; ++i) t[i] += part[w][i];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) sums[i] = t[i];
+    }
+}
+
 // out[(s*F + f)*8 + {0: log prob on, 1: log prob off, 2..6: d(log prob on)/d phi}]
 __global__ void __launch_bounds__(kEmitThreads) emission_kernel(const double* __restrict__ bg,
                                                                  const double* __restrict__ pix,
                                                                  const double* __restrict__ val,
-                                                                 const double* __restrict__ der, int F, int P,
+                                                                 const double* __restrict__ der,
+                                                                 const double* __restrict__ spot_sums, int F, int P,
                                                                  double twovar, double var, double c0,
                                                                  double* __restrict__ out) {
     const int sf = blockIdx.x;  // sample * F + frame
     const int f = sf % F;
     const double* G = bg + (size_t)sf * P;
     const double* I = pix + (size_t)f * P;
-    double acc[7] = {0, 0, 0, 0, 0, 0, 0};  // on, off, diff[5]
+    double acc[7] = {0, 0, 0, 0, 0, 0, 0};  // sum d v, sum d^2, sum der_n d (d = I - G)
     for (int p = threadIdx.x; p < P; p += kEmitThreads) {
         const double dI = I[p] - G[p];
-        const double e = I[p] - (G[p] + val[p]);
         acc[1] += dI * dI;
-        acc[0] += e * e;
+        acc[0] += dI * val[p];
         const double* d = der + (size_t)p * kM;
 #pragma unroll
-        for (int n = 0; n < kM; ++n) acc[2 + n] += d[n] * e;
+        for (int n = 0; n < kM; ++n) acc[2 + n] += d[n] * dI;
     }
 #pragma unroll
     for (int i = 0; i < 7; ++i)
@@ -88,32 +122,35 @@ __global__ void __launch_bounds__(kEmitThreads) emission_kernel(const double* __
 #pragma unroll
             for (int i = 0; i < 7; ++i) t[i] += part[w][i];
         double* o = out + (size_t)sf * 8;
-        o[0] = -t[0] / twovar - c0;
+        const double on = t[1] - 2.0 * t[0] + spot_sums[0];  // sum (d - v)^2
+        o[0] = -on / twovar - c0;
         o[1] = -t[1] / twovar - c0;
 #pragma unroll
-        for (int n = 0; n < kM; ++n) o[2 + n] = t[2 + n] / var;
+        for (int n = 0; n < kM; ++n) o[2 + n] = (t[2 + n] - spot_sums[1 + n]) / var;
         o[7] = 0.0;
     }
 }
 
-// One warp per sample, lanes 0..2 the three states j: each step every lane
-// holds the previous delta_i and its derivative for all i, forms its own
-// state's new values (forward_algorithm.h:196-224) and the three lanes
-// exchange them by shuffles. exp is skipped where its argument is exactly 0
-// (the largest term of each sum: exp(0) = 1) or carries ln(0) = -1e100 (the
+// One CTA per sample, one warp per state j: each step every warp holds the
+// previous delta_i and its derivative for all i, forms its own state's new
+// values (forward_algorithm.h:196-224) and the three warps exchange them
+// through shared memory. exp is skipped where its argument is exactly 0 (the
+// largest term of each sum: exp(0) = 1) or carries ln(0) = -1e100 (the
 // transitions the model forbids: exp = 0), which changes no result. lnA
 // row-major 3 x 3 and lnpi with ln(0) = -1e100 as the reference's ln.
 __device__ __forceinline__ double exp_term(double a) {
     return a == 0.0 ? 1.0 : (a < -1e99 ? 0.0 : exp(a));
 }
 
-__global__ void __launch_bounds__(32) forward_kernel(const double* __restrict__ em, int S, int F,
+__global__ void __launch_bounds__(96) forward_kernel(const double* __restrict__ em, int S, int F,
                                                       const double* __restrict__ lnA9,
                                                       const double* __restrict__ lnpi3, double* __restrict__ res) {
+    // one warp per state j; the new delta_j and its derivative go through
+    // shared memory (double-buffered, one barrier per frame)
+    __shared__ double sh[2][3][8];
     const int s = blockIdx.x;
-    const int lane = threadIdx.x;
-    if (s >= S) return;
-    const int j = lane < 3 ? lane : 0;
+    const int j = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
     double lnAj[3];
     for (int i = 0; i < 3; ++i) lnAj[i] = lnA9[i * 3 + j];
     const double* e = em + (size_t)s * F * 8;
@@ -135,14 +172,22 @@ __global__ void __launch_bounds__(32) forward_kernel(const double* __restrict__ 
         double top[kM] = {0, 0, 0, 0, 0};
         for (int i = 0; i < 3; ++i)
             for (int n = 0; n < kM; ++n) top[n] += dd[i][n] * w[i];
-        double ndd[kM];
-        for (int n = 0; n < kM; ++n) ndd[n] = (j == 0 ? et[2 + n] : 0.0) + top[n] / sum;
+        double* o = sh[t & 1][j];
+        if (lane == 0) {
+            // one reciprocal instead of five divisions (FP64 division is a long
+            // sequence here); the products differ from the quotients by an ulp
+            const double rs = 1.0 / sum;
+            o[0] = nd;
+            for (int n = 0; n < kM; ++n) o[1 + n] = (j == 0 ? et[2 + n] : 0.0) + top[n] * rs;
+        }
+        __syncthreads();
         for (int i = 0; i < 3; ++i) {
-            delta[i] = __shfl_sync(0xffffffffu, nd, i);
-            for (int n = 0; n < kM; ++n) dd[i][n] = __shfl_sync(0xffffffffu, ndd[n], i);
+            const double* q = sh[t & 1][i];
+            delta[i] = q[0];
+            for (int n = 0; n < kM; ++n) dd[i][n] = q[1 + n];
         }
     }
-    if (lane != 0) return;
+    if (threadIdx.x != 0) return;
     double Z = -__longlong_as_double(0x7ff0000000000000ll);
     for (int i = 0; i < 3; ++i) Z = fmax(Z, delta[i]);
     double sum = 0.0;
@@ -165,9 +210,11 @@ int launch_threeb(const double* bg, const double* pix, const int* pixels, int S,
                   double* val, double* der, double* em, double* res, void* stream) {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     spot_pixels_kernel<<<(P + 255) / 256, 256, 0, st>>>(pixels, P, phi_dev, zf, val, der);
-    emission_kernel<<<(unsigned)((long long)S * F), kEmitThreads, 0, st>>>(bg, pix, val, der, F, P,
+    double* sums = res + (size_t)S * 6;  // 6 doubles after the per-sample results
+    spot_sums_kernel<<<1, kSumThreads, 0, st>>>(val, der, P, sums);
+    emission_kernel<<<(unsigned)((long long)S * F), kEmitThreads, 0, st>>>(bg, pix, val, der, sums, F, P,
                                                                            2 * variance, variance, c0, em);
-    forward_kernel<<<S, 32, 0, st>>>(em, S, F, lnA_dev, lnpi_dev, res);
+    forward_kernel<<<S, 96, 0, st>>>(em, S, F, lnA_dev, lnpi_dev, res);
     return (int)cudaGetLastError();
 }
 
