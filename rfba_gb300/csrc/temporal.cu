@@ -157,7 +157,19 @@ __global__ void __launch_bounds__(256) temporal_kernel(const TemporalParams p) {
 
     // output position
     const long long nx = B.nreg[0], ny = B.nreg[1];
-    const long long x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
+    long long x, y, z;
+    if (v < 0x7fffffffLL) {
+        // 32-bit division: a 64-bit one is a long integer sequence per thread
+        const unsigned vv = (unsigned)v, ux = (unsigned)nx, uy = (unsigned)ny;
+        const unsigned q = vv / ux;
+        x = vv - q * ux;
+        y = q % uy;
+        z = q / uy;
+    } else {
+        x = v % nx;
+        y = (v / nx) % ny;
+        z = v / (nx * ny);
+    }
     p.out[B.out_offset + x * B.out_stride[0] + y * B.out_stride[1] + z * B.out_stride[2]] = result;
 }
 
