@@ -467,7 +467,9 @@ int fine_window_int(int mag, int dim, int* lo, int* hi) {
 // written once with the value the reference ends up with.
 int blocks_gradientcalc(const rfba_srrf_config& c, const int dims[4], rfba_block* out, int cap, std::string* err) {
     const int border = 2;
-    const int mag = c.mag[0];
+    // the reference has one magnification; the extended configuration's
+    // per-axis factors apply axis by axis (equal factors give the reference's blocks)
+    const int* mag = c.mag;
     int split[3];
     for (int a = 0; a < 3; ++a) {
         const int step = c.block_size[a] - 2 * border;
@@ -480,7 +482,7 @@ int blocks_gradientcalc(const rfba_srrf_config& c, const int dims[4], rfba_block
         if (num % step != 0) split[a] += 1;
         if (split[a] < 0) split[a] = 0;
     }
-    const long long W = (long long)dims[0] * mag, H = (long long)dims[1] * mag;
+    const long long W = (long long)dims[0] * mag[0], H = (long long)dims[1] * mag[1];
     int count = 0;
     for (int k = 0; k < split[2]; ++k)
         for (int j = 0; j < split[1]; ++j)
@@ -496,17 +498,18 @@ int blocks_gradientcalc(const rfba_srrf_config& c, const int dims[4], rfba_block
                     const int start = pos[a] == 0 ? 0 : pos[a] * step;
                     b.origin[a] = start;
                     b.size[a] = res;
-                    b.lo[a] = border * mag;
-                    b.hi[a] = last ? res * mag : (step + border) * mag;
-                    if (b.hi[a] > res * mag) b.hi[a] = res * mag;
+                    b.lo[a] = border * mag[a];
+                    b.hi[a] = last ? res * mag[a] : (step + border) * mag[a];
+                    if (b.hi[a] > res * mag[a]) b.hi[a] = res * mag[a];
                     if (b.hi[a] <= b.lo[a]) empty = true;
                 }
                 if (empty) continue;
                 b.out_stride[0] = 1;
                 b.out_stride[1] = W;
                 b.out_stride[2] = W * H;
-                b.out_offset = ((long long)b.origin[2] * mag + b.lo[2]) * W * H +
-                               ((long long)b.origin[1] * mag + b.lo[1]) * W + ((long long)b.origin[0] * mag + b.lo[0]);
+                b.out_offset = ((long long)b.origin[2] * mag[2] + b.lo[2]) * W * H +
+                               ((long long)b.origin[1] * mag[1] + b.lo[1]) * W +
+                               ((long long)b.origin[0] * mag[0] + b.lo[0]);
                 if (out && count < cap) out[count] = b;
                 ++count;
             }

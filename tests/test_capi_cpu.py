@@ -241,3 +241,25 @@ def test_context_without_gpu_reports_cuda_error(built_lib):
     with pytest.raises(srrf.RfbaError) as e:
         srrf.Context(0)
     assert e.value.status == -4
+
+
+def test_gradientcalc_blocks_with_per_axis_magnification(built_lib):
+    """The GradientCalc split with the extended per-axis magnification: every
+    map voxel outside the low border of 2 mag per axis is written by exactly
+    one block, and none inside it."""
+    from rfba_gb300 import srrf
+    cfg = srrf.Config.make(mag=(4, 3, 2), block_size=(16, 12, 10))
+    dims = (2, 23, 37, 41)  # T, D, H, W
+    b, n = srrf.blocks_gradientcalc(cfg, dims)
+    W, H, D = 41 * 4, 37 * 3, 23 * 2
+    cnt = np.zeros(W * H * D, np.int32)
+    for i in range(n):
+        bb = b[i]
+        nx, ny, nz = (bb.hi[a] - bb.lo[a] for a in range(3))
+        assert 0 < nx <= bb.size[0] * 4 and 0 < ny <= bb.size[1] * 3 and 0 < nz <= bb.size[2] * 2
+        zz, yy, xx = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+        idx = bb.out_offset + xx * bb.out_stride[0] + yy * bb.out_stride[1] + zz * bb.out_stride[2]
+        np.add.at(cnt, idx.ravel(), 1)
+    c = cnt.reshape(D, H, W)
+    assert (c[4:, 6:, 8:] == 1).all()
+    assert c[:4].max() == 0 and c[:, :6].max() == 0 and c[:, :, :8].max() == 0
