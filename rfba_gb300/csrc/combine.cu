@@ -153,8 +153,13 @@ __global__ void scale_kernel(const unsigned long long* __restrict__ v, long long
                              const unsigned long long* __restrict__ mx, uint16_t* __restrict__ out) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const unsigned long long vi = v[i];
+    if (vi == 0) {  // (0 / m) * 65535 rounds to 0: no FP64 division for the empty grid voxels
+        out[i] = 0;
+        return;
+    }
     const double m = (double)*mx;
-    double r = m > 0.0 ? ((double)v[i] / m) * 65535.0 : 0.0;
+    double r = m > 0.0 ? ((double)vi / m) * 65535.0 : 0.0;
     r = r >= 65535.0 ? 65535.0 : floor(r + 0.5);
     out[i] = (uint16_t)r;
 }
