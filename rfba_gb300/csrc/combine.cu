@@ -57,7 +57,42 @@ __global__ void box_y_kernel(const unsigned int* __restrict__ hist, int Xp, int 
 }
 
 // S[z][y][x] = sum over |dx| <= r of L for x in [r, X' - r - 1], else 0
-// (CombineBlock.m:103-114): one thread per (z, y) row, running sum along x.
+// (CombineBlock.m:103-114). One warp per (z, y) row, 8 rows per CTA: the row is
+// staged in shared memory with coalesced loads, then each lane runs the sum
+// along its own stretch of x.
+constexpr int kBoxRows = 8;
+__global__ void __launch_bounds__(32 * kBoxRows) box_x_warp_kernel(const unsigned char* __restrict__ L, int Xp,
+                                                                    int Yp, int Zp, int r,
+                                                                    unsigned short* __restrict__ S) {
+    extern __shared__ unsigned char srow[];  // [kBoxRows][Xp]
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long row = (long long)blockIdx.x * kBoxRows + w;
+    if (row >= (long long)Yp * Zp) return;  // whole warps only; no CTA barrier below
+    unsigned char* sr = srow + (size_t)w * Xp;
+    const unsigned char* l = L + (size_t)row * Xp;
+    for (int x = lane; x < Xp; x += 32) sr[x] = l[x];
+    __syncwarp();
+    unsigned short* o = S + (size_t)row * Xp;
+    const int chunk = (Xp + 31) / 32;
+    const int x0 = lane * chunk, x1 = min(Xp, x0 + chunk);
+    unsigned int sum = 0;
+    bool have = false;
+    for (int x = x0; x < x1; ++x) {
+        if (Xp < 2 * r + 1 || x < r || x > Xp - r - 1) {
+            o[x] = 0;
+            continue;
+        }
+        if (!have) {
+            for (int k = x - r; k <= x + r; ++k) sum += sr[k];
+            have = true;
+        } else {
+            sum += sr[x + r] - sr[x - r - 1];
+        }
+        o[x] = (unsigned short)sum;
+    }
+}
+
+// The same with one thread per row, for rows too long to stage.
 __global__ void box_x_kernel(const unsigned char* __restrict__ L, int Xp, int Yp, int Zp, int r,
                              unsigned short* __restrict__ S) {
     const long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -180,7 +215,11 @@ int launch_combine(const double* spots, long long n, int zoom, int Xp, int Yp, i
     cudaMemsetAsync(counters, 0, 3 * sizeof(unsigned long long), st);
     if (n > 0) hist_kernel<<<grid_for(n, 256), 256, 0, st>>>(spots, n, zoom, Xp, Yp, Zp, hist, counters);
     box_y_kernel<<<grid_for((long long)Xp * Zp, 256), 256, 0, st>>>(hist, Xp, Yp, Zp, r, L);
-    box_x_kernel<<<grid_for((long long)Yp * Zp, 256), 256, 0, st>>>(L, Xp, Yp, Zp, r, S);
+    if ((size_t)kBoxRows * Xp <= 48 * 1024)
+        box_x_warp_kernel<<<grid_for((long long)Yp * Zp, kBoxRows), 32 * kBoxRows, (size_t)kBoxRows * Xp, st>>>(
+            L, Xp, Yp, Zp, r, S);
+    else
+        box_x_kernel<<<grid_for((long long)Yp * Zp, 256), 256, 0, st>>>(L, Xp, Yp, Zp, r, S);
     box_z_mask_kernel<<<grid_for((long long)Xp * Yp, 256), 256, 0, st>>>(S, Xp, Yp, Zp, r, rz, thr, hist);
     compact_kernel<<<grid_for(nvox, 256), 256, 0, st>>>(hist, nvox, idx, val, counters + 1, cap);
     const size_t psf_bytes = (size_t)Kx * Ky * Kz * 2;
