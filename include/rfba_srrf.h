@@ -188,11 +188,26 @@ int rfba_srrf_forward_shifted(rfba_ctx* ctx, const rfba_srrf_config* cfg, const 
                               const int dims[4], float* out, void* stream);
 int rfba_srrf_backward(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* in, const float* shifts,
                        const int dims[4], const float* dL_dmap, float* dL_din, float* dL_dshift, void* stream);
+/* The same pair restricted to the fine region [lo, hi) of the magnified grid
+ * (x, y, z; 0 <= lo < hi <= dims * mag per axis), for splitting one series'
+ * map across processes (no counterpart in the reference). The forward writes
+ * the region packed [z][y][x] into out; the backward takes dL/dregion in that
+ * layout and writes the region's whole contribution to dL/din and dL/dshifts,
+ * so the contributions of disjoint regions that tile the map sum to
+ * rfba_srrf_backward's result. Region calls always recompute their stacks.
+ * Stream-ordered. */
+int rfba_srrf_forward_shifted_region(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* in,
+                                     const float* shifts, const int dims[4], const int lo[3], const int hi[3],
+                                     float* out, void* stream);
+int rfba_srrf_backward_region(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* in, const float* shifts,
+                              const int dims[4], const int lo[3], const int hi[3], const float* dL_dregion,
+                              float* dL_din, float* dL_dshift, void* stream);
 /* CUDA-event duration of the last backward (with timing enabled). */
 int rfba_ctx_last_backward_ms(rfba_ctx* ctx, double* ms);
 
 /* Block lists. GradientCalc.cpp:47-116 (border 2, put-back into the full
- * magnified output, isotropic mag = cfg->mag[0]); returns the block count, or a
+ * magnified output, magnification per axis, the reference's single Mag when the
+ * three are equal); returns the block count, or a
  * negative status. With blocks == NULL only counts. */
 int rfba_blocks_gradientcalc(const rfba_srrf_config* cfg, const int dims[4], rfba_block* blocks, int cap);
 /* doSplit.m (Matlab Scripts/doSplit.m:1-19) per axis with block edge max_size

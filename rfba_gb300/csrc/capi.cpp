@@ -1015,31 +1015,48 @@ static int read_checks(rfba_ctx* ctx, cudaStream_t st, const char* what) {
     return device_status(ctx, st, what);
 }
 
+// The whole volume as one block computing the fine region [lo, hi) (all of the
+// map when lo / hi are null), its output packed [z][y][x]; n receives the
+// region's element count.
+static int region_block(const rfba_srrf_config* cfg, const int dims[4], const int* lo, const int* hi, rfba_block* b,
+                        int64_t* n) {
+    std::memset(b, 0, sizeof *b);
+    for (int a = 0; a < 3; ++a) {
+        b->size[a] = dims[a];
+        b->lo[a] = lo ? lo[a] : 0;
+        b->hi[a] = hi ? hi[a] : dims[a] * cfg->mag[a];
+        if (b->lo[a] < 0 || b->hi[a] <= b->lo[a] || b->hi[a] > dims[a] * cfg->mag[a]) {
+            set_error("region outside the magnified grid or empty");
+            return RFBA_ERR_INVALID;
+        }
+    }
+    const int64_t nx = b->hi[0] - b->lo[0], ny = b->hi[1] - b->lo[1], nz = b->hi[2] - b->lo[2];
+    b->out_stride[0] = 1;
+    b->out_stride[1] = nx;
+    b->out_stride[2] = nx * ny;
+    *n = nx * ny * nz;
+    return RFBA_OK;
+}
+
 static int forward_shifted_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* in, const float* shifts,
-                                  const int dims[4], float* out, cudaStream_t st) {
+                                  const int dims[4], float* out, cudaStream_t st, const int* rlo = nullptr,
+                                  const int* rhi = nullptr) {
     int s = validate_common(cfg, in, dims, out);
     if (s) return s;
     RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
     if ((s = order_streams(ctx, st))) return s;
     if ((s = ctx->errw.ensure(256, "check word"))) return s;
     RFBA_CUDA(cudaMemsetAsync(ctx->errw.p, 0, 8, st), "check word clear");
+    rfba_block b;
+    int64_t n = 0;
+    if ((s = region_block(cfg, dims, rlo, rhi, &b, &n))) return s;
     const float* ip = nullptr;
     if ((s = apply_drift(ctx, in, shifts, dims, st, &ip))) return s;
-    rfba_block b;
-    std::memset(&b, 0, sizeof b);
-    for (int a = 0; a < 3; ++a) {
-        b.size[a] = dims[a];
-        b.hi[a] = dims[a] * cfg->mag[a];
-    }
-    b.out_stride[0] = 1;
-    b.out_stride[1] = b.hi[0];
-    b.out_stride[2] = (int64_t)b.hi[0] * b.hi[1];
-    const int64_t n = (int64_t)b.hi[0] * b.hi[1] * b.hi[2];
     if ((s = forward_blocks_locked(ctx, cfg, ip, RFBA_F32, dims, &b, 1, out, n, RFBA_DEVICE_PTRS, st, false)))
         return s;
     // the backward can reuse this forward's stacks when they are all resident and
     // the temporal reduction left them intact (ITC 1 bins the series in place)
-    if (ctx->last_passes == 1 && !(cfg->method == 3 && cfg->itc == 1)) {
+    if (!rlo && ctx->last_passes == 1 && !(cfg->method == 3 && cfg->itc == 1)) {
         std::vector<BlockDev> all;
         if ((s = make_blocks(ctx, *cfg, dims, &b, 1, &all))) return s;
         if (all.size() == 1) {
@@ -1060,7 +1077,7 @@ static int forward_shifted_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, co
 // offset 0 of the context's stacks: temporal adjoint, then the radiality
 // adjoint adding into dL/dI' (ctx->gin, cleared by the caller).
 static int adjoint_slab(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* iprime, const int dims[4],
-                        BlockDev blk, const float* gmap, cudaStream_t st) {
+                        BlockDev blk, const float* gmap, long long ngmap, cudaStream_t st) {
     int s;
     const int T = dims[3];
     const size_t nin = (size_t)dims[0] * dims[1] * dims[2] * T;
@@ -1086,10 +1103,9 @@ static int adjoint_slab(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float*
     float* gS = static_cast<float*>(ctx->gS.p);
     float* gI = static_cast<float*>(ctx->gI.p);
     unsigned long long* err = static_cast<unsigned long long*>(ctx->errw.p);
-    const long long nmap = (long long)dims[0] * cfg->mag[0] * dims[1] * cfg->mag[1] * dims[2] * cfg->mag[2];
     int e = launch_temporal_adjoint(dblk, V, static_cast<const float*>(ctx->rad.p),
                                     static_cast<const float*>(ctx->inten.p), gmap, T, cfg->method, cfg->trac_order,
-                                    cfg->intensity_w, cfg->renormalize == 1, cfg->remove_con == 1, gS, gI, nmap, err,
+                                    cfg->intensity_w, cfg->renormalize == 1, cfg->remove_con == 1, gS, gI, ngmap, err,
                                     st);
     if (e) return cuda_fail((cudaError_t)e, "temporal adjoint launch");
     RadParams rp = fill_rad_params(ctx, *cfg, iprime, dims, cza_for_mag(cfg->mag[2]));
@@ -1127,9 +1143,13 @@ static int adjoint_slab(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float*
 }
 
 static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* in, const float* shifts,
-                           const int dims[4], const float* gmap, float* din, float* dshift, cudaStream_t st) {
+                           const int dims[4], const float* gmap, float* din, float* dshift, cudaStream_t st,
+                           const int* rlo = nullptr, const int* rhi = nullptr) {
     int s = validate_common(cfg, in, dims, gmap);
     if (s) return s;
+    rfba_block b;
+    int64_t nreg = 0;
+    if ((s = region_block(cfg, dims, rlo, rhi, &b, &nreg))) return s;
     if (!din) {
         set_error("null argument");
         return RFBA_ERR_INVALID;
@@ -1140,36 +1160,26 @@ static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const flo
     }
     RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
     if ((s = order_streams(ctx, st))) return s;
-    const bool reuse = ctx->train.valid && same_cfg(ctx->train.cfg, *cfg) && ctx->train.in == in &&
+    const bool reuse = !rlo && ctx->train.valid && same_cfg(ctx->train.cfg, *cfg) && ctx->train.in == in &&
                        ctx->train.shifts == shifts && ctx->train.dims[0] == dims[0] && ctx->train.dims[1] == dims[1] &&
                        ctx->train.dims[2] == dims[2] && ctx->train.dims[3] == dims[3];
     if (ctx->timing) RFBA_CUDA(cudaEventRecord(ctx->ev[0], st), "event");
     const int T = dims[3];
     const size_t nin = (size_t)dims[0] * dims[1] * dims[2] * T;
-    const size_t nmap = (size_t)dims[0] * cfg->mag[0] * dims[1] * cfg->mag[1] * dims[2] * cfg->mag[2];
     if ((s = ensure_plan(ctx, *cfg, st))) return s;
     if ((s = ctx->gin.ensure(nin * 4, "input adjoint"))) return s;
     if ((s = ctx->errw.ensure(256, "check word"))) return s;
     if (reuse) {
         RFBA_CUDA(cudaMemsetAsync(ctx->gin.p, 0, nin * 4, st), "adjoint clear");
-        if ((s = adjoint_slab(ctx, cfg, ctx->train.iprime, dims, ctx->train.blk, gmap, st))) return s;
+        if ((s = adjoint_slab(ctx, cfg, ctx->train.iprime, dims, ctx->train.blk, gmap, nreg, st))) return s;
     } else {
         // The whole volume's slices under the stack budget: each slice's stacks are
         // recomputed by the forward kernels, then its adjoint runs (one slice when
         // everything fits).
-        if ((s = ctx->out.ensure(nmap * 4, "map"))) return s;
+        if ((s = ctx->out.ensure((size_t)nreg * 4, "map"))) return s;
         RFBA_CUDA(cudaMemsetAsync(ctx->errw.p, 0, 8, st), "check word clear");
         const float* ip = nullptr;
         if ((s = apply_drift(ctx, in, shifts, dims, st, &ip))) return s;
-        rfba_block b;
-        std::memset(&b, 0, sizeof b);
-        for (int a = 0; a < 3; ++a) {
-            b.size[a] = dims[a];
-            b.hi[a] = dims[a] * cfg->mag[a];
-        }
-        b.out_stride[0] = 1;
-        b.out_stride[1] = b.hi[0];
-        b.out_stride[2] = (int64_t)b.hi[0] * b.hi[1];
         std::vector<BlockDev> all;
         if ((s = make_blocks(ctx, *cfg, dims, &b, 1, &all))) return s;
         RFBA_CUDA(cudaMemsetAsync(ctx->gin.p, 0, nin * 4, st), "adjoint clear");
@@ -1178,7 +1188,7 @@ static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const flo
             if ((s = run_device(ctx, *cfg, ip, RFBA_F32, dims, one, static_cast<float*>(ctx->out.p), st))) return s;
             BlockDev blk = slab;
             blk.stack_off = 0;
-            if ((s = adjoint_slab(ctx, cfg, ip, dims, blk, gmap, st))) return s;
+            if ((s = adjoint_slab(ctx, cfg, ip, dims, blk, gmap, nreg, st))) return s;
         }
     }
     // through the drift operator
@@ -1338,6 +1348,29 @@ int rfba_ctx_check(rfba_ctx* c) {
     std::lock_guard<std::mutex> lk(c->mu);
     RFBA_CUDA(cudaSetDevice(c->device), "cudaSetDevice");
     return device_status(c, c->have_last ? c->last_stream : c->stream, "device work");
+}
+
+int rfba_srrf_forward_shifted_region(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* in,
+                                     const float* shifts, const int dims[4], const int lo[3], const int hi[3],
+                                     float* out, void* stream) {
+    if (!ctx || !lo || !hi) {
+        set_error("null argument");
+        return RFBA_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    return forward_shifted_locked(ctx, cfg, in, shifts, dims, out, static_cast<cudaStream_t>(stream), lo, hi);
+}
+
+int rfba_srrf_backward_region(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* in, const float* shifts,
+                              const int dims[4], const int lo[3], const int hi[3], const float* dL_dregion,
+                              float* dL_din, float* dL_dshift, void* stream) {
+    if (!ctx || !lo || !hi) {
+        set_error("null argument");
+        return RFBA_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    return backward_locked(ctx, cfg, in, shifts, dims, dL_dregion, dL_din, dL_dshift,
+                           static_cast<cudaStream_t>(stream), lo, hi);
 }
 
 int rfba_ctx_last_backward_ms(rfba_ctx* c, double* ms) {

@@ -158,6 +158,8 @@ def lib():
         L.rfba_srrf_plan_info.argtypes = [cp, ip, ip, ip, ip]
         L.rfba_srrf_forward_shifted.argtypes = [vp, cp, vp, vp, ip, vp, vp]
         L.rfba_srrf_backward.argtypes = [vp, cp, vp, vp, ip, vp, vp, vp, vp]
+        L.rfba_srrf_forward_shifted_region.argtypes = [vp, cp, vp, vp, ip, ip, ip, vp, vp]
+        L.rfba_srrf_backward_region.argtypes = [vp, cp, vp, vp, ip, ip, ip, vp, vp, vp, vp]
         L.rfba_ctx_last_backward_ms.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
         L.rfba_ctx_check.argtypes = [vp]
         dp = ctypes.POINTER(ctypes.c_double)
@@ -499,6 +501,40 @@ class Context:
         _check(lib().rfba_srrf_backward(self.h, ctypes.byref(cfg), ctypes.c_void_p(x.data_ptr()), sp, _iptr(dims),
                                         ctypes.c_void_p(dL_dmap.data_ptr()), ctypes.c_void_p(din.data_ptr()), dsp,
                                         st))
+        return din, dshift
+
+    def forward_shifted_region(self, cfg: Config, x, shifts, lo, hi, out=None, stream=None):
+        """forward_shifted restricted to the fine region [lo, hi) (x, y, z):
+        returns the region [z][y][x]."""
+        import torch
+        dims = _dims(x.shape)
+        if out is None:
+            out = torch.empty((hi[2] - lo[2], hi[1] - lo[1], hi[0] - lo[0]), dtype=torch.float32, device=x.device)
+        sp = ctypes.c_void_p(shifts.data_ptr()) if shifts is not None else None
+        st = _stream_arg(stream, True)
+        _check(lib().rfba_srrf_forward_shifted_region(self.h, ctypes.byref(cfg), ctypes.c_void_p(x.data_ptr()), sp,
+                                                      _iptr(dims), _iptr(np.asarray(lo, np.int32)),
+                                                      _iptr(np.asarray(hi, np.int32)),
+                                                      ctypes.c_void_p(out.data_ptr()), st))
+        return out
+
+    def backward_region(self, cfg: Config, x, shifts, lo, hi, dL_dregion, din=None, dshift=None, stream=None):
+        """The region's contribution to the adjoint of forward_shifted:
+        returns (dL/dx, dL/dshifts or None)."""
+        import torch
+        dims = _dims(x.shape)
+        if din is None:
+            din = torch.empty_like(x)
+        if dshift is None and shifts is not None:
+            dshift = torch.empty_like(shifts)
+        sp = ctypes.c_void_p(shifts.data_ptr()) if shifts is not None else None
+        dsp = ctypes.c_void_p(dshift.data_ptr()) if dshift is not None else None
+        st = _stream_arg(stream, True)
+        _check(lib().rfba_srrf_backward_region(self.h, ctypes.byref(cfg), ctypes.c_void_p(x.data_ptr()), sp,
+                                               _iptr(dims), _iptr(np.asarray(lo, np.int32)),
+                                               _iptr(np.asarray(hi, np.int32)),
+                                               ctypes.c_void_p(dL_dregion.data_ptr()),
+                                               ctypes.c_void_p(din.data_ptr()), dsp, st))
         return din, dshift
 
     def spot_gradient_3b(self, model: ThreeBModel, sample_bg, pix, pixels, spot, stream=None):
