@@ -1270,6 +1270,13 @@ int rfba_3b_spot_gradient(rfba_ctx* ctx, const rfba_3b_model* m, const double* s
         set_error("ptr_flags must be RFBA_HOST_PTRS or RFBA_DEVICE_PTRS");
         return RFBA_ERR_INVALID;
     }
+    for (int n = 0; n < 12; ++n) {
+        const double v = n < 9 ? m->A[n] : m->pi[n - 9];
+        if (!(v >= 0 && v <= 1)) {
+            set_error("transition and initial probabilities must lie in [0, 1]");
+            return RFBA_ERR_INVALID;
+        }
+    }
     if (spot[0] <= 0 || spot[1] <= 0) {  // multispot5.cc:618-619
         for (int n = 0; n < 5; ++n) out[n] = std::numeric_limits<double>::quiet_NaN();
         return RFBA_OK;
@@ -1281,7 +1288,7 @@ int rfba_3b_spot_gradient(rfba_ctx* ctx, const rfba_3b_model* m, const double* s
     if ((s = order_streams(ctx, st))) return s;
     const size_t nbg = (size_t)S * F * P, npix = (size_t)F * P;
     if ((s = ctx->tb_val.ensure((size_t)P * 8, "3B spot table")) || (s = ctx->tb_der.ensure((size_t)P * 40, "3B spot table")) ||
-        (s = ctx->tb_em.ensure((size_t)S * F * 64, "3B emissions")) || (s = ctx->tb_res.ensure((size_t)S * 48 + 48, "3B results")) ||
+        (s = ctx->tb_em.ensure((size_t)S * F * 80, "3B emissions")) || (s = ctx->tb_res.ensure((size_t)S * 48 + 48, "3B results")) ||
         (s = ctx->tb_par.ensure(17 * 8, "3B parameters")))
         return s;
     const double* dbg = sample_bg;
@@ -1298,12 +1305,11 @@ int rfba_3b_spot_gradient(rfba_ctx* ctx, const rfba_3b_model* m, const double* s
         dpix = static_cast<const double*>(ctx->tb_pix.p);
         dpixels = static_cast<const int*>(ctx->tb_pixels.p);
     }
-    // parameters: spot, ln A, ln pi with the reference's ln(0) = -1e100 (forward_algorithm.h:34-40)
-    auto ln0 = [](double x) { return x == 0 ? -1e100 : std::log(x); };
+    // parameters: spot, A (row-major), pi
     double par[17];
     for (int n = 0; n < 5; ++n) par[n] = spot[n];
-    for (int n = 0; n < 9; ++n) par[5 + n] = ln0(m->A[n]);
-    for (int n = 0; n < 3; ++n) par[14 + n] = ln0(m->pi[n]);
+    for (int n = 0; n < 9; ++n) par[5 + n] = m->A[n];
+    for (int n = 0; n < 3; ++n) par[14 + n] = m->pi[n];
     RFBA_CUDA(cudaMemcpyAsync(ctx->tb_par.p, par, sizeof par, cudaMemcpyHostToDevice, st), "parameter upload");
     const unsigned int n_pix = (unsigned int)P;
     const double c0 = n_pix * ::log(2 * M_PI * m->variance) / 2;  // spot_with_background.hh:126-127
@@ -1320,7 +1326,7 @@ int rfba_3b_spot_gradient(rfba_ctx* ctx, const rfba_3b_model* m, const double* s
     for (int i = 0; i < S; ++i)
         for (int n = 0; n < 5; ++n) sum[n] += res[(size_t)i * 6 + n];
     // storm.h:431-434: derivatives of the log-normal priors on brightness and blur
-    auto dlln = [&](double x, double mu, double sg) { return -(1 + (ln0(x) - mu) / (sg * sg)) / x; };
+    auto dlln = [&](double x, double mu, double sg) { return -(1 + (std::log(x) - mu) / (sg * sg)) / x; };
     const double prior[5] = {dlln(spot[0], m->mu_brightness, m->sigma_brightness),
                              dlln(spot[1], m->mu_blur, m->sigma_blur), 0, 0, 0};
     for (int n = 0; n < 5; ++n) out[n] = -(sum[n] / (double)S + prior[n]);

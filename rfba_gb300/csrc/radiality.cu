@@ -117,6 +117,12 @@ __device__ __forceinline__ float rsqrt_approx(float x) {
     return r;
 }
 
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 template <int V>
 struct IntC {
     static constexpr int value = V;
@@ -488,12 +494,10 @@ __global__ void __launch_bounds__(WIDE ? kMaxThreads : 128, WIDE ? 2 : 3)
                                 const float2 cp = fma2(hh, gz, mul2(ncc, gx));
                                 const float2 c2 = fma2(cp, cp, mul2(gy, gy));  // |g_perp|^2
                                 const float2 g2 = fma2(dot, dot, c2);          // |g|^2
-                                // sin = c2 / sqrt((c2 + 1e-12 g2) g2): one rsqrt per lane. The
-                                // guard term makes g parallel to u give 0 and leaves g = 0 at
-                                // 0 * inf = NaN (the reference's 0/0).
-                                const float2 xx = mul2(fma2(g2, dup(1e-12f), c2), g2);
-                                const float2 r = make_float2(rsqrt_approx(xx.x), rsqrt_approx(xx.y));
-                                const float2 sn = mul2(c2, r);
+                                // sin = sqrt(c2) / sqrt(g2): g parallel to u gives 0, g = 0
+                                // gives 0 * inf = NaN (the reference's 0/0).
+                                const float2 sn = mul2(make_float2(sqrt_approx(c2.x), sqrt_approx(c2.y)),
+                                                       make_float2(rsqrt_approx(g2.x), rsqrt_approx(g2.y)));
                                 const float2 om = fma2(sn, nun, dup(1.0f));     // 1 - Dk/r
                                 const float2 D = mul2(om, om);
                                 const float2 sw = make_float2(sign_weight(wgt, dot.x), sign_weight(wgt, dot.y));

@@ -190,7 +190,7 @@ int probe_fp32_fma(int device, double* tflops);
 // 3B spot gradient (threeb.cu): spot voxel table, emission sums per (sample,
 // frame), forward algorithm per sample; res[s] = (gradient[5], log probability).
 int launch_threeb(const double* bg, const double* pix, const int* pixels, int S, int F, int P, const double* phi_dev,
-                  double zf, double variance, double c0, const double* lnA_dev, const double* lnpi_dev,
+                  double zf, double variance, double c0, const double* A_dev, const double* pi_dev,
                   double* val, double* der, double* em, double* res, void* stream);
 
 }  // namespace rfba

@@ -14,9 +14,15 @@
 //      mask voxels in FP64 — the sums of squares reach 1e7-1e8 while the
 //      forward algorithm weighs states by exp of their differences, so FP32
 //      sums would be wrong by whole units of log probability;
-//   4. forward_kernel, one warp per state of each sample: the 3-state forward algorithm
+//   4. forward_kernel, one warp per sample: the 3-state forward algorithm
 //      with derivatives over the frames (forward_algorithm.h:157-259,
 //      compute_hessian = 0), giving each sample's log probability and gradient.
+//      The reference runs it in log space (a log-sum-exp per state and frame);
+//      here it runs on probabilities, each state's value kept as a mantissa and
+//      its own power-of-two exponent: the same sums with no exp or log inside
+//      the sequential chain, and no underflow however far apart the states'
+//      probabilities drift (an absorbing state can hold all the mass while the
+//      frames start to favour a state it cannot reach).
 // The host averages the samples' gradients and adds the log-normal priors'
 // derivatives (storm.h:431-434).
 #include <cuda_runtime.h>
@@ -28,9 +34,6 @@ namespace {
 
 constexpr int kM = 5;
 constexpr int kEmitThreads = 256;
-
-// forward_algorithm.h:34-40
-__device__ __forceinline__ double ln0(double x) { return x == 0.0 ? -1e100 : log(x); }
 
 __global__ void spot_pixels_kernel(const int* __restrict__ pixels, int P, const double* __restrict__ phi_in,
                                    double zf, double* __restrict__ val, double* __restrict__ der) {
@@ -86,7 +89,27 @@ __global__ void __launch_bounds__(kSumThreads) spot_sums_kernel(const double* __
     }
 }
 
-// out[(s*F + f)*8 + {0: log prob on, 1: log prob off, 2..6: d(log prob on)/d phi}]
+// Per (sample, frame), kEm doubles: the frame's emission probabilities relative
+// to the larger of the two, exp(log p_on - m) = mant_on 2^k_on and likewise for
+// off (one of them is exactly 1), d(log p_on)/d phi, and m itself:
+// {0: mant_on, 1: mant_off, 2: k_on, 3: k_off, 4..8: d(log p_on)/d phi, 9: m}.
+constexpr int kEm = 10;
+
+// exp(x) = mant 2^k for x <= 0 (mant in about [1, 2)); x = k ln2 + r with r
+// formed by one fused multiply-add, whose error (|k| ulp-sized) is far below
+// the log-space reference's own rounding. Probabilities below 2^-(2^24)
+// relative are 0.
+__device__ __forceinline__ void exp_split(double x, double* mant, double* k) {
+    const double kd = floor(x * 1.4426950408889634);
+    if (kd < -16777216.0) {
+        *mant = 0.0;
+        *k = 0.0;
+        return;
+    }
+    *mant = exp(fma(-kd, 0.6931471805599453, x));
+    *k = kd;
+}
+
 __global__ void __launch_bounds__(kEmitThreads) emission_kernel(const double* __restrict__ bg,
                                                                  const double* __restrict__ pix,
                                                                  const double* __restrict__ val,
@@ -121,92 +144,145 @@ __global__ void __launch_bounds__(kEmitThreads) emission_kernel(const double* __
         for (int w = 0; w < kEmitThreads / 32; ++w)
 #pragma unroll
             for (int i = 0; i < 7; ++i) t[i] += part[w][i];
-        double* o = out + (size_t)sf * 8;
-        const double on = t[1] - 2.0 * t[0] + spot_sums[0];  // sum (d - v)^2
-        o[0] = -on / twovar - c0;
-        o[1] = -t[1] / twovar - c0;
+        double* o = out + (size_t)sf * kEm;
+        // log p_on = -sum (d - v)^2 / 2var - c0, log p_off = -sum d^2 / 2var - c0;
+        // their difference is formed without the large common terms
+        const double off = -t[1] / twovar - c0;
+        const double gap = (2.0 * t[0] - spot_sums[0]) / twovar;  // log p_on - log p_off
+        if (gap <= 0.0) {
+            exp_split(gap, &o[0], &o[2]);
+            o[1] = 1.0;
+            o[3] = 0.0;
+            o[9] = off;
+        } else {
+            o[0] = 1.0;
+            o[2] = 0.0;
+            exp_split(-gap, &o[1], &o[3]);
+            o[9] = off + gap;
+        }
 #pragma unroll
-        for (int n = 0; n < kM; ++n) o[2 + n] = (t[2 + n] - spot_sums[1 + n]) / var;
-        o[7] = 0.0;
+        for (int n = 0; n < kM; ++n) o[4 + n] = (t[2 + n] - spot_sums[1 + n]) / var;
     }
 }
 
-// One CTA per sample, one warp per state j: each step every warp holds the
-// previous delta_i and its derivative for all i, forms its own state's new
-// values (forward_algorithm.h:196-224) and the three warps exchange them
-// through shared memory. exp is skipped where its argument is exactly 0 (the
-// largest term of each sum: exp(0) = 1) or carries ln(0) = -1e100 (the
-// transitions the model forbids: exp = 0), which changes no result. lnA
-// row-major 3 x 3 and lnpi with ln(0) = -1e100 as the reference's ln.
-__device__ __forceinline__ double exp_term(double a) {
-    return a == 0.0 ? 1.0 : (a < -1e99 ? 0.0 : exp(a));
+// One warp per sample. Lane l < 18 holds state j = l / 6 and component k =
+// l % 6: k < 5 the derivative part D_jk = alpha_j dd_jk, k = 5 the probability
+// alpha_j, both as x_jk 2^E_j with x_j5 in [0.5, 1) (E_j = kZeroExp when
+// alpha_j = 0); lanes 18..31 repeat lanes 0..13. In the reference's terms
+// alpha_j = exp(delta_j) up to a common factor and dd_jk is its derivative
+// table, so per frame t (forward_algorithm.h:196-224)
+//   alpha_j <- p_j(t) sum_i A_ij alpha_i,
+//   D_jk    <- p_j(t) sum_i A_ij D_ik + [j = on] alpha_j d(log p_on(t))/d phi_k,
+// and at the end log P = log sum_j alpha_j and the gradient is
+// sum_j D_jk / sum_j alpha_j (forward_algorithm.h:240-259). The sum over i is
+// aligned to the largest exponent among the states that can move to j; terms
+// more than 2^1022 below it are dropped (the reference's exp underflows there).
+constexpr int kZeroExp = -(1 << 29);
+
+__device__ __forceinline__ double pow2i(int d) {  // 2^d for -1022 <= d <= 1023
+    return __hiloint2double((d + 1023) << 20, 0);
 }
 
-__global__ void __launch_bounds__(96) forward_kernel(const double* __restrict__ em, int S, int F,
-                                                      const double* __restrict__ lnA9,
-                                                      const double* __restrict__ lnpi3, double* __restrict__ res) {
-    // one warp per state j; the new delta_j and its derivative go through
-    // shared memory (double-buffered, one barrier per frame)
-    __shared__ double sh[2][3][8];
+__global__ void __launch_bounds__(32) forward_kernel(const double* __restrict__ em, int S, int F,
+                                                      const double* __restrict__ A9,
+                                                      const double* __restrict__ pi3, double* __restrict__ res) {
     const int s = blockIdx.x;
-    const int j = threadIdx.x >> 5;
-    const int lane = threadIdx.x & 31;
-    double lnAj[3];
-    for (int i = 0; i < 3; ++i) lnAj[i] = lnA9[i * 3 + j];
-    const double* e = em + (size_t)s * F * 8;
-    double delta[3], dd[3][kM];
+    const int lane = threadIdx.x;
+    const int l = lane % 18;
+    const int j = l / 6, k = l % 6;
+    const unsigned full = 0xffffffffu;
+    double Aj[3];
+    bool nz[3];
+#pragma unroll
     for (int i = 0; i < 3; ++i) {
-        delta[i] = lnpi3[i] + (i == 0 ? e[0] : e[1]);
-        for (int n = 0; n < kM; ++n) dd[i][n] = i == 0 ? e[2 + n] : 0.0;
+        Aj[i] = A9[i * 3 + j];
+        nz[i] = Aj[i] != 0.0;
+    }
+    const double* e = em + (size_t)s * F * kEm;
+    // sum over the frames of the reference level m (lanes in parallel)
+    double base = 0.0;
+    for (int t = lane; t < F; t += 32) base += e[(size_t)t * kEm + 9];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) base += __shfl_xor_sync(full, base, o);
+
+    const int mi = j == 0 ? 0 : 1;  // the bleached state emits like "off"
+    const int ki = j == 0 ? 2 : 3;
+    const bool has_de = j == 0 && k < 5;
+    // normalise the new values y of this lane's state by the exponent of its
+    // probability lane; returns the state's new exponent
+    auto normalise = [&](double y, int Ebase, double* x) {
+        const double y5 = __shfl_sync(full, y, j * 6 + 5);
+        const int hi = __double2hiint(y5), lo = __double2loint(y5);
+        if (hi == 0 && lo == 0) {
+            *x = y;
+            return kZeroExp;
+        }
+        const int sh = ((hi >> 20) & 0x7ff) - 1022;  // y5 = m 2^sh, m in [0.5, 1)
+        *x = y * pow2i(-sh);
+        return Ebase + sh;
+    };
+    // frame 0: alpha_j = pi_j p_j(0)
+    double x;
+    int E[3];
+    {
+        const double a = pi3[j] * e[mi];
+        const double y = k == 5 ? a : (has_de ? a * e[4 + k] : 0.0);
+        const int En = normalise(y, (int)e[ki], &x);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) E[i] = __shfl_sync(full, En, i * 6 + 5);
+    }
+    // the next frame's loads go out one frame ahead
+    double nm = 0.0, nk = 0.0, nq = 0.0;
+    if (F > 1) {
+        const double* et = e + kEm;
+        nm = et[mi];
+        nk = et[ki];
+        nq = has_de ? et[4 + k] : 0.0;
     }
     for (int t = 1; t < F; ++t) {
-        const double* et = e + (size_t)t * 8;
-        double Z = -__longlong_as_double(0x7ff0000000000000ll);
-        for (int i = 0; i < 3; ++i) Z = fmax(Z, delta[i] + lnAj[i]);
-        double w[3], sum = 0.0;
-        for (int i = 0; i < 3; ++i) {
-            w[i] = exp_term(delta[i] + lnAj[i] - Z);
-            sum += w[i];
+        const double mant = nm, q = nq;
+        const int ke = (int)nk;
+        if (t + 1 < F) {
+            const double* et = e + (size_t)(t + 1) * kEm;
+            nm = et[mi];
+            nk = et[ki];
+            nq = has_de ? et[4 + k] : 0.0;
         }
-        const double nd = (j == 0 ? et[0] : et[1]) + Z + ln0(sum);
-        double top[kM] = {0, 0, 0, 0, 0};
+        int Em = kZeroExp;
+#pragma unroll
         for (int i = 0; i < 3; ++i)
-            for (int n = 0; n < kM; ++n) top[n] += dd[i][n] * w[i];
-        double* o = sh[t & 1][j];
-        if (lane == 0) {
-            // one reciprocal instead of five divisions (FP64 division is a long
-            // sequence here); the products differ from the quotients by an ulp
-            const double rs = 1.0 / sum;
-            o[0] = nd;
-            for (int n = 0; n < kM; ++n) o[1 + n] = (j == 0 ? et[2 + n] : 0.0) + top[n] * rs;
-        }
-        __syncthreads();
+            if (nz[i] && E[i] > Em) Em = E[i];
+        double c[3];
+#pragma unroll
         for (int i = 0; i < 3; ++i) {
-            const double* q = sh[t & 1][i];
-            delta[i] = q[0];
-            for (int n = 0; n < kM; ++n) dd[i][n] = q[1 + n];
+            const int d = E[i] - Em;
+            c[i] = (d >= -1022 && d <= 0) ? Aj[i] * pow2i(d) : 0.0;
         }
+        double xi[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) xi[i] = __shfl_sync(full, x, i * 6 + k);
+        double y = fma(c[2], xi[2], fma(c[1], xi[1], c[0] * xi[0])) * mant;
+        const double y05 = __shfl_sync(full, y, 5);
+        y = fma(y05, q, y);
+        const int En = normalise(y, Em + ke, &x);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) E[i] = __shfl_sync(full, En, i * 6 + 5);
     }
-    if (threadIdx.x != 0) return;
-    double Z = -__longlong_as_double(0x7ff0000000000000ll);
-    for (int i = 0; i < 3; ++i) Z = fmax(Z, delta[i]);
-    double sum = 0.0;
-    for (int i = 0; i < 3; ++i) sum += exp(delta[i] - Z);
-    const double logp = Z + ln0(sum);
-    double g[kM] = {0, 0, 0, 0, 0};
-    for (int i = 0; i < 3; ++i) {
-        const double w = exp(delta[i] - logp);
-        for (int n = 0; n < kM; ++n) g[n] += w * dd[i][n];
-    }
+    // log P and the gradient, the states aligned to the largest exponent
+    const int Em = max(E[0], max(E[1], E[2]));
+    const int d = E[j] - Em;
+    const double v = (d >= -1022) ? x * pow2i(d) : 0.0;
+    const double tot = v + __shfl_sync(full, v, (lane + 6) & 31) + __shfl_sync(full, v, (lane + 12) & 31);
+    const double den = __shfl_sync(full, tot, 5);
     double* r = res + (size_t)s * 6;
-    for (int n = 0; n < kM; ++n) r[n] = g[n];
-    r[5] = logp;
+    if (lane < 5) r[lane] = tot / den;
+    if (lane == 5) r[5] = base + log(den) + (double)Em * 0.6931471805599453;
 }
 
 }  // namespace
 
 int launch_threeb(const double* bg, const double* pix, const int* pixels, int S, int F, int P, const double* phi_dev,
-                  double zf, double variance, double c0, const double* lnA_dev, const double* lnpi_dev,
+                  double zf, double variance, double c0, const double* A_dev, const double* pi_dev,
                   double* val, double* der, double* em, double* res, void* stream) {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     spot_pixels_kernel<<<(P + 255) / 256, 256, 0, st>>>(pixels, P, phi_dev, zf, val, der);
@@ -214,7 +290,7 @@ int launch_threeb(const double* bg, const double* pix, const int* pixels, int S,
     spot_sums_kernel<<<1, kSumThreads, 0, st>>>(val, der, P, sums);
     emission_kernel<<<(unsigned)((long long)S * F), kEmitThreads, 0, st>>>(bg, pix, val, der, sums, F, P,
                                                                            2 * variance, variance, c0, em);
-    forward_kernel<<<S, 96, 0, st>>>(em, S, F, lnA_dev, lnpi_dev, res);
+    forward_kernel<<<S, 32, 0, st>>>(em, S, F, A_dev, pi_dev, res);
     return (int)cudaGetLastError();
 }
 

@@ -1,8 +1,9 @@
 """3B spot gradient on the GPU (rfba_3b_spot_gradient) against the FP64 oracle
 (pinned to the reference's headers in tests/test_threeb_cpu.py). Both compute
 in FP64; the GPU sums each frame's voxels in a tree instead of in sequence and
-uses CUDA's exp/log, so the gradient agrees to 1e-9 of its largest component
-and every sample's log probability to 1e-12 (relative)."""
+runs the forward algorithm on probabilities with a power-of-two exponent per
+state instead of in log space, so the gradient agrees to 1e-9 of its largest
+component and every sample's log probability to 1e-12 (relative)."""
 import numpy as np
 import pytest
 
@@ -58,3 +59,40 @@ def test_non_positive_brightness_or_blur_gives_nan(ctx):
         s[i] = -1.0
         got, _ = ctx.spot_gradient_3b(_model(1.0, 1.0), bg, pix, px, s)
         assert np.isnan(got).all()
+
+
+def test_long_bleach_then_bright_frames(ctx):
+    """1400 dark frames (the absorbing bleached state ends up holding all the
+    mass, more than e^709 above the others) followed by frames with a very
+    bright spot, which the bleached state cannot emit: probabilities without
+    their own exponents underflow to 0 here, the log-space reference does not."""
+    bg, pix, px, spot = T.synthetic_block(7, 3, 1400)
+    rng = np.random.default_rng(1)
+    pix = bg.mean(0) + rng.normal(0, 1, pix.shape)
+    d = px - spot[2:]
+    pix[-5:] += spot[0] * 3 / (spot[1] * np.sqrt(2 * np.pi)) * np.exp(-(d * d).sum(1) / (2 * spot[1] ** 2))
+    want, lpw = T.spot_neg_prob_diff(bg, pix, px, spot, with_logp=True)
+    got, lp = ctx.spot_gradient_3b(_model(1.0, 1.0), bg, pix, px, spot)
+    assert np.isfinite(want).all() and np.isfinite(lpw).all()
+    _compare(got, lp, want, lpw)
+
+
+def test_dense_transition_matrix(ctx):
+    """A model where every state can reach every other, with a non-zero start
+    probability for each."""
+    from rfba_gb300.srrf import ThreeBModel
+    A = np.array([[0.7, 0.2, 0.1], [0.3, 0.6, 0.1], [0.05, 0.05, 0.9]])
+    pi = np.array([0.2, 0.5, 0.3])
+    bg, pix, px, spot = T.synthetic_block(11, 5, 40, (8, 8, 6))
+    want, lpw = T.spot_neg_prob_diff(bg, pix, px, spot, A=A, pi=pi, with_logp=True)
+    got, lp = ctx.spot_gradient_3b(ThreeBModel.make(A, pi), bg, pix, px, spot)
+    _compare(got, lp, want, lpw)
+
+
+def test_rejects_probabilities_outside_unit_interval(ctx):
+    from rfba_gb300.srrf import RfbaError, ThreeBModel
+    bg, pix, px, spot = T.synthetic_block(8, 2, 4, (5, 5, 5))
+    A = T.A_SHIPPED.copy()
+    A[0, 0] = -0.1
+    with pytest.raises(RfbaError, match="probabilities"):
+        ctx.spot_gradient_3b(ThreeBModel.make(A, T.PI_SHIPPED), bg, pix, px, spot)
