@@ -96,14 +96,19 @@ def test_balance_and_slabs():
     assert shard.z_slabs(2, 4) == [(0, 1), (1, 2), (2, 2), (2, 2)]
 
 
-def test_repack_put_back_identity():
+@pytest.mark.parametrize("split", ["gradientcalc", "dosplit"])
+def test_repack_put_back_identity(split):
     """Packing any subset of blocks and putting it back reproduces the writes
-    of the original block list."""
+    of the original block list: GradientCalc's blocks put back into the whole
+    map, doSplit's written one after another."""
     from rfba_gb300 import shard, srrf
     cfg = srrf.Config.make(**KW)
-    blocks, n = srrf.blocks_gradientcalc(cfg, SHAPE)
+    if split == "gradientcalc":
+        blocks, n = srrf.blocks_gradientcalc(cfg, SHAPE)
+        total = SHAPE[1] * SHAPE[2] * SHAPE[3] * 8
+    else:
+        blocks, n, total = srrf.blocks_dosplit(cfg, SHAPE, 5, 1)
     assert n >= 4
-    total = SHAPE[1] * SHAPE[2] * SHAPE[3] * 8
     ref = np.zeros(total, np.float32)
     rng = np.random.default_rng(0)
     vals = []
