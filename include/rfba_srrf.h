@@ -248,7 +248,8 @@ typedef struct rfba_3b_model {
  * host or device memory (ptr_flags). spot, out[5] and log_prob[S] (each
  * sample's log probability; may be NULL) are host memory; the call returns
  * when out is written. spot[0] <= 0 or spot[1] <= 0 gives NaN, as the
- * reference does. FP64 throughout. */
+ * reference does; entries of A or pi outside [0, 1] give RFBA_ERR_INVALID.
+ * FP64 throughout. */
 int rfba_3b_spot_gradient(rfba_ctx* ctx, const rfba_3b_model* model, const double* sample_bg,
                           const double* pixel_intensities, const int* pixels, int S, int F, int P,
                           const double spot[5], double out[5], double* log_prob, int ptr_flags, void* stream);

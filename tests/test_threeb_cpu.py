@@ -61,3 +61,125 @@ def test_gradient_matches_central_differences():
         e[n] = h
         fd = (f(spot + e) - f(spot - e)) / (2 * h)
         assert abs(fd - g[n]) <= 1e-5 * max(1.0, abs(g[n])), (n, fd, g[n])
+
+
+def _bleach_then_bright():
+    """1400 dark frames, then 5 frames with a bright spot (see the GPU test)."""
+    bg, pix, px, spot = T.synthetic_block(7, 3, 1400)
+    rng = np.random.default_rng(1)
+    pix = bg.mean(0) + rng.normal(0, 1, pix.shape)
+    d = px - spot[2:]
+    pix[-5:] += spot[0] * 3 / (spot[1] * np.sqrt(2 * np.pi)) * np.exp(-(d * d).sum(1) / (2 * spot[1] ** 2))
+    return bg, pix, px, spot
+
+
+def test_oracle_reproduces_reference_bits_long_bleach():
+    if T.ref_lib() is None:
+        pytest.skip("oracle/_ref/libref3b_host.so not built (reference sources absent)")
+    bg, pix, px, spot = _bleach_then_bright()
+    a = T.spot_neg_prob_diff(bg, pix, px, spot)
+    b = T.ref_spot_neg_prob_diff(bg, pix, px, spot)
+    assert np.isfinite(a).all()
+    assert np.array_equal(a.view(np.uint64), b.view(np.uint64)), (a, b)
+
+
+def _emissions(bg, pix, px, spot):
+    """Per (sample, frame): log p_on - log p_off, log p_off and d(log p_on)/d phi
+    (spot_with_background.hh:98-133, unit z factor and variance)."""
+    x = px.astype(np.float64)
+    d0, d1, d2 = x[:, 0] - spot[2], x[:, 1] - spot[3], x[:, 2] - spot[4]
+    s = -(d0 * d0 + d1 * d1 + d2 * d2) / (2 * spot[1] ** 2)
+    k = np.exp(s) / (spot[1] * np.sqrt(2 * np.pi))
+    v = k * spot[0]
+    q = spot[0] / spot[1] ** 2
+    der = np.stack([k, k * (-spot[0] * (1 + 2 * s) / spot[1]), k * d0 * q, k * d1 * q, k * d2 * q], 1)
+    c0 = len(px) * np.log(2 * np.pi) / 2
+    r = pix[None] - bg
+    off = -(r * r).sum(-1) / 2 - c0
+    gap = ((r * v).sum(-1) * 2 - (v * v).sum()) / 2
+    de = np.einsum("sfp,pn->sfn", r - v, der)
+    return gap, off, de
+
+
+def _forward_exponent_form(gap, off, de, A, pi, per_state=True):
+    """The GPU kernel's recursion (rfba_gb300/csrc/threeb.cu forward_kernel) in
+    numpy: probabilities alpha_j and D_jk = alpha_j d(delta_j)/d phi_k as
+    mantissas with an integer exponent per state (per_state=False: one scale
+    for all states, which underflows when the mass sits in a state that cannot
+    reach the one the frames favour). Returns (mean gradient of log P, log P)."""
+    S, F = gap.shape
+    g = np.zeros((S, 5))
+    lp = np.zeros(S)
+    zero = -(1 << 29)
+    for s in range(S):
+        m = np.where(gap[s] <= 0, off[s], off[s] + gap[s])
+        p = np.stack([np.exp(np.minimum(gap[s], 0)), np.exp(np.minimum(-gap[s], 0))], 1)
+        p = np.column_stack([p[:, 0], p[:, 1], p[:, 1]])  # bleached emits like off
+        X = np.zeros((3, 6))
+        X[:, 5] = pi * p[0]
+        X[0, :5] = X[0, 5] * de[s, 0]
+        E = np.zeros(3, np.int64)
+
+        def normalise(X, E):
+            for j in range(3 if per_state else 1):
+                rows = [j] if per_state else [0, 1, 2]
+                ref = X[j, 5] if per_state else X[:, 5].sum()
+                if ref == 0:
+                    E[rows] = zero
+                    continue
+                sh = np.frexp(ref)[1]
+                X[rows] = np.ldexp(X[rows], -sh)
+                E[rows] += sh
+            return X, E
+
+        X, E = normalise(X, E)
+        for t in range(1, F):
+            Y = np.zeros((3, 6))
+            En = np.zeros(3, np.int64)
+            for j in range(3):
+                live = [i for i in range(3) if A[i, j] != 0]
+                Em = max([E[i] for i in live] + [zero])
+                c = np.array([A[i, j] * np.ldexp(1.0, int(E[i] - Em)) if -1022 <= E[i] - Em <= 0 else 0.0
+                              for i in range(3)])
+                Y[j] = p[t, j] * (c @ X)
+                En[j] = Em
+            Y[0, :5] += Y[0, 5] * de[s, t]
+            X, E = normalise(Y, En)
+        Em = E.max()
+        w = np.array([np.ldexp(1.0, int(e - Em)) if e - Em >= -1022 else 0.0 for e in E])
+        tot = w @ X
+        with np.errstate(all="ignore"):
+            g[s] = tot[:5] / tot[5]
+            lp[s] = m.sum() + np.log(tot[5]) + Em * np.log(2)
+    return g, lp
+
+
+def _prior(spot):
+    def dlln(x, mu, sg):
+        return -(1 + (np.log(x) - mu) / (sg * sg)) / x
+    return np.array([dlln(spot[0], 3.5, 1.0), dlln(spot[1], 0.252148, 0.1), 0, 0, 0])
+
+
+@pytest.mark.parametrize("case", ["seed0", "seed3", "dense", "long_bleach"])
+def test_exponent_form_matches_log_space(case):
+    """The probability form with per-state exponents (what the GPU runs) gives
+    the log-space reference's gradient to 1e-10 and log probability to 1e-13;
+    with one scale for all states the long-bleach case underflows to NaN."""
+    A, pi = T.A_SHIPPED, T.PI_SHIPPED
+    if case == "long_bleach":
+        bg, pix, px, spot = _bleach_then_bright()
+    elif case == "dense":
+        A = np.array([[0.7, 0.2, 0.1], [0.3, 0.6, 0.1], [0.05, 0.05, 0.9]])
+        pi = np.array([0.2, 0.5, 0.3])
+        bg, pix, px, spot = T.synthetic_block(11, 4, 40, (8, 8, 6))
+    else:
+        bg, pix, px, spot = T.synthetic_block(int(case[-1]), 4, 60)
+    want, lpw = T.spot_neg_prob_diff(bg, pix, px, spot, A=A, pi=pi, with_logp=True)
+    gap, off, de = _emissions(bg, pix, px, spot)
+    g, lp = _forward_exponent_form(gap, off, de, A, pi)
+    got = -(g.mean(0) + _prior(spot))
+    assert np.max(np.abs(got - want)) <= 1e-10 * np.max(np.abs(want)), (got, want)
+    assert np.max(np.abs(lp - lpw) / np.abs(lpw)) <= 1e-13
+    if case == "long_bleach":
+        g1, lp1 = _forward_exponent_form(gap, off, de, A, pi, per_state=False)
+        assert not np.isfinite(lp1).all()
