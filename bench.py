@@ -384,7 +384,24 @@ def measure_threeb(ctx, steps: int = 20) -> dict:
            "unit": "spot-gradient evaluations/s", "h2d_bytes_per_call": int(bg.nbytes + pix.nbytes + px.nbytes),
            "fp64_flops_per_call": int(S * F * np.prod(shape) * 18)}
     res["fp64_tflops_device"] = res["fp64_flops_per_call"] / (dev_ms * 1e-3) / 1e12
+    # one spot optimisation as 3B runs it (multispot5.cc:1614-1636): the shipped
+    # main.cg.max_iterations 5 and cg.max_motion 0.5 with the brightness limit
+    # scaled by the prior's std; samples and data copied in once per spot
+    lim = threeb_motion_limit()
+    ctx.optimise_spot_3b(model, *pin, spot, lim, 5)
+    t0 = time.perf_counter()
+    x_opt, it, ev = ctx.optimise_spot_3b(model, *pin, spot, lim, 5)
+    opt_ms = (time.perf_counter() - t0) * 1e3
+    res["optimise"] = {"what": "one spot optimisation (ConjugateGradientOnly<5>, 5 line searches, max motion 0.5), "
+                               "samples and data copied from pinned host memory once",
+                       "ms": opt_ms, "line_searches": it, "gradient_evaluations": ev,
+                       "ms_per_evaluation": opt_ms / max(ev, 1), "spot": x_opt.tolist()}
     return res
+
+
+def threeb_motion_limit(mu: float = 3.5, sigma: float = 1.0, max_motion: float = 0.5):
+    """3B's per-parameter step limits (multispot5.cc:1484, storm.h:386-389)."""
+    return max_motion * np.array([np.sqrt((np.exp(sigma ** 2) - 1) * np.exp(2 * mu + sigma ** 2)), 1, 1, 1, 1])
 
 
 def threeb_cpu_baseline(res: dict, reps: int = 3) -> dict:
@@ -398,10 +415,22 @@ def threeb_cpu_baseline(res: dict, reps: int = 3) -> dict:
     for _ in range(reps):
         T.spot_neg_prob_diff(bg, pix, px, spot, nthreads=os.cpu_count() or 1)
     cpu_ms = (time.perf_counter() - t0) / reps * 1e3
-    return {"cpu_ms": cpu_ms, "cpu_value": 1e3 / cpu_ms, "cores": os.cpu_count(),
-            "kind": "port (FP64 oracle, pinned bit for bit to the reference's headers; threads over samples)",
-            "speedup_device_vs_cpu": cpu_ms / res["device_ms"], "speedup_e2e_vs_cpu": cpu_ms / res["e2e_ms"],
-            "oracle_gradient": want.tolist()}
+    out = {"cpu_ms": cpu_ms, "cpu_value": 1e3 / cpu_ms, "cores": os.cpu_count(),
+           "kind": "port (FP64 oracle, pinned bit for bit to the reference's headers; threads over samples)",
+           "speedup_device_vs_cpu": cpu_ms / res["device_ms"], "speedup_e2e_vs_cpu": cpu_ms / res["e2e_ms"],
+           "oracle_gradient": want.tolist()}
+    if "optimise" in res:
+        # the same optimisation with the oracle's gradient on the host cores
+        from rfba_gb300 import srrf
+        nt = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        x_cpu, it, ev = srrf.cg_only_run(lambda x: T.spot_neg_prob_diff(bg, pix, px, x, nthreads=nt), spot,
+                                         threeb_motion_limit(), 5)
+        opt_ms = (time.perf_counter() - t0) * 1e3
+        out["optimise"] = {"ms": opt_ms, "gradient_evaluations": ev,
+                           "speedup_e2e_vs_cpu": opt_ms / res["optimise"]["ms"],
+                           "max_abs_spot_difference": float(np.max(np.abs(x_cpu - np.array(res["optimise"]["spot"]))))}
+    return out
 
 
 def measure_diff(ctx, steps: int, iters: int = 20, volumes=None) -> dict:

@@ -254,6 +254,28 @@ int rfba_3b_spot_gradient(rfba_ctx* ctx, const rfba_3b_model* model, const doubl
                           const double* pixel_intensities, const int* pixels, int S, int F, int P,
                           const double spot[5], double out[5], double* log_prob, int ptr_flags, void* stream);
 
+/* The spot optimisation 3B runs on each spot after drawing its background
+ * samples (RFBA Main/multispot5.cc:1614-1636): ConjugateGradientOnly<5>
+ * (conjugate_gradient_only.h) from `spot`, steps limited per parameter by
+ * `limit` (the reference's `limit` vector: cg.max_motion times
+ * (brightness limit, 1, 1, 1, 1)), at most max_iterations line searches
+ * (main.cg.max_iterations), with rfba_3b_spot_gradient's value as the gradient
+ * on data staged once on the device. Writes the final spot; iterations and
+ * evaluations (gradient calls) may be NULL. Same arguments, layouts and
+ * synchronous return as rfba_3b_spot_gradient. */
+int rfba_3b_optimise_spot(rfba_ctx* ctx, const rfba_3b_model* model, const double* sample_bg,
+                          const double* pixel_intensities, const int* pixels, int S, int F, int P,
+                          const double spot[5], const double limit[5], int max_iterations, double spot_out[5],
+                          int* iterations, int* evaluations, int ptr_flags, void* stream);
+
+/* The same optimiser on the host, with the gradient supplied by the caller
+ * (fn returns 0, or a non-zero value that stops the run and is returned). No
+ * device work; for optimisers whose gradient lives elsewhere and for checking
+ * the optimiser itself. */
+typedef int (*rfba_grad5_fn)(const double x[5], double grad[5], void* user);
+int rfba_cg_only_run(const double start[5], const double limit[5], int max_iterations, rfba_grad5_fn grad,
+                     void* user, double x_out[5], int* iterations, int* evaluations);
+
 /* Device-side failure check. No counterpart in the reference (GradientCalc.cpp
  * and kernel.cu check no CUDA status; every call returns 0). Waits for the
  * work the context last enqueued and reports failures its kernels recorded

@@ -89,3 +89,44 @@ extern "C" int ref3b_spot_neg_prob_diff(const double* sample_bg, const double* p
     for (int i = 0; i < 5; ++i) out[i] = r[i];
     return 0;
 }
+
+// The reference's own ConjugateGradientOnly<5> (conjugate_gradient_only.h),
+// driven as multispot5.cc:1624-1636 drives it, with the gradient above.
+#include "conjugate_gradient_only.h"
+
+namespace {
+struct RefSpotDeriv {
+    const double *sample_bg, *pix;
+    const int* pixels;
+    int S, F, P;
+    double zFactor, variance;
+    const double *A, *pi;
+    double mu_b, sigma_b, mu_r, sigma_r;
+    int nthreads;
+    Vector<5> operator()(const Vector<5>& x) const {
+        double s[5], out[5];
+        for (int i = 0; i < 5; ++i) s[i] = x[i];
+        ref3b_spot_neg_prob_diff(sample_bg, pix, pixels, S, F, P, s, zFactor, variance, A, pi, mu_b, sigma_b, mu_r,
+                                 sigma_r, nthreads, out);
+        return makeVector(out[0], out[1], out[2], out[3], out[4]);
+    }
+};
+}  // namespace
+
+extern "C" int ref3b_cg_optimise(const double* sample_bg, const double* pix, const int* pixels, int S, int F, int P,
+                                 const double* spot_in, double zFactor, double variance, const double* A_in,
+                                 const double* pi_in, double mu_brightness, double sigma_brightness, double mu_blur,
+                                 double sigma_blur, int nthreads, const double* limit_in, int max_iterations,
+                                 double* x_out, int* iterations) {
+    RefSpotDeriv d{sample_bg, pix, pixels, S, F, P, zFactor, variance, A_in, pi_in,
+                   mu_brightness, sigma_brightness, mu_blur, sigma_blur, nthreads};
+    Vector<5> start = makeVector(spot_in[0], spot_in[1], spot_in[2], spot_in[3], spot_in[4]);
+    Vector<5> limit = makeVector(limit_in[0], limit_in[1], limit_in[2], limit_in[3], limit_in[4]);
+    ConjugateGradientOnly<5> cg(start, d, limit);
+    cg.max_iterations = max_iterations;
+    while (cg.iterate(d)) {
+    }
+    for (int i = 0; i < 5; ++i) x_out[i] = cg.x[i];
+    *iterations = cg.iterations;
+    return 0;
+}

@@ -119,6 +119,33 @@ def ref_spot_neg_prob_diff(sample_bg, pix, pixels, spot, z_factor=1.0, variance=
     return out
 
 
+def ref_cg_optimise(sample_bg, pix, pixels, spot, limit, max_iterations, z_factor=1.0, variance=1.0, A=A_SHIPPED,
+                    pi=PI_SHIPPED, mu_brightness=3.5, sigma_brightness=1.0, mu_blur=0.252148, sigma_blur=0.1,
+                    nthreads=8):
+    """The reference's ConjugateGradientOnly<5> with the reference's spot
+    gradient (multispot5.cc:1624-1636), compiled on the host: (final spot,
+    line searches), or None when not built."""
+    L = ref_lib()
+    if L is None:
+        return None
+    if not hasattr(L, "cg"):
+        dp, ip = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
+        d, i = ctypes.c_double, ctypes.c_int
+        L.cg = L.ref3b_cg_optimise
+        L.cg.argtypes = [dp, dp, ip, i, i, i, dp, d, d, dp, dp, d, d, d, d, i, dp, i, dp, ip]
+        L.cg.restype = ctypes.c_int
+    sample_bg, pix, pixels, spot, A, pi, S, F, P = _args(sample_bg, pix, pixels, spot, A, pi)
+    limit = np.ascontiguousarray(limit, np.float64)
+    out = np.zeros(5)
+    it = ctypes.c_int()
+    rc = L.cg(_p(sample_bg, ctypes.c_double), _p(pix, ctypes.c_double), _p(pixels, ctypes.c_int), S, F, P,
+              _p(spot, ctypes.c_double), z_factor, variance, _p(A, ctypes.c_double), _p(pi, ctypes.c_double),
+              mu_brightness, sigma_brightness, mu_blur, sigma_blur, nthreads, _p(limit, ctypes.c_double),
+              int(max_iterations), _p(out, ctypes.c_double), ctypes.byref(it))
+    assert rc == 0
+    return out, it.value
+
+
 def synthetic_block(seed: int, S: int, F: int, shape=(9, 9, 7), n_spots: int = 6, spot=None, variance=1.0):
     """The seeded 3B block of rfba_gb300.synth.threeb_block (mask voxels, data,
     background samples, a starting spot)."""

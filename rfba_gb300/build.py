@@ -64,8 +64,11 @@ def _compile(src: Path, verbose_ptxas: bool) -> Path:
         if verbose_ptxas:
             cmd[1:1] = ["-Xptxas", "-v"]
     else:
-        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-I", _cuda_include(), "-I", str(PKG.parent / "include"),
-               "-c", str(src), "-o", str(obj)]
+        # no floating-point contraction: host arithmetic that follows the
+        # reference's (ring and window tables, the spot optimiser) gives the same
+        # bits on x86 and Arm
+        cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-I", _cuda_include(), "-I",
+               str(PKG.parent / "include"), "-c", str(src), "-o", str(obj)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

@@ -21,6 +21,7 @@
 #include <string>
 #include <vector>
 
+#include "cg_only.h"
 #include "srrf_internal.h"
 
 namespace rfba {
@@ -1226,6 +1227,99 @@ static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const flo
     return read_checks(ctx, st, "backward");
 }
 
+// ---- 3B spot gradient ------------------------------------------------------
+
+static int threeb_validate(const rfba_3b_model* m, int S, int F, int P, int ptr_flags) {
+    if (S < 1 || F < 1 || P < 1 || (long long)S * F >= (1LL << 31) || !(m->variance > 0) || m->z_factor == 0) {
+        set_error("bad sizes or model (S, F, P >= 1, S*F < 2^31, variance > 0, z_factor != 0)");
+        return RFBA_ERR_INVALID;
+    }
+    if (ptr_flags != RFBA_HOST_PTRS && ptr_flags != RFBA_DEVICE_PTRS) {
+        set_error("ptr_flags must be RFBA_HOST_PTRS or RFBA_DEVICE_PTRS");
+        return RFBA_ERR_INVALID;
+    }
+    for (int n = 0; n < 12; ++n) {
+        const double v = n < 9 ? m->A[n] : m->pi[n - 9];
+        if (!(v >= 0 && v <= 1)) {
+            set_error("transition and initial probabilities must lie in [0, 1]");
+            return RFBA_ERR_INVALID;
+        }
+    }
+    return RFBA_OK;
+}
+
+struct ThreeBData {
+    const double* bg = nullptr;
+    const double* pix = nullptr;
+    const int* pixels = nullptr;
+    int S = 0, F = 0, P = 0;
+};
+
+// Scratch for one evaluation, and the data on the device (copied in once when
+// the caller's pointers are host memory).
+static int threeb_stage(rfba_ctx* ctx, const double* sample_bg, const double* pixel_intensities, const int* pixels,
+                        int S, int F, int P, int ptr_flags, cudaStream_t st, ThreeBData* d) {
+    int s;
+    const size_t nbg = (size_t)S * F * P, npix = (size_t)F * P;
+    if ((s = ctx->tb_val.ensure((size_t)P * 8, "3B spot table")) || (s = ctx->tb_der.ensure((size_t)P * 40, "3B spot table")) ||
+        (s = ctx->tb_em.ensure((size_t)S * F * 80, "3B emissions")) || (s = ctx->tb_res.ensure((size_t)S * 48 + 48, "3B results")) ||
+        (s = ctx->tb_par.ensure(17 * 8, "3B parameters")))
+        return s;
+    d->bg = sample_bg;
+    d->pix = pixel_intensities;
+    d->pixels = pixels;
+    d->S = S;
+    d->F = F;
+    d->P = P;
+    if (ptr_flags == RFBA_HOST_PTRS) {
+        if ((s = ctx->tb_bg.ensure(nbg * 8, "3B samples")) || (s = ctx->tb_pix.ensure(npix * 8, "3B data")) ||
+            (s = ctx->tb_pixels.ensure((size_t)P * 12, "3B mask")))
+            return s;
+        RFBA_CUDA(cudaMemcpyAsync(ctx->tb_bg.p, sample_bg, nbg * 8, cudaMemcpyHostToDevice, st), "samples copy");
+        RFBA_CUDA(cudaMemcpyAsync(ctx->tb_pix.p, pixel_intensities, npix * 8, cudaMemcpyHostToDevice, st), "data copy");
+        RFBA_CUDA(cudaMemcpyAsync(ctx->tb_pixels.p, pixels, (size_t)P * 12, cudaMemcpyHostToDevice, st), "mask copy");
+        d->bg = static_cast<const double*>(ctx->tb_bg.p);
+        d->pix = static_cast<const double*>(ctx->tb_pix.p);
+        d->pixels = static_cast<const int*>(ctx->tb_pixels.p);
+    }
+    return RFBA_OK;
+}
+
+// One evaluation at `spot` (brightness and blur > 0) on staged data: the four
+// kernels, the samples' results back, their mean plus the priors' derivatives.
+static int threeb_eval(rfba_ctx* ctx, const rfba_3b_model* m, const ThreeBData& d, const double* spot, double* out,
+                       double* log_prob, cudaStream_t st) {
+    const int S = d.S, F = d.F, P = d.P;
+    // parameters: spot, A (row-major), pi
+    double par[17];
+    for (int n = 0; n < 5; ++n) par[n] = spot[n];
+    for (int n = 0; n < 9; ++n) par[5 + n] = m->A[n];
+    for (int n = 0; n < 3; ++n) par[14 + n] = m->pi[n];
+    RFBA_CUDA(cudaMemcpyAsync(ctx->tb_par.p, par, sizeof par, cudaMemcpyHostToDevice, st), "parameter upload");
+    const unsigned int n_pix = (unsigned int)P;
+    const double c0 = n_pix * ::log(2 * M_PI * m->variance) / 2;  // spot_with_background.hh:126-127
+    const double* dpar = static_cast<const double*>(ctx->tb_par.p);
+    int e = launch_threeb(d.bg, d.pix, d.pixels, S, F, P, dpar, m->z_factor, m->variance, c0, dpar + 5, dpar + 14,
+                          static_cast<double*>(ctx->tb_val.p), static_cast<double*>(ctx->tb_der.p),
+                          static_cast<double*>(ctx->tb_em.p), static_cast<double*>(ctx->tb_res.p), st);
+    if (e) return cuda_fail((cudaError_t)e, "3B spot gradient launch");
+    ctx->launches += 4;
+    std::vector<double> res((size_t)S * 6);
+    RFBA_CUDA(cudaMemcpyAsync(res.data(), ctx->tb_res.p, res.size() * 8, cudaMemcpyDeviceToHost, st), "result copy");
+    RFBA_CUDA(cudaStreamSynchronize(st), "synchronize");
+    double sum[5] = {0, 0, 0, 0, 0};
+    for (int i = 0; i < S; ++i)
+        for (int n = 0; n < 5; ++n) sum[n] += res[(size_t)i * 6 + n];
+    // storm.h:431-434: derivatives of the log-normal priors on brightness and blur
+    auto dlln = [&](double x, double mu, double sg) { return -(1 + (std::log(x) - mu) / (sg * sg)) / x; };
+    const double prior[5] = {dlln(spot[0], m->mu_brightness, m->sigma_brightness),
+                             dlln(spot[1], m->mu_blur, m->sigma_blur), 0, 0, 0};
+    for (int n = 0; n < 5; ++n) out[n] = -(sum[n] / (double)S + prior[n]);
+    if (log_prob)
+        for (int i = 0; i < S; ++i) log_prob[i] = res[(size_t)i * 6 + 5];
+    return RFBA_OK;
+}
+
 }  // namespace rfba
 
 using namespace rfba;
@@ -1262,21 +1356,8 @@ int rfba_3b_spot_gradient(rfba_ctx* ctx, const rfba_3b_model* m, const double* s
         set_error("null argument");
         return RFBA_ERR_INVALID;
     }
-    if (S < 1 || F < 1 || P < 1 || (long long)S * F >= (1LL << 31) || !(m->variance > 0) || m->z_factor == 0) {
-        set_error("bad sizes or model (S, F, P >= 1, S*F < 2^31, variance > 0, z_factor != 0)");
-        return RFBA_ERR_INVALID;
-    }
-    if (ptr_flags != RFBA_HOST_PTRS && ptr_flags != RFBA_DEVICE_PTRS) {
-        set_error("ptr_flags must be RFBA_HOST_PTRS or RFBA_DEVICE_PTRS");
-        return RFBA_ERR_INVALID;
-    }
-    for (int n = 0; n < 12; ++n) {
-        const double v = n < 9 ? m->A[n] : m->pi[n - 9];
-        if (!(v >= 0 && v <= 1)) {
-            set_error("transition and initial probabilities must lie in [0, 1]");
-            return RFBA_ERR_INVALID;
-        }
-    }
+    int s;
+    if ((s = threeb_validate(m, S, F, P, ptr_flags))) return s;
     if (spot[0] <= 0 || spot[1] <= 0) {  // multispot5.cc:618-619
         for (int n = 0; n < 5; ++n) out[n] = std::numeric_limits<double>::quiet_NaN();
         return RFBA_OK;
@@ -1284,54 +1365,65 @@ int rfba_3b_spot_gradient(rfba_ctx* ctx, const rfba_3b_model* m, const double* s
     std::lock_guard<std::mutex> lk(ctx->mu);
     RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    int s;
     if ((s = order_streams(ctx, st))) return s;
-    const size_t nbg = (size_t)S * F * P, npix = (size_t)F * P;
-    if ((s = ctx->tb_val.ensure((size_t)P * 8, "3B spot table")) || (s = ctx->tb_der.ensure((size_t)P * 40, "3B spot table")) ||
-        (s = ctx->tb_em.ensure((size_t)S * F * 80, "3B emissions")) || (s = ctx->tb_res.ensure((size_t)S * 48 + 48, "3B results")) ||
-        (s = ctx->tb_par.ensure(17 * 8, "3B parameters")))
-        return s;
-    const double* dbg = sample_bg;
-    const double* dpix = pixel_intensities;
-    const int* dpixels = pixels;
-    if (ptr_flags == RFBA_HOST_PTRS) {
-        if ((s = ctx->tb_bg.ensure(nbg * 8, "3B samples")) || (s = ctx->tb_pix.ensure(npix * 8, "3B data")) ||
-            (s = ctx->tb_pixels.ensure((size_t)P * 12, "3B mask")))
-            return s;
-        RFBA_CUDA(cudaMemcpyAsync(ctx->tb_bg.p, sample_bg, nbg * 8, cudaMemcpyHostToDevice, st), "samples copy");
-        RFBA_CUDA(cudaMemcpyAsync(ctx->tb_pix.p, pixel_intensities, npix * 8, cudaMemcpyHostToDevice, st), "data copy");
-        RFBA_CUDA(cudaMemcpyAsync(ctx->tb_pixels.p, pixels, (size_t)P * 12, cudaMemcpyHostToDevice, st), "mask copy");
-        dbg = static_cast<const double*>(ctx->tb_bg.p);
-        dpix = static_cast<const double*>(ctx->tb_pix.p);
-        dpixels = static_cast<const int*>(ctx->tb_pixels.p);
+    ThreeBData d;
+    if ((s = threeb_stage(ctx, sample_bg, pixel_intensities, pixels, S, F, P, ptr_flags, st, &d))) return s;
+    return threeb_eval(ctx, m, d, spot, out, log_prob, st);
+}
+
+// The spot optimisation of multispot5.cc:1614-1636: ConjugateGradientOnly<5>
+// (conjugate_gradient_only.h) from `spot` with motion limits `limit`, its
+// gradient the spot-gradient evaluation above on data staged once.
+int rfba_3b_optimise_spot(rfba_ctx* ctx, const rfba_3b_model* m, const double* sample_bg,
+                          const double* pixel_intensities, const int* pixels, int S, int F, int P, const double spot[5],
+                          const double limit[5], int max_iterations, double spot_out[5], int* iterations,
+                          int* evaluations, int ptr_flags, void* stream) {
+    if (!ctx || !m || !sample_bg || !pixel_intensities || !pixels || !spot || !limit || !spot_out) {
+        set_error("null argument");
+        return RFBA_ERR_INVALID;
     }
-    // parameters: spot, A (row-major), pi
-    double par[17];
-    for (int n = 0; n < 5; ++n) par[n] = spot[n];
-    for (int n = 0; n < 9; ++n) par[5 + n] = m->A[n];
-    for (int n = 0; n < 3; ++n) par[14 + n] = m->pi[n];
-    RFBA_CUDA(cudaMemcpyAsync(ctx->tb_par.p, par, sizeof par, cudaMemcpyHostToDevice, st), "parameter upload");
-    const unsigned int n_pix = (unsigned int)P;
-    const double c0 = n_pix * ::log(2 * M_PI * m->variance) / 2;  // spot_with_background.hh:126-127
-    const double* dpar = static_cast<const double*>(ctx->tb_par.p);
-    int e = launch_threeb(dbg, dpix, dpixels, S, F, P, dpar, m->z_factor, m->variance, c0, dpar + 5, dpar + 14,
-                          static_cast<double*>(ctx->tb_val.p), static_cast<double*>(ctx->tb_der.p),
-                          static_cast<double*>(ctx->tb_em.p), static_cast<double*>(ctx->tb_res.p), st);
-    if (e) return cuda_fail((cudaError_t)e, "3B spot gradient launch");
-    ctx->launches += 4;
-    std::vector<double> res((size_t)S * 6);
-    RFBA_CUDA(cudaMemcpyAsync(res.data(), ctx->tb_res.p, res.size() * 8, cudaMemcpyDeviceToHost, st), "result copy");
-    RFBA_CUDA(cudaStreamSynchronize(st), "synchronize");
-    double sum[5] = {0, 0, 0, 0, 0};
-    for (int i = 0; i < S; ++i)
-        for (int n = 0; n < 5; ++n) sum[n] += res[(size_t)i * 6 + n];
-    // storm.h:431-434: derivatives of the log-normal priors on brightness and blur
-    auto dlln = [&](double x, double mu, double sg) { return -(1 + (std::log(x) - mu) / (sg * sg)) / x; };
-    const double prior[5] = {dlln(spot[0], m->mu_brightness, m->sigma_brightness),
-                             dlln(spot[1], m->mu_blur, m->sigma_blur), 0, 0, 0};
-    for (int n = 0; n < 5; ++n) out[n] = -(sum[n] / (double)S + prior[n]);
-    if (log_prob)
-        for (int i = 0; i < S; ++i) log_prob[i] = res[(size_t)i * 6 + 5];
+    int s;
+    if ((s = threeb_validate(m, S, F, P, ptr_flags))) return s;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if ((s = order_streams(ctx, st))) return s;
+    ThreeBData d;
+    if ((s = threeb_stage(ctx, sample_bg, pixel_intensities, pixels, S, F, P, ptr_flags, st, &d))) return s;
+    auto grad = [&](const double* x, double* g) -> int {
+        if (x[0] <= 0 || x[1] <= 0) {  // multispot5.cc:618-619
+            for (int n = 0; n < 5; ++n) g[n] = std::numeric_limits<double>::quiet_NaN();
+            return RFBA_OK;
+        }
+        return threeb_eval(ctx, m, d, x, g, nullptr, st);
+    };
+    CgOnly5 cg;
+    if ((s = cg.start(spot, limit, grad))) return s;
+    cg.max_iterations = max_iterations;
+    if ((s = cg.run(grad))) return s;
+    for (int n = 0; n < 5; ++n) spot_out[n] = cg.x[n];
+    if (iterations) *iterations = cg.iterations;
+    if (evaluations) *evaluations = cg.evaluations;
+    return RFBA_OK;
+}
+
+// The same optimiser on the host with a caller-supplied gradient (no device
+// work).
+int rfba_cg_only_run(const double start[5], const double limit[5], int max_iterations, rfba_grad5_fn grad,
+                     void* user, double x_out[5], int* iterations, int* evaluations) {
+    if (!start || !limit || !grad || !x_out) {
+        set_error("null argument");
+        return RFBA_ERR_INVALID;
+    }
+    auto g = [&](const double* x, double* out) -> int { return grad(x, out, user); };
+    CgOnly5 cg;
+    int s;
+    if ((s = cg.start(start, limit, g))) return s;
+    cg.max_iterations = max_iterations;
+    if ((s = cg.run(g))) return s;
+    for (int n = 0; n < 5; ++n) x_out[n] = cg.x[n];
+    if (iterations) *iterations = cg.iterations;
+    if (evaluations) *evaluations = cg.evaluations;
     return RFBA_OK;
 }
 

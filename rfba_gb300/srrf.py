@@ -114,6 +114,9 @@ class Block(ctypes.Structure):
                 ("hi", ctypes.c_int32 * 3), ("out_offset", ctypes.c_int64), ("out_stride", ctypes.c_int64 * 3)]
 
 
+GRAD5_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                            ctypes.c_void_p)
+
 _lib_handle = None
 
 
@@ -165,6 +168,10 @@ def lib():
         dp = ctypes.POINTER(ctypes.c_double)
         L.rfba_3b_spot_gradient.argtypes = [vp, ctypes.POINTER(ThreeBModel), vp, vp, vp, ctypes.c_int, ctypes.c_int,
                                             ctypes.c_int, dp, dp, dp, ctypes.c_int, vp]
+        ipp = ctypes.POINTER(ctypes.c_int)
+        L.rfba_3b_optimise_spot.argtypes = [vp, ctypes.POINTER(ThreeBModel), vp, vp, vp, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_int, dp, dp, ctypes.c_int, dp, ipp, ipp, ctypes.c_int, vp]
+        L.rfba_cg_only_run.argtypes = [dp, dp, ctypes.c_int, GRAD5_FN, vp, dp, ipp, ipp]
         L.rfba_probe_fp32_fma_peak.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
         L.SRRFGradientCalc.argtypes = [fp, ip, fp]
         L.SRRFGetMag.argtypes = []
@@ -273,6 +280,36 @@ def blocks_dosplit(cfg: Config, shape: Sequence[int], max_size, border: int):
     arr = (Block * max(n, 1))()
     _check(lib().rfba_blocks_dosplit(ctypes.byref(cfg), _iptr(dims), _iptr(ms), border, arr, n, ctypes.byref(oe)))
     return arr, n, int(oe.value)
+
+
+def cg_only_run(grad, start, limit, max_iterations: int):
+    """ConjugateGradientOnly<5> (conjugate_gradient_only.h) on the host with a
+    Python gradient function grad(x: ndarray[5]) -> ndarray[5]: returns (final
+    x, line searches, gradient evaluations)."""
+    err = []
+
+    def cb(x, g, user):
+        try:
+            v = np.asarray(grad(np.ctypeslib.as_array(x, (5,)).copy()), np.float64)
+            for i in range(5):
+                g[i] = float(v[i])
+            return 0
+        except Exception as e:  # stop the run, re-raised below
+            err.append(e)
+            return -1
+
+    fn = GRAD5_FN(cb)
+    dp = ctypes.POINTER(ctypes.c_double)
+    st = np.ascontiguousarray(start, np.float64)
+    lim = np.ascontiguousarray(limit, np.float64)
+    out = np.zeros(5)
+    it, ev = ctypes.c_int(), ctypes.c_int()
+    rc = lib().rfba_cg_only_run(st.ctypes.data_as(dp), lim.ctypes.data_as(dp), int(max_iterations), fn, None,
+                                out.ctypes.data_as(dp), ctypes.byref(it), ctypes.byref(ev))
+    if err:
+        raise err[0]
+    _check(rc)
+    return out, it.value, ev.value
 
 
 def combine_psf(sigma: float = 3.5, crop_threshold: float = 1000.0) -> np.ndarray:
@@ -560,6 +597,33 @@ class Context:
                                            out.ctypes.data_as(dp), logp.ctypes.data_as(dp),
                                            RFBA_DEVICE_PTRS if dev else RFBA_HOST_PTRS, _stream_arg(stream, dev)))
         return out, logp
+
+    def optimise_spot_3b(self, model: ThreeBModel, sample_bg, pix, pixels, spot, limit, max_iterations: int,
+                         stream=None):
+        """3B's spot optimisation (multispot5.cc:1614-1636, ConjugateGradientOnly<5>)
+        with the GPU spot gradient on data staged once: returns (final spot [5],
+        line searches, gradient evaluations). Arguments as spot_gradient_3b, plus
+        the per-parameter motion limits and the iteration limit."""
+        dev = not isinstance(sample_bg, np.ndarray)
+        if dev:
+            S, F, P = (int(v) for v in sample_bg.shape)
+            ptrs = [ctypes.c_void_p(t.data_ptr()) for t in (sample_bg, pix, pixels)]
+        else:
+            sample_bg = np.ascontiguousarray(sample_bg, np.float64)
+            pix = np.ascontiguousarray(pix, np.float64)
+            pixels = np.ascontiguousarray(pixels, np.int32)
+            S, F, P = sample_bg.shape
+            ptrs = [ctypes.c_void_p(a.ctypes.data) for a in (sample_bg, pix, pixels)]
+        sp = np.ascontiguousarray(spot, np.float64)
+        lim = np.ascontiguousarray(limit, np.float64)
+        out = np.zeros(5)
+        it, ev = ctypes.c_int(), ctypes.c_int()
+        dp = ctypes.POINTER(ctypes.c_double)
+        _check(lib().rfba_3b_optimise_spot(self.h, ctypes.byref(model), *ptrs, S, F, P, sp.ctypes.data_as(dp),
+                                           lim.ctypes.data_as(dp), int(max_iterations), out.ctypes.data_as(dp),
+                                           ctypes.byref(it), ctypes.byref(ev),
+                                           RFBA_DEVICE_PTRS if dev else RFBA_HOST_PTRS, _stream_arg(stream, dev)))
+        return out, it.value, ev.value
 
     def check(self):
         """Wait for this context's queued work and raise RfbaError for a failure its

@@ -183,3 +183,100 @@ def test_exponent_form_matches_log_space(case):
     if case == "long_bleach":
         g1, lp1 = _forward_exponent_form(gap, off, de, A, pi, per_state=False)
         assert not np.isfinite(lp1).all()
+
+
+def _limit(mu=3.5, sigma=1.0, max_motion=0.5):
+    """The reference's motion limits (multispot5.cc:1484, storm.h:386-389):
+    cg.max_motion x (log-normal std of the brightness prior, 1, 1, 1, 1)."""
+    return max_motion * np.array([np.sqrt((np.exp(sigma ** 2) - 1) * np.exp(2 * mu + sigma ** 2)), 1, 1, 1, 1])
+
+
+OPT_CASES = [  # (seed, S, F, mask shape, start scale, max iterations)
+    (0, 4, 12, (7, 6, 5), (1.0, 1.0, 1, 1, 1), 5),
+    (1, 6, 30, (9, 9, 7), (1.0, 1.0, 1, 1, 1), 20),
+    (2, 3, 20, (8, 8, 6), (0.05, 1.0, 1, 1, 1), 5),   # dim start: the first steps reach brightness <= 0 (NaN)
+    (3, 2, 25, (9, 8, 6), (1.0, 3.0, 1, 1, 1), 8),    # wide start
+]
+
+
+@pytest.mark.parametrize("case", OPT_CASES, ids=[f"seed{c[0]}" for c in OPT_CASES])
+def test_optimiser_reproduces_reference_bits(case):
+    """rfba_cg_only_run (the library's ConjugateGradientOnly<5>) driven by the
+    oracle's gradient retraces the reference's own optimiser driven by the
+    reference's gradient, bit for bit, line search for line search."""
+    if T.ref_lib() is None:
+        pytest.skip("oracle/_ref/libref3b_host.so not built (reference sources absent)")
+    from rfba_gb300 import srrf
+    seed, S, F, shape, scale, iters = case
+    bg, pix, px, spot = T.synthetic_block(seed, S, F, shape)
+    spot = spot * np.array(scale)
+    limit = _limit()
+    want, it_want = T.ref_cg_optimise(bg, pix, px, spot, limit, iters)
+    got, it, ev = srrf.cg_only_run(lambda x: T.spot_neg_prob_diff(bg, pix, px, x), spot, limit, iters)
+    assert it == it_want
+    assert ev >= it + 1
+    assert np.array_equal(got.view(np.uint64), want.view(np.uint64)), (got, want)
+
+
+def test_optimiser_moves_towards_the_spot():
+    """On a block whose data hold the spot being fitted, the optimiser shrinks
+    the gradient and moves the position towards the spot's centre."""
+    from rfba_gb300 import srrf
+    bg, pix, px, spot = T.synthetic_block(4, 6, 40, (9, 9, 7))
+    g0 = T.spot_neg_prob_diff(bg, pix, px, spot)
+    got, it, ev = srrf.cg_only_run(lambda x: T.spot_neg_prob_diff(bg, pix, px, x), spot, _limit(), 30)
+    g1 = T.spot_neg_prob_diff(bg, pix, px, got)
+    assert np.all(np.isfinite(got)) and got[0] > 0 and got[1] > 0
+    assert np.max(np.abs(g1)) < 0.1 * np.max(np.abs(g0))
+
+
+def test_optimiser_callback_error_stops_the_run():
+    from rfba_gb300 import srrf
+    calls = []
+
+    def grad(x):
+        calls.append(1)
+        if len(calls) == 3:
+            raise RuntimeError("gradient failed")
+        return x - 1.0
+
+    with pytest.raises(RuntimeError, match="gradient failed"):
+        srrf.cg_only_run(grad, np.full(5, 3.0), np.ones(5), 10)
+    assert len(calls) == 3
+
+
+def test_optimiser_halves_steps_into_nan_region():
+    """A gradient that is NaN for x0 <= 0 (as the spot gradient is for
+    brightness or blur <= 0) with its minimum beyond that wall: the line search
+    halves the step until the gradient is finite and the run stays finite, on
+    the valid side."""
+    from rfba_gb300 import srrf
+    c = np.array([-5.0, 1.0, 2.0, -1.0, 0.5])
+    seen_nan = []
+
+    def grad(x):
+        if x[0] <= 0:
+            seen_nan.append(1)
+            return np.full(5, np.nan)
+        return x - c
+
+    x0 = np.array([0.5, 0.0, 0.0, 0.0, 0.0])
+    got, it, ev = srrf.cg_only_run(grad, x0, np.full(5, 2.0), 10)
+    assert seen_nan, "the first step should cross into the NaN region"
+    assert np.all(np.isfinite(got)) and got[0] > 0
+    assert np.sum((got - c) ** 2) < np.sum((x0 - c) ** 2)  # it still descends
+
+
+def test_optimiser_stops_on_a_zero_gradient():
+    """A start where the gradient is exactly zero: the allowed step is
+    infinite (the reference's search then steps to NaN, or halves an infinite
+    step forever when the gradient there is NaN); this one stays at the start
+    and finishes, the gradient being under tolerance."""
+    from rfba_gb300 import srrf
+    got, it, ev = srrf.cg_only_run(lambda x: np.zeros(5), np.ones(5), np.ones(5), 7)
+    np.testing.assert_array_equal(got, np.ones(5))
+    assert it == 1 and ev == 1
+    # a gradient that is NaN away from the start and zero at it
+    got, it, ev = srrf.cg_only_run(lambda x: np.zeros(5) if np.all(x == 1) else np.full(5, np.nan), np.ones(5),
+                                   np.ones(5), 7)
+    np.testing.assert_array_equal(got, np.ones(5))

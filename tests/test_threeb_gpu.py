@@ -96,3 +96,27 @@ def test_rejects_probabilities_outside_unit_interval(ctx):
     A[0, 0] = -0.1
     with pytest.raises(RfbaError, match="probabilities"):
         ctx.spot_gradient_3b(ThreeBModel.make(A, T.PI_SHIPPED), bg, pix, px, spot)
+
+
+def _limit(mu=3.5, sigma=1.0, max_motion=0.5):
+    return max_motion * np.array([np.sqrt((np.exp(sigma ** 2) - 1) * np.exp(2 * mu + sigma ** 2)), 1, 1, 1, 1])
+
+
+@pytest.mark.parametrize("seed,S,F,shape,iters", [(0, 4, 12, (7, 6, 5), 5), (1, 6, 30, (9, 9, 7), 20)])
+def test_optimise_spot_matches_host_optimiser(ctx, seed, S, F, shape, iters):
+    """rfba_3b_optimise_spot (the optimiser on the GPU gradient, data staged
+    once) against the same optimiser on the host driven by the oracle's
+    gradient (itself pinned bit for bit to the reference's optimiser in
+    tests/test_threeb_cpu.py). The gradients agree to ~1e-11, so the paths agree
+    to far better than the line search's tolerance."""
+    from rfba_gb300 import srrf
+    bg, pix, px, spot = T.synthetic_block(seed, S, F, shape)
+    want, it_w, ev_w = srrf.cg_only_run(lambda x: T.spot_neg_prob_diff(bg, pix, px, x), spot, _limit(), iters)
+    got, it, ev = ctx.optimise_spot_3b(_model(1.0, 1.0), bg, pix, px, spot, _limit(), iters)
+    np.testing.assert_allclose(got, want, rtol=1e-6, atol=1e-8)
+    assert it == it_w
+    import torch
+    d = [torch.from_numpy(a).cuda() for a in (bg, pix, px)]
+    got2, it2, ev2 = ctx.optimise_spot_3b(_model(1.0, 1.0), *d, spot, _limit(), iters)
+    np.testing.assert_array_equal(got2, got)  # the same device arithmetic either way
+    assert (it2, ev2) == (it, ev)
