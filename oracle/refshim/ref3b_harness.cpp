@@ -6,7 +6,9 @@
 // the composition of SpotNegProbabilityDiffWithSampledBackground::operator()
 // (multispot5.cc:616-664, in a file that cannot be compiled on its own) and of
 // compute_spot_intensity_derivatives (sampled_multispot.h:195-202) is written
-// out here, with the reference's per-thread partial sums done in sequence.
+// out here, with the reference's per-thread partial sums done in sequence, and
+// the spot optimisation loop of multispot5.cc:1624-1636 around the reference's
+// own ConjugateGradientOnly<5> (conjugate_gradient_only.h).
 // The three std::tr1 names the headers use are aliases of their std
 // counterparts, so the reference's `using namespace std; using namespace
 // std::tr1;` resolves without ambiguity in C++11.
