@@ -181,7 +181,8 @@ def refine_drift_sharded(backend, cfg, x, iters: int, start=None, lr: float = 0.
     """rfba_gb300.drift.refine_drift with the map cut into z slabs across the
     group's ranks. Every rank ends with the same shifts; rank 0 writes the
     checkpoint. Returns (DriftState, this rank's slab of the final map
-    [z1-z0][H*mag][W*mag], (z0, z1))."""
+    [z1-z0][H*mag][W*mag] or None when the slab is empty (more ranks than map
+    planes), (z0, z1))."""
     import torch
     rank, world = _rank_world(group)
     T, D, H, W = x.shape
