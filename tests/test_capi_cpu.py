@@ -235,6 +235,25 @@ def test_invalid_arguments_fail_cleanly(built_lib):
         srrf.blocks_gradientcalc(srrf.Config.make(block_size=4), (2, 8, 8, 8))
 
 
+def test_optimiser_entry_points_check_arguments(built_lib):
+    """The 3B optimiser entry points refuse null arguments before any device
+    work, and the host optimiser runs without a device."""
+    from rfba_gb300 import srrf
+    L = srrf.lib()
+    dp = ctypes.POINTER(ctypes.c_double)
+    x = np.ones(5)
+    out = np.zeros(5)
+    assert L.rfba_cg_only_run(x.ctypes.data_as(dp), x.ctypes.data_as(dp), 5, srrf.GRAD5_FN(0), None,
+                              out.ctypes.data_as(dp), None, None) == -1
+    assert "null" in srrf.last_error()
+    m = srrf.ThreeBModel.make(np.eye(3), [1, 0, 0])
+    assert L.rfba_3b_optimise_spot(None, ctypes.byref(m), None, None, None, 1, 1, 1, x.ctypes.data_as(dp),
+                                   x.ctypes.data_as(dp), 5, out.ctypes.data_as(dp), None, None, 0, None) == -1
+    got, it, ev = srrf.cg_only_run(lambda v: 2.0 * (v - 3.0), np.zeros(5), np.full(5, 10.0), 20)
+    np.testing.assert_allclose(got, 3.0, atol=1e-9)
+    assert ev > it >= 1
+
+
 @pytest.mark.skipif(__import__("tests.conftest", fromlist=["HAS_GPU"]).HAS_GPU, reason="checks the no-GPU path")
 def test_context_without_gpu_reports_cuda_error(built_lib):
     from rfba_gb300 import srrf
