@@ -280,3 +280,27 @@ def test_optimiser_stops_on_a_zero_gradient():
     got, it, ev = srrf.cg_only_run(lambda x: np.zeros(5) if np.all(x == 1) else np.full(5, np.nan), np.ones(5),
                                    np.ones(5), 7)
     np.testing.assert_array_equal(got, np.ones(5))
+
+
+def _golden_cases():
+    from pathlib import Path
+    z = np.load(Path(__file__).resolve().parent / "golden" / "threeb_golden.npz")
+    return [{k.split("_", 1)[1]: z[k] for k in z.files if k.startswith(f"c{i}_")} for i in range(int(z["ncases"]))]
+
+
+def test_golden_reproduced_by_oracle_and_optimiser():
+    """tests/golden/threeb_golden.npz holds the reference's own gradient and
+    optimised spot (its headers compiled on the host, make_golden_3b.py): the
+    oracle gives the same gradient bits and the library's optimiser, on the
+    oracle's gradient, the same spot bits and line-search count, without the
+    reference tree."""
+    from rfba_gb300 import srrf
+    limit = _limit()
+    for c in _golden_cases():
+        bg, pix, px, spot = c["bg"], c["pix"], c["px"], c["spot"]
+        g = T.spot_neg_prob_diff(bg, pix, px, spot)
+        assert np.array_equal(g.view(np.uint64), c["grad"].view(np.uint64)), (g, c["grad"])
+        x, it, ev = srrf.cg_only_run(lambda v: T.spot_neg_prob_diff(bg, pix, px, v), spot, limit,
+                                     int(c["iters"]))
+        assert it == int(c["opt_it"])
+        assert np.array_equal(x.view(np.uint64), c["opt"].view(np.uint64)), (x, c["opt"])

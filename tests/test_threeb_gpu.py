@@ -120,3 +120,18 @@ def test_optimise_spot_matches_host_optimiser(ctx, seed, S, F, shape, iters):
     got2, it2, ev2 = ctx.optimise_spot_3b(_model(1.0, 1.0), *d, spot, _limit(), iters)
     np.testing.assert_array_equal(got2, got)  # the same device arithmetic either way
     assert (it2, ev2) == (it, ev)
+
+
+def test_golden_gradient_and_optimiser(ctx):
+    """The GPU against the reference's own results committed in
+    tests/golden/threeb_golden.npz (make_golden_3b.py): gradient to 1e-9 of
+    its largest component, optimised spot to 1e-6."""
+    from pathlib import Path
+    z = np.load(Path(__file__).resolve().parent / "golden" / "threeb_golden.npz")
+    for i in range(int(z["ncases"])):
+        c = {k.split("_", 1)[1]: z[k] for k in z.files if k.startswith(f"c{i}_")}
+        g, _ = ctx.spot_gradient_3b(_model(1.0, 1.0), c["bg"], c["pix"], c["px"], c["spot"])
+        assert np.max(np.abs(g - c["grad"])) <= 1e-9 * np.max(np.abs(c["grad"])), (g, c["grad"])
+        x, it, ev = ctx.optimise_spot_3b(_model(1.0, 1.0), c["bg"], c["pix"], c["px"], c["spot"], _limit(),
+                                         int(c["iters"]))
+        np.testing.assert_allclose(x, c["opt"], rtol=1e-6, atol=1e-8)
