@@ -7,10 +7,12 @@
 # A cubin is GPU code, not host code, so the file built here also runs on the
 # Arm GPU host. baseline/_ref/ is git-ignored: nothing built here is committed.
 #
-# Usage: baseline/build_refgpu.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: baseline/build_refgpu.sh [REFERENCE_ROOT]
+# The tree is $RFBA_REFERENCE_ROOT when set, else the argument, else the
+# development container's mount point (/root/reference).
 set -euo pipefail
 here="$(cd "$(dirname "$0")" && pwd)"
-ref="${1:-/root/reference}"
+ref="${RFBA_REFERENCE_ROOT:-${1:-/root/reference}}"
 src="$ref/RFBA Main/GradientCalc"
 if [ ! -f "$src/kernel.cu" ]; then
   echo "build_refgpu: reference sources not found under $ref; skipping" >&2

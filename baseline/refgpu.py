@@ -52,8 +52,11 @@ def available() -> bool:
     return CUBIN.exists()
 
 
-def build(reference_root: str = "/root/reference") -> Path | None:
-    """Compile the cubin where the reference sources are present."""
+def build(reference_root: str | None = None) -> Path | None:
+    """Compile the cubin where the reference sources are present (found by
+    oracle.refroot.reference_root: RFBA_REFERENCE_ROOT, then the argument)."""
+    from oracle.refroot import reference_root as _root
+    reference_root = _root(reference_root)
     if os.path.isdir(reference_root):
         subprocess.run(["bash", str(HERE / "build_refgpu.sh"), reference_root], check=True)
     return CUBIN if CUBIN.exists() else None

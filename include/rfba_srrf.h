@@ -160,14 +160,19 @@ int rfba_srrf_forward_blocks_plain(rfba_ctx* ctx, const rfba_srrf_config* cfg, c
  * acquisition loop that must not stall on cudaMalloc's device-wide
  * synchronisation, a host whose device memory belongs to its own pool, a plugin
  * environment that forbids device allocation. in and out are device pointers
- * (layouts as rfba_srrf_forward); all temporaries live in one fixed 128 MiB
+ * of the current device, or managed memory (layouts as rfba_srrf_forward;
+ * another GPU's memory is refused with RFBA_ERR_INVALID); all temporaries
+ * live in one fixed 128 MiB
  * device array inside the library, which every GPU that loads the library holds
  * until the process exits. Volumes whose scratch (about 8 bytes per output
  * subvoxel per time point plus small tables) exceeds it are rejected with
  * RFBA_ERR_UNSUPPORTED and a message. The first call on a device looks the
  * array up (cudaGetSymbolAddress) and should come before any stream capture.
  * All calls share the array: calls that overlap on the GPU race, so serialise
- * them. Stream-ordered on `stream` (a cudaStream_t, NULL = the legacy default stream). */
+ * them. Stream-ordered on `stream` (a cudaStream_t, NULL = the legacy default
+ * stream); its tables and descriptors reach the array through small kernels
+ * that carry them as launch parameters, so no host buffer is read after the
+ * call returns. */
 int rfba_srrf_forward_static_scratch(const rfba_srrf_config* cfg, const void* in, rfba_dtype dtype,
                                      const int dims[4], float* out, void* stream);
 

@@ -10,10 +10,12 @@
 # loop). GradientCalc.cpp compiles from where it lies. Only the built library
 # lands in oracle/_ref/, which is git-ignored.
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]
+# The tree is $RFBA_REFERENCE_ROOT when set, else the argument, else the
+# development container's mount point (/root/reference).
 set -euo pipefail
 here="$(cd "$(dirname "$0")" && pwd)"
-ref="${1:-/root/reference}"
+ref="${RFBA_REFERENCE_ROOT:-${1:-/root/reference}}"
 src="$ref/RFBA Main/GradientCalc"
 if [ ! -f "$src/kernel.cu" ]; then
   echo "build_ref: reference sources not found under $ref; skipping" >&2

@@ -105,9 +105,12 @@ def build(force: bool = False) -> Path:
     return LIB_PATH
 
 
-def build_ref(reference_root: str = "/root/reference") -> Path | None:
+def build_ref(reference_root: str | None = None) -> Path | None:
     """Compile the reference's own sources as host code (oracle/build_ref.sh);
-    returns None when the reference tree is absent."""
+    returns None when the reference tree is absent. The tree is found by
+    oracle.refroot.reference_root (RFBA_REFERENCE_ROOT, then the argument)."""
+    from oracle.refroot import reference_root as _root
+    reference_root = _root(reference_root)
     if not os.path.isdir(reference_root):
         return None
     subprocess.run(["bash", str(HERE / "build_ref.sh"), reference_root], check=True)

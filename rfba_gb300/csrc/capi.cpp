@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "cg_only.h"
+#include "devbuf.h"
 #include "srrf_internal.h"
 
 namespace rfba {
@@ -70,35 +71,6 @@ static int cuda_fail(cudaError_t e, const char* what) {
         cudaError_t e__ = (call);                      \
         if (e__ != cudaSuccess) return cuda_fail(e__, what); \
     } while (0)
-
-// Device buffer that grows and is kept. Growing waits for all queued work
-// first, since kernels of earlier calls may still read the old allocation.
-struct DevBuf {
-    void* p = nullptr;
-    size_t n = 0;
-    int ensure(size_t bytes, const char* what) {
-        if (bytes <= n) return RFBA_OK;
-        if (p) {
-            cudaDeviceSynchronize();
-            cudaFree(p);
-        }
-        p = nullptr;
-        n = 0;
-        size_t want = std::max(bytes, (size_t)256);
-        cudaError_t e = cudaMalloc(&p, want);
-        if (e != cudaSuccess) {
-            p = nullptr;
-            return cuda_fail(e, what);
-        }
-        n = want;
-        return RFBA_OK;
-    }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
-    }
-};
 
 struct PlanCache {
     bool valid = false;

@@ -17,6 +17,13 @@
 // contraction. One deliberate difference: a line search whose allowed step is
 // not finite (direction all zero or NaN) returns without moving instead of
 // halving an infinite step forever.
+//
+// Licence and attribution. The step order above is that of B-cubed's
+// conjugate_gradient_only.h, Copyright (C) 2009, 2010, 2011 Edward Rosten and
+// Susan Cox, distributed under the GNU Lesser General Public License, version 3
+// or (at your option) any later version. Because this header restates that
+// algorithm step for step, it is offered under the same terms
+// (LGPL-3.0-or-later); the rest of the library is unaffected.
 #pragma once
 
 #include <cmath>
@@ -83,68 +90,68 @@ struct CgOnly5 {
     int line_search(Grad& grad) {
         ++iterations;
         for (int i = 0; i < 5; ++i) new_g[i] = g[i];
-        double f1 = dot(g, mh);
-        if (f1 > 0) return 0;  // not a descent direction: stay
-        double max_step = HUGE_VAL;
+        double slope_lo = dot(g, mh);
+        if (slope_lo > 0) return 0;  // not a descent direction: stay
+        double step_cap = HUGE_VAL;
         for (int i = 0; i < 5; ++i) {
             const double v = std::fabs(dmax[i] / h[i]);
-            max_step = (v < max_step) ? v : max_step;
+            step_cap = (v < step_cap) ? v : step_cap;
         }
         // With every direction component 0 or NaN the allowed step is not
         // finite; halving it never reaches the exit below and the reference's
         // search would not return. Stop this line search without moving.
-        if (!(max_step < HUGE_VAL)) return 0;
-        const double full_max_step = max_step;
+        if (!(step_cap < HUGE_VAL)) return 0;
+        const double first_step = step_cap;
         for (;;) {
-            if (int e = eval_along(grad, max_step, new_g)) return e;
+            if (int e = eval_along(grad, step_cap, new_g)) return e;
             if (!any_nan(new_g)) break;
-            max_step /= 2;
-            if (max_step < full_max_step * ls_tolerance) return 0;
+            step_cap /= 2;
+            if (step_cap < first_step * ls_tolerance) return 0;
         }
-        double f2 = dot(new_g, mh);
-        if (f2 < 0) {  // still descending at the largest step: take it
-            for (int i = 0; i < 5; ++i) x[i] += max_step * mh[i];
+        double slope_hi = dot(new_g, mh);
+        if (slope_hi < 0) {  // still descending at the largest step: take it
+            for (int i = 0; i < 5; ++i) x[i] += step_cap * mh[i];
             return 0;
         }
-        double s1 = 0, s2 = max_step, s_new = max_step;
-        int updates[2] = {0, 0};
+        double lo = 0, hi = step_cap, step = step_cap;
+        int moved[2] = {0, 0};
         // the bracket shrinks every step (bisection at least every other one),
         // so the cap is never reached by a finite gradient; it only bounds the
         // host loop
         for (int n = 0; n < kMaxBracketSteps &&
-                        std::fabs(s1 - s2) > std::fabs(s1 + s2) * ls_tolerance + ls_epsilon;
+                        std::fabs(lo - hi) > std::fabs(lo + hi) * ls_tolerance + ls_epsilon;
              ++n) {
-            if (updates[0] != updates[1] && updates[0] != 0) {
-                s_new = s1 + f1 * (s2 - s1) / (f1 - f2);  // secant on the directional derivative
-                if (int e = eval_along(grad, s_new, new_g)) return e;
-                const double f_new = dot(new_g, mh);
-                updates[0] = updates[1];
-                if (f_new == 0) break;
-                if (f_new < 0) {
-                    s1 = s_new;
-                    f1 = f_new;
-                    updates[1] = 1;
+            if (moved[0] != moved[1] && moved[0] != 0) {
+                step = lo + slope_lo * (hi - lo) / (slope_lo - slope_hi);  // secant on the directional derivative
+                if (int e = eval_along(grad, step, new_g)) return e;
+                const double slope = dot(new_g, mh);
+                moved[0] = moved[1];
+                if (slope == 0) break;
+                if (slope < 0) {
+                    lo = step;
+                    slope_lo = slope;
+                    moved[1] = 1;
                 } else {
-                    s2 = s_new;
-                    f2 = f_new;
-                    updates[1] = 2;
+                    hi = step;
+                    slope_hi = slope;
+                    moved[1] = 2;
                 }
             } else {
-                s_new = (s1 + s2) / 2;
-                if (int e = eval_along(grad, s_new, new_g)) return e;
-                const double f_new = dot(new_g, mh);
-                if (f_new < 0) {
-                    s1 = s_new;
-                    f1 = f_new;
-                    updates[0] = 1;
+                step = (lo + hi) / 2;
+                if (int e = eval_along(grad, step, new_g)) return e;
+                const double slope = dot(new_g, mh);
+                if (slope < 0) {
+                    lo = step;
+                    slope_lo = slope;
+                    moved[0] = 1;
                 } else {
-                    s2 = s_new;
-                    f2 = f_new;
-                    updates[0] = 2;
+                    hi = step;
+                    slope_hi = slope;
+                    moved[0] = 2;
                 }
             }
         }
-        for (int i = 0; i < 5; ++i) x[i] += mh[i] * s_new;
+        for (int i = 0; i < 5; ++i) x[i] += mh[i] * step;
         return 0;
     }
 

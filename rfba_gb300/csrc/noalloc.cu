@@ -16,6 +16,11 @@
 // contents behind, so calls whose work overlaps on the GPU (different streams,
 // or different host threads) race; serialise them. The work counter that must
 // start at zero is cleared by each call on its stream.
+//
+// Nothing is copied from host memory: the block descriptor, the tile list, the
+// voxel prefix and the weight tables reach the scratch through small set-up
+// kernels that carry them in their launch parameters, so the call never reads
+// a host buffer after it has returned and never waits on a pageable copy.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -66,13 +71,59 @@ int scratch_address(void** out) {
     return RFBA_OK;
 }
 
-bool is_device_ptr(const void* p) {
+// Device memory of device `dev` (the current one), or managed memory, which
+// every device can address. Memory of another GPU is refused: without peer
+// access the kernels would fault on it, with peer access they would read and
+// write across the link.
+bool is_device_ptr(const void* p, int dev) {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    if (a.type == cudaMemoryTypeManaged) return true;
+    return a.type == cudaMemoryTypeDevice && a.device == dev;
+}
+
+using rfba::BlockDev;
+using rfba::TileDesc;
+
+// Set-up kernels: descriptors and tables travel in the launch parameters.
+struct SetupArgs {
+    BlockDev block;
+    long long prefix[2];
+    int ntile[3];
+    int ntiles;
+};
+
+__global__ void static_setup_kernel(const SetupArgs a, BlockDev* blk, TileDesc* tiles, long long* prefix,
+                                    unsigned int* counter) {
+    const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i0 == 0) {
+        *blk = a.block;
+        prefix[0] = a.prefix[0];
+        prefix[1] = a.prefix[1];
+    }
+    if (i0 < 64) counter[i0] = 0u;
+    // tile order: x fastest, then y, then z
+    for (int i = i0; i < a.ntiles; i += gridDim.x * blockDim.x) {
+        TileDesc d;
+        d.block = 0;
+        d.tx = i % a.ntile[0];
+        d.ty = (i / a.ntile[0]) % a.ntile[1];
+        d.tz = i / (a.ntile[0] * a.ntile[1]);
+        tiles[i] = d;
+    }
+}
+
+constexpr int kChunkWords = 960;  // 3.8 KB of parameters per launch
+struct TableChunk {
+    int n;
+    float w[kChunkWords];
+};
+
+__global__ void static_tables_kernel(const TableChunk c, float* dst) {
+    for (int i = threadIdx.x; i < c.n; i += blockDim.x) dst[i] = c.w[i];
 }
 
 }  // namespace
@@ -87,8 +138,31 @@ extern "C" int rfba_srrf_forward_static_scratch(const rfba_srrf_config* cfg, con
     if (dtype != RFBA_F32 && dtype != RFBA_U16) return fail(RFBA_ERR_INVALID, "dtype must be RFBA_F32 or RFBA_U16");
     for (int a = 0; a < 4; ++a)
         if (dims[a] < 1) return fail(RFBA_ERR_INVALID, "dims must be positive");
-    if (!is_device_ptr(in) || !is_device_ptr(out))
-        return fail(RFBA_ERR_INVALID, "the static-scratch forward takes device pointers for input and output");
+    // sizes in 64 bits; the fixed scratch is checked before any host work
+    const long long plane = (long long)dims[0] * dims[1] * dims[2];
+    if (plane * dims[3] > (1LL << 40)) return fail(RFBA_ERR_INVALID, "input too large");
+    long long nreg64[3];
+    for (int a = 0; a < 3; ++a) nreg64[a] = (long long)dims[a] * cfg->mag[a];
+    const long long vox64 = nreg64[0] * nreg64[1] * nreg64[2];
+    const long long stack64 = vox64 * dims[3] * (long long)sizeof(float);
+    // the two stacks alone (the tables, descriptors and tiles come on top)
+    if (2 * stack64 > (long long)kStaticScratchBytes || nreg64[0] > INT32_MAX / 2 || nreg64[1] > INT32_MAX / 2 ||
+        nreg64[2] > INT32_MAX / 2) {
+        char buf[256];
+        std::snprintf(buf, sizeof buf,
+                      "volume needs at least %lld bytes of scratch; the static scratch holds %zu bytes "
+                      "(use rfba_srrf_forward for this size)",
+                      2 * stack64, kStaticScratchBytes);
+        return fail(RFBA_ERR_UNSUPPORTED, buf);
+    }
+    int cur_dev = 0;
+    {
+        const cudaError_t e = cudaGetDevice(&cur_dev);
+        if (e != cudaSuccess) return fail(RFBA_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    }
+    if (!is_device_ptr(in, cur_dev) || !is_device_ptr(out, cur_dev))
+        return fail(RFBA_ERR_INVALID,
+                    "the static-scratch forward takes device pointers of the current device for input and output");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
 
     // ring plan and tables
@@ -126,17 +200,14 @@ extern "C" int rfba_srrf_forward_static_scratch(const rfba_srrf_config* cfg, con
     b.out_stride[0] = 1;
     b.out_stride[1] = b.hi[0];
     b.out_stride[2] = (long long)b.hi[0] * b.hi[1];
-    std::vector<TileDesc> tiles;
-    for (int tz = 0; tz < b.ntile[2]; ++tz)
-        for (int ty = 0; ty < b.ntile[1]; ++ty)
-            for (int tx = 0; tx < b.ntile[0]; ++tx) tiles.push_back({0, tx, ty, tz});
+    const long long ntiles64 = (long long)b.ntile[0] * b.ntile[1] * b.ntile[2];
     const long long prefix[2] = {0, b.vox};
 
     // scratch layout: tables | block | tiles | prefix | counter | radiality | intensity
     const size_t o_tab = 0;
     const size_t o_blk = align256(o_tab + words.size() * sizeof(float));
     const size_t o_til = align256(o_blk + sizeof(BlockDev));
-    const size_t o_pre = align256(o_til + tiles.size() * sizeof(TileDesc));
+    const size_t o_pre = align256(o_til + (size_t)ntiles64 * sizeof(TileDesc));
     const size_t o_cnt = align256(o_pre + sizeof(prefix));
     const size_t o_rad = align256(o_cnt + 256);
     const size_t stack_bytes = (size_t)b.vox * (size_t)T * sizeof(float);
@@ -159,17 +230,30 @@ extern "C" int rfba_srrf_forward_static_scratch(const rfba_srrf_config* cfg, con
         if (e == cudaSuccess) return RFBA_OK;
         return fail(RFBA_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
     };
-    if ((s = cuda_ok(cudaMemcpyAsync(sc + o_tab, words.data(), words.size() * sizeof(float), cudaMemcpyHostToDevice, st),
-                     "tables upload")))
-        return s;
-    if ((s = cuda_ok(cudaMemcpyAsync(sc + o_blk, &b, sizeof b, cudaMemcpyHostToDevice, st), "block upload"))) return s;
-    if ((s = cuda_ok(cudaMemcpyAsync(sc + o_til, tiles.data(), tiles.size() * sizeof(TileDesc), cudaMemcpyHostToDevice,
-                                     st),
-                     "tiles upload")))
-        return s;
-    if ((s = cuda_ok(cudaMemcpyAsync(sc + o_pre, prefix, sizeof prefix, cudaMemcpyHostToDevice, st), "prefix upload")))
-        return s;
-    if ((s = cuda_ok(cudaMemsetAsync(sc + o_cnt, 0, 256, st), "counter reset"))) return s;
+    // tables, descriptors, tile list and the cleared work counter, written by
+    // kernels from their launch parameters
+    for (size_t w0 = 0; w0 < words.size(); w0 += kChunkWords) {
+        TableChunk c;
+        c.n = (int)std::min<size_t>(kChunkWords, words.size() - w0);
+        std::memcpy(c.w, words.data() + w0, (size_t)c.n * sizeof(float));
+        static_tables_kernel<<<1, 256, 0, st>>>(c, reinterpret_cast<float*>(sc + o_tab) + w0);
+        if ((s = cuda_ok(cudaGetLastError(), "tables set-up"))) return s;
+    }
+    {
+        SetupArgs a;
+        std::memset(&a, 0, sizeof a);
+        a.block = b;
+        a.prefix[0] = prefix[0];
+        a.prefix[1] = prefix[1];
+        for (int k = 0; k < 3; ++k) a.ntile[k] = b.ntile[k];
+        a.ntiles = (int)ntiles64;
+        const int nb = (int)std::min<long long>(64, std::max<long long>(1, (ntiles64 + 255) / 256));
+        static_setup_kernel<<<nb, 256, 0, st>>>(a, reinterpret_cast<BlockDev*>(sc + o_blk),
+                                                reinterpret_cast<TileDesc*>(sc + o_til),
+                                                reinterpret_cast<long long*>(sc + o_pre),
+                                                reinterpret_cast<unsigned int*>(sc + o_cnt));
+        if ((s = cuda_ok(cudaGetLastError(), "descriptor set-up"))) return s;
+    }
 
     RadParams rp;
     std::memset(&rp, 0, sizeof rp);
@@ -213,7 +297,7 @@ extern "C" int rfba_srrf_forward_static_scratch(const rfba_srrf_config* cfg, con
     rp.smem_table_words = tl.words;
     rp.blocks = reinterpret_cast<const BlockDev*>(sc + o_blk);
     rp.tiles = reinterpret_cast<const TileDesc*>(sc + o_til);
-    rp.ntiles = (int)tiles.size();
+    rp.ntiles = (int)ntiles64;
     rp.rad_stack = reinterpret_cast<float*>(sc + o_rad);
     rp.int_stack = reinterpret_cast<float*>(sc + o_int);
     rp.work_counter = reinterpret_cast<unsigned int*>(sc + o_cnt);

@@ -106,7 +106,9 @@ def legacy_ref(x: np.ndarray, conf) -> np.ndarray:
     return out, ini
 
 
-def main(ref_root: str = "/root/reference"):
+def main(ref_root: str | None = None):
+    from oracle.refroot import reference_root
+    ref_root = reference_root(ref_root)
     O.build()
     if O.build_ref(ref_root) is None:
         raise SystemExit("reference sources not found; fixtures need the reference")

@@ -50,7 +50,8 @@ def test_rejects_mismatched_and_bad_files(cli, tmp_path):
 
 
 def test_reads_reference_test_data(cli):
-    p = Path("/root/reference/Test Data/Microbubule.tif")
+    from oracle.refroot import reference_root
+    p = Path(reference_root(), "Test Data", "Microbubule.tif")
     if not p.exists():
         pytest.skip("reference test data not present")
     r = subprocess.run([cli, "--info", str(p)], capture_output=True, text=True, check=True)

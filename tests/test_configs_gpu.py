@@ -4,8 +4,9 @@ shape and model, rfba_gb300/synth.py), and regions of it near the low corner,
 in the middle and near the high corner are compared with the FP64 oracle
 computed on the same full-size input. Tolerances, relative L-inf with identical
 NaN masks: 1e-5 for the temporal mean, 1e-4 for TRAC maps. The large series
-runs 20 of its 200 volumes (all of its spatial extent) to keep the test short;
-the batching series is the 160^3 variant with 216 blocks."""
+runs in full (200 volumes, TRAC-4) with its map cut into 16-plane z slices, the
+checked regions straddling slice boundaries; the batching series is the 160^3
+variant with 216 blocks."""
 import numpy as np
 import pytest
 
@@ -108,6 +109,37 @@ def test_large_trac4_20_volumes(ctx, oracle_mod):
     _check_regions(got, x.astype(np.float32), oracle_mod, kw,
                    [((16, 16, 8), (24, 24, 14)), ((510, 510, 126), (518, 518, 132)),
                     ((1000, 1004, 240), (1008, 1012, 246))], 1e-4, "large 20 x 256x256x128, mag 4x4x2, TRAC-4")
+
+
+def test_large_trac4_all_200_volumes(oracle_mod):
+    """The large configuration in full: 200 x 256x256x128 u16, mag 4x4x2, TRAC-4
+    ITC 0 (kernel.cu:469-500 with order 4). The radiality + intensity stacks of
+    the whole map would take 430 GB, so the forward cuts the map into z slices
+    under the context's scratch budget, each slice computed for all 200
+    volumes. The budget here, 16 planes x 1024 x 1024 subvoxels x 200 volumes x
+    8 bytes, fixes the slices at z = 16 k; every checked region below straddles a
+    slice boundary (z 16, 128, 240) and together they cover the low corner, the
+    middle and the high corner of the map plus seeded interior boxes."""
+    from rfba_gb300 import srrf
+    x, _ = _workload("large")
+    assert x.shape == (200, 128, 256, 256)
+    kw = dict(mag=(4, 4, 2), method=3, itc=0, trac_order=4, **SMOOTH)
+    budget = 16 * 1024 * 1024 * 200 * 8
+    c = srrf.Context(0, budget)
+    try:
+        got = c.forward(srrf.Config.make(**kw), x)
+    finally:
+        c.close()
+    rng = np.random.default_rng(2026)
+    regions = [((16, 16, 12), (24, 24, 20)), ((508, 510, 124), (516, 518, 132)),
+               ((1000, 1004, 236), (1008, 1012, 244))]
+    for _ in range(5):  # interior boxes, each across one of the 15 inner slice boundaries
+        x0, y0 = (int(v) for v in rng.integers(12, 1004, size=2))
+        zb = 16 * int(rng.integers(1, 16))
+        regions.append(((x0, y0, zb - 4), (x0 + 8, y0 + 8, zb + 4)))
+    xf = x.astype(np.float32)
+    del x
+    _check_regions(got, xf, oracle_mod, kw, regions, 1e-4, "large 200 x 256x256x128, mag 4x4x2, TRAC-4")
 
 
 def test_mid_trac2_itc1_reduced_t(ctx, oracle_mod):

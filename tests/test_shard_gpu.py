@@ -73,8 +73,11 @@ def test_region_rejects_bad_boxes(ctx):
                                        out=torch.empty(1024, device="cuda"))
 
 
-@pytest.mark.parametrize("world", [2, 3])
+@pytest.mark.parametrize("world", [2, 3, 8])
 def test_block_partition_puts_back_the_map(ctx, world):
+    """Each rank computes its blocks from its own input box (shard.crop: the
+    union of its blocks' sub-volumes with their halos, origins rebased to the
+    box). With 8 ranks one rank's box starts off the origin on every axis."""
     import torch
     from rfba_gb300 import shard, srrf
     cfg = srrf.Config.make(mag=2, method=3, itc=0, trac_order=2, block_size=(12, 12, 12), **SHIPPED)
@@ -85,10 +88,15 @@ def test_block_partition_puts_back_the_map(ctx, world):
     total = D * H * W * 8
     one = ctx.forward_blocks(cfg, xd, blocks, n, total).cpu().numpy()
     out = np.zeros(total, np.float32)
+    box_lo = []
     for r in range(world):
         idx, packed = shard.forward_local(ctx, cfg, xd, blocks, n, r, world)
+        if idx:
+            box_lo.append(shard.input_box(blocks, idx)[0])
         shard.put_back(out, blocks, idx, packed)
     np.testing.assert_array_equal(out, one)
+    if world == 8:
+        assert any(all(v > 0 for v in lo) for lo in box_lo), box_lo
 
 
 def test_sharded_drift_one_process_equals_drift(ctx):
