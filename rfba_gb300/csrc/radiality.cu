@@ -204,7 +204,7 @@ __device__ __forceinline__ float4 gradient_generic(const float* base, int NIX, i
 }
 
 template <int MZ, int CZ, typename Tin, bool WIDE>
-__global__ void __launch_bounds__(WIDE ? kMaxThreads : 128, WIDE ? 2 : 3)
+__global__ void __launch_bounds__(WIDE ? kMaxThreads : 128, WIDE ? 2 : RFBA_FWD_CTAS)
     radiality_kernel(const RadParams p, const __grid_constant__ CUtensorMap tmap) {
     constexpr int FZ = MZ * CZ;
     constexpr int NW = CZ + 4;

@@ -21,9 +21,17 @@ constexpr int kMaxGradRange = 3;
 constexpr int kAdjRows = 16;
 constexpr int kAdjThreads = kTileX * kAdjRows / 2;
 
-// Coarse z cells per tile for a given z magnification (FZ = MZ * CZ).
+// Coarse z cells per tile for a given z magnification (FZ = MZ * CZ), and the
+// forward kernel's resident CTAs per SM (launch bound; 128-thread tiles).
+// Compile-time tuning knobs: -DRFBA_CZ_MZ2=n / -DRFBA_FWD_CTAS=n.
+#ifndef RFBA_CZ_MZ2
+#define RFBA_CZ_MZ2 8
+#endif
+#ifndef RFBA_FWD_CTAS
+#define RFBA_FWD_CTAS 3
+#endif
 constexpr int cz_for_mag(int mz) {
-    return mz == 1 ? 8 : mz == 2 ? 8 : mz == 3 ? 5 : mz == 4 ? 4 : mz == 5 ? 3 : 2;
+    return mz == 1 ? 8 : mz == 2 ? RFBA_CZ_MZ2 : mz == 3 ? 5 : mz == 4 ? 4 : mz == 5 ? 3 : 2;
 }
 
 // Coarse z cells per tile of the adjoint kernel (it holds twice the register
