@@ -281,6 +281,62 @@ typedef int (*rfba_grad5_fn)(const double x[5], double grad[5], void* user);
 int rfba_cg_only_run(const double start[5], const double limit[5], int max_iterations, rfba_grad5_fn grad,
                      void* user, double x_out[5], int* iterations, int* evaluations);
 
+/* get_spot_pixels (RFBA Main/multispot5.cc:1001-1020) for K spots: the mask of
+ * spot k is every pixel whose position equals the spot's rounded centre
+ * (half away from zero) plus an offset of getBall(blur * 6 + 1)
+ * (multispot5.cc:1259-1272), in the ball's order; pixels [P][3] (x, y, z) must
+ * be sorted by (z, y, x) as the reference's pixel list is. Writes
+ * mask_offsets[K + 1] and, when mask_pixels is not NULL, up to cap pixel
+ * indices; *nnz receives the total. Host memory, no device work. */
+int rfba_3b_spot_masks(const int* pixels, int P, const double* spots, int K, int* mask_offsets, int* mask_pixels,
+                       long long cap, long long* nnz);
+
+/* GibbsSampler2 (RFBA Main/sampled_multispot.h:360-690) on the GPU: a fresh
+ * sampler (every spot off in every frame) draws n_draws samples, each after
+ * `sweeps` passes over the spots (main.gibbs.samples and gibbs.mixing_iterations
+ * in multispot5.cfg). Per spot: remove it over its mask where it is on, the
+ * frames' log probabilities with it on and off over the mask, the 3-state
+ * forward filter, a backward draw of its states, add it back. Spot k's
+ * intensity is spot_shape at every pixel (storm.h:229-235, model->z_factor);
+ * masks as rfba_3b_spot_masks writes them (mask_offsets[K + 1], mask_pixels).
+ * pixel_intensities [F][P], pixels [P][3], spots [K][5] (brightness, blur, x,
+ * y, z). Outputs (either may be NULL): states [n_draws][K][F] (0 on, 1 off,
+ * 2 bleached) and sample_intensities [n_draws][F][P], the sampler's
+ * intensities after each draw (sampled_multispot.h:684-689); with
+ * exclude_spot = s >= 0 spot s's intensity is taken off every pixel of the
+ * frames where it is on, as multispot5.cc:1606-1608 does before the spot
+ * optimiser uses the draws as background samples. Random numbers:
+ * Philox4x32-10 keyed by seed (the reference's distribution, not its MT19937
+ * stream). 1 <= F <= 2048. Synchronous. */
+int rfba_3b_gibbs_sample(rfba_ctx* ctx, const rfba_3b_model* model, const double* pixel_intensities, const int* pixels,
+                         const double* spots, const int* mask_offsets, const int* mask_pixels, int K, int F, int P,
+                         int sweeps, int n_draws, unsigned long long seed, int exclude_spot, uint8_t* states,
+                         double* sample_intensities, int ptr_flags, void* stream);
+
+/* One sweep of the sampler above from all spots off, with what each spot's
+ * draw was made from: log_prob [K][F][2] the frame's log probability with the
+ * spot on and off (SpotWithBackgroundMasked, spot_with_background.hh:98-137)
+ * and filtered [K][F][3] the forward filter's state distribution per frame
+ * (forward_algorithm_delta2, forward_algorithm.h:385-431, normalised), given
+ * the states the sweep drew for the spots before it; states [K][F]. Any output
+ * may be NULL. Synchronous. */
+int rfba_3b_gibbs_trace(rfba_ctx* ctx, const rfba_3b_model* model, const double* pixel_intensities, const int* pixels,
+                        const double* spots, const int* mask_offsets, const int* mask_pixels, int K, int F, int P,
+                        unsigned long long seed, uint8_t* states, double* log_prob, double* filtered, int ptr_flags,
+                        void* stream);
+
+/* NegativeFreeEnergy::compute_with_mask (RFBA Main/multispot5.cc:335-405): the
+ * model's negative free energy by slow-growth thermodynamic integration, the
+ * Gibbs sampler above drawing `samples` times (add_remove.thermo.samples) with
+ * the noise variance grown as variance_from_sample and the derivative by a
+ * five-point stencil, plus the log-normal priors; *value is what
+ * compute_with_mask returns. residuals [samples] (may be NULL) receives each
+ * draw's sum of squared residuals over all frames and pixels. Synchronous. */
+int rfba_3b_free_energy(rfba_ctx* ctx, const rfba_3b_model* model, const double* pixel_intensities, const int* pixels,
+                        const double* spots, const int* mask_offsets, const int* mask_pixels, int K, int F, int P,
+                        int samples, int sweeps, unsigned long long seed, double* value, double* residuals,
+                        int ptr_flags, void* stream);
+
 /* Device-side failure check. No counterpart in the reference (GradientCalc.cpp
  * and kernel.cu check no CUDA status; every call returns 0). Waits for the
  * work the context last enqueued and reports failures its kernels recorded

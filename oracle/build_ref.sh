@@ -43,3 +43,11 @@ main="$ref/RFBA Main"
 g++ -O2 -std=c++11 -ffp-contract=off -fno-fast-math -fPIC -shared -w \
   -I "$main/include" -I "$main" "$here/refshim/ref3b_harness.cpp" -o "$out/libref3b_host.so"
 echo "build_ref: built $out/libref3b_host.so"
+# The 3B Gibbs sampler (sampled_multispot.h's GibbsSampler2 with MT19937 from
+# mersenne.cpp) and the free-energy loop around it, through
+# oracle/refshim/ref3b_gibbs_harness.cpp. image3d.h qualifies Ref3D's members
+# redundantly, which g++ accepts with -fpermissive.
+g++ -O2 -std=c++11 -fpermissive -ffp-contract=off -fno-fast-math -fPIC -shared -w \
+  -I "$main/include" -I "$main" "$here/refshim/ref3b_gibbs_harness.cpp" "$main/mersenne.cpp" \
+  -o "$out/libref3b_gibbs_host.so" -lpthread
+echo "build_ref: built $out/libref3b_gibbs_host.so"

@@ -195,6 +195,38 @@ void set_error(const std::string& msg);
 // FP32 FMA throughput probe (probe.cu): best of three timed launches, TFLOP/s.
 int probe_fp32_fma(int device, double* tflops);
 
+// 3B Gibbs sampling of the spot states (gibbs.cu): one chain per launch,
+// frames dealt out to co-resident CTAs (cooperative launch).
+struct GibbsParams {
+    const double* pix;        // [F][P] data
+    const double* si;         // [K][P] each spot's intensity at every pixel
+    const int* moff;          // [K + 1] mask offsets
+    const int* midx;          // mask pixel indices
+    int K, F, P;
+    double A[9], pi[3];
+    double variance;          // noise variance (when var_draw is null)
+    const double* var_draw;   // [n_draws] variance of each draw, or null
+    int sweeps;               // sweeps over all spots per draw
+    int n_draws;
+    unsigned long long seed;
+    unsigned long long draw_base;  // counter offset of the first draw
+    unsigned char* state;     // [K][F] current states, in/out
+    double* cur;              // [F][P] current sample intensities, in/out
+    double* em;               // [F][4] scratch: emission mantissas / exponents
+    unsigned int* bar;        // grid barrier: count, generation (zeroed)
+    unsigned long long* err;  // barrier failures (site << 56 | spot)
+    unsigned char* out_state;  // [n_draws][K][F] or null
+    double* out_int;           // [n_draws][F][P] or null
+    int exclude_spot;          // >= 0: out_int without that spot where it is on (all pixels)
+    double* out_err;           // [n_draws][F] sums of squared residuals, or null
+    double* rec_lp;            // [K][F][2] log p(on), log p(off) of the first sweep, or null
+    double* rec_filt;          // [K][F][3] filtering distribution of the first sweep, or null
+};
+size_t gibbs_smem_bytes(int F);
+int gibbs_max_blocks(int F, int* out);
+int launch_gibbs(const GibbsParams& p, int grid, void* stream);
+int launch_spot_intensity(const int* pixels, int P, const double* spots, int K, double zf, double* out, void* stream);
+
 // 3B spot gradient (threeb.cu): spot voxel table, emission sums per (sample,
 // frame), forward algorithm per sample; res[s] = (gradient[5], log probability).
 int launch_threeb(const double* bg, const double* pix, const int* pixels, int S, int F, int P, const double* phi_dev,

@@ -169,6 +169,17 @@ def lib():
         L.rfba_3b_spot_gradient.argtypes = [vp, ctypes.POINTER(ThreeBModel), vp, vp, vp, ctypes.c_int, ctypes.c_int,
                                             ctypes.c_int, dp, dp, dp, ctypes.c_int, vp]
         ipp = ctypes.POINTER(ctypes.c_int)
+        ull = ctypes.c_ulonglong
+        L.rfba_3b_spot_masks.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int, vp, vp, ctypes.c_longlong,
+                                         ctypes.POINTER(ctypes.c_longlong)]
+        L.rfba_3b_gibbs_sample.argtypes = [vp, ctypes.POINTER(ThreeBModel), vp, vp, vp, vp, vp, ctypes.c_int,
+                                           ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ull, ctypes.c_int,
+                                           vp, vp, ctypes.c_int, vp]
+        L.rfba_3b_gibbs_trace.argtypes = [vp, ctypes.POINTER(ThreeBModel), vp, vp, vp, vp, vp, ctypes.c_int,
+                                          ctypes.c_int, ctypes.c_int, ull, vp, vp, vp, ctypes.c_int, vp]
+        L.rfba_3b_free_energy.argtypes = [vp, ctypes.POINTER(ThreeBModel), vp, vp, vp, vp, vp, ctypes.c_int,
+                                          ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ull,
+                                          ctypes.POINTER(ctypes.c_double), vp, ctypes.c_int, vp]
         L.rfba_3b_optimise_spot.argtypes = [vp, ctypes.POINTER(ThreeBModel), vp, vp, vp, ctypes.c_int, ctypes.c_int,
                                             ctypes.c_int, dp, dp, ctypes.c_int, dp, ipp, ipp, ctypes.c_int, vp]
         L.rfba_cg_only_run.argtypes = [dp, dp, ctypes.c_int, GRAD5_FN, vp, dp, ipp, ipp]
@@ -625,6 +636,73 @@ class Context:
                                            RFBA_DEVICE_PTRS if dev else RFBA_HOST_PTRS, _stream_arg(stream, dev)))
         return out, it.value, ev.value
 
+    def gibbs_sample_3b(self, model: ThreeBModel, pix, pixels, spots, masks=None, sweeps: int = 1,
+                        n_draws: int = 1, seed: int = 0, exclude_spot: int = -1, want_states: bool = True,
+                        want_intensities: bool = True):
+        """GibbsSampler2 (sampled_multispot.h:360-690) on the GPU from all spots off:
+        returns (states [n_draws][K][F] uint8 or None, sample intensities
+        [n_draws][F][P] or None). pix [F][P] float64, pixels [P][3] int32 sorted by
+        (z, y, x), spots [K][5]; masks = (offsets, indices), default spot_masks_3b."""
+        pix = np.ascontiguousarray(pix, np.float64)
+        pixels = np.ascontiguousarray(pixels, np.int32)
+        spots = np.ascontiguousarray(spots, np.float64).reshape(-1, 5)
+        moff, midx = masks if masks is not None else spot_masks_3b(pixels, spots)
+        moff = np.ascontiguousarray(moff, np.int32)
+        midx = np.ascontiguousarray(midx, np.int32) if len(midx) else np.zeros(1, np.int32)
+        F, P = pix.shape
+        K = len(spots)
+        st = np.empty((n_draws, K, F), np.uint8) if want_states else None
+        ints = np.empty((n_draws, F, P)) if want_intensities else None
+        vp = ctypes.c_void_p
+        _check(lib().rfba_3b_gibbs_sample(self.h, ctypes.byref(model), vp(pix.ctypes.data), vp(pixels.ctypes.data),
+                                          vp(spots.ctypes.data), vp(moff.ctypes.data), vp(midx.ctypes.data), K, F, P,
+                                          sweeps, n_draws, seed, exclude_spot,
+                                          vp(st.ctypes.data) if st is not None else None,
+                                          vp(ints.ctypes.data) if ints is not None else None, RFBA_HOST_PTRS, None))
+        return st, ints
+
+    def gibbs_trace_3b(self, model: ThreeBModel, pix, pixels, spots, masks=None, seed: int = 0):
+        """One sweep from all spots off: (states [K][F], log p(on / off) [K][F][2],
+        forward filter [K][F][3])."""
+        pix = np.ascontiguousarray(pix, np.float64)
+        pixels = np.ascontiguousarray(pixels, np.int32)
+        spots = np.ascontiguousarray(spots, np.float64).reshape(-1, 5)
+        moff, midx = masks if masks is not None else spot_masks_3b(pixels, spots)
+        moff = np.ascontiguousarray(moff, np.int32)
+        midx = np.ascontiguousarray(midx, np.int32) if len(midx) else np.zeros(1, np.int32)
+        F, P = pix.shape
+        K = len(spots)
+        st = np.empty((K, F), np.uint8)
+        lp = np.empty((K, F, 2))
+        filt = np.empty((K, F, 3))
+        vp = ctypes.c_void_p
+        _check(lib().rfba_3b_gibbs_trace(self.h, ctypes.byref(model), vp(pix.ctypes.data), vp(pixels.ctypes.data),
+                                         vp(spots.ctypes.data), vp(moff.ctypes.data), vp(midx.ctypes.data), K, F, P,
+                                         seed, vp(st.ctypes.data), vp(lp.ctypes.data), vp(filt.ctypes.data),
+                                         RFBA_HOST_PTRS, None))
+        return st, lp, filt
+
+    def free_energy_3b(self, model: ThreeBModel, pix, pixels, spots, masks=None, samples: int = 1000,
+                       sweeps: int = 1, seed: int = 0):
+        """NegativeFreeEnergy::compute_with_mask (multispot5.cc:335-405): returns
+        (its value, each draw's sum of squared residuals [samples])."""
+        pix = np.ascontiguousarray(pix, np.float64)
+        pixels = np.ascontiguousarray(pixels, np.int32)
+        spots = np.ascontiguousarray(spots, np.float64).reshape(-1, 5)
+        moff, midx = masks if masks is not None else spot_masks_3b(pixels, spots)
+        moff = np.ascontiguousarray(moff, np.int32)
+        midx = np.ascontiguousarray(midx, np.int32) if len(midx) else np.zeros(1, np.int32)
+        F, P = pix.shape
+        K = len(spots)
+        v = ctypes.c_double()
+        res = np.empty(samples)
+        vp = ctypes.c_void_p
+        _check(lib().rfba_3b_free_energy(self.h, ctypes.byref(model), vp(pix.ctypes.data), vp(pixels.ctypes.data),
+                                         vp(spots.ctypes.data), vp(moff.ctypes.data), vp(midx.ctypes.data), K, F, P,
+                                         samples, sweeps, seed, ctypes.byref(v), vp(res.ctypes.data),
+                                         RFBA_HOST_PTRS, None))
+        return v.value, res
+
     def check(self):
         """Wait for this context's queued work and raise RfbaError for a failure its
         kernels recorded (a bounded device wait that gave up: RFBA_ERR_TIMEOUT).
@@ -645,6 +723,23 @@ class Context:
         _check(lib().rfba_srrf_forward_blocks_plain(self.h, ctypes.byref(cfg), ptr, dt, _iptr(dims), blocks, nblocks,
                                                     ctypes.c_void_p(out.ctypes.data), out_elems))
         return out
+
+
+def spot_masks_3b(pixels, spots):
+    """get_spot_pixels (multispot5.cc:1001-1020) for every spot: (offsets [K+1],
+    indices); pixels [P][3] sorted by (z, y, x). Host only."""
+    px = np.ascontiguousarray(pixels, np.int32)
+    sp = np.ascontiguousarray(spots, np.float64).reshape(-1, 5)
+    K, P = len(sp), len(px)
+    off = np.zeros(K + 1, np.int32)
+    nnz = ctypes.c_longlong()
+    vp = ctypes.c_void_p
+    _check(lib().rfba_3b_spot_masks(vp(px.ctypes.data), P, vp(sp.ctypes.data), K, vp(off.ctypes.data), None, 0,
+                                    ctypes.byref(nnz)))
+    idx = np.zeros(max(nnz.value, 1), np.int32)
+    _check(lib().rfba_3b_spot_masks(vp(px.ctypes.data), P, vp(sp.ctypes.data), K, vp(off.ctypes.data),
+                                    vp(idx.ctypes.data), nnz.value, ctypes.byref(nnz)))
+    return off, idx[:nnz.value]
 
 
 def _stream_arg(stream, device_tensors: bool):
