@@ -337,6 +337,31 @@ int rfba_3b_free_energy(rfba_ctx* ctx, const rfba_3b_model* model, const double*
                         int samples, int sweeps, unsigned long long seed, double* value, double* residuals,
                         int ptr_flags, void* stream);
 
+/* One pass of FitSpots::optimize_each_spot_in_turn_for_several_passes (RFBA
+ * Main/multispot5.cc:1511-1690), the main loop of a 3B block fit, on the GPU:
+ * the spots (spots [*nspots][5], host, updated in place) are ordered by
+ * position as pass `pass` orders them (x ascending, x descending, then y
+ * descending; the reference's third branch repeats "% 4 == 1" and is never
+ * taken), their masks kept at their old places as the reference's reordering
+ * leaves them (multispot5.cc:1570); then each spot in turn: a fresh Gibbs
+ * sampler (rfba_3b_gibbs_sample) draws main_samples samples with `sweeps`
+ * passes each, the spot is taken off them, ConjugateGradientOnly<5> optimises
+ * it on rfba_3b_spot_gradient over those samples (at most cg_max_iterations
+ * line searches, motion limits `limit`), its mask is recomputed, and it is
+ * erased when the mask is empty or, with position_extra_radius >= 0, when its
+ * rounded position leaves the pixels dilated by getBall(position_extra_radius)
+ * (the position prior, multispot5.cc:1280-1290, 1653-1674); *nspots receives
+ * the spots kept. Spot s's draws use the seed rfba_3b_pass_seed(seed, pass, s).
+ * pixel_intensities [F][P] and pixels [P][3] (sorted by (z, y, x)) are host
+ * memory; *evaluations (may be NULL) receives the gradient evaluations.
+ * Synchronous. */
+int rfba_3b_optimise_pass(rfba_ctx* ctx, const rfba_3b_model* model, const double* pixel_intensities,
+                          const int* pixels, int F, int P, double* spots, int* nspots, int pass, int main_samples,
+                          int sweeps, int cg_max_iterations, const double limit[5], double position_extra_radius,
+                          unsigned long long seed, int* evaluations);
+/* The Gibbs seed of spot s in pass `pass` of rfba_3b_optimise_pass. */
+unsigned long long rfba_3b_pass_seed(unsigned long long seed, int pass, int s);
+
 /* Device-side failure check. No counterpart in the reference (GradientCalc.cpp
  * and kernel.cu check no CUDA status; every call returns 0). Waits for the
  * work the context last enqueued and reports failures its kernels recorded

@@ -10,6 +10,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
+#include <set>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -1602,6 +1604,158 @@ int rfba_3b_gibbs_sample(rfba_ctx* ctx, const rfba_3b_model* m, const double* pi
     copy_out(sample_intensities, ctx->gb_oint.p, (size_t)n_draws * F * P * 8, ptr_flags, st, &s);
     if (s) return s;
     RFBA_CUDA(cudaStreamSynchronize(st), "synchronize");
+    return RFBA_OK;
+}
+
+// Seed of spot `s`'s draws in pass `pass` of rfba_3b_optimise_pass: SplitMix64
+// (Steele, Lea, Flood, OOPSLA 2014) of the caller's seed mixed with both.
+static unsigned long long pass_seed(unsigned long long seed, int pass, int s) {
+    unsigned long long z = seed ^ ((unsigned long long)(unsigned)pass << 32) ^ (unsigned long long)(unsigned)s;
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+unsigned long long rfba_3b_pass_seed(unsigned long long seed, int pass, int s) { return pass_seed(seed, pass, s); }
+
+// One pass of FitSpots::optimize_each_spot_in_turn_for_several_passes
+// (multispot5.cc:1511-1690).
+int rfba_3b_optimise_pass(rfba_ctx* ctx, const rfba_3b_model* m, const double* pixel_intensities, const int* pixels,
+                          int F, int P, double* spots, int* nspots, int pass, int main_samples, int sweeps,
+                          int cg_max_iterations, const double limit[5], double position_extra_radius,
+                          unsigned long long seed, int* evaluations) {
+    int s;
+    if (!nspots || !spots || !limit || !pixel_intensities || !pixels) {
+        set_error("null argument");
+        return RFBA_ERR_INVALID;
+    }
+    int K = *nspots;
+    if ((s = gibbs_check(ctx, m, K, F, P, RFBA_HOST_PTRS))) return s;
+    if (main_samples < 1 || sweeps < 1 || cg_max_iterations < 0) {
+        set_error("main_samples and sweeps must be >= 1, cg_max_iterations >= 0");
+        return RFBA_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = ctx->stream;
+    if ((s = order_streams(ctx, st))) return s;
+    // masks of every spot (multispot5.cc:1518-1521)
+    std::vector<int> off((size_t)K + 1);
+    long long nnz = 0;
+    if ((s = rfba_3b_spot_masks(pixels, P, spots, K, off.data(), nullptr, 0, &nnz))) return s;
+    std::vector<int> idx((size_t)nnz);
+    if ((s = rfba_3b_spot_masks(pixels, P, spots, K, off.data(), idx.data(), nnz, &nnz))) return s;
+    std::vector<std::vector<int> > masks((size_t)K);
+    for (int k = 0; k < K; ++k) masks[k].assign(idx.begin() + off[k], idx.begin() + off[k + 1]);
+    // allowed area: the pixels dilated by getBall(extra_radius) (multispot5.cc:1280-1290)
+    std::set<long long> allowed;
+    auto key = [](int x, int y, int z) {
+        return ((long long)(x + (1 << 20)) << 42) | ((long long)(y + (1 << 20)) << 21) | (long long)(z + (1 << 20));
+    };
+    const bool use_prior = position_extra_radius >= 0;
+    if (use_prior) {
+        const std::vector<int> b = ball((float)position_extra_radius);
+        for (int p = 0; p < P; ++p)
+            for (size_t j = 0; j < b.size(); j += 3)
+                allowed.insert(key(pixels[3 * p] + b[j], pixels[3 * p + 1] + b[j + 1], pixels[3 * p + 2] + b[j + 2]));
+    }
+    // the sweep order (multispot5.cc:1541-1560): by x or y position, ascending
+    // or descending; the reference's third branch repeats `% 4 == 1` and is never
+    // taken, so passes 2 and 3 both sort by descending y
+    std::vector<int> order((size_t)K);
+    for (int k = 0; k < K; ++k) order[k] = k;
+    std::vector<std::array<double, 5> > sp((size_t)K);
+    for (int k = 0; k < K; ++k)
+        for (int n = 0; n < 5; ++n) sp[k][n] = spots[5 * k + n];
+    const int mode = pass % 4 == 0 ? 0 : pass % 4 == 1 ? 1 : 2;
+    const int first = mode == 2 ? 3 : 2, second = first == 2 ? 3 : 2;
+    std::sort(order.begin(), order.end(), [&](int a, int b) {
+        const double fa = sp[a][first], fb = sp[b][first];
+        const bool desc = mode != 0;
+        if (desc ? fa > fb : fa < fb) return true;
+        if (fa == fb) return desc ? sp[a][second] > sp[b][second] : sp[a][second] < sp[b][second];
+        return false;
+    });
+    {
+        std::vector<std::array<double, 5> > t((size_t)K);
+        for (int k = 0; k < K; ++k) t[k] = sp[order[k]];
+        sp.swap(t);
+        // masks stay where they were: the reference swaps tmp_spot_pixels[i]
+        // with spot_pixels[i], not spot_pixels[index[i]] (multispot5.cc:1570), so
+        // a spot's mask is the one at its new position until it is optimised
+    }
+    // data on the device once
+    const size_t FP = (size_t)F * P;
+    if ((s = ctx->gb_pix.ensure(FP * 8, "3B data")) || (s = ctx->gb_pixels.ensure((size_t)P * 12, "3B pixels")) ||
+        (s = ctx->gb_spots.ensure((size_t)K * 40 + 8, "3B spots")))
+        return s;
+    RFBA_CUDA(cudaMemcpyAsync(ctx->gb_pix.p, pixel_intensities, FP * 8, cudaMemcpyHostToDevice, st), "data copy");
+    RFBA_CUDA(cudaMemcpyAsync(ctx->gb_pixels.p, pixels, (size_t)P * 12, cudaMemcpyHostToDevice, st), "pixels copy");
+    int evals = 0;
+    for (int k = 0; k < K; ++k) {
+        // a fresh sampler for this spot: main_samples draws, the spot taken off
+        // them (multispot5.cc:1591-1608)
+        std::vector<int> hoff((size_t)K + 1, 0), hidx;
+        for (int j = 0; j < K; ++j) {
+            hidx.insert(hidx.end(), masks[j].begin(), masks[j].end());
+            hoff[j + 1] = (int)hidx.size();
+        }
+        std::vector<double> flat((size_t)K * 5);
+        for (int j = 0; j < K; ++j)
+            for (int n = 0; n < 5; ++n) flat[5 * j + n] = sp[j][n];
+        RFBA_CUDA(cudaMemcpyAsync(ctx->gb_spots.p, flat.data(), flat.size() * 8, cudaMemcpyHostToDevice, st),
+                  "spots copy");
+        GibbsCall c;
+        c.K = K;
+        c.F = F;
+        c.P = P;
+        c.sweeps = sweeps;
+        c.n_draws = main_samples;
+        c.seed = pass_seed(seed, pass, k);
+        c.exclude = k;
+        c.want_int = true;
+        if ((s = gibbs_run(ctx, m, static_cast<const double*>(ctx->gb_pix.p), static_cast<const int*>(ctx->gb_pixels.p),
+                           static_cast<const double*>(ctx->gb_spots.p), hoff, hidx, c, RFBA_DEVICE_PTRS, st)))
+            return s;
+        // optimise the spot on those samples (multispot5.cc:1611-1636)
+        ThreeBData d;
+        if ((s = threeb_stage(ctx, static_cast<const double*>(ctx->gb_oint.p), static_cast<const double*>(ctx->gb_pix.p),
+                              static_cast<const int*>(ctx->gb_pixels.p), main_samples, F, P, RFBA_DEVICE_PTRS, st, &d)))
+            return s;
+        auto grad = [&](const double* x, double* g) -> int {
+            if (x[0] <= 0 || x[1] <= 0) {
+                for (int n = 0; n < 5; ++n) g[n] = std::numeric_limits<double>::quiet_NaN();
+                return RFBA_OK;
+            }
+            return threeb_eval(ctx, m, d, x, g, nullptr, st);
+        };
+        CgOnly5 cg;
+        if ((s = cg.start(sp[k].data(), limit, grad))) return s;
+        cg.max_iterations = cg_max_iterations;
+        if ((s = cg.run(grad))) return s;
+        evals += cg.evaluations;
+        for (int n = 0; n < 5; ++n) sp[k][n] = cg.x[n];
+        // new mask; eject the spot if it has no pixels or left the allowed area
+        // (multispot5.cc:1651-1674)
+        int o2[2];
+        long long n2 = 0;
+        if ((s = rfba_3b_spot_masks(pixels, P, sp[k].data(), 1, o2, nullptr, 0, &n2))) return s;
+        masks[k].assign((size_t)n2, 0);
+        if (n2 && (s = rfba_3b_spot_masks(pixels, P, sp[k].data(), 1, o2, masks[k].data(), n2, &n2))) return s;
+        const bool zero_prior =
+            use_prior && !allowed.count(key(round_away(sp[k][2]), round_away(sp[k][3]), round_away(sp[k][4])));
+        if (masks[k].empty() || zero_prior) {
+            sp.erase(sp.begin() + k);
+            masks.erase(masks.begin() + k);
+            --K;
+            --k;
+        }
+    }
+    for (int k = 0; k < K; ++k)
+        for (int n = 0; n < 5; ++n) spots[5 * k + n] = sp[k][n];
+    *nspots = K;
+    if (evaluations) *evaluations = evals;
     return RFBA_OK;
 }
 

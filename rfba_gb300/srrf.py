@@ -180,6 +180,11 @@ def lib():
         L.rfba_3b_free_energy.argtypes = [vp, ctypes.POINTER(ThreeBModel), vp, vp, vp, vp, vp, ctypes.c_int,
                                           ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ull,
                                           ctypes.POINTER(ctypes.c_double), vp, ctypes.c_int, vp]
+        L.rfba_3b_optimise_pass.argtypes = [vp, ctypes.POINTER(ThreeBModel), vp, vp, ctypes.c_int, ctypes.c_int, vp,
+                                            ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_int, vp, ctypes.c_double, ull, ctypes.POINTER(ctypes.c_int)]
+        L.rfba_3b_pass_seed.argtypes = [ull, ctypes.c_int, ctypes.c_int]
+        L.rfba_3b_pass_seed.restype = ull
         L.rfba_3b_optimise_spot.argtypes = [vp, ctypes.POINTER(ThreeBModel), vp, vp, vp, ctypes.c_int, ctypes.c_int,
                                             ctypes.c_int, dp, dp, ctypes.c_int, dp, ipp, ipp, ctypes.c_int, vp]
         L.rfba_cg_only_run.argtypes = [dp, dp, ctypes.c_int, GRAD5_FN, vp, dp, ipp, ipp]
@@ -702,6 +707,25 @@ class Context:
                                          samples, sweeps, seed, ctypes.byref(v), vp(res.ctypes.data),
                                          RFBA_HOST_PTRS, None))
         return v.value, res
+
+    def optimise_pass_3b(self, model: ThreeBModel, pix, pixels, spots, pass_index: int = 0, main_samples: int = 10,
+                         sweeps: int = 1, cg_max_iterations: int = 5, limit=None, position_extra_radius: float = -1.0,
+                         seed: int = 0):
+        """One pass of FitSpots' main loop (multispot5.cc:1511-1690): returns (spots
+        [K'][5] after the pass, gradient evaluations)."""
+        pix = np.ascontiguousarray(pix, np.float64)
+        pixels = np.ascontiguousarray(pixels, np.int32)
+        sp = np.ascontiguousarray(spots, np.float64).reshape(-1, 5).copy()
+        lim = np.ascontiguousarray(limit if limit is not None else [0.5] * 5, np.float64)
+        F, P = pix.shape
+        n = ctypes.c_int(len(sp))
+        ev = ctypes.c_int()
+        vp = ctypes.c_void_p
+        _check(lib().rfba_3b_optimise_pass(self.h, ctypes.byref(model), vp(pix.ctypes.data), vp(pixels.ctypes.data),
+                                           F, P, vp(sp.ctypes.data), ctypes.byref(n), pass_index, main_samples, sweeps,
+                                           cg_max_iterations, vp(lim.ctypes.data), float(position_extra_radius),
+                                           seed, ctypes.byref(ev)))
+        return sp[:n.value].copy(), ev.value
 
     def check(self):
         """Wait for this context's queued work and raise RfbaError for a failure its

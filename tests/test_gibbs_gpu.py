@@ -158,3 +158,44 @@ def test_argument_checks(ctx):
     # and the context still samples afterwards
     st, _ = ctx.gibbs_sample_3b(m, pix, pixels, spots, n_draws=2, want_intensities=False)
     assert st.shape == (2, 2, 10)
+
+
+def test_pass_replays_its_pieces(ctx):
+    """With one spot, a pass is: the spot's Gibbs draws (seed rfba_3b_pass_seed,
+    the spot taken off them) then the conjugate-gradient optimisation on them;
+    the pass must equal those two calls made separately, bit for bit."""
+    from rfba_gb300 import srrf
+    pix, pixels, spots = _block(31, 40, 1, (10, 10, 8))
+    m = _model()
+    lim = np.array([0.5 * 20, 0.5, 0.5, 0.5, 0.5])
+    for pass_index in (0, 3):
+        got, ev = ctx.optimise_pass_3b(m, pix, pixels, spots, pass_index=pass_index, main_samples=6,
+                                       cg_max_iterations=5, limit=lim, seed=12)
+        seed = srrf.lib().rfba_3b_pass_seed(12, pass_index, 0)
+        _, bg = ctx.gibbs_sample_3b(m, pix, pixels, spots, n_draws=6, seed=seed, exclude_spot=0, want_states=False)
+        want, _, ev2 = ctx.optimise_spot_3b(m, bg, pix, pixels, spots[0], lim, 5)
+        np.testing.assert_array_equal(got[0], want)
+        assert ev == ev2
+
+
+def test_pass_moves_spots_towards_the_data_and_ejects(ctx):
+    from rfba_gb300 import synth
+    rng = np.random.default_rng(4)
+    pix, pixels, spots = synth.threeb_spots_block(41, 60, (14, 14, 10), 4)
+    start = spots.copy()
+    start[:, 2:] += rng.normal(0, 0.6, (4, 3))
+    m = _model()
+    lim = np.array([0.5 * 20, 0.5, 0.5, 0.5, 0.5])
+    cur = start.copy()
+    for p in range(3):
+        cur, ev = ctx.optimise_pass_3b(m, pix, pixels, cur, pass_index=p, main_samples=10, limit=lim, seed=3)
+        assert len(cur) == 4 and ev > 0
+    err0 = np.linalg.norm(start[:, 2:] - spots[:, 2:], axis=1).mean()
+    err1 = np.linalg.norm(cur[:, 2:] - spots[:, 2:], axis=1).mean()
+    print(f"[3B pass] mean position error {err0:.3f} -> {err1:.3f} after 3 passes")
+    assert err1 < err0
+    # a spot far outside the block has no pixels in its mask and is erased
+    far = np.vstack([cur, [[40.0, 1.0, -60.0, 3.0, 3.0]]])
+    kept, _ = ctx.optimise_pass_3b(m, pix, pixels, far, pass_index=0, main_samples=4, cg_max_iterations=1, limit=lim,
+                                   seed=3)
+    assert len(kept) == 4
