@@ -16,7 +16,9 @@ order where that decides the bits:
 - `free_energy`: the arithmetic of NegativeFreeEnergy::compute_with_mask
   (multispot5.cc:335-405) given each draw's sum of squared residuals.
 
-`ref_*` run the reference's own code compiled on the host
+`port_*` run the C++ port in oracle/gibbs_port.cpp (the reference's MT19937
+stream, sampler and main-loop pass restated; built everywhere, the CPU
+baseline of bench.py). `ref_*` run the reference's own code compiled on the host
 (oracle/_ref/libref3b_gibbs_host.so, built by oracle/build_ref.sh where the
 reference tree exists), which pins this module in tests/test_gibbs_cpu.py.
 """
@@ -277,3 +279,63 @@ def ref_free_energy(pix, pixels, spots, moff, midx, A, pi, variance, z_factor, m
                               _p(pi, ctypes.c_double), variance, z_factor, mu_b, sigma_b, mu_blur, sigma_blur,
                               samples, sweeps, seed, _p(res, ctypes.c_double))
     return v, res
+
+
+# ---- the C++ port (oracle/gibbs_port.cpp) -------------------------------------
+
+_port = None
+
+
+def port():
+    global _port
+    if _port is None:
+        from oracle import threeb as T3
+        T3.build()
+        L = ctypes.CDLL(str(T3.LIB_PATH))
+        dp, ip = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
+        bp = ctypes.POINTER(ctypes.c_ubyte)
+        d, i = ctypes.c_double, ctypes.c_int
+        L.port_gibbs_run.argtypes = [dp, dp, ip, ip, i, i, i, dp, dp, d, i, i, i, bp, dp]
+        L.port_optimise_pass.argtypes = [dp, ip, i, i, dp, ip, i, i, i, i, dp, d, dp, dp, d, d, d, d, d, d, i, i, i,
+                                         dp]
+        _port = L
+    return _port
+
+
+def port_run(pix, si, moff, midx, A, pi, variance, sweeps, n_draws, seed, want_int=False):
+    pix = np.ascontiguousarray(pix, np.float64)
+    si = np.ascontiguousarray(si, np.float64)
+    F, P = pix.shape
+    K = len(si)
+    moff = np.ascontiguousarray(moff, np.int32)
+    midx = np.ascontiguousarray(midx, np.int32) if len(midx) else np.zeros(1, np.int32)
+    A = np.ascontiguousarray(A, np.float64).reshape(9)
+    pi = np.ascontiguousarray(pi, np.float64)
+    st = np.empty((n_draws, K, F), np.uint8)
+    ints = np.empty((n_draws, F, P)) if want_int else None
+    port().port_gibbs_run(_p(pix, ctypes.c_double), _p(si, ctypes.c_double), _p(moff, ctypes.c_int),
+                          _p(midx, ctypes.c_int), K, F, P, _p(A, ctypes.c_double), _p(pi, ctypes.c_double), variance,
+                          sweeps, n_draws, seed, _p(st, ctypes.c_ubyte),
+                          _p(ints, ctypes.c_double) if want_int else None)
+    return st, ints
+
+
+def port_pass(pix, pixels, spots, pass_index, main_samples, sweeps, cg_max_iterations, limit, extra_radius, A, pi,
+              variance, z_factor, mu_b, sigma_b, mu_blur, sigma_blur, seed, nthreads=16, max_spots=-1):
+    """(spots after the pass, (seconds in the sampler, seconds in the optimiser))."""
+    pix = np.ascontiguousarray(pix, np.float64)
+    F, P = pix.shape
+    px = np.ascontiguousarray(pixels, np.int32)
+    sp = np.ascontiguousarray(spots, np.float64).reshape(-1, 5).copy()
+    lim = np.ascontiguousarray(limit, np.float64)
+    A = np.ascontiguousarray(A, np.float64).reshape(9)
+    pi = np.ascontiguousarray(pi, np.float64)
+    n = ctypes.c_int(len(sp))
+    sec = np.zeros(2)
+    rc = port().port_optimise_pass(_p(pix, ctypes.c_double), _p(px, ctypes.c_int), F, P, _p(sp, ctypes.c_double),
+                                   ctypes.byref(n), pass_index, main_samples, sweeps, cg_max_iterations,
+                                   _p(lim, ctypes.c_double), extra_radius, _p(A, ctypes.c_double),
+                                   _p(pi, ctypes.c_double), variance, z_factor, mu_b, sigma_b, mu_blur, sigma_blur,
+                                   seed, nthreads, max_spots, _p(sec, ctypes.c_double))
+    assert rc == 0
+    return sp[:n.value].copy(), (float(sec[0]), float(sec[1]))

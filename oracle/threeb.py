@@ -28,13 +28,19 @@ _lib = None
 _ref = None
 
 
+# the CPU port of the Gibbs sampler and of a main-loop pass, in the same library
+GIBBS_SRC = HERE / "gibbs_port.cpp"
+CG_HDR = HERE.parent / "rfba_gb300" / "csrc" / "cg_only.h"
+
+
 def build(force: bool = False) -> Path:
-    if LIB_PATH.exists() and not force and LIB_PATH.stat().st_mtime >= SRC.stat().st_mtime:
+    newest = max(p.stat().st_mtime for p in (SRC, GIBBS_SRC, CG_HDR))
+    if LIB_PATH.exists() and not force and LIB_PATH.stat().st_mtime >= newest:
         return LIB_PATH
     LIB_PATH.parent.mkdir(parents=True, exist_ok=True)
     tmp = LIB_PATH.with_suffix(".so.tmp")
     subprocess.run(["g++", "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
-                    str(SRC), "-o", str(tmp)], check=True)
+                    str(SRC), str(GIBBS_SRC), "-o", str(tmp)], check=True)
     tmp.replace(LIB_PATH)
     return LIB_PATH
 

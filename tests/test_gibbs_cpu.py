@@ -105,3 +105,27 @@ def test_reference_sampler_follows_the_posterior():
         freq = (st[:, 0, :] == j).mean(0)
         sd = np.sqrt(post[0, :, j] * (1 - post[0, :, j]) / n) + 1e-3
         assert np.all(np.abs(freq - post[0, :, j]) < 5 * sd), (j, freq, post[0, :, j])
+
+
+@needs_ref
+@pytest.mark.parametrize("seed,sweeps", [(3, 1), (17, 2)])
+def test_port_draws_are_the_references_draws(seed, sweeps):
+    """The C++ port (the bench's CPU baseline) with the reference's MT19937
+    stream: the same states and intensities as the reference's GibbsSampler2,
+    bit for bit."""
+    pix, pixels, spots, moff, midx = _block(seed, F=30, n=4)
+    si = G.spot_intensity(pixels, spots, 1.0)
+    a = G.port_run(pix, si, moff, midx, T3.A_SHIPPED, T3.PI_SHIPPED, 1.0, sweeps, 5, seed, want_int=True)
+    b = G.ref_run(pix, si, moff, midx, T3.A_SHIPPED, T3.PI_SHIPPED, 1.0, sweeps, 5, seed, want_int=True)
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
+
+
+def test_port_pass_runs_and_keeps_spots():
+    from rfba_gb300 import synth
+    pix, pixels, spots = synth.threeb_spots_block(41, 30, (12, 12, 9), 3)
+    lim = np.array([10.0, 0.5, 0.5, 0.5, 0.5])
+    out, (tg, tc) = G.port_pass(pix, pixels, spots, 0, 4, 1, 3, lim, 2.3, T3.A_SHIPPED, T3.PI_SHIPPED, 1.0, 1.0,
+                                np.log(40.0), 0.5, 0.0, 0.1, 5, nthreads=4)
+    assert out.shape == (3, 5) and tg > 0 and tc > 0
+    assert np.all(np.isfinite(out)) and np.all(out[:, 0] > 0)
