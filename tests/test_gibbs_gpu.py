@@ -51,7 +51,7 @@ def test_trace_matches_oracle(ctx, seed, F, n):
     e_f = float(np.max(np.abs(filt - filt_o)))
     print(f"[gibbs trace] K={n} F={F}: log p rel {e_lp:.1e}, filter abs {e_f:.1e}")
     assert e_lp < 1e-12
-    assert e_f < 1e-11
+    assert e_f < 1e-10
     assert set(np.unique(st)) <= {0, 1, 2}
     assert (st == 0).any() and (st != 0).any()
 
