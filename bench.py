@@ -396,7 +396,59 @@ def measure_threeb(ctx, steps: int = 20) -> dict:
                                "samples and data copied from pinned host memory once",
                        "ms": opt_ms, "line_searches": it, "gradient_evaluations": ev,
                        "ms_per_evaluation": opt_ms / max(ev, 1), "spot": x_opt.tolist()}
+    res.update(measure_gibbs(ctx))
     return res
+
+
+THREEB_BLOCK = dict(seed=91, F=100, shape=(29, 29, 29), K=20)
+
+
+def _gibbs_block():
+    from rfba_gb300 import synth
+    b = THREEB_BLOCK
+    return synth.threeb_spots_block(b["seed"], b["F"], b["shape"], b["K"])
+
+
+def _threeb_model():
+    from rfba_gb300 import srrf
+    return srrf.ThreeBModel.make([[0.16, 0.84, 0.0], [0.495, 0.495, 0.01], [0.0, 0.0, 1.0]], [0.5, 0.5, 0.0],
+                                 variance=1.0, z_factor=1.0, mu_brightness=3.5, sigma_brightness=1.0,
+                                 mu_blur=0.12869, sigma_blur=0.1)
+
+
+def measure_gibbs(ctx) -> dict:
+    """3B's Gibbs sampler, free energy and one main-loop pass on a 29^3 block
+    with 20 spots and 100 frames (the shipped gibbs.mixing_iterations 1,
+    main.gibbs.samples 10, add_remove.thermo.samples 1000, main.cg.max_iterations
+    5, cg.max_motion 0.5, position.extra_radius 2.3): GPU wall time per call,
+    data from host memory."""
+    from rfba_gb300 import srrf
+    pix, pixels, spots = _gibbs_block()
+    m = _threeb_model()
+    K, F = len(spots), pix.shape[0]
+    masks = srrf.spot_masks_3b(pixels, spots)
+    ctx.gibbs_sample_3b(m, pix, pixels, spots, masks, n_draws=10, seed=1)
+    t0 = time.perf_counter()
+    reps = 5
+    for r in range(reps):
+        ctx.gibbs_sample_3b(m, pix, pixels, spots, masks, n_draws=10, seed=2 + r)
+    g_ms = (time.perf_counter() - t0) / reps * 1e3
+    t0 = time.perf_counter()
+    fe, _ = ctx.free_energy_3b(m, pix, pixels, spots, masks, samples=1000, seed=3)
+    fe_ms = (time.perf_counter() - t0) * 1e3
+    lim = threeb_motion_limit(3.5, 1.0, 0.5)
+    ctx.optimise_pass_3b(m, pix, pixels, spots[:2], 0, 10, 1, 5, lim, 2.3, seed=4)  # warm-up
+    t0 = time.perf_counter()
+    out, ev = ctx.optimise_pass_3b(m, pix, pixels, spots, 0, 10, 1, 5, lim, 2.3, seed=5)
+    pass_ms = (time.perf_counter() - t0) * 1e3
+    return {"gibbs": {"what": f"GibbsSampler2 from all spots off: 10 draws x 1 sweep over {K} spots, {F} frames, "
+                              f"{len(pixels)} mask voxels (masks {int(masks[0][-1])} voxels in all)",
+                      "ms": g_ms, "spot_updates_per_s": 10 * K / (g_ms * 1e-3)},
+            "free_energy": {"what": f"NegativeFreeEnergy::compute_with_mask, 1000 thermodynamic samples, {K} spots",
+                            "ms": fe_ms, "value": fe},
+            "pass": {"what": f"one pass of optimize_each_spot_in_turn over {K} spots (10 Gibbs draws + "
+                             "conjugate gradient per spot)", "ms": pass_ms, "gradient_evaluations": ev,
+                     "spots_kept": len(out)}}
 
 
 def threeb_motion_limit(mu: float = 3.5, sigma: float = 1.0, max_motion: float = 0.5):
@@ -430,7 +482,43 @@ def threeb_cpu_baseline(res: dict, reps: int = 3) -> dict:
         out["optimise"] = {"ms": opt_ms, "gradient_evaluations": ev,
                            "speedup_e2e_vs_cpu": opt_ms / res["optimise"]["ms"],
                            "max_abs_spot_difference": float(np.max(np.abs(x_cpu - np.array(res["optimise"]["spot"]))))}
+    if "gibbs" in res:
+        out.update(gibbs_cpu_baseline(res))
     return out
+
+
+def gibbs_cpu_baseline(res: dict) -> dict:
+    """The C++ port of the sampler and of the pass (oracle/gibbs_port.cpp, the
+    reference's MT19937 stream and order; the sampler single-threaded as the
+    reference's GibbsSampler2::next is, the spot gradient over all host cores)
+    on bounded samples of the same workloads, scaled up: the free energy on 20
+    of its 1000 draws, the pass on 2 of its 20 spots."""
+    from oracle import gibbs_oracle as G
+    from rfba_gb300 import srrf
+    pix, pixels, spots = _gibbs_block()
+    K = len(spots)
+    moff, midx = srrf.spot_masks_3b(pixels, spots)
+    si = G.spot_intensity(pixels, spots, 1.0)
+    A = np.array([[0.16, 0.84, 0.0], [0.495, 0.495, 0.01], [0.0, 0.0, 1.0]])
+    pi = np.array([0.5, 0.5, 0.0])
+    t0 = time.perf_counter()
+    G.port_run(pix, si, moff, midx, A, pi, 1.0, 1, 10, 1)
+    g_ms = (time.perf_counter() - t0) * 1e3
+    t0 = time.perf_counter()
+    G.port_run(pix, si, moff, midx, A, pi, 1.0, 1, 20, 3)
+    fe_ms = (time.perf_counter() - t0) * 1e3 * 1000 / 20
+    lim = threeb_motion_limit(3.5, 1.0, 0.5)
+    nt = os.cpu_count() or 1
+    _, (tg, tc) = G.port_pass(pix, pixels, spots, 0, 10, 1, 5, lim, 2.3, A, pi, 1.0, 1.0, 3.5, 1.0, 0.12869, 0.1, 5,
+                              nthreads=nt, max_spots=2)
+    pass_ms = (tg + tc) * 1e3 * K / 2
+    return {"gibbs": {"cpu_ms": g_ms, "speedup_vs_cpu": g_ms / res["gibbs"]["ms"], "cores": 1,
+                      "kind": "port (draws bit-identical to the reference's GibbsSampler2)"},
+            "free_energy": {"cpu_ms": fe_ms, "speedup_vs_cpu": fe_ms / res["free_energy"]["ms"], "cores": 1,
+                            "sample": "20 of 1000 draws, scaled by 50"},
+            "pass": {"cpu_ms": pass_ms, "speedup_vs_cpu": pass_ms / res["pass"]["ms"], "cores": nt,
+                     "sample": "2 of 20 spots, scaled by 10", "cpu_gibbs_s_per_spot": tg / 2,
+                     "cpu_optimiser_s_per_spot": tc / 2}}
 
 
 def measure_diff(ctx, steps: int, iters: int = 20, volumes=None) -> dict:
