@@ -524,7 +524,10 @@ void shift_volume_adjoint(const double* g, double* out, int W, int H, int D, con
 }
 
 // Adjoint of the temporal reduction for one subvoxel: dL/drad_t and dL/dI_t
-// from dL/dmap. TRA (kernel.cu:291-327) and TRAC with ITC 0 (kernel.cu:469-507).
+// from dL/dmap. TRA (kernel.cu:291-327), TRM (kernel.cu:332-366: the maximum's
+// first argmax carries the derivative, none when the maximum is the seed 0),
+// TRPPM (kernel.cu:372-419, in the closed form ((sum r+)^2 + sum r+^2) / 2 /
+// count) and TRAC with ITC 0 (kernel.cu:469-507).
 bool temporal_adjoint(const oconf& c, const double* r, const double* I, int T, double g, double* gr, double* gi) {
     for (int t = 0; t < T; ++t) gr[t] = gi[t] = 0.0;
     const bool iw = c.intensity_w == 1;
@@ -532,6 +535,39 @@ bool temporal_adjoint(const oconf& c, const double* r, const double* I, int T, d
         for (int t = 0; t < T; ++t) {
             gr[t] = g * (iw ? I[t] : 1.0) / T;
             gi[t] = iw ? g * r[t] / T : 0.0;
+        }
+        return true;
+    }
+    if (c.method == 0) {
+        double mip = 0.0;
+        int arg = -1;
+        for (int t = 0; t < T; ++t) {
+            const double v = iw ? r[t] * I[t] : r[t];
+            if (v > mip) {
+                mip = v;
+                arg = t;
+            }
+        }
+        if (arg >= 0) {
+            gr[arg] = g * (iw ? I[arg] : 1.0);
+            gi[arg] = iw ? g * r[arg] : 0.0;
+        }
+        return true;
+    }
+    if (c.method == 2) {
+        double s1 = 0, s2 = 0, si = 0;
+        for (int t = 0; t < T; ++t) {
+            const double rp = r[t] > 0 ? r[t] : 0.0;
+            s1 += rp;
+            s2 += rp * rp;
+            si += I[t];
+        }
+        const double count = std::max(0.5 * T * (T + 1), 1.0);
+        const double scale = iw ? si / T : 1.0;
+        const double pps = 0.5 * (s1 * s1 + s2) / count;
+        for (int t = 0; t < T; ++t) {
+            gr[t] = r[t] > 0 ? g * (s1 + r[t]) / count * scale : 0.0;
+            gi[t] = iw ? g * pps / T : 0.0;
         }
         return true;
     }
@@ -596,7 +632,7 @@ bool temporal_adjoint(const oconf& c, const double* r, const double* I, int T, d
 }
 
 // Forward + adjoint on one whole block. Returns false for configurations
-// without a derivative here (TRM, TRPPM, TRAC with ITC 1).
+// without a derivative here (TRAC with ITC 1).
 bool objective_adjoint(const float* in, const int dims[4], const oconf& c, const double* shifts, const double* gmap,
                        double* map_out, double* dL_din, double* dL_dshift) {
     const int W = dims[0], H = dims[1], D = dims[2], T = dims[3];

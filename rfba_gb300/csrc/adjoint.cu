@@ -290,6 +290,50 @@ __global__ void temporal_adjoint_kernel(const BlockDev* __restrict__ blocks, con
         return;
     }
     const float invT = 1.f / (float)T;
+    if (method == 0 || method == 2) {
+        // TRM (kernel.cu:332-366): the first argmax of the seeded maximum carries
+        // the derivative. TRPPM (kernel.cu:372-419): d/dr_t of ((sum r+)^2 +
+        // sum r+^2) / 2 / count is (sum r+ + r_t) / count where r_t > 0.
+        int arg = -1;
+        float mip = 0.f;
+        KSum s1, s2, si;
+        for (int t = 0; t < T; ++t) {
+            const float rv = r[t * V], Iv = I[t * V];
+            if (method == 0) {
+                const float val = iw ? rv * Iv : rv;
+                if (val > mip) {
+                    mip = val;
+                    arg = t;
+                }
+            } else {
+                const float rp = fmaxf(rv, 0.f);
+                s1.add(rp);
+                s2.add(rp * rp);
+                si.add(Iv);
+            }
+        }
+        const float count = fmaxf(0.5f * (float)T * (float)(T + 1), 1.f);
+        const float scale = iw ? si.s * invT : 1.f;
+        const float pps = 0.5f * (s1.s * s1.s + s2.s) / count;
+        for (int t = 0; t < T; ++t) {
+            const float rv = r[t * V], Iv = I[t * V];
+            float gr = 0.f, gi = 0.f;
+            if (method == 0) {
+                if (t == arg) {
+                    gr = g * (iw ? Iv : 1.f);
+                    gi = iw ? g * rv : 0.f;
+                }
+            } else {
+                gr = rv > 0.f ? g * (s1.s + rv) / count * scale : 0.f;
+                gi = iw ? g * pps * invT : 0.f;
+            }
+            if (renorm) gr *= 0.5f;
+            if (poscon && !(rv > 0.f)) gr = 0.f;
+            gS[t * V + v] = gr;
+            gI[t * V + v] = Iv > 0.f ? gi : 0.f;
+        }
+        return;
+    }
     const float m = ms.s * invT;
     const float IW = iws.s * invT;
     const float scale_iw = iw ? IW : 1.f;

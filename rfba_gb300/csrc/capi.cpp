@@ -1132,8 +1132,8 @@ static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const flo
         set_error("null argument");
         return RFBA_ERR_INVALID;
     }
-    if (!(cfg->method == 1 || (cfg->method == 3 && cfg->itc != 1))) {
-        set_error("the adjoint covers TRA (Method 1) and TRAC with Integrate_Temporal_Correlations 0");
+    if (cfg->method == 3 && cfg->itc == 1) {
+        set_error("the adjoint covers TRM, TRA, TRPPM and TRAC with Integrate_Temporal_Correlations 0");
         return RFBA_ERR_UNSUPPORTED;
     }
     RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");

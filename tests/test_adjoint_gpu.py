@@ -52,6 +52,10 @@ CASES = [
      False),
     ("trac2_aniso_nosmooth", dict(mag=(2, 2, 1), method=3, itc=0, trac_order=2), (8, 9, 9, 10), True),
     ("trac2_mag442_deep_tiles", dict(mag=(4, 4, 2), method=3, itc=0, trac_order=2, **SHIPPED), (5, 9, 7, 8), True),
+    ("trm_iw_drift", dict(mag=2, method=0, **SHIPPED), (6, 9, 9, 10), True),
+    ("trppm_iw_drift", dict(mag=2, method=2, **SHIPPED), (7, 9, 10, 9), True),
+    ("trppm_no_iw_renorm", dict(mag=(2, 2, 1), method=2, intensity_w=0, renormalize=1, **SHIPPED), (6, 8, 9, 9),
+     False),
 ]
 
 

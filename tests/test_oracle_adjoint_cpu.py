@@ -28,6 +28,9 @@ CASES = [
     ("trac3_aniso", dict(mag=(2, 2, 1), method=3, itc=0, trac_order=3, gradient_smooth=0), (6, 8, 8, 9)),
     ("trac4_renorm", dict(mag=2, method=3, itc=0, trac_order=4, renormalize=1, **SHIPPED), (7, 8, 8, 8)),
     ("tra_no_iw_mag3", dict(mag=3, method=1, intensity_w=0, **SHIPPED), (5, 7, 7, 8)),
+    ("trm_iw", dict(mag=2, method=0, **SHIPPED), (5, 8, 8, 9)),
+    ("trppm_iw", dict(mag=2, method=2, **SHIPPED), (6, 8, 9, 8)),
+    ("trppm_no_iw_poscon", dict(mag=2, method=2, intensity_w=0, remove_con=1, **SHIPPED), (5, 8, 8, 8)),
 ]
 
 
