@@ -885,6 +885,70 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+def run_sharded(args, make_backend=None, series=None, cfg_kw=None, block=(29, 1)):
+    """--parallelism sharded: one series' block forward split across the ranks
+    by rfba_gb300.shard (strong scaling: the work is fixed, the ranks share it).
+    Workload: the batching series, 50 x 160^3 uint16 cut by doSplit's rule into
+    216 blocks of at most 29^3 with a 1-voxel border, mag 3, TRA. Each rank
+    crops its input box, runs rfba_srrf_forward_blocks on its blocks (host
+    buffers: the copies are inside the timed region), and rank 0 gathers the
+    packed maps (one tensor gather) and puts them back. The time is the
+    slowest rank's wall time per step; the rate counts the blocks' output
+    voxel-volumes once. make_backend / series / cfg_kw / block replace the
+    GPU context and the workload (CPU tests). Returns (line, map) on rank 0."""
+    import torch
+    import torch.distributed as dist
+    ws, rank, local = dist_env()
+    gpu = make_backend is None
+    if gpu:
+        torch.cuda.set_device(local)
+    if ws > 1 and not dist.is_initialized():
+        dist.init_process_group("nccl" if gpu else "gloo")
+    from rfba_gb300 import shard, srrf
+    kw = cfg_kw or dict(mag=3, method=1, gradient_smooth=1, main_range=1, x_range=1, y_range=1, z_range=1)
+    cfg = srrf.Config.make(**kw)
+    if series is None:
+        from rfba_gb300 import synth
+        w = dict(synth.WORKLOADS["batching"])
+        seed = 1234 + w["index"]
+        scene = synth.make_scene(seed, w["n_vol"], (160, 160, 160), w["n_emitters"], w["curves"], w["drift"])
+        series = synth.render_parallel(scene, (160, 160, 160), seed, w["dtype"])
+    x = series
+    blocks, n, oe = srrf.blocks_dosplit(cfg, x.shape, block[0], block[1])
+    units = sum(shard.block_cost(blocks[i], x.shape[0]) for i in range(n))
+    backend = make_backend() if make_backend else srrf.Context(local)
+    launches0 = backend.timing().launches if gpu else 0
+    out = None
+    for _ in range(args.warmup):
+        out = shard.forward_sharded(backend, cfg, x, blocks, n, oe)
+    if ws > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        out = shard.forward_sharded(backend, cfg, x, blocks, n, oe)
+    if gpu:
+        torch.cuda.synchronize()
+    sec = max_over_ranks(time.perf_counter() - t0)
+    launches = (backend.timing().launches - launches0) if gpu else 0
+    line = {"metric": "radiality voxel-volumes/s", "value": units * args.steps / sec, "unit": "voxel-volumes/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": f"batching: {x.shape[0]} x {x.shape[3]}x{x.shape[2]}x{x.shape[1]} -> {n} doSplit "
+                                   f"blocks ({block[0]}, border {block[1]}), mag {kw['mag']}, method {kw['method']}",
+                       "parallelism": "sharded", "blocks": n,
+                       "timing": "wall time per step on every rank (crop, host copies, kernels, tensor gather to "
+                                 "rank 0, put-back), slowest rank"},
+            "e2e": {"value": units * args.steps / sec, "unit": "voxel-volumes/s",
+                    "h2d_bytes_per_step": int(x.nbytes), "d2h_bytes_per_step": int(oe * 4)},
+            "gpu_launches": int(launches)}
+    if gpu:
+        backend.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return (line, out) if rank == 0 else (None, None)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -898,6 +962,9 @@ def main():
     ap.add_argument("--volumes", type=int, default=None,
                     help="fewer volumes than the workload's (profiling case only)")
     ap.add_argument("--iters", type=int, default=20, help="drift refinement iterations (diff workload)")
+    ap.add_argument("--parallelism", default="replicas", choices=["replicas", "sharded"],
+                    help="N > 1: replicas of the headline workload (default) or one batching series sharded by "
+                         "blocks across the ranks")
     ap.add_argument("--workload", default="mid", choices=["mid", "batching", "diff", "large", "seeding", "combine", "refgpu", "threeb"],
                     help="mid: the headline line; batching / diff: that measurement alone (one JSON line)")
     args = ap.parse_args()
@@ -905,6 +972,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.parallelism == "sharded":
+        run_sharded(args)
     elif args.workload != "mid":
         run_single_workload(args)
     else:

@@ -705,10 +705,9 @@ __global__ void __launch_bounds__(kAdjThreads, 2) radiality_adjoint_kernel(const
                     for (int w = 0; w < NW; ++w) gP[w] = gE[w] = gZ[w] = make_float2(0.f, 0.f);
                     for (int qi = pair_pt[pi]; qi < pair_pt[pi + 1]; ++qi) {
                         const float4 pv = pt_vec[qi];
-                        const float2 hh = dup(pv.x), cc = dup(pv.y), ncc = dup(-pv.y);
-                        const float wgt = pv.z;
-                        const float2 nun2 = dup(2.0f * pv.w);  // -2|u|
-                        const float2 nun = dup(pv.w);          // -|u|
+                        const float2 hh = dup(pv.x), cc = dup(pv.y), ncc = dup(-pv.y), nhh = dup(-pv.x);
+                        const float wgt2 = pv.z * (-2.0f * pv.w);  // multiplicity / n times 2|u|
+                        const float2 nun = dup(pv.w);              // -|u|
                         const int zc = pt_zval[qi];
                         const float* wzc = wz + zc * (MZ * 4);
                         const int offmask = offz[zc];
@@ -737,17 +736,21 @@ __global__ void __launch_bounds__(kAdjThreads, 2) radiality_adjoint_kernel(const
                                 const float2 inv = make_float2(rsqrt_approx(fmaxf(xx.x, 1e-30f)),
                                                                rsqrt_approx(fmaxf(xx.y, 1e-30f)));
                                 const float2 sn = mul2(c2, inv);                          // sin
-                                const float2 nsq = mul2(mul2(sn, inv), mul2(inv, mul2(c2, dup(-1.0f))));  // -sin/|g|^2
                                 const float2 om = fma2(sn, nun, dup(1.0f));               // 1 - Dk/r
-                                const float2 sw = make_float2(sign_weight(wgt, dot.x), sign_weight(wgt, dot.y));
-                                // dS/dsin = sw * 2 om * (-|u|), times dL/dS
-                                const float2 coef = mul2(mul2(sw, om), mul2(nun2, gS[z]));
-                                const float2 ci = mul2(cp, inv);
-                                // d sin / d(P, E, Z) = g_perp/(|g||g_perp|) - sin g/|g|^2,
-                                // g_perp = (-c cp, E, h cp)
-                                const float2 dP = mul2(coef, fma2(nsq, gx, mul2(ncc, ci)));
-                                const float2 dE = mul2(coef, mul2(gy, __fadd2_rn(inv, nsq)));
-                                const float2 dZ = mul2(coef, fma2(nsq, gz, mul2(hh, ci)));
+                                // -dL/dsin = (dL/dS) (+-w) 2 om |u| (signed weight and 2|u|
+                                // folded into one table value)
+                                const float2 sw = make_float2(sign_weight(wgt2, dot.x), sign_weight(wgt2, dot.y));
+                                const float2 coef = mul2(mul2(sw, om), gS[z]);
+                                // d sin / d(P, E, Z) = g_perp/(|g||g_perp|) - sin g/|g|^2 with
+                                // g_perp = (-c cp, E, h cp) and 1/(|g||g_perp|) = inv, sin/|g|^2
+                                // = sin^2 inv; times dL/dsin = -coef:
+                                //   dP = k (sin^2 P + c cp), dZ = k (sin^2 Z - h cp),
+                                //   dE = k (sin^2 - 1) E,   k = coef inv
+                                const float2 k = mul2(coef, inv);
+                                const float2 s2 = mul2(sn, sn);
+                                const float2 dP = mul2(k, fma2(s2, gx, mul2(cc, cp)));
+                                const float2 dZ = mul2(k, fma2(s2, gz, mul2(nhh, cp)));
+                                const float2 dE = mul2(fma2(s2, k, make_float2(-k.x, -k.y)), gy);
 #pragma unroll
                                 for (int m = 0; m < 4; ++m) {
                                     gP[zi + o + m] = fma2(w4[m], dP, gP[zi + o + m]);

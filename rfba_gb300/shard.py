@@ -7,9 +7,9 @@ without exchanging map data:
   doSplit.m's) is dealt out longest first, each block to the rank with the
   least work so far (work = region voxels x volumes). Every rank computes its
   blocks from its own input box (the union of its blocks' sub-volumes, halos
-  included) into one packed buffer; rank 0 gathers the buffers and puts each
-  block's region back where the original block list placed it. No collective
-  touches the maps, only that gather.
+  included) into one packed buffer; rank 0 gathers the buffers (one tensor
+  gather) and puts each block's region back where the original block list
+  placed it. No collective touches the maps, only that gather.
 - Drift refinement (rfba_gb300.drift's Adam loop on the per-volume shifts).
   The fine map is cut into z slabs, one per rank. Each rank runs the region
   forward and region adjoint (rfba_srrf_forward_shifted_region /
@@ -134,23 +134,50 @@ def forward_local(backend, cfg, x, blocks, nblocks: int, rank: int, world: int, 
     return idx, packed
 
 
+def gather_packed(packed: np.ndarray, group=None):
+    """Every rank's packed float32 buffer on rank 0 (a list in rank order; None
+    on the other ranks), as tensors: the lengths first (one all-gather of an
+    int64), then one gather of the buffers padded to the longest. Tensors live
+    where the backend wants them (CUDA for NCCL); the values travel bit for
+    bit, NaN included."""
+    import torch
+    import torch.distributed as dist
+    rank, world = _rank_world(group)
+    packed = np.ascontiguousarray(packed, np.float32).reshape(-1)
+    if world == 1:
+        return [packed]
+    dev = "cuda" if dist.get_backend(group) == "nccl" else "cpu"
+    n = torch.tensor([packed.size], dtype=torch.int64, device=dev)
+    sizes = [torch.zeros_like(n) for _ in range(world)]
+    dist.all_gather(sizes, n, group=group)
+    sizes = [int(v.item()) for v in sizes]
+    m = max(max(sizes), 1)
+    buf = torch.zeros(m, dtype=torch.float32, device=dev)
+    if packed.size:
+        buf[:packed.size] = torch.from_numpy(packed).to(dev)
+    root = dist.get_global_rank(group, 0) if group is not None else 0
+    bufs = [torch.empty(m, dtype=torch.float32, device=dev) for _ in range(world)] if rank == 0 else None
+    dist.gather(buf, bufs, dst=root, group=group)
+    if rank != 0:
+        return None
+    return [b[:k].cpu().numpy() for b, k in zip(bufs, sizes)]
+
+
 def forward_sharded(backend, cfg, x, blocks, nblocks: int, out_elems: int, group=None, stream=None):
     """Block forward split across the group's ranks; rank 0 returns the flat
     output (as one process's rfba_srrf_forward_blocks writes it, starting from
-    zeros), the other ranks None."""
-    import torch.distributed as dist
+    zeros), the other ranks None. The ranks' block lists follow from `balance`
+    on every rank alike, so only the packed maps travel (gather_packed)."""
     rank, world = _rank_world(group)
-    part = forward_local(backend, cfg, x, blocks, nblocks, rank, world, stream)
-    if world == 1:
-        parts = [part]
-    else:
-        parts = [None] * world if rank == 0 else None
-        dist.gather_object(part, parts, dst=dist.get_global_rank(group, 0) if group is not None else 0, group=group)
+    T = x.shape[0]
+    parts = balance([block_cost(blocks[i], T) for i in range(nblocks)], world)
+    idx, packed = forward_local(backend, cfg, x, blocks, nblocks, rank, world, stream)
+    maps = gather_packed(packed, group)
     if rank != 0:
         return None
     out = np.zeros(out_elems, np.float32)
-    for idx, packed in parts:
-        put_back(out, blocks, idx, packed)
+    for r in range(world):
+        put_back(out, blocks, parts[r], maps[r])
     return out
 
 
