@@ -184,9 +184,10 @@ int rfba_srrf_forward_static_scratch(const rfba_srrf_config* cfg, const void* in
  * SRRF forward; out is the map as rfba_srrf_forward writes it.
  * The backward takes dL/dmap (device, map layout; NaN map voxels get no
  * gradient) and writes dL/din (T x D x H x W) and, if dL_dshift is not NULL,
- * dL/dshifts (T x 3). It covers TRM, TRA and TRPPM (Methods 0-2; TRM's
- * derivative goes to the first time point that reaches the maximum) and TRAC
- * with Integrate_Temporal_Correlations 0, and reuses the radiality stacks of the
+ * dL/dshifts (T x 3). It covers every temporal method: TRM, TRA and TRPPM
+ * (Methods 0-2; TRM's derivative goes to the first time point that reaches
+ * the maximum) and TRAC with Integrate_Temporal_Correlations 0 or 1 (the
+ * shipped setting; its backward always recomputes the stacks). It reuses the radiality stacks of the
  * last rfba_srrf_forward_shifted on the same context with the same
  * configuration, input and shifts (otherwise it runs that forward itself); the
  * interpolated gradient field is recomputed, not stored. Stream-ordered. */

@@ -523,6 +523,133 @@ void shift_volume_adjoint(const double* g, double* out, int W, int H, int D, con
     std::copy(a.begin(), a.end(), out);
 }
 
+// Adjoint of TRAC with ITC 1 (kernel.cu:437-555) for one subvoxel. The forward
+// bins the series in place level after level (entry t of level l + 1 is the
+// mean of entries tk .. tk + k - 1 of level l for t < nB - k, entry 0 reading
+// itself as the 0 it was just set to, entries past the series reading 0; the
+// other entries keep their values) and accumulates, per level, AB (reset each
+// level) and ABC / ABCD, CD, AC, BD, AD, BC (not reset) around the level-0
+// mean; out = sum over levels of |C_level| / nB_level, times the intensity
+// weight. Every level's series is a linear map of the input series, so the
+// adjoint is reverse mode over the levels: the derivative of out with respect
+// to each level's partial sums (suffix sums over the levels that see them),
+// the sums' derivatives with respect to the level's entries, the transposed
+// binning down to level 0, and the mean's share.
+static bool temporal_adjoint_itc1(const oconf& c, const double* r, const double* I, int T, double g, double* gr,
+                                  double* gi) {
+    const int k = c.trac_order;
+    const bool iw = c.intensity_w == 1;
+    double m = 0, IW = 0;
+    for (int t = 0; t < T; ++t) {
+        m += r[t];
+        IW += r[t] * I[t];
+    }
+    m /= T;
+    IW /= T;
+    std::vector<std::vector<double> > states;
+    std::vector<int> nbs;
+    std::vector<double> Cl, ABl, CDa, ACa, BDa, ADa, BCa;
+    std::vector<double> s(T + 4, 0.0);
+    for (int t = 0; t < T; ++t) s[t] = r[t];
+    double ABC = 0, ABCD = 0, CD = 0, AC = 0, BD = 0, AD = 0, BC = 0, out_raw = 0;
+    int nB = T;
+    while (nB > k) {
+        states.push_back(s);
+        nbs.push_back(nB);
+        double AB = 0;
+        for (int t = 0; t < nB - k; ++t) {
+            const double A = s[t] - m, B = s[t + 1] - m;
+            AB += A * B;
+            if (k == 3) ABC += A * B * (s[t + 2] - m);
+            if (k == 4) {
+                const double Cc = s[t + 2] - m, Dd = s[t + 3] - m;
+                ABCD += A * B * Cc * Dd;
+                CD += Cc * Dd;
+                AC += A * Cc;
+                BD += B * Dd;
+                AD += A * Dd;
+                BC += B * Cc;
+            }
+            s[t] = 0;
+            if (t * k < nB)
+                for (int j = 0; j < k; ++j) s[t] += s[t * k + j] / k;
+        }
+        const double C = k == 2 ? AB : (k == 3 ? ABC : ABCD - AB * CD - AC * BD - AD * BC);
+        Cl.push_back(C);
+        ABl.push_back(AB);
+        CDa.push_back(CD);
+        ACa.push_back(AC);
+        BDa.push_back(BD);
+        ADa.push_back(AD);
+        BCa.push_back(BC);
+        out_raw += std::fabs(C) / nB;
+        nB = nB / k;
+    }
+    const int L = (int)Cl.size();
+    // d out / d(partial sums of level l)
+    std::vector<double> wM(L), wAB(L), wCD(L), wAC(L), wBD(L), wAD(L), wBC(L);
+    double ss = 0, scd = 0, sac = 0, sbd = 0, sad = 0, sbc = 0;
+    for (int l = L - 1; l >= 0; --l) {
+        const double sl = (Cl[l] > 0 ? 1.0 : (Cl[l] < 0 ? -1.0 : 0.0)) / nbs[l];
+        ss += sl;
+        scd += sl * -ABl[l];
+        sac += sl * -BDa[l];
+        sbd += sl * -ACa[l];
+        sad += sl * -BCa[l];
+        sbc += sl * -ADa[l];
+        wM[l] = k == 2 ? sl : ss;
+        wAB[l] = sl * -CDa[l];
+        wCD[l] = scd;
+        wAC[l] = sac;
+        wBD[l] = sbd;
+        wAD[l] = sad;
+        wBC[l] = sbc;
+    }
+    std::vector<double> G(T + 4, 0.0);
+    double dm = 0;
+    for (int l = L - 1; l >= 0; --l) {
+        const std::vector<double>& S = states[l];
+        const int nb = nbs[l], N = nb - k;
+        std::vector<double> Gn(T + 4, 0.0);
+        for (int p = 0; p < T; ++p)
+            if (p >= N) Gn[p] = G[p];
+        for (int t = 0; t < N; ++t)
+            if (t * k < nb)
+                for (int j = 0; j < k; ++j) {
+                    const int src = t * k + j;
+                    if (src != t && src < T) Gn[src] += G[t] / k;
+                }
+        for (int t = 0; t < N; ++t) {
+            const double A = S[t] - m, B = S[t + 1] - m, Cc = S[t + 2] - m, Dd = S[t + 3] - m;
+            double d[4] = {0, 0, 0, 0};
+            if (k == 2) {
+                d[0] = wM[l] * B;
+                d[1] = wM[l] * A;
+            } else if (k == 3) {
+                d[0] = wM[l] * B * Cc;
+                d[1] = wM[l] * A * Cc;
+                d[2] = wM[l] * A * B;
+            } else {
+                d[0] = wM[l] * B * Cc * Dd + wAB[l] * B + wAC[l] * Cc + wAD[l] * Dd;
+                d[1] = wM[l] * A * Cc * Dd + wAB[l] * A + wBD[l] * Dd + wBC[l] * Cc;
+                d[2] = wM[l] * A * B * Dd + wCD[l] * Dd + wAC[l] * A + wBC[l] * B;
+                d[3] = wM[l] * A * B * Cc + wCD[l] * Cc + wBD[l] * B + wAD[l] * A;
+            }
+            for (int q = 0; q < k; ++q) {
+                Gn[t + q] += d[q];
+                dm += d[q];
+            }
+        }
+        G.swap(Gn);
+    }
+    const double scale = iw ? IW : 1.0;
+    for (int t = 0; t < T; ++t) {
+        gr[t] = g * (scale * (G[t] - dm / T) + (iw ? out_raw * I[t] / T : 0.0));
+        gi[t] = iw ? g * out_raw * r[t] / T : 0.0;
+    }
+    return true;
+}
+
 // Adjoint of the temporal reduction for one subvoxel: dL/drad_t and dL/dI_t
 // from dL/dmap. TRA (kernel.cu:291-327), TRM (kernel.cu:332-366: the maximum's
 // first argmax carries the derivative, none when the maximum is the seed 0),
@@ -571,7 +698,8 @@ bool temporal_adjoint(const oconf& c, const double* r, const double* I, int T, d
         }
         return true;
     }
-    if (c.method != 3 || c.itc == 1) return false;
+    if (c.method == 3 && c.itc == 1) return temporal_adjoint_itc1(c, r, I, T, g, gr, gi);
+    if (c.method != 3) return false;
     const int k = c.trac_order;
     double m = 0, IW = 0;
     for (int t = 0; t < T; ++t) {
@@ -631,8 +759,7 @@ bool temporal_adjoint(const oconf& c, const double* r, const double* I, int T, d
     return true;
 }
 
-// Forward + adjoint on one whole block. Returns false for configurations
-// without a derivative here (TRAC with ITC 1).
+// Forward + adjoint on one whole block (every temporal method).
 bool objective_adjoint(const float* in, const int dims[4], const oconf& c, const double* shifts, const double* gmap,
                        double* map_out, double* dL_din, double* dL_dshift) {
     const int W = dims[0], H = dims[1], D = dims[2], T = dims[3];

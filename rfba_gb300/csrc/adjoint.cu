@@ -257,9 +257,159 @@ struct KSum {
     }
 };
 
+// Adjoint of TRAC with ITC 1 (kernel.cu:437-555) for one subvoxel; r, I its
+// radiality and intensity series (stride V), m and IW the level-0 mean and
+// intensity weight. The forward bins the series in place level after level
+// (entry t < nB - k becomes the mean of entries tk .. tk + k - 1, entry 0
+// reading itself as 0, entries past the series reading 0; the rest keep their
+// values) and sums per level AB (reset) and ABC / ABCD, CD, AC, BD, AD, BC (not
+// reset) around m; out = sum_l |C_l| / nB_l. Reverse mode over the levels with
+// O(T) memory per subvoxel: one forward sweep gives each level's sums, hence
+// d out / d(each level's partial sums) as suffix sums over the levels; then,
+// from the deepest level up, the level's array state is replayed from r into
+// S (the dL/dI buffer, free until the end) and the gradient with respect to
+// that state is formed in place in Gd (the dL/dS buffer): the level's own
+// sums' derivatives plus its transposed binning of the next level's gradient,
+// walking the entries downwards so that every entry a later bin reads is still
+// the next level's. The level-0 mean takes minus the sum of all direct terms
+// over T. FP32 with compensated sums in the forward sweep.
+constexpr int kMaxLevels = 32;
+
+__device__ void trac_itc1_adjoint(const float* r, const float* I, long long V, int T, int k, int iw, int renorm,
+                                  int poscon, float g, float m, float IW, float* Gd, float* S) {
+    float Cl[kMaxLevels], ABl[kMaxLevels], CDa[kMaxLevels], ACa[kMaxLevels], BDa[kMaxLevels], ADa[kMaxLevels],
+        BCa[kMaxLevels];
+    int nbl[kMaxLevels];
+    const float invk = 1.f / (float)k;
+    // binning of one level in place (the forward's order)
+    auto bin_level = [&](int nb) {
+        for (int t = 0; t < nb - k; ++t) {
+            float nv = 0.f;
+            if (t * k < nb)
+                for (int j = 0; j < k; ++j) {
+                    const int src = t * k + j;
+                    const float rv = (src == t || src >= T) ? 0.f : S[(long long)src * V];
+                    nv += rv / (float)k;
+                }
+            S[(long long)t * V] = nv;
+        }
+    };
+    for (int t = 0; t < T; ++t) S[(long long)t * V] = r[(long long)t * V];
+    KSum ABC, ABCD, CD, AC, BD, AD, BC;
+    float out_raw = 0.f;
+    int L = 0, nB = T;
+    while (nB > k && L < kMaxLevels) {
+        KSum AB;
+        for (int t = 0; t < nB - k; ++t) {
+            const float A = S[(long long)t * V] - m, B = S[(long long)(t + 1) * V] - m;
+            AB.add(A * B);
+            if (k >= 3) {
+                const float C = S[(long long)(t + 2) * V] - m;
+                if (k == 3) ABC.add(A * B * C);
+                if (k == 4) {
+                    const float D = S[(long long)(t + 3) * V] - m;
+                    ABCD.add(A * B * C * D);
+                    CD.add(C * D);
+                    AC.add(A * C);
+                    BD.add(B * D);
+                    AD.add(A * D);
+                    BC.add(B * C);
+                }
+            }
+        }
+        bin_level(nB);
+        const float C = k == 2 ? AB.s : (k == 3 ? ABC.s : ABCD.s - AB.s * CD.s - AC.s * BD.s - AD.s * BC.s);
+        Cl[L] = C;
+        ABl[L] = AB.s;
+        CDa[L] = CD.s;
+        ACa[L] = AC.s;
+        BDa[L] = BD.s;
+        ADa[L] = AD.s;
+        BCa[L] = BC.s;
+        nbl[L] = nB;
+        out_raw += fabsf(C) / (float)nB;
+        ++L;
+        nB = nB / k;
+    }
+    // d out / d(partial sums of each level): suffix sums over the levels
+    float wM[kMaxLevels], wAB[kMaxLevels], wCD[kMaxLevels], wAC[kMaxLevels], wBD[kMaxLevels], wAD[kMaxLevels],
+        wBC[kMaxLevels];
+    {
+        float ss = 0.f, scd = 0.f, sac = 0.f, sbd = 0.f, sad = 0.f, sbc = 0.f;
+        for (int l = L - 1; l >= 0; --l) {
+            const float sl = (Cl[l] > 0.f ? 1.f : (Cl[l] < 0.f ? -1.f : 0.f)) / (float)nbl[l];
+            ss += sl;
+            scd -= sl * ABl[l];
+            sac -= sl * BDa[l];
+            sbd -= sl * ACa[l];
+            sad -= sl * BCa[l];
+            sbc -= sl * ADa[l];
+            wM[l] = k == 2 ? sl : ss;
+            wAB[l] = -sl * CDa[l];
+            wCD[l] = scd;
+            wAC[l] = sac;
+            wBD[l] = sbd;
+            wAD[l] = sad;
+            wBC[l] = sbc;
+        }
+    }
+    for (int t = 0; t < T; ++t) Gd[(long long)t * V] = 0.f;
+    float dm = 0.f;
+    for (int l = L - 1; l >= 0; --l) {
+        // replay level l's state
+        for (int t = 0; t < T; ++t) S[(long long)t * V] = r[(long long)t * V];
+        int nb = T;
+        for (int j = 0; j < l; ++j) {
+            bin_level(nb);
+            nb /= k;
+        }
+        const int N = nb - k;
+        auto sv = [&](int t) { return S[(long long)t * V] - m; };
+        for (int p = T - 1; p >= 0; --p) {
+            // transposed binning: entries at or past N keep their value, entry
+            // p feeds bin p / k
+            float gp = p >= N ? Gd[(long long)p * V] : 0.f;
+            const int tb = p / k;
+            if (tb < N && tb * k < nb && p != tb) gp += Gd[(long long)tb * V] * invk;
+            // this level's sums: the products starting at t = p - q hold entry p
+            float dp = 0.f;
+            for (int q = 0; q < k; ++q) {
+                const int t = p - q;
+                if (t < 0 || t >= N) continue;
+                const float A = sv(t), B = sv(t + 1);
+                if (k == 2) {
+                    dp += wM[l] * (q == 0 ? B : A);
+                } else if (k == 3) {
+                    const float C = sv(t + 2);
+                    dp += wM[l] * (q == 0 ? B * C : (q == 1 ? A * C : A * B));
+                } else {
+                    const float C = sv(t + 2), D = sv(t + 3);
+                    if (q == 0) dp += wM[l] * B * C * D + wAB[l] * B + wAC[l] * C + wAD[l] * D;
+                    if (q == 1) dp += wM[l] * A * C * D + wAB[l] * A + wBD[l] * D + wBC[l] * C;
+                    if (q == 2) dp += wM[l] * A * B * D + wCD[l] * D + wAC[l] * A + wBC[l] * B;
+                    if (q == 3) dp += wM[l] * A * B * C + wCD[l] * C + wBD[l] * B + wAD[l] * A;
+                }
+            }
+            Gd[(long long)p * V] = gp + dp;
+            dm += dp;
+        }
+    }
+    const float invT = 1.f / (float)T;
+    const float scale = iw ? IW : 1.f;
+    for (int t = 0; t < T; ++t) {
+        const float rv = r[(long long)t * V], Iv = I[(long long)t * V];
+        float gr = g * (scale * (Gd[(long long)t * V] - dm * invT) + (iw ? out_raw * Iv * invT : 0.f));
+        const float gi = iw ? g * out_raw * rv * invT : 0.f;
+        if (renorm) gr *= 0.5f;
+        if (poscon && !(rv > 0.f)) gr = 0.f;
+        Gd[(long long)t * V] = gr;
+        S[(long long)t * V] = Iv > 0.f ? gi : 0.f;
+    }
+}
+
 __global__ void temporal_adjoint_kernel(const BlockDev* __restrict__ blocks, const float* __restrict__ rad,
                                         const float* __restrict__ inten, const float* __restrict__ gmap, int T,
-                                        int method, int order, int iw, int renorm, int poscon,
+                                        int method, int itc, int order, int iw, int renorm, int poscon,
                                         float* __restrict__ gS, float* __restrict__ gI, long long nmap,
                                         unsigned long long* err) {
     const BlockDev& B = blocks[0];
@@ -332,6 +482,10 @@ __global__ void temporal_adjoint_kernel(const BlockDev* __restrict__ blocks, con
             gS[t * V + v] = gr;
             gI[t * V + v] = Iv > 0.f ? gi : 0.f;
         }
+        return;
+    }
+    if (method == 3 && itc == 1) {
+        trac_itc1_adjoint(r, I, V, T, order, iw, renorm, poscon, g, ms.s * invT, iws.s * invT, gS + v, gI + v);
         return;
     }
     const float m = ms.s * invT;
@@ -1007,12 +1161,12 @@ int radiality_adjoint_max_ctas_per_sm(const RadParams& p, int* out) {
 }
 
 int launch_temporal_adjoint(const BlockDev* blocks, long long vox, const float* rad, const float* inten,
-                            const float* gmap, int T, int method, int order, int iw, int renorm, int poscon, float* gS,
-                            float* gI, long long nmap, unsigned long long* err, void* stream) {
+                            const float* gmap, int T, int method, int itc, int order, int iw, int renorm, int poscon,
+                            float* gS, float* gI, long long nmap, unsigned long long* err, void* stream) {
     if (vox == 0) return 0;
     const long long grid = (vox + 127) / 128;
     temporal_adjoint_kernel<<<(unsigned)grid, 128, 0, static_cast<cudaStream_t>(stream)>>>(
-        blocks, rad, inten, gmap, T, method, order, iw, renorm, poscon, gS, gI, nmap, err);
+        blocks, rad, inten, gmap, T, method, itc, order, iw, renorm, poscon, gS, gI, nmap, err);
     return (int)cudaGetLastError();
 }
 

@@ -1082,7 +1082,8 @@ static int adjoint_slab(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float*
     float* gI = static_cast<float*>(ctx->gI.p);
     unsigned long long* err = static_cast<unsigned long long*>(ctx->errw.p);
     int e = launch_temporal_adjoint(dblk, V, static_cast<const float*>(ctx->rad.p),
-                                    static_cast<const float*>(ctx->inten.p), gmap, T, cfg->method, cfg->trac_order,
+                                    static_cast<const float*>(ctx->inten.p), gmap, T, cfg->method, cfg->itc,
+                                    cfg->trac_order,
                                     cfg->intensity_w, cfg->renormalize == 1, cfg->remove_con == 1, gS, gI, ngmap, err,
                                     st);
     if (e) return cuda_fail((cudaError_t)e, "temporal adjoint launch");
@@ -1132,10 +1133,6 @@ static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const flo
         set_error("null argument");
         return RFBA_ERR_INVALID;
     }
-    if (cfg->method == 3 && cfg->itc == 1) {
-        set_error("the adjoint covers TRM, TRA, TRPPM and TRAC with Integrate_Temporal_Correlations 0");
-        return RFBA_ERR_UNSUPPORTED;
-    }
     RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
     if ((s = order_streams(ctx, st))) return s;
     const bool reuse = !rlo && ctx->train.valid && same_cfg(ctx->train.cfg, *cfg) && ctx->train.in == in &&
@@ -1161,9 +1158,14 @@ static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const flo
         std::vector<BlockDev> all;
         if ((s = make_blocks(ctx, *cfg, dims, &b, 1, &all))) return s;
         RFBA_CUDA(cudaMemsetAsync(ctx->gin.p, 0, nin * 4, st), "adjoint clear");
+        // the recomputed stacks must stay as the radiality kernel wrote them: TRAC
+        // with ITC 1 would bin them in place, so its map (unused here) is formed
+        // with ITC 0, which only reads them
+        rfba_srrf_config fcfg = *cfg;
+        if (fcfg.method == 3) fcfg.itc = 0;
         for (const BlockDev& slab : all) {
             std::vector<BlockDev> one(1, slab);
-            if ((s = run_device(ctx, *cfg, ip, RFBA_F32, dims, one, static_cast<float*>(ctx->out.p), st))) return s;
+            if ((s = run_device(ctx, fcfg, ip, RFBA_F32, dims, one, static_cast<float*>(ctx->out.p), st))) return s;
             BlockDev blk = slab;
             blk.stack_off = 0;
             if ((s = adjoint_slab(ctx, cfg, ip, dims, blk, gmap, nreg, st))) return s;

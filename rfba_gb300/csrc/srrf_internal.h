@@ -156,8 +156,8 @@ int launch_radiality_adjoint(const RadParams& p, const AdjParams& a, int grid, s
 size_t radiality_adjoint_smem_bytes(const RadParams& p);
 int radiality_adjoint_max_ctas_per_sm(const RadParams& p, int* out);
 int launch_temporal_adjoint(const BlockDev* blocks, long long vox, const float* rad, const float* inten,
-                            const float* gmap, int T, int method, int order, int iw, int renorm, int poscon, float* gS,
-                            float* gI, long long nmap, unsigned long long* err, void* stream);
+                            const float* gmap, int T, int method, int itc, int order, int iw, int renorm, int poscon,
+                            float* gS, float* gI, long long nmap, unsigned long long* err, void* stream);
 int launch_shift_axis(const float* src, float* dst, int W, int H, int D, int T, int axis, const float* shifts, int mode,
                       unsigned long long* err, void* stream);
 // Drift operator, all axes fused: mode 0 resamples src into dst; mode 1 adds

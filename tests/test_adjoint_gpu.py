@@ -56,6 +56,9 @@ CASES = [
     ("trppm_iw_drift", dict(mag=2, method=2, **SHIPPED), (7, 9, 10, 9), True),
     ("trppm_no_iw_renorm", dict(mag=(2, 2, 1), method=2, intensity_w=0, renormalize=1, **SHIPPED), (6, 8, 9, 9),
      False),
+    ("trac2_itc1_shipped_drift", dict(mag=2, method=3, itc=1, trac_order=2, **SHIPPED), (13, 9, 9, 10), True),
+    ("trac3_itc1_no_iw", dict(mag=2, method=3, itc=1, trac_order=3, intensity_w=0, **SHIPPED), (14, 8, 9, 9), True),
+    ("trac4_itc1_mag442", dict(mag=(4, 4, 2), method=3, itc=1, trac_order=4, **SHIPPED), (21, 7, 7, 8), False),
 ]
 
 

@@ -31,6 +31,9 @@ CASES = [
     ("trm_iw", dict(mag=2, method=0, **SHIPPED), (5, 8, 8, 9)),
     ("trppm_iw", dict(mag=2, method=2, **SHIPPED), (6, 8, 9, 8)),
     ("trppm_no_iw_poscon", dict(mag=2, method=2, intensity_w=0, remove_con=1, **SHIPPED), (5, 8, 8, 8)),
+    ("trac2_itc1", dict(mag=2, method=3, itc=1, trac_order=2, **SHIPPED), (11, 8, 8, 8)),
+    ("trac3_itc1_no_iw", dict(mag=2, method=3, itc=1, trac_order=3, intensity_w=0, **SHIPPED), (13, 8, 8, 8)),
+    ("trac4_itc1", dict(mag=2, method=3, itc=1, trac_order=4, **SHIPPED), (21, 7, 7, 8)),
 ]
 
 
