@@ -39,7 +39,7 @@ def build(force: bool = False) -> Path:
         return LIB_PATH
     LIB_PATH.parent.mkdir(parents=True, exist_ok=True)
     tmp = LIB_PATH.with_suffix(".so.tmp")
-    subprocess.run(["g++", "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+    subprocess.run(["g++", "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-Wno-psabi",
                     str(SRC), str(GIBBS_SRC), "-o", str(tmp)], check=True)
     tmp.replace(LIB_PATH)
     return LIB_PATH

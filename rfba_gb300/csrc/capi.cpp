@@ -1395,7 +1395,7 @@ static int gibbs_run(rfba_ctx* ctx, const rfba_3b_model* m, const double* pix, c
     if ((s = ctx->gb_moff.ensure((K + 1) * 4, "3B mask offsets")) || (s = ctx->gb_midx.ensure(nnz * 4 + 4, "3B masks")) ||
         (s = ctx->gb_si.ensure(K * P * 8 + 8, "3B spot intensities")) ||
         (s = ctx->gb_state.ensure(K * F + 1, "3B spot states")) || (s = ctx->gb_cur.ensure(F * P * 8, "3B sample intensities")) ||
-        (s = ctx->gb_em.ensure(F * 32, "3B emissions")) || (s = ctx->gb_bar.ensure(256, "3B barrier")))
+        (s = ctx->gb_em.ensure(F * 64, "3B emissions")) || (s = ctx->gb_bar.ensure(256, "3B barrier")))
         return s;
     const double* dpix = pix;
     const int* dpixels = pixels;

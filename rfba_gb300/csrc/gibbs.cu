@@ -16,8 +16,12 @@
 // One cooperative kernel runs a whole chain: the frames are dealt out to the
 // CTAs, which do the per-frame work (remove / add over the mask, the two sums
 // of squares, the emission probabilities) in parallel; after a grid barrier
-// one warp of CTA 0 runs the forward filter and the backward draw, and after a
-// second barrier every CTA adds the spot back into its frames. The filter runs
+// one warp of every CTA runs the forward filter and the backward draw over all
+// frames from the same emission table and random counters (so every CTA draws
+// the same states, and no second barrier is needed), and every CTA adds the
+// spot back into its own frames. A frame's state is only ever read by the CTA
+// that owns the frame, and the emission table alternates between two buffers
+// from one spot update to the next. The filter runs
 // on probabilities, each state's value a mantissa with its own power-of-two
 // exponent (no exp or log in the sequential chain; the frames' emission terms
 // are split into mantissa and exponent in parallel beforehand), which is the
@@ -111,10 +115,13 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
 __global__ void __launch_bounds__(kGibbsThreads) gibbs_chain_kernel(const GibbsParams g) {
     extern __shared__ double gsm[];
     // shared: per frame and state the forward value's mantissa and exponent,
-    // then the frame's uniform for the backward draw
+    // the frame's uniform for the backward draw, the frames' emission terms,
+    // and the spot's drawn states
     double* xs = gsm;                                          // [F][3]
     int* es = reinterpret_cast<int*>(xs + (size_t)3 * g.F);    // [F][3]
     double* us = reinterpret_cast<double*>(es + ((3 * g.F + 1) & ~1));  // [F]
+    double* emc = us + g.F;                                    // [F][4]
+    unsigned char* sts = reinterpret_cast<unsigned char*>(emc + (size_t)4 * g.F);  // [F]
     __shared__ double red[kGibbsThreads / 32];
     const int c = blockIdx.x, G = gridDim.x;
     const int F = g.F, P = g.P, K = g.K;
@@ -126,6 +133,11 @@ __global__ void __launch_bounds__(kGibbsThreads) gibbs_chain_kernel(const GibbsP
         const double twovar = 2 * var;
         for (int it = 0; it < g.sweeps; ++it) {
             for (int k = 0; k < K; ++k) {
+                // the emission table alternates between two buffers from one spot
+                // update to the next: a CTA can start writing the next update's
+                // terms while a slower one still reads this update's
+                const unsigned long long upd = ((unsigned long long)d * g.sweeps + it) * K + k;
+                double* emb = g.em + (size_t)(upd & 1) * 4 * F;
                 const int m0 = g.moff[k], m1 = g.moff[k + 1];
                 const int npix = m1 - m0;
                 const double* vk = g.si + (size_t)k * P;
@@ -159,7 +171,7 @@ __global__ void __launch_bounds__(kGibbsThreads) gibbs_chain_kernel(const GibbsP
                         int ko, kf;
                         exp_split(lon - m, &mo, &ko);
                         exp_split(loff - m, &mf, &kf);
-                        double* em = g.em + (size_t)f * 4;
+                        double* em = emb + (size_t)f * 4;
                         em[0] = mo;
                         em[1] = (double)ko;
                         em[2] = mf;
@@ -174,10 +186,13 @@ __global__ void __launch_bounds__(kGibbsThreads) gibbs_chain_kernel(const GibbsP
                     if (threadIdx.x == 0) atomicCAS(g.err, 0ull, (0x47ull << 56) | (unsigned long long)k);
                     return;
                 }
-                // phase B: forward filter and backward draw (CTA 0, warp 0)
-                if (c == 0 && threadIdx.x < 32) {
+                // phase B: forward filter and backward draw, run by warp 0 of every
+                // CTA on the same inputs and counters, so every CTA draws the same
+                // states and only the barrier above is needed per spot
+                if (threadIdx.x < 32) {
                     const int lane = threadIdx.x;
                     const unsigned full = 0xffffffffu;
+                    for (int i = lane; i < 4 * F; i += 32) emc[i] = __ldcg(emb + i);
                     // uniforms of this spot's draw, one per frame
                     const unsigned long long ctr = (unsigned long long)d * g.sweeps + it + g.draw_base;
                     for (int f = lane; f < F; f += 32) {
@@ -185,6 +200,7 @@ __global__ void __launch_bounds__(kGibbsThreads) gibbs_chain_kernel(const GibbsP
                         Philox::gen(cc, (uint32_t)g.seed, (uint32_t)(g.seed >> 32));
                         us[f] = u53(cc[0], cc[1]);
                     }
+                    __syncwarp();
                     const int j = lane < 3 ? lane : 2;
                     double Aj[3];
                     bool nz[3];
@@ -198,15 +214,14 @@ __global__ void __launch_bounds__(kGibbsThreads) gibbs_chain_kernel(const GibbsP
                     double x;
                     int E;
                     {
-                        const double mant0 = __ldcg(g.em + mi), k0 = __ldcg(g.em + mi + 1);
-                        const double y = g.pi[j] * mant0;
+                        const double y = g.pi[j] * emc[mi];
                         if (y == 0.0) {
                             x = 0.0;
                             E = kZeroExp;
                         } else {
                             int sh;
                             x = frexp(y, &sh);
-                            E = (int)k0 + sh;
+                            E = (int)emc[mi + 1] + sh;
                         }
                     }
                     if (lane < 3) {
@@ -217,9 +232,8 @@ __global__ void __launch_bounds__(kGibbsThreads) gibbs_chain_kernel(const GibbsP
 #pragma unroll
                     for (int i = 0; i < 3; ++i) Ev[i] = __shfl_sync(full, E, i);
                     for (int t = 1; t < F; ++t) {
-                        const double* em = g.em + (size_t)t * 4;
-                        const double mant = __ldcg(em + mi);
-                        const int ke = (int)__ldcg(em + mi + 1);
+                        const double mant = emc[(size_t)t * 4 + mi];
+                        const int ke = (int)emc[(size_t)t * 4 + mi + 1];
                         int Em = kZeroExp;
 #pragma unroll
                         for (int i = 0; i < 3; ++i)
@@ -251,7 +265,7 @@ __global__ void __launch_bounds__(kGibbsThreads) gibbs_chain_kernel(const GibbsP
                     }
                     __syncwarp();
                     // filtering distribution per frame (trace mode, first sweep)
-                    if (g.rec_filt && d == 0 && it == 0) {
+                    if (c == 0 && g.rec_filt && d == 0 && it == 0) {
                         for (int t = lane; t < F; t += 32) {
                             const int* e3 = es + (size_t)t * 3;
                             const int Em = max(e3[0], max(e3[1], e3[2]));
@@ -266,7 +280,6 @@ __global__ void __launch_bounds__(kGibbsThreads) gibbs_chain_kernel(const GibbsP
                     }
                     // backward draw (select_random_element on the unscaled weights)
                     if (lane == 0) {
-                        unsigned char* st = g.state + (size_t)k * F;
                         int next = -1;
                         for (int t = F - 1; t >= 0; --t) {
                             const double* x3 = xs + (size_t)t * 3;
@@ -284,27 +297,25 @@ __global__ void __launch_bounds__(kGibbsThreads) gibbs_chain_kernel(const GibbsP
                             }
                             const double choice = us[t] * tot;
                             double run = 0.0;
-                            int s = 2;
+                            int sdraw = 2;
                             for (int i = 0; i < 3; ++i) {
                                 run += a[i];
                                 if (choice <= run) {
-                                    s = i;
+                                    sdraw = i;
                                     break;
                                 }
                             }
-                            st[t] = (unsigned char)s;
-                            next = s;
+                            sts[t] = (unsigned char)sdraw;
+                            next = sdraw;
                         }
-                        __threadfence();
                     }
                 }
-                if (!grid_barrier(g.bar, g.bar + 1, G)) {
-                    if (threadIdx.x == 0) atomicCAS(g.err, 0ull, (0x47ull << 56) | (unsigned long long)k);
-                    return;
-                }
-                // phase C: add spot k back where its new state is on
+                __syncthreads();
+                // phase C: record the drawn states of this CTA's frames and add spot
+                // k back where it is on
                 for (int f = c; f < F; f += G) {
-                    if (vstate[(size_t)k * F + f] != 0) continue;
+                    if (threadIdx.x == 0) g.state[(size_t)k * F + f] = sts[f];
+                    if (sts[f] != 0) continue;
                     double* cur = g.cur + (size_t)f * P;
                     for (int q = m0 + threadIdx.x; q < m1; q += kGibbsThreads) {
                         const int p = g.midx[q];
@@ -359,7 +370,8 @@ __global__ void spot_intensity_kernel(const int* __restrict__ pixels, int P, con
 }  // namespace
 
 size_t gibbs_smem_bytes(int F) {
-    return (size_t)F * 3 * sizeof(double) + (size_t)((3 * F + 1) & ~1) * sizeof(int) + (size_t)F * sizeof(double);
+    return (size_t)F * 3 * sizeof(double) + (size_t)((3 * F + 1) & ~1) * sizeof(int) + (size_t)F * sizeof(double) +
+           (size_t)F * 4 * sizeof(double) + (size_t)F;
 }
 
 int gibbs_max_blocks(int F, int* out) {

@@ -212,7 +212,7 @@ struct GibbsParams {
     unsigned long long draw_base;  // counter offset of the first draw
     unsigned char* state;     // [K][F] current states, in/out
     double* cur;              // [F][P] current sample intensities, in/out
-    double* em;               // [F][4] scratch: emission mantissas / exponents
+    double* em;               // [2][F][4] scratch: emission mantissas / exponents (two buffers)
     unsigned int* bar;        // grid barrier: count, generation (zeroed)
     unsigned long long* err;  // barrier failures (site << 56 | spot)
     unsigned char* out_state;  // [n_draws][K][F] or null
