@@ -278,33 +278,40 @@ __global__ void __launch_bounds__(kGibbsThreads) gibbs_chain_kernel(const GibbsP
                             for (int i = 0; i < 3; ++i) g.rec_filt[((size_t)k * F + t) * 3 + i] = w[i] / tot;
                         }
                     }
-                    // backward draw (select_random_element on the unscaled weights)
-                    if (lane == 0) {
-                        int next = -1;
-                        for (int t = F - 1; t >= 0; --t) {
-                            const double* x3 = xs + (size_t)t * 3;
-                            const int* e3 = es + (size_t)t * 3;
-                            double a[3];
+                    // backward draw (select_random_element on the unscaled weights).
+                    // The lanes first tabulate, for every frame and each state the
+                    // next frame may hold (index 3: none, for the last frame), the
+                    // cumulative thresholds of states 0 and 1 as fractions of the
+                    // total; the sequential walk then only compares its uniform
+                    // with a table entry. The table reuses the emission staging area.
+                    float2* thr = reinterpret_cast<float2*>(emc);  // [F][4]
+                    for (int t = lane; t < F; t += 32) {
+                        const double* x3 = xs + (size_t)t * 3;
+                        const int* e3 = es + (size_t)t * 3;
+                        for (int nx = 0; nx < 4; ++nx) {
                             int Em = kZeroExp;
                             for (int i = 0; i < 3; ++i)
-                                if ((next < 0 || g.A[i * 3 + next] != 0.0) && x3[i] != 0.0 && e3[i] > Em) Em = e3[i];
-                            double tot = 0.0;
+                                if ((nx == 3 || g.A[i * 3 + nx] != 0.0) && x3[i] != 0.0 && e3[i] > Em) Em = e3[i];
+                            double a[3], tot = 0.0;
                             for (int i = 0; i < 3; ++i) {
-                                const double tr = next < 0 ? 1.0 : g.A[i * 3 + next];
+                                const double tr = nx == 3 ? 1.0 : g.A[i * 3 + nx];
                                 const int dd = e3[i] - Em;
                                 a[i] = (tr != 0.0 && x3[i] != 0.0 && dd >= -1022) ? x3[i] * pow2i(dd) * tr : 0.0;
                                 tot += a[i];
                             }
-                            const double choice = us[t] * tot;
-                            double run = 0.0;
-                            int sdraw = 2;
-                            for (int i = 0; i < 3; ++i) {
-                                run += a[i];
-                                if (choice <= run) {
-                                    sdraw = i;
-                                    break;
-                                }
-                            }
+                            // no weight at all: the walk takes state 0, as a zero total does
+                            thr[(size_t)t * 4 + nx] =
+                                tot > 0.0 ? make_float2((float)(a[0] / tot), (float)((a[0] + a[1]) / tot))
+                                          : make_float2(1.f, 1.f);
+                        }
+                    }
+                    __syncwarp();
+                    if (lane == 0) {
+                        int next = 3;
+                        for (int t = F - 1; t >= 0; --t) {
+                            const float2 th = thr[(size_t)t * 4 + next];
+                            const double u = us[t];
+                            const int sdraw = u <= (double)th.x ? 0 : (u <= (double)th.y ? 1 : 2);
                             sts[t] = (unsigned char)sdraw;
                             next = sdraw;
                         }
