@@ -201,67 +201,68 @@ __global__ void __launch_bounds__(kGibbsThreads) gibbs_chain_kernel(const GibbsP
                         us[f] = u53(cc[0], cc[1]);
                     }
                     __syncwarp();
-                    const int j = lane < 3 ? lane : 2;
-                    double Aj[3];
-                    bool nz[3];
-#pragma unroll
-                    for (int i = 0; i < 3; ++i) {
-                        Aj[i] = g.A[i * 3 + j];
-                        nz[i] = Aj[i] != 0.0;
-                    }
-                    const int mi = j == 0 ? 0 : 2;  // "off" and bleached emit alike
-                    // frame 0
-                    double x;
-                    int E;
-                    {
-                        const double y = g.pi[j] * emc[mi];
-                        if (y == 0.0) {
-                            x = 0.0;
-                            E = kZeroExp;
-                        } else {
-                            int sh;
-                            x = frexp(y, &sh);
-                            E = (int)emc[mi + 1] + sh;
-                        }
-                    }
+                    // the recursion runs on the three lanes that carry a state; the
+                    // FP64 pipe of this GPU is narrow, so the other lanes stay idle
                     if (lane < 3) {
-                        xs[j] = x;
-                        es[j] = E;
-                    }
-                    int Ev[3];
-#pragma unroll
-                    for (int i = 0; i < 3; ++i) Ev[i] = __shfl_sync(full, E, i);
-                    for (int t = 1; t < F; ++t) {
-                        const double mant = emc[(size_t)t * 4 + mi];
-                        const int ke = (int)emc[(size_t)t * 4 + mi + 1];
-                        int Em = kZeroExp;
-#pragma unroll
-                        for (int i = 0; i < 3; ++i)
-                            if (nz[i] && Ev[i] > Em) Em = Ev[i];
-                        double xi[3];
-#pragma unroll
-                        for (int i = 0; i < 3; ++i) xi[i] = __shfl_sync(full, x, i);
-                        double y = 0.0;
+                        const unsigned m3 = 0x7u;
+                        const int j = lane;
+                        double Aj[3];
+                        bool nz[3];
 #pragma unroll
                         for (int i = 0; i < 3; ++i) {
-                            const int dd = Ev[i] - Em;
-                            if (nz[i] && dd >= -1022) y = fma(Aj[i] * pow2i(dd), xi[i], y);
+                            Aj[i] = g.A[i * 3 + j];
+                            nz[i] = Aj[i] != 0.0;
                         }
-                        y *= mant;
-                        if (y == 0.0 || Em == kZeroExp || ke == kZeroExp) {
-                            x = 0.0;
-                            E = kZeroExp;
-                        } else {
-                            int sh;
-                            x = frexp(y, &sh);
-                            E = Em + ke + sh;
+                        const int mi = j == 0 ? 0 : 2;  // "off" and bleached emit alike
+                        // frame 0
+                        double x;
+                        int E;
+                        {
+                            const double y = g.pi[j] * emc[mi];
+                            if (y == 0.0) {
+                                x = 0.0;
+                                E = kZeroExp;
+                            } else {
+                                int sh;
+                                x = frexp(y, &sh);
+                                E = (int)emc[mi + 1] + sh;
+                            }
                         }
-                        if (lane < 3) {
+                        xs[j] = x;
+                        es[j] = E;
+                        int Ev[3];
+#pragma unroll
+                        for (int i = 0; i < 3; ++i) Ev[i] = __shfl_sync(m3, E, i);
+                        for (int t = 1; t < F; ++t) {
+                            const double mant = emc[(size_t)t * 4 + mi];
+                            const int ke = (int)emc[(size_t)t * 4 + mi + 1];
+                            int Em = kZeroExp;
+#pragma unroll
+                            for (int i = 0; i < 3; ++i)
+                                if (nz[i] && Ev[i] > Em) Em = Ev[i];
+                            double xi[3];
+#pragma unroll
+                            for (int i = 0; i < 3; ++i) xi[i] = __shfl_sync(m3, x, i);
+                            double y = 0.0;
+#pragma unroll
+                            for (int i = 0; i < 3; ++i) {
+                                const int dd = Ev[i] - Em;
+                                if (nz[i] && dd >= -1022) y = fma(Aj[i] * pow2i(dd), xi[i], y);
+                            }
+                            y *= mant;
+                            if (y == 0.0 || Em == kZeroExp || ke == kZeroExp) {
+                                x = 0.0;
+                                E = kZeroExp;
+                            } else {
+                                int sh;
+                                x = frexp(y, &sh);
+                                E = Em + ke + sh;
+                            }
                             xs[(size_t)t * 3 + j] = x;
                             es[(size_t)t * 3 + j] = E;
-                        }
 #pragma unroll
-                        for (int i = 0; i < 3; ++i) Ev[i] = __shfl_sync(full, E, i);
+                            for (int i = 0; i < 3; ++i) Ev[i] = __shfl_sync(m3, E, i);
+                        }
                     }
                     __syncwarp();
                     // filtering distribution per frame (trace mode, first sweep)
