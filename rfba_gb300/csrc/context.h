@@ -1,0 +1,144 @@
+// The library context (rfba_ctx) and the host helpers its translation units
+// share: the error string, CUDA-error mapping, stream ordering between calls.
+// A context owns the device scratch of every entry point (grown on demand and
+// kept), the cached ring plan and weight tables, autotuned schedules and
+// captured graphs; one mutex serialises the calls made on it.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "devbuf.h"
+#include "srrf_internal.h"
+
+struct rfba_ctx;
+
+namespace rfba {
+
+void set_error(const std::string& msg);
+// Records `what: <CUDA error>`; RFBA_ERR_NOMEM for an allocation failure,
+// RFBA_ERR_CUDA otherwise.
+int cuda_fail(cudaError_t e, const char* what);
+// Makes `st` wait for the previous call's work when that call used another
+// stream (calls share the context's scratch).
+int order_streams(rfba_ctx* ctx, cudaStream_t st);
+
+#define RFBA_CUDA(call, what)                          \
+    do {                                               \
+        cudaError_t e__ = (call);                      \
+        if (e__ != cudaSuccess) return cuda_fail(e__, what); \
+    } while (0)
+
+struct PlanCache {
+    bool valid = false;
+    float ring_radius = 0.f;
+    int axes = 0, mag[3] = {0, 0, 0};
+    RingPlan ring;
+    std::vector<float> words;
+    TableLayout tl;
+    int zero_pair = -1;
+};
+
+// Schedule choices of the forward: tile rows (tile shape) and tile order
+// (block-to-CTA schedule). 0 = defaults.
+struct Tuning {
+    int ty = 0;
+    int order = 0;  // 0: largest blocks first, raster inside a block; 1: tiles interleaved across blocks
+};
+
+// One pass = the blocks whose radiality + intensity stacks fit the budget
+// together; lists of all passes are concatenated (tile block indices are
+// relative to the pass's first block).
+struct PassPlan {
+    size_t b0 = 0, b1 = 0, t0 = 0, t1 = 0, p0 = 0;
+    long long stack_elems = 0;
+    int chunk = 1, nchunks = 1, grid = 1;
+    size_t smem = 0;
+    long long nitems = 0, units = 0;
+};
+struct PassSet {
+    std::vector<BlockDev> blocks;
+    std::vector<TileDesc> tiles;
+    std::vector<long long> prefix;
+    std::vector<PassPlan> passes;
+    long long max_stack = 0;
+    int ty = 0;
+};
+
+
+// A captured forward: the whole launch sequence of one call (copies, clears,
+// all passes) replayed with one cudaGraphLaunch while the call's arguments and
+// the scratch it was captured on are unchanged.
+struct GraphPlan {
+    std::string key;
+    std::vector<const void*> deps;  // scratch pointers baked into the graph
+    cudaGraphExec_t exec = nullptr;
+    PassSet ps;
+    DevBuf blocks, tiles, prefix, counters;
+    std::vector<cudaEvent_t> evs;
+    ~GraphPlan() {
+        if (exec) cudaGraphExecDestroy(exec);
+        for (cudaEvent_t e : evs) cudaEventDestroy(e);
+        blocks.release();
+        tiles.release();
+        prefix.release();
+        counters.release();
+    }
+};
+
+
+}  // namespace rfba
+
+struct rfba_ctx {
+    int device = 0;
+    int sm_count = 0;
+    size_t budget = 0;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;
+    rfba::DevBuf in, out, rad, inten, blocks, tiles, tables, counter, prefix;
+    rfba::PlanCache plan;
+    bool timing = false;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // calls share the scratch: a call on another stream than the previous call
+    // first waits for that call's work
+    cudaEvent_t xev = nullptr;
+    cudaStream_t last_stream = nullptr;
+    bool have_last = false;
+    double last_rad_ms = 0.0, last_temporal_ms = 0.0;
+    long long launches = 0;
+    long long last_flop_units = 0;  // subvoxel-time-points computed by the last call
+    int grid_override = 0;          // CTAs for the radiality kernel (0 = occupancy x SMs)
+    int chunk_override = 0;         // time points per work item (0 = automatic)
+    int last_passes = 0;            // passes of the last forward (1 = its stacks are all resident)
+    // differentiable path: buffers and the forward the backward can reuse
+    rfba::DevBuf shifted, tmp1, tmp2, gS, gI, gin, dshift, ablocks, atiles, acounter, errw;
+    struct Train {
+        bool valid = false;
+        rfba_srrf_config cfg;
+        int dims[4] = {0, 0, 0, 0};
+        const void* in = nullptr;
+        const void* shifts = nullptr;
+        const float* iprime = nullptr;
+        rfba::BlockDev blk;
+    } train;
+    double last_backward_ms = 0.0;
+    // forward schedule: per-pass timing events, autotuned schedules, captured graphs
+    std::vector<cudaEvent_t> pev;
+    cudaStream_t cap = nullptr;  // stream the graphs are captured on
+    std::map<std::string, std::pair<int, int>> tunes;  // schedule key -> (tile rows, tile order)
+    std::vector<std::unique_ptr<rfba::GraphPlan>> graphs;  // most recent first
+    // spot seeding scratch
+    rfba::DevBuf seed_w, seed_sums, seed_carry, seed_map, seed_vox, seed_xyz;
+    // 3B spot-gradient scratch
+    rfba::DevBuf tb_val, tb_der, tb_em, tb_res, tb_par, tb_bg, tb_pix, tb_pixels;
+    // 3B Gibbs sampler scratch
+    rfba::DevBuf gb_pix, gb_pixels, gb_spots, gb_si, gb_moff, gb_midx, gb_state, gb_cur, gb_em, gb_bar, gb_var,
+        gb_ostate, gb_oint, gb_oerr, gb_lp, gb_filt;
+    int last_ty = 0, last_order = 0, last_graph = 0, last_tuned = 0;
+};
