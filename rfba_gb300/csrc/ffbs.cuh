@@ -1,0 +1,230 @@
+// Forward filtering and backward-sampling tables of 3B's three-state spot
+// chain (on / off / bleached), shared by the Gibbs sampler and the
+// sampled-background Hessian.
+//
+// The filter (forward_algorithm_delta / _delta2, RFBA Main/forward_algorithm.h:
+// 385-431) is the reference's log-space recursion held in other coordinates:
+// each state's forward value is a mantissa in [0.5, 1) with its own
+// power-of-two exponent, so the sequential chain needs neither exp nor log.
+// The mantissas are double-float numbers (an unevaluated sum hi + lo of two
+// floats, |lo| <= ulp(hi) / 2; Dekker, "A floating-point technique for
+// extending the available precision", Numer. Math. 18, 1971, with the
+// products' error terms from fused multiply-adds), about 2^-46 relative per
+// step: on this GPU a dependent FP64 operation costs on the order of a hundred
+// cycles and the FP32 pipe 64 times the FP64 one, and the chain is strictly
+// sequential over frames. Terms more than 2^100 below the largest term of a
+// step are dropped (far below the format's precision).
+//
+// Backward sampling (backward_sampling, forward_algorithm.h:546-570) draws
+// the last frame from the filter and every earlier frame from the filter
+// weighted by the transition into the next frame's state. For every frame and
+// each state the next frame may hold (index 3: none, for the last frame) the
+// two cumulative thresholds of states 0 and 1 are formed in FP32 and compared
+// with the frame's 53-bit uniform exactly, as integers (u <= p exactly when
+// u * 2^53 <= floor(p * 2^53)).
+#pragma once
+#include <cstdint>
+
+namespace rfba {
+namespace ffbs {
+
+constexpr int kZeroExp = -(1 << 29);  // exponent of a zero forward value
+constexpr int kDropBits = 100;
+
+__device__ __forceinline__ float2 df_from(double v) {
+    const float h = __double2float_rn(v);
+    return make_float2(h, __double2float_rn(v - (double)h));
+}
+__device__ __forceinline__ double df_to(float2 a) { return (double)a.x + (double)a.y; }
+// s + e with |s| >= |e| as a normalised pair
+__device__ __forceinline__ float2 df_fast_two_sum(float s, float e) {
+    const float r = s + e;
+    return make_float2(r, e - (r - s));
+}
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
+    const float p = a.x * b.x;
+    float e = fmaf(a.x, b.x, -p);
+    e = fmaf(a.x, b.y, e);
+    e = fmaf(a.y, b.x, e);
+    return df_fast_two_sum(p, e);
+}
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+    const float s = a.x + b.x;
+    const float v = s - a.x;
+    float e = (a.x - (s - v)) + (b.x - v);
+    e += a.y + b.y;
+    return df_fast_two_sum(s, e);
+}
+// 2^d as a float, -126 <= d <= 127
+__device__ __forceinline__ float pow2f(int d) { return __int_as_float((d + 127) << 23); }
+
+// exp(x) = mant 2^k for x <= 0 (mant in [1, 2)): x = k ln2 + r with r by one
+// fused multiply-add. Relative probabilities below 2^-(2^24) are 0. exp(0) is
+// (1, 0) without a call.
+__device__ __forceinline__ void exp_split(double x, double* mant, int* k) {
+    if (x == 0.0) {
+        *mant = 1.0;
+        *k = 0;
+        return;
+    }
+    const double kd = floor(x * 1.4426950408889634);
+    if (kd < -16777216.0) {
+        *mant = 0.0;
+        *k = kZeroExp;
+        return;
+    }
+    *mant = exp(fma(-kd, 0.6931471805599453, x));
+    *k = (int)kd;
+}
+
+// A frame's emission terms (p(on), p(off) relative to their larger one) in
+// filter form: double-float mantissas emf[2t + s] and exponents emk[2t + s],
+// s = 0 on, 1 off (the bleached state emits as off).
+__device__ __forceinline__ void emission_terms(double lon, double loff, float2* emf, int* emk) {
+    const double m = lon > loff ? lon : loff;
+    double mo, mf;
+    int ko, kf;
+    exp_split(lon - m, &mo, &ko);
+    exp_split(loff - m, &mf, &kf);
+    emf[0] = df_from(mo);
+    emk[0] = ko;
+    emf[1] = df_from(mf);
+    emk[1] = kf;
+}
+
+// The forward filter over F frames, run by one warp (lanes 0-2 carry the
+// states; the step is branch-free, so the three lanes never diverge).
+// xs[3t + j], es[3t + j]: frame t's forward value of state j.
+__device__ __forceinline__ void forward_filter(int lane, int F, const double* A, const double* pi, const float2* emf,
+                                               const int* emk, float2* xs, int* es) {
+    if (lane >= 3) return;
+    const unsigned m3 = 0x7u;
+    const int j = lane;
+    float2 Aj[3];
+    bool nz[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        Aj[i] = df_from(A[i * 3 + j]);
+        nz[i] = A[i * 3 + j] != 0.0;
+    }
+    const int es_sel = j == 0 ? 0 : 1;
+    float2 x;
+    int E;
+    // y * 2^base as a mantissa in [0.5, 1) and an exponent; zero when y is not
+    // a positive normal float or base is the zero exponent
+    auto normalise = [&](float2 y, int base) {
+        const int ex = (__float_as_int(y.x) >> 23) & 0xff;
+        const bool zero = !(y.x > 0.f) || ex == 0 || base == kZeroExp;
+        const int sh = ex - 126;
+        const float sc = pow2f(zero ? 0 : -sh);
+        x = zero ? make_float2(0.f, 0.f) : make_float2(y.x * sc, y.y * sc);
+        E = zero ? kZeroExp : base + sh;
+    };
+    {
+        const int ke = emk[es_sel];
+        normalise(df_mul(df_from(pi[j]), emf[es_sel]), (pi[j] == 0.0 || ke == kZeroExp) ? kZeroExp : ke);
+    }
+    xs[j] = x;
+    es[j] = E;
+    for (int t = 1; t < F; ++t) {
+        const float2 mant = emf[2 * t + es_sel];
+        const int ke = emk[2 * t + es_sel];
+        int Ev[3];
+        float2 xv[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            Ev[i] = __shfl_sync(m3, E, i);
+            xv[i].x = __shfl_sync(m3, x.x, i);
+            xv[i].y = __shfl_sync(m3, x.y, i);
+        }
+        int Em = kZeroExp;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) Em = (nz[i] && Ev[i] > Em) ? Ev[i] : Em;
+        float2 y = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const int dd = Ev[i] - Em;
+            const bool use = nz[i] && Ev[i] != kZeroExp && dd >= -kDropBits;
+            const float sc = use ? pow2f(dd < -126 ? -126 : dd) : 0.f;
+            float2 tm = df_mul(Aj[i], xv[i]);
+            tm.x *= sc;
+            tm.y *= sc;
+            y = df_add(y, tm);
+        }
+        normalise(df_mul(y, mant), (Em == kZeroExp || ke == kZeroExp) ? kZeroExp : Em + ke);
+        xs[3 * t + j] = x;
+        es[3 * t + j] = E;
+    }
+}
+
+// floor(p * 2^53) for a float p in [0, 1], by integer arithmetic
+__device__ __forceinline__ unsigned long long threshold53(float p) {
+    const int b = __float_as_int(p);
+    const int e = (b >> 23) & 0xff;
+    if (p <= 0.f || e == 0) return 0ull;
+    const unsigned long long m = (unsigned long long)((b & 0x7fffff) | 0x800000);  // p = m 2^(e - 150)
+    const int s = e - 97;                                                          // p 2^53 = m 2^s
+    return s >= 0 ? (m << s) : (s > -64 ? (m >> -s) : 0ull);
+}
+
+// The draws of frame t for each state the next frame may hold (index 3: no
+// next frame) from the frame's uniform U (53-bit integer): the filter's
+// values weighted by the transition into that state, cumulative thresholds of
+// states 0 and 1 as fractions of their total in FP32 (no weight at all: state
+// 0, as a zero total gives in the reference). Af: A as floats; nzA: bit 3i + n
+// set where A[i][n] != 0.
+__device__ __forceinline__ void frame_draws(int t, unsigned long long U, const float2* xs, const int* es,
+                                            const float* Af, unsigned nzA, unsigned char out[4]) {
+    float xv[3];
+    int ev[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        xv[i] = xs[3 * t + i].x;
+        ev[i] = es[3 * t + i];
+    }
+#pragma unroll
+    for (int nx = 0; nx < 4; ++nx) {
+        int Em = kZeroExp;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const bool use = (nx == 3 || ((nzA >> (3 * i + nx)) & 1u)) && ev[i] != kZeroExp;
+            Em = (use && ev[i] > Em) ? ev[i] : Em;
+        }
+        float a[3], tot = 0.f;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const bool use = (nx == 3 || ((nzA >> (3 * i + nx)) & 1u)) && ev[i] != kZeroExp;
+            const int dd = ev[i] - Em;
+            const float tr = nx == 3 ? 1.f : Af[3 * i + nx];
+            a[i] = (use && dd >= -126) ? xv[i] * pow2f(dd < -126 ? -126 : dd) * tr : 0.f;
+            tot += a[i];
+        }
+        unsigned long long T0 = 1ull << 53, T1 = 1ull << 53;
+        if (tot > 0.f) {
+            T0 = threshold53(a[0] / tot);
+            T1 = threshold53((a[0] + a[1]) / tot);
+        }
+        out[nx] = (unsigned char)(U <= T0 ? 0 : (U <= T1 ? 1 : 2));
+    }
+}
+
+// 53-bit integer uniform of Philox outputs a, b (u53 = U 2^-53)
+__device__ __forceinline__ unsigned long long uniform53(uint32_t a, uint32_t b) {
+    return ((unsigned long long)(a >> 5) << 26) | (unsigned long long)(b >> 6);
+}
+
+// The filtering distribution of frame t (trace output).
+__device__ __forceinline__ void filter_probs(int t, const float2* xs, const int* es, double out[3]) {
+    int Em = kZeroExp;
+    for (int i = 0; i < 3; ++i) Em = max(Em, es[3 * t + i]);
+    double w[3], tot = 0.0;
+    for (int i = 0; i < 3; ++i) {
+        const int dd = es[3 * t + i] - Em;
+        w[i] = (es[3 * t + i] != kZeroExp && dd >= -1022) ? df_to(xs[3 * t + i]) * ldexp(1.0, dd) : 0.0;
+        tot += w[i];
+    }
+    for (int i = 0; i < 3; ++i) out[i] = w[i] / tot;
+}
+
+}  // namespace ffbs
+}  // namespace rfba
