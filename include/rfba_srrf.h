@@ -364,6 +364,107 @@ int rfba_3b_optimise_pass(rfba_ctx* ctx, const rfba_3b_model* model, const doubl
 /* The Gibbs seed of spot s in pass `pass` of rfba_3b_optimise_pass. */
 unsigned long long rfba_3b_pass_seed(unsigned long long seed, int pass, int s);
 
+/* sampled_background_spot_hessian_ffbs (RFBA Main/multispot5.cc:824-985): the
+ * Hessian of one spot's log probability with the other spots' intensities
+ * sampled by the S draws sample_bg [S][F][P] (the spot taken off them, as
+ * rfba_3b_gibbs_sample's exclude_spot gives them) and the spot's own states by
+ * bs_iterations backward samples per draw of its forward-filtered on / off
+ * chain (SpotWithBackground over all P pixels, spot_with_background.hh:
+ * 98-150): the sum over samples of hess + deriv deriv^T over the frames where
+ * the spot is on (hess = sum_p e H_p - g_p g_p^T, deriv = sum_p e g_p, e the
+ * residual with the spot on, g_p and H_p the spot's gradient and Hessian at
+ * pixel p, storm.h:87-146), divided by (bs_iterations S variance), less the
+ * outer product of the mean derivative, plus the second derivatives of the
+ * log-normal priors on brightness and blur (storm.h:446-449). hess[25]
+ * (row-major, symmetric; the reference leaves its entry [4][3] unwritten) is
+ * host memory. Random numbers: Philox4x32-10 keyed by seed. 1 <= F <= 2048,
+ * bs_iterations >= 1. FP64. Synchronous. */
+int rfba_3b_spot_hessian(rfba_ctx* ctx, const rfba_3b_model* model, const double* sample_bg,
+                         const double* pixel_intensities, const int* pixels, int S, int F, int P,
+                         const double spot[5], int bs_iterations, unsigned long long seed, double hess[25],
+                         int ptr_flags, void* stream);
+
+/* Settings of a 3B block fit (FitSpots, RFBA Main/multispot5.cc:1329-1505), the
+ * reference's variable names and multispot5.cfg values in brackets. */
+typedef struct rfba_3b_fit_params {
+    int main_passes;             /* main.passes (4) */
+    int main_samples;            /* main.gibbs.samples (10) */
+    int main_cg_max_iterations;  /* main.cg.max_iterations (5) */
+    int sweeps;                  /* gibbs.mixing_iterations (1) */
+    int add_remove_tries;        /* add_remove.tries (10) */
+    int opt_samples;             /* add_remove.optimizer.samples (20) */
+    int opt_attempts;            /* add_remove.optimizer.attempts (10) */
+    int opt_hess_inner_samples;  /* add_remove.optimizer.hessian_inner_samples (1000) */
+    int h_outer_samples;         /* add_remove.hessian.outer_samples (100) */
+    int h_inner_samples;         /* add_remove.hessian.inner_samples (1000) */
+    int thermo_samples;          /* add_remove.thermo.samples (1000) */
+    double limit[5];             /* cg.max_motion x (brightness limit, 1, 1, 1, 1) */
+    double position_extra_radius; /* position.extra_radius (2.3); < 0: position.use_prior = 0 */
+} rfba_3b_fit_params;
+
+/* What one model modification did. */
+typedef struct rfba_3b_modify_record {
+    int added;        /* 1: a spot was proposed for addition; 0: one for removal */
+    int kept;         /* 1: the model without the mobile spot, 2: with it */
+    int zero_prior;   /* the optimised mobile spot left the allowed area */
+    int bad_hessian;  /* the Hessian there was not negative definite: the original model kept */
+    int evaluations;  /* gradient evaluations of the mobile spot's optimisation */
+    double model1_energy, model2_energy;  /* -free energy of each model (when compared) */
+    double occam;     /* -log(det(-H / 2 pi)) / 2, Laplace's approximation */
+    double position_log_prior;  /* log prior of model 2 minus model 1 */
+    double spot[5];   /* the optimised mobile spot */
+} rfba_3b_modify_record;
+
+/* One try of FitSpots::try_modifying_model (RFBA Main/multispot5.cc:1840-2160)
+ * on the GPU. Model 1 is the spots without, model 2 with, a mobile spot: with
+ * probability 1/2 (always when *nspots <= 1) a spot is proposed at a random
+ * pixel plus a uniform offset in [-0.5, 0.5) per axis, with the modes of the
+ * brightness and blur priors, else a random spot is proposed for removal. The
+ * mobile spot is optimised on opt_samples GibbsSampler2 draws
+ * (ConjugateGradientOnly<5>, at most 500 line searches per attempt); after
+ * each attempt but the last the sampled-background Hessian
+ * (rfba_3b_spot_hessian, opt_hess_inner_samples) is decomposed and, unless it
+ * is negative definite, the optimiser restarts 0.1 along the eigenvector of its
+ * fourth-smallest eigenvalue. A mobile spot outside the allowed area keeps
+ * model 1. Otherwise the Hessian is taken again on h_outer_samples draws of the
+ * sampler over all pixels (GibbsSampler, sampled_multispot.h:240-330) with
+ * h_inner_samples backward samples; when its negation's smallest eigenvalue is
+ * above 1e-6, model 2 is kept if its negative free energy (rfba_3b_free_energy,
+ * thermo_samples) plus -log(det(-H / 2 pi)) / 2 plus the position prior's log
+ * ratio exceeds model 1's, and otherwise the original model is kept. spots
+ * [capacity][5] (capacity >= *nspots + 1), pixel_intensities [F][P] and pixels
+ * [P][3] (sorted by (z, y, x)) are host memory; *nspots receives the model
+ * kept; record may be NULL. The proposal's random choices come from a
+ * SplitMix64 stream of seed, the draws' from Philox4x32-10 with seeds mixed
+ * from it. Eigenvectors are signed with their largest component positive (the
+ * reference's LAPACK sign is not specified). Synchronous. */
+int rfba_3b_modify_model(rfba_ctx* ctx, const rfba_3b_model* model, const double* pixel_intensities,
+                         const int* pixels, int F, int P, double* spots, int* nspots, int capacity,
+                         const rfba_3b_fit_params* params, unsigned long long seed, rfba_3b_modify_record* record);
+
+/* Progress of rfba_3b_fit after each step of iteration `iteration`: step <
+ * main_passes is the pass just finished, step >= main_passes the model
+ * modification step - main_passes; spots [nspots][5] are the current ones. A
+ * non-zero return stops the fit there (it returns RFBA_OK with those spots). */
+typedef int (*rfba_3b_fit_fn)(int iteration, int step, const double* spots, int nspots, void* user);
+
+/* FitSpots::run (RFBA Main/multispot5.cc:2234-2278) on the GPU: `iterations`
+ * iterations from first_iteration, each main_passes passes
+ * (rfba_3b_optimise_pass, ordered by pass + iteration as the reference orders
+ * them) and add_remove_tries model modifications (rfba_3b_modify_model); a
+ * modification is skipped when spots has no room for another spot. Arguments
+ * as rfba_3b_modify_model; progress may be NULL. Synchronous. */
+int rfba_3b_fit(rfba_ctx* ctx, const rfba_3b_model* model, const double* pixel_intensities, const int* pixels, int F,
+                int P, double* spots, int* nspots, int capacity, const rfba_3b_fit_params* params,
+                int first_iteration, int iterations, unsigned long long seed, rfba_3b_fit_fn progress, void* user);
+
+/* Host helpers of the model modification, exported for testing: eigenvalues
+ * (ascending) and eigenvectors (rows, largest-magnitude component positive)
+ * of a symmetric 5x5 matrix by cyclic Jacobi rotations, and the determinant of
+ * a 5x5 matrix by Gaussian elimination with partial pivoting. No device work. */
+int rfba_sym_eigen5(const double a[25], double evals[5], double evecs[25]);
+double rfba_det5(const double a[25]);
+
 /* Device-side failure check. No counterpart in the reference (GradientCalc.cpp
  * and kernel.cu check no CUDA status; every call returns 0). Waits for the
  * work the context last enqueued and reports failures its kernels recorded

@@ -14,7 +14,16 @@ order where that decides the bits:
   filter (forward_algorithm.h:385-431, normalised) and the forward-backward
   posterior (forward_algorithm.h:447-484);
 - `free_energy`: the arithmetic of NegativeFreeEnergy::compute_with_mask
-  (multispot5.cc:335-405) given each draw's sum of squared residuals.
+  (multispot5.cc:335-405) given each draw's sum of squared residuals;
+- `spot_hessian_table`: spot_shape_hess_position (storm.h:87-146), value,
+  gradient and Hessian of a spot at every pixel;
+- `hessian_expectation`: what sampled_background_spot_hessian_ffbs
+  (multispot5.cc:824-985) converges to as its backward samples grow: the
+  per-frame parts over all pixels, the posterior of the spot's chain per
+  sample (SpotWithBackground, forward_algorithm_delta, backward_sampling) and
+  the expectation of hess + deriv deriv^T under it, exactly, from the
+  posterior's single and pair marginals (backward sampling walks a reverse-time
+  Markov chain, so P(s_t = 0, s_u = 0) is a product of its transitions).
 
 `port_*` run the C++ port in oracle/gibbs_port.cpp (the reference's MT19937
 stream, sampler and main-loop pass restated; built everywhere, the CPU
@@ -192,6 +201,96 @@ def free_energy(residuals, variance, P, F, spots, mu_b, sigma_b, mu_blur, sigma_
     return -(total + priors - log_final)
 
 
+def spot_hessian_table(pixels, spot, z_factor):
+    """(value [P], gradient [P][5], Hessian [P][5][5]) of spot_shape_hess_position
+    at every pixel (storm.h:87-146), symmetric (the reference leaves [4][3]
+    unwritten)."""
+    px = np.asarray(pixels, np.float64).reshape(-1, 3)
+    p0, p1 = float(spot[0]), float(spot[1])
+    dx, dy, dz = px[:, 0] - spot[2], px[:, 1] - spot[3], px[:, 2] - spot[4]
+    s = -(dx * dx + dy * dy + (dz / z_factor) ** 2) / (2 * p1 * p1)
+    r = math.sqrt(2 * math.pi)
+    es = np.exp(s)
+    val = es * p0 / (p1 * r)
+    c = es / (p1 * r)
+    g = np.stack([c, c * (-p0 * (1 + 2 * s) / p1), c * dx * (p0 / p1 ** 2), c * dy * (p0 / p1 ** 2),
+                  c * dz * (p0 / p1 ** 2)], 1)
+    H = np.zeros((len(px), 5, 5))
+    H[:, 0, 1] = -es * (1 + 2 * s) / (p1 * p1 * r)
+    for a, d in ((2, dx), (3, dy), (4, dz)):
+        H[:, 0, a] = es * d / (p1 ** 3 * r)
+        H[:, 1, a] = -p0 * es * (3 + 2 * s) * d / (p1 ** 4 * r)
+        H[:, a, a] = p0 * es * (d * d - p1 * p1) / (r * p1 ** 5)
+    H[:, 1, 1] = 2 * p0 * es * (1 + 5 * s + 2 * s * s) / (p1 ** 3 * r)
+    H[:, 2, 3] = p0 * es * dx * dy / (r * p1 ** 5)
+    H[:, 2, 4] = p0 * es * dx * dz / (r * p1 ** 5)
+    H[:, 3, 4] = p0 * es * dy * dz / (r * p1 ** 5)
+    iu = np.triu_indices(5, 1)
+    H[:, iu[1], iu[0]] = H[:, iu[0], iu[1]]
+    return val, g, H
+
+
+def _posterior_chain(lp_on, lp_off, A, pi):
+    """Single marginals m [F][3] and the reverse-time transitions R [F][3][3]
+    (R[t][j][i] = P(s_t = i | s_{t+1} = j)) of the chain's posterior."""
+    F = len(lp_on)
+    A = np.asarray(A, np.float64).reshape(3, 3)
+    lB = np.stack([lp_on, lp_off, lp_off], 1)
+    alpha = np.empty((F, 3))
+    a = np.asarray(pi, np.float64) * np.exp(lB[0] - lB[0].max())
+    alpha[0] = a / a.sum()
+    for t in range(1, F):
+        a = (alpha[t - 1] @ A) * np.exp(lB[t] - lB[t].max())
+        alpha[t] = a / a.sum()
+    R = np.zeros((F, 3, 3))
+    for t in range(F - 1):
+        w = alpha[t][:, None] * A  # [i][j]
+        tot = w.sum(0)
+        R[t] = np.where(tot[:, None] > 0, (w / np.where(tot > 0, tot, 1)).T, 0)
+    m = np.empty((F, 3))
+    m[F - 1] = alpha[F - 1]
+    for t in range(F - 2, -1, -1):
+        m[t] = m[t + 1] @ R[t]
+    return m, R
+
+
+def hessian_expectation(bg, pix, pixels, spot, A, pi, variance, z_factor, mu_b, sigma_b, mu_blur, sigma_blur):
+    """The limit of sampled_background_spot_hessian_ffbs as bs_iterations grows."""
+    bg = np.asarray(bg, np.float64)
+    pix = np.asarray(pix, np.float64)
+    S, F, P = bg.shape
+    val, g, H = spot_hessian_table(pixels, spot, z_factor)
+    gg = np.einsum("pa,pb->ab", g, g)
+    cst = P * math.log(2 * math.pi * variance) / 2
+    sum_h = np.zeros((5, 5))
+    sum_d = np.zeros(5)
+    for i in range(S):
+        e = pix - (bg[i] + val)  # [F][P]
+        hp = np.einsum("fp,pab->fab", e, H) - gg
+        dp = e @ g
+        lon = -np.sum(e * e, 1) / (2 * variance) - cst
+        loff = -np.sum((pix - bg[i]) ** 2, 1) / (2 * variance) - cst
+        m, R = _posterior_chain(lon, loff, A, pi)
+        on = m[:, 0]
+        sum_h += np.einsum("f,fab->ab", on, hp)
+        sum_d += on @ dp
+        # E[D D^T] = sum_t P(t on) d_t d_t^T + sum_{t < u} P(t on, u on) (d_t d_u^T + d_u d_t^T)
+        for u in range(F):
+            sum_h += on[u] * np.outer(dp[u], dp[u])
+            cond = np.array([1.0, 0.0, 0.0])  # P(s_t = . | s_u = 0), walking t down from u
+            for t in range(u - 1, -1, -1):
+                cond = cond @ R[t]
+                pj = on[u] * cond[0]
+                if pj != 0:
+                    sum_h += pj * (np.outer(dp[t], dp[u]) + np.outer(dp[u], dp[t]))
+    sum_h /= S * variance
+    sum_d /= S * variance
+    out = sum_h - np.outer(sum_d, sum_d)
+    out[0, 0] += (1 + (_ln(spot[0]) - mu_b - 1) / (sigma_b * sigma_b)) / (spot[0] * spot[0])
+    out[1, 1] += (1 + (_ln(spot[1]) - mu_blur - 1) / (sigma_blur * sigma_blur)) / (spot[1] * spot[1])
+    return out
+
+
 # ---- the reference's own code (compiled here) --------------------------------
 
 def ref_available() -> bool:
@@ -214,6 +313,7 @@ def ref():
         L.ref_gibbs_run.argtypes = [dp, dp, ip, ip, i, i, i, dp, dp, d, i, i, i, bp, dp]
         L.ref_free_energy.argtypes = [dp, ip, dp, ip, ip, i, i, i, dp, dp, d, d, d, d, d, d, i, i, i, dp]
         L.ref_free_energy.restype = d
+        L.ref_spot_hessian.argtypes = [dp, dp, ip, i, i, i, dp, dp, dp, d, d, d, d, d, d, i, i, dp]
         _ref = L
     return _ref
 
@@ -279,6 +379,24 @@ def ref_free_energy(pix, pixels, spots, moff, midx, A, pi, variance, z_factor, m
                               _p(pi, ctypes.c_double), variance, z_factor, mu_b, sigma_b, mu_blur, sigma_blur,
                               samples, sweeps, seed, _p(res, ctypes.c_double))
     return v, res
+
+
+def ref_spot_hessian(bg, pix, pixels, spot, A, pi, variance, z_factor, mu_b, sigma_b, mu_blur, sigma_blur,
+                     bs_iterations, seed):
+    """The reference's sampled_background_spot_hessian_ffbs (one thread, its
+    MT19937 seeded by simple_seed(seed)); entry [4][3] is indeterminate."""
+    bg = np.ascontiguousarray(bg, np.float64)
+    pix = np.ascontiguousarray(pix, np.float64)
+    S, F, P = bg.shape
+    px = np.ascontiguousarray(pixels, np.int32)
+    sp = np.ascontiguousarray(spot, np.float64)
+    A = np.ascontiguousarray(A, np.float64).reshape(9)
+    pi = np.ascontiguousarray(pi, np.float64)
+    out = np.empty((5, 5))
+    ref().ref_spot_hessian(_p(bg, ctypes.c_double), _p(pix, ctypes.c_double), _p(px, ctypes.c_int), S, F, P,
+                           _p(sp, ctypes.c_double), _p(A, ctypes.c_double), _p(pi, ctypes.c_double), variance, z_factor,
+                           mu_b, sigma_b, mu_blur, sigma_blur, bs_iterations, seed, _p(out, ctypes.c_double))
+    return out
 
 
 # ---- the C++ port (oracle/gibbs_port.cpp) -------------------------------------

@@ -154,6 +154,70 @@ int ref_gibbs_run(const double* pix, const double* si, const int* moff, const in
     return 0;
 }
 
+// sampled_background_spot_hessian_ffbs (multispot5.cc:824-985) for one thread
+// (MAXTHREAD = 1: one MT19937, simple_seed(seed), draws every backward sample):
+// the reference's compute_spot_intensity_hessian, compute_spot_intensity,
+// SpotWithBackground over all pixels, forward_algorithm_delta and
+// backward_sampling, the per-frame parts and sums written out as hess_handler
+// has them. bg [S][F][P]; hess [25] row-major. The reference never writes
+// entry [4][3] of its per-pixel Hessian (storm.h:143), so hess[4 * 5 + 3] is
+// indeterminate; the upper triangle is what is defined.
+int ref_spot_hessian(const double* bg, const double* pix, const int* pixels, int S, int F, int P, const double* spot,
+                     const double* A_in, const double* pi_in, double variance, double zFactor, double mu_brightness,
+                     double sigma_brightness, double mu_blur, double sigma_blur, int bs_iterations, int seed,
+                     double* hess) {
+    const vector<vector<double> > pixel_intensities = frames_of(pix, F, P);
+    const vector<Ref3D> px = refs_of(pixels, P);
+    const Vector<5> sp = makeVector(spot[0], spot[1], spot[2], spot[3], spot[4]);
+    const vector<tuple<double, Vector<5>, Matrix<5> > > spot_hess_etc =
+        SampledMultispot::compute_spot_intensity_hessian(px, sp, zFactor);
+    const vector<double> spot_intensities = SampledMultispot::compute_spot_intensity(px, sp, zFactor);
+    const Matrix<3> A = A_of(A_in);
+    const Vector<3> pi = makeVector(pi_in[0], pi_in[1], pi_in[2]);
+    const vector<int> O = SampledMultispot::sequence(F);
+    MT19937 rng;
+    rng.simple_seed(seed);
+    Matrix<5> sum_hess = Zeros;
+    Vector<5> sum_deriv = Zeros;
+    vector<pair<Matrix<5>, Vector<5> > > hess_and_deriv_part(F);
+    for (int i = 0; i < S; i++) {
+        const vector<vector<double> > bgi = frames_of(bg + (size_t)i * F * P, F, P);
+        SpotWithBackground B(bgi, spot_intensities, pixel_intensities, variance);
+        for (int frame = 0; frame < F; frame++) {
+            Matrix<5> h = Zeros;
+            Vector<5> d = Zeros;
+            for (int pixel = 0; pixel < P; pixel++) {
+                double e = pixel_intensities[frame][pixel] - (bgi[frame][pixel] + spot_intensities[pixel]);
+                h += e * get<2>(spot_hess_etc[pixel]) -
+                     get<1>(spot_hess_etc[pixel]).as_col() * get<1>(spot_hess_etc[pixel]).as_row();
+                d += e * get<1>(spot_hess_etc[pixel]);
+            }
+            hess_and_deriv_part[frame] = make_pair(h, d);
+        }
+        std::vector<array<double, 3> > delta = forward_algorithm_delta(A, pi, B, O);
+        for (int b = 0; b < bs_iterations; b++) {
+            vector<State> current_sample = backward_sampling<3, State>(A, delta, rng);
+            Matrix<5> h = Zeros;
+            Vector<5> d = Zeros;
+            for (int frame = 0; frame < F; frame++)
+                if (current_sample[frame] == 0) {
+                    h += hess_and_deriv_part[frame].first;
+                    d += hess_and_deriv_part[frame].second;
+                }
+            sum_hess += h + d.as_col() * d.as_row();
+            sum_deriv += d;
+        }
+    }
+    sum_hess /= (bs_iterations * S * variance);
+    sum_deriv /= (bs_iterations * S * variance);
+    sum_hess -= sum_deriv.as_col() * sum_deriv.as_row();
+    sum_hess[0][0] += hess_log_log_normal(sp[0], mu_brightness, sigma_brightness);
+    sum_hess[1][1] += hess_log_log_normal(sp[1], mu_blur, sigma_blur);
+    for (int r = 0; r < 5; ++r)
+        for (int c = 0; c < 5; ++c) hess[r * 5 + c] = sum_hess[r][c];
+    return 0;
+}
+
 // NegativeFreeEnergy::compute_with_mask (multispot5.cc:335-405), its steps in
 // order, on the reference's GibbsSampler2 and MT19937 (simple_seed(seed)).
 // residuals [samples] receives each draw's -err_sum (may be NULL).

@@ -1199,7 +1199,8 @@ int rfba_ctx_destroy(rfba_ctx* c) {
                       &c->tb_pix, &c->tb_pixels, &c->seed_w, &c->seed_sums, &c->seed_carry, &c->seed_map, &c->seed_vox,
                       &c->seed_xyz, &c->gb_pix, &c->gb_pixels, &c->gb_spots, &c->gb_si, &c->gb_moff, &c->gb_midx,
                       &c->gb_state, &c->gb_cur, &c->gb_em, &c->gb_bar, &c->gb_var, &c->gb_ostate, &c->gb_oint,
-                      &c->gb_oerr, &c->gb_lp, &c->gb_filt})
+                      &c->gb_oerr, &c->gb_lp, &c->gb_filt, &c->hs_tab, &c->hs_part, &c->hs_gg, &c->hs_phi,
+                      &c->hs_frame, &c->hs_out})
         b->release();
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);

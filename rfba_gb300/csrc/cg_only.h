@@ -86,6 +86,23 @@ struct CgOnly5 {
         return 0;
     }
 
+    // Restart from s0 with gvec taken as the gradient there, without an
+    // evaluation (conjugate_gradient_only.h:65-86, init(start, deriv)).
+    void restart(const double s0[5], const double gvec[5]) {
+        const double eps = std::numeric_limits<double>::epsilon();
+        for (int i = 0; i < 5; ++i) {
+            x[i] = s0[i];
+            g[i] = gvec[i];
+            h[i] = g[i];
+            mh[i] = -h[i];
+        }
+        tolerance = std::sqrt(eps);
+        ls_tolerance = std::sqrt(eps);
+        ls_epsilon = 1e-20;
+        max_iterations = 5 * 100;
+        iterations = 0;
+    }
+
     template <class Grad>
     int line_search(Grad& grad) {
         ++iterations;

@@ -140,5 +140,7 @@ struct rfba_ctx {
     // 3B Gibbs sampler scratch
     rfba::DevBuf gb_pix, gb_pixels, gb_spots, gb_si, gb_moff, gb_midx, gb_state, gb_cur, gb_em, gb_bar, gb_var,
         gb_ostate, gb_oint, gb_oerr, gb_lp, gb_filt;
+    // 3B sampled-background Hessian scratch
+    rfba::DevBuf hs_tab, hs_part, hs_gg, hs_phi, hs_frame, hs_out;
     int last_ty = 0, last_order = 0, last_graph = 0, last_tuned = 0;
 };

@@ -167,45 +167,53 @@ __device__ __forceinline__ unsigned long long threshold53(float p) {
     return s >= 0 ? (m << s) : (s > -64 ? (m >> -s) : 0ull);
 }
 
-// The draws of frame t for each state the next frame may hold (index 3: no
-// next frame) from the frame's uniform U (53-bit integer): the filter's
-// values weighted by the transition into that state, cumulative thresholds of
-// states 0 and 1 as fractions of their total in FP32 (no weight at all: state
-// 0, as a zero total gives in the reference). Af: A as floats; nzA: bit 3i + n
-// set where A[i][n] != 0.
-__device__ __forceinline__ void frame_draws(int t, unsigned long long U, const float2* xs, const int* es,
-                                            const float* Af, unsigned nzA, unsigned char out[4]) {
-    float xv[3];
-    int ev[3];
+// Cumulative thresholds (p0, p1) of states 0 and 1 for frame t when the next
+// frame holds state nx (3: no next frame): the filter's values weighted by the
+// transition into nx, as fractions of their total, in FP32; no weight at all
+// gives (1, 1), state 0, as a zero total does in the reference. Af: A as
+// floats; nzA: bit 3i + n set where A[i][n] != 0.
+__device__ __forceinline__ float2 frame_thresholds(int t, int nx, const float2* xs, const int* es, const float* Af,
+                                                   unsigned nzA) {
+    int Em = kZeroExp;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        xv[i] = xs[3 * t + i].x;
-        ev[i] = es[3 * t + i];
+        const bool use = (nx == 3 || ((nzA >> (3 * i + nx)) & 1u)) && es[3 * t + i] != kZeroExp;
+        Em = (use && es[3 * t + i] > Em) ? es[3 * t + i] : Em;
     }
+    float a[3], tot = 0.f;
 #pragma unroll
-    for (int nx = 0; nx < 4; ++nx) {
-        int Em = kZeroExp;
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            const bool use = (nx == 3 || ((nzA >> (3 * i + nx)) & 1u)) && ev[i] != kZeroExp;
-            Em = (use && ev[i] > Em) ? ev[i] : Em;
-        }
-        float a[3], tot = 0.f;
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            const bool use = (nx == 3 || ((nzA >> (3 * i + nx)) & 1u)) && ev[i] != kZeroExp;
-            const int dd = ev[i] - Em;
-            const float tr = nx == 3 ? 1.f : Af[3 * i + nx];
-            a[i] = (use && dd >= -126) ? xv[i] * pow2f(dd < -126 ? -126 : dd) * tr : 0.f;
-            tot += a[i];
-        }
-        unsigned long long T0 = 1ull << 53, T1 = 1ull << 53;
-        if (tot > 0.f) {
-            T0 = threshold53(a[0] / tot);
-            T1 = threshold53((a[0] + a[1]) / tot);
-        }
-        out[nx] = (unsigned char)(U <= T0 ? 0 : (U <= T1 ? 1 : 2));
+    for (int i = 0; i < 3; ++i) {
+        const bool use = (nx == 3 || ((nzA >> (3 * i + nx)) & 1u)) && es[3 * t + i] != kZeroExp;
+        const int dd = es[3 * t + i] - Em;
+        const float tr = nx == 3 ? 1.f : Af[3 * i + nx];
+        a[i] = (use && dd >= -126) ? xs[3 * t + i].x * pow2f(dd < -126 ? -126 : dd) * tr : 0.f;
+        tot += a[i];
     }
+    return tot > 0.f ? make_float2(a[0] / tot, (a[0] + a[1]) / tot) : make_float2(1.f, 1.f);
+}
+
+// The state drawn by a uniform U (53-bit integer) against thresholds (p0, p1).
+__device__ __forceinline__ int draw_state(unsigned long long U, float2 th) {
+    return U <= threshold53(th.x) ? 0 : (U <= threshold53(th.y) ? 1 : 2);
+}
+
+// The draws of frame t from its uniform U for each state the next frame may
+// hold (index 3: no next frame).
+__device__ __forceinline__ void frame_draws(int t, unsigned long long U, const float2* xs, const int* es,
+                                            const float* Af, unsigned nzA, unsigned char out[4]) {
+#pragma unroll
+    for (int nx = 0; nx < 4; ++nx) out[nx] = (unsigned char)draw_state(U, frame_thresholds(t, nx, xs, es, Af, nzA));
+}
+
+// A as floats and its non-zero pattern, for frame_thresholds.
+__device__ __forceinline__ void transition_floats(const double* A, float Af[9], unsigned* nzA) {
+    unsigned m = 0;
+#pragma unroll
+    for (int n = 0; n < 9; ++n) {
+        Af[n] = (float)A[n];
+        m |= A[n] != 0.0 ? 1u << n : 0u;
+    }
+    *nzA = m;
 }
 
 // 53-bit integer uniform of Philox outputs a, b (u53 = U 2^-53)

@@ -130,11 +130,8 @@ __global__ void __launch_bounds__(kGibbsThreads) gibbs_chain_kernel(const GibbsP
     const volatile unsigned char* vstate = g.state;
     EmFrame* em_all = reinterpret_cast<EmFrame*>(g.em);
     float Af[9];
-    unsigned nzA = 0;
-    for (int n = 0; n < 9; ++n) {
-        Af[n] = (float)g.A[n];
-        nzA |= g.A[n] != 0.0 ? 1u << n : 0u;
-    }
+    unsigned nzA;
+    ffbs::transition_floats(g.A, Af, &nzA);
 
     for (int d = 0; d < g.n_draws; ++d) {
         const double var = g.var_draw ? g.var_draw[d] : g.variance;

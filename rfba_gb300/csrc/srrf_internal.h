@@ -227,6 +227,23 @@ int gibbs_max_blocks(int F, int* out);
 int launch_gibbs(const GibbsParams& p, int grid, void* stream);
 int launch_spot_intensity(const int* pixels, int P, const double* spots, int K, double zf, double* out, void* stream);
 
+// 3B sampled-background spot Hessian (hessian.cu). Sizes: tab [P][21],
+// part [nc][S * F][22], gg [15], frame [S][F][20], out [S][20].
+struct HessParams {
+    const double* bg;      // [S][F][P] background samples (the spot taken off)
+    const double* pix;     // [F][P] data
+    const int* pixels;     // [P][3]
+    const double* phi;     // [5] spot, device
+    double zf, variance;
+    double A[9], pi[3];
+    int S, F, P, nc, bs;
+    unsigned long long seed;
+    double *tab, *part, *gg, *frame, *out;
+};
+int hessian_chunks(long long S, long long F, int P, int sm_count);
+size_t hessian_ffbs_smem(int F);
+int launch_spot_hessian(const HessParams& h, void* stream);
+
 // 3B spot gradient (threeb.cu): spot voxel table, emission sums per (sample,
 // frame), forward algorithm per sample; res[s] = (gradient[5], log probability).
 int launch_threeb(const double* bg, const double* pix, const int* pixels, int S, int F, int P, const double* phi_dev,

@@ -333,6 +333,580 @@ static double log_log_normal(double x, double mu, double sigma) {
     return -(a * a) / (2 * (sigma * sigma)) - ref_ln(x) - ref_ln(sigma * std::sqrt(2 * M_PI));
 }
 
+// ---- 3B main loop: passes, sampled-background Hessian, model modification ---
+
+// SplitMix64 (Steele, Lea, Flood, OOPSLA 2014) of a seed mixed with two
+// integers: the seeds of the sub-steps of a pass, a modification and a fit.
+static unsigned long long mix_seed(unsigned long long seed, long long a, long long b) {
+    unsigned long long z = seed ^ ((unsigned long long)a << 32) ^ (unsigned long long)(unsigned)b;
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// Seed of spot `s`'s draws in pass `pass` of rfba_3b_optimise_pass.
+static unsigned long long pass_seed(unsigned long long seed, int pass, int s) {
+    return mix_seed(seed, (unsigned)pass, s);
+}
+
+// Uniform doubles in [0, 1) from a SplitMix64 stream: the host's random
+// choices of a model modification (the reference's rng()).
+struct HostUniform {
+    unsigned long long state;
+    double next() {
+        unsigned long long z = (state += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+    }
+};
+
+typedef std::array<double, 5> Spot;
+
+// The allowed area of the position prior: the pixels dilated by
+// getBall(extra_radius) (dilate_mask, multispot5.cc:1280-1290); off when the
+// radius is negative.
+struct AllowedArea {
+    bool use = false;
+    std::set<long long> cells;
+    static long long key(int x, int y, int z) {
+        return ((long long)(x + (1 << 20)) << 42) | ((long long)(y + (1 << 20)) << 21) | (long long)(z + (1 << 20));
+    }
+    void build(const int* pixels, int P, double radius) {
+        use = radius >= 0;
+        cells.clear();
+        if (!use) return;
+        const std::vector<int> b = ball((float)radius);
+        for (int p = 0; p < P; ++p)
+            for (size_t j = 0; j < b.size(); j += 3)
+                cells.insert(key(pixels[3 * p] + b[j], pixels[3 * p + 1] + b[j + 1], pixels[3 * p + 2] + b[j + 2]));
+    }
+    // is_zero_prior at the spot's rounded position (ir_rounded3D, multispot5.cc:989-995)
+    bool outside(const Spot& s) const {
+        return use && !cells.count(key(round_away(s[2]), round_away(s[3]), round_away(s[4])));
+    }
+};
+
+// get_spot_pixels for one spot (host).
+static int spot_mask(const int* pixels, int P, const Spot& s, std::vector<int>* out) {
+    int off[2];
+    long long n = 0;
+    int e;
+    if ((e = rfba_3b_spot_masks(pixels, P, s.data(), 1, off, nullptr, 0, &n))) return e;
+    out->assign((size_t)n, 0);
+    if (n && (e = rfba_3b_spot_masks(pixels, P, s.data(), 1, off, out->data(), n, &n))) return e;
+    return RFBA_OK;
+}
+
+static void flatten_masks(const std::vector<std::vector<int> >& masks, size_t count, std::vector<int>* off,
+                          std::vector<int>* idx) {
+    off->assign(count + 1, 0);
+    idx->clear();
+    for (size_t k = 0; k < count; ++k) {
+        idx->insert(idx->end(), masks[k].begin(), masks[k].end());
+        (*off)[k + 1] = (int)idx->size();
+    }
+}
+
+static int upload_spots(rfba_ctx* ctx, const std::vector<Spot>& sp, cudaStream_t st) {
+    int s;
+    if ((s = ctx->gb_spots.ensure(sp.size() * 40 + 8, "3B spots"))) return s;
+    if (!sp.empty())
+        RFBA_CUDA(cudaMemcpyAsync(ctx->gb_spots.p, sp.data(), sp.size() * 40, cudaMemcpyHostToDevice, st), "spots copy");
+    return RFBA_OK;
+}
+
+// The block's data on the device (the context's Gibbs data buffers).
+static int stage_block(rfba_ctx* ctx, const double* pix, const int* pixels, int F, int P, cudaStream_t st) {
+    int s;
+    const size_t FP = (size_t)F * P;
+    if ((s = ctx->gb_pix.ensure(FP * 8, "3B data")) || (s = ctx->gb_pixels.ensure((size_t)P * 12, "3B pixels"))) return s;
+    RFBA_CUDA(cudaMemcpyAsync(ctx->gb_pix.p, pix, FP * 8, cudaMemcpyHostToDevice, st), "data copy");
+    RFBA_CUDA(cudaMemcpyAsync(ctx->gb_pixels.p, pixels, (size_t)P * 12, cudaMemcpyHostToDevice, st), "pixels copy");
+    return RFBA_OK;
+}
+
+// Gibbs draws of the staged block with the spots `sp` (uploaded here) and
+// flattened masks; the draws' intensities, spot `exclude` taken off, stay in
+// gb_oint.
+static int draws_without(rfba_ctx* ctx, const rfba_3b_model* m, int F, int P, const std::vector<Spot>& sp,
+                         const std::vector<int>& hoff, const std::vector<int>& hidx, int n_draws, int sweeps,
+                         int exclude, unsigned long long seed, cudaStream_t st) {
+    int s;
+    if ((s = upload_spots(ctx, sp, st))) return s;
+    GibbsCall c;
+    c.K = (int)sp.size();
+    c.F = F;
+    c.P = P;
+    c.sweeps = sweeps;
+    c.n_draws = n_draws;
+    c.seed = seed;
+    c.exclude = exclude;
+    c.want_int = true;
+    return gibbs_run(ctx, m, static_cast<const double*>(ctx->gb_pix.p), static_cast<const int*>(ctx->gb_pixels.p),
+                     static_cast<const double*>(ctx->gb_spots.p), hoff, hidx, c, RFBA_DEVICE_PTRS, st);
+}
+
+// The spot optimiser's gradient on staged samples (NaN outside brightness,
+// blur > 0, multispot5.cc:618-619).
+struct StagedGradient {
+    rfba_ctx* ctx;
+    const rfba_3b_model* m;
+    ThreeBData d;
+    cudaStream_t st;
+    int operator()(const double* x, double* g) {
+        if (x[0] <= 0 || x[1] <= 0) {
+            for (int n = 0; n < 5; ++n) g[n] = std::numeric_limits<double>::quiet_NaN();
+            return RFBA_OK;
+        }
+        return threeb_eval(ctx, m, d, x, g, nullptr, st);
+    }
+};
+
+// One pass of FitSpots::optimize_each_spot_in_turn_for_several_passes
+// (multispot5.cc:1511-1690) on the staged block: spots sorted by the sweep
+// order of `order_pass`, spot k's draws seeded pass_seed(seed, seed_pass, k).
+static int optimise_pass_core(rfba_ctx* ctx, const rfba_3b_model* m, const int* pixels, int F, int P,
+                              std::vector<Spot>* spots, int order_pass, int main_samples, int sweeps,
+                              int cg_max_iterations, const double* limit, const AllowedArea& area,
+                              unsigned long long seed, int seed_pass, int* evaluations, cudaStream_t st) {
+    int s;
+    std::vector<Spot>& sp = *spots;
+    int K = (int)sp.size();
+    // masks of every spot (multispot5.cc:1518-1521)
+    std::vector<std::vector<int> > masks((size_t)K);
+    for (int k = 0; k < K; ++k)
+        if ((s = spot_mask(pixels, P, sp[k], &masks[k]))) return s;
+    // the sweep order (multispot5.cc:1541-1560): by x or y position, ascending
+    // or descending; the reference's third branch repeats `% 4 == 1` and is never
+    // taken, so passes 2 and 3 both sort by descending y
+    std::vector<int> order((size_t)K);
+    for (int k = 0; k < K; ++k) order[k] = k;
+    const int mode = order_pass % 4 == 0 ? 0 : order_pass % 4 == 1 ? 1 : 2;
+    const int first = mode == 2 ? 3 : 2, second = first == 2 ? 3 : 2;
+    std::sort(order.begin(), order.end(), [&](int a, int b) {
+        const double fa = sp[a][first], fb = sp[b][first];
+        const bool desc = mode != 0;
+        if (desc ? fa > fb : fa < fb) return true;
+        if (fa == fb) return desc ? sp[a][second] > sp[b][second] : sp[a][second] < sp[b][second];
+        return false;
+    });
+    {
+        std::vector<Spot> t((size_t)K);
+        for (int k = 0; k < K; ++k) t[k] = sp[order[k]];
+        sp.swap(t);
+        // masks stay where they were: the reference swaps tmp_spot_pixels[i]
+        // with spot_pixels[i], not spot_pixels[index[i]] (multispot5.cc:1570), so
+        // a spot's mask is the one at its new position until it is optimised
+    }
+    int evals = 0;
+    for (int k = 0; k < K; ++k) {
+        // a fresh sampler for this spot: main_samples draws, the spot taken off
+        // them (multispot5.cc:1591-1608)
+        std::vector<int> hoff, hidx;
+        flatten_masks(masks, (size_t)K, &hoff, &hidx);
+        if ((s = draws_without(ctx, m, F, P, sp, hoff, hidx, main_samples, sweeps, k, pass_seed(seed, seed_pass, k),
+                               st)))
+            return s;
+        // optimise the spot on those samples (multispot5.cc:1611-1636)
+        StagedGradient grad{ctx, m, ThreeBData(), st};
+        if ((s = threeb_stage(ctx, static_cast<const double*>(ctx->gb_oint.p), static_cast<const double*>(ctx->gb_pix.p),
+                              static_cast<const int*>(ctx->gb_pixels.p), main_samples, F, P, RFBA_DEVICE_PTRS, st,
+                              &grad.d)))
+            return s;
+        CgOnly5 cg;
+        if ((s = cg.start(sp[k].data(), limit, grad))) return s;
+        cg.max_iterations = cg_max_iterations;
+        if ((s = cg.run(grad))) return s;
+        evals += cg.evaluations;
+        for (int n = 0; n < 5; ++n) sp[k][n] = cg.x[n];
+        // new mask; eject the spot if it has no pixels or left the allowed area
+        // (multispot5.cc:1651-1674)
+        if ((s = spot_mask(pixels, P, sp[k], &masks[k]))) return s;
+        if (masks[k].empty() || area.outside(sp[k])) {
+            sp.erase(sp.begin() + k);
+            masks.erase(masks.begin() + k);
+            --K;
+            --k;
+        }
+    }
+    if (evaluations) *evaluations += evals;
+    return RFBA_OK;
+}
+
+// The draws' residual sums into NegativeFreeEnergy::compute_with_mask's value
+// (multispot5.cc:354-405), host arithmetic in the reference's order; err
+// [samples][F]. residuals [samples] may be null.
+static double free_energy_value(const rfba_3b_model* m, const std::vector<double>& err, int samples, int F, int P,
+                                const double* spots, int K, double* residuals) {
+    const double base_sigma = std::sqrt(m->variance);
+    const double scale_pow = 100.0;
+    const unsigned int npixels = (unsigned int)P, nframes = (unsigned int)F;
+    double sum = 0;
+    for (int sample = 0; sample < samples; sample++) {
+        const double var1 = variance_from_sample(sample - 2, samples, base_sigma, scale_pow);
+        const double var2 = variance_from_sample(sample - 1, samples, base_sigma, scale_pow);
+        const double var3 = variance_from_sample(sample + 1, samples, base_sigma, scale_pow);
+        const double var4 = variance_from_sample(sample + 2, samples, base_sigma, scale_pow);
+        double err_sum = 0;
+        for (int f = 0; f < F; ++f) err_sum -= err[(size_t)sample * F + f];
+        if (residuals) residuals[sample] = -err_sum;
+        const double e1 = err_sum / (2 * var1) - npixels * nframes * ::log(2 * M_PI * var1) / 2;
+        const double e2 = err_sum / (2 * var2) - npixels * nframes * ::log(2 * M_PI * var2) / 2;
+        const double e3 = err_sum / (2 * var3) - npixels * nframes * ::log(2 * M_PI * var3) / 2;
+        const double e4 = err_sum / (2 * var4) - npixels * nframes * ::log(2 * M_PI * var4) / 2;
+        sum += (-e1 + 8 * e2 - 8 * e3 + e4) / 12;
+    }
+    const double log_final =
+        (::log(variance_from_sample(samples, samples, base_sigma, scale_pow) * 2 * M_PI) / 2) * npixels * nframes;
+    double priors = 0;
+    for (int i = 0; i < K; i++) {
+        priors += log_log_normal(spots[i * 5 + 0], m->mu_brightness, m->sigma_brightness);
+        priors += log_log_normal(spots[i * 5 + 1], m->mu_blur, m->sigma_blur);
+    }
+    return -(sum + priors - log_final);
+}
+
+// The free-energy draws: `samples` Gibbs draws from all spots off, draw i at
+// the variance of thermodynamic step i - 1; their residual sums per frame.
+static int free_energy_draws(rfba_ctx* ctx, const rfba_3b_model* m, const double* pix, const int* pixels,
+                             const double* spots, const std::vector<int>& hoff, const std::vector<int>& hidx, int K,
+                             int F, int P, int samples, int sweeps, unsigned long long seed, int ptr_flags,
+                             cudaStream_t st, std::vector<double>* err) {
+    const double base_sigma = std::sqrt(m->variance);
+    std::vector<double> var2((size_t)samples);
+    for (int i = 0; i < samples; ++i) var2[i] = variance_from_sample(i - 1, samples, base_sigma, 100.0);
+    GibbsCall c;
+    c.K = K;
+    c.F = F;
+    c.P = P;
+    c.sweeps = sweeps;
+    c.n_draws = samples;
+    c.seed = seed;
+    c.var_draw = var2.data();
+    c.want_err = true;
+    int s;
+    if ((s = gibbs_run(ctx, m, pix, pixels, spots, hoff, hidx, c, ptr_flags, st))) return s;
+    err->assign((size_t)samples * F, 0.0);
+    RFBA_CUDA(cudaMemcpyAsync(err->data(), ctx->gb_oerr.p, err->size() * 8, cudaMemcpyDeviceToHost, st),
+              "residual read-back");
+    RFBA_CUDA(cudaStreamSynchronize(st), "synchronize");
+    return RFBA_OK;
+}
+
+// -compute_with_mask of the staged block with spots `sp` and masks (the first
+// sp.size() of `masks`).
+static int model_energy(rfba_ctx* ctx, const rfba_3b_model* m, int F, int P, const std::vector<Spot>& sp,
+                        const std::vector<std::vector<int> >& masks, int samples, int sweeps, unsigned long long seed,
+                        cudaStream_t st, double* energy) {
+    int s;
+    std::vector<int> hoff, hidx;
+    flatten_masks(masks, sp.size(), &hoff, &hidx);
+    if ((s = upload_spots(ctx, sp, st))) return s;
+    std::vector<double> err;
+    if ((s = free_energy_draws(ctx, m, static_cast<const double*>(ctx->gb_pix.p), static_cast<const int*>(ctx->gb_pixels.p),
+                               static_cast<const double*>(ctx->gb_spots.p), hoff, hidx, (int)sp.size(), F, P, samples,
+                               sweeps, seed, RFBA_DEVICE_PTRS, st, &err)))
+        return s;
+    *energy = -free_energy_value(m, err, samples, F, P, sp.empty() ? nullptr : sp[0].data(), (int)sp.size(), nullptr);
+    return RFBA_OK;
+}
+
+// hess_log_log_normal (storm.h:446-449)
+static double hess_log_log_normal(double x, double mu, double sigma) {
+    return (1 + (ref_ln(x) - mu - 1) / (sigma * sigma)) / (x * x);
+}
+
+// The device part of sampled_background_spot_hessian_ffbs on device data and
+// the reference's normalisation on the host (multispot5.cc:902-985).
+static int spot_hessian_dev(rfba_ctx* ctx, const rfba_3b_model* m, const double* bg, const double* pix,
+                            const int* pixels, int S, int F, int P, const double spot[5], int bs,
+                            unsigned long long seed, double hess[25], cudaStream_t st) {
+    int s;
+    const int nc = hessian_chunks(S, F, P, ctx->sm_count);
+    const size_t nq = (size_t)S * F;
+    if ((s = ctx->hs_tab.ensure((size_t)P * 21 * 8, "3B Hessian table")) ||
+        (s = ctx->hs_part.ensure((size_t)nc * nq * 22 * 8, "3B Hessian parts")) ||
+        (s = ctx->hs_gg.ensure(15 * 8, "3B Hessian outer products")) ||
+        (s = ctx->hs_phi.ensure(5 * 8, "3B Hessian spot")) ||
+        (s = ctx->hs_frame.ensure(nq * 20 * 8, "3B Hessian frame parts")) ||
+        (s = ctx->hs_out.ensure((size_t)S * 20 * 8, "3B Hessian sums")))
+        return s;
+    RFBA_CUDA(cudaMemcpyAsync(ctx->hs_phi.p, spot, 40, cudaMemcpyHostToDevice, st), "spot upload");
+    HessParams h;
+    h.bg = bg;
+    h.pix = pix;
+    h.pixels = pixels;
+    h.phi = static_cast<const double*>(ctx->hs_phi.p);
+    h.zf = m->z_factor;
+    h.variance = m->variance;
+    for (int n = 0; n < 9; ++n) h.A[n] = m->A[n];
+    for (int n = 0; n < 3; ++n) h.pi[n] = m->pi[n];
+    h.S = S;
+    h.F = F;
+    h.P = P;
+    h.nc = nc;
+    h.bs = bs;
+    h.seed = seed;
+    h.tab = static_cast<double*>(ctx->hs_tab.p);
+    h.part = static_cast<double*>(ctx->hs_part.p);
+    h.gg = static_cast<double*>(ctx->hs_gg.p);
+    h.frame = static_cast<double*>(ctx->hs_frame.p);
+    h.out = static_cast<double*>(ctx->hs_out.p);
+    const int e = launch_spot_hessian(h, st);
+    if (e) return cuda_fail((cudaError_t)e, "3B Hessian launch");
+    ctx->launches += 4;
+    std::vector<double> out((size_t)S * 20);
+    RFBA_CUDA(cudaMemcpyAsync(out.data(), ctx->hs_out.p, out.size() * 8, cudaMemcpyDeviceToHost, st),
+              "Hessian read-back");
+    RFBA_CUDA(cudaStreamSynchronize(st), "synchronize");
+    double sh[15] = {0}, sd[5] = {0};
+    for (int i = 0; i < S; ++i) {
+        for (int n = 0; n < 15; ++n) sh[n] += out[(size_t)i * 20 + n];
+        for (int r = 0; r < 5; ++r) sd[r] += out[(size_t)i * 20 + 15 + r];
+    }
+    const double norm = (double)((size_t)bs * (size_t)S) * m->variance;
+    for (int r = 0, n = 0; r < 5; ++r)
+        for (int c = r; c < 5; ++c, ++n) hess[r * 5 + c] = hess[c * 5 + r] = sh[n] / norm;
+    for (int r = 0; r < 5; ++r) sd[r] /= norm;
+    for (int r = 0; r < 5; ++r)
+        for (int c = 0; c < 5; ++c) hess[r * 5 + c] -= sd[r] * sd[c];
+    hess[0] += hess_log_log_normal(spot[0], m->mu_brightness, m->sigma_brightness);
+    hess[6] += hess_log_log_normal(spot[1], m->mu_blur, m->sigma_blur);
+    return RFBA_OK;
+}
+
+// Eigen-decomposition of a symmetric 5x5 matrix by cyclic Jacobi rotations
+// (Jacobi 1846; Golub and Van Loan, Matrix Computations, sec. 8.5): eigenvalues
+// ascending, eigenvectors as rows, each with its largest-magnitude component
+// positive.
+static void sym_eigen5(const double a_in[25], double evals[5], double evecs[25]) {
+    double a[5][5], v[5][5];
+    for (int r = 0; r < 5; ++r)
+        for (int c = 0; c < 5; ++c) {
+            a[r][c] = 0.5 * (a_in[r * 5 + c] + a_in[c * 5 + r]);
+            v[r][c] = r == c ? 1.0 : 0.0;
+        }
+    for (int sweep = 0; sweep < 64; ++sweep) {
+        double off = 0, diag = 0;
+        for (int r = 0; r < 5; ++r) {
+            diag += a[r][r] * a[r][r];
+            for (int c = r + 1; c < 5; ++c) off += a[r][c] * a[r][c];
+        }
+        if (off <= 1e-30 * diag || off == 0) break;
+        for (int p = 0; p < 4; ++p)
+            for (int q = p + 1; q < 5; ++q) {
+                if (a[p][q] == 0) continue;
+                const double theta = (a[q][q] - a[p][p]) / (2 * a[p][q]);
+                const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1));
+                const double c = 1 / std::sqrt(t * t + 1), s = t * c;
+                for (int k = 0; k < 5; ++k) {
+                    if (k == p || k == q) continue;
+                    const double akp = a[k][p], akq = a[k][q];
+                    a[k][p] = a[p][k] = c * akp - s * akq;
+                    a[k][q] = a[q][k] = s * akp + c * akq;
+                }
+                const double apq = a[p][q];
+                a[p][p] -= t * apq;
+                a[q][q] += t * apq;
+                a[p][q] = a[q][p] = 0;
+                for (int k = 0; k < 5; ++k) {
+                    const double vkp = v[k][p], vkq = v[k][q];
+                    v[k][p] = c * vkp - s * vkq;
+                    v[k][q] = s * vkp + c * vkq;
+                }
+            }
+    }
+    int idx[5] = {0, 1, 2, 3, 4};
+    std::sort(idx, idx + 5, [&](int x, int y) { return a[x][x] < a[y][y]; });
+    for (int n = 0; n < 5; ++n) {
+        const int j = idx[n];
+        evals[n] = a[j][j];
+        int big = 0;
+        for (int k = 1; k < 5; ++k)
+            if (std::fabs(v[k][j]) > std::fabs(v[big][j])) big = k;
+        const double sg = v[big][j] < 0 ? -1.0 : 1.0;
+        for (int k = 0; k < 5; ++k) evecs[n * 5 + k] = sg * v[k][j];
+    }
+}
+
+// Determinant of a 5x5 matrix by Gaussian elimination with partial pivoting.
+static double det5(const double a_in[25]) {
+    double a[5][5];
+    for (int r = 0; r < 5; ++r)
+        for (int c = 0; c < 5; ++c) a[r][c] = a_in[r * 5 + c];
+    double det = 1;
+    for (int c = 0; c < 5; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < 5; ++r)
+            if (std::fabs(a[r][c]) > std::fabs(a[piv][c])) piv = r;
+        if (a[piv][c] == 0) return 0;
+        if (piv != c) {
+            for (int k = 0; k < 5; ++k) std::swap(a[c][k], a[piv][k]);
+            det = -det;
+        }
+        det *= a[c][c];
+        for (int r = c + 1; r < 5; ++r) {
+            const double f = a[r][c] / a[c][c];
+            for (int k = c; k < 5; ++k) a[r][k] -= f * a[c][k];
+        }
+    }
+    return det;
+}
+
+// log_normal_mode (storm.h:402-405)
+static double log_normal_mode(double mu, double sigma) { return std::exp(mu - sigma * sigma); }
+
+// One try of FitSpots::try_modifying_model (multispot5.cc:1840-2160) on the
+// staged block.
+static int modify_core(rfba_ctx* ctx, const rfba_3b_model* m, const int* pixels, int F, int P,
+                       std::vector<Spot>* spots, const rfba_3b_fit_params& prm, const AllowedArea& area,
+                       unsigned long long seed, rfba_3b_modify_record* rec, cudaStream_t st) {
+    int s;
+    HostUniform rng{seed};
+    std::vector<Spot>& sp = *spots;
+    const int K = (int)sp.size();
+    std::memset(rec, 0, sizeof *rec);
+    // add with probability 1/2, always with one spot (multispot5.cc:1851) and,
+    // here, with none (the reference would index an empty list)
+    const bool add = rng.next() > 0.5 || K <= 1;
+    std::vector<Spot> model1, model2;
+    int original;
+    if (add) {
+        model1 = sp;
+        model2 = sp;
+        const int r = std::min(P - 1, (int)(rng.next() * P));
+        Spot n;
+        n[0] = log_normal_mode(m->mu_brightness, m->sigma_brightness);
+        n[1] = log_normal_mode(m->mu_blur, m->sigma_blur);
+        for (int a = 0; a < 3; ++a) n[2 + a] = pixels[3 * r + a] + rng.next() - .5;
+        model2.push_back(n);
+        original = 1;
+    } else {
+        const int a = std::min(K - 1, (int)(rng.next() * K));
+        model1 = sp;
+        std::swap(model1[K - 1], model1[a]);
+        model2 = model1;
+        model1.pop_back();
+        original = 2;
+    }
+    rec->added = add ? 1 : 0;
+    const int spot = (int)model2.size() - 1;
+    std::vector<std::vector<int> > masks2(model2.size());
+    for (size_t k = 0; k < model2.size(); ++k)
+        if ((s = spot_mask(pixels, P, model2[k], &masks2[k]))) return s;
+    // optimise the mobile spot on GibbsSampler2 draws (multispot5.cc:1935-2010)
+    {
+        std::vector<int> hoff, hidx;
+        flatten_masks(masks2, model2.size(), &hoff, &hidx);
+        const int S = prm.opt_samples;
+        if ((s = draws_without(ctx, m, F, P, model2, hoff, hidx, S, prm.sweeps, spot, mix_seed(seed, 1, 0), st)))
+            return s;
+        StagedGradient grad{ctx, m, ThreeBData(), st};
+        if ((s = threeb_stage(ctx, static_cast<const double*>(ctx->gb_oint.p), static_cast<const double*>(ctx->gb_pix.p),
+                              static_cast<const int*>(ctx->gb_pixels.p), S, F, P, RFBA_DEVICE_PTRS, st, &grad.d)))
+            return s;
+        CgOnly5 cg;
+        if ((s = cg.start(model2[spot].data(), prm.limit, grad))) return s;
+        for (int attempt = 0; attempt < prm.opt_attempts; attempt++) {
+            if ((s = cg.run(grad))) return s;
+            if (attempt < prm.opt_attempts - 1) {
+                double H[25], ev[5], V[25];
+                if ((s = spot_hessian_dev(ctx, m, static_cast<const double*>(ctx->gb_oint.p),
+                                          static_cast<const double*>(ctx->gb_pix.p),
+                                          static_cast<const int*>(ctx->gb_pixels.p), S, F, P, cg.x,
+                                          prm.opt_hess_inner_samples, mix_seed(seed, 2, attempt), H, st)))
+                    return s;
+                sym_eigen5(H, ev, V);
+                if (ev[4] < 0) break;  // negative definite
+                // restart along the fourth eigenvector (ascending order)
+                double x0[5];
+                for (int n = 0; n < 5; ++n) x0[n] = cg.x[n] + 0.1 * V[15 + n];
+                cg.restart(x0, V + 15);
+            }
+        }
+        for (int n = 0; n < 5; ++n) model2[spot][n] = cg.x[n];
+        rec->evaluations = cg.evaluations;
+        if ((s = spot_mask(pixels, P, model2[spot], &masks2[spot]))) return s;
+    }
+    for (int n = 0; n < 5; ++n) rec->spot[n] = model2[spot][n];
+    int keep = original;
+    if (area.outside(model2[spot])) {
+        keep = 1;  // model 2's spot has zero prior probability
+        rec->zero_prior = 1;
+    } else {
+        const double pos_lp =
+            area.use ? (double)(model2.size() - model1.size()) * ref_ln(1.0 / (double)area.cells.size()) : 0.0;
+        rec->position_log_prior = pos_lp;
+        // the Hessian at model 2's spot on GibbsSampler draws over all pixels
+        // (multispot5.cc:2050-2075)
+        std::vector<int> hoff((size_t)model2.size() + 1), hidx((size_t)model2.size() * P);
+        for (size_t k = 0; k < model2.size(); ++k) {
+            hoff[k] = (int)(k * P);
+            for (int p = 0; p < P; ++p) hidx[k * P + p] = p;
+        }
+        hoff[model2.size()] = (int)(model2.size() * P);
+        const int S = prm.h_outer_samples;
+        if ((s = draws_without(ctx, m, F, P, model2, hoff, hidx, S, prm.sweeps, spot, mix_seed(seed, 3, 0), st)))
+            return s;
+        double H[25], negH[25], ev[5], V[25];
+        if ((s = spot_hessian_dev(ctx, m, static_cast<const double*>(ctx->gb_oint.p),
+                                  static_cast<const double*>(ctx->gb_pix.p), static_cast<const int*>(ctx->gb_pixels.p), S,
+                                  F, P, model2[spot].data(), prm.h_inner_samples, mix_seed(seed, 4, 0), H, st)))
+            return s;
+        double scaled[25];
+        for (int n = 0; n < 25; ++n) {
+            negH[n] = -H[n];
+            scaled[n] = -H[n] / (M_PI * 2);
+        }
+        const double det = det5(scaled);
+        sym_eigen5(negH, ev, V);
+        if (ev[0] > 1e-6) {
+            double e2 = 0, e1 = 0;
+            if ((s = model_energy(ctx, m, F, P, model2, masks2, prm.thermo_samples, prm.sweeps, mix_seed(seed, 5, 0), st,
+                                  &e2)) ||
+                (s = model_energy(ctx, m, F, P, model1, masks2, prm.thermo_samples, prm.sweeps, mix_seed(seed, 6, 0), st,
+                                  &e1)))
+                return s;
+            const double occam = -0.5 * std::log(det);
+            const double p2 = e2 + occam + pos_lp;
+            rec->model1_energy = e1;
+            rec->model2_energy = e2;
+            rec->occam = occam;
+            keep = p2 > e1 ? 2 : 1;
+        } else {
+            rec->bad_hessian = 1;  // a saddle point: keep the original model
+        }
+    }
+    rec->kept = keep;
+    sp = keep == 2 ? model2 : model1;
+    return RFBA_OK;
+}
+
+static int fit_check(rfba_ctx* ctx, const rfba_3b_model* m, const double* pix, const int* pixels, int F, int P,
+                     const double* spots, const int* nspots, int capacity, const rfba_3b_fit_params* prm) {
+    int s;
+    if (!pix || !pixels || !spots || !nspots || !prm) {
+        set_error("null argument");
+        return RFBA_ERR_INVALID;
+    }
+    if ((s = gibbs_check(ctx, m, *nspots, F, P, RFBA_HOST_PTRS))) return s;
+    if (capacity < *nspots + 1) {
+        set_error("spots capacity must hold one spot more than *nspots");
+        return RFBA_ERR_INVALID;
+    }
+    if (prm->main_samples < 1 || prm->sweeps < 1 || prm->main_cg_max_iterations < 0 || prm->main_passes < 0 ||
+        prm->add_remove_tries < 0 || prm->opt_samples < 1 || prm->opt_attempts < 1 ||
+        prm->opt_hess_inner_samples < 1 || prm->h_outer_samples < 1 || prm->h_inner_samples < 1 ||
+        prm->thermo_samples < 1) {
+        set_error("fit settings: sample counts and attempts must be >= 1, passes / tries / iterations >= 0");
+        return RFBA_ERR_INVALID;
+    }
+    return RFBA_OK;
+}
+
 }  // namespace rfba
 
 using namespace rfba;
@@ -424,16 +998,6 @@ int rfba_3b_gibbs_sample(rfba_ctx* ctx, const rfba_3b_model* m, const double* pi
     return RFBA_OK;
 }
 
-// Seed of spot `s`'s draws in pass `pass` of rfba_3b_optimise_pass: SplitMix64
-// (Steele, Lea, Flood, OOPSLA 2014) of the caller's seed mixed with both.
-static unsigned long long pass_seed(unsigned long long seed, int pass, int s) {
-    unsigned long long z = seed ^ ((unsigned long long)(unsigned)pass << 32) ^ (unsigned long long)(unsigned)s;
-    z += 0x9E3779B97F4A7C15ull;
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-    return z ^ (z >> 31);
-}
-
 unsigned long long rfba_3b_pass_seed(unsigned long long seed, int pass, int s) { return pass_seed(seed, pass, s); }
 
 // One pass of FitSpots::optimize_each_spot_in_turn_for_several_passes
@@ -447,7 +1011,7 @@ int rfba_3b_optimise_pass(rfba_ctx* ctx, const rfba_3b_model* m, const double* p
         set_error("null argument");
         return RFBA_ERR_INVALID;
     }
-    int K = *nspots;
+    const int K = *nspots;
     if ((s = gibbs_check(ctx, m, K, F, P, RFBA_HOST_PTRS))) return s;
     if (main_samples < 1 || sweeps < 1 || cg_max_iterations < 0) {
         set_error("main_samples and sweeps must be >= 1, cg_max_iterations >= 0");
@@ -457,121 +1021,19 @@ int rfba_3b_optimise_pass(rfba_ctx* ctx, const rfba_3b_model* m, const double* p
     RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
     cudaStream_t st = ctx->stream;
     if ((s = order_streams(ctx, st))) return s;
-    // masks of every spot (multispot5.cc:1518-1521)
-    std::vector<int> off((size_t)K + 1);
-    long long nnz = 0;
-    if ((s = rfba_3b_spot_masks(pixels, P, spots, K, off.data(), nullptr, 0, &nnz))) return s;
-    std::vector<int> idx((size_t)nnz);
-    if ((s = rfba_3b_spot_masks(pixels, P, spots, K, off.data(), idx.data(), nnz, &nnz))) return s;
-    std::vector<std::vector<int> > masks((size_t)K);
-    for (int k = 0; k < K; ++k) masks[k].assign(idx.begin() + off[k], idx.begin() + off[k + 1]);
-    // allowed area: the pixels dilated by getBall(extra_radius) (multispot5.cc:1280-1290)
-    std::set<long long> allowed;
-    auto key = [](int x, int y, int z) {
-        return ((long long)(x + (1 << 20)) << 42) | ((long long)(y + (1 << 20)) << 21) | (long long)(z + (1 << 20));
-    };
-    const bool use_prior = position_extra_radius >= 0;
-    if (use_prior) {
-        const std::vector<int> b = ball((float)position_extra_radius);
-        for (int p = 0; p < P; ++p)
-            for (size_t j = 0; j < b.size(); j += 3)
-                allowed.insert(key(pixels[3 * p] + b[j], pixels[3 * p + 1] + b[j + 1], pixels[3 * p + 2] + b[j + 2]));
-    }
-    // the sweep order (multispot5.cc:1541-1560): by x or y position, ascending
-    // or descending; the reference's third branch repeats `% 4 == 1` and is never
-    // taken, so passes 2 and 3 both sort by descending y
-    std::vector<int> order((size_t)K);
-    for (int k = 0; k < K; ++k) order[k] = k;
-    std::vector<std::array<double, 5> > sp((size_t)K);
+    AllowedArea area;
+    area.build(pixels, P, position_extra_radius);
+    std::vector<Spot> sp((size_t)K);
     for (int k = 0; k < K; ++k)
         for (int n = 0; n < 5; ++n) sp[k][n] = spots[5 * k + n];
-    const int mode = pass % 4 == 0 ? 0 : pass % 4 == 1 ? 1 : 2;
-    const int first = mode == 2 ? 3 : 2, second = first == 2 ? 3 : 2;
-    std::sort(order.begin(), order.end(), [&](int a, int b) {
-        const double fa = sp[a][first], fb = sp[b][first];
-        const bool desc = mode != 0;
-        if (desc ? fa > fb : fa < fb) return true;
-        if (fa == fb) return desc ? sp[a][second] > sp[b][second] : sp[a][second] < sp[b][second];
-        return false;
-    });
-    {
-        std::vector<std::array<double, 5> > t((size_t)K);
-        for (int k = 0; k < K; ++k) t[k] = sp[order[k]];
-        sp.swap(t);
-        // masks stay where they were: the reference swaps tmp_spot_pixels[i]
-        // with spot_pixels[i], not spot_pixels[index[i]] (multispot5.cc:1570), so
-        // a spot's mask is the one at its new position until it is optimised
-    }
-    // data on the device once
-    const size_t FP = (size_t)F * P;
-    if ((s = ctx->gb_pix.ensure(FP * 8, "3B data")) || (s = ctx->gb_pixels.ensure((size_t)P * 12, "3B pixels")) ||
-        (s = ctx->gb_spots.ensure((size_t)K * 40 + 8, "3B spots")))
-        return s;
-    RFBA_CUDA(cudaMemcpyAsync(ctx->gb_pix.p, pixel_intensities, FP * 8, cudaMemcpyHostToDevice, st), "data copy");
-    RFBA_CUDA(cudaMemcpyAsync(ctx->gb_pixels.p, pixels, (size_t)P * 12, cudaMemcpyHostToDevice, st), "pixels copy");
+    if ((s = stage_block(ctx, pixel_intensities, pixels, F, P, st))) return s;
     int evals = 0;
-    for (int k = 0; k < K; ++k) {
-        // a fresh sampler for this spot: main_samples draws, the spot taken off
-        // them (multispot5.cc:1591-1608)
-        std::vector<int> hoff((size_t)K + 1, 0), hidx;
-        for (int j = 0; j < K; ++j) {
-            hidx.insert(hidx.end(), masks[j].begin(), masks[j].end());
-            hoff[j + 1] = (int)hidx.size();
-        }
-        std::vector<double> flat((size_t)K * 5);
-        for (int j = 0; j < K; ++j)
-            for (int n = 0; n < 5; ++n) flat[5 * j + n] = sp[j][n];
-        RFBA_CUDA(cudaMemcpyAsync(ctx->gb_spots.p, flat.data(), flat.size() * 8, cudaMemcpyHostToDevice, st),
-                  "spots copy");
-        GibbsCall c;
-        c.K = K;
-        c.F = F;
-        c.P = P;
-        c.sweeps = sweeps;
-        c.n_draws = main_samples;
-        c.seed = pass_seed(seed, pass, k);
-        c.exclude = k;
-        c.want_int = true;
-        if ((s = gibbs_run(ctx, m, static_cast<const double*>(ctx->gb_pix.p), static_cast<const int*>(ctx->gb_pixels.p),
-                           static_cast<const double*>(ctx->gb_spots.p), hoff, hidx, c, RFBA_DEVICE_PTRS, st)))
-            return s;
-        // optimise the spot on those samples (multispot5.cc:1611-1636)
-        ThreeBData d;
-        if ((s = threeb_stage(ctx, static_cast<const double*>(ctx->gb_oint.p), static_cast<const double*>(ctx->gb_pix.p),
-                              static_cast<const int*>(ctx->gb_pixels.p), main_samples, F, P, RFBA_DEVICE_PTRS, st, &d)))
-            return s;
-        auto grad = [&](const double* x, double* g) -> int {
-            if (x[0] <= 0 || x[1] <= 0) {
-                for (int n = 0; n < 5; ++n) g[n] = std::numeric_limits<double>::quiet_NaN();
-                return RFBA_OK;
-            }
-            return threeb_eval(ctx, m, d, x, g, nullptr, st);
-        };
-        CgOnly5 cg;
-        if ((s = cg.start(sp[k].data(), limit, grad))) return s;
-        cg.max_iterations = cg_max_iterations;
-        if ((s = cg.run(grad))) return s;
-        evals += cg.evaluations;
-        for (int n = 0; n < 5; ++n) sp[k][n] = cg.x[n];
-        // new mask; eject the spot if it has no pixels or left the allowed area
-        // (multispot5.cc:1651-1674)
-        int o2[2];
-        long long n2 = 0;
-        if ((s = rfba_3b_spot_masks(pixels, P, sp[k].data(), 1, o2, nullptr, 0, &n2))) return s;
-        masks[k].assign((size_t)n2, 0);
-        if (n2 && (s = rfba_3b_spot_masks(pixels, P, sp[k].data(), 1, o2, masks[k].data(), n2, &n2))) return s;
-        const bool zero_prior =
-            use_prior && !allowed.count(key(round_away(sp[k][2]), round_away(sp[k][3]), round_away(sp[k][4])));
-        if (masks[k].empty() || zero_prior) {
-            sp.erase(sp.begin() + k);
-            masks.erase(masks.begin() + k);
-            --K;
-            --k;
-        }
-    }
-    for (int k = 0; k < K; ++k)
+    if ((s = optimise_pass_core(ctx, m, pixels, F, P, &sp, pass, main_samples, sweeps, cg_max_iterations, limit, area,
+                                seed, pass, &evals, st)))
+        return s;
+    for (size_t k = 0; k < sp.size(); ++k)
         for (int n = 0; n < 5; ++n) spots[5 * k + n] = sp[k][n];
-    *nspots = K;
+    *nspots = (int)sp.size();
     if (evaluations) *evaluations = evals;
     return RFBA_OK;
 }
@@ -638,50 +1100,126 @@ int rfba_3b_free_energy(rfba_ctx* ctx, const rfba_3b_model* m, const double* pix
     // NegativeFreeEnergy::compute_with_mask (multispot5.cc:335-405): slow-growth
     // thermodynamic integration over `samples` draws, draw i taken at the
     // variance of step i - 1 and differentiated by a five-point stencil
-    const double base_sigma = std::sqrt(m->variance);
-    const double scale_pow = 100.0;
-    std::vector<double> var2((size_t)samples);
-    for (int i = 0; i < samples; ++i) var2[i] = variance_from_sample(i - 1, samples, base_sigma, scale_pow);
-    GibbsCall c;
-    c.K = K;
-    c.F = F;
-    c.P = P;
-    c.sweeps = sweeps;
-    c.n_draws = samples;
-    c.seed = seed;
-    c.var_draw = var2.data();
-    c.want_err = true;
-    if ((s = gibbs_run(ctx, m, pixel_intensities, pixels, spots, hoff, hidx, c, ptr_flags, st))) return s;
-    std::vector<double> err((size_t)samples * F);
-    RFBA_CUDA(cudaMemcpyAsync(err.data(), ctx->gb_oerr.p, err.size() * 8, cudaMemcpyDeviceToHost, st),
-              "residual read-back");
-    RFBA_CUDA(cudaStreamSynchronize(st), "synchronize");
-    const unsigned int npixels = (unsigned int)P, nframes = (unsigned int)F;
-    double sum = 0;
-    for (int sample = 0; sample < samples; sample++) {
-        const double var1 = variance_from_sample(sample - 2, samples, base_sigma, scale_pow);
-        const double var2s = variance_from_sample(sample - 1, samples, base_sigma, scale_pow);
-        const double var3 = variance_from_sample(sample + 1, samples, base_sigma, scale_pow);
-        const double var4 = variance_from_sample(sample + 2, samples, base_sigma, scale_pow);
-        double err_sum = 0;
-        for (int f = 0; f < F; ++f) err_sum -= err[(size_t)sample * F + f];
-        if (residuals) residuals[sample] = -err_sum;
-        const double e1 = err_sum / (2 * var1) - npixels * nframes * ::log(2 * M_PI * var1) / 2;
-        const double e2 = err_sum / (2 * var2s) - npixels * nframes * ::log(2 * M_PI * var2s) / 2;
-        const double e3 = err_sum / (2 * var3) - npixels * nframes * ::log(2 * M_PI * var3) / 2;
-        const double e4 = err_sum / (2 * var4) - npixels * nframes * ::log(2 * M_PI * var4) / 2;
-        sum += (-e1 + 8 * e2 - 8 * e3 + e4) / 12;
-    }
-    const double log_final =
-        (::log(variance_from_sample(samples, samples, base_sigma, scale_pow) * 2 * M_PI) / 2) * npixels * nframes;
-    double priors = 0;
-    for (int i = 0; i < K; i++) {
-        priors += log_log_normal(hsp[i * 5 + 0], m->mu_brightness, m->sigma_brightness);
-        priors += log_log_normal(hsp[i * 5 + 1], m->mu_blur, m->sigma_blur);
-    }
-    *value = -(sum + priors - log_final);
+    std::vector<double> err;
+    if ((s = free_energy_draws(ctx, m, pixel_intensities, pixels, spots, hoff, hidx, K, F, P, samples, sweeps, seed,
+                               ptr_flags, st, &err)))
+        return s;
+    *value = free_energy_value(m, err, samples, F, P, hsp.data(), K, residuals);
     return RFBA_OK;
 }
+
+// sampled_background_spot_hessian_ffbs (multispot5.cc:902-985)
+int rfba_3b_spot_hessian(rfba_ctx* ctx, const rfba_3b_model* m, const double* sample_bg,
+                         const double* pixel_intensities, const int* pixels, int S, int F, int P,
+                         const double spot[5], int bs_iterations, unsigned long long seed, double hess[25],
+                         int ptr_flags, void* stream) {
+    if (!ctx || !m || !sample_bg || !pixel_intensities || !pixels || !spot || !hess) {
+        set_error("null argument");
+        return RFBA_ERR_INVALID;
+    }
+    int s;
+    if ((s = threeb_validate(m, S, F, P, ptr_flags))) return s;
+    if (F > 2048 || bs_iterations < 1) {
+        set_error("F must be <= 2048 and bs_iterations >= 1");
+        return RFBA_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if ((s = order_streams(ctx, st))) return s;
+    ThreeBData d;
+    if ((s = threeb_stage(ctx, sample_bg, pixel_intensities, pixels, S, F, P, ptr_flags, st, &d))) return s;
+    return spot_hessian_dev(ctx, m, d.bg, d.pix, d.pixels, S, F, P, spot, bs_iterations, seed, hess, st);
+}
+
+// One try of FitSpots::try_modifying_model (multispot5.cc:1840-2160).
+int rfba_3b_modify_model(rfba_ctx* ctx, const rfba_3b_model* m, const double* pixel_intensities, const int* pixels,
+                         int F, int P, double* spots, int* nspots, int capacity, const rfba_3b_fit_params* prm,
+                         unsigned long long seed, rfba_3b_modify_record* record) {
+    int s;
+    if ((s = fit_check(ctx, m, pixel_intensities, pixels, F, P, spots, nspots, capacity, prm))) return s;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = ctx->stream;
+    if ((s = order_streams(ctx, st))) return s;
+    AllowedArea area;
+    area.build(pixels, P, prm->position_extra_radius);
+    std::vector<Spot> sp((size_t)*nspots);
+    for (size_t k = 0; k < sp.size(); ++k)
+        for (int n = 0; n < 5; ++n) sp[k][n] = spots[5 * k + n];
+    if ((s = stage_block(ctx, pixel_intensities, pixels, F, P, st))) return s;
+    rfba_3b_modify_record rec;
+    if ((s = modify_core(ctx, m, pixels, F, P, &sp, *prm, area, seed, &rec, st))) return s;
+    for (size_t k = 0; k < sp.size(); ++k)
+        for (int n = 0; n < 5; ++n) spots[5 * k + n] = sp[k][n];
+    *nspots = (int)sp.size();
+    if (record) *record = rec;
+    return RFBA_OK;
+}
+
+// FitSpots::run (multispot5.cc:2234-2278): iterations of the passes and the
+// model modifications.
+int rfba_3b_fit(rfba_ctx* ctx, const rfba_3b_model* m, const double* pixel_intensities, const int* pixels, int F,
+                int P, double* spots, int* nspots, int capacity, const rfba_3b_fit_params* prm, int first_iteration,
+                int iterations, unsigned long long seed, rfba_3b_fit_fn progress, void* user) {
+    int s;
+    if ((s = fit_check(ctx, m, pixel_intensities, pixels, F, P, spots, nspots, capacity, prm))) return s;
+    if (first_iteration < 0 || iterations < 0) {
+        set_error("first_iteration and iterations must be >= 0");
+        return RFBA_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = ctx->stream;
+    if ((s = order_streams(ctx, st))) return s;
+    AllowedArea area;
+    area.build(pixels, P, prm->position_extra_radius);
+    std::vector<Spot> sp((size_t)*nspots);
+    for (size_t k = 0; k < sp.size(); ++k)
+        for (int n = 0; n < 5; ++n) sp[k][n] = spots[5 * k + n];
+    if ((s = stage_block(ctx, pixel_intensities, pixels, F, P, st))) return s;
+    std::vector<double> flat;
+    auto report = [&](int it, int step) -> bool {
+        if (!progress) return false;
+        flat.assign(sp.size() * 5, 0.0);
+        for (size_t k = 0; k < sp.size(); ++k)
+            for (int n = 0; n < 5; ++n) flat[5 * k + n] = sp[k][n];
+        return progress(it, step, flat.data(), (int)sp.size(), user) != 0;
+    };
+    bool stop = false;
+    for (int it = first_iteration; it < first_iteration + iterations && !stop; ++it) {
+        const unsigned long long it_seed = mix_seed(seed, it, -1);
+        for (int pass = 0; pass < prm->main_passes && !stop; ++pass) {
+            int evals = 0;
+            if ((s = optimise_pass_core(ctx, m, pixels, F, P, &sp, pass + it, prm->main_samples, prm->sweeps,
+                                        prm->main_cg_max_iterations, prm->limit, area, it_seed, pass, &evals, st)))
+                return s;
+            stop = report(it, pass);
+        }
+        for (int t = 0; t < prm->add_remove_tries && !stop; ++t) {
+            if ((int)sp.size() + 1 > capacity) break;
+            rfba_3b_modify_record rec;
+            if ((s = modify_core(ctx, m, pixels, F, P, &sp, *prm, area, mix_seed(it_seed, 1 << 20, t), &rec, st)))
+                return s;
+            stop = report(it, prm->main_passes + t);
+        }
+    }
+    for (size_t k = 0; k < sp.size(); ++k)
+        for (int n = 0; n < 5; ++n) spots[5 * k + n] = sp[k][n];
+    *nspots = (int)sp.size();
+    return RFBA_OK;
+}
+
+int rfba_sym_eigen5(const double a[25], double evals[5], double evecs[25]) {
+    if (!a || !evals || !evecs) {
+        set_error("null argument");
+        return RFBA_ERR_INVALID;
+    }
+    sym_eigen5(a, evals, evecs);
+    return RFBA_OK;
+}
+
+double rfba_det5(const double a[25]) { return a ? det5(a) : 0.0; }
 
 
 // SpotNegProbabilityDiffWithSampledBackground::operator() (multispot5.cc:616-664)

@@ -106,6 +106,48 @@ class ThreeBModel(ctypes.Structure):
         return m
 
 
+class ThreeBFitParams(ctypes.Structure):
+    """rfba_3b_fit_params: settings of a 3B block fit (FitSpots), defaults the
+    shipped multispot5.cfg's."""
+
+    _fields_ = [("main_passes", ctypes.c_int), ("main_samples", ctypes.c_int),
+                ("main_cg_max_iterations", ctypes.c_int), ("sweeps", ctypes.c_int),
+                ("add_remove_tries", ctypes.c_int), ("opt_samples", ctypes.c_int), ("opt_attempts", ctypes.c_int),
+                ("opt_hess_inner_samples", ctypes.c_int), ("h_outer_samples", ctypes.c_int),
+                ("h_inner_samples", ctypes.c_int), ("thermo_samples", ctypes.c_int),
+                ("limit", ctypes.c_double * 5), ("position_extra_radius", ctypes.c_double)]
+
+    @classmethod
+    def make(cls, limit, **kw) -> "ThreeBFitParams":
+        p = cls()
+        d = dict(main_passes=4, main_samples=10, main_cg_max_iterations=5, sweeps=1, add_remove_tries=10,
+                 opt_samples=20, opt_attempts=10, opt_hess_inner_samples=1000, h_outer_samples=100,
+                 h_inner_samples=1000, thermo_samples=1000, position_extra_radius=2.3)
+        d.update(kw)
+        for k, v in d.items():
+            setattr(p, k, v)
+        p.limit[:] = [float(v) for v in np.asarray(limit, np.float64).reshape(5)]
+        return p
+
+
+class ThreeBModifyRecord(ctypes.Structure):
+    """rfba_3b_modify_record: what one model modification did."""
+
+    _fields_ = [("added", ctypes.c_int), ("kept", ctypes.c_int), ("zero_prior", ctypes.c_int),
+                ("bad_hessian", ctypes.c_int), ("evaluations", ctypes.c_int), ("model1_energy", ctypes.c_double),
+                ("model2_energy", ctypes.c_double), ("occam", ctypes.c_double),
+                ("position_log_prior", ctypes.c_double), ("spot", ctypes.c_double * 5)]
+
+    def as_dict(self) -> dict:
+        d = {f: getattr(self, f) for f, _ in self._fields_}
+        d["spot"] = list(self.spot)
+        return d
+
+
+FIT_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_int,
+                          ctypes.c_void_p)
+
+
 class Block(ctypes.Structure):
     """rfba_block: an independent input sub-volume and the magnified region of
     it that is computed and written."""
@@ -188,6 +230,17 @@ def lib():
         L.rfba_3b_optimise_spot.argtypes = [vp, ctypes.POINTER(ThreeBModel), vp, vp, vp, ctypes.c_int, ctypes.c_int,
                                             ctypes.c_int, dp, dp, ctypes.c_int, dp, ipp, ipp, ctypes.c_int, vp]
         L.rfba_cg_only_run.argtypes = [dp, dp, ctypes.c_int, GRAD5_FN, vp, dp, ipp, ipp]
+        L.rfba_3b_spot_hessian.argtypes = [vp, ctypes.POINTER(ThreeBModel), vp, vp, vp, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_int, dp, ctypes.c_int, ull, dp, ctypes.c_int, vp]
+        L.rfba_3b_modify_model.argtypes = [vp, ctypes.POINTER(ThreeBModel), vp, vp, ctypes.c_int, ctypes.c_int, vp,
+                                           ipp, ctypes.c_int, ctypes.POINTER(ThreeBFitParams), ull,
+                                           ctypes.POINTER(ThreeBModifyRecord)]
+        L.rfba_3b_fit.argtypes = [vp, ctypes.POINTER(ThreeBModel), vp, vp, ctypes.c_int, ctypes.c_int, vp, ipp,
+                                  ctypes.c_int, ctypes.POINTER(ThreeBFitParams), ctypes.c_int, ctypes.c_int, ull,
+                                  FIT_FN, vp]
+        L.rfba_sym_eigen5.argtypes = [dp, dp, dp]
+        L.rfba_det5.argtypes = [dp]
+        L.rfba_det5.restype = ctypes.c_double
         L.rfba_probe_fp32_fma_peak.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
         L.SRRFGradientCalc.argtypes = [fp, ip, fp]
         L.SRRFGetMag.argtypes = []
@@ -727,6 +780,71 @@ class Context:
                                            seed, ctypes.byref(ev)))
         return sp[:n.value].copy(), ev.value
 
+    def spot_hessian_3b(self, model: ThreeBModel, sample_bg, pix, pixels, spot, bs_iterations: int = 1000,
+                        seed: int = 0, stream=None):
+        """sampled_background_spot_hessian_ffbs (multispot5.cc:824-985) on the GPU:
+        the 5x5 Hessian of the spot's log probability. Arguments as
+        spot_gradient_3b."""
+        dev = not isinstance(sample_bg, np.ndarray)
+        if dev:
+            S, F, P = (int(v) for v in sample_bg.shape)
+            ptrs = [ctypes.c_void_p(t.data_ptr()) for t in (sample_bg, pix, pixels)]
+        else:
+            sample_bg = np.ascontiguousarray(sample_bg, np.float64)
+            pix = np.ascontiguousarray(pix, np.float64)
+            pixels = np.ascontiguousarray(pixels, np.int32)
+            S, F, P = sample_bg.shape
+            ptrs = [ctypes.c_void_p(a.ctypes.data) for a in (sample_bg, pix, pixels)]
+        sp = np.ascontiguousarray(spot, np.float64)
+        out = np.zeros((5, 5))
+        dp = ctypes.POINTER(ctypes.c_double)
+        _check(lib().rfba_3b_spot_hessian(self.h, ctypes.byref(model), *ptrs, S, F, P, sp.ctypes.data_as(dp),
+                                          int(bs_iterations), seed, out.ctypes.data_as(dp),
+                                          RFBA_DEVICE_PTRS if dev else RFBA_HOST_PTRS, _stream_arg(stream, dev)))
+        return out
+
+    def modify_model_3b(self, model: ThreeBModel, pix, pixels, spots, params: ThreeBFitParams, seed: int = 0):
+        """One try of FitSpots::try_modifying_model (multispot5.cc:1840-2160):
+        returns (spots kept [K'][5], record dict)."""
+        pix = np.ascontiguousarray(pix, np.float64)
+        pixels = np.ascontiguousarray(pixels, np.int32)
+        sp0 = np.ascontiguousarray(spots, np.float64).reshape(-1, 5)
+        sp = np.zeros((len(sp0) + 1, 5))
+        sp[:len(sp0)] = sp0
+        F, P = pix.shape
+        n = ctypes.c_int(len(sp0))
+        rec = ThreeBModifyRecord()
+        vp = ctypes.c_void_p
+        _check(lib().rfba_3b_modify_model(self.h, ctypes.byref(model), vp(pix.ctypes.data), vp(pixels.ctypes.data), F,
+                                          P, vp(sp.ctypes.data), ctypes.byref(n), len(sp), ctypes.byref(params),
+                                          seed, ctypes.byref(rec)))
+        return sp[:n.value].copy(), rec.as_dict()
+
+    def fit_3b(self, model: ThreeBModel, pix, pixels, spots, params: ThreeBFitParams, iterations: int = 1,
+               first_iteration: int = 0, seed: int = 0, capacity: int = 0, progress=None):
+        """FitSpots::run (multispot5.cc:2234-2278) on the GPU: returns the spots
+        after `iterations` iterations. progress(iteration, step, spots) may
+        return True to stop."""
+        pix = np.ascontiguousarray(pix, np.float64)
+        pixels = np.ascontiguousarray(pixels, np.int32)
+        sp0 = np.ascontiguousarray(spots, np.float64).reshape(-1, 5)
+        cap = max(capacity, len(sp0) + max(1, params.add_remove_tries) * max(1, iterations) + 1)
+        sp = np.zeros((cap, 5))
+        sp[:len(sp0)] = sp0
+        F, P = pix.shape
+        n = ctypes.c_int(len(sp0))
+
+        def cb(it, step, ptr, k, user):
+            arr = np.ctypeslib.as_array(ptr, shape=(k * 5,)).reshape(k, 5).copy() if k else np.zeros((0, 5))
+            return 1 if (progress is not None and progress(it, step, arr)) else 0
+
+        fn = FIT_FN(cb)
+        vp = ctypes.c_void_p
+        _check(lib().rfba_3b_fit(self.h, ctypes.byref(model), vp(pix.ctypes.data), vp(pixels.ctypes.data), F, P,
+                                 vp(sp.ctypes.data), ctypes.byref(n), cap, ctypes.byref(params), first_iteration,
+                                 iterations, seed, fn, None))
+        return sp[:n.value].copy()
+
     def check(self):
         """Wait for this context's queued work and raise RfbaError for a failure its
         kernels recorded (a bounded device wait that gave up: RFBA_ERR_TIMEOUT).
@@ -764,6 +882,21 @@ def spot_masks_3b(pixels, spots):
     _check(lib().rfba_3b_spot_masks(vp(px.ctypes.data), P, vp(sp.ctypes.data), K, vp(off.ctypes.data),
                                     vp(idx.ctypes.data), nnz.value, ctypes.byref(nnz)))
     return off, idx[:nnz.value]
+
+
+def sym_eigen5(a):
+    """Eigenvalues (ascending) and eigenvectors (rows) of a symmetric 5x5 matrix,
+    the library's host routine for 3B's model modification."""
+    a = np.ascontiguousarray(a, np.float64).reshape(5, 5)
+    ev, V = np.zeros(5), np.zeros((5, 5))
+    dp = ctypes.POINTER(ctypes.c_double)
+    _check(lib().rfba_sym_eigen5(a.ctypes.data_as(dp), ev.ctypes.data_as(dp), V.ctypes.data_as(dp)))
+    return ev, V
+
+
+def det5(a) -> float:
+    a = np.ascontiguousarray(a, np.float64).reshape(5, 5)
+    return float(lib().rfba_det5(a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
 
 
 def _stream_arg(stream, device_tensors: bool):
