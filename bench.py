@@ -417,11 +417,14 @@ def _threeb_model():
 
 
 def measure_gibbs(ctx) -> dict:
-    """3B's Gibbs sampler, free energy and one main-loop pass on a 29^3 block
-    with 20 spots and 100 frames (the shipped gibbs.mixing_iterations 1,
-    main.gibbs.samples 10, add_remove.thermo.samples 1000, main.cg.max_iterations
-    5, cg.max_motion 0.5, position.extra_radius 2.3): GPU wall time per call,
-    data from host memory."""
+    """3B's Gibbs sampler, free energy, one main-loop pass, the sampled-background
+    Hessian and one model modification on a 29^3 block with 20 spots and 100
+    frames (multispot5.cfg's settings: gibbs.mixing_iterations 1,
+    main.gibbs.samples 10, add_remove.thermo.samples 1000,
+    main.cg.max_iterations 5, cg.max_motion 0.5, position.extra_radius 2.3,
+    add_remove.hessian.outer / inner samples 100 / 1000): GPU wall time per
+    call, data from host memory (the Hessian's 100 draws already on the
+    device)."""
     from rfba_gb300 import srrf
     pix, pixels, spots = _gibbs_block()
     m = _threeb_model()
@@ -441,7 +444,34 @@ def measure_gibbs(ctx) -> dict:
     t0 = time.perf_counter()
     out, ev = ctx.optimise_pass_3b(m, pix, pixels, spots, 0, 10, 1, 5, lim, 2.3, seed=5)
     pass_ms = (time.perf_counter() - t0) * 1e3
-    return {"gibbs": {"what": f"GibbsSampler2 from all spots off: 10 draws x 1 sweep over {K} spots, {F} frames, "
+    # the sampled-background Hessian at spot 0 on 100 draws (add_remove.hessian
+    # outer / inner samples 100 / 1000), the draws' intensities staged on the device
+    import torch
+    _, bg = ctx.gibbs_sample_3b(m, pix, pixels, spots, masks, n_draws=100, seed=6, exclude_spot=0,
+                                want_states=False)
+    bg_d, pix_d, px_d = (torch.from_numpy(a).cuda() for a in (bg, pix, pixels))
+    del bg
+    ctx.spot_hessian_3b(m, bg_d, pix_d, px_d, spots[0], bs_iterations=1000, seed=7)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for r in range(3):
+        ctx.spot_hessian_3b(m, bg_d, pix_d, px_d, spots[0], bs_iterations=1000, seed=8 + r)
+    hess_ms = (time.perf_counter() - t0) / 3 * 1e3
+    del bg_d, pix_d, px_d
+    torch.cuda.empty_cache()
+    # one try of try_modifying_model with the shipped settings
+    prm = srrf.ThreeBFitParams.make(lim)
+    t0 = time.perf_counter()
+    kept, rec = ctx.modify_model_3b(m, pix, pixels, spots, prm, seed=9)
+    mod_ms = (time.perf_counter() - t0) * 1e3
+    return {"hessian": {"what": f"sampled_background_spot_hessian_ffbs: 100 background draws x 1000 backward "
+                                f"samples, {F} frames, {len(pixels)} pixels", "ms": hess_ms},
+            "modify": {"what": f"one try of try_modifying_model on {K} spots with multispot5.cfg's settings "
+                               "(optimiser 20 draws x 10 attempts with 1000-sample Hessians, Hessian 100 x 1000, "
+                               "two free energies of 1000 draws)", "ms": mod_ms, "proposal": "add" if rec["added"]
+                       else "remove", "kept_model": rec["kept"], "gradient_evaluations": rec["evaluations"],
+                       "spots_after": len(kept)},
+            "gibbs": {"what": f"GibbsSampler2 from all spots off: 10 draws x 1 sweep over {K} spots, {F} frames, "
                               f"{len(pixels)} mask voxels (masks {int(masks[0][-1])} voxels in all)",
                       "ms": g_ms, "spot_updates_per_s": 10 * K / (g_ms * 1e-3)},
             "free_energy": {"what": f"NegativeFreeEnergy::compute_with_mask, 1000 thermodynamic samples, {K} spots",
@@ -487,6 +517,15 @@ def threeb_cpu_baseline(res: dict, reps: int = 3) -> dict:
     return out
 
 
+def _port_hessian_draws(pix, pixels, spots, moff, midx, si, A, pi):
+    """Four GibbsSampler2 draws of the block with spot 0 taken off (the port)."""
+    from oracle import gibbs_oracle as G
+    st, ints = G.port_run(pix, si, moff, midx, A, pi, 1.0, 1, 4, 11, want_int=True)
+    for d in range(4):
+        ints[d][st[d, 0] == 0] -= si[0]
+    return st, ints
+
+
 def gibbs_cpu_baseline(res: dict) -> dict:
     """The C++ port of the sampler and of the pass (oracle/gibbs_port.cpp, the
     reference's MT19937 stream and order; the sampler single-threaded as the
@@ -512,7 +551,15 @@ def gibbs_cpu_baseline(res: dict) -> dict:
     _, (tg, tc) = G.port_pass(pix, pixels, spots, 0, 10, 1, 5, lim, 2.3, A, pi, 1.0, 1.0, 3.5, 1.0, 0.12869, 0.1, 5,
                               nthreads=nt, max_spots=2)
     pass_ms = (tg + tc) * 1e3 * K / 2
-    return {"gibbs": {"cpu_ms": g_ms, "speedup_vs_cpu": g_ms / res["gibbs"]["ms"], "cores": 1,
+    # the Hessian on 4 of its 100 background draws, scaled by 25
+    _, bg4 = _port_hessian_draws(pix, pixels, spots, moff, midx, si, A, pi)
+    t0 = time.perf_counter()
+    G.port_spot_hessian(bg4, pix, pixels, spots[0], A, pi, 1.0, 1.0, 3.5, 1.0, 0.12869, 0.1, 1000, 8, nthreads=4)
+    hess_ms = (time.perf_counter() - t0) * 1e3 * 25
+    return {"hessian": {"cpu_ms": hess_ms, "speedup_vs_cpu": hess_ms / res["hessian"]["ms"], "cores": 4,
+                        "sample": "4 of 100 background draws on 4 threads (the reference's threads each take draws), "
+                                  "scaled by 25", "kind": "port"},
+            "gibbs": {"cpu_ms": g_ms, "speedup_vs_cpu": g_ms / res["gibbs"]["ms"], "cores": 1,
                       "kind": "port (draws bit-identical to the reference's GibbsSampler2)"},
             "free_energy": {"cpu_ms": fe_ms, "speedup_vs_cpu": fe_ms / res["free_energy"]["ms"], "cores": 1,
                             "sample": "20 of 1000 draws, scaled by 50"},

@@ -416,6 +416,7 @@ def port():
         L.port_gibbs_run.argtypes = [dp, dp, ip, ip, i, i, i, dp, dp, d, i, i, i, bp, dp]
         L.port_optimise_pass.argtypes = [dp, ip, i, i, dp, ip, i, i, i, i, dp, d, dp, dp, d, d, d, d, d, d, i, i, i,
                                          dp]
+        L.port_spot_hessian.argtypes = [dp, dp, ip, i, i, i, dp, d, d, dp, dp, d, d, d, d, i, i, i, dp]
         _port = L
     return _port
 
@@ -457,3 +458,22 @@ def port_pass(pix, pixels, spots, pass_index, main_samples, sweeps, cg_max_itera
                                    seed, nthreads, max_spots, _p(sec, ctypes.c_double))
     assert rc == 0
     return sp[:n.value].copy(), (float(sec[0]), float(sec[1]))
+
+
+def port_spot_hessian(bg, pix, pixels, spot, A, pi, variance, z_factor, mu_b, sigma_b, mu_blur, sigma_blur,
+                      bs_iterations, seed, nthreads=16):
+    """The port of sampled_background_spot_hessian_ffbs (threads over samples,
+    MT19937 per thread)."""
+    bg = np.ascontiguousarray(bg, np.float64)
+    pix = np.ascontiguousarray(pix, np.float64)
+    S, F, P = bg.shape
+    px = np.ascontiguousarray(pixels, np.int32)
+    sp = np.ascontiguousarray(spot, np.float64)
+    A = np.ascontiguousarray(A, np.float64).reshape(9)
+    pi = np.ascontiguousarray(pi, np.float64)
+    out = np.empty((5, 5))
+    port().port_spot_hessian(_p(bg, ctypes.c_double), _p(pix, ctypes.c_double), _p(px, ctypes.c_int), S, F, P,
+                             _p(sp, ctypes.c_double), z_factor, variance, _p(A, ctypes.c_double),
+                             _p(pi, ctypes.c_double), mu_b, sigma_b, mu_blur, sigma_blur, bs_iterations, seed, nthreads,
+                             _p(out, ctypes.c_double))
+    return out

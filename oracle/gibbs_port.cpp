@@ -18,6 +18,10 @@
 //   dilate_mask
 //   one pass of optimize_each_spot_in_turn_for_several_passes
 //                                       multispot5.cc:1511-1690
+//   sampled_background_spot_hessian_ffbs multispot5.cc:824-985 with
+//                                       spot_shape_hess_position (storm.h:
+//                                       87-146), SpotWithBackground over all
+//                                       pixels and forward_algorithm_delta
 //
 // With the same seed its draws are the reference's draws, bit for bit
 // (tests/test_gibbs_cpu.py checks that against the reference compiled on the
@@ -188,9 +192,129 @@ double spot_shape(const int* x, const double* phi, double zf) {
     return std::exp(s) * phi[0] / (phi[1] * r_2_pi);
 }
 
+// spot_shape_hess_position (storm.h:87-146): value, gradient and Hessian
+// (symmetric) of a spot at a pixel.
+void spot_shape_hess(const int* x, const double* phi, double zf, double* val, double g[5], double H[5][5]) {
+    const double d0 = x[0] - phi[2], d1 = x[1] - phi[3], d2 = x[2] - phi[4];
+    const double d2s = d2 / zf;
+    const double s = -(d0 * d0 + d1 * d1 + d2s * d2s) / (2 * phi[1] * phi[1]);
+    const double r = std::sqrt(2 * M_PI), es = std::exp(s), p0 = phi[0], p1 = phi[1];
+    *val = es * p0 / (p1 * r);
+    const double c = es / (p1 * r);
+    const double dv[3] = {d0, d1, d2};
+    g[0] = c;
+    g[1] = c * (-p0 * (1 + 2 * s) / p1);
+    for (int a = 0; a < 3; ++a) g[2 + a] = c * (dv[a] * (p0 / sq(p1)));
+    H[0][0] = 0;
+    H[0][1] = H[1][0] = -es * (1 + 2 * s) / (p1 * p1 * r);
+    H[1][1] = 2 * p0 * es * (1 + 5 * s + 2 * s * s) / (std::pow(p1, 3) * r);
+    for (int a = 0; a < 3; ++a) {
+        H[0][2 + a] = H[2 + a][0] = es * dv[a] / (std::pow(p1, 3) * r);
+        H[1][2 + a] = H[2 + a][1] = -p0 * es * (3 + 2 * s) * dv[a] / (std::pow(p1, 4) * r);
+        for (int b = a; b < 3; ++b)
+            H[2 + a][2 + b] = H[2 + b][2 + a] =
+                a == b ? p0 * es * (sq(dv[a]) - sq(p1)) / (r * std::pow(p1, 5))
+                       : p0 * es * dv[a] * dv[b] / (r * std::pow(p1, 5));
+    }
+}
+
 }  // namespace
 
 extern "C" {
+
+// sampled_background_spot_hessian_ffbs (multispot5.cc:824-985): the samples
+// split over nthreads threads as the reference's threads take them (sample i
+// on thread i % nthreads), each thread with its own MT19937 (simple_seed(seed
+// + thread)). bg [S][F][P]; hess [25].
+int port_spot_hessian(const double* bg, const double* pix, const int* pixels, int S, int F, int P, const double* spot,
+                      double zFactor, double variance, const double* A, const double* pi, double mu_b,
+                      double sigma_b, double mu_blur, double sigma_blur, int bs_iterations, int seed, int nthreads,
+                      double* hess) {
+    std::vector<double> val((size_t)P), g((size_t)P * 5), H((size_t)P * 25);
+    for (int p = 0; p < P; ++p) {
+        double h[5][5];
+        spot_shape_hess(pixels + 3 * p, spot, zFactor, &val[p], &g[(size_t)p * 5], h);
+        for (int a = 0; a < 5; ++a)
+            for (int b = 0; b < 5; ++b) H[(size_t)p * 25 + a * 5 + b] = h[a][b];
+    }
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > S) nthreads = S;
+    std::vector<double> th_hess((size_t)nthreads * 25, 0.0), th_deriv((size_t)nthreads * 5, 0.0);
+    double lA[9];
+    for (int i = 0; i < 9; i++) lA[i] = ln_(A[i]);
+#pragma omp parallel for num_threads(nthreads) schedule(static, 1)
+    for (int t = 0; t < nthreads; ++t) {
+        RefRng rng(seed + t);
+        std::vector<double> part((size_t)F * 30);  // per frame: Hessian [25], derivative [5]
+        std::vector<std::array<double, 3> > delta((size_t)F);
+        std::vector<unsigned char> st((size_t)F);
+        double* sh = th_hess.data() + (size_t)t * 25;
+        double* sd = th_deriv.data() + (size_t)t * 5;
+        for (int i = t; i < S; i += nthreads) {
+            const double* b = bg + (size_t)i * F * P;
+            std::vector<std::pair<double, double> > lp((size_t)F);
+            for (int f = 0; f < F; ++f) {
+                double* hp = part.data() + (size_t)f * 30;
+                std::fill(hp, hp + 30, 0.0);
+                double log_prob_off = 0, log_prob_on = 0;
+                for (int p = 0; p < P; ++p) {
+                    const double d = pix[(size_t)f * P + p], c = b[(size_t)f * P + p];
+                    const double e = d - (c + val[p]);
+                    log_prob_off -= sq(d - c);
+                    log_prob_on -= sq(e);
+                    const double* gp = &g[(size_t)p * 5];
+                    const double* Hp = &H[(size_t)p * 25];
+                    for (int a = 0; a < 5; ++a)
+                        for (int c2 = 0; c2 < 5; ++c2) hp[a * 5 + c2] += e * Hp[a * 5 + c2] - gp[a] * gp[c2];
+                    for (int a = 0; a < 5; ++a) hp[25 + a] += e * gp[a];
+                }
+                lp[f] = std::make_pair(log_prob_on / (2 * variance) - P * ::log(2 * M_PI * variance) / 2,
+                                       log_prob_off / (2 * variance) - P * ::log(2 * M_PI * variance) / 2);
+            }
+            auto B = [&](int s2, int f) { return s2 == 0 ? lp[f].first : lp[f].second; };
+            for (int k = 0; k < 3; k++) delta[0][k] = ln_(pi[k]) + B(k, 0);
+            for (int f = 1; f < F; f++)
+                for (int j = 0; j < 3; j++) {
+                    double Z = -HUGE_VAL;
+                    for (int k = 0; k < 3; k++) Z = std::max(Z, delta[f - 1][k] + lA[k * 3 + j]);
+                    double sum = 0;
+                    for (int k = 0; k < 3; k++) sum += std::exp(delta[f - 1][k] + lA[k * 3 + j] - Z);
+                    delta[f][j] = B(j, f) + Z + ln_(sum);
+                }
+            for (int it = 0; it < bs_iterations; ++it) {
+                st[F - 1] = (unsigned char)sample_unscaled_log(delta[F - 1], rng);
+                for (int f = F - 2; f >= 0; f--) {
+                    std::array<double, 3> r = delta[f];
+                    for (int j = 0; j < 3; j++) r[j] += lA[j * 3 + st[f + 1]];
+                    st[f] = (unsigned char)sample_unscaled_log(r, rng);
+                }
+                double h[25] = {0}, d[5] = {0};
+                for (int f = 0; f < F; ++f)
+                    if (st[f] == 0) {
+                        const double* hp = part.data() + (size_t)f * 30;
+                        for (int a = 0; a < 25; ++a) h[a] += hp[a];
+                        for (int a = 0; a < 5; ++a) d[a] += hp[25 + a];
+                    }
+                for (int a = 0; a < 5; ++a)
+                    for (int c2 = 0; c2 < 5; ++c2) sh[a * 5 + c2] += h[a * 5 + c2] + d[a] * d[c2];
+                for (int a = 0; a < 5; ++a) sd[a] += d[a];
+            }
+        }
+    }
+    double sum_hess[25] = {0}, sum_deriv[5] = {0};
+    for (int t = 0; t < nthreads; ++t) {
+        for (int a = 0; a < 25; ++a) sum_hess[a] += th_hess[(size_t)t * 25 + a];
+        for (int a = 0; a < 5; ++a) sum_deriv[a] += th_deriv[(size_t)t * 5 + a];
+    }
+    const double norm = (double)bs_iterations * S * variance;
+    for (int a = 0; a < 25; ++a) sum_hess[a] /= norm;
+    for (int a = 0; a < 5; ++a) sum_deriv[a] /= norm;
+    for (int a = 0; a < 5; ++a)
+        for (int c2 = 0; c2 < 5; ++c2) hess[a * 5 + c2] = sum_hess[a * 5 + c2] - sum_deriv[a] * sum_deriv[c2];
+    hess[0] += (1 + (ln_(spot[0]) - mu_b - 1) / sq(sigma_b)) / sq(spot[0]);
+    hess[6] += (1 + (ln_(spot[1]) - mu_blur - 1) / sq(sigma_blur)) / sq(spot[1]);
+    return 0;
+}
 
 // GibbsSampler2: n_draws calls of next() from all spots off, MT19937 seeded by
 // simple_seed(seed). si [K][P] spot intensities, masks as offsets / indices.

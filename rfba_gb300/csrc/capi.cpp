@@ -52,7 +52,7 @@ static bool checks_enabled() {
 static int test_tma_stall();
 static int device_status(rfba_ctx* ctx, cudaStream_t st, const char* what);
 
-static bool verbose() {
+bool verbose() {
     static int v = -1;
     if (v < 0) {
         const char* e = std::getenv("RFBA_VERBOSE");

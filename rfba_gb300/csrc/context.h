@@ -28,6 +28,8 @@ int cuda_fail(cudaError_t e, const char* what);
 // Makes `st` wait for the previous call's work when that call used another
 // stream (calls share the context's scratch).
 int order_streams(rfba_ctx* ctx, cudaStream_t st);
+// RFBA_VERBOSE=1: per-call schedule and timing lines on stderr.
+bool verbose();
 
 #define RFBA_CUDA(call, what)                          \
     do {                                               \

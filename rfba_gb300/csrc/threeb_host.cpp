@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <array>
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -769,6 +770,12 @@ static int modify_core(rfba_ctx* ctx, const rfba_3b_model* m, const int* pixels,
     std::vector<Spot>& sp = *spots;
     const int K = (int)sp.size();
     std::memset(rec, 0, sizeof *rec);
+    // seconds in: draws, optimiser, Hessians, free energies
+    double secs[4] = {0, 0, 0, 0};
+    auto clock = [] { return std::chrono::steady_clock::now(); };
+    auto since = [](std::chrono::steady_clock::time_point t0) {
+        return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    };
     // add with probability 1/2, always with one spot (multispot5.cc:1851) and,
     // here, with none (the reference would index an empty list)
     const bool add = rng.next() > 0.5 || K <= 1;
@@ -802,8 +809,10 @@ static int modify_core(rfba_ctx* ctx, const rfba_3b_model* m, const int* pixels,
         std::vector<int> hoff, hidx;
         flatten_masks(masks2, model2.size(), &hoff, &hidx);
         const int S = prm.opt_samples;
+        auto t0 = clock();
         if ((s = draws_without(ctx, m, F, P, model2, hoff, hidx, S, prm.sweeps, spot, mix_seed(seed, 1, 0), st)))
             return s;
+        secs[0] += since(t0);
         StagedGradient grad{ctx, m, ThreeBData(), st};
         if ((s = threeb_stage(ctx, static_cast<const double*>(ctx->gb_oint.p), static_cast<const double*>(ctx->gb_pix.p),
                               static_cast<const int*>(ctx->gb_pixels.p), S, F, P, RFBA_DEVICE_PTRS, st, &grad.d)))
@@ -811,14 +820,18 @@ static int modify_core(rfba_ctx* ctx, const rfba_3b_model* m, const int* pixels,
         CgOnly5 cg;
         if ((s = cg.start(model2[spot].data(), prm.limit, grad))) return s;
         for (int attempt = 0; attempt < prm.opt_attempts; attempt++) {
+            t0 = clock();
             if ((s = cg.run(grad))) return s;
+            secs[1] += since(t0);
             if (attempt < prm.opt_attempts - 1) {
                 double H[25], ev[5], V[25];
+                t0 = clock();
                 if ((s = spot_hessian_dev(ctx, m, static_cast<const double*>(ctx->gb_oint.p),
                                           static_cast<const double*>(ctx->gb_pix.p),
                                           static_cast<const int*>(ctx->gb_pixels.p), S, F, P, cg.x,
                                           prm.opt_hess_inner_samples, mix_seed(seed, 2, attempt), H, st)))
                     return s;
+                secs[2] += since(t0);
                 sym_eigen5(H, ev, V);
                 if (ev[4] < 0) break;  // negative definite
                 // restart along the fourth eigenvector (ascending order)
@@ -849,13 +862,17 @@ static int modify_core(rfba_ctx* ctx, const rfba_3b_model* m, const int* pixels,
         }
         hoff[model2.size()] = (int)(model2.size() * P);
         const int S = prm.h_outer_samples;
+        auto t0 = clock();
         if ((s = draws_without(ctx, m, F, P, model2, hoff, hidx, S, prm.sweeps, spot, mix_seed(seed, 3, 0), st)))
             return s;
+        secs[0] += since(t0);
         double H[25], negH[25], ev[5], V[25];
+        t0 = clock();
         if ((s = spot_hessian_dev(ctx, m, static_cast<const double*>(ctx->gb_oint.p),
                                   static_cast<const double*>(ctx->gb_pix.p), static_cast<const int*>(ctx->gb_pixels.p), S,
                                   F, P, model2[spot].data(), prm.h_inner_samples, mix_seed(seed, 4, 0), H, st)))
             return s;
+        secs[2] += since(t0);
         double scaled[25];
         for (int n = 0; n < 25; ++n) {
             negH[n] = -H[n];
@@ -865,11 +882,13 @@ static int modify_core(rfba_ctx* ctx, const rfba_3b_model* m, const int* pixels,
         sym_eigen5(negH, ev, V);
         if (ev[0] > 1e-6) {
             double e2 = 0, e1 = 0;
+            t0 = clock();
             if ((s = model_energy(ctx, m, F, P, model2, masks2, prm.thermo_samples, prm.sweeps, mix_seed(seed, 5, 0), st,
                                   &e2)) ||
                 (s = model_energy(ctx, m, F, P, model1, masks2, prm.thermo_samples, prm.sweeps, mix_seed(seed, 6, 0), st,
                                   &e1)))
                 return s;
+            secs[3] += since(t0);
             const double occam = -0.5 * std::log(det);
             const double p2 = e2 + occam + pos_lp;
             rec->model1_energy = e1;
@@ -882,6 +901,11 @@ static int modify_core(rfba_ctx* ctx, const rfba_3b_model* m, const int* pixels,
     }
     rec->kept = keep;
     sp = keep == 2 ? model2 : model1;
+    if (verbose())
+        std::fprintf(stderr,
+                     "rfba: 3B modification (%s, kept %d): draws %.3f s, optimiser %.3f s (%d evaluations), "
+                     "Hessians %.3f s, free energies %.3f s\n",
+                     add ? "add" : "remove", keep, secs[0], secs[1], rec->evaluations, secs[2], secs[3]);
     return RFBA_OK;
 }
 
@@ -934,23 +958,44 @@ int rfba_3b_spot_masks(const int* pixels, int P, const double* spots, int K, int
     mask_offsets[0] = 0;
     for (int k = 0; k < K; ++k) {
         const double* sp = spots + 5 * (size_t)k;
-        const std::vector<int> b = ball((float)(sp[1] * 6 + 1));
+        const float radius = (float)(sp[1] * 6 + 1);
         const int ox = round_away(sp[2]), oy = round_away(sp[3]), oz = round_away(sp[4]);
-        for (size_t j = 0; j < b.size(); j += 3) {
-            const int t[3] = {b[j] + ox, b[j + 1] + oy, b[j + 2] + oz};
-            int lo = 0, hi = P;  // lower_bound
-            while (lo < hi) {
-                const int mid = (lo + hi) / 2;
-                const int* q = pixels + 3 * mid;
-                const bool lt = q[2] < t[2] || (q[2] == t[2] && q[1] < t[1]) || (q[2] == t[2] && q[1] == t[1] && q[0] < t[0]);
-                if (lt)
-                    lo = mid + 1;
-                else
-                    hi = mid;
+        const double r = std::ceil((double)radius + 1);
+        if (!(r < 1024) || (2 * r + 1) * (2 * r + 1) * (2 * r + 1) > (double)P) {
+            // a ball with more offsets than the block has pixels: test the
+            // pixels instead. They are sorted by (z, y, x), and so are their
+            // offsets from the centre, which is the ball's order; a blur that is
+            // not finite gives an empty mask
+            for (int q = 0; q < P; ++q) {
+                const long long d[3] = {(long long)pixels[3 * q] - ox, (long long)pixels[3 * q + 1] - oy,
+                                        (long long)pixels[3 * q + 2] - oz};
+                if (std::fabs((double)d[0]) > r || std::fabs((double)d[1]) > r || std::fabs((double)d[2]) > r) continue;
+                const unsigned int m2 = (unsigned int)(d[0] * d[0]) + (unsigned int)(d[1] * d[1]) +
+                                        (unsigned int)(d[2] * d[2]);
+                if ((float)m2 <= radius * radius) {
+                    if (mask_pixels && n < cap) mask_pixels[n] = q;
+                    ++n;
+                }
             }
-            if (lo < P && pixels[3 * lo] == t[0] && pixels[3 * lo + 1] == t[1] && pixels[3 * lo + 2] == t[2]) {
-                if (mask_pixels && n < cap) mask_pixels[n] = lo;
-                ++n;
+        } else {
+            const std::vector<int> b = ball(radius);
+            for (size_t j = 0; j < b.size(); j += 3) {
+                const int t[3] = {b[j] + ox, b[j + 1] + oy, b[j + 2] + oz};
+                int lo = 0, hi = P;  // lower_bound
+                while (lo < hi) {
+                    const int mid = (lo + hi) / 2;
+                    const int* q = pixels + 3 * mid;
+                    const bool lt = q[2] < t[2] || (q[2] == t[2] && q[1] < t[1]) ||
+                                    (q[2] == t[2] && q[1] == t[1] && q[0] < t[0]);
+                    if (lt)
+                        lo = mid + 1;
+                    else
+                        hi = mid;
+                }
+                if (lo < P && pixels[3 * lo] == t[0] && pixels[3 * lo + 1] == t[1] && pixels[3 * lo + 2] == t[2]) {
+                    if (mask_pixels && n < cap) mask_pixels[n] = lo;
+                    ++n;
+                }
             }
         }
         if (n > INT32_MAX) {

@@ -57,6 +57,28 @@ def test_library_masks_equal_oracle(built_lib):
                                 off.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), None, 0, ctypes.byref(nnz)) == -1
 
 
+def test_masks_of_wide_spots_scan_the_pixels(built_lib):
+    """A ball with more offsets than the block has pixels is found by testing
+    the pixels (in their (z, y, x) order, which is the ball's order): the same
+    masks as enumerating the ball, on an irregular pixel set; a blur that is not
+    finite or enormous still returns at once."""
+    from oracle import gibbs_oracle as G
+    from rfba_gb300 import srrf
+    rng = np.random.default_rng(3)
+    n = 17
+    zz, yy, xx = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    pixels = np.stack([xx.ravel(), yy.ravel(), zz.ravel()], 1).astype(np.int32)
+    pixels = pixels[rng.random(len(pixels)) < 0.8]
+    spots = np.array([[30, 0.3, 8.2, 7.6, 8.9], [30, 1.1, 3.4, 12.5, 5.5], [30, 2.5, 8, 8, 8],
+                      [30, 4.0, 2.2, 3.3, 14.6], [30, 0.8, -3.2, 20.4, 8.0]])
+    off, idx = srrf.spot_masks_3b(pixels, spots)
+    off2, idx2 = G.spot_masks(pixels, spots)
+    np.testing.assert_array_equal(off, off2)
+    np.testing.assert_array_equal(idx, idx2)
+    off, _ = srrf.spot_masks_3b(pixels, np.array([[30, 1e6, 8, 8, 8], [30, np.nan, 8, 8, 8]]))
+    assert off.tolist() == [0, len(pixels), len(pixels)]
+
+
 @needs_ref
 def test_spot_intensity_matches_reference():
     pix, pixels, spots, moff, midx = _block()
