@@ -256,7 +256,10 @@ typedef struct rfba_3b_model {
  * sample's log probability; may be NULL) are host memory; the call returns
  * when out is written. spot[0] <= 0 or spot[1] <= 0 gives NaN, as the
  * reference does; entries of A or pi outside [0, 1] give RFBA_ERR_INVALID.
- * FP64 throughout. */
+ * FP64 throughout when log_prob is requested; without it (as the spot
+ * optimisers call it) the per-frame sums over the pixels run in double-float
+ * arithmetic on the FP32 pipe (about 2^-46 relative per operation) on
+ * residuals staged once. */
 int rfba_3b_spot_gradient(rfba_ctx* ctx, const rfba_3b_model* model, const double* sample_bg,
                           const double* pixel_intensities, const int* pixels, int S, int F, int P,
                           const double spot[5], double out[5], double* log_prob, int ptr_flags, void* stream);

@@ -138,7 +138,7 @@ struct rfba_ctx {
     // spot seeding scratch
     rfba::DevBuf seed_w, seed_sums, seed_carry, seed_map, seed_vox, seed_xyz;
     // 3B spot-gradient scratch
-    rfba::DevBuf tb_val, tb_der, tb_em, tb_res, tb_par, tb_bg, tb_pix, tb_pixels;
+    rfba::DevBuf tb_val, tb_der, tb_em, tb_res, tb_par, tb_bg, tb_pix, tb_pixels, tb_dfd, tb_vdf;
     // 3B Gibbs sampler scratch
     rfba::DevBuf gb_pix, gb_pixels, gb_spots, gb_si, gb_moff, gb_midx, gb_state, gb_cur, gb_em, gb_bar, gb_var,
         gb_ostate, gb_oint, gb_oerr, gb_lp, gb_filt;

@@ -25,38 +25,15 @@
 #pragma once
 #include <cstdint>
 
+#include "dfloat.cuh"
+
 namespace rfba {
 namespace ffbs {
 
+using namespace dfloat;
+
 constexpr int kZeroExp = -(1 << 29);  // exponent of a zero forward value
 constexpr int kDropBits = 100;
-
-__device__ __forceinline__ float2 df_from(double v) {
-    const float h = __double2float_rn(v);
-    return make_float2(h, __double2float_rn(v - (double)h));
-}
-__device__ __forceinline__ double df_to(float2 a) { return (double)a.x + (double)a.y; }
-// s + e with |s| >= |e| as a normalised pair
-__device__ __forceinline__ float2 df_fast_two_sum(float s, float e) {
-    const float r = s + e;
-    return make_float2(r, e - (r - s));
-}
-__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
-    const float p = a.x * b.x;
-    float e = fmaf(a.x, b.x, -p);
-    e = fmaf(a.x, b.y, e);
-    e = fmaf(a.y, b.x, e);
-    return df_fast_two_sum(p, e);
-}
-__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
-    const float s = a.x + b.x;
-    const float v = s - a.x;
-    float e = (a.x - (s - v)) + (b.x - v);
-    e += a.y + b.y;
-    return df_fast_two_sum(s, e);
-}
-// 2^d as a float, -126 <= d <= 127
-__device__ __forceinline__ float pow2f(int d) { return __int_as_float((d + 127) << 23); }
 
 // exp(x) = mant 2^k for x <= 0 (mant in [1, 2)): x = k ln2 + r with r by one
 // fused multiply-add. Relative probabilities below 2^-(2^24) are 0. exp(0) is

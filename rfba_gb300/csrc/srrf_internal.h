@@ -1,6 +1,8 @@
 // Internal definitions shared by the host planner (plan.cpp, capi.cpp) and the
 // CUDA kernels (radiality.cu, temporal.cu). Not part of the public C-ABI.
 #pragma once
+#include <vector_types.h>
+
 #include <cstdint>
 #include <cstddef>
 #include <string>
@@ -248,6 +250,10 @@ int launch_spot_hessian(const HessParams& h, void* stream);
 // frame), forward algorithm per sample; res[s] = (gradient[5], log probability).
 int launch_threeb(const double* bg, const double* pix, const int* pixels, int S, int F, int P, const double* phi_dev,
                   double zf, double variance, double c0, const double* A_dev, const double* pi_dev,
-                  double* val, double* der, double* em, double* res, void* stream);
+                  double* val, double* der, double* em, double* res, const float2* dfd, float2* vdf,
+                  void* stream);
+// The samples' residuals (data minus background) as double-floats [S][F][P],
+// for the gradient-only evaluations of launch_threeb (dfd; vdf is [P][6]).
+int launch_threeb_residual(const double* bg, const double* pix, int S, int F, int P, float2* dfd, void* stream);
 
 }  // namespace rfba

@@ -25,8 +25,19 @@
 //      frames start to favour a state it cannot reach).
 // The host averages the samples' gradients and adds the log-normal priors'
 // derivatives (storm.h:431-434).
+//
+// The spot optimiser evaluates the gradient thousands of times on the same
+// samples and needs no log probability, so for it the samples' residuals
+// (data minus background) are staged once as double-float numbers
+// (residual_df_kernel) and emission_df_kernel forms the gradient's sums
+// (sum d v, sum der_n d) on the FP32 pipe in double-float arithmetic, about
+// 2^-46 relative per operation, four samples of a frame per CTA so the spot's
+// table is read once per four: the FP64 pipe, 1/64 of the FP32 one here,
+// would otherwise bound every evaluation. The log-probability path keeps the
+// FP64 sums.
 #include <cuda_runtime.h>
 
+#include "dfloat.cuh"
 #include "srrf_internal.h"
 
 namespace rfba {
@@ -35,58 +46,78 @@ namespace {
 constexpr int kM = 5;
 constexpr int kEmitThreads = 256;
 
-__global__ void spot_pixels_kernel(const int* __restrict__ pixels, int P, const double* __restrict__ phi_in,
-                                   double zf, double* __restrict__ val, double* __restrict__ der) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= P) return;
-    const double phi0 = phi_in[0], phi1 = phi_in[1], phi2 = phi_in[2], phi3 = phi_in[3], phi4 = phi_in[4];
-    const double x0 = pixels[3 * p], x1 = pixels[3 * p + 1], x2 = pixels[3 * p + 2];
-    const double d0 = x0 - phi2, d1 = x1 - phi3, d2 = (x2 - phi4) / zf;
-    const double s = -(d0 * d0 + d1 * d1 + d2 * d2) / (2 * phi1 * phi1);
-    const double r_2_pi = sqrt(2 * 3.14159265358979323846);
-    const double es = exp(s);
-    val[p] = es * phi0 / (phi1 * r_2_pi);
-    const double k = es / (phi1 * r_2_pi);
-    const double q = phi0 / (phi1 * phi1);
-    double* d = der + (size_t)p * kM;
-    d[0] = k;
-    d[1] = k * (-phi0 * (1 + 2 * s) / phi1);
-    d[2] = k * ((x0 - phi2) * q);
-    d[3] = k * ((x1 - phi3) * q);
-    d[4] = k * ((x2 - phi4) * q);
-}
+using namespace dfloat;
 
-// The spot's own sums over the mask, sum v^2 and sum der_n v (one CTA, fixed
-// order): with d = I - G, sum (d - v)^2 = sum d^2 - 2 sum d v + sum v^2 and
-// sum der_n (d - v) = sum der_n d - sum der_n v, so the per-(sample, frame)
-// pass needs 8 FP64 operations per voxel instead of 10.
-constexpr int kSumThreads = 512;
-__global__ void __launch_bounds__(kSumThreads) spot_sums_kernel(const double* __restrict__ val,
-                                                                 const double* __restrict__ der, int P,
-                                                                 double* __restrict__ sums) {
-    double acc[6] = {0, 0, 0, 0, 0, 0};
-    for (int p = threadIdx.x; p < P; p += kSumThreads) {
-        const double v = val[p];
-        acc[0] += v * v;
+constexpr int kPixThreads = 256;
+__global__ void __launch_bounds__(kPixThreads) spot_pixels_kernel(const int* __restrict__ pixels, int P,
+                                                                   const double* __restrict__ phi_in, double zf,
+                                                                   double* __restrict__ val, double* __restrict__ der,
+                                                                   float2* __restrict__ vdf,
+                                                                   double* __restrict__ partial) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc[6] = {0, 0, 0, 0, 0, 0};  // this pixel's v^2 and der_n v
+    if (p < P) {
+        const double phi0 = phi_in[0], phi1 = phi_in[1], phi2 = phi_in[2], phi3 = phi_in[3], phi4 = phi_in[4];
+        const double x0 = pixels[3 * p], x1 = pixels[3 * p + 1], x2 = pixels[3 * p + 2];
+        const double d0 = x0 - phi2, d1 = x1 - phi3, d2 = (x2 - phi4) / zf;
+        const double s = -(d0 * d0 + d1 * d1 + d2 * d2) / (2 * phi1 * phi1);
+        const double r_2_pi = sqrt(2 * 3.14159265358979323846);
+        const double es = exp(s);
+        val[p] = es * phi0 / (phi1 * r_2_pi);
+        const double k = es / (phi1 * r_2_pi);
+        const double q = phi0 / (phi1 * phi1);
+        double* d = der + (size_t)p * kM;
+        d[0] = k;
+        d[1] = k * (-phi0 * (1 + 2 * s) / phi1);
+        d[2] = k * ((x0 - phi2) * q);
+        d[3] = k * ((x1 - phi3) * q);
+        d[4] = k * ((x2 - phi4) * q);
+        if (vdf) {  // value and derivative as double-floats: [P][6]
+            float2* o = vdf + (size_t)p * 6;
+            o[0] = df_from(val[p]);
 #pragma unroll
-        for (int n = 0; n < kM; ++n) acc[1 + n] += der[(size_t)p * kM + n] * v;
+            for (int n = 0; n < kM; ++n) o[1 + n] = df_from(d[n]);
+        }
+        const double v = val[p];
+        acc[0] = v * v;
+#pragma unroll
+        for (int n = 0; n < kM; ++n) acc[1 + n] = d[n] * v;
     }
+    // the block's share of the spot's sums, in a fixed order
 #pragma unroll
     for (int i = 0; i < 6; ++i)
         for (int o = 16; o > 0; o >>= 1) acc[i] += __shfl_down_sync(0xffffffffu, acc[i], o);
-    __shared__ double part[kSumThreads / 32][6];
+    __shared__ double part[kPixThreads / 32][6];
     if ((threadIdx.x & 31) == 0)
 #pragma unroll
         for (int i = 0; i < 6; ++i) part[threadIdx.x >> 5][i] = acc[i];
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double t[6] = {0, 0, 0, 0, 0, 0};
-        for (int w = 0; w < kSumThreads / 32; ++w)
-#pragma unroll
-            for (int i = 0; i < 6; ++i) t[i] += part[w][i];
-#pragma unroll
-        for (int i = 0; i < 6; ++i) sums[i] = t[i];
+    if (threadIdx.x < 6) {
+        double t = 0;
+        for (int w = 0; w < kPixThreads / 32; ++w) t += part[w][threadIdx.x];
+        partial[(size_t)blockIdx.x * 6 + threadIdx.x] = t;
     }
+}
+
+// The samples' residuals, data minus background, as double-floats [S][F][P].
+__global__ void residual_df_kernel(const double* __restrict__ bg, const double* __restrict__ pix, int F, int P,
+                                   long long n, float2* __restrict__ out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const long long fp = i % ((long long)F * P);
+    out[i] = df_from(pix[fp] - bg[i]);
+}
+
+// The spot's own sums over the mask, sum v^2 and sum der_n v, from the
+// blocks' partial sums in block order (one thread per sum): with d = I - G,
+// sum (d - v)^2 = sum d^2 - 2 sum d v + sum v^2 and sum der_n (d - v) =
+// sum der_n d - sum der_n v, so the per-(sample, frame) pass needs 8 FP64
+// operations per voxel instead of 10.
+__global__ void spot_sums_kernel(const double* __restrict__ partial, int nblocks, double* __restrict__ sums) {
+    if (threadIdx.x >= 6) return;
+    double t = 0;
+    for (int b = 0; b < nblocks; ++b) t += partial[(size_t)b * 6 + threadIdx.x];
+    sums[threadIdx.x] = t;
 }
 
 // Per (sample, frame), kEm doubles: the frame's emission probabilities relative
@@ -162,6 +193,84 @@ __global__ void __launch_bounds__(kEmitThreads) emission_kernel(const double* __
         }
 #pragma unroll
         for (int n = 0; n < kM; ++n) o[4 + n] = (t[2 + n] - spot_sums[1 + n]) / var;
+    }
+}
+
+// The gradient's emission terms from the double-float residuals, kDfTile
+// samples of one frame per CTA (blockIdx.x = frame, blockIdx.y = sample
+// tile): per sample sum d v and sum der_n d in double-float, then the same
+// terms as emission_kernel writes except the frame's level (entry 9, used by
+// the log probability only), which is 0.
+constexpr int kDfTile = 4;
+__global__ void __launch_bounds__(kEmitThreads) emission_df_kernel(const float2* __restrict__ dfd,
+                                                                    const float2* __restrict__ vdf,
+                                                                    const double* __restrict__ spot_sums, int S, int F,
+                                                                    int P, double twovar, double var,
+                                                                    double* __restrict__ out) {
+    const int f = blockIdx.x, s0 = blockIdx.y * kDfTile;
+    const int ns = min(kDfTile, S - s0);
+    float2 acc[kDfTile][6];
+#pragma unroll
+    for (int a = 0; a < kDfTile; ++a)
+#pragma unroll
+        for (int n = 0; n < 6; ++n) acc[a][n] = make_float2(0.f, 0.f);
+    for (int p = threadIdx.x; p < P; p += kEmitThreads) {
+        // every load of the iteration goes out before its arithmetic (a tile's
+        // missing samples read 0 and add 0)
+        float2 w[6], d[kDfTile];
+#pragma unroll
+        for (int a = 0; a < kDfTile; ++a)
+            d[a] = a < ns ? __ldg(dfd + ((size_t)(s0 + a) * F + f) * P + p) : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int n = 0; n < 6; ++n) w[n] = __ldg(vdf + (size_t)p * 6 + n);
+#pragma unroll
+        for (int a = 0; a < kDfTile; ++a)
+#pragma unroll
+            for (int n = 0; n < 6; ++n) df_acc_mul(acc[a][n], w[n], d[a]);
+    }
+#pragma unroll
+    for (int a = 0; a < kDfTile; ++a)
+#pragma unroll
+        for (int n = 0; n < 6; ++n) acc[a][n] = df_two_sum(acc[a][n].x, acc[a][n].y);
+    __shared__ float2 part[kEmitThreads / 32][kDfTile][6];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int a = 0; a < kDfTile; ++a)
+#pragma unroll
+        for (int n = 0; n < 6; ++n) {
+            float2 v = acc[a][n];
+            for (int o = 16; o > 0; o >>= 1) {
+                float2 u;
+                u.x = __shfl_down_sync(0xffffffffu, v.x, o);
+                u.y = __shfl_down_sync(0xffffffffu, v.y, o);
+                v = df_add(v, u);
+            }
+            if (lane == 0) part[warp][a][n] = v;
+        }
+    __syncthreads();
+    if (threadIdx.x < ns) {
+        const int a = threadIdx.x;
+        double t[6];
+#pragma unroll
+        for (int n = 0; n < 6; ++n) {
+            float2 v = part[0][a][n];
+            for (int w = 1; w < kEmitThreads / 32; ++w) v = df_add(v, part[w][a][n]);
+            t[n] = df_to(v);
+        }
+        double* o = out + ((size_t)(s0 + a) * F + f) * kEm;
+        const double gap = (2.0 * t[0] - spot_sums[0]) / twovar;  // log p_on - log p_off
+        if (gap <= 0.0) {
+            exp_split(gap, &o[0], &o[2]);
+            o[1] = 1.0;
+            o[3] = 0.0;
+        } else {
+            o[0] = 1.0;
+            o[2] = 0.0;
+            exp_split(-gap, &o[1], &o[3]);
+        }
+        o[9] = 0.0;
+#pragma unroll
+        for (int n = 0; n < kM; ++n) o[4 + n] = (t[1 + n] - spot_sums[1 + n]) / var;
     }
 }
 
@@ -281,15 +390,29 @@ __global__ void __launch_bounds__(32) forward_kernel(const double* __restrict__ 
 
 }  // namespace
 
+int launch_threeb_residual(const double* bg, const double* pix, int S, int F, int P, float2* dfd, void* stream) {
+    const long long n = (long long)S * F * P;
+    if (n == 0) return 0;
+    residual_df_kernel<<<(unsigned)((n + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(bg, pix, F, P, n,
+                                                                                                    dfd);
+    return (int)cudaGetLastError();
+}
+
 int launch_threeb(const double* bg, const double* pix, const int* pixels, int S, int F, int P, const double* phi_dev,
                   double zf, double variance, double c0, const double* A_dev, const double* pi_dev,
-                  double* val, double* der, double* em, double* res, void* stream) {
+                  double* val, double* der, double* em, double* res, const float2* dfd, float2* vdf, void* stream) {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    spot_pixels_kernel<<<(P + 255) / 256, 256, 0, st>>>(pixels, P, phi_dev, zf, val, der);
-    double* sums = res + (size_t)S * 6;  // 6 doubles after the per-sample results
-    spot_sums_kernel<<<1, kSumThreads, 0, st>>>(val, der, P, sums);
-    emission_kernel<<<(unsigned)((long long)S * F), kEmitThreads, 0, st>>>(bg, pix, val, der, sums, F, P,
-                                                                           2 * variance, variance, c0, em);
+    const int nblk = (P + kPixThreads - 1) / kPixThreads;
+    double* sums = res + (size_t)S * 6;  // 6 doubles after the per-sample results, then the blocks' partials
+    spot_pixels_kernel<<<nblk, kPixThreads, 0, st>>>(pixels, P, phi_dev, zf, val, der, dfd ? vdf : nullptr,
+                                                     sums + 6);
+    spot_sums_kernel<<<1, 32, 0, st>>>(sums + 6, nblk, sums);
+    if (dfd)
+        emission_df_kernel<<<dim3((unsigned)F, (unsigned)((S + kDfTile - 1) / kDfTile)), kEmitThreads, 0, st>>>(
+            dfd, vdf, sums, S, F, P, 2 * variance, variance, em);
+    else
+        emission_kernel<<<(unsigned)((long long)S * F), kEmitThreads, 0, st>>>(bg, pix, val, der, sums, F, P,
+                                                                               2 * variance, variance, c0, em);
     forward_kernel<<<S, 32, 0, st>>>(em, S, F, A_dev, pi_dev, res);
     return (int)cudaGetLastError();
 }

@@ -47,17 +47,19 @@ struct ThreeBData {
     const double* bg = nullptr;
     const double* pix = nullptr;
     const int* pixels = nullptr;
+    const float2* dfd = nullptr;  // the residuals as double-floats, for gradient-only evaluations
     int S = 0, F = 0, P = 0;
 };
 
 // Scratch for one evaluation, and the data on the device (copied in once when
-// the caller's pointers are host memory).
+// the caller's pointers are host memory). residual_df: also stage the
+// residuals as double-floats for an optimiser's gradient-only evaluations.
 static int threeb_stage(rfba_ctx* ctx, const double* sample_bg, const double* pixel_intensities, const int* pixels,
-                        int S, int F, int P, int ptr_flags, cudaStream_t st, ThreeBData* d) {
+                        int S, int F, int P, int ptr_flags, cudaStream_t st, ThreeBData* d, bool residual_df = false) {
     int s;
     const size_t nbg = (size_t)S * F * P, npix = (size_t)F * P;
     if ((s = ctx->tb_val.ensure((size_t)P * 8, "3B spot table")) || (s = ctx->tb_der.ensure((size_t)P * 40, "3B spot table")) ||
-        (s = ctx->tb_em.ensure((size_t)S * F * 80, "3B emissions")) || (s = ctx->tb_res.ensure((size_t)S * 48 + 48, "3B results")) ||
+        (s = ctx->tb_em.ensure((size_t)S * F * 80, "3B emissions")) || (s = ctx->tb_res.ensure((size_t)S * 48 + 48 + (size_t)(P / 256 + 1) * 48, "3B results")) ||
         (s = ctx->tb_par.ensure(17 * 8, "3B parameters")))
         return s;
     d->bg = sample_bg;
@@ -76,6 +78,14 @@ static int threeb_stage(rfba_ctx* ctx, const double* sample_bg, const double* pi
         d->bg = static_cast<const double*>(ctx->tb_bg.p);
         d->pix = static_cast<const double*>(ctx->tb_pix.p);
         d->pixels = static_cast<const int*>(ctx->tb_pixels.p);
+    }
+    if (residual_df) {
+        if ((s = ctx->tb_dfd.ensure(nbg * 8, "3B residuals")) || (s = ctx->tb_vdf.ensure((size_t)P * 48, "3B spot table")))
+            return s;
+        const int e = launch_threeb_residual(d->bg, d->pix, S, F, P, static_cast<float2*>(ctx->tb_dfd.p), st);
+        if (e) return cuda_fail((cudaError_t)e, "3B residual launch");
+        ++ctx->launches;
+        d->dfd = static_cast<const float2*>(ctx->tb_dfd.p);
     }
     return RFBA_OK;
 }
@@ -96,7 +106,8 @@ static int threeb_eval(rfba_ctx* ctx, const rfba_3b_model* m, const ThreeBData& 
     const double* dpar = static_cast<const double*>(ctx->tb_par.p);
     int e = launch_threeb(d.bg, d.pix, d.pixels, S, F, P, dpar, m->z_factor, m->variance, c0, dpar + 5, dpar + 14,
                           static_cast<double*>(ctx->tb_val.p), static_cast<double*>(ctx->tb_der.p),
-                          static_cast<double*>(ctx->tb_em.p), static_cast<double*>(ctx->tb_res.p), st);
+                          static_cast<double*>(ctx->tb_em.p), static_cast<double*>(ctx->tb_res.p),
+                          log_prob ? nullptr : d.dfd, static_cast<float2*>(ctx->tb_vdf.p), st);
     if (e) return cuda_fail((cudaError_t)e, "3B spot gradient launch");
     ctx->launches += 4;
     std::vector<double> res((size_t)S * 6);
@@ -515,7 +526,7 @@ static int optimise_pass_core(rfba_ctx* ctx, const rfba_3b_model* m, const int* 
         StagedGradient grad{ctx, m, ThreeBData(), st};
         if ((s = threeb_stage(ctx, static_cast<const double*>(ctx->gb_oint.p), static_cast<const double*>(ctx->gb_pix.p),
                               static_cast<const int*>(ctx->gb_pixels.p), main_samples, F, P, RFBA_DEVICE_PTRS, st,
-                              &grad.d)))
+                              &grad.d, true)))
             return s;
         CgOnly5 cg;
         if ((s = cg.start(sp[k].data(), limit, grad))) return s;
@@ -815,7 +826,8 @@ static int modify_core(rfba_ctx* ctx, const rfba_3b_model* m, const int* pixels,
         secs[0] += since(t0);
         StagedGradient grad{ctx, m, ThreeBData(), st};
         if ((s = threeb_stage(ctx, static_cast<const double*>(ctx->gb_oint.p), static_cast<const double*>(ctx->gb_pix.p),
-                              static_cast<const int*>(ctx->gb_pixels.p), S, F, P, RFBA_DEVICE_PTRS, st, &grad.d)))
+                              static_cast<const int*>(ctx->gb_pixels.p), S, F, P, RFBA_DEVICE_PTRS, st, &grad.d,
+                              true)))
             return s;
         CgOnly5 cg;
         if ((s = cg.start(model2[spot].data(), prm.limit, grad))) return s;
@@ -1286,7 +1298,8 @@ int rfba_3b_spot_gradient(rfba_ctx* ctx, const rfba_3b_model* m, const double* s
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if ((s = order_streams(ctx, st))) return s;
     ThreeBData d;
-    if ((s = threeb_stage(ctx, sample_bg, pixel_intensities, pixels, S, F, P, ptr_flags, st, &d))) return s;
+    if ((s = threeb_stage(ctx, sample_bg, pixel_intensities, pixels, S, F, P, ptr_flags, st, &d, !log_prob)))
+        return s;
     return threeb_eval(ctx, m, d, spot, out, log_prob, st);
 }
 
@@ -1308,7 +1321,7 @@ int rfba_3b_optimise_spot(rfba_ctx* ctx, const rfba_3b_model* m, const double* s
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if ((s = order_streams(ctx, st))) return s;
     ThreeBData d;
-    if ((s = threeb_stage(ctx, sample_bg, pixel_intensities, pixels, S, F, P, ptr_flags, st, &d))) return s;
+    if ((s = threeb_stage(ctx, sample_bg, pixel_intensities, pixels, S, F, P, ptr_flags, st, &d, true))) return s;
     auto grad = [&](const double* x, double* g) -> int {
         if (x[0] <= 0 || x[1] <= 0) {  // multispot5.cc:618-619
             for (int n = 0; n < 5; ++n) g[n] = std::numeric_limits<double>::quiet_NaN();

@@ -643,11 +643,13 @@ class Context:
                                                ctypes.c_void_p(din.data_ptr()), dsp, st))
         return din, dshift
 
-    def spot_gradient_3b(self, model: ThreeBModel, sample_bg, pix, pixels, spot, stream=None):
+    def spot_gradient_3b(self, model: ThreeBModel, sample_bg, pix, pixels, spot, stream=None,
+                         want_log_prob: bool = True):
         """SpotNegProbabilityDiffWithSampledBackground (multispot5.cc:616-664) on the
-        GPU: returns (gradient [5], log probability per sample [S]). sample_bg
-        [S][F][P], pix [F][P] (float64) and pixels [P][3] (int32) are numpy arrays
-        (copied in) or CUDA tensors."""
+        GPU: returns (gradient [5], log probability per sample [S] or None).
+        sample_bg [S][F][P], pix [F][P] (float64) and pixels [P][3] (int32) are
+        numpy arrays (copied in) or CUDA tensors. Without the log probabilities
+        the sums run in double-float arithmetic, as the optimisers run them."""
         dev = not isinstance(sample_bg, np.ndarray)
         if dev:
             S, F, P = (int(v) for v in sample_bg.shape)
@@ -660,10 +662,10 @@ class Context:
             ptrs = [ctypes.c_void_p(a.ctypes.data) for a in (sample_bg, pix, pixels)]
         sp = np.ascontiguousarray(spot, np.float64)
         out = np.zeros(5)
-        logp = np.zeros(S)
+        logp = np.zeros(S) if want_log_prob else None
         dp = ctypes.POINTER(ctypes.c_double)
         _check(lib().rfba_3b_spot_gradient(self.h, ctypes.byref(model), *ptrs, S, F, P, sp.ctypes.data_as(dp),
-                                           out.ctypes.data_as(dp), logp.ctypes.data_as(dp),
+                                           out.ctypes.data_as(dp), logp.ctypes.data_as(dp) if want_log_prob else None,
                                            RFBA_DEVICE_PTRS if dev else RFBA_HOST_PTRS, _stream_arg(stream, dev)))
         return out, logp
 
