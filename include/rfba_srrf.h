@@ -403,6 +403,15 @@ typedef struct rfba_3b_fit_params {
     int thermo_samples;          /* add_remove.thermo.samples (1000) */
     double limit[5];             /* cg.max_motion x (brightness limit, 1, 1, 1, 1) */
     double position_extra_radius; /* position.extra_radius (2.3); < 0: position.use_prior = 0 */
+    /* add_guide = 1 (multispot5_headless.cc:177-179): proposed spots are drawn
+     * from this SRRF map as InitGuide / GetPoint draw them (multispot5.cc:
+     * 2164-2231; rfba_srrf_seed_spots' distribution over the pixels' subvoxels):
+     * host memory [z][y][x], guide_dims its x, y, z extents, guide_mag the
+     * magnification, in the pixels' coordinates (the SRRF.raw of the same
+     * image). NULL: a uniform pixel plus a uniform offset. */
+    const float* guide_map;
+    int guide_dims[3];
+    int guide_mag;
 } rfba_3b_fit_params;
 
 /* What one model modification did. */
@@ -429,7 +438,8 @@ typedef struct rfba_3b_modify_record {
  * (rfba_3b_spot_hessian, opt_hess_inner_samples) is decomposed and, unless it
  * is negative definite, the optimiser restarts 0.1 along the eigenvector of its
  * fourth-smallest eigenvalue. A mobile spot outside the allowed area keeps
- * model 1. Otherwise the Hessian is taken again on h_outer_samples draws of the
+ * model 1 (with a guide map the proposal's position is drawn from the map
+ * instead). Otherwise the Hessian is taken again on h_outer_samples draws of the
  * sampler over all pixels (GibbsSampler, sampled_multispot.h:240-330) with
  * h_inner_samples backward samples; when its negation's smallest eigenvalue is
  * above 1e-6, model 2 is kept if its negative free energy (rfba_3b_free_energy,

@@ -1249,6 +1249,19 @@ int rfba_srrf_seed_spots(rfba_ctx* ctx, const float* map, const int map_dims[3],
     cudaStream_t st = static_cast<cudaStream_t>(stream);  // NULL = legacy default stream
     int s;
     if ((s = order_streams(ctx, st))) return s;
+    return seed_spots_locked(ctx, map, map_dims, mag, voxels, nvoxels, num_spots, seed, xyz, ptr_flags, st);
+}
+
+}  // extern "C"
+
+namespace rfba {
+
+// The seeding draw with the context already held and its stream ordered.
+int seed_spots_locked(rfba_ctx* ctx, const float* map, const int map_dims[3], int mag, const int* voxels, int nvoxels,
+                      int num_spots, unsigned long long seed, float* xyz, int ptr_flags, cudaStream_t st) {
+    int s;
+    const long long ncand = (long long)nvoxels * mag * mag * mag;
+    const long long n1 = (ncand + 511) / 512, n2 = (n1 + 511) / 512;
     if ((s = ctx->seed_w.ensure((size_t)ncand * 8, "seeding weights")) ||
         (s = ctx->seed_sums.ensure((size_t)n1 * 8, "seeding scan")) ||
         (s = ctx->seed_carry.ensure((size_t)(n2 + 1) * 8, "seeding scan")) || (s = ctx->errw.ensure(256, "check word")))
@@ -1290,6 +1303,10 @@ int rfba_srrf_seed_spots(rfba_ctx* ctx, const float* map, const int map_dims[3],
     }
     return RFBA_OK;
 }
+
+}  // namespace rfba
+
+extern "C" {
 
 int rfba_combine_render(rfba_ctx* ctx, const double* spots, long long nspots, const int img_dims[3], int zoom,
                         const uint16_t* psf, const int psf_dims[3], int noise_r, int noise_rz, int noise_threshold,

@@ -30,6 +30,9 @@ int cuda_fail(cudaError_t e, const char* what);
 int order_streams(rfba_ctx* ctx, cudaStream_t st);
 // RFBA_VERBOSE=1: per-call schedule and timing lines on stderr.
 bool verbose();
+// rfba_srrf_seed_spots with the context held and `st` ordered.
+int seed_spots_locked(rfba_ctx* ctx, const float* map, const int map_dims[3], int mag, const int* voxels, int nvoxels,
+                      int num_spots, unsigned long long seed, float* xyz, int ptr_flags, cudaStream_t st);
 
 #define RFBA_CUDA(call, what)                          \
     do {                                               \

@@ -795,11 +795,19 @@ static int modify_core(rfba_ctx* ctx, const rfba_3b_model* m, const int* pixels,
     if (add) {
         model1 = sp;
         model2 = sp;
-        const int r = std::min(P - 1, (int)(rng.next() * P));
         Spot n;
         n[0] = log_normal_mode(m->mu_brightness, m->sigma_brightness);
         n[1] = log_normal_mode(m->mu_blur, m->sigma_blur);
-        for (int a = 0; a < 3; ++a) n[2 + a] = pixels[3 * r + a] + rng.next() - .5;
+        if (prm.guide_map) {  // GetPoint (multispot5.cc:2210-2231): a subvoxel drawn by the SRRF map
+            float xyz[3];
+            if ((s = seed_spots_locked(ctx, prm.guide_map, prm.guide_dims, prm.guide_mag, pixels, P, 1,
+                                       mix_seed(seed, 7, 0), xyz, RFBA_HOST_PTRS, st)))
+                return s;
+            for (int a = 0; a < 3; ++a) n[2 + a] = xyz[a];
+        } else {
+            const int r = std::min(P - 1, (int)(rng.next() * P));
+            for (int a = 0; a < 3; ++a) n[2 + a] = pixels[3 * r + a] + rng.next() - .5;
+        }
         model2.push_back(n);
         original = 1;
     } else {
@@ -938,6 +946,11 @@ static int fit_check(rfba_ctx* ctx, const rfba_3b_model* m, const double* pix, c
         prm->opt_hess_inner_samples < 1 || prm->h_outer_samples < 1 || prm->h_inner_samples < 1 ||
         prm->thermo_samples < 1) {
         set_error("fit settings: sample counts and attempts must be >= 1, passes / tries / iterations >= 0");
+        return RFBA_ERR_INVALID;
+    }
+    if (prm->guide_map && (prm->guide_mag < 1 || prm->guide_dims[0] < 1 || prm->guide_dims[1] < 1 ||
+                           prm->guide_dims[2] < 1)) {
+        set_error("guide map: magnification and dims must be >= 1");
         return RFBA_ERR_INVALID;
     }
     return RFBA_OK;

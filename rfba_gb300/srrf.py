@@ -115,10 +115,13 @@ class ThreeBFitParams(ctypes.Structure):
                 ("add_remove_tries", ctypes.c_int), ("opt_samples", ctypes.c_int), ("opt_attempts", ctypes.c_int),
                 ("opt_hess_inner_samples", ctypes.c_int), ("h_outer_samples", ctypes.c_int),
                 ("h_inner_samples", ctypes.c_int), ("thermo_samples", ctypes.c_int),
-                ("limit", ctypes.c_double * 5), ("position_extra_radius", ctypes.c_double)]
+                ("limit", ctypes.c_double * 5), ("position_extra_radius", ctypes.c_double),
+                ("guide_map", ctypes.c_void_p), ("guide_dims", ctypes.c_int * 3), ("guide_mag", ctypes.c_int)]
 
     @classmethod
-    def make(cls, limit, **kw) -> "ThreeBFitParams":
+    def make(cls, limit, guide=None, guide_mag: int = 1, **kw) -> "ThreeBFitParams":
+        """guide: the SRRF map [z][y][x] proposed spots are drawn from
+        (add_guide = 1), in the pixels' coordinates magnified by guide_mag."""
         p = cls()
         d = dict(main_passes=4, main_samples=10, main_cg_max_iterations=5, sweeps=1, add_remove_tries=10,
                  opt_samples=20, opt_attempts=10, opt_hess_inner_samples=1000, h_outer_samples=100,
@@ -127,6 +130,12 @@ class ThreeBFitParams(ctypes.Structure):
         for k, v in d.items():
             setattr(p, k, v)
         p.limit[:] = [float(v) for v in np.asarray(limit, np.float64).reshape(5)]
+        if guide is not None:
+            g = np.ascontiguousarray(guide, np.float32)
+            p._guide = g  # kept alive with the settings
+            p.guide_map = g.ctypes.data
+            p.guide_dims[:] = [g.shape[2], g.shape[1], g.shape[0]]
+            p.guide_mag = int(guide_mag)
         return p
 
 

@@ -76,6 +76,23 @@ def test_empty_model_gains_the_spot(ctx):
     assert kept >= 1
 
 
+def test_srrf_guided_proposals_land_on_the_spot(ctx):
+    """add_guide = 1: a proposal's position is drawn from the SRRF map (GetPoint),
+    so with the map peaked at the spot every proposal converges onto it and
+    is kept, where uniform placement mostly missed it."""
+    pix, pixels, c = one_spot_block(1)
+    mag, n = 2, 9
+    zz, yy, xx = np.meshgrid(np.arange(n * mag), np.arange(n * mag), np.arange(n * mag), indexing="ij")
+    pos = np.stack([xx, yy, zz], -1) / mag
+    guide = np.exp(-((pos - c) ** 2).sum(-1) / (2 * 0.4 ** 2)).astype(np.float32)
+    for seed in range(4):
+        got, rec = ctx.modify_model_3b(_model(), pix, pixels, np.zeros((0, 5)), _params(guide=guide, guide_mag=mag),
+                                       seed=seed)
+        print(f"[3B modify] guided, seed {seed}: kept {rec['kept']}, spot {np.round(rec['spot'], 2)}")
+        assert rec["added"] == 1 and rec["kept"] == 2
+        assert np.linalg.norm(got[0, 2:] - c) < 0.1
+
+
 def test_extra_spot_on_an_explained_spot_is_rejected(ctx):
     """With the data's spot already in the model every proposal is an addition
     (one spot); one that converges (a negative definite Hessian) finds nothing
