@@ -387,6 +387,22 @@ int rfba_3b_spot_hessian(rfba_ctx* ctx, const rfba_3b_model* model, const double
                          const double spot[5], int bs_iterations, unsigned long long seed, double hess[25],
                          int ptr_flags, void* stream);
 
+/* FreeEnergyHessian::hessian (RFBA Main/multispot5.cc:693-775), the "pure
+ * MCMC" Hessian of the negative free energy with respect to spot `spot`: the
+ * unmasked Gibbs sampler (GibbsSampler, sampled_multispot.h:240-330) draws
+ * `samples` times (`sweeps` sweeps each) with every spot of spots [K][5] in
+ * the model; per draw, over the frames where the spot is on, h = sum_p e H_p
+ * - g_p g_p^T and d = sum_p e g_p with e the residual of the draw (which
+ * holds the spot), plus the log-normal priors' derivatives; the result is
+ * (sum h + sum d d^T) / (samples variance) less the outer product of
+ * sum d / (samples variance), as the reference forms it. The reference's
+ * modification step has this call commented out (multispot5.cc:2042-2043) in
+ * favour of rfba_3b_spot_hessian; it is here for callers of the class.
+ * Host memory; hess[25] row-major. Philox draws keyed by seed. Synchronous. */
+int rfba_3b_free_energy_hessian(rfba_ctx* ctx, const rfba_3b_model* model, const double* pixel_intensities,
+                                const int* pixels, const double* spots, int K, int F, int P, int spot, int samples,
+                                int sweeps, unsigned long long seed, double hess[25]);
+
 /* Settings of a 3B block fit (FitSpots, RFBA Main/multispot5.cc:1329-1505), the
  * reference's variable names and multispot5.cfg values in brackets. */
 typedef struct rfba_3b_fit_params {

@@ -17,6 +17,8 @@ order where that decides the bits:
   (multispot5.cc:335-405) given each draw's sum of squared residuals;
 - `spot_hessian_table`: spot_shape_hess_position (storm.h:87-146), value,
   gradient and Hessian of a spot at every pixel;
+- `free_energy_hessian_draws`: FreeEnergyHessian::hessian (multispot5.cc:
+  693-775) given the sampler's draws;
 - `hessian_expectation`: what sampled_background_spot_hessian_ffbs
   (multispot5.cc:824-985) converges to as its backward samples grow: the
   per-frame parts over all pixels, the posterior of the spot's chain per
@@ -230,6 +232,34 @@ def spot_hessian_table(pixels, spot, z_factor):
     return val, g, H
 
 
+def free_energy_hessian_draws(pix, pixels, spots, spot, states, ints, variance, z_factor, mu_b, sigma_b, mu_blur,
+                              sigma_blur):
+    """FreeEnergyHessian::hessian given the draws: states [S][K][F], draw
+    intensities [S][F][P] (holding every spot)."""
+    pix = np.asarray(pix, np.float64)
+    S = len(states)
+    sp = np.asarray(spots, np.float64).reshape(-1, 5)[spot]
+    _, g, H = spot_hessian_table(pixels, sp, z_factor)
+    gg = np.einsum("pa,pb->ab", g, g)
+    sum1, sum2, sumd = np.zeros((5, 5)), np.zeros((5, 5)), np.zeros(5)
+    for i in range(S):
+        on = np.asarray(states[i][spot]) == 0
+        e = (pix - ints[i])[on]  # [frames on][P]
+        h = np.einsum("fp,pab->ab", e, H) - on.sum() * gg
+        d = (e @ g).sum(0)
+        h[0, 0] += (1 + (_ln(sp[0]) - mu_b - 1) / (sigma_b * sigma_b)) / (sp[0] * sp[0])
+        h[1, 1] += (1 + (_ln(sp[1]) - mu_blur - 1) / (sigma_blur * sigma_blur)) / (sp[1] * sp[1])
+        d[0] += -(1 + (_ln(sp[0]) - mu_b) / (sigma_b * sigma_b)) / sp[0]
+        d[1] += -(1 + (_ln(sp[1]) - mu_blur) / (sigma_blur * sigma_blur)) / sp[1]
+        sum1 += h
+        sum2 += np.outer(d, d)
+        sumd += d
+    sum1 /= S * variance
+    sum2 /= S * variance
+    sumd /= S * variance
+    return sum1 + sum2 - np.outer(sumd, sumd)
+
+
 def _posterior_chain(lp_on, lp_off, A, pi):
     """Single marginals m [F][3] and the reverse-time transitions R [F][3][3]
     (R[t][j][i] = P(s_t = i | s_{t+1} = j)) of the chain's posterior."""
@@ -314,6 +344,7 @@ def ref():
         L.ref_free_energy.argtypes = [dp, ip, dp, ip, ip, i, i, i, dp, dp, d, d, d, d, d, d, i, i, i, dp]
         L.ref_free_energy.restype = d
         L.ref_spot_hessian.argtypes = [dp, dp, ip, i, i, i, dp, dp, dp, d, d, d, d, d, d, i, i, dp]
+        L.ref_free_energy_hessian_draws.argtypes = [dp, ip, dp, i, i, i, i, i, bp, dp, d, d, d, d, d, d, dp]
         _ref = L
     return _ref
 
@@ -396,6 +427,22 @@ def ref_spot_hessian(bg, pix, pixels, spot, A, pi, variance, z_factor, mu_b, sig
     ref().ref_spot_hessian(_p(bg, ctypes.c_double), _p(pix, ctypes.c_double), _p(px, ctypes.c_int), S, F, P,
                            _p(sp, ctypes.c_double), _p(A, ctypes.c_double), _p(pi, ctypes.c_double), variance, z_factor,
                            mu_b, sigma_b, mu_blur, sigma_blur, bs_iterations, seed, _p(out, ctypes.c_double))
+    return out
+
+
+def ref_free_energy_hessian_draws(pix, pixels, spots, spot, states, ints, variance, z_factor, mu_b, sigma_b, mu_blur,
+                                  sigma_blur):
+    pix = np.ascontiguousarray(pix, np.float64)
+    F, P = pix.shape
+    px = np.ascontiguousarray(pixels, np.int32)
+    sp = np.ascontiguousarray(spots, np.float64).reshape(-1, 5)
+    st = np.ascontiguousarray(states, np.uint8)
+    ints = np.ascontiguousarray(ints, np.float64)
+    out = np.empty((5, 5))
+    ref().ref_free_energy_hessian_draws(_p(pix, ctypes.c_double), _p(px, ctypes.c_int), _p(sp, ctypes.c_double),
+                                        len(sp), F, P, spot, len(st), _p(st, ctypes.c_ubyte), _p(ints, ctypes.c_double),
+                                        variance, z_factor, mu_b, sigma_b, mu_blur, sigma_blur,
+                                        _p(out, ctypes.c_double))
     return out
 
 

@@ -218,6 +218,54 @@ int ref_spot_hessian(const double* bg, const double* pix, const int* pixels, int
     return 0;
 }
 
+// FreeEnergyHessian::hessian (multispot5.cc:693-775) given the sampler's
+// draws (states [S][K][F], intensities [S][F][P], which hold every spot): the
+// loop after sampler.next written out around the reference's
+// compute_spot_intensity_hessian and log-normal prior derivatives. hess [25];
+// entry [4][3] is indeterminate as in ref_spot_hessian.
+int ref_free_energy_hessian_draws(const double* pix, const int* pixels, const double* spots_in, int K, int F, int P,
+                                  int spot, int samples, const unsigned char* states, const double* ints,
+                                  double variance, double zFactor, double mu_brightness, double sigma_brightness,
+                                  double mu_blur, double sigma_blur, double* hess) {
+    const vector<vector<double> > pixel_intensities = frames_of(pix, F, P);
+    const vector<Ref3D> px = refs_of(pixels, P);
+    const double* sp = spots_in + 5 * (size_t)spot;
+    const Vector<5> s5 = makeVector(sp[0], sp[1], sp[2], sp[3], sp[4]);
+    const vector<tuple<double, Vector<5>, Matrix<5> > > spot_hess_etc =
+        SampledMultispot::compute_spot_intensity_hessian(px, s5, zFactor);
+    Matrix<5> sum_hess1 = Zeros;
+    Matrix<5> sum_hess2 = Zeros;
+    Vector<5> sum_deriv = Zeros;
+    for (int sample = 0; sample < samples; sample++) {
+        const double* si = ints + (size_t)sample * F * P;
+        Matrix<5> h = Zeros;
+        Vector<5> deriv = Zeros;
+        for (int frame = 0; frame < F; frame++)
+            for (int pixel = 0; pixel < P; pixel++) {
+                double e = pixel_intensities[frame][pixel] - si[(size_t)frame * P + pixel];
+                if (states[((size_t)sample * K + spot) * F + frame] == 0) {
+                    h += e * get<2>(spot_hess_etc[pixel]) -
+                         get<1>(spot_hess_etc[pixel]).as_col() * get<1>(spot_hess_etc[pixel]).as_row();
+                    deriv += e * get<1>(spot_hess_etc[pixel]);
+                }
+            }
+        h[0][0] += hess_log_log_normal(s5[0], mu_brightness, sigma_brightness);
+        h[1][1] += hess_log_log_normal(s5[1], mu_blur, sigma_blur);
+        sum_hess1 += h;
+        deriv[0] += diff_log_log_normal(s5[0], mu_brightness, sigma_brightness);
+        deriv[1] += diff_log_log_normal(s5[1], mu_blur, sigma_blur);
+        sum_hess2 += deriv.as_col() * deriv.as_row();
+        sum_deriv = sum_deriv + deriv;
+    }
+    sum_hess1 /= (samples * variance);
+    sum_hess2 /= (samples * variance);
+    sum_deriv /= (samples * variance);
+    const Matrix<5> out = sum_hess1 + sum_hess2 - sum_deriv.as_col() * sum_deriv.as_row();
+    for (int r = 0; r < 5; ++r)
+        for (int c = 0; c < 5; ++c) hess[r * 5 + c] = out[r][c];
+    return 0;
+}
+
 // NegativeFreeEnergy::compute_with_mask (multispot5.cc:335-405), its steps in
 // order, on the reference's GibbsSampler2 and MT19937 (simple_seed(seed)).
 // residuals [samples] receives each draw's -err_sum (may be NULL).

@@ -15,6 +15,10 @@
 // product of the mean derivative and adds the log-normal priors' second
 // derivatives.
 //
+// FreeEnergyHessian::hessian (multispot5.cc:693-775), the "pure MCMC"
+// Hessian, uses the first three kernels on draws that hold every spot
+// (e = data - sample) and finishes on the host from the drawn states.
+//
 // Kernels:
 //   hess_table_kernel   one thread per pixel: value, gradient (5) and the 15
 //                       upper entries of the spot's Hessian at the pixel
@@ -87,10 +91,13 @@ __global__ void hess_table_kernel(const int* __restrict__ pixels, int P, const d
 }
 
 // part[c][q][22], q = f * S + i: the chunk's sums for frame f of sample i
+// spot_scale 1: the samples lack the spot (e = d - (s + v)); 0: they hold it
+// already (e = d - s, FreeEnergyHessian).
 __global__ void __launch_bounds__(kPartThreads) hess_parts_kernel(const double* __restrict__ bg,
                                                                    const double* __restrict__ pix,
                                                                    const double* __restrict__ tab, int S, int F, int P,
-                                                                   int chunk, double* __restrict__ part) {
+                                                                   int chunk, double spot_scale,
+                                                                   double* __restrict__ part) {
     const long long q = (long long)blockIdx.x * kPartThreads + threadIdx.x;
     const long long nq = (long long)S * F;
     if (q >= nq) return;
@@ -104,7 +111,7 @@ __global__ void __launch_bounds__(kPartThreads) hess_parts_kernel(const double* 
     for (int p = p0; p < p1; ++p) {
         const double* t = tab + (size_t)p * kTab;
         const double dv = __ldg(d + p), sv = __ldg(b + p);
-        const double e = dv - (sv + __ldg(t));
+        const double e = dv - (sv + spot_scale * __ldg(t));
         on += e * e;
         const double o = dv - sv;
         off += o * o;
@@ -266,7 +273,7 @@ int hessian_chunks(long long S, long long F, int P, int sm_count) {
 
 size_t hessian_ffbs_smem(int F) { return ffbs_smem(F); }
 
-int launch_spot_hessian(const HessParams& h, void* stream) {
+int launch_hessian_parts(const HessParams& h, bool samples_hold_spot, void* stream) {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     hess_table_kernel<<<(h.P + 127) / 128, 128, 0, st>>>(h.pixels, h.P, h.phi, h.zf, h.tab);
     cudaError_t e = cudaGetLastError();
@@ -274,10 +281,16 @@ int launch_spot_hessian(const HessParams& h, void* stream) {
     const int chunk = (h.P + h.nc - 1) / h.nc;
     const long long nq = (long long)h.S * h.F;
     hess_parts_kernel<<<dim3((unsigned)((nq + kPartThreads - 1) / kPartThreads), (unsigned)h.nc), kPartThreads, 0, st>>>(
-        h.bg, h.pix, h.tab, h.S, h.F, h.P, chunk, h.part);
+        h.bg, h.pix, h.tab, h.S, h.F, h.P, chunk, samples_hold_spot ? 0.0 : 1.0, h.part);
     if ((e = cudaGetLastError()) != cudaSuccess) return (int)e;
     hess_gg_kernel<<<1, kFfbsThreads, 0, st>>>(h.tab, h.P, h.gg);
-    if ((e = cudaGetLastError()) != cudaSuccess) return (int)e;
+    return (int)cudaGetLastError();
+}
+
+int launch_spot_hessian(const HessParams& h, void* stream) {
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = (cudaError_t)launch_hessian_parts(h, false, stream);
+    if (e != cudaSuccess) return (int)e;
     FfbsArgs a;
     a.part = h.part;
     a.gg = h.gg;

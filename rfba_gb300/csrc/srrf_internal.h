@@ -245,6 +245,9 @@ struct HessParams {
 int hessian_chunks(long long S, long long F, int P, int sm_count);
 size_t hessian_ffbs_smem(int F);
 int launch_spot_hessian(const HessParams& h, void* stream);
+// The table, the per-(frame, sample) parts and sum g g^T only (part, gg);
+// samples_hold_spot: the draws include the spot (e = data - sample).
+int launch_hessian_parts(const HessParams& h, bool samples_hold_spot, void* stream);
 
 // 3B spot gradient (threeb.cu): spot voxel table, emission sums per (sample,
 // frame), forward algorithm per sample; res[s] = (gradient[5], log probability).

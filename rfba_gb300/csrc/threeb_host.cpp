@@ -690,6 +690,110 @@ static int spot_hessian_dev(rfba_ctx* ctx, const rfba_3b_model* m, const double*
     return RFBA_OK;
 }
 
+// diff_log_log_normal (storm.h:431-434)
+static double diff_log_log_normal(double x, double mu, double sigma) {
+    return -(1 + (ref_ln(x) - mu) / (sigma * sigma)) / x;
+}
+
+// FreeEnergyHessian::hessian (multispot5.cc:693-775) on the staged block: the
+// unmasked sampler (GibbsSampler) draws `samples` times with every spot in
+// the model; per draw, over the frames where spot `which` is on, the spot's
+// hess + its priors' second derivatives and deriv + its priors' first
+// derivatives; the sums of hess and of deriv deriv^T over the draws, over
+// (samples variance), less the outer product of the mean deriv.
+static int free_energy_hessian_dev(rfba_ctx* ctx, const rfba_3b_model* m, int F, int P, const std::vector<Spot>& sp,
+                                   int which, int samples, int sweeps, unsigned long long seed, double hess[25],
+                                   cudaStream_t st) {
+    int s;
+    const int K = (int)sp.size();
+    std::vector<int> hoff((size_t)K + 1), hidx((size_t)K * P);
+    for (int k = 0; k < K; ++k) {
+        hoff[k] = k * P;
+        for (int q = 0; q < P; ++q) hidx[(size_t)k * P + q] = q;
+    }
+    hoff[K] = K * P;
+    if ((s = upload_spots(ctx, sp, st))) return s;
+    GibbsCall c;
+    c.K = K;
+    c.F = F;
+    c.P = P;
+    c.sweeps = sweeps;
+    c.n_draws = samples;
+    c.seed = seed;
+    c.want_state = true;
+    c.want_int = true;
+    if ((s = gibbs_run(ctx, m, static_cast<const double*>(ctx->gb_pix.p), static_cast<const int*>(ctx->gb_pixels.p),
+                       static_cast<const double*>(ctx->gb_spots.p), hoff, hidx, c, RFBA_DEVICE_PTRS, st)))
+        return s;
+    const int nc = hessian_chunks(samples, F, P, ctx->sm_count);
+    const size_t nq = (size_t)samples * F;
+    if ((s = ctx->hs_tab.ensure((size_t)P * 21 * 8, "3B Hessian table")) ||
+        (s = ctx->hs_part.ensure((size_t)nc * nq * 22 * 8, "3B Hessian parts")) ||
+        (s = ctx->hs_gg.ensure(15 * 8, "3B Hessian outer products")) || (s = ctx->hs_phi.ensure(5 * 8, "3B Hessian spot")))
+        return s;
+    RFBA_CUDA(cudaMemcpyAsync(ctx->hs_phi.p, sp[which].data(), 40, cudaMemcpyHostToDevice, st), "spot upload");
+    HessParams h;
+    std::memset(&h, 0, sizeof h);
+    h.bg = static_cast<const double*>(ctx->gb_oint.p);
+    h.pix = static_cast<const double*>(ctx->gb_pix.p);
+    h.pixels = static_cast<const int*>(ctx->gb_pixels.p);
+    h.phi = static_cast<const double*>(ctx->hs_phi.p);
+    h.zf = m->z_factor;
+    h.S = samples;
+    h.F = F;
+    h.P = P;
+    h.nc = nc;
+    h.tab = static_cast<double*>(ctx->hs_tab.p);
+    h.part = static_cast<double*>(ctx->hs_part.p);
+    h.gg = static_cast<double*>(ctx->hs_gg.p);
+    const int e = launch_hessian_parts(h, true, st);
+    if (e) return cuda_fail((cudaError_t)e, "3B free-energy Hessian launch");
+    ctx->launches += 3;
+    std::vector<double> part((size_t)nc * nq * 22), gg(15);
+    std::vector<unsigned char> states((size_t)samples * K * F);
+    RFBA_CUDA(cudaMemcpyAsync(part.data(), ctx->hs_part.p, part.size() * 8, cudaMemcpyDeviceToHost, st), "parts read");
+    RFBA_CUDA(cudaMemcpyAsync(gg.data(), ctx->hs_gg.p, 15 * 8, cudaMemcpyDeviceToHost, st), "parts read");
+    RFBA_CUDA(cudaMemcpyAsync(states.data(), ctx->gb_ostate.p, states.size(), cudaMemcpyDeviceToHost, st),
+              "states read");
+    RFBA_CUDA(cudaStreamSynchronize(st), "synchronize");
+    const Spot& sw = sp[which];
+    double sum1[25] = {0}, sum2[25] = {0}, sumd[5] = {0};
+    for (int i = 0; i < samples; ++i) {
+        double H[25] = {0}, d[5] = {0};
+        for (int f = 0; f < F; ++f) {
+            if (states[((size_t)i * K + which) * F + f] != 0) continue;
+            const size_t q = (size_t)f * samples + i;
+            double v[22] = {0};
+            for (int ch = 0; ch < nc; ++ch)
+                for (int n = 0; n < 22; ++n) v[n] += part[((size_t)ch * nq + q) * 22 + n];
+            for (int r = 0, n = 0; r < 5; ++r)
+                for (int cc = r; cc < 5; ++cc, ++n) {
+                    const double x = v[2 + n] - gg[n];
+                    H[r * 5 + cc] += x;
+                    if (cc != r) H[cc * 5 + r] += x;
+                }
+            for (int r = 0; r < 5; ++r) d[r] += v[17 + r];
+        }
+        H[0] += hess_log_log_normal(sw[0], m->mu_brightness, m->sigma_brightness);
+        H[6] += hess_log_log_normal(sw[1], m->mu_blur, m->sigma_blur);
+        d[0] += diff_log_log_normal(sw[0], m->mu_brightness, m->sigma_brightness);
+        d[1] += diff_log_log_normal(sw[1], m->mu_blur, m->sigma_blur);
+        for (int n = 0; n < 25; ++n) sum1[n] += H[n];
+        for (int r = 0; r < 5; ++r)
+            for (int cc = 0; cc < 5; ++cc) sum2[r * 5 + cc] += d[r] * d[cc];
+        for (int r = 0; r < 5; ++r) sumd[r] += d[r];
+    }
+    const double norm = (double)samples * m->variance;
+    for (int n = 0; n < 25; ++n) {
+        sum1[n] /= norm;
+        sum2[n] /= norm;
+    }
+    for (int r = 0; r < 5; ++r) sumd[r] /= norm;
+    for (int r = 0; r < 5; ++r)
+        for (int cc = 0; cc < 5; ++cc) hess[r * 5 + cc] = sum1[r * 5 + cc] + sum2[r * 5 + cc] - sumd[r] * sumd[cc];
+    return RFBA_OK;
+}
+
 // Eigen-decomposition of a symmetric 5x5 matrix by cyclic Jacobi rotations
 // (Jacobi 1846; Golub and Van Loan, Matrix Computations, sec. 8.5): eigenvalues
 // ascending, eigenvectors as rows, each with its largest-magnitude component
@@ -1278,6 +1382,31 @@ int rfba_3b_fit(rfba_ctx* ctx, const rfba_3b_model* m, const double* pixel_inten
         for (int n = 0; n < 5; ++n) spots[5 * k + n] = sp[k][n];
     *nspots = (int)sp.size();
     return RFBA_OK;
+}
+
+// FreeEnergyHessian::hessian (multispot5.cc:693-775)
+int rfba_3b_free_energy_hessian(rfba_ctx* ctx, const rfba_3b_model* m, const double* pixel_intensities,
+                                const int* pixels, const double* spots, int K, int F, int P, int spot, int samples,
+                                int sweeps, unsigned long long seed, double hess[25]) {
+    int s;
+    if (!pixel_intensities || !pixels || !spots || !hess) {
+        set_error("null argument");
+        return RFBA_ERR_INVALID;
+    }
+    if ((s = gibbs_check(ctx, m, K, F, P, RFBA_HOST_PTRS))) return s;
+    if (K < 1 || spot < 0 || spot >= K || samples < 1 || sweeps < 1) {
+        set_error("spot outside [0, K), or samples / sweeps < 1");
+        return RFBA_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = ctx->stream;
+    if ((s = order_streams(ctx, st))) return s;
+    std::vector<Spot> sp((size_t)K);
+    for (int k = 0; k < K; ++k)
+        for (int n = 0; n < 5; ++n) sp[k][n] = spots[5 * k + n];
+    if ((s = stage_block(ctx, pixel_intensities, pixels, F, P, st))) return s;
+    return free_energy_hessian_dev(ctx, m, F, P, sp, spot, samples, sweeps, seed, hess, st);
 }
 
 int rfba_sym_eigen5(const double a[25], double evals[5], double evecs[25]) {

@@ -247,6 +247,9 @@ def lib():
         L.rfba_3b_fit.argtypes = [vp, ctypes.POINTER(ThreeBModel), vp, vp, ctypes.c_int, ctypes.c_int, vp, ipp,
                                   ctypes.c_int, ctypes.POINTER(ThreeBFitParams), ctypes.c_int, ctypes.c_int, ull,
                                   FIT_FN, vp]
+        L.rfba_3b_free_energy_hessian.argtypes = [vp, ctypes.POINTER(ThreeBModel), vp, vp, vp, ctypes.c_int,
+                                                  ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                  ull, dp]
         L.rfba_sym_eigen5.argtypes = [dp, dp, dp]
         L.rfba_det5.argtypes = [dp]
         L.rfba_det5.restype = ctypes.c_double
@@ -812,6 +815,22 @@ class Context:
         _check(lib().rfba_3b_spot_hessian(self.h, ctypes.byref(model), *ptrs, S, F, P, sp.ctypes.data_as(dp),
                                           int(bs_iterations), seed, out.ctypes.data_as(dp),
                                           RFBA_DEVICE_PTRS if dev else RFBA_HOST_PTRS, _stream_arg(stream, dev)))
+        return out
+
+    def free_energy_hessian_3b(self, model: ThreeBModel, pix, pixels, spots, spot: int, samples: int = 100,
+                               sweeps: int = 1, seed: int = 0):
+        """FreeEnergyHessian::hessian (multispot5.cc:693-775): the 5x5 Hessian of
+        the negative free energy with respect to spots[spot]."""
+        pix = np.ascontiguousarray(pix, np.float64)
+        pixels = np.ascontiguousarray(pixels, np.int32)
+        sp = np.ascontiguousarray(spots, np.float64).reshape(-1, 5)
+        F, P = pix.shape
+        out = np.zeros((5, 5))
+        vp = ctypes.c_void_p
+        _check(lib().rfba_3b_free_energy_hessian(self.h, ctypes.byref(model), vp(pix.ctypes.data),
+                                                 vp(pixels.ctypes.data), vp(sp.ctypes.data), len(sp), F, P, spot,
+                                                 samples, sweeps, seed,
+                                                 out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
         return out
 
     def modify_model_3b(self, model: ThreeBModel, pix, pixels, spots, params: ThreeBFitParams, seed: int = 0):

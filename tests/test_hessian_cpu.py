@@ -103,3 +103,21 @@ def test_fit_entry_points_check_arguments():
     assert L.rfba_3b_spot_hessian(None, ctypes.byref(m), vp(pix.ctypes.data), vp(pix.ctypes.data),
                                   vp(pixels.ctypes.data), 1, 4, 8, sp.ctypes.data_as(dp), 10, 0,
                                   hess.ctypes.data_as(dp), srrf.RFBA_HOST_PTRS, None) == -1
+
+
+def test_free_energy_hessian_oracle_matches_reference():
+    """FreeEnergyHessian::hessian given the reference sampler's own draws
+    (GibbsSampler2 with every pixel in every mask is the unmasked GibbsSampler):
+    the oracle's restatement against the reference's loop compiled here."""
+    G = _ref()
+    from rfba_gb300 import synth
+    pix, pixels, spots = synth.threeb_spots_block(8, 20, (9, 9, 9), 3)
+    si = G.spot_intensity(pixels, spots, 1.0)
+    P, K = len(pixels), len(spots)
+    moff = np.arange(K + 1, dtype=np.int32) * P
+    midx = np.tile(np.arange(P, dtype=np.int32), K)
+    st, ints = G.ref_run(pix, si, moff, midx, A_MAIN, PI_MAIN, 1.0, 1, 6, 5, want_int=True)
+    for spot in range(K):
+        want = G.ref_free_energy_hessian_draws(pix, pixels, spots, spot, st, ints, **MODEL)
+        got = G.free_energy_hessian_draws(pix, pixels, spots, spot, st, ints, **MODEL)
+        assert np.max(np.abs(got[IU] - want[IU])) <= 1e-12 * np.abs(want[IU]).max()

@@ -73,3 +73,22 @@ def test_argument_checks(ctx):
     big = np.zeros((1, 2049, 8))
     with pytest.raises(srrf.RfbaError):
         ctx.spot_hessian_3b(m, big, np.zeros((2049, 8)), pixels[:8], spot, bs_iterations=1)
+
+
+def test_free_energy_hessian_replays_its_draws(ctx):
+    """rfba_3b_free_energy_hessian against the oracle given the same draws: the
+    unmasked sampler is rfba_3b_gibbs_sample with every pixel in every mask and
+    the same seed, so the GPU's draws are replayed exactly."""
+    from oracle import gibbs_oracle as G
+    from rfba_gb300 import synth
+    pix, pixels, spots = synth.threeb_spots_block(8, 20, (9, 9, 9), 3)
+    m = _model(A_MAIN, PI_MAIN)
+    P, K = len(pixels), len(spots)
+    masks = (np.arange(K + 1, dtype=np.int32) * P, np.tile(np.arange(P, dtype=np.int32), K))
+    st, ints = ctx.gibbs_sample_3b(m, pix, pixels, spots, masks, sweeps=1, n_draws=12, seed=21)
+    for spot in range(K):
+        got = ctx.free_energy_hessian_3b(m, pix, pixels, spots, spot, samples=12, seed=21)
+        want = G.free_energy_hessian_draws(pix, pixels, spots, spot, st, ints, **MODEL)
+        err = np.max(np.abs(got - want)) / np.abs(want).max()
+        print(f"[3B free-energy Hessian] spot {spot}: rel L-inf {err:.1e}, on in {(st[:, spot] == 0).sum()} frames")
+        assert err <= 1e-10
