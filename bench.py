@@ -404,9 +404,12 @@ THREEB_BLOCK = dict(seed=91, F=100, shape=(29, 29, 29), K=20)
 
 
 def _gibbs_block():
+    """The 3B block of the sampler / fit timings: 20 blinking spots in a 29^3
+    block over 100 frames, normalised as 3B's preprocessing leaves data (no
+    background, unit noise)."""
     from rfba_gb300 import synth
     b = THREEB_BLOCK
-    return synth.threeb_spots_block(b["seed"], b["F"], b["shape"], b["K"])
+    return synth.threeb_spots_block(b["seed"], b["F"], b["shape"], b["K"], background=0.0)
 
 
 def _threeb_model():

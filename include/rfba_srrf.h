@@ -342,6 +342,17 @@ int rfba_3b_free_energy(rfba_ctx* ctx, const rfba_3b_model* model, const double*
                         int samples, int sweeps, unsigned long long seed, double* value, double* residuals,
                         int ptr_flags, void* stream);
 
+/* rfba_3b_free_energy for nmodels (1 or 2) models of one block side by side,
+ * their Gibbs chains in one launch (a model comparison, which the reference
+ * runs on two threads, multispot5.cc:2096-2108): model i has K[i] spots
+ * spots[i] [K[i]][5] with masks mask_offsets[i] / mask_pixels[i] and its own
+ * seed; values[i] is what compute_with_mask returns. Each model's value equals
+ * rfba_3b_free_energy's with the same seed. Host memory. Synchronous. */
+int rfba_3b_free_energy_models(rfba_ctx* ctx, const rfba_3b_model* model, const double* pixel_intensities,
+                               const int* pixels, int F, int P, int nmodels, const double* const* spots, const int* K,
+                               const int* const* mask_offsets, const int* const* mask_pixels, int samples, int sweeps,
+                               const unsigned long long* seeds, double* values);
+
 /* One pass of FitSpots::optimize_each_spot_in_turn_for_several_passes (RFBA
  * Main/multispot5.cc:1511-1690), the main loop of a 3B block fit, on the GPU:
  * the spots (spots [*nspots][5], host, updated in place) are ordered by

@@ -1197,11 +1197,10 @@ int rfba_ctx_destroy(rfba_ctx* c) {
                       &c->shifted, &c->tmp1, &c->tmp2, &c->gS, &c->gI, &c->gin, &c->dshift, &c->ablocks, &c->atiles,
                       &c->acounter, &c->errw, &c->tb_val, &c->tb_der, &c->tb_em, &c->tb_res, &c->tb_par, &c->tb_bg,
                       &c->tb_pix, &c->tb_pixels, &c->tb_dfd, &c->tb_vdf, &c->seed_w, &c->seed_sums, &c->seed_carry, &c->seed_map, &c->seed_vox,
-                      &c->seed_xyz, &c->gb_pix, &c->gb_pixels, &c->gb_spots, &c->gb_si, &c->gb_moff, &c->gb_midx,
-                      &c->gb_state, &c->gb_cur, &c->gb_em, &c->gb_bar, &c->gb_var, &c->gb_ostate, &c->gb_oint,
-                      &c->gb_oerr, &c->gb_lp, &c->gb_filt, &c->hs_tab, &c->hs_part, &c->hs_gg, &c->hs_phi,
+                      &c->seed_xyz, &c->gb_pix, &c->gb_pixels, &c->gb_par, &c->hs_tab, &c->hs_part, &c->hs_gg, &c->hs_phi,
                       &c->hs_frame, &c->hs_out})
         b->release();
+    for (auto& g : c->gb) g.release();
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
     c->graphs.clear();

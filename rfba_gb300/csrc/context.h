@@ -98,6 +98,16 @@ struct GraphPlan {
 };
 
 
+// The device scratch of one Gibbs chain: its spots, spot intensities, masks,
+// states, current sample, emission buffers, barrier counter and outputs.
+struct GibbsScratch {
+    DevBuf spots, si, moff, midx, state, cur, em, bar, var, ostate, oint, oerr, lp, filt;
+    void release() {
+        for (DevBuf* b : {&spots, &si, &moff, &midx, &state, &cur, &em, &bar, &var, &ostate, &oint, &oerr, &lp, &filt})
+            b->release();
+    }
+};
+
 }  // namespace rfba
 
 struct rfba_ctx {
@@ -143,8 +153,8 @@ struct rfba_ctx {
     // 3B spot-gradient scratch
     rfba::DevBuf tb_val, tb_der, tb_em, tb_res, tb_par, tb_bg, tb_pix, tb_pixels, tb_dfd, tb_vdf;
     // 3B Gibbs sampler scratch
-    rfba::DevBuf gb_pix, gb_pixels, gb_spots, gb_si, gb_moff, gb_midx, gb_state, gb_cur, gb_em, gb_bar, gb_var,
-        gb_ostate, gb_oint, gb_oerr, gb_lp, gb_filt;
+    rfba::DevBuf gb_pix, gb_pixels, gb_par;
+    rfba::GibbsScratch gb[2];  // one set per chain run side by side
     // 3B sampled-background Hessian scratch
     rfba::DevBuf hs_tab, hs_part, hs_gg, hs_phi, hs_frame, hs_out;
     int last_ty = 0, last_order = 0, last_graph = 0, last_tuned = 0;

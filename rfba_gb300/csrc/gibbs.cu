@@ -13,7 +13,8 @@
 // sampler under a slowly growing noise variance; FitSpots (multispot5.cc:
 // 1591-1604) keeps its draws as the background samples of the spot optimiser.
 //
-// One cooperative kernel runs a whole chain: the frames are dealt out to the
+// One cooperative kernel runs a whole chain (or several independent chains
+// side by side, each on its own share of the CTAs): the frames are dealt out to the
 // CTAs, which do the per-frame work (remove / add over the mask, the two sums
 // of squares, the emission terms) in parallel; after a grid barrier one warp
 // of every CTA runs the forward filter and the backward draw over all frames
@@ -112,9 +113,14 @@ struct EmFrame {
     int pad[2];
 };
 
-__global__ void __launch_bounds__(kGibbsThreads) gibbs_chain_kernel(const GibbsParams g) {
+// Several independent chains may share one launch: chain i runs on CTAs
+// [i G, (i + 1) G) with its own parameters, scratch and barrier counter.
+__global__ void __launch_bounds__(kGibbsThreads) gibbs_chain_kernel(const GibbsParams* __restrict__ chains,
+                                                                     int nchains) {
     extern __shared__ double gsm[];
-    const int c = blockIdx.x, G = gridDim.x;
+    const int G = gridDim.x / nchains;
+    const int c = blockIdx.x % G;
+    const GibbsParams& g = chains[blockIdx.x / G];
     const int F = g.F, P = g.P, K = g.K;
     // shared: per frame and state the forward value (double-float mantissa,
     // exponent), the frames' emission terms, the backward draw's decision table
@@ -332,14 +338,15 @@ int gibbs_max_blocks(int F, int* out) {
     return 0;
 }
 
-int launch_gibbs(const GibbsParams& p, int grid, void* stream) {
-    const size_t smem = gibbs_smem_bytes(p.F);
+int launch_gibbs(const GibbsParams* chains_dev, int nchains, int grid_per_chain, int F, void* stream) {
+    const size_t smem = gibbs_smem_bytes(F);
     cudaError_t e = cudaFuncSetAttribute(gibbs_chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
-    GibbsParams q = p;
-    void* args[] = {&q};
-    e = cudaLaunchCooperativeKernel((const void*)gibbs_chain_kernel, dim3(grid), dim3(kGibbsThreads), args, smem,
-                                    static_cast<cudaStream_t>(stream));
+    const GibbsParams* q = chains_dev;
+    int n = nchains;
+    void* args[] = {&q, &n};
+    e = cudaLaunchCooperativeKernel((const void*)gibbs_chain_kernel, dim3(grid_per_chain * nchains), dim3(kGibbsThreads),
+                                    args, smem, static_cast<cudaStream_t>(stream));
     return (int)e;
 }
 

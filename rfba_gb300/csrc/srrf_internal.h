@@ -226,7 +226,8 @@ struct GibbsParams {
 };
 size_t gibbs_smem_bytes(int F);
 int gibbs_max_blocks(int F, int* out);
-int launch_gibbs(const GibbsParams& p, int grid, void* stream);
+// chains_dev: nchains parameter sets in device memory, all with the same F.
+int launch_gibbs(const GibbsParams* chains_dev, int nchains, int grid_per_chain, int F, void* stream);
 int launch_spot_intensity(const int* pixels, int P, const double* spots, int K, double zf, double* out, void* stream);
 
 // 3B sampled-background spot Hessian (hessian.cu). Sizes: tab [P][21],

@@ -32,9 +32,12 @@
 // (residual_df_kernel) and emission_df_kernel forms the gradient's sums
 // (sum d v, sum der_n d) on the FP32 pipe in double-float arithmetic, about
 // 2^-46 relative per operation, four samples of a frame per CTA so the spot's
-// table is read once per four: the FP64 pipe, 1/64 of the FP32 one here,
-// would otherwise bound every evaluation. The log-probability path keeps the
-// FP64 sums.
+// table is read once per four, over the spot's support only (the pixels where
+// its Gaussian factor is at least 2^-60, listed in pixel order by
+// support_compact_kernel); forward_df_kernel runs the recursion in
+// double-float too. The FP64 pipe, 1/64 of the FP32 one here, would otherwise
+// bound every evaluation. The log-probability path keeps the FP64 sums over
+// every pixel.
 #include <cuda_runtime.h>
 
 #include "dfloat.cuh"
@@ -45,6 +48,10 @@ namespace {
 
 constexpr int kM = 5;
 constexpr int kEmitThreads = 256;
+// The double-float path sums only over the spot's support: the pixels where
+// its Gaussian factor exp(s) is at least 2^-60 (terms below that are far under
+// the 2^-46 resolution of the double-float sums they would join).
+constexpr double kSupportS = -41.58883083359672;  // ln(2^-60)
 
 using namespace dfloat;
 
@@ -53,7 +60,8 @@ __global__ void __launch_bounds__(kPixThreads) spot_pixels_kernel(const int* __r
                                                                    const double* __restrict__ phi_in, double zf,
                                                                    double* __restrict__ val, double* __restrict__ der,
                                                                    float2* __restrict__ vdf,
-                                                                   double* __restrict__ partial) {
+                                                                   double* __restrict__ partial,
+                                                                   unsigned char* __restrict__ support) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     double acc[6] = {0, 0, 0, 0, 0, 0};  // this pixel's v^2 and der_n v
     if (p < P) {
@@ -72,6 +80,7 @@ __global__ void __launch_bounds__(kPixThreads) spot_pixels_kernel(const int* __r
         d[2] = k * ((x0 - phi2) * q);
         d[3] = k * ((x1 - phi3) * q);
         d[4] = k * ((x2 - phi4) * q);
+        if (support) support[p] = s >= kSupportS;
         if (vdf) {  // value and derivative as double-floats: [P][6]
             float2* o = vdf + (size_t)p * 6;
             o[0] = df_from(val[p]);
@@ -118,6 +127,44 @@ __global__ void spot_sums_kernel(const double* __restrict__ partial, int nblocks
     double t = 0;
     for (int b = 0; b < nblocks; ++b) t += partial[(size_t)b * 6 + threadIdx.x];
     sums[threadIdx.x] = t;
+}
+
+// The support's pixel indices in pixel order (one CTA): each thread counts a
+// contiguous run of flags, a block-wide exclusive scan places the runs, and
+// the indices are written in order; count[0] = the support's size.
+constexpr int kScanThreads = 1024;
+__global__ void __launch_bounds__(kScanThreads) support_compact_kernel(const unsigned char* __restrict__ flag, int P,
+                                                                        int* __restrict__ idx,
+                                                                        int* __restrict__ count) {
+    const int per = (P + kScanThreads - 1) / kScanThreads;
+    const int p0 = min(P, threadIdx.x * per), p1 = min(P, p0 + per);
+    int n = 0;
+    for (int q = p0; q < p1; ++q) n += flag[q];
+    // inclusive scan of n over the block
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int v = n;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += u;
+    }
+    __shared__ int wsum[kScanThreads / 32];
+    if (lane == 31) wsum[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        int w = wsum[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += u;
+        }
+        wsum[lane] = w;
+    }
+    __syncthreads();
+    int base = v - n + (warp > 0 ? wsum[warp - 1] : 0);
+    for (int q = p0; q < p1; ++q)
+        if (flag[q]) idx[base++] = q;
+    if (threadIdx.x == kScanThreads - 1) count[0] = base;
 }
 
 // Per (sample, frame), kEm doubles: the frame's emission probabilities relative
@@ -196,17 +243,28 @@ __global__ void __launch_bounds__(kEmitThreads) emission_kernel(const double* __
     }
 }
 
+// A frame's emission terms for the double-float forward recursion: the
+// mantissas (double-float) and exponents of p(on) and p(off) relative to the
+// larger one, and d(log p_on)/d phi.
+struct __align__(16) EmDf {
+    float2 mant[2];
+    int k[2];
+    float2 q[kM];
+};
+
 // The gradient's emission terms from the double-float residuals, kDfTile
 // samples of one frame per CTA (blockIdx.x = frame, blockIdx.y = sample
-// tile): per sample sum d v and sum der_n d in double-float, then the same
-// terms as emission_kernel writes except the frame's level (entry 9, used by
-// the log probability only), which is 0.
+// tile): per sample sum d v and sum der_n d in double-float, then the terms
+// emission_kernel forms except the frame's level (used by the log probability
+// only), written as double-floats for forward_df_kernel.
 constexpr int kDfTile = 4;
 __global__ void __launch_bounds__(kEmitThreads) emission_df_kernel(const float2* __restrict__ dfd,
                                                                     const float2* __restrict__ vdf,
+                                                                    const int* __restrict__ sup,
+                                                                    const int* __restrict__ nsup,
                                                                     const double* __restrict__ spot_sums, int S, int F,
                                                                     int P, double twovar, double var,
-                                                                    double* __restrict__ out) {
+                                                                    EmDf* __restrict__ out) {
     const int f = blockIdx.x, s0 = blockIdx.y * kDfTile;
     const int ns = min(kDfTile, S - s0);
     float2 acc[kDfTile][6];
@@ -214,7 +272,9 @@ __global__ void __launch_bounds__(kEmitThreads) emission_df_kernel(const float2*
     for (int a = 0; a < kDfTile; ++a)
 #pragma unroll
         for (int n = 0; n < 6; ++n) acc[a][n] = make_float2(0.f, 0.f);
-    for (int p = threadIdx.x; p < P; p += kEmitThreads) {
+    const int n = *nsup;
+    for (int i = threadIdx.x; i < n; i += kEmitThreads) {
+        const int p = __ldg(sup + i);
         // every load of the iteration goes out before its arithmetic (a tile's
         // missing samples read 0 and add 0)
         float2 w[6], d[kDfTile];
@@ -257,20 +317,26 @@ __global__ void __launch_bounds__(kEmitThreads) emission_df_kernel(const float2*
             for (int w = 1; w < kEmitThreads / 32; ++w) v = df_add(v, part[w][a][n]);
             t[n] = df_to(v);
         }
-        double* o = out + ((size_t)(s0 + a) * F + f) * kEm;
+        EmDf* o = out + (size_t)(s0 + a) * F + f;
         const double gap = (2.0 * t[0] - spot_sums[0]) / twovar;  // log p_on - log p_off
+        double m[2], k[2];
         if (gap <= 0.0) {
-            exp_split(gap, &o[0], &o[2]);
-            o[1] = 1.0;
-            o[3] = 0.0;
+            exp_split(gap, &m[0], &k[0]);
+            m[1] = 1.0;
+            k[1] = 0.0;
         } else {
-            o[0] = 1.0;
-            o[2] = 0.0;
-            exp_split(-gap, &o[1], &o[3]);
+            m[0] = 1.0;
+            k[0] = 0.0;
+            exp_split(-gap, &m[1], &k[1]);
         }
-        o[9] = 0.0;
+        EmDf r;
+        for (int i = 0; i < 2; ++i) {
+            r.mant[i] = df_from(m[i]);
+            r.k[i] = (int)k[i];
+        }
 #pragma unroll
-        for (int n = 0; n < kM; ++n) o[4 + n] = (t[1 + n] - spot_sums[1 + n]) / var;
+        for (int n = 0; n < kM; ++n) r.q[n] = df_from((t[1 + n] - spot_sums[1 + n]) / var);
+        *o = r;
     }
 }
 
@@ -388,6 +454,123 @@ __global__ void __launch_bounds__(32) forward_kernel(const double* __restrict__ 
     if (lane == 5) r[5] = base + log(den) + (double)Em * 0.6931471805599453;
 }
 
+// The forward recursion of forward_kernel in double-float arithmetic, for
+// the gradient only (the log probability is not formed): each lane's value a
+// double-float mantissa with the state's exponent, the same alignment to the
+// largest exponent among the states that reach j, terms more than 2^100 below
+// it dropped (below the format's precision).
+__global__ void __launch_bounds__(32) forward_df_kernel(const EmDf* __restrict__ em, int S, int F,
+                                                         const double* __restrict__ A9, const double* __restrict__ pi3,
+                                                         double* __restrict__ res) {
+    const int s = blockIdx.x;
+    const int lane = threadIdx.x;
+    const int l = lane % 18;
+    const int j = l / 6, k = l % 6;
+    const unsigned full = 0xffffffffu;
+    float2 Aj[3];
+    bool nz[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        Aj[i] = df_from(A9[i * 3 + j]);
+        nz[i] = A9[i * 3 + j] != 0.0;
+    }
+    const EmDf* e = em + (size_t)s * F;
+    const int mi = j == 0 ? 0 : 1;  // the bleached state emits like "off"
+    const bool has_de = j == 0 && k < 5;
+    auto shfl2 = [&](float2 v, int src) {
+        return make_float2(__shfl_sync(full, v.x, src), __shfl_sync(full, v.y, src));
+    };
+    // normalise the new values y of this lane's state by the exponent of its
+    // probability lane; returns the state's new exponent
+    // (branch-free: the lanes of a state whose probability is 0 must not
+    // diverge from the others)
+    auto normalise = [&](float2 y, int Ebase, float2* x) {
+        const float2 y5 = shfl2(y, j * 6 + 5);
+        const int ex = (__float_as_int(y5.x) >> 23) & 0xff;
+        const bool zero = y5.x == 0.f || ex == 0 || Ebase == kZeroExp;
+        const int sh = ex - 126;  // y5 = m 2^sh, m in [0.5, 1)
+        const float sc = zero ? 1.f : pow2f(-sh);
+        *x = make_float2(y.x * sc, y.y * sc);
+        return zero ? kZeroExp : Ebase + sh;
+    };
+    float2 x;
+    int E[3];
+    {
+        const float2 a = df_mul(df_from(pi3[j]), e[0].mant[mi]);
+        const float2 y = k == 5 ? a : (has_de ? df_mul(a, e[0].q[k]) : make_float2(0.f, 0.f));
+        const int En = normalise(y, pi3[j] == 0.0 ? kZeroExp : e[0].k[mi], &x);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) E[i] = __shfl_sync(full, En, i * 6 + 5);
+    }
+    // the frames' terms pass through shared memory 32 at a time: the next
+    // chunk is loaded into registers while this one is used, and stored at
+    // its end (a chain step is shorter than a load's latency)
+    const int kq = k < 5 ? k : 0;
+    const float qmask = has_de ? 1.f : 0.f;
+    __shared__ __align__(16) EmDf chunk[2][32];
+    float4 nxt[4];
+    auto fetch = [&](int c) {
+        const int t = c * 32 + lane;
+        const float4* src = reinterpret_cast<const float4*>(e + (t < F ? t : F - 1));
+#pragma unroll
+        for (int w = 0; w < 4; ++w) nxt[w] = src[w];
+    };
+    auto store = [&](int slot) {
+        float4* dst = reinterpret_cast<float4*>(&chunk[slot][lane]);
+#pragma unroll
+        for (int w = 0; w < 4; ++w) dst[w] = nxt[w];
+    };
+    const int nchunk = (F + 31) / 32;
+    fetch(0);
+    store(0);
+    __syncwarp();
+    for (int c = 0; c < nchunk; ++c) {
+        if (c + 1 < nchunk) fetch(c + 1);
+        const EmDf* cur = chunk[c & 1];
+        const int t1 = min(F, c * 32 + 32);
+        for (int t = max(1, c * 32); t < t1; ++t) {
+            const EmDf& et = cur[t - c * 32];
+            const float2 mant = et.mant[mi];
+            const float2 qv = et.q[kq];
+            const float2 q = make_float2(qv.x * qmask, qv.y * qmask);
+            const int ke = et.k[mi];
+            int Em = kZeroExp;
+#pragma unroll
+            for (int i = 0; i < 3; ++i) Em = (nz[i] && E[i] > Em) ? E[i] : Em;
+            float2 y = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const float2 xi = shfl2(x, i * 6 + k);
+                const int d = E[i] - Em;
+                const bool use = nz[i] && E[i] != kZeroExp && d >= -100;
+                const float sc = use ? pow2f(d < -126 ? -126 : d) : 0.f;
+                float2 tm = df_mul(Aj[i], xi);
+                tm.x *= sc;
+                tm.y *= sc;
+                y = df_add(y, tm);
+            }
+            y = df_mul(y, mant);
+            const float2 y05 = shfl2(y, 5);
+            y = df_add(y, df_mul(y05, q));
+            const int En = normalise(y, (Em == kZeroExp || ke == kZeroExp) ? kZeroExp : Em + ke, &x);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) E[i] = __shfl_sync(full, En, i * 6 + 5);
+        }
+        __syncwarp();
+        if (c + 1 < nchunk) store((c + 1) & 1);
+        __syncwarp();
+    }
+    // the gradient, the states aligned to the largest exponent
+    const int Em = max(E[0], max(E[1], E[2]));
+    const int d = E[j] - Em;
+    const double v = (d >= -1022 && E[j] != kZeroExp) ? df_to(x) * ldexp(1.0, d) : 0.0;
+    const double tot = v + __shfl_sync(full, v, (lane + 6) & 31) + __shfl_sync(full, v, (lane + 12) & 31);
+    const double den = __shfl_sync(full, tot, 5);
+    double* r = res + (size_t)s * 6;
+    if (lane < 5) r[lane] = tot / den;
+    if (lane == 5) r[5] = 0.0;
+}
+
 }  // namespace
 
 int launch_threeb_residual(const double* bg, const double* pix, int S, int F, int P, float2* dfd, void* stream) {
@@ -404,15 +587,23 @@ int launch_threeb(const double* bg, const double* pix, const int* pixels, int S,
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int nblk = (P + kPixThreads - 1) / kPixThreads;
     double* sums = res + (size_t)S * 6;  // 6 doubles after the per-sample results, then the blocks' partials
+    // the double-float path's support flags and list share the table's buffer:
+    // vdf [P][6] float2, then P flag bytes, then the P indices and the count
+    unsigned char* flag = dfd ? reinterpret_cast<unsigned char*>(vdf + (size_t)P * 6) : nullptr;
+    int* sup = dfd ? reinterpret_cast<int*>(flag + (((size_t)P + 15) & ~(size_t)15)) : nullptr;
     spot_pixels_kernel<<<nblk, kPixThreads, 0, st>>>(pixels, P, phi_dev, zf, val, der, dfd ? vdf : nullptr,
-                                                     sums + 6);
+                                                     sums + 6, flag);
     spot_sums_kernel<<<1, 32, 0, st>>>(sums + 6, nblk, sums);
-    if (dfd)
+    if (dfd) {
+        support_compact_kernel<<<1, kScanThreads, 0, st>>>(flag, P, sup, sup + P);
+        EmDf* emd = reinterpret_cast<EmDf*>(em);  // 64 B per (sample, frame), within the FP64 path's 80
         emission_df_kernel<<<dim3((unsigned)F, (unsigned)((S + kDfTile - 1) / kDfTile)), kEmitThreads, 0, st>>>(
-            dfd, vdf, sums, S, F, P, 2 * variance, variance, em);
-    else
-        emission_kernel<<<(unsigned)((long long)S * F), kEmitThreads, 0, st>>>(bg, pix, val, der, sums, F, P,
-                                                                               2 * variance, variance, c0, em);
+            dfd, vdf, sup, sup + P, sums, S, F, P, 2 * variance, variance, emd);
+        forward_df_kernel<<<S, 32, 0, st>>>(emd, S, F, A_dev, pi_dev, res);
+        return (int)cudaGetLastError();
+    }
+    emission_kernel<<<(unsigned)((long long)S * F), kEmitThreads, 0, st>>>(bg, pix, val, der, sums, F, P,
+                                                                           2 * variance, variance, c0, em);
     forward_kernel<<<S, 32, 0, st>>>(em, S, F, A_dev, pi_dev, res);
     return (int)cudaGetLastError();
 }

@@ -80,7 +80,8 @@ static int threeb_stage(rfba_ctx* ctx, const double* sample_bg, const double* pi
         d->pixels = static_cast<const int*>(ctx->tb_pixels.p);
     }
     if (residual_df) {
-        if ((s = ctx->tb_dfd.ensure(nbg * 8, "3B residuals")) || (s = ctx->tb_vdf.ensure((size_t)P * 48, "3B spot table")))
+        if ((s = ctx->tb_dfd.ensure(nbg * 8, "3B residuals")) || (s = ctx->tb_vdf.ensure((size_t)P * 48 + (((size_t)P + 15) & ~(size_t)15) + (size_t)P * 4 + 16,
+                                   "3B spot table")))
             return s;
         const int e = launch_threeb_residual(d->bg, d->pix, S, F, P, static_cast<float2*>(ctx->tb_dfd.p), st);
         if (e) return cuda_fail((cudaError_t)e, "3B residual launch");
@@ -211,92 +212,102 @@ struct GibbsCall {
     bool want_state = false, want_int = false, want_err = false, trace = false;
 };
 
-// Stage the data, compute the spot intensities, run one chain from all spots
-// off. Outputs stay in the context's gb_* buffers; returns after the kernel
-// has finished and its status has been read.
-static int gibbs_run(rfba_ctx* ctx, const rfba_3b_model* m, const double* pix, const int* pixels,
-                     const double* spots, const std::vector<int>& hoff, const std::vector<int>& hidx,
-                     const GibbsCall& c, int ptr_flags, cudaStream_t st) {
+// Stage one chain in scratch set `set` (the data, the spot intensities, all
+// spots off) and fill its kernel parameters; nothing is launched.
+static int gibbs_prepare(rfba_ctx* ctx, const rfba_3b_model* m, const double* pix, const int* pixels,
+                         const double* spots, const std::vector<int>& hoff, const std::vector<int>& hidx,
+                         const GibbsCall& c, int ptr_flags, cudaStream_t st, int set, GibbsParams* gp) {
     int s;
+    GibbsScratch& gs = ctx->gb[set];
     const size_t K = (size_t)c.K, F = (size_t)c.F, P = (size_t)c.P, nnz = hidx.size();
-    if ((s = ctx->gb_moff.ensure((K + 1) * 4, "3B mask offsets")) || (s = ctx->gb_midx.ensure(nnz * 4 + 4, "3B masks")) ||
-        (s = ctx->gb_si.ensure(K * P * 8 + 8, "3B spot intensities")) ||
-        (s = ctx->gb_state.ensure(K * F + 1, "3B spot states")) || (s = ctx->gb_cur.ensure(F * P * 8, "3B sample intensities")) ||
-        (s = ctx->gb_em.ensure(F * 64, "3B emissions")) || (s = ctx->gb_bar.ensure(256, "3B barrier")))
+    if ((s = gs.moff.ensure((K + 1) * 4, "3B mask offsets")) || (s = gs.midx.ensure(nnz * 4 + 4, "3B masks")) ||
+        (s = gs.si.ensure(K * P * 8 + 8, "3B spot intensities")) ||
+        (s = gs.state.ensure(K * F + 1, "3B spot states")) || (s = gs.cur.ensure(F * P * 8, "3B sample intensities")) ||
+        (s = gs.em.ensure(F * 64, "3B emissions")) || (s = gs.bar.ensure(256, "3B barrier")))
         return s;
     const double* dpix = pix;
     const int* dpixels = pixels;
     const double* dspots = spots;
     if (ptr_flags == RFBA_HOST_PTRS) {
         if ((s = ctx->gb_pix.ensure(F * P * 8, "3B data")) || (s = ctx->gb_pixels.ensure(P * 12, "3B pixels")) ||
-            (s = ctx->gb_spots.ensure(K * 40 + 8, "3B spots")))
+            (s = gs.spots.ensure(K * 40 + 8, "3B spots")))
             return s;
         RFBA_CUDA(cudaMemcpyAsync(ctx->gb_pix.p, pix, F * P * 8, cudaMemcpyHostToDevice, st), "data copy");
         RFBA_CUDA(cudaMemcpyAsync(ctx->gb_pixels.p, pixels, P * 12, cudaMemcpyHostToDevice, st), "pixels copy");
-        if (K) RFBA_CUDA(cudaMemcpyAsync(ctx->gb_spots.p, spots, K * 40, cudaMemcpyHostToDevice, st), "spots copy");
+        if (K) RFBA_CUDA(cudaMemcpyAsync(gs.spots.p, spots, K * 40, cudaMemcpyHostToDevice, st), "spots copy");
         dpix = static_cast<const double*>(ctx->gb_pix.p);
         dpixels = static_cast<const int*>(ctx->gb_pixels.p);
-        dspots = static_cast<const double*>(ctx->gb_spots.p);
+        dspots = static_cast<const double*>(gs.spots.p);
     }
-    RFBA_CUDA(cudaMemcpyAsync(ctx->gb_moff.p, hoff.data(), (K + 1) * 4, cudaMemcpyHostToDevice, st), "mask offsets copy");
-    if (nnz) RFBA_CUDA(cudaMemcpyAsync(ctx->gb_midx.p, hidx.data(), nnz * 4, cudaMemcpyHostToDevice, st), "mask copy");
+    RFBA_CUDA(cudaMemcpyAsync(gs.moff.p, hoff.data(), (K + 1) * 4, cudaMemcpyHostToDevice, st), "mask offsets copy");
+    if (nnz) RFBA_CUDA(cudaMemcpyAsync(gs.midx.p, hidx.data(), nnz * 4, cudaMemcpyHostToDevice, st), "mask copy");
     if (K) {
-        int e = launch_spot_intensity(dpixels, c.P, dspots, c.K, m->z_factor, static_cast<double*>(ctx->gb_si.p), st);
+        int e = launch_spot_intensity(dpixels, c.P, dspots, c.K, m->z_factor, static_cast<double*>(gs.si.p), st);
         if (e) return cuda_fail((cudaError_t)e, "3B spot intensity launch");
         ++ctx->launches;
     }
     // all spots off (state 2), no spot intensity in the current sample
-    RFBA_CUDA(cudaMemsetAsync(ctx->gb_state.p, 2, K * F + 1, st), "state init");
-    RFBA_CUDA(cudaMemsetAsync(ctx->gb_cur.p, 0, F * P * 8, st), "sample init");
-    RFBA_CUDA(cudaMemsetAsync(ctx->gb_bar.p, 0, 256, st), "barrier init");
+    RFBA_CUDA(cudaMemsetAsync(gs.state.p, 2, K * F + 1, st), "state init");
+    RFBA_CUDA(cudaMemsetAsync(gs.cur.p, 0, F * P * 8, st), "sample init");
+    RFBA_CUDA(cudaMemsetAsync(gs.bar.p, 0, 256, st), "barrier init");
     RFBA_CUDA(cudaMemsetAsync(ctx->errw.p, 0, 8, st), "status clear");
     const size_t nd = (size_t)c.n_draws;
     if (c.var_draw) {
-        if ((s = ctx->gb_var.ensure(nd * 8, "3B variance schedule"))) return s;
-        RFBA_CUDA(cudaMemcpyAsync(ctx->gb_var.p, c.var_draw, nd * 8, cudaMemcpyHostToDevice, st), "schedule copy");
+        if ((s = gs.var.ensure(nd * 8, "3B variance schedule"))) return s;
+        RFBA_CUDA(cudaMemcpyAsync(gs.var.p, c.var_draw, nd * 8, cudaMemcpyHostToDevice, st), "schedule copy");
     }
-    if (c.want_state && (s = ctx->gb_ostate.ensure(nd * K * F + 1, "3B drawn states"))) return s;
-    if (c.want_int && (s = ctx->gb_oint.ensure(nd * F * P * 8, "3B drawn intensities"))) return s;
-    if (c.want_err && (s = ctx->gb_oerr.ensure(nd * F * 8, "3B residual sums"))) return s;
-    if (c.trace && ((s = ctx->gb_lp.ensure(K * F * 16 + 16, "3B trace")) || (s = ctx->gb_filt.ensure(K * F * 24 + 24, "3B trace"))))
+    if (c.want_state && (s = gs.ostate.ensure(nd * K * F + 1, "3B drawn states"))) return s;
+    if (c.want_int && (s = gs.oint.ensure(nd * F * P * 8, "3B drawn intensities"))) return s;
+    if (c.want_err && (s = gs.oerr.ensure(nd * F * 8, "3B residual sums"))) return s;
+    if (c.trace && ((s = gs.lp.ensure(K * F * 16 + 16, "3B trace")) || (s = gs.filt.ensure(K * F * 24 + 24, "3B trace"))))
         return s;
-    GibbsParams g;
+    GibbsParams& g = *gp;
     std::memset(&g, 0, sizeof g);
     g.pix = dpix;
-    g.si = static_cast<const double*>(ctx->gb_si.p);
-    g.moff = static_cast<const int*>(ctx->gb_moff.p);
-    g.midx = static_cast<const int*>(ctx->gb_midx.p);
+    g.si = static_cast<const double*>(gs.si.p);
+    g.moff = static_cast<const int*>(gs.moff.p);
+    g.midx = static_cast<const int*>(gs.midx.p);
     g.K = c.K;
     g.F = c.F;
     g.P = c.P;
     for (int n = 0; n < 9; ++n) g.A[n] = m->A[n];
     for (int n = 0; n < 3; ++n) g.pi[n] = m->pi[n];
     g.variance = m->variance;
-    g.var_draw = c.var_draw ? static_cast<const double*>(ctx->gb_var.p) : nullptr;
+    g.var_draw = c.var_draw ? static_cast<const double*>(gs.var.p) : nullptr;
     g.sweeps = c.sweeps;
     g.n_draws = c.n_draws;
     g.seed = c.seed;
     g.draw_base = 0;
-    g.state = static_cast<unsigned char*>(ctx->gb_state.p);
-    g.cur = static_cast<double*>(ctx->gb_cur.p);
-    g.em = static_cast<double*>(ctx->gb_em.p);
-    g.bar = static_cast<unsigned int*>(ctx->gb_bar.p);
+    g.state = static_cast<unsigned char*>(gs.state.p);
+    g.cur = static_cast<double*>(gs.cur.p);
+    g.em = static_cast<double*>(gs.em.p);
+    g.bar = static_cast<unsigned int*>(gs.bar.p);
     g.err = static_cast<unsigned long long*>(ctx->errw.p);
-    g.out_state = c.want_state ? static_cast<unsigned char*>(ctx->gb_ostate.p) : nullptr;
-    g.out_int = c.want_int ? static_cast<double*>(ctx->gb_oint.p) : nullptr;
+    g.out_state = c.want_state ? static_cast<unsigned char*>(gs.ostate.p) : nullptr;
+    g.out_int = c.want_int ? static_cast<double*>(gs.oint.p) : nullptr;
     g.exclude_spot = c.exclude;
-    g.out_err = c.want_err ? static_cast<double*>(ctx->gb_oerr.p) : nullptr;
-    g.rec_lp = c.trace ? static_cast<double*>(ctx->gb_lp.p) : nullptr;
-    g.rec_filt = c.trace ? static_cast<double*>(ctx->gb_filt.p) : nullptr;
+    g.out_err = c.want_err ? static_cast<double*>(gs.oerr.p) : nullptr;
+    g.rec_lp = c.trace ? static_cast<double*>(gs.lp.p) : nullptr;
+    g.rec_filt = c.trace ? static_cast<double*>(gs.filt.p) : nullptr;
+    return RFBA_OK;
+}
+
+// Launch nchains prepared chains side by side in one cooperative kernel, wait
+// for it and read its status.
+static int gibbs_launch(rfba_ctx* ctx, const GibbsParams* g, int nchains, int F, cudaStream_t st) {
+    int s;
+    if ((s = ctx->gb_par.ensure(sizeof(GibbsParams) * (size_t)nchains, "3B Gibbs parameters"))) return s;
+    RFBA_CUDA(cudaMemcpyAsync(ctx->gb_par.p, g, sizeof(GibbsParams) * (size_t)nchains, cudaMemcpyHostToDevice, st),
+              "parameter copy");
     int maxb = 0;
-    int e = gibbs_max_blocks(c.F, &maxb);
+    int e = gibbs_max_blocks(F, &maxb);
     if (e) return cuda_fail((cudaError_t)e, "3B Gibbs occupancy");
-    if (maxb < 1) {
-        set_error("3B Gibbs kernel does not fit on an SM");
+    const int grid = std::min(std::min(F, maxb / nchains), ctx->sm_count);
+    if (grid < 1) {
+        set_error("3B Gibbs kernel does not fit on the GPU");
         return RFBA_ERR_UNSUPPORTED;
     }
-    const int grid = std::min(std::min(c.F, maxb), ctx->sm_count);
-    e = launch_gibbs(g, grid, st);
+    e = launch_gibbs(static_cast<const GibbsParams*>(ctx->gb_par.p), nchains, grid, F, st);
     if (e) return cuda_fail((cudaError_t)e, "3B Gibbs launch");
     ++ctx->launches;
     unsigned long long w = 0;
@@ -310,6 +321,16 @@ static int gibbs_run(rfba_ctx* ctx, const rfba_3b_model* m, const double* pix, c
         return RFBA_ERR_TIMEOUT;
     }
     return RFBA_OK;
+}
+
+// One chain from all spots off in scratch set 0; the outputs stay there.
+static int gibbs_run(rfba_ctx* ctx, const rfba_3b_model* m, const double* pix, const int* pixels,
+                     const double* spots, const std::vector<int>& hoff, const std::vector<int>& hidx,
+                     const GibbsCall& c, int ptr_flags, cudaStream_t st) {
+    GibbsParams g;
+    int s;
+    if ((s = gibbs_prepare(ctx, m, pix, pixels, spots, hoff, hidx, c, ptr_flags, st, 0, &g))) return s;
+    return gibbs_launch(ctx, &g, 1, c.F, st);
 }
 
 static int gibbs_check(rfba_ctx* ctx, const rfba_3b_model* m, int K, int F, int P, int ptr_flags) {
@@ -422,11 +443,12 @@ static void flatten_masks(const std::vector<std::vector<int> >& masks, size_t co
     }
 }
 
-static int upload_spots(rfba_ctx* ctx, const std::vector<Spot>& sp, cudaStream_t st) {
+static int upload_spots(rfba_ctx* ctx, const std::vector<Spot>& sp, cudaStream_t st, int set = 0) {
     int s;
-    if ((s = ctx->gb_spots.ensure(sp.size() * 40 + 8, "3B spots"))) return s;
+    if ((s = ctx->gb[set].spots.ensure(sp.size() * 40 + 8, "3B spots"))) return s;
     if (!sp.empty())
-        RFBA_CUDA(cudaMemcpyAsync(ctx->gb_spots.p, sp.data(), sp.size() * 40, cudaMemcpyHostToDevice, st), "spots copy");
+        RFBA_CUDA(cudaMemcpyAsync(ctx->gb[set].spots.p, sp.data(), sp.size() * 40, cudaMemcpyHostToDevice, st),
+                  "spots copy");
     return RFBA_OK;
 }
 
@@ -458,7 +480,7 @@ static int draws_without(rfba_ctx* ctx, const rfba_3b_model* m, int F, int P, co
     c.exclude = exclude;
     c.want_int = true;
     return gibbs_run(ctx, m, static_cast<const double*>(ctx->gb_pix.p), static_cast<const int*>(ctx->gb_pixels.p),
-                     static_cast<const double*>(ctx->gb_spots.p), hoff, hidx, c, RFBA_DEVICE_PTRS, st);
+                     static_cast<const double*>(ctx->gb[0].spots.p), hoff, hidx, c, RFBA_DEVICE_PTRS, st);
 }
 
 // The spot optimiser's gradient on staged samples (NaN outside brightness,
@@ -524,7 +546,7 @@ static int optimise_pass_core(rfba_ctx* ctx, const rfba_3b_model* m, const int* 
             return s;
         // optimise the spot on those samples (multispot5.cc:1611-1636)
         StagedGradient grad{ctx, m, ThreeBData(), st};
-        if ((s = threeb_stage(ctx, static_cast<const double*>(ctx->gb_oint.p), static_cast<const double*>(ctx->gb_pix.p),
+        if ((s = threeb_stage(ctx, static_cast<const double*>(ctx->gb[0].oint.p), static_cast<const double*>(ctx->gb_pix.p),
                               static_cast<const int*>(ctx->gb_pixels.p), main_samples, F, P, RFBA_DEVICE_PTRS, st,
                               &grad.d, true)))
             return s;
@@ -602,27 +624,51 @@ static int free_energy_draws(rfba_ctx* ctx, const rfba_3b_model* m, const double
     int s;
     if ((s = gibbs_run(ctx, m, pix, pixels, spots, hoff, hidx, c, ptr_flags, st))) return s;
     err->assign((size_t)samples * F, 0.0);
-    RFBA_CUDA(cudaMemcpyAsync(err->data(), ctx->gb_oerr.p, err->size() * 8, cudaMemcpyDeviceToHost, st),
+    RFBA_CUDA(cudaMemcpyAsync(err->data(), ctx->gb[0].oerr.p, err->size() * 8, cudaMemcpyDeviceToHost, st),
               "residual read-back");
     RFBA_CUDA(cudaStreamSynchronize(st), "synchronize");
     return RFBA_OK;
 }
 
-// -compute_with_mask of the staged block with spots `sp` and masks (the first
-// sp.size() of `masks`).
-static int model_energy(rfba_ctx* ctx, const rfba_3b_model* m, int F, int P, const std::vector<Spot>& sp,
-                        const std::vector<std::vector<int> >& masks, int samples, int sweeps, unsigned long long seed,
-                        cudaStream_t st, double* energy) {
+// The negative free energies of n (1 or 2) models of the staged block side by
+// side: their chains in one launch, as the reference runs the two of a model
+// comparison on two threads (multispot5.cc:2096-2108). Model i uses the first
+// sp[i]->size() masks of *masks[i].
+static int model_energies(rfba_ctx* ctx, const rfba_3b_model* m, int F, int P, int n, const std::vector<Spot>* sp[],
+                          const std::vector<std::vector<int> >* masks[], int samples, int sweeps,
+                          const unsigned long long seeds[], cudaStream_t st, double energy[]) {
     int s;
-    std::vector<int> hoff, hidx;
-    flatten_masks(masks, sp.size(), &hoff, &hidx);
-    if ((s = upload_spots(ctx, sp, st))) return s;
-    std::vector<double> err;
-    if ((s = free_energy_draws(ctx, m, static_cast<const double*>(ctx->gb_pix.p), static_cast<const int*>(ctx->gb_pixels.p),
-                               static_cast<const double*>(ctx->gb_spots.p), hoff, hidx, (int)sp.size(), F, P, samples,
-                               sweeps, seed, RFBA_DEVICE_PTRS, st, &err)))
-        return s;
-    *energy = -free_energy_value(m, err, samples, F, P, sp.empty() ? nullptr : sp[0].data(), (int)sp.size(), nullptr);
+    const double base_sigma = std::sqrt(m->variance);
+    std::vector<double> var2((size_t)samples);
+    for (int i = 0; i < samples; ++i) var2[i] = variance_from_sample(i - 1, samples, base_sigma, 100.0);
+    GibbsParams g[2];
+    for (int i = 0; i < n; ++i) {
+        std::vector<int> hoff, hidx;
+        flatten_masks(*masks[i], sp[i]->size(), &hoff, &hidx);
+        if ((s = upload_spots(ctx, *sp[i], st, i))) return s;
+        GibbsCall c;
+        c.K = (int)sp[i]->size();
+        c.F = F;
+        c.P = P;
+        c.sweeps = sweeps;
+        c.n_draws = samples;
+        c.seed = seeds[i];
+        c.var_draw = var2.data();
+        c.want_err = true;
+        if ((s = gibbs_prepare(ctx, m, static_cast<const double*>(ctx->gb_pix.p),
+                               static_cast<const int*>(ctx->gb_pixels.p), static_cast<const double*>(ctx->gb[i].spots.p),
+                               hoff, hidx, c, RFBA_DEVICE_PTRS, st, i, &g[i])))
+            return s;
+    }
+    if ((s = gibbs_launch(ctx, g, n, F, st))) return s;
+    for (int i = 0; i < n; ++i) {
+        std::vector<double> err((size_t)samples * F);
+        RFBA_CUDA(cudaMemcpyAsync(err.data(), ctx->gb[i].oerr.p, err.size() * 8, cudaMemcpyDeviceToHost, st),
+                  "residual read-back");
+        RFBA_CUDA(cudaStreamSynchronize(st), "synchronize");
+        energy[i] = -free_energy_value(m, err, samples, F, P, sp[i]->empty() ? nullptr : (*sp[i])[0].data(),
+                                       (int)sp[i]->size(), nullptr);
+    }
     return RFBA_OK;
 }
 
@@ -723,7 +769,7 @@ static int free_energy_hessian_dev(rfba_ctx* ctx, const rfba_3b_model* m, int F,
     c.want_state = true;
     c.want_int = true;
     if ((s = gibbs_run(ctx, m, static_cast<const double*>(ctx->gb_pix.p), static_cast<const int*>(ctx->gb_pixels.p),
-                       static_cast<const double*>(ctx->gb_spots.p), hoff, hidx, c, RFBA_DEVICE_PTRS, st)))
+                       static_cast<const double*>(ctx->gb[0].spots.p), hoff, hidx, c, RFBA_DEVICE_PTRS, st)))
         return s;
     const int nc = hessian_chunks(samples, F, P, ctx->sm_count);
     const size_t nq = (size_t)samples * F;
@@ -734,7 +780,7 @@ static int free_energy_hessian_dev(rfba_ctx* ctx, const rfba_3b_model* m, int F,
     RFBA_CUDA(cudaMemcpyAsync(ctx->hs_phi.p, sp[which].data(), 40, cudaMemcpyHostToDevice, st), "spot upload");
     HessParams h;
     std::memset(&h, 0, sizeof h);
-    h.bg = static_cast<const double*>(ctx->gb_oint.p);
+    h.bg = static_cast<const double*>(ctx->gb[0].oint.p);
     h.pix = static_cast<const double*>(ctx->gb_pix.p);
     h.pixels = static_cast<const int*>(ctx->gb_pixels.p);
     h.phi = static_cast<const double*>(ctx->hs_phi.p);
@@ -753,7 +799,7 @@ static int free_energy_hessian_dev(rfba_ctx* ctx, const rfba_3b_model* m, int F,
     std::vector<unsigned char> states((size_t)samples * K * F);
     RFBA_CUDA(cudaMemcpyAsync(part.data(), ctx->hs_part.p, part.size() * 8, cudaMemcpyDeviceToHost, st), "parts read");
     RFBA_CUDA(cudaMemcpyAsync(gg.data(), ctx->hs_gg.p, 15 * 8, cudaMemcpyDeviceToHost, st), "parts read");
-    RFBA_CUDA(cudaMemcpyAsync(states.data(), ctx->gb_ostate.p, states.size(), cudaMemcpyDeviceToHost, st),
+    RFBA_CUDA(cudaMemcpyAsync(states.data(), ctx->gb[0].ostate.p, states.size(), cudaMemcpyDeviceToHost, st),
               "states read");
     RFBA_CUDA(cudaStreamSynchronize(st), "synchronize");
     const Spot& sw = sp[which];
@@ -937,7 +983,7 @@ static int modify_core(rfba_ctx* ctx, const rfba_3b_model* m, const int* pixels,
             return s;
         secs[0] += since(t0);
         StagedGradient grad{ctx, m, ThreeBData(), st};
-        if ((s = threeb_stage(ctx, static_cast<const double*>(ctx->gb_oint.p), static_cast<const double*>(ctx->gb_pix.p),
+        if ((s = threeb_stage(ctx, static_cast<const double*>(ctx->gb[0].oint.p), static_cast<const double*>(ctx->gb_pix.p),
                               static_cast<const int*>(ctx->gb_pixels.p), S, F, P, RFBA_DEVICE_PTRS, st, &grad.d,
                               true)))
             return s;
@@ -950,7 +996,7 @@ static int modify_core(rfba_ctx* ctx, const rfba_3b_model* m, const int* pixels,
             if (attempt < prm.opt_attempts - 1) {
                 double H[25], ev[5], V[25];
                 t0 = clock();
-                if ((s = spot_hessian_dev(ctx, m, static_cast<const double*>(ctx->gb_oint.p),
+                if ((s = spot_hessian_dev(ctx, m, static_cast<const double*>(ctx->gb[0].oint.p),
                                           static_cast<const double*>(ctx->gb_pix.p),
                                           static_cast<const int*>(ctx->gb_pixels.p), S, F, P, cg.x,
                                           prm.opt_hess_inner_samples, mix_seed(seed, 2, attempt), H, st)))
@@ -992,7 +1038,7 @@ static int modify_core(rfba_ctx* ctx, const rfba_3b_model* m, const int* pixels,
         secs[0] += since(t0);
         double H[25], negH[25], ev[5], V[25];
         t0 = clock();
-        if ((s = spot_hessian_dev(ctx, m, static_cast<const double*>(ctx->gb_oint.p),
+        if ((s = spot_hessian_dev(ctx, m, static_cast<const double*>(ctx->gb[0].oint.p),
                                   static_cast<const double*>(ctx->gb_pix.p), static_cast<const int*>(ctx->gb_pixels.p), S,
                                   F, P, model2[spot].data(), prm.h_inner_samples, mix_seed(seed, 4, 0), H, st)))
             return s;
@@ -1005,13 +1051,14 @@ static int modify_core(rfba_ctx* ctx, const rfba_3b_model* m, const int* pixels,
         const double det = det5(scaled);
         sym_eigen5(negH, ev, V);
         if (ev[0] > 1e-6) {
-            double e2 = 0, e1 = 0;
             t0 = clock();
-            if ((s = model_energy(ctx, m, F, P, model2, masks2, prm.thermo_samples, prm.sweeps, mix_seed(seed, 5, 0), st,
-                                  &e2)) ||
-                (s = model_energy(ctx, m, F, P, model1, masks2, prm.thermo_samples, prm.sweeps, mix_seed(seed, 6, 0), st,
-                                  &e1)))
+            const std::vector<Spot>* models[2] = {&model2, &model1};
+            const std::vector<std::vector<int> >* mk[2] = {&masks2, &masks2};
+            const unsigned long long seeds[2] = {mix_seed(seed, 5, 0), mix_seed(seed, 6, 0)};
+            double en[2];
+            if ((s = model_energies(ctx, m, F, P, 2, models, mk, prm.thermo_samples, prm.sweeps, seeds, st, en)))
                 return s;
+            const double e2 = en[0], e1 = en[1];
             secs[3] += since(t0);
             const double occam = -0.5 * std::log(det);
             const double p2 = e2 + occam + pos_lp;
@@ -1165,8 +1212,8 @@ int rfba_3b_gibbs_sample(rfba_ctx* ctx, const rfba_3b_model* m, const double* pi
     c.want_state = states != nullptr;
     c.want_int = sample_intensities != nullptr;
     if ((s = gibbs_run(ctx, m, pixel_intensities, pixels, spots, hoff, hidx, c, ptr_flags, st))) return s;
-    copy_out(states, ctx->gb_ostate.p, (size_t)n_draws * K * F, ptr_flags, st, &s);
-    copy_out(sample_intensities, ctx->gb_oint.p, (size_t)n_draws * F * P * 8, ptr_flags, st, &s);
+    copy_out(states, ctx->gb[0].ostate.p, (size_t)n_draws * K * F, ptr_flags, st, &s);
+    copy_out(sample_intensities, ctx->gb[0].oint.p, (size_t)n_draws * F * P * 8, ptr_flags, st, &s);
     if (s) return s;
     RFBA_CUDA(cudaStreamSynchronize(st), "synchronize");
     return RFBA_OK;
@@ -1236,9 +1283,9 @@ int rfba_3b_gibbs_trace(rfba_ctx* ctx, const rfba_3b_model* m, const double* pix
     c.want_state = true;
     c.trace = true;
     if ((s = gibbs_run(ctx, m, pixel_intensities, pixels, spots, hoff, hidx, c, ptr_flags, st))) return s;
-    copy_out(states, ctx->gb_ostate.p, (size_t)K * F, ptr_flags, st, &s);
-    copy_out(log_prob, ctx->gb_lp.p, (size_t)K * F * 16, ptr_flags, st, &s);
-    copy_out(filtered, ctx->gb_filt.p, (size_t)K * F * 24, ptr_flags, st, &s);
+    copy_out(states, ctx->gb[0].ostate.p, (size_t)K * F, ptr_flags, st, &s);
+    copy_out(log_prob, ctx->gb[0].lp.p, (size_t)K * F * 16, ptr_flags, st, &s);
+    copy_out(filtered, ctx->gb[0].filt.p, (size_t)K * F * 24, ptr_flags, st, &s);
     if (s) return s;
     RFBA_CUDA(cudaStreamSynchronize(st), "synchronize");
     return RFBA_OK;
@@ -1407,6 +1454,54 @@ int rfba_3b_free_energy_hessian(rfba_ctx* ctx, const rfba_3b_model* m, const dou
         for (int n = 0; n < 5; ++n) sp[k][n] = spots[5 * k + n];
     if ((s = stage_block(ctx, pixel_intensities, pixels, F, P, st))) return s;
     return free_energy_hessian_dev(ctx, m, F, P, sp, spot, samples, sweeps, seed, hess, st);
+}
+
+// NegativeFreeEnergy::compute_with_mask for one or two models side by side
+// (the two chains in one launch).
+int rfba_3b_free_energy_models(rfba_ctx* ctx, const rfba_3b_model* m, const double* pixel_intensities,
+                               const int* pixels, int F, int P, int nmodels, const double* const* spots, const int* K,
+                               const int* const* mask_offsets, const int* const* mask_pixels, int samples, int sweeps,
+                               const unsigned long long* seeds, double* values) {
+    int s;
+    if (!pixel_intensities || !pixels || !spots || !K || !mask_offsets || !mask_pixels || !seeds || !values ||
+        nmodels < 1 || nmodels > 2 || samples < 1 || sweeps < 1) {
+        set_error("null argument, nmodels outside [1, 2], or samples / sweeps < 1");
+        return RFBA_ERR_INVALID;
+    }
+    for (int i = 0; i < nmodels; ++i) {
+        if ((s = gibbs_check(ctx, m, K[i], F, P, RFBA_HOST_PTRS))) return s;
+        if (K[i] > 0 && (!spots[i] || !mask_pixels[i])) {
+            set_error("null spots or masks");
+            return RFBA_ERR_INVALID;
+        }
+    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = ctx->stream;
+    if ((s = order_streams(ctx, st))) return s;
+    std::vector<Spot> sp[2];
+    std::vector<std::vector<int> > masks[2];
+    for (int i = 0; i < nmodels; ++i) {
+        if (!mask_offsets[i]) {
+            set_error("null mask offsets");
+            return RFBA_ERR_INVALID;
+        }
+        std::vector<int> hoff, hidx;
+        if ((s = gibbs_masks(mask_offsets[i], mask_pixels[i], K[i], P, RFBA_HOST_PTRS, st, &hoff, &hidx))) return s;
+        sp[i].resize((size_t)K[i]);
+        masks[i].resize((size_t)K[i]);
+        for (int k = 0; k < K[i]; ++k) {
+            for (int n = 0; n < 5; ++n) sp[i][k][n] = spots[i][5 * k + n];
+            masks[i][k].assign(hidx.begin() + hoff[k], hidx.begin() + hoff[k + 1]);
+        }
+    }
+    if ((s = stage_block(ctx, pixel_intensities, pixels, F, P, st))) return s;
+    const std::vector<Spot>* models[2] = {&sp[0], &sp[1]};
+    const std::vector<std::vector<int> >* mk[2] = {&masks[0], &masks[1]};
+    double en[2];
+    if ((s = model_energies(ctx, m, F, P, nmodels, models, mk, samples, sweeps, seeds, st, en))) return s;
+    for (int i = 0; i < nmodels; ++i) values[i] = -en[i];
+    return RFBA_OK;
 }
 
 int rfba_sym_eigen5(const double a[25], double evals[5], double evecs[25]) {

@@ -250,6 +250,8 @@ def lib():
         L.rfba_3b_free_energy_hessian.argtypes = [vp, ctypes.POINTER(ThreeBModel), vp, vp, vp, ctypes.c_int,
                                                   ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                   ull, dp]
+        L.rfba_3b_free_energy_models.argtypes = [vp, ctypes.POINTER(ThreeBModel), vp, vp, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.c_int, vp, vp, vp, vp, ctypes.c_int, ctypes.c_int, vp, dp]
         L.rfba_sym_eigen5.argtypes = [dp, dp, dp]
         L.rfba_det5.argtypes = [dp]
         L.rfba_det5.restype = ctypes.c_double
@@ -816,6 +818,31 @@ class Context:
                                           int(bs_iterations), seed, out.ctypes.data_as(dp),
                                           RFBA_DEVICE_PTRS if dev else RFBA_HOST_PTRS, _stream_arg(stream, dev)))
         return out
+
+    def free_energies_3b(self, model: ThreeBModel, pix, pixels, models, samples: int = 1000, sweeps: int = 1,
+                         seeds=(0, 1)):
+        """rfba_3b_free_energy_models: compute_with_mask's value for one or two
+        models (lists of spots [K][5]) side by side; masks from spot_masks_3b."""
+        pix = np.ascontiguousarray(pix, np.float64)
+        pixels = np.ascontiguousarray(pixels, np.int32)
+        F, P = pix.shape
+        n = len(models)
+        keep = []
+        sp_p, off_p, idx_p = (ctypes.c_void_p * n)(), (ctypes.c_void_p * n)(), (ctypes.c_void_p * n)()
+        Ks = (ctypes.c_int * n)()
+        for i, sp in enumerate(models):
+            sp = np.ascontiguousarray(sp, np.float64).reshape(-1, 5)
+            off, idx = spot_masks_3b(pixels, sp)
+            idx = np.ascontiguousarray(idx if len(idx) else np.zeros(1, np.int32), np.int32)
+            keep += [sp, off, idx]
+            sp_p[i], off_p[i], idx_p[i], Ks[i] = sp.ctypes.data, off.ctypes.data, idx.ctypes.data, len(sp)
+        sd = (ctypes.c_ulonglong * n)(*[int(v) for v in seeds[:n]])
+        vals = np.zeros(n)
+        _check(lib().rfba_3b_free_energy_models(self.h, ctypes.byref(model), ctypes.c_void_p(pix.ctypes.data),
+                                                ctypes.c_void_p(pixels.ctypes.data), F, P, n, sp_p, Ks, off_p, idx_p,
+                                                samples, sweeps, sd,
+                                                vals.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return vals
 
     def free_energy_hessian_3b(self, model: ThreeBModel, pix, pixels, spots, spot: int, samples: int = 100,
                                sweeps: int = 1, seed: int = 0):

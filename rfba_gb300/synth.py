@@ -272,13 +272,17 @@ def threeb_block(seed: int, S: int, F: int, shape=(9, 9, 7), n_spots: int = 6, s
     return samples, pix, pixels, np.asarray(spot, np.float64)
 
 
-def threeb_spots_block(seed: int, F: int, shape=(12, 12, 9), n_spots: int = 4, variance=1.0, blink=(0.3, 0.1)):
+def threeb_spots_block(seed: int, F: int, shape=(12, 12, 9), n_spots: int = 4, variance=1.0, blink=(0.3, 0.1),
+                       background: float = 2.0):
     """Seeded stand-in for one 3B block with several spots, for the Gibbs
     sampler: the mask's voxels [P][3] in the reference's (z, y, x) order, a data
     series [F][P] of Gaussian spots blinking as 2-state Markov chains (on -> off
-    and off -> on probabilities `blink`) over a flat background of 2 plus
-    Gaussian noise, and the spots [K][5] (brightness, blur, x, y, z) near the
-    true ones, in the normalised units 3B works in."""
+    and off -> on probabilities `blink`) over a flat background plus Gaussian
+    noise, and the spots [K][5] (brightness, blur, x, y, z) near the true ones.
+    background 0 is data as 3B's preprocessing leaves it (background removed,
+    unit noise: load_and_normalize_images, storm_imagery.cc:358-410); 3B's
+    model has no background term, so a constant offset pulls the fitted blur
+    wide."""
     rng = np.random.default_rng(seed)
     X, Y, Z = shape
     zz, yy, xx = np.meshgrid(np.arange(Z), np.arange(Y), np.arange(X), indexing="ij")
@@ -294,7 +298,7 @@ def threeb_spots_block(seed: int, F: int, shape=(12, 12, 9), n_spots: int = 4, v
         on[f] = state
         flip = rng.random(n_spots)
         state = np.where(state, flip >= blink[0], flip < blink[1])
-    pix = 2.0 + on.astype(np.float64) @ shapes + rng.normal(0, np.sqrt(variance), (F, len(pixels)))
+    pix = background + on.astype(np.float64) @ shapes + rng.normal(0, np.sqrt(variance), (F, len(pixels)))
     spots = np.column_stack([bright * rng.uniform(0.9, 1.1, n_spots), blur * rng.uniform(0.95, 1.05, n_spots),
                              centres + rng.normal(0, 0.2, (n_spots, 3))])
     return pix, pixels, spots

@@ -206,3 +206,18 @@ def test_pass_moves_spots_towards_the_data_and_ejects(ctx):
     kept, _ = ctx.optimise_pass_3b(m, pix, pixels, far, pass_index=0, main_samples=4, cg_max_iterations=1, limit=lim,
                                    seed=3)
     assert len(kept) == 4
+
+
+def test_free_energies_side_by_side_equal_single_runs(ctx):
+    """Two models' chains in one launch (a model comparison) give each model the
+    value of its own single run with the same seed, bit for bit: a frame's work
+    stays on one CTA in the same order whatever the grid."""
+    from rfba_gb300 import synth
+    pix, pixels, spots = synth.threeb_spots_block(41, 30, (12, 12, 9), 3, background=0.0)
+    m = _model()
+    a, b = spots, spots[:2]
+    pair = ctx.free_energies_3b(m, pix, pixels, [a, b], samples=60, seeds=(5, 9))
+    one_a, _ = ctx.free_energy_3b(m, pix, pixels, a, samples=60, seed=5)
+    one_b, _ = ctx.free_energy_3b(m, pix, pixels, b, samples=60, seed=9)
+    assert pair.tolist() == [one_a, one_b]
+    assert ctx.free_energies_3b(m, pix, pixels, [b], samples=60, seeds=(9,)).tolist() == [one_b]
