@@ -498,6 +498,16 @@ int rfba_3b_fit(rfba_ctx* ctx, const rfba_3b_model* model, const double* pixel_i
                 int P, double* spots, int* nspots, int capacity, const rfba_3b_fit_params* params,
                 int first_iteration, int iterations, unsigned long long seed, rfba_3b_fit_fn progress, void* user);
 
+/* The masks the library's unmasked sampler (GibbsSampler, used for the model
+ * modification's Hessian draws and rfba_3b_free_energy_hessian) runs with:
+ * each spot's support, the pixels where its Gaussian factor exp(-|x - mu|^2 /
+ * (2 blur^2)), the z difference divided by z_factor, is at least 2^-60, in
+ * pixel order. A frame's on - off log probability, the only part of it the
+ * filter uses, then differs from the all-pixel sums' by less than 2^-60 of
+ * the terms kept. Same outputs as rfba_3b_spot_masks. Host only. */
+int rfba_3b_support_masks(const int* pixels, int P, const double* spots, int K, double z_factor, int* mask_offsets,
+                          int* mask_pixels, long long cap, long long* nnz);
+
 /* Host helpers of the model modification, exported for testing: eigenvalues
  * (ascending) and eigenvectors (rows, largest-magnitude component positive)
  * of a symmetric 5x5 matrix by cyclic Jacobi rotations, and the determinant of

@@ -443,6 +443,29 @@ static void flatten_masks(const std::vector<std::vector<int> >& masks, size_t co
     }
 }
 
+// ln(2^-60): a spot's support is the pixels where its Gaussian factor is at
+// least 2^-60 (threeb.cu's double-float gradient uses the same cut).
+static constexpr double kSupportS = -41.58883083359672;
+
+// The unmasked sampler's masks (GibbsSampler sums over every pixel): each
+// spot's support in pixel order. The terms left out change a frame's on - off
+// log probability, the only part of it the filter uses, by less than 2^-60 of
+// the terms kept, far under the rounding of the all-pixel sums.
+static void support_masks(const int* pixels, int P, const std::vector<Spot>& sp, double zf, std::vector<int>* off,
+                          std::vector<int>* idx) {
+    off->assign(sp.size() + 1, 0);
+    idx->clear();
+    for (size_t k = 0; k < sp.size(); ++k) {
+        const Spot& s = sp[k];
+        for (int q = 0; q < P; ++q) {
+            const double d0 = pixels[3 * q] - s[2], d1 = pixels[3 * q + 1] - s[3], d2 = (pixels[3 * q + 2] - s[4]) / zf;
+            const double e = -(d0 * d0 + d1 * d1 + d2 * d2) / (2 * s[1] * s[1]);
+            if (e >= kSupportS) idx->push_back(q);
+        }
+        (*off)[k + 1] = (int)idx->size();
+    }
+}
+
 static int upload_spots(rfba_ctx* ctx, const std::vector<Spot>& sp, cudaStream_t st, int set = 0) {
     int s;
     if ((s = ctx->gb[set].spots.ensure(sp.size() * 40 + 8, "3B spots"))) return s;
@@ -747,17 +770,13 @@ static double diff_log_log_normal(double x, double mu, double sigma) {
 // hess + its priors' second derivatives and deriv + its priors' first
 // derivatives; the sums of hess and of deriv deriv^T over the draws, over
 // (samples variance), less the outer product of the mean deriv.
-static int free_energy_hessian_dev(rfba_ctx* ctx, const rfba_3b_model* m, int F, int P, const std::vector<Spot>& sp,
-                                   int which, int samples, int sweeps, unsigned long long seed, double hess[25],
-                                   cudaStream_t st) {
+static int free_energy_hessian_dev(rfba_ctx* ctx, const rfba_3b_model* m, const int* pixels, int F, int P,
+                                   const std::vector<Spot>& sp, int which, int samples, int sweeps,
+                                   unsigned long long seed, double hess[25], cudaStream_t st) {
     int s;
     const int K = (int)sp.size();
-    std::vector<int> hoff((size_t)K + 1), hidx((size_t)K * P);
-    for (int k = 0; k < K; ++k) {
-        hoff[k] = k * P;
-        for (int q = 0; q < P; ++q) hidx[(size_t)k * P + q] = q;
-    }
-    hoff[K] = K * P;
+    std::vector<int> hoff, hidx;
+    support_masks(pixels, P, sp, m->z_factor, &hoff, &hidx);
     if ((s = upload_spots(ctx, sp, st))) return s;
     GibbsCall c;
     c.K = K;
@@ -1025,12 +1044,8 @@ static int modify_core(rfba_ctx* ctx, const rfba_3b_model* m, const int* pixels,
         rec->position_log_prior = pos_lp;
         // the Hessian at model 2's spot on GibbsSampler draws over all pixels
         // (multispot5.cc:2050-2075)
-        std::vector<int> hoff((size_t)model2.size() + 1), hidx((size_t)model2.size() * P);
-        for (size_t k = 0; k < model2.size(); ++k) {
-            hoff[k] = (int)(k * P);
-            for (int p = 0; p < P; ++p) hidx[k * P + p] = p;
-        }
-        hoff[model2.size()] = (int)(model2.size() * P);
+        std::vector<int> hoff, hidx;
+        support_masks(pixels, P, model2, m->z_factor, &hoff, &hidx);
         const int S = prm.h_outer_samples;
         auto t0 = clock();
         if ((s = draws_without(ctx, m, F, P, model2, hoff, hidx, S, prm.sweeps, spot, mix_seed(seed, 3, 0), st)))
@@ -1453,7 +1468,7 @@ int rfba_3b_free_energy_hessian(rfba_ctx* ctx, const rfba_3b_model* m, const dou
     for (int k = 0; k < K; ++k)
         for (int n = 0; n < 5; ++n) sp[k][n] = spots[5 * k + n];
     if ((s = stage_block(ctx, pixel_intensities, pixels, F, P, st))) return s;
-    return free_energy_hessian_dev(ctx, m, F, P, sp, spot, samples, sweeps, seed, hess, st);
+    return free_energy_hessian_dev(ctx, m, pixels, F, P, sp, spot, samples, sweeps, seed, hess, st);
 }
 
 // NegativeFreeEnergy::compute_with_mask for one or two models side by side
@@ -1501,6 +1516,23 @@ int rfba_3b_free_energy_models(rfba_ctx* ctx, const rfba_3b_model* m, const doub
     double en[2];
     if ((s = model_energies(ctx, m, F, P, nmodels, models, mk, samples, sweeps, seeds, st, en))) return s;
     for (int i = 0; i < nmodels; ++i) values[i] = -en[i];
+    return RFBA_OK;
+}
+
+int rfba_3b_support_masks(const int* pixels, int P, const double* spots, int K, double z_factor, int* mask_offsets,
+                          int* mask_pixels, long long cap, long long* nnz) {
+    if (!pixels || P < 1 || K < 0 || (K > 0 && !spots) || !mask_offsets || !nnz || z_factor == 0) {
+        set_error("null argument, bad sizes or z_factor 0");
+        return RFBA_ERR_INVALID;
+    }
+    std::vector<Spot> sp((size_t)K);
+    for (int k = 0; k < K; ++k)
+        for (int n = 0; n < 5; ++n) sp[k][n] = spots[5 * k + n];
+    std::vector<int> off, idx;
+    support_masks(pixels, P, sp, z_factor, &off, &idx);
+    std::memcpy(mask_offsets, off.data(), off.size() * sizeof(int));
+    if (mask_pixels) std::memcpy(mask_pixels, idx.data(), std::min<size_t>(idx.size(), (size_t)std::max(cap, 0LL)) * 4);
+    *nnz = (long long)idx.size();
     return RFBA_OK;
 }
 

@@ -252,6 +252,8 @@ def lib():
                                                   ull, dp]
         L.rfba_3b_free_energy_models.argtypes = [vp, ctypes.POINTER(ThreeBModel), vp, vp, ctypes.c_int, ctypes.c_int,
                                                  ctypes.c_int, vp, vp, vp, vp, ctypes.c_int, ctypes.c_int, vp, dp]
+        L.rfba_3b_support_masks.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int, ctypes.c_double, vp, vp,
+                                            ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)]
         L.rfba_sym_eigen5.argtypes = [dp, dp, dp]
         L.rfba_det5.argtypes = [dp]
         L.rfba_det5.restype = ctypes.c_double
@@ -938,6 +940,23 @@ def spot_masks_3b(pixels, spots):
     idx = np.zeros(max(nnz.value, 1), np.int32)
     _check(lib().rfba_3b_spot_masks(vp(px.ctypes.data), P, vp(sp.ctypes.data), K, vp(off.ctypes.data),
                                     vp(idx.ctypes.data), nnz.value, ctypes.byref(nnz)))
+    return off, idx[:nnz.value]
+
+
+def support_masks_3b(pixels, spots, z_factor: float = 1.0):
+    """Each spot's support (Gaussian factor >= 2^-60) in pixel order, the masks of
+    the library's unmasked sampler: (offsets [K+1], indices). Host only."""
+    px = np.ascontiguousarray(pixels, np.int32)
+    sp = np.ascontiguousarray(spots, np.float64).reshape(-1, 5)
+    K, P = len(sp), len(px)
+    off = np.zeros(K + 1, np.int32)
+    nnz = ctypes.c_longlong()
+    vp = ctypes.c_void_p
+    _check(lib().rfba_3b_support_masks(vp(px.ctypes.data), P, vp(sp.ctypes.data), K, float(z_factor),
+                                       vp(off.ctypes.data), None, 0, ctypes.byref(nnz)))
+    idx = np.zeros(max(nnz.value, 1), np.int32)
+    _check(lib().rfba_3b_support_masks(vp(px.ctypes.data), P, vp(sp.ctypes.data), K, float(z_factor),
+                                       vp(off.ctypes.data), vp(idx.ctypes.data), nnz.value, ctypes.byref(nnz)))
     return off, idx[:nnz.value]
 
 

@@ -121,3 +121,19 @@ def test_free_energy_hessian_oracle_matches_reference():
         want = G.ref_free_energy_hessian_draws(pix, pixels, spots, spot, st, ints, **MODEL)
         got = G.free_energy_hessian_draws(pix, pixels, spots, spot, st, ints, **MODEL)
         assert np.max(np.abs(got[IU] - want[IU])) <= 1e-12 * np.abs(want[IU]).max()
+
+
+def test_support_masks_are_the_spots_supports():
+    """rfba_3b_support_masks: each spot's pixels with Gaussian factor >= 2^-60 (z
+    scaled by the z factor), in pixel order."""
+    from rfba_gb300 import srrf, synth
+    for zf in (1.0, 1.7):
+        pix, pixels, spots = synth.threeb_spots_block(12, 4, (29, 21, 17), 5)
+        off, idx = srrf.support_masks_3b(pixels, spots, zf)
+        d = (pixels[None, :, :] - spots[:, None, 2:]).astype(np.float64)
+        d[:, :, 2] /= zf
+        e = -(d ** 2).sum(2) / (2 * spots[:, 1:2] ** 2)
+        for k in range(len(spots)):
+            want = np.nonzero(e[k] >= -41.58883083359672)[0]
+            np.testing.assert_array_equal(idx[off[k]:off[k + 1]], want)
+        assert 0 < off[1] < len(pixels)  # a support cut by the threshold, not the block

@@ -77,14 +77,15 @@ def test_argument_checks(ctx):
 
 def test_free_energy_hessian_replays_its_draws(ctx):
     """rfba_3b_free_energy_hessian against the oracle given the same draws: the
-    unmasked sampler is rfba_3b_gibbs_sample with every pixel in every mask and
-    the same seed, so the GPU's draws are replayed exactly."""
+    unmasked sampler is rfba_3b_gibbs_sample with each spot's support as its
+    mask (rfba_3b_support_masks) and the same seed, so the GPU's draws are
+    replayed exactly."""
     from oracle import gibbs_oracle as G
-    from rfba_gb300 import synth
+    from rfba_gb300 import srrf, synth
     pix, pixels, spots = synth.threeb_spots_block(8, 20, (9, 9, 9), 3)
     m = _model(A_MAIN, PI_MAIN)
     P, K = len(pixels), len(spots)
-    masks = (np.arange(K + 1, dtype=np.int32) * P, np.tile(np.arange(P, dtype=np.int32), K))
+    masks = srrf.support_masks_3b(pixels, spots, 1.0)
     st, ints = ctx.gibbs_sample_3b(m, pix, pixels, spots, masks, sweeps=1, n_draws=12, seed=21)
     for spot in range(K):
         got = ctx.free_energy_hessian_3b(m, pix, pixels, spots, spot, samples=12, seed=21)
