@@ -117,17 +117,17 @@ __device__ __forceinline__ void forward_filter(int lane, int F, const double* A,
         int Em = kZeroExp;
 #pragma unroll
         for (int i = 0; i < 3; ++i) Em = (nz[i] && Ev[i] > Em) ? Ev[i] : Em;
-        float2 y = make_float2(0.f, 0.f);
+        float2 tm[3];
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
             const int dd = Ev[i] - Em;
             const bool use = nz[i] && Ev[i] != kZeroExp && dd >= -kDropBits;
             const float sc = use ? pow2f(dd < -126 ? -126 : dd) : 0.f;
-            float2 tm = df_mul(Aj[i], xv[i]);
-            tm.x *= sc;
-            tm.y *= sc;
-            y = df_add(y, tm);
+            tm[i] = df_mul(Aj[i], xv[i]);
+            tm[i].x *= sc;
+            tm[i].y *= sc;
         }
+        const float2 y = df_add(df_add(tm[0], tm[1]), tm[2]);
         normalise(df_mul(y, mant), (Em == kZeroExp || ke == kZeroExp) ? kZeroExp : Em + ke);
         xs[3 * t + j] = x;
         es[3 * t + j] = E;
@@ -191,6 +191,46 @@ __device__ __forceinline__ void transition_floats(const double* A, float Af[9], 
         m |= A[n] != 0.0 ? 1u << n : 0u;
     }
     *nzA = m;
+}
+
+// The backward walk through a decision table, by one warp: sel[4t + n] is the
+// state frame t takes when frame t + 1 holds n (n = 3: no next frame), so
+// frame t's decisions are a map from {0..3} to {0..2}, packed here as four
+// 2-bit fields. The walk s_t = f_t(s_{t+1}), s_F = 3, is a suffix composition
+// of those maps: each lane composes the maps of its chunk of frames, a
+// Kogge-Stone scan over the lanes composes the chunks that follow, and each
+// lane then walks its own chunk from the state its successors hand it.
+__device__ __forceinline__ unsigned map_compose(unsigned g, unsigned h) {  // g after h: n -> g(h(n))
+    unsigned r = 0;
+#pragma unroll
+    for (int n = 0; n < 4; ++n) r |= ((g >> (2 * ((h >> (2 * n)) & 3u))) & 3u) << (2 * n);
+    return r;
+}
+__device__ __forceinline__ void walk_decisions(int lane, int F, const unsigned char* sel, unsigned char* sts) {
+    const unsigned full = 0xffffffffu;
+    const int per = (F + 31) / 32;
+    const int a = min(F, lane * per), b = min(F, a + per);
+    auto code = [&](int t) {
+        const unsigned w = *reinterpret_cast<const unsigned*>(sel + 4 * t);  // four decision bytes
+        return (w & 3u) | ((w >> 6) & 0xCu) | ((w >> 12) & 0x30u) | ((w >> 18) & 0xC0u);
+    };
+    // this chunk's map: s_a from s_b
+    unsigned h = 0xE4u;  // identity
+    for (int t = b - 1; t >= a; --t) h = map_compose(code(t), h);
+    // suffix scan: H_l = h_l after h_(l+1) after ... (lanes past the last frame hold the identity)
+    unsigned H = h;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned nxt = __shfl_down_sync(full, H, o);
+        if (lane + o < 32) H = map_compose(H, nxt);
+    }
+    // the state of frame b (the chunk after this one's first frame) is H_(l+1)(3)
+    const unsigned after = __shfl_down_sync(full, H, 1);
+    int s = lane + 1 < 32 ? (int)((after >> 6) & 3u) : 3;
+    for (int t = b - 1; t >= a; --t) {
+        s = sel[4 * t + s];
+        sts[t] = (unsigned char)s;
+    }
 }
 
 // 53-bit integer uniform of Philox outputs a, b (u53 = U 2^-53)

@@ -238,13 +238,7 @@ __global__ void __launch_bounds__(kGibbsThreads) gibbs_chain_kernel(const GibbsP
                     ffbs::frame_draws(t, ffbs::uniform53(cc[0], cc[1]), xs, es, Af, nzA, sel + 4 * t);
                 }
                 __syncthreads();
-                if (threadIdx.x == 0) {
-                    int next = 3;
-                    for (int t = F - 1; t >= 0; --t) {
-                        next = sel[4 * t + next];
-                        sts[t] = (unsigned char)next;
-                    }
-                }
+                if (threadIdx.x < 32) ffbs::walk_decisions(threadIdx.x, F, sel, sts);
                 __syncthreads();
                 // phase C: record the drawn states of this CTA's frames and add spot
                 // k back where it is on
