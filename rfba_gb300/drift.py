@@ -58,14 +58,71 @@ def grad_map(m):
     return torch.where(torch.isnan(m), torch.zeros_like(m), -f / torch.sqrt((f.double() ** 2).sum()).float())
 
 
+def make_objective(kind: str = "l2", p: float = 8.0, border: int = 0):
+    """(value, dL/dmap) of a sharpness objective on the map's finite voxels,
+    for `refine_drift`. `border` output voxels are left out on every side.
+
+    kind "l2":       L = -||m||_2 (the default objective above).
+    kind "lp":       L = -(sum max(m, 0)^p)^(1/p): the positive peaks weigh
+                     more as p grows.
+    kind "kurtosis": L = -N sum m^4 / (sum m^2)^2, scale-free.
+    Sums are float64; the gradient is float32 with zeros on NaN voxels and in
+    the border."""
+    import torch
+
+    def inner(m):
+        f = torch.nan_to_num(m, nan=0.0).double()
+        return f[border:-border, border:-border, border:-border] if border else f
+
+    def value(m):
+        f = inner(m)
+        if kind == "l2":
+            return -torch.sqrt((f * f).sum())
+        if kind == "lp":
+            q = torch.clamp(f, min=0.0)
+            s = q.max()
+            return -s * ((q / s) ** p).sum() ** (1.0 / p) if float(s.detach()) > 0 else -s
+        if kind == "kurtosis":
+            return -f.numel() * (f ** 4).sum() / (f * f).sum() ** 2
+        raise ValueError(f"unknown objective {kind!r}")
+
+    def grad(m):
+        f = inner(m)
+        if kind == "l2":
+            gi = -f / torch.sqrt((f * f).sum())
+        elif kind == "lp":
+            q = torch.clamp(f, min=0.0)
+            s = q.max()
+            if float(s) > 0:
+                r = q / s
+                gi = -(r ** (p - 1)) * (r ** p).sum() ** (1.0 / p - 1.0)
+            else:
+                gi = torch.zeros_like(f)
+        elif kind == "kurtosis":
+            s2, s4 = (f * f).sum(), (f ** 4).sum()
+            gi = -f.numel() * (4 * f ** 3 / s2 ** 2 - 4 * s4 * f / s2 ** 3)
+        else:
+            raise ValueError(f"unknown objective {kind!r}")
+        g = torch.zeros(m.shape, dtype=torch.float64, device=m.device)
+        if border:
+            g[border:-border, border:-border, border:-border] = gi
+        else:
+            g = gi
+        return torch.where(torch.isnan(m), torch.zeros_like(m), g.float()).contiguous()
+
+    return value, grad
+
+
 def refine_drift(ctx, cfg, x, iters: int, start=None, lr: float = 0.03, betas=(0.9, 0.999), eps: float = 1e-12,
-                 checkpoint=None, resume: bool = False, stream=None):
+                 checkpoint=None, resume: bool = False, stream=None, grad_fn=None):
     """Run Adam on the shifts until `iters` iterations are done.
 
-    ctx: rfba_gb300.srrf.Context; cfg: Config (TRA, or TRAC with ITC 0);
+    ctx: rfba_gb300.srrf.Context; cfg: Config (any temporal method);
     x: CUDA float32 tensor [T][D][H][W]; start: initial shifts [T][3] (default
     0); checkpoint: file written after every iteration; resume: continue from
-    that file when it exists. Returns (DriftState, map of the final shifts)."""
+    that file when it exists; grad_fn: dL/dmap of the objective minimised
+    (default `grad_map`, L = -||map||_2; `make_objective` gives others).
+    Returns (DriftState, map of the final shifts)."""
     import torch
     T = x.shape[0]
     dev = x.device
@@ -84,7 +141,7 @@ def refine_drift(ctx, cfg, x, iters: int, start=None, lr: float = 0.03, betas=(0
     m = None
     for it in range(st.it, iters):
         m = ctx.forward_shifted(cfg, x, sh, out=m, stream=s)
-        _, gs = ctx.backward(cfg, x, sh, grad_map(m), stream=s)
+        _, gs = ctx.backward(cfg, x, sh, (grad_fn or grad_map)(m), stream=s)
         mom = b1 * mom + (1 - b1) * gs
         var = b2 * var + (1 - b2) * gs * gs
         sh = sh - lr * (mom / (1 - b1 ** (it + 1))) / (torch.sqrt(var / (1 - b2 ** (it + 1))) + eps)
