@@ -686,6 +686,24 @@ def measure_large(ctx, iters: int = 20, volumes=None) -> dict:
     plain_s = time.perf_counter() - t0
     del x, plain_out
     stream = torch.cuda.current_stream()
+    # The forward alone (no drift correction), device input: the frames in time
+    # batches of 25 volumes with the TRAC-4 window sums carried between them
+    # (the automatic choice when the whole series' stacks exceed the scratch
+    # budget), and the map in z slices of all 200 volumes.
+    whole = {}
+    for name, tbv in (("time_batches", 0), ("z_slices", -1)):
+        ctx.set_time_batch(tbv)
+        mm = ctx.forward(cfg, xd, stream=stream.cuda_stream)  # schedule tuning and graph capture
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        ctx.forward(cfg, xd, out=mm, stream=stream.cuda_stream)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        vb, nb = ctx.last_time_batches()
+        whole[name] = {"forward_s": ev0.elapsed_time(ev1) / 1e3, "batch_volumes": vb, "batches": nb,
+                       "z_slices": ctx.last_passes(), "value": units / (ev0.elapsed_time(ev1) / 1e3)}
+        del mm
+    ctx.set_time_batch(0)
 
     objective, grad_map = drift.objective, drift.grad_map
 
@@ -721,7 +739,7 @@ def measure_large(ctx, iters: int = 20, volumes=None) -> dict:
             "refine_iterations": iters, "refine_wall_s": wall_s, "refine_s_per_iteration": wall_s / max(iters, 1),
             "objective_before": L0, "objective_after": float(objective(m)),
             "drift_rms_error_before": rms0, "drift_rms_error_after": rms(sh),
-            "plain_forward_s": plain_s, "plain_blocks": gn,
+            "plain_forward_s": plain_s, "plain_blocks": gn, "forward_only": whole,
             "plain_note": "GradientCalc 16^3 blocks, border 2, one launch sequence and copy pair per block",
             "batched_forward_speedup_vs_plain": plain_s / (fwd_ms / 1e3)}
 

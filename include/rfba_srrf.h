@@ -538,6 +538,24 @@ int rfba_ctx_last_timing(rfba_ctx* ctx, double* radiality_ms, double* temporal_m
 /* Launch overrides for tuning: CTAs of the radiality kernel and time points per
  * work item (0 = automatic). */
 int rfba_ctx_set_launch(rfba_ctx* ctx, int grid, int t_chunk);
+/* Time batches of rfba_srrf_forward / rfba_srrf_forward_blocks. A series whose
+ * radiality and intensity stacks fit the context's scratch budget is reduced
+ * whole; a longer one runs in batches of 25 volumes: the radiality of a batch
+ * fills its stacks, then its values are folded into a per-subvoxel temporal
+ * state carried to the next batch (TRM, TRA, TRPPM: the same sums in the same
+ * order, maps bit-identical to the one-pass reduction; TRAC with ITC 0: the
+ * cumulant window sums around the first batch's mean, combined in double at
+ * the end, equal to rounding). The map is cut into z slices only where one
+ * batch's stacks and the state still exceed the budget. TRAC with ITC 1 bins
+ * the whole series and slices space instead. volumes > 0 forces batches of that
+ * many volumes, < 0 turns batches off, 0 restores the automatic choice. The
+ * reference holds its whole series in memory (GradientCalc.cpp, one block at a
+ * time); the batches correspond to streaming the series' frames through HBM. */
+int rfba_ctx_set_time_batch(rfba_ctx* ctx, int volumes);
+/* Volumes per batch and batches of the last forward (0, 0: one pass over the
+ * whole series), and its spatial passes (z slices or groups of blocks whose
+ * stacks fit the budget together; 1 when everything fit at once). */
+int rfba_ctx_last_time_batches(rfba_ctx* ctx, int* volumes, int* batches, int* passes);
 /* SRRF-guided spot seeding: replaces the rejection loops of
  * multispot5_place_methods.cc:291-341 (place_spots_intensity_sampled) and
  * multispot5.cc:2164-2231 (InitGuide / GetPoint). Candidates are the mag^3

@@ -154,12 +154,14 @@ int order_streams(rfba_ctx* ctx, cudaStream_t st) {
 // Turn caller blocks into device block descriptors, splitting regions along z
 // so that one pass's radiality + intensity stack fits the scratch budget.
 static int make_blocks(rfba_ctx* ctx, const rfba_srrf_config& cfg, const int dims[4], const rfba_block* blocks,
-                       int nblocks, std::vector<BlockDev>* outb, int ty = 0) {
+                       int nblocks, std::vector<BlockDev>* outb, int ty = 0, int tb = 0, int fields = 0) {
     const RingPlan& rp = ctx->plan.ring;
     const int T = dims[3];
     const int FZ = fz_for(cfg.mag[2]);
     outb->clear();
-    const size_t per_vox = (size_t)T * 2 * sizeof(float);
+    // bytes per subvoxel: the stacks of the volumes held at once plus the
+    // carried temporal state when the series runs in time batches
+    const size_t per_vox = (size_t)(tb > 0 ? tb : T) * 2 * sizeof(float) + (size_t)fields * sizeof(float);
     const long long max_vox = std::max<long long>((long long)(ctx->budget / per_vox), 1);
     for (int i = 0; i < nblocks; ++i) {
         const rfba_block& b = blocks[i];
@@ -264,12 +266,18 @@ static RadParams fill_rad_params(rfba_ctx* ctx, const rfba_srrf_config& cfg, con
 static int plan_passes(rfba_ctx* ctx, const rfba_srrf_config& cfg, rfba_dtype dtype, const int dims[4],
                        const std::vector<BlockDev>& all, const Tuning& tune, PassSet* ps) {
     const int T = dims[3];
-    const size_t per_vox = (size_t)T * sizeof(float);
+    // volumes the stacks hold at once, and the carried state of time batches
+    const int stack_t = tune.tb > 0 ? std::min(tune.tb, T) : T;
+    ps->tb = tune.tb > 0 ? stack_t : 0;
+    ps->fields = ps->tb > 0 ? temporal_stream_fields(cfg.method, cfg.trac_order) : 0;
+    ps->nbatch = (T + stack_t - 1) / stack_t;
+    const size_t per_vox = (size_t)stack_t * 2 * sizeof(float) + (size_t)ps->fields * sizeof(float);
     ps->blocks.clear();
     ps->tiles.clear();
     ps->prefix.clear();
     ps->passes.clear();
     ps->max_stack = 0;
+    ps->max_vox = 0;
     ps->ty = tune.ty > 0 ? tune.ty : tile_rows_for_mag(cfg.mag[1]);
     RadParams rp = fill_rad_params(ctx, cfg, nullptr, dims, cz_for_mag(cfg.mag[2]), ps->ty);
     rp.tma_bx = radiality_tma_box_x(rp, dtype == RFBA_U16);
@@ -292,7 +300,7 @@ static int plan_passes(rfba_ctx* ctx, const rfba_srrf_config& cfg, rfba_dtype dt
         long long vox = 0;
         while (i1 < all.size()) {
             const long long nv = vox + all[i1].vox;
-            if (i1 > i0 && (size_t)nv * per_vox * 2 > ctx->budget) break;
+            if (i1 > i0 && (size_t)nv * per_vox > ctx->budget) break;
             vox = nv;
             ++i1;
         }
@@ -305,7 +313,7 @@ static int plan_passes(rfba_ctx* ctx, const rfba_srrf_config& cfg, rfba_dtype dt
         for (size_t b = i0; b < i1; ++b) {
             BlockDev d = all[b];
             d.stack_off = off;
-            off += d.vox * T;
+            off += d.vox * stack_t;
             pre += d.vox;
             ps->prefix.push_back(pre);
             ps->blocks.push_back(d);
@@ -339,17 +347,19 @@ static int plan_passes(rfba_ctx* ctx, const rfba_srrf_config& cfg, rfba_dtype dt
         pp.t1 = ps->tiles.size();
         pp.stack_elems = off;
         pp.units = vox * T;
+        pp.vox = vox;
+        ps->max_vox = std::max(ps->max_vox, vox);
         const long long nt = (long long)(pp.t1 - pp.t0);
         // time chunk: enough work items for ~8 per CTA slot
         int chunk = ctx->chunk_override;
         if (chunk <= 0) {
             const long long want = 8LL * slots;
             long long nch = (want + nt - 1) / nt;
-            nch = std::max<long long>(1, std::min<long long>(nch, T));
-            chunk = (int)((T + nch - 1) / nch);
+            nch = std::max<long long>(1, std::min<long long>(nch, stack_t));
+            chunk = (int)((stack_t + nch - 1) / nch);
         }
         pp.chunk = chunk;
-        pp.nchunks = (T + chunk - 1) / chunk;
+        pp.nchunks = (stack_t + chunk - 1) / chunk;
         pp.nitems = nt * pp.nchunks;
         int grid = ctx->grid_override > 0 ? ctx->grid_override : slots;
         grid = (int)std::min<long long>(grid, pp.nitems);
@@ -373,10 +383,11 @@ static int enqueue_passes(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void
     auto rec = [&](cudaEvent_t e) {
         return capturing ? cudaEventRecordWithFlags(e, st, cudaEventRecordExternal) : cudaEventRecord(e, st);
     };
+    const int T = dims[3];
+    const int tb = ps.tb > 0 ? ps.tb : T;
     for (size_t i = 0; i < ps.passes.size(); ++i) {
         const PassPlan& pp = ps.passes[i];
         unsigned int* counter = dcounters + 64 * i;
-        RFBA_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned int), st), "counter reset");
         RadParams rp = fill_rad_params(ctx, cfg, in_dev, dims, cz_for_mag(cfg.mag[2]), ps.ty);
         rp.tma_bx = radiality_tma_box_x(rp, dtype == RFBA_U16);
         rp.err = static_cast<unsigned long long*>(ctx->errw.p);
@@ -404,16 +415,59 @@ static int enqueue_passes(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void
         tp.rad_stack = rp.rad_stack;
         tp.int_stack = rp.int_stack;
         tp.out = out_dev;
+        StreamParams sp;
+        std::memset(&sp, 0, sizeof sp);
+        sp.blocks = tp.blocks;
+        sp.vox_prefix = tp.vox_prefix;
+        sp.nblocks = tp.nblocks;
+        sp.total_vox = tp.total_vox;
+        sp.T = T;
+        sp.method = cfg.method;
+        sp.order = cfg.trac_order;
+        sp.iw = cfg.intensity_w;
+        sp.state = static_cast<float*>(ctx->tstate.p);
+        sp.state_stride = ps.max_vox;
+        sp.rad_stack = rp.rad_stack;
+        sp.int_stack = rp.int_stack;
+        sp.out = out_dev;
+        // Time batches: the radiality of volumes [t_lo, t_hi) into the stacks,
+        // then that batch folded into the carried state (the map after the
+        // last). With the whole series in one batch the stacks hold it all and
+        // the one-pass temporal kernel reduces them. The events time the
+        // radiality launches (with the carries of all batches but the last)
+        // and the last temporal launch.
         if (evs) RFBA_CUDA(rec(evs[3 * i]), "event");
-        int le = launch_radiality(rp, pp.grid, pp.smem, dtype == RFBA_U16, st);
-        if (le != 0) return cuda_fail((cudaError_t)le, "radiality launch");
-        if (evs) RFBA_CUDA(rec(evs[3 * i + 1]), "event");
-        le = launch_temporal(tp, st);
-        if (le != 0) return cuda_fail((cudaError_t)le, "temporal launch");
+        for (int b = 0; b < ps.nbatch; ++b) {
+            RadParams rb = rp;
+            rb.t_lo = b * tb;
+            rb.t_hi = std::min(T, rb.t_lo + tb);
+            rb.stack_t0 = ps.tb > 0 ? rb.t_lo : 0;
+            rb.nchunks = (rb.t_hi - rb.t_lo + pp.chunk - 1) / pp.chunk;
+            rb.nitems = (long long)rb.ntiles * rb.nchunks;
+            const int grid = (int)std::max<long long>(1, std::min<long long>(pp.grid, rb.nitems));
+            RFBA_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned int), st), "counter reset");
+            int le = launch_radiality(rb, grid, pp.smem, dtype == RFBA_U16, st);
+            if (le != 0) return cuda_fail((cudaError_t)le, "radiality launch");
+            if (ps.tb > 0) {
+                const bool last = b == ps.nbatch - 1;
+                if (last && evs) RFBA_CUDA(rec(evs[3 * i + 1]), "event");
+                sp.t_lo = rb.t_lo;
+                sp.t_hi = rb.t_hi;
+                sp.last = last ? 1 : 0;
+                le = launch_temporal_stream(sp, st);
+                if (le != 0) return cuda_fail((cudaError_t)le, "temporal launch");
+            }
+        }
+        if (ps.tb == 0) {
+            if (evs) RFBA_CUDA(rec(evs[3 * i + 1]), "event");
+            const int le = launch_temporal(tp, st);
+            if (le != 0) return cuda_fail((cudaError_t)le, "temporal launch");
+        }
         if (evs) RFBA_CUDA(rec(evs[3 * i + 2]), "event");
         if (verbose())
-            std::fprintf(stderr, "rfba: pass blocks=%zu tiles=%d ty=%d chunk=%d items=%lld grid=%d smem=%zu\n",
-                         pp.b1 - pp.b0, rp.ntiles, ps.ty, pp.chunk, pp.nitems, pp.grid, pp.smem);
+            std::fprintf(stderr,
+                         "rfba: pass blocks=%zu tiles=%d ty=%d chunk=%d items=%lld grid=%d smem=%zu batches=%d of %d\n",
+                         pp.b1 - pp.b0, rp.ntiles, ps.ty, pp.chunk, pp.nitems, pp.grid, pp.smem, ps.nbatch, tb);
     }
     return RFBA_OK;
 }
@@ -443,7 +497,9 @@ static int collect_timing(rfba_ctx* ctx, const PassSet& ps, const std::vector<cu
 
 static void account(rfba_ctx* ctx, const PassSet& ps) {
     ctx->last_passes = (int)ps.passes.size();
-    ctx->launches += 2 * (long long)ps.passes.size();
+    ctx->launches += 2 * (long long)ps.passes.size() * ps.nbatch;
+    ctx->last_time_batch = ps.tb;
+    ctx->last_batches = ps.tb > 0 ? ps.nbatch : 0;
     ctx->last_flop_units = 0;
     for (const PassPlan& pp : ps.passes) ctx->last_flop_units += pp.units;
 }
@@ -461,6 +517,7 @@ static int run_device(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void* in
     const size_t np = ps.passes.size();
     if ((s = ctx->rad.ensure((size_t)ps.max_stack * 4, "radiality stack"))) return s;
     if ((s = ctx->inten.ensure((size_t)ps.max_stack * 4, "intensity stack"))) return s;
+    if (ps.tb > 0 && (s = ctx->tstate.ensure((size_t)ps.fields * ps.max_vox * 4, "temporal state"))) return s;
     if ((s = ctx->blocks.ensure(ps.blocks.size() * sizeof(BlockDev), "blocks"))) return s;
     if ((s = ctx->tiles.ensure(ps.tiles.size() * sizeof(TileDesc), "tiles"))) return s;
     if ((s = ctx->prefix.ensure(ps.prefix.size() * sizeof(long long), "prefix"))) return s;
@@ -619,6 +676,29 @@ static int autotune(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void* in_d
     return rc;
 }
 
+// Volumes per time batch for a forward (0: the whole series at once). A
+// series whose stacks fit the budget runs whole; a longer one runs in batches
+// of kTimeBatch volumes with the temporal reduction carried between them, so
+// the map is cut into fewer z slices (none when the carried state and one
+// batch's stacks fit). TRAC with ITC 1 bins the whole series and slices
+// instead. rfba_ctx_set_time_batch overrides the choice.
+static constexpr int kTimeBatch = 25;
+static int choose_time_batch(const rfba_ctx* ctx, const rfba_srrf_config& cfg, const int dims[4],
+                             const rfba_block* blocks, int nblocks) {
+    const int T = dims[3];
+    if (cfg.method == 3 && cfg.itc == 1) return 0;
+    if (ctx->time_batch < 0) return 0;
+    if (ctx->time_batch > 0) return ctx->time_batch < T ? ctx->time_batch : 0;
+    double vox = 0.0;
+    for (int i = 0; i < nblocks; ++i) {
+        double v = 1.0;
+        for (int a = 0; a < 3; ++a) v *= std::max(blocks[i].hi[a] - blocks[i].lo[a], 0);
+        vox += v;
+    }
+    if (vox * T * 2 * sizeof(float) <= (double)ctx->budget) return 0;
+    return T > kTimeBatch ? kTimeBatch : 0;
+}
+
 static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const void* in, rfba_dtype dtype,
                                  const int dims[4], const rfba_block* blocks, int nblocks, float* out,
                                  long long out_elems, int flags, cudaStream_t st, bool zero_out, bool fast) {
@@ -635,8 +715,10 @@ static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, con
     RFBA_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
     if ((s = order_streams(ctx, st))) return s;
     if ((s = ensure_plan(ctx, *cfg, st))) return s;
+    const int tb = choose_time_batch(ctx, *cfg, dims, blocks, nblocks);
+    const int tfields = tb > 0 ? temporal_stream_fields(cfg->method, cfg->trac_order) : 0;
     std::vector<BlockDev> all;
-    if ((s = make_blocks(ctx, *cfg, dims, blocks, nblocks, &all))) return s;
+    if ((s = make_blocks(ctx, *cfg, dims, blocks, nblocks, &all, 0, tb, tfields))) return s;
     long long work = 0;
     for (const BlockDev& b : all) {
         const long long last = b.out_offset + (long long)(b.nreg[0] - 1) * b.out_stride[0] +
@@ -677,8 +759,9 @@ static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, con
             ctx->last_tuned = 1;
         }
         if (tune.ty > 0 && tune.ty != tile_rows_for_mag(cfg->mag[1]) &&
-            (s = make_blocks(ctx, *cfg, dims, blocks, nblocks, &all, tune.ty)))
+            (s = make_blocks(ctx, *cfg, dims, blocks, nblocks, &all, tune.ty, tb, tfields)))
             return s;
+        tune.tb = tb;
         ctx->last_ty = tune.ty > 0 ? tune.ty : tile_rows_for_mag(cfg->mag[1]);
         ctx->last_order = tune.order;
         // replay: the whole call as one CUDA graph (device pointers, or pinned host buffers)
@@ -692,10 +775,12 @@ static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, con
             key_put(&gkey, &zero_out, 1);
             const int stall = test_tma_stall();
             key_put(&gkey, &stall, 1);
+            key_put(&gkey, &tb, 1);
             key_put(&gkey, blocks, (size_t)nblocks);
             const bool host = flags == RFBA_HOST_PTRS;
             auto deps_now = [&]() {
-                return std::vector<const void*>{ctx->rad.p, ctx->inten.p, ctx->tables.p, ctx->errw.p,
+                return std::vector<const void*>{ctx->rad.p,   ctx->inten.p, ctx->tables.p,
+                                                ctx->errw.p,  ctx->tstate.p,
                                                 host ? ctx->in.p : nullptr, host ? ctx->out.p : nullptr};
             };
             GraphPlan* gp = nullptr;
@@ -717,6 +802,9 @@ static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, con
                 const size_t np = ps.passes.size();
                 if ((s = ctx->rad.ensure((size_t)ps.max_stack * 4, "radiality stack"))) return s;
                 if ((s = ctx->inten.ensure((size_t)ps.max_stack * 4, "intensity stack"))) return s;
+                if (ps.tb > 0 &&
+                    (s = ctx->tstate.ensure((size_t)ps.fields * ps.max_vox * 4, "temporal state")))
+                    return s;
                 if (host) {
                     if ((s = ctx->in.ensure(in_bytes, "input"))) return s;
                     if ((s = ctx->out.ensure((size_t)out_elems * 4, "output"))) return s;
@@ -806,7 +894,9 @@ static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, con
     } else if (zero_out) {
         RFBA_CUDA(cudaMemsetAsync(out_dev, 0, (size_t)out_elems * 4, st), "output clear");
     }
-    if ((s = run_device(ctx, *cfg, in_dev, dtype, dims, all, out_dev, st))) return s;
+    Tuning plain;
+    plain.tb = tb;
+    if ((s = run_device(ctx, *cfg, in_dev, dtype, dims, all, out_dev, st, plain))) return s;
     if (flags == RFBA_HOST_PTRS) {
         RFBA_CUDA(cudaMemcpyAsync(out, out_dev, (size_t)out_elems * 4, cudaMemcpyDeviceToHost, st), "output copy");
         return device_status(ctx, st, "forward");
@@ -1198,7 +1288,7 @@ int rfba_ctx_destroy(rfba_ctx* c) {
                       &c->acounter, &c->errw, &c->tb_val, &c->tb_der, &c->tb_em, &c->tb_res, &c->tb_par, &c->tb_bg,
                       &c->tb_pix, &c->tb_pixels, &c->tb_dfd, &c->tb_vdf, &c->seed_w, &c->seed_sums, &c->seed_carry, &c->seed_map, &c->seed_vox,
                       &c->seed_xyz, &c->gb_pix, &c->gb_pixels, &c->gb_par, &c->hs_tab, &c->hs_part, &c->hs_gg, &c->hs_phi,
-                      &c->hs_frame, &c->hs_out})
+                      &c->hs_frame, &c->hs_out, &c->tstate})
         b->release();
     for (auto& g : c->gb) g.release();
     for (auto& e : c->ev)
@@ -1379,6 +1469,19 @@ int rfba_ctx_set_launch(rfba_ctx* c, int grid, int t_chunk) {
     if (!c) return RFBA_ERR_INVALID;
     c->grid_override = grid;
     c->chunk_override = t_chunk;
+    return RFBA_OK;
+}
+int rfba_ctx_set_time_batch(rfba_ctx* c, int volumes) {
+    if (!c) return RFBA_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(c->mu);
+    c->time_batch = volumes;
+    return RFBA_OK;
+}
+int rfba_ctx_last_time_batches(rfba_ctx* c, int* volumes, int* batches, int* passes) {
+    if (!c) return RFBA_ERR_INVALID;
+    if (volumes) *volumes = c->last_time_batch;
+    if (batches) *batches = c->last_batches;
+    if (passes) *passes = c->last_passes;
     return RFBA_OK;
 }
 

@@ -55,6 +55,7 @@ struct PlanCache {
 struct Tuning {
     int ty = 0;
     int order = 0;  // 0: largest blocks first, raster inside a block; 1: tiles interleaved across blocks
+    int tb = 0;     // time batch (volumes per batch; 0 = the whole series at once)
 };
 
 // One pass = the blocks whose radiality + intensity stacks fit the budget
@@ -66,6 +67,7 @@ struct PassPlan {
     int chunk = 1, nchunks = 1, grid = 1;
     size_t smem = 0;
     long long nitems = 0, units = 0;
+    long long vox = 0;  // region subvoxels of the pass
 };
 struct PassSet {
     std::vector<BlockDev> blocks;
@@ -73,7 +75,12 @@ struct PassSet {
     std::vector<long long> prefix;
     std::vector<PassPlan> passes;
     long long max_stack = 0;
+    long long max_vox = 0;
     int ty = 0;
+    // time batches: the stacks hold tb volumes and the temporal reduction is
+    // carried across batches in `fields` floats per subvoxel (tb 0: the whole
+    // series at once)
+    int tb = 0, fields = 0, nbatch = 1;
 };
 
 
@@ -131,6 +138,12 @@ struct rfba_ctx {
     int grid_override = 0;          // CTAs for the radiality kernel (0 = occupancy x SMs)
     int chunk_override = 0;         // time points per work item (0 = automatic)
     int last_passes = 0;            // passes of the last forward (1 = its stacks are all resident)
+    // time batches of a forward (0 = automatic: batches of kTimeBatch volumes when
+    // the whole series' stacks do not fit the budget, < 0 = never, > 0 = always,
+    // this many volumes), what the last forward used, and the carried state
+    int time_batch = 0;
+    int last_time_batch = 0, last_batches = 0;
+    rfba::DevBuf tstate;
     // differentiable path: buffers and the forward the backward can reuse
     rfba::DevBuf shifted, tmp1, tmp2, gS, gI, gin, dshift, ablocks, atiles, acounter, errw;
     struct Train {

@@ -293,8 +293,8 @@ __global__ void __launch_bounds__(WIDE ? kMaxThreads : 128, WIDE ? 2 : RFBA_FWD_
         const long long vb = ((long long)(Yb - B.lo[1])) * B.nreg[0] + (X - B.lo[0]);
         const long long zstride = (long long)B.nreg[0] * B.nreg[1];
 
-        const int t0 = chunk * p.t_chunk;
-        const int t1 = min(p.T, t0 + p.t_chunk);
+        const int t0 = p.t_lo + chunk * p.t_chunk;
+        const int t1 = min(p.t_hi > 0 ? p.t_hi : p.T, t0 + p.t_chunk);
         // TMA box origin: x rounded down to a 16-byte boundary; the offset back
         // (0 .. 16 bytes / element size - 1) is where the tile starts in a staged row
         constexpr int kAl = 16 / (int)sizeof(Tin);
@@ -314,7 +314,7 @@ __global__ void __launch_bounds__(WIDE ? kMaxThreads : 128, WIDE ? 2 : RFBA_FWD_
             if (!p.test_skip_copy) issue(t0);
         }
         for (int t = t0; t < t1; ++t) {
-            const long long sbase = B.stack_off + (long long)t * V;
+            const long long sbase = B.stack_off + (long long)(t - p.stack_t0) * V;
             // 1. input tile with block-edge clamp; 16 lanes per row, one division
             //    per row
             const long long tbase = (long long)t * p.D * p.H * p.W;

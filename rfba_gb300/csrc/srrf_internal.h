@@ -128,6 +128,10 @@ struct RadParams {
     // failure-detection test (RFBA_TEST_TMA_STALL): the first copy request of
     // every work item is left out, so the bounded staging wait gives up
     int test_skip_copy;
+    // time window of this launch: volumes [t_lo, t_hi) (t_hi 0: up to T), and
+    // the volume held by the first [t] row of the stacks (0 when they hold the
+    // whole series, t_lo when they hold one batch)
+    int t_lo, t_hi, stack_t0;
 };
 
 // Temporal reduction parameters.
@@ -139,6 +143,24 @@ struct TemporalParams {
     int T;
     int method, itc, order, iw;
     float* rad_stack;             // ITC=1 bins the series in place
+    const float* int_stack;
+    float* out;
+};
+
+// Temporal reduction of one time batch into the carried state
+// (temporal_stream.cu).
+struct StreamParams {
+    const BlockDev* blocks;
+    const long long* vox_prefix;
+    int nblocks;
+    long long total_vox;
+    int T;                 // the whole series
+    int t_lo, t_hi;        // this batch; the stacks hold its [t_hi - t_lo][v]
+    int method, order, iw;
+    int last;              // write the map after this batch
+    float* state;          // [field][state_stride]
+    long long state_stride;
+    const float* rad_stack;
     const float* int_stack;
     float* out;
 };
@@ -177,6 +199,9 @@ size_t radiality_smem_bytes(const RadParams& p);
 int tile_rows_for_mag(int my);
 int radiality_max_ctas_per_sm(const RadParams& p, int in_u16, int* out);
 int launch_temporal(const TemporalParams& p, void* stream);
+int launch_temporal_stream(const StreamParams& p, void* stream);
+// state floats per subvoxel for a method (0 TRM, 1 TRA, 2 TRPPM, 3 TRAC ITC 0) and TRAC order
+int temporal_stream_fields(int method, int order);
 int launch_combine(const double* spots, long long n, int zoom, int Xp, int Yp, int Zp, int r, int rz, int thr,
                    const uint16_t* psf, int Kx, int Ky, int Kz, unsigned int* hist, unsigned char* L,
                    unsigned short* S, unsigned long long* idx, unsigned int* val, unsigned long long cap,

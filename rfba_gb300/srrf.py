@@ -191,6 +191,8 @@ def lib():
         L.rfba_ctx_last_timing.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                                            ctypes.POINTER(ctypes.c_longlong)]
         L.rfba_ctx_set_launch.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+        L.rfba_ctx_set_time_batch.argtypes = [vp, ctypes.c_int]
+        L.rfba_ctx_last_time_batches.argtypes = [vp, ip, ip, ip]
         L.rfba_ctx_last_schedule.argtypes = [vp, ip, ip, ip, ip]
         L.rfba_combine_psf.argtypes = [ctypes.c_double, ctypes.c_double, vp, ctypes.c_longlong, ip]
         L.rfba_combine_load_result.argtypes = [ctypes.c_char_p, ctypes.c_int, ip, ip, vp, ctypes.c_longlong,
@@ -463,6 +465,25 @@ class Context:
 
     def set_launch(self, grid: int = 0, t_chunk: int = 0):
         _check(lib().rfba_ctx_set_launch(self.h, grid, t_chunk))
+
+    def set_time_batch(self, volumes: int = 0):
+        """Time batches of forward / forward_blocks: 0 automatic (batches of 25
+        volumes when the whole series' stacks do not fit the scratch budget),
+        > 0 always batches of that many volumes, < 0 never."""
+        _check(lib().rfba_ctx_set_time_batch(self.h, int(volumes)))
+
+    def last_time_batches(self):
+        """(volumes per batch, batches) of the last forward; (0, 0) when it
+        reduced the whole series in one pass."""
+        v, b = ctypes.c_int(0), ctypes.c_int(0)
+        _check(lib().rfba_ctx_last_time_batches(self.h, ctypes.byref(v), ctypes.byref(b), None))
+        return v.value, b.value
+
+    def last_passes(self) -> int:
+        """Spatial passes of the last forward (z slices or block groups)."""
+        n = ctypes.c_int(0)
+        _check(lib().rfba_ctx_last_time_batches(self.h, None, None, ctypes.byref(n)))
+        return n.value
 
     def combine_render(self, spots, img_dims, zoom: int = 10, psf=None, noise_r: int = 30, noise_rz: int = 3,
                        noise_threshold: int = 70):

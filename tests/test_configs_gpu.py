@@ -29,14 +29,16 @@ def _workload(name, n_vol=None, shape=None):
     return synth.render_parallel(scene, w["shape"], seed, w["dtype"]), scene
 
 
-def _check_regions(got, img, oracle_mod, kw, regions, tol, label):
+def _check_regions(got, img, oracle_mod, kw, regions, tol, label, also=()):
+    """Regions of `got` (and of every map in `also`) against the oracle."""
     conf = oracle_mod.make_conf(**kw)
     worst = 0.0
     for lo, hi in regions:
         ref = oracle_mod.srrf_region(img, conf, lo, hi)
         assert np.isfinite(ref).any(), f"{label}: region {lo}-{hi} lies outside the window"
-        sub = got[lo[2]:hi[2], lo[1]:hi[1], lo[0]:hi[0]]
-        worst = max(worst, assert_parity(sub, ref, tol, f"{label} region {lo}-{hi}"))
+        for i, m in enumerate((got,) + tuple(also)):
+            sub = m[lo[2]:hi[2], lo[1]:hi[1], lo[0]:hi[0]]
+            worst = max(worst, assert_parity(sub, ref, tol, f"{label} map {i} region {lo}-{hi}"))
     print(f"[config] {label}: rel L-inf {worst:.2e} over {len(regions)} regions (tolerance {tol:.0e})")
     return worst
 
@@ -119,17 +121,29 @@ def test_large_trac4_all_200_volumes(oracle_mod):
     volumes. The budget here, 16 planes x 1024 x 1024 subvoxels x 200 volumes x
     8 bytes, fixes the slices at z = 16 k; every checked region below straddles a
     slice boundary (z 16, 128, 240) and together they cover the low corner, the
-    middle and the high corner of the map plus seeded interior boxes."""
+    middle and the high corner of the map plus seeded interior boxes.
+
+    The same budget with the series in time batches (the automatic choice: 25
+    volumes a batch, the TRAC-4 window sums carried between batches) holds the
+    stacks of 25 volumes and the carried state for 64 planes at a time; that map
+    is checked on the same regions and against the sliced one."""
     from rfba_gb300 import srrf
+    from tests.parity import assert_parity
     x, _ = _workload("large")
     assert x.shape == (200, 128, 256, 256)
     kw = dict(mag=(4, 4, 2), method=3, itc=0, trac_order=4, **SMOOTH)
     budget = 16 * 1024 * 1024 * 200 * 8
     c = srrf.Context(0, budget)
     try:
+        c.set_time_batch(-1)
         got = c.forward(srrf.Config.make(**kw), x)
+        assert c.last_time_batches() == (0, 0)
+        c.set_time_batch(0)
+        streamed = c.forward(srrf.Config.make(**kw), x)
+        assert c.last_time_batches() == (25, 8)
     finally:
         c.close()
+    assert_parity(streamed, got, 1e-4, "large TRAC-4: time batches vs z slices")
     rng = np.random.default_rng(2026)
     regions = [((16, 16, 12), (24, 24, 20)), ((508, 510, 124), (516, 518, 132)),
                ((1000, 1004, 236), (1008, 1012, 244))]
@@ -139,7 +153,8 @@ def test_large_trac4_all_200_volumes(oracle_mod):
         regions.append(((x0, y0, zb - 4), (x0 + 8, y0 + 8, zb + 4)))
     xf = x.astype(np.float32)
     del x
-    _check_regions(got, xf, oracle_mod, kw, regions, 1e-4, "large 200 x 256x256x128, mag 4x4x2, TRAC-4")
+    _check_regions(got, xf, oracle_mod, kw, regions, 1e-4,
+                   "large 200 x 256x256x128, mag 4x4x2, TRAC-4 (z slices; time batches)", also=(streamed,))
 
 
 def test_mid_trac2_itc1_reduced_t(ctx, oracle_mod):

@@ -1,0 +1,141 @@
+"""Forward in time batches with the temporal reduction carried between them
+(temporal_stream.cu): against the one-pass reduction and the FP64 oracle, for
+every method, ragged and one-volume batches, series no longer than the TRAC
+order, block lists, host buffers and the automatic choice under a small
+scratch budget."""
+import numpy as np
+import pytest
+
+from tests.parity import assert_parity
+
+pytestmark = pytest.mark.gpu
+
+SHIPPED = dict(gradient_smooth=1, main_range=1, x_range=1, y_range=1, z_range=1)
+
+
+def _series(seed, T, D, H, W, emitters=20):
+    from rfba_gb300 import synth
+    scene = synth.make_scene(seed, T, (W, H, D), emitters)
+    return synth.render(scene, (W, H, D), seed, np.uint16)
+
+
+def _both(ctx, cfg, x, batch):
+    """(one pass, batches of `batch` volumes) on the same context."""
+    ctx.set_time_batch(-1)
+    try:
+        whole = ctx.forward(cfg, x)
+        assert ctx.last_time_batches() == (0, 0)
+        ctx.set_time_batch(batch)
+        parts = ctx.forward(cfg, x)
+        T = x.shape[0]
+        if batch < T:
+            assert ctx.last_time_batches() == (batch, -(-T // batch))
+    finally:
+        ctx.set_time_batch(0)
+    return whole, parts
+
+
+@pytest.mark.parametrize("method", [0, 1, 2])
+@pytest.mark.parametrize("iw", [0, 1])
+def test_trm_tra_trppm_bit_identical(ctx, method, iw):
+    """TRM, TRA and TRPPM add the same values in the same order in batches as in
+    one pass: the maps are bit-identical (kernel.cu:291-419)."""
+    from rfba_gb300 import srrf
+    cfg = srrf.Config.make(mag=2, method=method, intensity_w=iw, **SHIPPED)
+    x = _series(70 + method, 23, 10, 12, 14)
+    for batch in (1, 5, 22):
+        whole, parts = _both(ctx, cfg, x, batch)
+        assert np.array_equal(np.isnan(whole), np.isnan(parts))
+        assert np.array_equal(np.nan_to_num(whole), np.nan_to_num(parts)), (method, iw, batch)
+
+
+@pytest.mark.parametrize("order", [2, 3, 4])
+@pytest.mark.parametrize("iw", [0, 1])
+def test_trac_itc0_carried_cumulants(ctx, oracle_mod, order, iw):
+    """TRAC with ITC 0 (kernel.cu:423-500): the window sums carried around the
+    first batch's mean equal the one-pass reduction to rounding and the FP64
+    oracle within the TRAC tolerance (1e-4 relative L-inf), with the same NaN
+    mask, for batches of one volume, a ragged last batch and batches shorter
+    than the order."""
+    from rfba_gb300 import srrf
+    kw = dict(mag=2, method=3, itc=0, trac_order=order, intensity_w=iw, **SHIPPED)
+    cfg = srrf.Config.make(**kw)
+    x = _series(80 + order, 31, 10, 11, 13)
+    ref = oracle_mod.srrf_region(x.astype(np.float32), oracle_mod.make_conf(**kw))
+    for batch in (1, 3, 7, 25):
+        whole, parts = _both(ctx, cfg, x, batch)
+        assert_parity(whole, ref, 1e-4, f"one pass TRAC-{order}")
+        assert_parity(parts, ref, 1e-4, f"batches of {batch}, TRAC-{order}")
+        assert_parity(parts, whole, 1e-5, f"batches of {batch} vs one pass, TRAC-{order}")
+
+
+@pytest.mark.parametrize("T,order", [(2, 2), (3, 2), (4, 4), (5, 4), (1, 3)])
+def test_trac_short_series(ctx, oracle_mod, T, order):
+    """Series no longer than (or just past) the TRAC order: an empty or one-term
+    window, in one-volume batches."""
+    from rfba_gb300 import srrf
+    kw = dict(mag=2, method=3, itc=0, trac_order=order, **SHIPPED)
+    cfg = srrf.Config.make(**kw)
+    x = _series(90 + T, T, 6, 7, 8, emitters=4)
+    whole, parts = _both(ctx, cfg, x, 1)
+    ref = oracle_mod.srrf_region(x.astype(np.float32), oracle_mod.make_conf(**kw))
+    assert_parity(parts, ref, 1e-4, f"T={T} TRAC-{order}")
+    assert_parity(parts, whole, 1e-5, f"T={T} TRAC-{order} vs one pass")
+
+
+def test_block_list_in_batches(ctx):
+    """A doSplit block list (uneven blocks, one pass each or together) in
+    batches equals the one-pass block forward."""
+    from rfba_gb300 import srrf
+    cfg = srrf.Config.make(mag=3, method=3, itc=0, trac_order=3, **SHIPPED)
+    x = _series(95, 17, 20, 26, 30)
+    blocks, n, oe = srrf.blocks_dosplit(cfg, x.shape, (15, 15, 11), 1)
+    assert n > 4
+    ctx.set_time_batch(-1)
+    try:
+        whole = ctx.forward_blocks(cfg, x, blocks, n, oe)
+        ctx.set_time_batch(4)
+        parts = ctx.forward_blocks(cfg, x, blocks, n, oe)
+        assert ctx.last_time_batches() == (4, 5)
+    finally:
+        ctx.set_time_batch(0)
+    assert_parity(parts, whole, 1e-5, "block list in batches")
+
+
+def test_automatic_batches_under_a_small_budget(oracle_mod):
+    """With a scratch budget below the whole series' stacks but above one
+    batch's stacks plus the carried state, the forward runs in batches of 25
+    volumes without cutting the map; host buffers go through the captured
+    graph."""
+    from rfba_gb300 import srrf
+    kw = dict(mag=2, method=3, itc=0, trac_order=4, **SHIPPED)
+    cfg = srrf.Config.make(**kw)
+    T, D, H, W = 60, 12, 14, 16
+    x = _series(97, T, D, H, W)
+    vox = D * H * W * 8
+    fields = 38  # TRAC-4 state floats per subvoxel
+    budget = vox * (25 * 8 + fields * 4) + 4096
+    assert budget < vox * T * 8
+    c = srrf.Context(0, budget)
+    try:
+        got = c.forward(cfg, x)
+        assert c.last_time_batches() == (25, 3)
+        again = c.forward(cfg, x)
+    finally:
+        c.close()
+    assert np.array_equal(np.nan_to_num(got), np.nan_to_num(again))
+    ref = oracle_mod.srrf_region(x.astype(np.float32), oracle_mod.make_conf(**kw))
+    assert_parity(got, ref, 1e-4, "automatic batches, TRAC-4")
+
+
+def test_itc1_never_batched(ctx):
+    """TRAC with ITC 1 bins the whole series: a forced batch size is ignored."""
+    from rfba_gb300 import srrf
+    cfg = srrf.Config.make(mag=2, method=3, itc=1, trac_order=2, **SHIPPED)
+    x = _series(98, 12, 8, 9, 10)
+    ctx.set_time_batch(3)
+    try:
+        ctx.forward(cfg, x)
+        assert ctx.last_time_batches() == (0, 0)
+    finally:
+        ctx.set_time_batch(0)
