@@ -900,9 +900,12 @@ def run_gpu(args):
             ctx.forward(cfg, pinned_np, out=outh_np)
         if ws > 1:
             torch.distributed.barrier()
+        e2e_step_ms = []
         t0 = time.perf_counter()
         for _ in range(args.steps):
+            t1 = time.perf_counter()
             ctx.forward(cfg, pinned_np, out=outh_np)
+            e2e_step_ms.append((time.perf_counter() - t1) * 1e3)
         e2e_s = time.perf_counter() - t0
         e2e_s = max_over_ranks(e2e_s)
         e2e = whole_job_rate(units_per_step * args.steps, ws, e2e_s)
@@ -937,7 +940,10 @@ def run_gpu(args):
                    "global_batch": T, "parallelism": "replicas" if ws > 1 else "single",
                    "l2": "inputs larger than L2 (210 MB input, 26.8 GB radiality/intensity stack per step)"},
         "e2e": {"value": e2e, "unit": "voxel-volumes/s", "h2d_bytes_per_step": int(x.nbytes),
-                "d2h_bytes_per_step": int(np.prod(out_shape) * 4)},
+                "d2h_bytes_per_step": int(np.prod(out_shape) * 4),
+                "step_ms_min": min(e2e_step_ms) if e2e else None,
+                "step_ms_median": statistics.median(e2e_step_ms) if e2e else None,
+                "step_ms_max": max(e2e_step_ms) if e2e else None},
         "gpu_launches": int(launches),
         "clocks": clocks,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
