@@ -834,6 +834,24 @@ def run_single_workload(args):
     print(json.dumps({"workload": args.workload, **r}), flush=True)
 
 
+def temporal_roofline(tmp_ms, units_per_step: int, T: int, peaks: dict) -> dict:
+    """HBM roofline of the temporal reduction (TRAC-2 with intensity
+    weighting): per output subvoxel it must read T radiality and T intensity
+    values and write the map value (the cumulant pass reads the radiality
+    series a second time, mostly from L2), against the measured copy
+    bandwidth."""
+    if not tmp_ms:
+        return {}
+    ms = statistics.mean(tmp_ms)
+    vox = units_per_step // T
+    algo = vox * (2 * T * 4 + 4)
+    hbm = float(peaks.get("hbm_gbs", 0.0)) or None
+    achieved = algo / (ms / 1e3) / 1e9
+    return {"kernel_ms": ms, "algorithmic_bytes": algo, "achieved_gbs": achieved, "peak_gbs": hbm,
+            "frac": achieved / hbm if hbm else None, "unit": "GB/s",
+            "note": "T radiality + T intensity values read and one map value written per subvoxel"}
+
+
 def run_gpu(args):
     import torch
     ws, rank, local = dist_env()
@@ -876,9 +894,12 @@ def run_gpu(args):
     e1 = torch.cuda.Event(enable_timing=True)
     rad_ms = []
     e0.record(stream)
+    tmp_ms = []
     for _ in range(args.steps):
         step()
-        rad_ms.append(ctx.timing().radiality_ms)
+        tm = ctx.timing()
+        rad_ms.append(tm.radiality_ms)
+        tmp_ms.append(tm.temporal_ms)
     e1.record(stream)
     torch.cuda.synchronize()
     clocks = sampler.stop()
@@ -956,6 +977,7 @@ def run_gpu(args):
                      "peak_measured_note": "FP32 FMA chains on every SM (rfba_probe_fp32_fma_peak), measured in "
                                            "this run"},
         "direct_equivalent_tflops": fl["direct_distinct"] * units_per_step / (rad_avg_ms / 1e3) / 1e12,
+        "temporal_kernel": temporal_roofline(tmp_ms, units_per_step, T, peaks),
     }
     if rank == 0 and not args.no_extras:
         line["batching"] = measure_batching(ctx, max(2, args.steps // 2))
