@@ -806,6 +806,50 @@ def measure_combine(ctx, steps: int = 3) -> dict:
             "cpu_grid_voxels_per_s": (40 * 5) * (40 * 5) * (30 * 5) / cpu_s}
 
 
+def measure_stream(ctx, steps: int = 3, volumes=None) -> dict:
+    """The forward in time batches against the one-pass forward: 100 volumes of
+    64^3 uint16 (the mid workload's emitter model), mag 4x4x2 (256x256x128
+    map), TRAC-4 ITC 0 with intensity weighting; batches of 25 volumes with the
+    window sums carried between them (8.4 M subvoxels: 1.7 GB of stacks per
+    batch and 1.3 GB of carried state) against all 100 volumes' stacks (6.7 GB)
+    reduced at once. Device input, CUDA events."""
+    import torch
+    from rfba_gb300 import srrf, synth
+    x, _ = synth.workload("mid", n_vol=volumes or 100, shape=(64, 64, 64))
+    cfg = srrf.Config.make(**{**CFG_KW, "trac_order": 4})
+    xd = torch.from_numpy(x.view(np.int16)).cuda()
+    stream = torch.cuda.current_stream()
+    T = x.shape[0]
+    units = 256 * 256 * 128 * T
+    res, maps = {}, {}
+    # time batches first: their scratch (3 GB) is all the device holds while they run
+    for name, tb in (("time_batches", 25), ("one_pass", -1)):
+        ctx.set_time_batch(tb)
+        m = ctx.forward(cfg, xd, stream=stream.cuda_stream)
+        for _ in range(2):
+            ctx.forward(cfg, xd, out=m, stream=stream.cuda_stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            ctx.forward(cfg, xd, out=m, stream=stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        vb, nb = ctx.last_time_batches()
+        res[name] = {"forward_ms": ms, "value": units / (ms / 1e3), "batch_volumes": vb, "batches": nb}
+        maps[name] = m.cpu().numpy()
+    ctx.set_time_batch(0)
+    a, b = maps["one_pass"].astype(np.float64), maps["time_batches"].astype(np.float64)
+    fin = np.isfinite(a) & np.isfinite(b)
+    scale = float(np.max(np.abs(a[fin]))) if fin.any() else 0.0
+    rel = float(np.max(np.abs(a[fin] - b[fin]))) / scale if scale > 0 else 0.0
+    return {"workload": "stream: 100 x 64^3 u16 -> 256x256x128 map, mag 4x4x2, TRAC-4 ITC0, IW; time batches of "
+                        "25 volumes vs one pass", "voxel_volumes": units, **res,
+            "time_batches_over_one_pass": res["time_batches"]["forward_ms"] / res["one_pass"]["forward_ms"],
+            "nan_masks_equal": bool(np.array_equal(np.isnan(a), np.isnan(b))),
+            "rel_linf_time_batches_vs_one_pass": rel}
+
+
 def run_single_workload(args):
     """One of the secondary measurements alone, printed as its own JSON line."""
     import torch
@@ -824,6 +868,8 @@ def run_single_workload(args):
         r = measure_combine(ctx)
     elif args.workload == "refgpu":
         r = measure_reference_gpu(ctx)
+    elif args.workload == "stream":
+        r = measure_stream(ctx, max(1, args.steps), volumes=args.volumes)
     elif args.workload == "threeb":
         r = measure_threeb(ctx)
         if not args.no_cpu:
@@ -1075,7 +1121,8 @@ def main():
     ap.add_argument("--parallelism", default="replicas", choices=["replicas", "sharded"],
                     help="N > 1: replicas of the headline workload (default) or one batching series sharded by "
                          "blocks across the ranks")
-    ap.add_argument("--workload", default="mid", choices=["mid", "batching", "diff", "large", "seeding", "combine", "refgpu", "threeb"],
+    ap.add_argument("--workload", default="mid", choices=["mid", "batching", "diff", "large", "seeding", "combine", "refgpu", "threeb",
+                             "stream"],
                     help="mid: the headline line; batching / diff: that measurement alone (one JSON line)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":

@@ -67,23 +67,73 @@ int temporal_stream_fields(int method, int order) {
 
 namespace {
 
+// Each thread's values of the batch are staged in shared memory by cp.async
+// (no register staging, a chunk's copies all in flight at once), double
+// buffered in chunks of kChunk volumes; the sums then read shared memory.
+// Only the thread that copied a value reads it back.
+constexpr int kStreamThreads = 256;
+constexpr int kChunk = 8;
+using Stage = float[2][kChunk][kStreamThreads];
+
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// f(i, r, I) for the batch's values i = 0 .. nb - 1 in order (I is 0 when the
+// intensity stack is not needed).
+template <class F>
+__device__ __forceinline__ void for_each_value(const float* rad, const float* inten, long long V, int nb,
+                                               bool need_int, Stage& sr, Stage& si, F&& f) {
+    const int tx = threadIdx.x;
+    auto issue = [&](int buf, int c0) {
+        const int n = min(kChunk, nb - c0);
+        for (int j = 0; j < n; ++j) {
+            cp_async4(&sr[buf][j][tx], rad + (long long)(c0 + j) * V);
+            if (need_int) cp_async4(&si[buf][j][tx], inten + (long long)(c0 + j) * V);
+        }
+        cp_async_commit();
+    };
+    issue(0, 0);
+    int buf = 0;
+    for (int c0 = 0; c0 < nb; c0 += kChunk) {
+        if (c0 + kChunk < nb) {
+            issue(buf ^ 1, c0 + kChunk);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        const int n = min(kChunk, nb - c0);
+        for (int j = 0; j < n; ++j) f(c0 + j, sr[buf][j][tx], need_int ? si[buf][j][tx] : 0.f);
+        buf ^= 1;
+    }
+}
+
 template <int K>
 __device__ __forceinline__ void trac_carry(const StreamParams& p, long long g, const float* rad, const float* inten,
-                                           long long V, float* out_val) {
+                                           long long V, Stage& sr, Stage& si, float* out_val) {
     constexpr int NS = trac_sums(K);
+    constexpr int NF = 5 + (K - 1) + 2 * NS;
     float* st = p.state + g;
     const long long S = p.state_stride;
-    float reg[5 + (K - 1) + 2 * NS];
+    float reg[NF];
     const int nb = p.t_hi - p.t_lo;
+    const bool iw = p.iw == 1;
     if (p.t_lo == 0) {
         // K: the mean of the first batch, in the order the values arrive
         float m = 0.f;
-        for (int t = 0; t < nb; ++t) m += rad[t * V];
+        for_each_value(rad, inten, V, nb, false, sr, si, [&](int, float r, float) { m += r; });
         reg[0] = m / (float)nb;
-        for (int f = 1; f < 5 + (K - 1) + 2 * NS; ++f) reg[f] = 0.f;
+#pragma unroll
+        for (int f = 1; f < NF; ++f) reg[f] = 0.f;
     } else {
 #pragma unroll
-        for (int f = 0; f < 5 + (K - 1) + 2 * NS; ++f) reg[f] = st[f * S];
+        for (int f = 0; f < NF; ++f) reg[f] = st[f * S];
     }
     const float shift = reg[0];
     KahanRef ysum{&reg[1], &reg[2]};
@@ -92,12 +142,11 @@ __device__ __forceinline__ void trac_carry(const StreamParams& p, long long g, c
     float* sums = &reg[5 + (K - 1)];
     auto sum = [&](int i) { return KahanRef{&sums[2 * i], &sums[2 * i + 1]}; };
     const int N = p.T - K;  // window length
-    for (int i = 0; i < nb; ++i) {
+    for_each_value(rad, inten, V, nb, iw, sr, si, [&](int i, float r, float I) {
         const int t = p.t_lo + i;
-        const float r = rad[i * V];
         const float y = r - shift;
         ysum.add(y);
-        iws.add(r * inten[i * V]);
+        if (iw) iws.add(r * I);
         const int w = t - (K - 1);
         if (w >= 0 && w < N) {
             if (K == 2) {
@@ -136,10 +185,10 @@ __device__ __forceinline__ void trac_carry(const StreamParams& p, long long g, c
 #pragma unroll
         for (int j = K - 2; j > 0; --j) prev[j] = prev[j - 1];
         prev[0] = y;
-    }
+    });
     if (!p.last) {
 #pragma unroll
-        for (int f = 0; f < 5 + (K - 1) + 2 * NS; ++f) st[f * S] = reg[f];
+        for (int f = 0; f < NF; ++f) st[f * S] = reg[f];
         return;
     }
     double out = 0.0;
@@ -152,7 +201,7 @@ __device__ __forceinline__ void trac_carry(const StreamParams& p, long long g, c
         } else if (K == 3) {
             out = fabs(v(6) - c * (v(3) + v(4) + v(5)) + c * c * (v(0) + v(1) + v(2)) - n * c * c * c);
         } else {
-            auto pair = [&](int pij, int si, int sj) { return v(pij) - c * (v(si) + v(sj)) + n * c * c; };
+            auto pair = [&](int pij, int si_, int sj) { return v(pij) - c * (v(si_) + v(sj)) + n * c * c; };
             const double ab = pair(4, 0, 1), ac = pair(5, 0, 2), ad = pair(6, 0, 3);
             const double bc = pair(7, 1, 2), bd = pair(8, 1, 3), cd = pair(9, 2, 3);
             const double abcd = v(14) - c * (v(10) + v(11) + v(12) + v(13)) +
@@ -163,11 +212,12 @@ __device__ __forceinline__ void trac_carry(const StreamParams& p, long long g, c
         out /= (double)p.T;
     }
     float res = (float)out;
-    if (p.iw == 1) res = (float)(iws.value() / (double)p.T) * res;
+    if (iw) res = (float)(iws.value() / (double)p.T) * res;
     *out_val = res;
 }
 
-__global__ void __launch_bounds__(256) temporal_stream_kernel(const StreamParams p) {
+__global__ void __launch_bounds__(kStreamThreads) temporal_stream_kernel(const StreamParams p) {
+    __shared__ Stage sr, si;
     const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= p.total_vox) return;
     int lo = 0, hi = p.nblocks - 1;
@@ -185,15 +235,13 @@ __global__ void __launch_bounds__(256) temporal_stream_kernel(const StreamParams
     float* st = p.state + gid;
     const int nb = p.t_hi - p.t_lo;
     const bool first = p.t_lo == 0;
+    const bool iw = p.iw == 1;
     float result = 0.f;
 
     if (p.method == 1) {  // TRA
         float s = first ? 0.f : st[0], c = first ? 0.f : st[S];
         KahanRef k{&s, &c};
-        if (p.iw == 1)
-            for (int t = 0; t < nb; ++t) k.add(rad[t * V] * inten[t * V]);
-        else
-            for (int t = 0; t < nb; ++t) k.add(rad[t * V]);
+        for_each_value(rad, inten, V, nb, iw, sr, si, [&](int, float r, float I) { k.add(iw ? r * I : r); });
         if (!p.last) {
             st[0] = s;
             st[S] = c;
@@ -202,7 +250,8 @@ __global__ void __launch_bounds__(256) temporal_stream_kernel(const StreamParams
         result = s / (float)p.T;
     } else if (p.method == 0) {  // TRM
         float mip = first ? 0.f : st[0];
-        for (int t = 0; t < nb; ++t) mip = fmaxf(p.iw == 1 ? rad[t * V] * inten[t * V] : rad[t * V], mip);
+        for_each_value(rad, inten, V, nb, iw, sr, si,
+                       [&](int, float r, float I) { mip = fmaxf(iw ? r * I : r, mip); });
         if (!p.last) {
             st[0] = mip;
             return;
@@ -211,25 +260,25 @@ __global__ void __launch_bounds__(256) temporal_stream_kernel(const StreamParams
     } else if (p.method == 2) {  // TRPPM
         float r6[6];
         for (int f = 0; f < 6; ++f) r6[f] = first ? 0.f : st[f * S];
-        KahanRef s1{&r6[0], &r6[1]}, s2{&r6[2], &r6[3]}, si{&r6[4], &r6[5]};
-        for (int t = 0; t < nb; ++t) {
-            const float r = fmaxf(rad[t * V], 0.f);
+        KahanRef s1{&r6[0], &r6[1]}, s2{&r6[2], &r6[3]}, s3{&r6[4], &r6[5]};
+        for_each_value(rad, inten, V, nb, iw, sr, si, [&](int, float rv, float I) {
+            const float r = fmaxf(rv, 0.f);
             s1.add(r);
             s2.add(r * r);
-            if (p.iw == 1) si.add(inten[t * V]);
-        }
+            if (iw) s3.add(I);
+        });
         if (!p.last) {
             for (int f = 0; f < 6; ++f) st[f * S] = r6[f];
             return;
         }
         const float count = fmaxf(0.5f * (float)p.T * (float)(p.T + 1), 1.f);
         float pps = (0.5f * (r6[0] * r6[0] + r6[2])) / count;
-        if (p.iw == 1) pps *= r6[4] / (float)p.T;
+        if (iw) pps *= r6[4] / (float)p.T;
         result = pps;
     } else {  // TRAC, ITC 0
-        if (p.order == 3) trac_carry<3>(p, gid, rad, inten, V, &result);
-        else if (p.order == 4) trac_carry<4>(p, gid, rad, inten, V, &result);
-        else trac_carry<2>(p, gid, rad, inten, V, &result);
+        if (p.order == 3) trac_carry<3>(p, gid, rad, inten, V, sr, si, &result);
+        else if (p.order == 4) trac_carry<4>(p, gid, rad, inten, V, sr, si, &result);
+        else trac_carry<2>(p, gid, rad, inten, V, sr, si, &result);
         if (!p.last) return;
     }
 
@@ -253,8 +302,8 @@ __global__ void __launch_bounds__(256) temporal_stream_kernel(const StreamParams
 
 int launch_temporal_stream(const StreamParams& p, void* stream) {
     if (p.total_vox == 0 || p.t_hi <= p.t_lo) return 0;
-    const long long grid = (p.total_vox + 255) / 256;
-    temporal_stream_kernel<<<(unsigned)grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(p);
+    const long long grid = (p.total_vox + kStreamThreads - 1) / kStreamThreads;
+    temporal_stream_kernel<<<(unsigned)grid, kStreamThreads, 0, static_cast<cudaStream_t>(stream)>>>(p);
     return (int)cudaGetLastError();
 }
 
