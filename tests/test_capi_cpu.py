@@ -254,6 +254,17 @@ def test_optimiser_entry_points_check_arguments(built_lib):
     assert ev > it >= 1
 
 
+def test_time_batch_entry_points_check_arguments(built_lib):
+    """The time-batch setter and report refuse a null context without touching
+    a device."""
+    from rfba_gb300 import srrf
+    L = srrf.lib()
+    v, b, n = ctypes.c_int(7), ctypes.c_int(7), ctypes.c_int(7)
+    assert L.rfba_ctx_set_time_batch(None, 25) == -1
+    assert L.rfba_ctx_last_time_batches(None, ctypes.byref(v), ctypes.byref(b), ctypes.byref(n)) == -1
+    assert (v.value, b.value, n.value) == (7, 7, 7)
+
+
 @pytest.mark.skipif(__import__("tests.conftest", fromlist=["HAS_GPU"]).HAS_GPU, reason="checks the no-GPU path")
 def test_context_without_gpu_reports_cuda_error(built_lib):
     from rfba_gb300 import srrf

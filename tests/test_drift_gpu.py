@@ -28,3 +28,24 @@ def test_resume_from_checkpoint_matches_uninterrupted(ctx, tmp_path):
     L0 = float(drift.objective(ctx.forward_shifted(cfg, xd, torch.from_numpy(start).cuda())))
     assert float(drift.objective(m_rest)) < L0
     assert abs(float(drift.objective(m_rest)) - float(drift.objective(m_full))) <= 1e-4 * abs(L0)
+
+
+@pytest.mark.parametrize("kind,p", [("lp", 8.0), ("kurtosis", 4.0)])
+def test_refinement_with_other_objectives(ctx, kind, p):
+    """refine_drift minimises whichever objective's gradient it is given: with
+    make_objective's peak-weighted and scale-free objectives (border left out)
+    the objective after a few steps is below its start."""
+    import torch
+    from rfba_gb300 import drift, srrf, synth
+    scene = synth.make_scene(33, 6, (16, 15, 14), 14, drift_sigma=0.2)
+    x = synth.render(scene, (16, 15, 14), 33, np.float32)
+    cfg = srrf.Config.make(mag=2, method=3, itc=0, trac_order=2, gradient_smooth=1, x_range=1, y_range=1,
+                           z_range=1)
+    xd = torch.from_numpy(x).cuda()
+    value, grad = drift.make_objective(kind, p, border=4)
+    start = np.full((6, 3), 0.5, np.float32)
+    L0 = float(value(ctx.forward_shifted(cfg, xd, torch.from_numpy(start).cuda())))
+    st, m = drift.refine_drift(ctx, cfg, xd, 5, start=start, lr=0.01, grad_fn=grad)
+    torch.cuda.synchronize()
+    assert st.it == 5 and np.isfinite(st.shifts).all()
+    assert float(value(m)) < L0
