@@ -372,13 +372,23 @@ static int plan_passes(rfba_ctx* ctx, const rfba_srrf_config& cfg, rfba_dtype dt
     return RFBA_OK;
 }
 
+// Input copy windows of a captured host-buffer forward: volumes [t[k], t[k+1])
+// are on the device once ready[k] has fired.
+struct InputWindows {
+    int n = 0;
+    int t[3] = {0, 0, 0};
+    const cudaEvent_t* ready = nullptr;
+};
+
 // Queue the passes on st: counter reset, radiality, temporal per pass. The
 // device lists hold ps's concatenated blocks / tiles / prefixes; evs (3 per
-// pass) are recorded around the kernels when given.
+// pass) are recorded around the kernels when given. With input windows the
+// radiality of a single whole-series pass runs window by window, each launch
+// waiting for its window's copy.
 static int enqueue_passes(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void* in_dev, rfba_dtype dtype,
                           const int dims[4], const PassSet& ps, const BlockDev* dblocks, const TileDesc* dtiles,
                           const long long* dprefix, unsigned int* dcounters, float* out_dev, cudaStream_t st,
-                          const cudaEvent_t* evs, bool capturing = false) {
+                          const cudaEvent_t* evs, bool capturing = false, const InputWindows* win = nullptr) {
     // inside a stream capture the events become event-record nodes of the graph
     auto rec = [&](cudaEvent_t e) {
         return capturing ? cudaEventRecordWithFlags(e, st, cudaEventRecordExternal) : cudaEventRecord(e, st);
@@ -437,10 +447,20 @@ static int enqueue_passes(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void
         // radiality launches (with the carries of all batches but the last)
         // and the last temporal launch.
         if (evs) RFBA_CUDA(rec(evs[3 * i]), "event");
-        for (int b = 0; b < ps.nbatch; ++b) {
+        // input windows (one pass over the whole series only): the radiality of
+        // each window's volumes waits for that window's host copy
+        const bool windows = win && ps.tb == 0 && ps.passes.size() == 1;
+        const int nlaunch = windows ? win->n : ps.nbatch;
+        for (int b = 0; b < nlaunch; ++b) {
             RadParams rb = rp;
-            rb.t_lo = b * tb;
-            rb.t_hi = std::min(T, rb.t_lo + tb);
+            if (windows) {
+                rb.t_lo = win->t[b];
+                rb.t_hi = win->t[b + 1];
+                RFBA_CUDA(cudaStreamWaitEvent(st, win->ready[b], 0), "input window wait");
+            } else {
+                rb.t_lo = b * tb;
+                rb.t_hi = std::min(T, rb.t_lo + tb);
+            }
             rb.stack_t0 = ps.tb > 0 ? rb.t_lo : 0;
             rb.nchunks = (rb.t_hi - rb.t_lo + pp.chunk - 1) / pp.chunk;
             rb.nitems = (long long)rb.ntiles * rb.nchunks;
@@ -497,7 +517,7 @@ static int collect_timing(rfba_ctx* ctx, const PassSet& ps, const std::vector<cu
 
 static void account(rfba_ctx* ctx, const PassSet& ps) {
     ctx->last_passes = (int)ps.passes.size();
-    ctx->launches += 2 * (long long)ps.passes.size() * ps.nbatch;
+    ctx->launches += (long long)ps.passes.size() * (ps.nwin > 0 ? ps.nwin + 1 : 2 * ps.nbatch);
     ctx->last_time_batch = ps.tb;
     ctx->last_batches = ps.tb > 0 ? ps.nbatch : 0;
     ctx->last_flop_units = 0;
@@ -776,6 +796,8 @@ static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, con
             const int stall = test_tma_stall();
             key_put(&gkey, &stall, 1);
             key_put(&gkey, &tb, 1);
+            const int overlap = env_on("RFBA_OVERLAP", true) ? 1 : 0;
+            key_put(&gkey, &overlap, 1);
             key_put(&gkey, blocks, (size_t)nblocks);
             const bool host = flags == RFBA_HOST_PTRS;
             auto deps_now = [&]() {
@@ -798,6 +820,12 @@ static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, con
                 Tuning t2 = tune;
                 if ((s = ctx->errw.ensure(256, "check word"))) return s;
                 if ((s = plan_passes(ctx, *cfg, dtype, dims, all, t2, &g->ps))) return s;
+                // Host input over one whole-series pass: the first tenth of the
+                // volumes is copied first and the rest on a second stream while
+                // the radiality of the first window runs
+                const int T = dims[3];
+                const bool windowed = overlap && host && g->ps.tb == 0 && g->ps.passes.size() == 1 && T >= 2;
+                g->ps.nwin = windowed ? 2 : 0;
                 const PassSet& ps = g->ps;
                 const size_t np = ps.passes.size();
                 if ((s = ctx->rad.ensure((size_t)ps.max_stack * 4, "radiality stack"))) return s;
@@ -821,12 +849,40 @@ static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, con
                 RFBA_CUDA(cudaMemcpy(g->prefix.p, ps.prefix.data(), ps.prefix.size() * sizeof(long long),
                                      cudaMemcpyHostToDevice), "prefix upload");
                 if (!ctx->cap) RFBA_CUDA(cudaStreamCreateWithFlags(&ctx->cap, cudaStreamNonBlocking), "stream");
+                InputWindows win;
+                if (windowed) {
+                    if (!ctx->cap2) RFBA_CUDA(cudaStreamCreateWithFlags(&ctx->cap2, cudaStreamNonBlocking), "stream");
+                    while (g->copy_evs.size() < 3) {
+                        cudaEvent_t e;
+                        RFBA_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+                        g->copy_evs.push_back(e);
+                    }
+                    win.n = 2;
+                    win.t[0] = 0;
+                    win.t[1] = std::max(1, T / 10);
+                    win.t[2] = T;
+                    win.ready = g->copy_evs.data() + 1;
+                }
                 const void* gin = host ? ctx->in.p : in;
                 float* gout = host ? static_cast<float*>(ctx->out.p) : out;
                 RFBA_CUDA(cudaStreamBeginCapture(ctx->cap, cudaStreamCaptureModeThreadLocal), "graph capture");
                 int cs = RFBA_OK;
                 cudaError_t ce = cudaSuccess;
-                if (host) {
+                if (host && windowed) {
+                    // fork: the copy stream takes the input windows, each followed by
+                    // the event its radiality launch waits for (the last wait joins it)
+                    const size_t vol = in_bytes / (size_t)T;
+                    const size_t b0 = vol * (size_t)win.t[1];
+                    ce = cudaEventRecord(g->copy_evs[0], ctx->cap);
+                    if (ce == cudaSuccess) ce = cudaStreamWaitEvent(ctx->cap2, g->copy_evs[0], 0);
+                    if (ce == cudaSuccess) ce = cudaMemcpyAsync(ctx->in.p, in, b0, cudaMemcpyHostToDevice, ctx->cap2);
+                    if (ce == cudaSuccess) ce = cudaEventRecord(g->copy_evs[1], ctx->cap2);
+                    if (ce == cudaSuccess)
+                        ce = cudaMemcpyAsync(static_cast<char*>(ctx->in.p) + b0, static_cast<const char*>(in) + b0,
+                                             in_bytes - b0, cudaMemcpyHostToDevice, ctx->cap2);
+                    if (ce == cudaSuccess) ce = cudaEventRecord(g->copy_evs[2], ctx->cap2);
+                    if (ce == cudaSuccess) ce = cudaMemsetAsync(gout, 0, (size_t)out_elems * 4, ctx->cap);
+                } else if (host) {
                     ce = cudaMemcpyAsync(ctx->in.p, in, in_bytes, cudaMemcpyHostToDevice, ctx->cap);
                     if (ce == cudaSuccess) ce = cudaMemsetAsync(gout, 0, (size_t)out_elems * 4, ctx->cap);
                 } else if (zero_out) {
@@ -837,7 +893,7 @@ static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, con
                                         static_cast<const TileDesc*>(g->tiles.p),
                                         static_cast<const long long*>(g->prefix.p),
                                         static_cast<unsigned int*>(g->counters.p), gout, ctx->cap, g->evs.data(),
-                                        true);
+                                        true, windowed ? &win : nullptr);
                 if (ce == cudaSuccess && cs == RFBA_OK && host)
                     ce = cudaMemcpyAsync(out, gout, (size_t)out_elems * 4, cudaMemcpyDeviceToHost, ctx->cap);
                 cudaGraph_t graph = nullptr;
@@ -1296,6 +1352,7 @@ int rfba_ctx_destroy(rfba_ctx* c) {
     c->graphs.clear();
     for (cudaEvent_t e : c->pev) cudaEventDestroy(e);
     if (c->cap) cudaStreamDestroy(c->cap);
+    if (c->cap2) cudaStreamDestroy(c->cap2);
     if (c->xev) cudaEventDestroy(c->xev);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;

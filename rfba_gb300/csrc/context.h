@@ -81,6 +81,7 @@ struct PassSet {
     // carried across batches in `fields` floats per subvoxel (tb 0: the whole
     // series at once)
     int tb = 0, fields = 0, nbatch = 1;
+    int nwin = 0;  // radiality launches per pass when the input copy is windowed (0: not)
 };
 
 
@@ -94,9 +95,12 @@ struct GraphPlan {
     PassSet ps;
     DevBuf blocks, tiles, prefix, counters;
     std::vector<cudaEvent_t> evs;
+    // fork of the copy stream and the end of each input copy window
+    std::vector<cudaEvent_t> copy_evs;
     ~GraphPlan() {
         if (exec) cudaGraphExecDestroy(exec);
         for (cudaEvent_t e : evs) cudaEventDestroy(e);
+        for (cudaEvent_t e : copy_evs) cudaEventDestroy(e);
         blocks.release();
         tiles.release();
         prefix.release();
@@ -158,7 +162,8 @@ struct rfba_ctx {
     double last_backward_ms = 0.0;
     // forward schedule: per-pass timing events, autotuned schedules, captured graphs
     std::vector<cudaEvent_t> pev;
-    cudaStream_t cap = nullptr;  // stream the graphs are captured on
+    cudaStream_t cap = nullptr;   // stream the graphs are captured on
+    cudaStream_t cap2 = nullptr;  // the captured input copies' stream
     std::map<std::string, std::pair<int, int>> tunes;  // schedule key -> (tile rows, tile order)
     std::vector<std::unique_ptr<rfba::GraphPlan>> graphs;  // most recent first
     // spot seeding scratch

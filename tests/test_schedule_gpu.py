@@ -122,3 +122,27 @@ def test_graph_replay_reports_kernel_times(ctx, env):
             assert t.radiality_ms > 0 and t.temporal_ms > 0
     finally:
         ctx.set_timing(False)
+
+
+@pytest.mark.parametrize("T", [1, 2, 13])
+def test_pinned_forward_with_windowed_input_copy(ctx, env, T):
+    """With pinned host buffers the captured forward copies the first tenth of
+    the volumes, then the rest on a second stream while the first window's
+    radiality runs; the map equals the one from a single input copy
+    (RFBA_OVERLAP=0) and from device buffers, bit for bit."""
+    import torch
+    from rfba_gb300 import srrf
+    cfg = srrf.Config.make(mag=(4, 4, 2), method=3, itc=0, trac_order=2, intensity_w=1, **SHIPPED)
+    x = _volume(T, (20, 18, 14), seed=9)
+    xd = torch.from_numpy(x.view(np.int16)).cuda()
+    ref = ctx.forward(cfg, xd).cpu().numpy()
+    pin_in = torch.empty(x.nbytes, dtype=torch.uint8).pin_memory().numpy().view(np.uint16).reshape(x.shape)
+    pin_in[...] = x
+    pin_out = torch.empty(ref.size, dtype=torch.float32).pin_memory().numpy().reshape(ref.shape)
+    for overlap in ("1", "0", "1"):
+        env.setenv("RFBA_OVERLAP", overlap)
+        for _ in range(2):  # capture, then replay
+            pin_out[...] = 0
+            ctx.forward(cfg, pin_in, out=pin_out)
+            assert ctx.schedule()["graph"]
+            assert _same(pin_out, ref), (T, overlap)
