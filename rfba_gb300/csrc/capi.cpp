@@ -1062,9 +1062,11 @@ static int forward_shifted_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, co
     if ((s = apply_drift(ctx, in, shifts, dims, st, &ip))) return s;
     if ((s = forward_blocks_locked(ctx, cfg, ip, RFBA_F32, dims, &b, 1, out, n, RFBA_DEVICE_PTRS, st, false)))
         return s;
-    // the backward can reuse this forward's stacks when they are all resident and
-    // the temporal reduction left them intact (ITC 1 bins the series in place)
-    if (!rlo && ctx->last_passes == 1 && !(cfg->method == 3 && cfg->itc == 1)) {
+    // the backward can reuse this forward's stacks when they are all resident
+    // (one spatial pass over the whole series at once: a forward in time batches
+    // keeps only its last batch) and the temporal reduction left them intact
+    // (ITC 1 bins the series in place)
+    if (!rlo && ctx->last_passes == 1 && ctx->last_time_batch == 0 && !(cfg->method == 3 && cfg->itc == 1)) {
         std::vector<BlockDev> all;
         if ((s = make_blocks(ctx, *cfg, dims, &b, 1, &all))) return s;
         if (all.size() == 1) {
