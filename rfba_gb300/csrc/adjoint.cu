@@ -723,10 +723,12 @@ __global__ void __launch_bounds__(kAdjThreads, 2) radiality_adjoint_kernel(const
         const long long va = ((long long)(Ya - B.lo[1])) * B.nreg[0] + (X - B.lo[0]);
         const long long vb = va + B.nreg[0];
         const long long zstride = (long long)B.nreg[0] * B.nreg[1];
-        const int t0 = chunk * p.t_chunk;
-        const int t1 = min(p.T, t0 + p.t_chunk);
+        // volumes [t_lo, t_hi) of this launch (t_hi 0: up to T); dL/dS and dL/dI
+        // hold rows from volume stack_t0 on
+        const int t0 = p.t_lo + chunk * p.t_chunk;
+        const int t1 = min(p.t_hi > 0 ? p.t_hi : p.T, t0 + p.t_chunk);
         for (int t = t0; t < t1; ++t) {
-            const long long sbase = B.stack_off + (long long)t * V;
+            const long long sbase = B.stack_off + (long long)(t - p.stack_t0) * V;
             const long long tbase = (long long)t * p.D * p.H * p.W;
             // forward: input tile, gradient cells; clear the adjoint cells
             for (int r = tid / kTileX; r < NIY * NIZ; r += nthr / kTileX) {

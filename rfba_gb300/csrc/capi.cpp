@@ -437,6 +437,7 @@ static int enqueue_passes(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void
         sp.iw = cfg.intensity_w;
         sp.state = static_cast<float*>(ctx->tstate.p);
         sp.state_stride = ps.max_vox;
+        sp.keep = ctx->keep_tstate ? 1 : 0;
         sp.rad_stack = rp.rad_stack;
         sp.int_stack = rp.int_stack;
         sp.out = out_dev;
@@ -1087,9 +1088,14 @@ static int forward_shifted_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, co
 // offset 0 of the context's stacks: temporal adjoint, then the radiality
 // adjoint adding into dL/dI' (ctx->gin, cleared by the caller).
 static int adjoint_slab(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* iprime, const int dims[4],
-                        BlockDev blk, const float* gmap, long long ngmap, cudaStream_t st) {
+                        BlockDev blk, const float* gmap, long long ngmap, cudaStream_t st, int t_lo = 0,
+                        int t_hi = 0) {
+    // t_hi > 0: only the volumes [t_lo, t_hi), whose dL/dS and dL/dI the caller
+    // has put in ctx->gS / ctx->gI from row 0 on (no temporal adjoint here)
     int s;
     const int T = dims[3];
+    const bool window = t_hi > 0;
+    const int TW = window ? t_hi - t_lo : T;
     const size_t nin = (size_t)dims[0] * dims[1] * dims[2] * T;
     const long long V = blk.vox;
     blk.stack_off = 0;
@@ -1100,7 +1106,7 @@ static int adjoint_slab(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float*
     for (int tz = 0; tz < blk.ntile[2]; ++tz)
         for (int ty = 0; ty < blk.ntile[1]; ++ty)
             for (int tx = 0; tx < blk.ntile[0]; ++tx) tiles.push_back({0, tx, ty, tz});
-    if ((s = ctx->gS.ensure((size_t)V * T * 4, "adjoint stack")) || (s = ctx->gI.ensure((size_t)V * T * 4, "adjoint stack")) ||
+    if ((s = ctx->gS.ensure((size_t)V * TW * 4, "adjoint stack")) || (s = ctx->gI.ensure((size_t)V * TW * 4, "adjoint stack")) ||
         (s = ctx->ablocks.ensure(sizeof(BlockDev), "blocks")) ||
         (s = ctx->atiles.ensure(tiles.size() * sizeof(TileDesc), "tiles")) || (s = ctx->acounter.ensure(256, "counter")) ||
         (s = ctx->errw.ensure(256, "check word")))
@@ -1113,12 +1119,14 @@ static int adjoint_slab(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float*
     float* gS = static_cast<float*>(ctx->gS.p);
     float* gI = static_cast<float*>(ctx->gI.p);
     unsigned long long* err = static_cast<unsigned long long*>(ctx->errw.p);
-    int e = launch_temporal_adjoint(dblk, V, static_cast<const float*>(ctx->rad.p),
+    int e = 0;
+    if (!window) {
+        e = launch_temporal_adjoint(dblk, V, static_cast<const float*>(ctx->rad.p),
                                     static_cast<const float*>(ctx->inten.p), gmap, T, cfg->method, cfg->itc,
-                                    cfg->trac_order,
-                                    cfg->intensity_w, cfg->renormalize == 1, cfg->remove_con == 1, gS, gI, ngmap, err,
-                                    st);
-    if (e) return cuda_fail((cudaError_t)e, "temporal adjoint launch");
+                                    cfg->trac_order, cfg->intensity_w, cfg->renormalize == 1, cfg->remove_con == 1,
+                                    gS, gI, ngmap, err, st);
+        if (e) return cuda_fail((cudaError_t)e, "temporal adjoint launch");
+    }
     RadParams rp = fill_rad_params(ctx, *cfg, iprime, dims, cza_for_mag(cfg->mag[2]));
     rp.TY = kAdjRows;
     rp.NV = (kAdjRows - 1) / cfg->mag[1] + 2 + 4;
@@ -1141,16 +1149,141 @@ static int adjoint_slab(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float*
     }
     const int slots = per_sm * ctx->sm_count;
     long long nch = (8LL * slots + rp.ntiles - 1) / rp.ntiles;
-    nch = std::max<long long>(1, std::min<long long>(nch, T));
-    rp.t_chunk = (int)((T + nch - 1) / nch);
-    rp.nchunks = (T + rp.t_chunk - 1) / rp.t_chunk;
+    nch = std::max<long long>(1, std::min<long long>(nch, TW));
+    rp.t_chunk = (int)((TW + nch - 1) / nch);
+    rp.nchunks = (TW + rp.t_chunk - 1) / rp.t_chunk;
     rp.nitems = (long long)rp.ntiles * rp.nchunks;
+    rp.t_lo = window ? t_lo : 0;
+    rp.t_hi = window ? t_hi : T;
+    rp.stack_t0 = rp.t_lo;
     const int grid = (int)std::max<long long>(1, std::min<long long>(slots, rp.nitems));
-    AdjParams ap{gS, gI, static_cast<float*>(ctx->gin.p), (long long)nin, (long long)V * T, err};
+    AdjParams ap{gS, gI, static_cast<float*>(ctx->gin.p), (long long)nin, (long long)V * TW, err};
     e = launch_radiality_adjoint(rp, ap, grid, smem, st);
     if (e) return cuda_fail((cudaError_t)e, "radiality adjoint launch");
-    ctx->launches += 2;
+    ctx->launches += window ? 1 : 2;
     return RFBA_OK;
+}
+
+// Backward in time batches (TRA, TRAC with ITC 0), used when the context
+// forces a time batch size: per z slice of the map, a state pass (the
+// radiality of every batch folded into the carried temporal state, kept after
+// the last batch), then per batch the radiality of the batch and of the k - 1
+// volumes on either side that TRAC's lagged products reach, the batch's
+// temporal adjoint from the state, and the radiality adjoint of its volumes
+// into dL/dI'. Scratch per subvoxel: the window's stacks, the batch's adjoint
+// stacks and the state, instead of the whole series' four stacks.
+static int backward_batched(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* ip, const int dims[4],
+                            const rfba_block& b, int tb, const float* gmap, long long nreg, cudaStream_t st) {
+    int s;
+    const int T = dims[3];
+    const bool trac = cfg->method == 3;
+    const int h = trac ? cfg->trac_order - 1 : 0;
+    // TRA's state pass runs TRAC-2's carry: its sum of y is finite exactly when
+    // every radiality value of the series is
+    rfba_srrf_config scfg = *cfg;
+    if (!trac) {
+        scfg.method = 3;
+        scfg.itc = 0;
+        scfg.trac_order = 2;
+    }
+    const int fields = temporal_stream_fields(3, scfg.trac_order);
+    const int wl = std::min(T, tb + 2 * h);
+    std::vector<BlockDev> all;
+    if ((s = make_blocks(ctx, scfg, dims, &b, 1, &all, 0, wl + tb, fields))) return s;
+    unsigned long long* err = static_cast<unsigned long long*>(ctx->errw.p);
+    for (const BlockDev& slab : all) {
+        std::vector<BlockDev> one(1, slab);
+        Tuning ts;
+        ts.tb = tb;
+        ctx->keep_tstate = true;
+        s = run_device(ctx, scfg, ip, RFBA_F32, dims, one, static_cast<float*>(ctx->out.p), st, ts);
+        ctx->keep_tstate = false;
+        if (s) return s;
+        // the window plan: the same slab with wl volumes of stacks
+        PassSet ps;
+        Tuning tw;
+        tw.tb = wl;
+        if ((s = plan_passes(ctx, scfg, RFBA_F32, dims, one, tw, &ps))) return s;
+        if (ps.passes.size() != 1) {
+            set_error("time-batched backward: a slice does not fit one pass");
+            return RFBA_ERR_UNSUPPORTED;
+        }
+        const PassPlan& pp = ps.passes[0];
+        const long long V = slab.vox;
+        if ((s = ctx->rad.ensure((size_t)V * wl * 4, "radiality stack")) ||
+            (s = ctx->inten.ensure((size_t)V * wl * 4, "intensity stack")) ||
+            (s = ctx->gS.ensure((size_t)V * tb * 4, "adjoint stack")) ||
+            (s = ctx->gI.ensure((size_t)V * tb * 4, "adjoint stack")) ||
+            (s = ctx->blocks.ensure(ps.blocks.size() * sizeof(BlockDev), "blocks")) ||
+            (s = ctx->tiles.ensure(ps.tiles.size() * sizeof(TileDesc), "tiles")) ||
+            (s = ctx->counter.ensure(256, "counter")))
+            return s;
+        RFBA_CUDA(cudaMemcpyAsync(ctx->blocks.p, ps.blocks.data(), ps.blocks.size() * sizeof(BlockDev),
+                                  cudaMemcpyHostToDevice, st), "blocks upload");
+        RFBA_CUDA(cudaMemcpyAsync(ctx->tiles.p, ps.tiles.data(), ps.tiles.size() * sizeof(TileDesc),
+                                  cudaMemcpyHostToDevice, st), "tiles upload");
+        const BlockDev* dblk = static_cast<const BlockDev*>(ctx->blocks.p);
+        RadParams rp = fill_rad_params(ctx, scfg, ip, dims, cz_for_mag(scfg.mag[2]), ps.ty);
+        rp.tma_bx = radiality_tma_box_x(rp, 0);
+        rp.err = err;
+        rp.blocks = dblk;
+        rp.tiles = static_cast<const TileDesc*>(ctx->tiles.p);
+        rp.ntiles = (int)(pp.t1 - pp.t0);
+        rp.rad_stack = static_cast<float*>(ctx->rad.p);
+        rp.int_stack = static_cast<float*>(ctx->inten.p);
+        rp.work_counter = static_cast<unsigned int*>(ctx->counter.p);
+        rp.t_chunk = pp.chunk;
+        BlockDev blk = slab;
+        blk.stack_off = 0;
+        for (int t_lo = 0; t_lo < T; t_lo += tb) {
+            const int t_hi = std::min(T, t_lo + tb);
+            RadParams rb = rp;
+            rb.t_lo = std::max(0, t_lo - h);
+            rb.t_hi = std::min(T, t_hi + h);
+            rb.stack_t0 = rb.t_lo;
+            rb.nchunks = (rb.t_hi - rb.t_lo + pp.chunk - 1) / pp.chunk;
+            rb.nitems = (long long)rb.ntiles * rb.nchunks;
+            const int grid = (int)std::max<long long>(1, std::min<long long>(pp.grid, rb.nitems));
+            RFBA_CUDA(cudaMemsetAsync(ctx->counter.p, 0, sizeof(unsigned int), st), "counter reset");
+            int e = launch_radiality(rb, grid, pp.smem, 0, st);
+            if (e) return cuda_fail((cudaError_t)e, "radiality launch");
+            StreamAdjParams ap;
+            std::memset(&ap, 0, sizeof ap);
+            ap.block = dblk;
+            ap.T = T;
+            ap.t_lo = t_lo;
+            ap.t_hi = t_hi;
+            ap.w_lo = rb.t_lo;
+            ap.w_hi = rb.t_hi;
+            ap.method = cfg->method;
+            ap.order = scfg.trac_order;
+            ap.iw = cfg->intensity_w;
+            ap.renorm = cfg->renormalize == 1;
+            ap.poscon = cfg->remove_con == 1;
+            ap.state = static_cast<const float*>(ctx->tstate.p);
+            ap.state_stride = V;
+            ap.rad = static_cast<const float*>(ctx->rad.p);
+            ap.inten = static_cast<const float*>(ctx->inten.p);
+            ap.gmap = gmap;
+            ap.nmap = nreg;
+            ap.gS = static_cast<float*>(ctx->gS.p);
+            ap.gI = static_cast<float*>(ctx->gI.p);
+            ap.err = err;
+            e = launch_temporal_stream_adjoint(ap, V, st);
+            if (e) return cuda_fail((cudaError_t)e, "temporal adjoint launch");
+            ctx->launches += 2;
+            if ((s = adjoint_slab(ctx, cfg, ip, dims, blk, gmap, nreg, st, t_lo, t_hi))) return s;
+        }
+    }
+    return RFBA_OK;
+}
+
+// Volumes per batch of a backward: batches only where the context forces a
+// size (rfba_ctx_set_time_batch > 0) and the method carries (TRA, TRAC with
+// ITC 0); otherwise z slices, which recompute the forward once instead of twice.
+static int backward_time_batch(const rfba_ctx* ctx, const rfba_srrf_config& cfg, int T) {
+    if (!(cfg.method == 1 || (cfg.method == 3 && cfg.itc == 0))) return 0;
+    return ctx->time_batch > 0 && ctx->time_batch < T ? ctx->time_batch : 0;
 }
 
 static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* in, const float* shifts,
@@ -1187,9 +1320,13 @@ static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const flo
         RFBA_CUDA(cudaMemsetAsync(ctx->errw.p, 0, 8, st), "check word clear");
         const float* ip = nullptr;
         if ((s = apply_drift(ctx, in, shifts, dims, st, &ip))) return s;
-        std::vector<BlockDev> all;
-        if ((s = make_blocks(ctx, *cfg, dims, &b, 1, &all))) return s;
         RFBA_CUDA(cudaMemsetAsync(ctx->gin.p, 0, nin * 4, st), "adjoint clear");
+        const int btb = backward_time_batch(ctx, *cfg, T);
+        if (btb > 0) {
+            if ((s = backward_batched(ctx, cfg, ip, dims, b, btb, gmap, nreg, st))) return s;
+        }
+        std::vector<BlockDev> all;
+        if (btb == 0 && (s = make_blocks(ctx, *cfg, dims, &b, 1, &all))) return s;
         // the recomputed stacks must stay as the radiality kernel wrote them: TRAC
         // with ITC 1 would bin them in place, so its map (unused here) is formed
         // with ITC 0, which only reads them

@@ -148,6 +148,7 @@ struct rfba_ctx {
     int time_batch = 0;
     int last_time_batch = 0, last_batches = 0;
     rfba::DevBuf tstate;
+    bool keep_tstate = false;  // a time-batched forward stores its final state (for the backward)
     // differentiable path: buffers and the forward the backward can reuse
     rfba::DevBuf shifted, tmp1, tmp2, gS, gI, gin, dshift, ablocks, atiles, acounter, errw;
     struct Train {

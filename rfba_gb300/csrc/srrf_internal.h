@@ -158,11 +158,30 @@ struct StreamParams {
     int t_lo, t_hi;        // this batch; the stacks hold its [t_hi - t_lo][v]
     int method, order, iw;
     int last;              // write the map after this batch
+    int keep;              // after the last batch, store the state as well (for a backward)
     float* state;          // [field][state_stride]
     long long state_stride;
     const float* rad_stack;
     const float* int_stack;
     float* out;
+};
+
+// Adjoint of the carried temporal reduction for one batch of one block
+// (temporal_stream.cu): dL/dS and dL/dI of the volumes [t_lo, t_hi) from
+// dL/dmap, the final carried state and the window stacks [w_lo, w_hi).
+struct StreamAdjParams {
+    const BlockDev* block;  // stack_off 0
+    int T, t_lo, t_hi, w_lo, w_hi;
+    int method, order, iw, renorm, poscon;
+    const float* state;
+    long long state_stride;
+    const float* rad;    // [t - w_lo][v]
+    const float* inten;
+    const float* gmap;
+    long long nmap;
+    float* gS;           // [t - t_lo][v]
+    float* gI;
+    unsigned long long* err;
 };
 
 // Adjoint inputs and output of the radiality adjoint kernel.
@@ -200,6 +219,7 @@ int tile_rows_for_mag(int my);
 int radiality_max_ctas_per_sm(const RadParams& p, int in_u16, int* out);
 int launch_temporal(const TemporalParams& p, void* stream);
 int launch_temporal_stream(const StreamParams& p, void* stream);
+int launch_temporal_stream_adjoint(const StreamAdjParams& p, long long vox, void* stream);
 // state floats per subvoxel for a method (0 TRM, 1 TRA, 2 TRPPM, 3 TRAC ITC 0) and TRAC order
 int temporal_stream_fields(int method, int order);
 int launch_combine(const double* spots, long long n, int zoom, int Xp, int Yp, int Zp, int r, int rz, int thr,

@@ -186,11 +186,11 @@ __device__ __forceinline__ void trac_carry(const StreamParams& p, long long g, c
         for (int j = K - 2; j > 0; --j) prev[j] = prev[j - 1];
         prev[0] = y;
     });
-    if (!p.last) {
+    if (!p.last || p.keep) {
 #pragma unroll
         for (int f = 0; f < NF; ++f) st[f * S] = reg[f];
-        return;
     }
+    if (!p.last) return;
     double out = 0.0;
     if (N > 0) {
         const double c = ysum.value() / (double)p.T;
@@ -298,7 +298,185 @@ __global__ void __launch_bounds__(kStreamThreads) temporal_stream_kernel(const S
     p.out[B.out_offset + x * B.out_stride[0] + y * B.out_stride[1] + z * B.out_stride[2]] = result;
 }
 
+// Window sums of deviation products d_t = r_t - mean, in double, from the
+// carried sums of y_t = r_t - K (c = mean - K): S_j = sum_{t<N} d_{t+j},
+// P_ij = sum d_{t+i} d_{t+j}, P_ijk, P_0123 over the window t = 0 .. N-1.
+struct DevSums {
+    double S[4], P2[6], P3[4], P4;  // P2: 01 02 03 12 13 23; P3: 012 013 023 123
+};
+
+template <int K>
+__device__ __forceinline__ DevSums deviation_sums(const float* st, long long S, double c, double n) {
+    constexpr int base = 5 + (K - 1);
+    auto v = [&](int i) { return (double)st[(base + 2 * i) * S] - (double)st[(base + 2 * i + 1) * S]; };
+    DevSums d;
+    for (int i = 0; i < 4; ++i) d.S[i] = 0.0;
+    for (int i = 0; i < 6; ++i) d.P2[i] = 0.0;
+    for (int i = 0; i < 4; ++i) d.P3[i] = 0.0;
+    d.P4 = 0.0;
+    double ys[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int j = 0; j < K; ++j) {
+        ys[j] = v(j);
+        d.S[j] = ys[j] - n * c;
+    }
+    if (K == 2) {
+        d.P2[0] = v(2) - c * (ys[0] + ys[1]) + n * c * c;
+    } else if (K == 3) {
+        const double p01 = v(3), p02 = v(4), p12 = v(5);
+        d.P2[0] = p01 - c * (ys[0] + ys[1]) + n * c * c;
+        d.P2[1] = p02 - c * (ys[0] + ys[2]) + n * c * c;
+        d.P2[3] = p12 - c * (ys[1] + ys[2]) + n * c * c;
+        d.P3[0] = v(6) - c * (p01 + p02 + p12) + c * c * (ys[0] + ys[1] + ys[2]) - n * c * c * c;
+    } else {
+        const int pi[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+        double py[6];
+        for (int q = 0; q < 6; ++q) {
+            py[q] = v(4 + q);
+            d.P2[q] = py[q] - c * (ys[pi[q][0]] + ys[pi[q][1]]) + n * c * c;
+        }
+        // triples 012, 013, 023, 123 and the pairs each contains
+        const int tri[4][3] = {{0, 1, 2}, {0, 1, 3}, {0, 2, 3}, {1, 2, 3}};
+        const int tp[4][3] = {{0, 1, 3}, {0, 2, 4}, {1, 2, 5}, {3, 4, 5}};
+        double p3y[4];
+        for (int q = 0; q < 4; ++q) {
+            p3y[q] = v(10 + q);
+            d.P3[q] = p3y[q] - c * (py[tp[q][0]] + py[tp[q][1]] + py[tp[q][2]]) +
+                      c * c * (ys[tri[q][0]] + ys[tri[q][1]] + ys[tri[q][2]]) - n * c * c * c;
+        }
+        d.P4 = v(14) - c * (p3y[0] + p3y[1] + p3y[2] + p3y[3]) +
+               c * c * (py[0] + py[1] + py[2] + py[3] + py[4] + py[5]) -
+               c * c * c * (ys[0] + ys[1] + ys[2] + ys[3]) + n * c * c * c * c;
+    }
+    return d;
+}
+
+// Adjoint of the carried temporal reduction for the volumes [t_lo, t_hi) of
+// one block (temporal_adjoint_kernel's derivatives, kernel.cu:291-327 and
+// 423-500, with the whole-series quantities taken from the carried state):
+// TRA needs only whether every radiality value was finite (the state pass runs
+// the TRAC-2 carry, whose sum of y is finite exactly then); TRAC with ITC 0
+// needs the mean, the intensity-weighted mean, the cumulant and its window
+// pair sums, and the mean over s of dC/da_s, all polynomials in the carried
+// sums; dC/da_t itself reads the deviations of volumes t - k + 1 .. t + k - 1
+// from the window stacks, which hold [w_lo, w_hi) (the batch and that halo).
+template <int K>
+__device__ __forceinline__ void trac_adjoint_batch(const StreamAdjParams& p, long long v, long long V, float g,
+                                                  const float* st, long long S) {
+    const int T = p.T;
+    const float invT = 1.f / (float)T;
+    const double c = ((double)st[S] - (double)st[2 * S]) / (double)T;
+    const float m = (float)((double)st[0] + c);
+    const float IW = (float)(((double)st[3 * S] - (double)st[4 * S]) / (double)T);
+    const int N = T - K;
+    float C = 0.f, AB = 0.f, CD = 0.f, AC = 0.f, BD = 0.f, AD = 0.f, BC = 0.f, mean_d = 0.f;
+    if (N > 0) {
+        const DevSums d = deviation_sums<K>(st, S, c, (double)N);
+        double sumd;
+        if (K == 2) {
+            C = (float)d.P2[0];
+            sumd = d.S[0] + d.S[1];
+        } else if (K == 3) {
+            C = (float)d.P3[0];
+            sumd = d.P2[3] + d.P2[1] + d.P2[0];
+        } else {
+            const double ab = d.P2[0], ac = d.P2[1], ad = d.P2[2], bc = d.P2[3], bd = d.P2[4], cd = d.P2[5];
+            C = (float)(d.P4 - ab * cd - ac * bd - ad * bc);
+            AB = (float)ab, AC = (float)ac, AD = (float)ad, BC = (float)bc, BD = (float)bd, CD = (float)cd;
+            sumd = (d.P3[3] + d.P3[2] + d.P3[1] + d.P3[0]) - (d.S[1] * cd + d.S[2] * bd + d.S[3] * bc) -
+                   (d.S[0] * cd + d.S[3] * ac + d.S[2] * ad) - (d.S[3] * ab + d.S[0] * bd + d.S[1] * ad) -
+                   (d.S[2] * ab + d.S[1] * ac + d.S[0] * bc);
+        }
+        mean_d = (float)(sumd / (double)T);
+    }
+    const float* r = p.rad + v;
+    const float* I = p.inten + v;
+    auto a = [&](int t) -> float { return (t >= 0 && t < T) ? r[(long long)(t - p.w_lo) * V] - m : 0.f; };
+    auto dCda = [&](int s) -> float {
+        float d = 0.f;
+        for (int l = 0; l < K; ++l) {
+            const int t0 = s - l;  // the product starting at t0 holds a_s at lag l
+            if (t0 < 0 || t0 >= N) continue;
+            if (K == 2) {
+                d += a(t0 + 1 - l);
+            } else if (K == 3) {
+                float q = 1.f;
+                for (int j = 0; j < 3; ++j)
+                    if (j != l) q *= a(t0 + j);
+                d += q;
+            } else {
+                const float A = a(t0), Bv = a(t0 + 1), Cv = a(t0 + 2), Dv = a(t0 + 3);
+                if (l == 0) d += Bv * Cv * Dv - Bv * CD - Cv * BD - Dv * BC;
+                if (l == 1) d += A * Cv * Dv - A * CD - Dv * AC - Cv * AD;
+                if (l == 2) d += A * Bv * Dv - Dv * AB - A * BD - Bv * AD;
+                if (l == 3) d += A * Bv * Cv - Cv * AB - Bv * AC - A * BC;
+            }
+        }
+        return d;
+    };
+    const float scale_iw = p.iw ? IW : 1.f;
+    const float sgn = C > 0.f ? 1.f : (C < 0.f ? -1.f : 0.f);
+    const float aC = fabsf(C);
+    for (int t = p.t_lo; t < p.t_hi; ++t) {
+        const float rv = r[(long long)(t - p.w_lo) * V], Iv = I[(long long)(t - p.w_lo) * V];
+        float gr = g * (sgn * invT * scale_iw * (dCda(t) - mean_d) + (p.iw ? aC * invT * Iv * invT : 0.f));
+        const float gi = p.iw ? g * aC * invT * rv * invT : 0.f;
+        if (p.renorm) gr *= 0.5f;
+        if (p.poscon && !(rv > 0.f)) gr = 0.f;
+        p.gS[(long long)(t - p.t_lo) * V + v] = gr;
+        p.gI[(long long)(t - p.t_lo) * V + v] = Iv > 0.f ? gi : 0.f;
+    }
+}
+
+__global__ void __launch_bounds__(256) temporal_stream_adjoint_kernel(const StreamAdjParams p) {
+    const BlockDev& B = *p.block;
+    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= B.vox) return;
+    const long long V = B.vox;
+    const long long nx = B.nreg[0], ny = B.nreg[1];
+    const long long x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
+    const long long gidx = B.out_offset + x * B.out_stride[0] + y * B.out_stride[1] + z * B.out_stride[2];
+    if (gidx < 0 || gidx >= p.nmap) {
+        if (p.err) atomicCAS(p.err, 0ull, (5ull << 56) | ((unsigned long long)gidx & 0x00ffffffffffffffull));
+        return;
+    }
+    const float g = p.gmap[gidx];
+    const float* st = p.state + v;
+    const long long S = p.state_stride;
+    // every radiality value of the series finite: the carried sum of y is
+    const bool finite = isfinite(g) && isfinite(st[S]) && isfinite(st[2 * S]);
+    if (!finite) {
+        for (int t = p.t_lo; t < p.t_hi; ++t) {
+            p.gS[(long long)(t - p.t_lo) * V + v] = 0.f;
+            p.gI[(long long)(t - p.t_lo) * V + v] = 0.f;
+        }
+        return;
+    }
+    if (p.method == 1) {  // TRA
+        const float invT = 1.f / (float)p.T;
+        for (int t = p.t_lo; t < p.t_hi; ++t) {
+            const float rv = p.rad[(long long)(t - p.w_lo) * V + v], Iv = p.inten[(long long)(t - p.w_lo) * V + v];
+            float gr = g * (p.iw ? Iv : 1.f) * invT;
+            const float gi = p.iw ? g * rv * invT : 0.f;
+            if (p.renorm) gr *= 0.5f;
+            if (p.poscon && !(rv > 0.f)) gr = 0.f;
+            p.gS[(long long)(t - p.t_lo) * V + v] = gr;
+            p.gI[(long long)(t - p.t_lo) * V + v] = Iv > 0.f ? gi : 0.f;
+        }
+        return;
+    }
+    if (p.order == 3) trac_adjoint_batch<3>(p, v, V, g, st, S);
+    else if (p.order == 4) trac_adjoint_batch<4>(p, v, V, g, st, S);
+    else trac_adjoint_batch<2>(p, v, V, g, st, S);
+}
+
 }  // namespace
+
+int launch_temporal_stream_adjoint(const StreamAdjParams& p, long long vox, void* stream) {
+    if (vox == 0 || p.t_hi <= p.t_lo) return 0;
+    const long long grid = (vox + 255) / 256;
+    temporal_stream_adjoint_kernel<<<(unsigned)grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(p);
+    return (int)cudaGetLastError();
+}
 
 int launch_temporal_stream(const StreamParams& p, void* stream) {
     if (p.total_vox == 0 || p.t_hi <= p.t_lo) return 0;

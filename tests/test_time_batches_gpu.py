@@ -139,3 +139,55 @@ def test_itc1_never_batched(ctx):
         assert ctx.last_time_batches() == (0, 0)
     finally:
         ctx.set_time_batch(0)
+
+
+def _drift_case(seed, T, D, H, W):
+    from rfba_gb300 import synth
+    scene = synth.make_scene(seed, T, (W, H, D), 10)
+    x = synth.render(scene, (W, H, D), seed, np.float32)
+    sh = np.random.default_rng(seed).normal(0, 0.3, size=(T, 3)).astype(np.float32)
+    return x, sh
+
+
+def _fwd_bwd(ctx, cfg, x, sh):
+    import torch
+    xd = torch.from_numpy(x).cuda()
+    sd = torch.from_numpy(sh).cuda()
+    m = ctx.forward_shifted(cfg, xd, sd)
+    torch.cuda.synchronize()
+    mh = m.cpu().numpy()
+    f = np.where(np.isfinite(mh), mh, 0.0).astype(np.float64)
+    g = np.where(np.isfinite(mh), -f / np.sqrt(np.sum(f * f)), 0.0).astype(np.float32)
+    din, dsh = ctx.backward(cfg, xd, sd, torch.from_numpy(g).cuda())
+    torch.cuda.synchronize()
+    return mh, din.cpu().numpy(), dsh.cpu().numpy()
+
+
+@pytest.mark.parametrize("kw,T,batch", [
+    (dict(method=1, intensity_w=1), 23, 5),
+    (dict(method=1, intensity_w=0, renormalize=1), 17, 4),
+    (dict(method=3, itc=0, trac_order=2, intensity_w=1), 23, 5),
+    (dict(method=3, itc=0, trac_order=3, intensity_w=0, remove_con=1), 19, 3),
+    (dict(method=3, itc=0, trac_order=4, intensity_w=1), 26, 7),
+    (dict(method=3, itc=0, trac_order=4, intensity_w=1, renormalize=1), 9, 2),
+    (dict(method=3, itc=0, trac_order=4, intensity_w=0), 5, 1),
+], ids=["tra_iw", "tra_renorm", "trac2_iw", "trac3_poscon", "trac4_iw", "trac4_renorm_short", "trac4_T5"])
+def test_backward_in_time_batches(ctx, kw, T, batch):
+    """The drift-corrected forward and its backward in time batches (forced
+    size): the backward's state pass, the windows of batch + k - 1 volumes on
+    either side and the carried derivatives give the gradients of the
+    resident one-pass path to 1e-4 (float atomics and summation order)."""
+    from tests.parity import rel_linf
+    from rfba_gb300 import srrf
+    cfg = srrf.Config.make(mag=2, **kw, **SHIPPED)
+    x, sh = _drift_case(100 + T, T, 7, 8, 9)
+    m0, din0, dsh0 = _fwd_bwd(ctx, cfg, x, sh)
+    ctx.set_time_batch(batch)
+    try:
+        m1, din1, dsh1 = _fwd_bwd(ctx, cfg, x, sh)
+    finally:
+        ctx.set_time_batch(0)
+    assert np.array_equal(np.isnan(m0), np.isnan(m1))
+    assert rel_linf(m1, m0) < 1e-5
+    assert rel_linf(din1, din0) < 1e-4, rel_linf(din1, din0)
+    assert rel_linf(dsh1, dsh0) < 1e-4, rel_linf(dsh1, dsh0)
