@@ -435,8 +435,8 @@ static int enqueue_passes(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void
         sp.method = cfg.method;
         sp.order = cfg.trac_order;
         sp.iw = cfg.intensity_w;
-        sp.state = static_cast<float*>(ctx->tstate.p);
-        sp.state_stride = ps.max_vox;
+        sp.state = ctx->tstate_ext ? ctx->tstate_ext : static_cast<float*>(ctx->tstate.p);
+        sp.state_stride = ctx->tstate_ext ? ctx->tstate_ext_stride : ps.max_vox;
         sp.keep = ctx->keep_tstate ? 1 : 0;
         sp.rad_stack = rp.rad_stack;
         sp.int_stack = rp.int_stack;
@@ -531,6 +531,7 @@ static int run_device(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void* in
                       const int dims[4], const std::vector<BlockDev>& all, float* out_dev, cudaStream_t st,
                       const Tuning& tune = Tuning()) {
     ctx->train.valid = false;
+    if (!ctx->tstate_ext) ctx->trainb.valid = false;
     PassSet ps;
     int s;
     if ((s = ctx->errw.ensure(256, "check word"))) return s;
@@ -538,7 +539,9 @@ static int run_device(rfba_ctx* ctx, const rfba_srrf_config& cfg, const void* in
     const size_t np = ps.passes.size();
     if ((s = ctx->rad.ensure((size_t)ps.max_stack * 4, "radiality stack"))) return s;
     if ((s = ctx->inten.ensure((size_t)ps.max_stack * 4, "intensity stack"))) return s;
-    if (ps.tb > 0 && (s = ctx->tstate.ensure((size_t)ps.fields * ps.max_vox * 4, "temporal state"))) return s;
+    if (ps.tb > 0 && !ctx->tstate_ext &&
+        (s = ctx->tstate.ensure((size_t)ps.fields * ps.max_vox * 4, "temporal state")))
+        return s;
     if ((s = ctx->blocks.ensure(ps.blocks.size() * sizeof(BlockDev), "blocks"))) return s;
     if ((s = ctx->tiles.ensure(ps.tiles.size() * sizeof(TileDesc), "tiles"))) return s;
     if ((s = ctx->prefix.ensure(ps.prefix.size() * sizeof(long long), "prefix"))) return s;
@@ -913,6 +916,7 @@ static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, con
                 gp = ctx->graphs.front().get();
             }
             ctx->train.valid = false;
+            ctx->trainb.valid = false;
             RFBA_CUDA(cudaGraphLaunch(gp->exec, st), "graph launch");
             account(ctx, gp->ps);
             ctx->last_graph = 1;
@@ -963,6 +967,14 @@ static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, con
 
 // ---------------------------------------------------------------------------
 // Differentiable path
+
+// Volumes per batch of a backward: batches only where the context forces a
+// size (rfba_ctx_set_time_batch > 0) and the method carries (TRA, TRAC with
+// ITC 0); otherwise z slices, which recompute the forward once instead of twice.
+static int backward_time_batch(const rfba_ctx* ctx, const rfba_srrf_config& cfg, int T) {
+    if (!(cfg.method == 1 || (cfg.method == 3 && cfg.itc == 0))) return 0;
+    return ctx->time_batch > 0 && ctx->time_batch < T ? ctx->time_batch : 0;
+}
 
 static bool same_cfg(const rfba_srrf_config& a, const rfba_srrf_config& b) {
     return std::memcmp(&a, &b, sizeof a) == 0;
@@ -1061,6 +1073,49 @@ static int forward_shifted_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, co
     if ((s = region_block(cfg, dims, rlo, rhi, &b, &n))) return s;
     const float* ip = nullptr;
     if ((s = apply_drift(ctx, in, shifts, dims, st, &ip))) return s;
+    ctx->trainb.valid = false;
+    const int T = dims[3];
+    const int tbb = (!rlo && cfg->method == 3 && cfg->itc == 0) ? backward_time_batch(ctx, *cfg, T) : 0;
+    if (tbb > 0) {
+        // TRAC in forced time batches: the map in the z slices the backward
+        // will use, every slice's final carried state kept (slice i at off[i],
+        // stride total) so that the backward needs no state pass of its own
+        if ((s = ensure_plan(ctx, *cfg, st))) return s;
+        const int fields = temporal_stream_fields(3, cfg->trac_order);
+        const int wl = std::min(T, tbb + 2 * (cfg->trac_order - 1));
+        std::vector<BlockDev> all;
+        if ((s = make_blocks(ctx, *cfg, dims, &b, 1, &all, 0, wl + tbb, fields))) return s;
+        std::vector<long long> off;
+        long long total = 0;
+        for (const BlockDev& sl : all) {
+            off.push_back(total);
+            total += sl.vox;
+        }
+        if ((s = ctx->tstate.ensure((size_t)fields * (size_t)total * 4, "temporal state"))) return s;
+        Tuning tt;
+        tt.tb = tbb;
+        for (size_t i = 0; i < all.size(); ++i) {
+            std::vector<BlockDev> one(1, all[i]);
+            ctx->tstate_ext = static_cast<float*>(ctx->tstate.p) + off[i];
+            ctx->tstate_ext_stride = total;
+            ctx->keep_tstate = true;
+            s = run_device(ctx, *cfg, ip, RFBA_F32, dims, one, out, st, tt);
+            ctx->tstate_ext = nullptr;
+            ctx->keep_tstate = false;
+            if (s) return s;
+        }
+        ctx->last_passes = (int)all.size();
+        ctx->trainb.valid = true;
+        ctx->trainb.cfg = *cfg;
+        for (int a = 0; a < 4; ++a) ctx->trainb.dims[a] = dims[a];
+        ctx->trainb.in = in;
+        ctx->trainb.shifts = shifts;
+        ctx->trainb.tb = tbb;
+        ctx->trainb.slabs = all;
+        ctx->trainb.off = off;
+        ctx->trainb.total = total;
+        return read_checks(ctx, st, "forward_shifted");
+    }
     if ((s = forward_blocks_locked(ctx, cfg, ip, RFBA_F32, dims, &b, 1, out, n, RFBA_DEVICE_PTRS, st, false)))
         return s;
     // the backward can reuse this forward's stacks when they are all resident
@@ -1173,7 +1228,10 @@ static int adjoint_slab(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float*
 // into dL/dI'. Scratch per subvoxel: the window's stacks, the batch's adjoint
 // stacks and the state, instead of the whole series' four stacks.
 static int backward_batched(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* ip, const int dims[4],
-                            const rfba_block& b, int tb, const float* gmap, long long nreg, cudaStream_t st) {
+                            const rfba_block& b, int tb, const float* gmap, long long nreg, cudaStream_t st,
+                            bool kept) {
+    // kept: the forward before this call ran in these batches and kept every
+    // slice's final state (ctx->trainb): no state pass
     int s;
     const int T = dims[3];
     const bool trac = cfg->method == 3;
@@ -1189,16 +1247,27 @@ static int backward_batched(rfba_ctx* ctx, const rfba_srrf_config* cfg, const fl
     const int fields = temporal_stream_fields(3, scfg.trac_order);
     const int wl = std::min(T, tb + 2 * h);
     std::vector<BlockDev> all;
-    if ((s = make_blocks(ctx, scfg, dims, &b, 1, &all, 0, wl + tb, fields))) return s;
+    if (kept)
+        all = ctx->trainb.slabs;
+    else if ((s = make_blocks(ctx, scfg, dims, &b, 1, &all, 0, wl + tb, fields)))
+        return s;
     unsigned long long* err = static_cast<unsigned long long*>(ctx->errw.p);
-    for (const BlockDev& slab : all) {
+    for (size_t si = 0; si < all.size(); ++si) {
+        const BlockDev& slab = all[si];
         std::vector<BlockDev> one(1, slab);
-        Tuning ts;
-        ts.tb = tb;
-        ctx->keep_tstate = true;
-        s = run_device(ctx, scfg, ip, RFBA_F32, dims, one, static_cast<float*>(ctx->out.p), st, ts);
-        ctx->keep_tstate = false;
-        if (s) return s;
+        const float* state = static_cast<const float*>(ctx->tstate.p);
+        long long sstride = slab.vox;
+        if (kept) {
+            state += ctx->trainb.off[si];
+            sstride = ctx->trainb.total;
+        } else {
+            Tuning ts;
+            ts.tb = tb;
+            ctx->keep_tstate = true;
+            s = run_device(ctx, scfg, ip, RFBA_F32, dims, one, static_cast<float*>(ctx->out.p), st, ts);
+            ctx->keep_tstate = false;
+            if (s) return s;
+        }
         // the window plan: the same slab with wl volumes of stacks
         PassSet ps;
         Tuning tw;
@@ -1260,8 +1329,8 @@ static int backward_batched(rfba_ctx* ctx, const rfba_srrf_config* cfg, const fl
             ap.iw = cfg->intensity_w;
             ap.renorm = cfg->renormalize == 1;
             ap.poscon = cfg->remove_con == 1;
-            ap.state = static_cast<const float*>(ctx->tstate.p);
-            ap.state_stride = V;
+            ap.state = state;
+            ap.state_stride = sstride;
             ap.rad = static_cast<const float*>(ctx->rad.p);
             ap.inten = static_cast<const float*>(ctx->inten.p);
             ap.gmap = gmap;
@@ -1276,14 +1345,6 @@ static int backward_batched(rfba_ctx* ctx, const rfba_srrf_config* cfg, const fl
         }
     }
     return RFBA_OK;
-}
-
-// Volumes per batch of a backward: batches only where the context forces a
-// size (rfba_ctx_set_time_batch > 0) and the method carries (TRA, TRAC with
-// ITC 0); otherwise z slices, which recompute the forward once instead of twice.
-static int backward_time_batch(const rfba_ctx* ctx, const rfba_srrf_config& cfg, int T) {
-    if (!(cfg.method == 1 || (cfg.method == 3 && cfg.itc == 0))) return 0;
-    return ctx->time_batch > 0 && ctx->time_batch < T ? ctx->time_batch : 0;
 }
 
 static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* in, const float* shifts,
@@ -1322,8 +1383,12 @@ static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const flo
         if ((s = apply_drift(ctx, in, shifts, dims, st, &ip))) return s;
         RFBA_CUDA(cudaMemsetAsync(ctx->gin.p, 0, nin * 4, st), "adjoint clear");
         const int btb = backward_time_batch(ctx, *cfg, T);
+        const bool kept = btb > 0 && !rlo && ctx->trainb.valid && ctx->trainb.tb == btb &&
+                          same_cfg(ctx->trainb.cfg, *cfg) && ctx->trainb.in == in && ctx->trainb.shifts == shifts &&
+                          ctx->trainb.dims[0] == dims[0] && ctx->trainb.dims[1] == dims[1] &&
+                          ctx->trainb.dims[2] == dims[2] && ctx->trainb.dims[3] == dims[3];
         if (btb > 0) {
-            if ((s = backward_batched(ctx, cfg, ip, dims, b, btb, gmap, nreg, st))) return s;
+            if ((s = backward_batched(ctx, cfg, ip, dims, b, btb, gmap, nreg, st, kept))) return s;
         }
         std::vector<BlockDev> all;
         if (btb == 0 && (s = make_blocks(ctx, *cfg, dims, &b, 1, &all))) return s;

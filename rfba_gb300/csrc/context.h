@@ -149,6 +149,22 @@ struct rfba_ctx {
     int last_time_batch = 0, last_batches = 0;
     rfba::DevBuf tstate;
     bool keep_tstate = false;  // a time-batched forward stores its final state (for the backward)
+    // when set, the carried state lives here ([field][tstate_ext_stride]) instead of tstate
+    float* tstate_ext = nullptr;
+    long long tstate_ext_stride = 0;
+    // a drift-corrected forward in time batches whose slices' final states are
+    // kept in tstate (slice i at off[i], stride total) for the backward
+    struct TrainBatched {
+        bool valid = false;
+        rfba_srrf_config cfg;
+        int dims[4] = {0, 0, 0, 0};
+        const void* in = nullptr;
+        const void* shifts = nullptr;
+        int tb = 0;
+        std::vector<rfba::BlockDev> slabs;
+        std::vector<long long> off;
+        long long total = 0;
+    } trainb;
     // differentiable path: buffers and the forward the backward can reuse
     rfba::DevBuf shifted, tmp1, tmp2, gS, gI, gin, dshift, ablocks, atiles, acounter, errw;
     struct Train {

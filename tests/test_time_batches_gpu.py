@@ -191,3 +191,33 @@ def test_backward_in_time_batches(ctx, kw, T, batch):
     assert rel_linf(m1, m0) < 1e-5
     assert rel_linf(din1, din0) < 1e-4, rel_linf(din1, din0)
     assert rel_linf(dsh1, dsh0) < 1e-4, rel_linf(dsh1, dsh0)
+
+
+def test_backward_after_an_intervening_forward(ctx):
+    """A forward on other data between a time-batched drift forward and its
+    backward overwrites the carried state the backward would reuse: the
+    backward must then run its own state pass and still give the resident
+    path's gradients."""
+    import torch
+    from tests.parity import rel_linf
+    from rfba_gb300 import srrf
+    cfg = srrf.Config.make(mag=2, method=3, itc=0, trac_order=4, intensity_w=1, **SHIPPED)
+    x, sh = _drift_case(131, 21, 7, 8, 9)
+    other, _ = _drift_case(132, 21, 7, 8, 9)
+    m0, din0, dsh0 = _fwd_bwd(ctx, cfg, x, sh)
+    ctx.set_time_batch(6)
+    try:
+        xd = torch.from_numpy(x).cuda()
+        sd = torch.from_numpy(sh).cuda()
+        m1 = ctx.forward_shifted(cfg, xd, sd).cpu().numpy()
+        ctx.forward_shifted(cfg, torch.from_numpy(other).cuda(), sd)  # same shape, other data
+        f = np.where(np.isfinite(m1), m1, 0.0).astype(np.float64)
+        g = np.where(np.isfinite(m1), -f / np.sqrt(np.sum(f * f)), 0.0).astype(np.float32)
+        din1, dsh1 = ctx.backward(cfg, xd, sd, torch.from_numpy(g).cuda())
+        torch.cuda.synchronize()
+        din1, dsh1 = din1.cpu().numpy(), dsh1.cpu().numpy()
+    finally:
+        ctx.set_time_batch(0)
+    assert rel_linf(m1, m0) < 1e-5
+    assert rel_linf(din1, din0) < 1e-4
+    assert rel_linf(dsh1, dsh0) < 1e-4
