@@ -968,12 +968,18 @@ static int forward_blocks_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, con
 // ---------------------------------------------------------------------------
 // Differentiable path
 
-// Volumes per batch of a backward: batches only where the context forces a
-// size (rfba_ctx_set_time_batch > 0) and the method carries (TRA, TRAC with
-// ITC 0); otherwise z slices, which recompute the forward once instead of twice.
-static int backward_time_batch(const rfba_ctx* ctx, const rfba_srrf_config& cfg, int T) {
+// Volumes per batch of a drift-corrected forward that keeps its carried state
+// for the backward, and of that backward (0: z slices). TRA and TRAC with ITC 0
+// carry; a forced size (rfba_ctx_set_time_batch > 0) applies to both. The
+// automatic choice batches TRAC with ITC 0 when the whole series' stacks
+// exceed the budget: its forward keeps every slice's state, so the backward
+// needs no extra forward pass and holds a fifth of the scratch of z slices.
+static int drift_time_batch(const rfba_ctx* ctx, const rfba_srrf_config& cfg, int T, double vox) {
     if (!(cfg.method == 1 || (cfg.method == 3 && cfg.itc == 0))) return 0;
-    return ctx->time_batch > 0 && ctx->time_batch < T ? ctx->time_batch : 0;
+    if (ctx->time_batch < 0) return 0;
+    if (ctx->time_batch > 0) return ctx->time_batch < T ? ctx->time_batch : 0;
+    if (cfg.method == 3 && T > kTimeBatch && vox * T * 2 * sizeof(float) > (double)ctx->budget) return kTimeBatch;
+    return 0;
 }
 
 static bool same_cfg(const rfba_srrf_config& a, const rfba_srrf_config& b) {
@@ -1075,7 +1081,8 @@ static int forward_shifted_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, co
     if ((s = apply_drift(ctx, in, shifts, dims, st, &ip))) return s;
     ctx->trainb.valid = false;
     const int T = dims[3];
-    const int tbb = (!rlo && cfg->method == 3 && cfg->itc == 0) ? backward_time_batch(ctx, *cfg, T) : 0;
+    const double rvox = (double)(b.hi[0] - b.lo[0]) * (b.hi[1] - b.lo[1]) * (b.hi[2] - b.lo[2]);
+    const int tbb = (!rlo && cfg->method == 3 && cfg->itc == 0) ? drift_time_batch(ctx, *cfg, T, rvox) : 0;
     if (tbb > 0) {
         // TRAC in forced time batches: the map in the z slices the backward
         // will use, every slice's final carried state kept (slice i at off[i],
@@ -1382,11 +1389,18 @@ static int backward_locked(rfba_ctx* ctx, const rfba_srrf_config* cfg, const flo
         const float* ip = nullptr;
         if ((s = apply_drift(ctx, in, shifts, dims, st, &ip))) return s;
         RFBA_CUDA(cudaMemsetAsync(ctx->gin.p, 0, nin * 4, st), "adjoint clear");
-        const int btb = backward_time_batch(ctx, *cfg, T);
-        const bool kept = btb > 0 && !rlo && ctx->trainb.valid && ctx->trainb.tb == btb &&
-                          same_cfg(ctx->trainb.cfg, *cfg) && ctx->trainb.in == in && ctx->trainb.shifts == shifts &&
-                          ctx->trainb.dims[0] == dims[0] && ctx->trainb.dims[1] == dims[1] &&
-                          ctx->trainb.dims[2] == dims[2] && ctx->trainb.dims[3] == dims[3];
+        // batches when forced, or when the forward before this call ran in batches
+        // and kept its state for these arguments (the automatic case)
+        const bool kept_ok = !rlo && ctx->trainb.valid && same_cfg(ctx->trainb.cfg, *cfg) &&
+                             ctx->trainb.in == in && ctx->trainb.shifts == shifts && ctx->trainb.dims[0] == dims[0] &&
+                             ctx->trainb.dims[1] == dims[1] && ctx->trainb.dims[2] == dims[2] &&
+                             ctx->trainb.dims[3] == dims[3];
+        int btb = (cfg->method == 1 || (cfg->method == 3 && cfg->itc == 0)) && ctx->time_batch > 0 &&
+                          ctx->time_batch < T
+                      ? ctx->time_batch
+                      : 0;
+        if (btb == 0 && ctx->time_batch == 0 && kept_ok) btb = ctx->trainb.tb;
+        const bool kept = btb > 0 && kept_ok && ctx->trainb.tb == btb;
         if (btb > 0) {
             if ((s = backward_batched(ctx, cfg, ip, dims, b, btb, gmap, nreg, st, kept))) return s;
         }

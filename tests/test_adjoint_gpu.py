@@ -149,20 +149,20 @@ def test_backward_in_slices_matches_resident(ctx, oracle_mod):
 
 
 def test_backward_after_time_batched_forward(ctx):
-    """A drift-corrected forward whose series runs in time batches in one spatial
-    pass keeps only its last batch's stacks: the backward must not reuse them,
-    it recomputes the stacks (in z slices) and gives the gradients of the
-    resident path (to the order of the float atomics)."""
+    """A drift-corrected TRA forward whose series runs in time batches in one
+    spatial pass keeps only its last batch's stacks: the backward must not
+    reuse them, it recomputes the stacks (in z slices) and gives the gradients
+    of the resident path (to the order of the float atomics)."""
+    import torch
     from rfba_gb300 import srrf
-    kw = dict(mag=2, method=3, itc=0, trac_order=2, **SHIPPED)
+    kw = dict(mag=2, method=1, intensity_w=1, **SHIPPED)
     cfg = srrf.Config.make(**kw)
     T, D, H, W = 60, 8, 9, 10
     x, sh = _case(29, T, D, H, W, drift=0.2)
     m, din, dsh = _gpu(ctx, cfg, x, sh)
     vox = D * H * W * 8
-    budget = vox * (25 * 8 + 12 * 4) + 4096   # one batch of 25 plus the TRAC-2 state, not all 60 volumes
+    budget = vox * (25 * 8 + 2 * 4) + 4096   # one batch of 25 plus the TRA state, not all 60 volumes
     assert budget < vox * T * 8
-    import torch
     small = srrf.Context(0, budget)
     try:
         xd = torch.from_numpy(x).cuda()
@@ -170,6 +170,41 @@ def test_backward_after_time_batched_forward(ctx):
         m2 = small.forward_shifted(cfg, xd, sd)
         torch.cuda.synchronize()
         assert small.last_time_batches() == (25, 3) and small.last_passes() == 1
+        m2 = m2.cpu().numpy()
+        g = torch.from_numpy(_gmap(m2).astype(np.float32)).cuda()
+        din2, dsh2 = small.backward(cfg, xd, sd, g)
+        torch.cuda.synchronize()
+        din2, dsh2 = din2.cpu().numpy(), dsh2.cpu().numpy()
+    finally:
+        small.close()
+    assert np.array_equal(np.isnan(m), np.isnan(m2))
+    assert rel_linf(m2, m) < 1e-5
+    assert rel_linf(din2, din) < 1e-4
+    assert rel_linf(dsh2, dsh) < 1e-4
+
+
+def test_automatic_batches_keep_the_state_for_the_backward(ctx):
+    """TRAC with ITC 0 on a series whose stacks exceed the budget: the drift-
+    corrected forward runs in batches of 25 volumes in the z slices the backward
+    will use and keeps every slice's carried state; the backward that follows
+    reuses it (batched, no state pass) and gives the resident path's gradients."""
+    import torch
+    from rfba_gb300 import srrf
+    kw = dict(mag=2, method=3, itc=0, trac_order=2, intensity_w=1, **SHIPPED)
+    cfg = srrf.Config.make(**kw)
+    T, D, H, W = 60, 8, 9, 10
+    x, sh = _case(30, T, D, H, W, drift=0.2)
+    m, din, dsh = _gpu(ctx, cfg, x, sh)
+    vox = D * H * W * 8
+    budget = vox * 300
+    assert budget < vox * T * 8
+    small = srrf.Context(0, budget)
+    try:
+        xd = torch.from_numpy(x).cuda()
+        sd = torch.from_numpy(sh).cuda()
+        m2 = small.forward_shifted(cfg, xd, sd)
+        torch.cuda.synchronize()
+        assert small.last_time_batches() == (25, 3)
         m2 = m2.cpu().numpy()
         g = torch.from_numpy(_gmap(m2).astype(np.float32)).cuda()
         din2, dsh2 = small.backward(cfg, xd, sd, g)
