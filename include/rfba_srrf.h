@@ -549,10 +549,13 @@ int rfba_ctx_set_launch(rfba_ctx* ctx, int grid, int t_chunk);
  * batch's stacks and the state still exceed the budget. TRAC with ITC 1 bins
  * the whole series and slices space instead. volumes > 0 forces batches of that
  * many volumes (rfba_srrf_backward then runs in batches too for TRA and TRAC
- * with ITC 0: a state pass, then per batch the radiality of the batch and of
- * the TRAC order - 1 volumes on either side, its temporal adjoint from the
- * carried state and its radiality adjoint), < 0 turns batches off, 0 restores
- * the automatic choice (forward only; the backward slices space). The
+ * with ITC 0: per batch the radiality of the batch and of the TRAC order - 1
+ * volumes on either side, its temporal adjoint from the carried state and its
+ * radiality adjoint), < 0 turns batches off, 0 restores the automatic choice:
+ * batches of 25 where the whole series' stacks exceed the budget; for TRAC with
+ * ITC 0 rfba_srrf_forward_shifted then keeps every slice's carried state and the
+ * rfba_srrf_backward that follows with the same arguments reuses it (without
+ * one, the backward slices space). The
  * reference holds its whole series in memory (GradientCalc.cpp, one block at a
  * time); the batches correspond to streaming the series' frames through HBM. */
 int rfba_ctx_set_time_batch(rfba_ctx* ctx, int volumes);
