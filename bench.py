@@ -826,7 +826,9 @@ def measure_stream(ctx, steps: int = 3, volumes=None) -> dict:
     map), TRAC-4 ITC 0 with intensity weighting; batches of 25 volumes with the
     window sums carried between them (8.4 M subvoxels: 1.7 GB of stacks per
     batch and 1.3 GB of carried state) against all 100 volumes' stacks (6.7 GB)
-    reduced at once. Device input, CUDA events."""
+    reduced at once; then the drift-corrected forward and its backward both
+    ways (the batched backward reusing the state its forward kept), with the
+    gradients compared. Device input, CUDA events."""
     import torch
     from rfba_gb300 import srrf, synth
     x, _ = synth.workload("mid", n_vol=volumes or 100, shape=(64, 64, 64))
@@ -853,14 +855,43 @@ def measure_stream(ctx, steps: int = 3, volumes=None) -> dict:
         res[name] = {"forward_ms": ms, "value": units / (ms / 1e3), "batch_volumes": vb, "batches": nb}
         maps[name] = m.cpu().numpy()
     ctx.set_time_batch(0)
-    a, b = maps["one_pass"].astype(np.float64), maps["time_batches"].astype(np.float64)
-    fin = np.isfinite(a) & np.isfinite(b)
-    scale = float(np.max(np.abs(a[fin]))) if fin.any() else 0.0
-    rel = float(np.max(np.abs(a[fin] - b[fin]))) / scale if scale > 0 else 0.0
+    def rel_linf(got, ref):
+        got, ref = np.asarray(got, np.float64), np.asarray(ref, np.float64)
+        fin = np.isfinite(got) & np.isfinite(ref)
+        scale = float(np.max(np.abs(ref[fin]))) if fin.any() else 0.0
+        return float(np.max(np.abs(got[fin] - ref[fin]))) / scale if scale > 0 else 0.0
+
+    rel = rel_linf(maps["time_batches"], maps["one_pass"])
+    # the drift-corrected forward and its backward (L = -||map||, random shifts of
+    # 0.2 voxel): in batches of 25 volumes with the carried state kept from the
+    # forward for the backward, against the resident one-pass pair
+    xf = xd.to(torch.int32).bitwise_and(0xFFFF).to(torch.float32)
+    sh = torch.from_numpy(np.random.default_rng(7).normal(0, 0.2, size=(T, 3)).astype(np.float32)).cuda()
+    fb = {}
+    for name, tb in (("time_batches", 25), ("one_pass", -1)):
+        ctx.set_time_batch(tb)
+        for rep in range(2):
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record(stream)
+            m = ctx.forward_shifted(cfg, xf, sh, stream=stream.cuda_stream)
+            e1.record(stream)
+            g = torch.where(torch.isnan(m), torch.zeros_like(m),
+                            -torch.nan_to_num(m) / torch.sqrt((torch.nan_to_num(m).double() ** 2).sum()).float())
+            din, dsh = ctx.backward(cfg, xf, sh, g, stream=stream.cuda_stream)
+            e2.record(stream)
+            torch.cuda.synchronize()
+        fb[name] = {"forward_ms": e0.elapsed_time(e1), "forward_backward_ms": e0.elapsed_time(e2),
+                    "din": din.cpu().numpy(), "dsh": dsh.cpu().numpy()}
+    ctx.set_time_batch(0)
+    diff_block = {
+        name: {k: v for k, v in r.items() if k not in ("din", "dsh")} for name, r in fb.items()}
+    diff_block["rel_linf_din"] = rel_linf(fb["time_batches"]["din"], fb["one_pass"]["din"])
+    diff_block["rel_linf_dshift"] = rel_linf(fb["time_batches"]["dsh"], fb["one_pass"]["dsh"])
     return {"workload": "stream: 100 x 64^3 u16 -> 256x256x128 map, mag 4x4x2, TRAC-4 ITC0, IW; time batches of "
                         "25 volumes vs one pass", "voxel_volumes": units, **res,
+            "drift_forward_backward": diff_block,
             "time_batches_over_one_pass": res["time_batches"]["forward_ms"] / res["one_pass"]["forward_ms"],
-            "nan_masks_equal": bool(np.array_equal(np.isnan(a), np.isnan(b))),
+            "nan_masks_equal": bool(np.array_equal(np.isnan(maps["one_pass"]), np.isnan(maps["time_batches"]))),
             "rel_linf_time_batches_vs_one_pass": rel}
 
 
