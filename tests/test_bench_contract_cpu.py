@@ -27,3 +27,20 @@ def test_reference_arm_prints_one_contract_line():
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == line["value"]
     assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
+
+
+def test_temporal_roofline_block():
+    """The bench line's temporal-kernel block: T radiality and T intensity values
+    read and one map value written per subvoxel, over the mean launch time,
+    against the measured copy bandwidth (absent without timings)."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    units, T = 512 * 512 * 128 * 100, 100
+    r = bench.temporal_roofline([6.0, 7.0], units, T, {"hbm_gbs": 6782.1})
+    vox = units // T
+    assert r["algorithmic_bytes"] == vox * (2 * T * 4 + 4)
+    assert abs(r["kernel_ms"] - 6.5) < 1e-12
+    assert abs(r["achieved_gbs"] - r["algorithmic_bytes"] / 6.5e-3 / 1e9) < 1e-6
+    assert abs(r["frac"] - r["achieved_gbs"] / 6782.1) < 1e-12
+    assert bench.temporal_roofline([], units, T, {}) == {}
+    assert bench.temporal_roofline([6.0], units, T, {})["frac"] is None
