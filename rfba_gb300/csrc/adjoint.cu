@@ -492,17 +492,30 @@ __global__ void temporal_adjoint_kernel(const BlockDev* __restrict__ blocks, con
     const float IW = iws.s * invT;
     const float scale_iw = iw ? IW : 1.f;
     float C = 0.f, AB = 0.f, CD = 0.f, AC = 0.f, BD = 0.f, AD = 0.f, BC = 0.f;
+    // sum over s of dC/da_s, in closed form from window sums of the same pass:
+    // order 2: S0 + S1; order 3: P12 + P02 + P01; order 4: the four triple sums
+    // minus each lag's three single-sum x pair-sum terms
+    float sumd = 0.f;
     const int N = T - order;
     if (method == 3) {
-        KSum c1, s4, ab, cd, ac, bd, ad, bc;
+        KSum c1, s4, ab, cd, ac, bd, ad, bc, s0, s1, s2, s3, p012, p013, p023, p123;
         for (int t = 0; t < N; ++t) {
             const float A = r[t * V] - m, Bv = r[(t + 1) * V] - m;
+            s0.add(A);
+            s1.add(Bv);
             if (order == 2) c1.add(A * Bv);
             if (order >= 3) {
                 const float Cv = r[(t + 2) * V] - m;
-                if (order == 3) c1.add(A * Bv * Cv);
+                s2.add(Cv);
+                if (order == 3) {
+                    c1.add(A * Bv * Cv);
+                    ab.add(A * Bv);
+                    ac.add(A * Cv);
+                    bc.add(Bv * Cv);
+                }
                 if (order == 4) {
                     const float Dv = r[(t + 3) * V] - m;
+                    s3.add(Dv);
                     s4.add(A * Bv * Cv * Dv);
                     ab.add(A * Bv);
                     cd.add(Cv * Dv);
@@ -510,12 +523,25 @@ __global__ void temporal_adjoint_kernel(const BlockDev* __restrict__ blocks, con
                     bd.add(Bv * Dv);
                     ad.add(A * Dv);
                     bc.add(Bv * Cv);
+                    p012.add(A * Bv * Cv);
+                    p013.add(A * Bv * Dv);
+                    p023.add(A * Cv * Dv);
+                    p123.add(Bv * Cv * Dv);
                 }
             }
         }
         C = c1.s;
         AB = ab.s, CD = cd.s, AC = ac.s, BD = bd.s, AD = ad.s, BC = bc.s;
         if (order == 4) C = s4.s - AB * CD - AC * BD - AD * BC;
+        if (order == 2) {
+            sumd = s0.s + s1.s;
+        } else if (order == 3) {
+            sumd = BC + AC + AB;
+        } else {
+            sumd = (p123.s + p023.s + p013.s + p012.s) - (s1.s * CD + s2.s * BD + s3.s * BC) -
+                   (s0.s * CD + s3.s * AC + s2.s * AD) - (s3.s * AB + s0.s * BD + s1.s * AD) -
+                   (s2.s * AB + s1.s * AC + s0.s * BC);
+        }
     }
     // dC/da_s for every s, then centring (dC/dr_t = dC/da_t - mean_s dC/da_s)
     auto dCda = [&](int s) -> float {
@@ -540,10 +566,7 @@ __global__ void temporal_adjoint_kernel(const BlockDev* __restrict__ blocks, con
         }
         return d;
     };
-    KSum md;
-    if (method == 3)
-        for (int s = 0; s < T; ++s) md.add(dCda(s));
-    const float mean_d = md.s * invT;
+    const float mean_d = sumd * invT;
     const float sgn = C > 0.f ? 1.f : (C < 0.f ? -1.f : 0.f);
     const float aC = fabsf(C);
     for (int t = 0; t < T; ++t) {
