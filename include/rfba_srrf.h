@@ -189,8 +189,11 @@ int rfba_srrf_forward_static_scratch(const rfba_srrf_config* cfg, const void* in
  * the maximum) and TRAC with Integrate_Temporal_Correlations 0 or 1 (the
  * shipped setting; its backward always recomputes the stacks). It reuses the radiality stacks of the
  * last rfba_srrf_forward_shifted on the same context with the same
- * configuration, input and shifts (otherwise it runs that forward itself); the
- * interpolated gradient field is recomputed, not stored. Stream-ordered. */
+ * configuration, input and shifts when that forward held the whole series at
+ * once, or the carried temporal state it kept when it ran in time batches
+ * (TRAC with ITC 0, see rfba_ctx_set_time_batch); otherwise it runs that
+ * forward itself. The interpolated gradient field is recomputed, not stored.
+ * Stream-ordered. */
 int rfba_srrf_forward_shifted(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* in, const float* shifts,
                               const int dims[4], float* out, void* stream);
 int rfba_srrf_backward(rfba_ctx* ctx, const rfba_srrf_config* cfg, const float* in, const float* shifts,
