@@ -221,3 +221,28 @@ def test_backward_after_an_intervening_forward(ctx):
     assert rel_linf(m1, m0) < 1e-5
     assert rel_linf(din1, din0) < 1e-4
     assert rel_linf(dsh1, dsh0) < 1e-4
+
+
+def test_batches_in_the_captured_graph_with_pinned_buffers(ctx):
+    """Pinned host buffers go through the captured graph; with time batches the
+    graph holds every batch's radiality launch and carry, and its replays give
+    the eager map bit for bit."""
+    import torch
+    from rfba_gb300 import srrf
+    cfg = srrf.Config.make(mag=2, method=3, itc=0, trac_order=3, intensity_w=1, **SHIPPED)
+    x = _series(133, 23, 9, 10, 11)
+    ctx.set_time_batch(6)
+    try:
+        eager = ctx.forward(cfg, x)   # pageable: eager
+        assert not ctx.schedule()["graph"]
+        pin_in = torch.empty(x.nbytes, dtype=torch.uint8).pin_memory().numpy().view(np.uint16).reshape(x.shape)
+        pin_in[...] = x
+        pin_out = torch.empty(eager.size, dtype=torch.float32).pin_memory().numpy().reshape(eager.shape)
+        for _ in range(3):  # capture, then replays
+            pin_out[...] = 0
+            ctx.forward(cfg, pin_in, out=pin_out)
+            assert ctx.schedule()["graph"] and ctx.last_time_batches() == (6, 4)
+            assert np.array_equal(np.isnan(pin_out), np.isnan(eager))
+            assert np.array_equal(np.nan_to_num(pin_out), np.nan_to_num(eager))
+    finally:
+        ctx.set_time_batch(0)
